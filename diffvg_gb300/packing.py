@@ -1,0 +1,262 @@
+"""Packs pydiffvg's flat scene argument list into the C ABI's scene layout.
+
+RenderFunction.serialize_scene (reference: pydiffvg/render_pytorch.py:22-172)
+flattens a scene into a list of Python scalars, enums and tensors, and
+RenderFunction.forward unpacks it again (render_pytorch.py:186-363).  This
+module performs that unpacking once per call and splits the result in two:
+
+  * the TOPOLOGY (int32 arrays laid out as DvgSceneDesc in
+    include/diffvg_gb300.h), which is hashed so that the device copy of an
+    unchanged topology is reused across optimisation steps, and
+  * the PARAMETERS: every differentiable tensor of the list, in list order,
+    concatenated into one fp32 arena.  Each ParamSlot records where an input
+    tensor lives in the arena so that its gradient is a view of the gradient
+    arena.
+"""
+from dataclasses import dataclass, field
+import hashlib
+
+import numpy as np
+import torch
+
+from .diffvg import ShapeType, ColorType, FilterType
+
+SHAPE_INFO_STRIDE = 8
+GROUP_INFO_STRIDE = 12
+PAINT_NONE = -1
+
+
+class SceneError(ValueError):
+    """Raised for a scene the renderer cannot read safely."""
+
+
+@dataclass
+class ParamSlot:
+    arg_index: int        # index into the *args list of RenderFunction.apply
+    offset: int           # first float in the parameter arena
+    numel: int
+    shape: tuple
+    differentiable: bool  # False: the reference returns None for this slot
+
+
+@dataclass
+class PackedScene:
+    canvas_width: int
+    canvas_height: int
+    num_shapes: int
+    num_groups: int
+    output_type: int
+    use_prefiltering: bool
+    eval_positions: torch.Tensor
+    shape_info: np.ndarray
+    segment_ctrl: np.ndarray
+    group_info: np.ndarray
+    group_shapes: np.ndarray
+    filter_type: int
+    filter_radius_off: int
+    num_params: int
+    slots: list = field(default_factory=list)
+    tensors: list = field(default_factory=list)
+    topology_key: bytes = b''
+
+    def param_arena(self, device):
+        """The parameter values as one contiguous fp32 tensor on `device`."""
+        if not self.tensors:
+            return torch.zeros(1, dtype=torch.float32, device=device)
+        flat = [t.detach().reshape(-1).to(device=device, dtype=torch.float32) for t in self.tensors]
+        return torch.cat(flat)
+
+
+def _as_tensor(x):
+    if isinstance(x, torch.Tensor):
+        return x
+    return torch.tensor(x, dtype=torch.float32)
+
+
+def _enum_value(v):
+    return int(v.value) if hasattr(v, 'value') else int(v)
+
+
+def pack_scene(args):
+    """Parses the flat list produced by serialize_scene (the `*args` of
+    RenderFunction.apply) into a PackedScene.  Follows the unpacking order of
+    render_pytorch.py:186-363."""
+    i = 0
+    canvas_width = int(args[i]); i += 1
+    canvas_height = int(args[i]); i += 1
+    num_shapes = int(args[i]); i += 1
+    num_groups = int(args[i]); i += 1
+    output_type = _enum_value(args[i]); i += 1
+    use_prefiltering = bool(args[i]); i += 1
+    eval_positions = args[i]; i += 1
+    if eval_positions is None:
+        eval_positions = torch.tensor([])
+
+    slots, tensors = [], []
+    off = 0
+
+    def add(arg_index, t, differentiable=True):
+        nonlocal off
+        t = _as_tensor(t)
+        n = t.numel()
+        slots.append(ParamSlot(arg_index, off, n, tuple(t.shape), differentiable))
+        tensors.append(t)
+        off += n
+        return off - n
+
+    shape_info = np.zeros((num_shapes, SHAPE_INFO_STRIDE), dtype=np.int32)
+    seg_ctrl = []
+    key = [canvas_width, canvas_height, num_shapes, num_groups]
+    for s in range(num_shapes):
+        kind = _enum_value(args[i]); i += 1
+        info = shape_info[s]
+        info[0] = kind
+        info[5] = -1
+        if kind == ShapeType.circle:
+            r = _as_tensor(args[i])
+            if r.numel() != 1:
+                raise SceneError('circle radius must be a scalar')
+            info[1] = add(i, r); i += 1
+            c = _as_tensor(args[i])
+            if c.numel() != 2:
+                raise SceneError('circle center must have 2 elements')
+            add(i, c); i += 1
+        elif kind == ShapeType.ellipse:
+            r = _as_tensor(args[i])
+            if r.numel() != 2:
+                raise SceneError('ellipse radius must have 2 elements')
+            info[1] = add(i, r); i += 1
+            c = _as_tensor(args[i])
+            if c.numel() != 2:
+                raise SceneError('ellipse center must have 2 elements')
+            add(i, c); i += 1
+        elif kind == ShapeType.path:
+            ncp = args[i]; i += 1
+            ncp = np.asarray(ncp.detach().cpu() if isinstance(ncp, torch.Tensor) else ncp, dtype=np.int64).reshape(-1)
+            pts = _as_tensor(args[i])
+            if pts.dim() != 2 or pts.shape[1] != 2:
+                raise SceneError('path points must have shape [N, 2]')
+            npts = int(pts.shape[0])
+            info[1] = add(i, pts); i += 1
+            thickness = args[i]
+            if thickness is not None:
+                thickness = _as_tensor(thickness)
+                if thickness.numel() != npts:
+                    raise SceneError('path thickness must have one entry per point')
+                info[5] = add(i, thickness)
+            i += 1
+            is_closed = bool(args[i]); i += 1
+            use_approx = bool(args[i]); i += 1
+            if np.any((ncp < 0) | (ncp > 2)):
+                raise SceneError('num_control_points entries must be 0, 1 or 2')
+            # every segment reads points point_id .. point_id + ncp (+1 wrapped)
+            pid = 0
+            for nc in ncp:
+                if pid + int(nc) >= npts:
+                    raise SceneError('num_control_points does not fit the number of points')
+                pid += int(nc) + 1
+            info[2] = npts
+            info[3] = len(ncp)
+            info[4] = len(seg_ctrl)
+            info[6] = (1 if is_closed else 0) | (2 if use_approx else 0)
+            seg_ctrl.extend(int(v) for v in ncp)
+            key.append(('p', npts, ncp.tobytes(), thickness is not None, int(info[6])))
+        elif kind == ShapeType.rect:
+            pmin = _as_tensor(args[i])
+            if pmin.numel() != 2:
+                raise SceneError('rect p_min must have 2 elements')
+            info[1] = add(i, pmin); i += 1
+            pmax = _as_tensor(args[i])
+            if pmax.numel() != 2:
+                raise SceneError('rect p_max must have 2 elements')
+            add(i, pmax); i += 1
+        else:
+            raise SceneError('unknown shape type %r' % (kind,))
+        sw = _as_tensor(args[i])
+        if sw.numel() != 1:
+            raise SceneError('stroke_width slot must be a scalar')
+        # a thickness path's stroke_width slot is a placeholder (render_pytorch.py:94-95, 775-776)
+        info[7] = add(i, sw, differentiable=(info[5] < 0)); i += 1
+        key.append(('s', kind))
+
+    group_info = np.zeros((num_groups, GROUP_INFO_STRIDE), dtype=np.int32)
+    group_shapes = []
+
+    def read_paint(gi, kind_col):
+        nonlocal i
+        ctype = args[i]; i += 1
+        if ctype is None:
+            gi[kind_col] = PAINT_NONE
+            return ('none',)
+        ctype = _enum_value(ctype)
+        gi[kind_col] = ctype
+        if ctype == ColorType.constant:
+            c = _as_tensor(args[i])
+            if c.numel() != 4:
+                raise SceneError('constant colour must have 4 elements')
+            gi[kind_col + 1] = add(i, c); i += 1
+            gi[kind_col + 2] = 0
+            return ('c',)
+        if ctype in (ColorType.linear_gradient, ColorType.radial_gradient):
+            a = _as_tensor(args[i])
+            if a.numel() != 2:
+                raise SceneError('gradient begin/center must have 2 elements')
+            gi[kind_col + 1] = add(i, a); i += 1
+            b = _as_tensor(args[i])
+            if b.numel() != 2:
+                raise SceneError('gradient end/radius must have 2 elements')
+            add(i, b); i += 1
+            offs = _as_tensor(args[i])
+            k = offs.numel()
+            if k < 1:
+                raise SceneError('gradient needs at least one stop')
+            add(i, offs); i += 1
+            cols = _as_tensor(args[i])
+            if cols.numel() != 4 * k:
+                raise SceneError('gradient stop_colors must have shape [num_stops, 4]')
+            add(i, cols); i += 1
+            gi[kind_col + 2] = k
+            return ('g', ctype, k)
+        raise SceneError('unknown colour type %r' % (ctype,))
+
+    for g in range(num_groups):
+        gi = group_info[g]
+        ids = args[i]; i += 1
+        ids = np.asarray(ids.detach().cpu() if isinstance(ids, torch.Tensor) else ids, dtype=np.int64).reshape(-1)
+        if ids.size < 1:
+            raise SceneError('a shape group needs at least one shape')
+        if np.any((ids < 0) | (ids >= num_shapes)):
+            raise SceneError('shape group refers to a shape id out of range')
+        gi[0] = ids.size
+        gi[1] = len(group_shapes)
+        group_shapes.extend(int(v) for v in ids)
+        kf = read_paint(gi, 2)
+        ks = read_paint(gi, 5)
+        gi[8] = 1 if bool(args[i]) else 0; i += 1
+        m = _as_tensor(args[i])
+        if m.numel() != 9:
+            raise SceneError('shape_to_canvas must be a 3x3 matrix')
+        gi[9] = add(i, m); i += 1
+        key.append(('g', ids.tobytes(), kf, ks, int(gi[8])))
+
+    ftype = _enum_value(args[i]); i += 1
+    if ftype not in (FilterType.box, FilterType.tent, FilterType.parabolic, FilterType.hann):
+        raise SceneError('unknown filter type %r' % (ftype,))
+    fr = _as_tensor(args[i])
+    if fr.numel() != 1:
+        raise SceneError('filter radius must be a scalar')
+    filter_radius_off = add(i, fr); i += 1
+    key.append(('f', ftype))
+
+    seg = np.asarray(seg_ctrl, dtype=np.int32)
+    gsh = np.asarray(group_shapes, dtype=np.int32)
+    h = hashlib.blake2b(digest_size=16)
+    h.update(repr(key).encode())
+    return PackedScene(
+        canvas_width=canvas_width, canvas_height=canvas_height,
+        num_shapes=num_shapes, num_groups=num_groups,
+        output_type=output_type, use_prefiltering=use_prefiltering,
+        eval_positions=eval_positions,
+        shape_info=shape_info, segment_ctrl=seg, group_info=group_info,
+        group_shapes=gsh, filter_type=ftype, filter_radius_off=filter_radius_off,
+        num_params=off, slots=slots, tensors=tensors, topology_key=h.digest())

@@ -1,0 +1,102 @@
+"""Seeded synthetic scenes for the benchmark configurations.
+
+The reference publishes no benchmark data; these generators produce scenes
+with the sizes and value distributions of the five workload configurations
+(plain small circle, stroke-heavy paths, fill-heavy prefiltered gradients,
+batched mixed sizes, served requests).  Every generator takes `mod`, a module
+with pydiffvg's scene classes (this package, or the reference pydiffvg), so
+the same scene can be built for both implementations, and draws its random
+numbers from a torch.Generator in the order documented in each function.
+"""
+import math
+
+import torch
+
+
+def _u(gen, *shape, lo=0.0, hi=1.0):
+    return lo + (hi - lo) * torch.rand(*shape, generator=gen, dtype=torch.float32)
+
+
+def circle_scene(mod, center=(128.0, 128.0), radius=40.0, color=(0.3, 0.6, 0.3, 1.0), canvas=256):
+    """Config 1: one filled circle on a transparent canvas."""
+    shapes = [mod.Circle(radius=torch.tensor(radius), center=torch.tensor(list(center)))]
+    groups = [mod.ShapeGroup(shape_ids=torch.tensor([0]), fill_color=torch.tensor(list(color)))]
+    return canvas, canvas, shapes, groups
+
+
+def stroke_scene(mod, seed=1, num_paths=2048, canvas=512, step=20.0, num_segments=4,
+                 width_range=(1.0, 4.0)):
+    """Config 2: open cubic paths, stroked, no fill.
+
+    Draw order per path: first point U[0,canvas)^2, then 3*num_segments steps
+    U[-step,step]^2 (cumulative), stroke half-width U[width_range], stroke
+    RGBA U[0,1]^4."""
+    gen = torch.Generator().manual_seed(seed)
+    shapes, groups = [], []
+    npts = 3 * num_segments + 1
+    for i in range(num_paths):
+        p0 = _u(gen, 2, hi=float(canvas))
+        steps = _u(gen, npts - 1, 2, lo=-step, hi=step)
+        pts = torch.cat([p0[None], p0[None] + torch.cumsum(steps, 0)], 0).contiguous()
+        sw = _u(gen, 1, lo=width_range[0], hi=width_range[1])[0]
+        col = _u(gen, 4)
+        shapes.append(mod.Path(num_control_points=torch.full((num_segments,), 2, dtype=torch.int32),
+                               points=pts, is_closed=False, stroke_width=sw))
+        groups.append(mod.ShapeGroup(shape_ids=torch.tensor([i]), fill_color=None, stroke_color=col))
+    return canvas, canvas, shapes, groups
+
+
+def fill_scene(mod, seed=3, num_paths=512, canvas=1024, seg_range=(8, 32), radius_range=(10.0, 120.0),
+               jitter=0.15, stroke_fraction=0.1, width_range=(0.5, 3.0)):
+    """Config 3: closed star-shaped cubic paths with constant / linear / radial
+    fills, a tenth also stroked (constant colour).
+
+    Draw order per path: segment count U{seg_range}, centre U[0,canvas)^2,
+    base radius U[radius_range], per-point jitter U[-jitter,jitter], then the
+    fill paint (i%4 in {0,1}: RGBA U[0,1]^4; 2: linear c-R -> c+R with 3 stops
+    of RGBA U[0,1]^4 at offsets 0, .5, 1; 3: radial at c, radius (R,R), same
+    stops), then a stroke coin U[0,1) < stroke_fraction with half-width
+    U[width_range] and RGBA U[0,1]^4."""
+    gen = torch.Generator().manual_seed(seed)
+    shapes, groups = [], []
+    for i in range(num_paths):
+        nseg = int(torch.randint(seg_range[0], seg_range[1] + 1, (1,), generator=gen)[0])
+        c = _u(gen, 2, hi=float(canvas))
+        R = float(_u(gen, 1, lo=radius_range[0], hi=radius_range[1])[0])
+        n = 3 * nseg
+        ang = torch.arange(n, dtype=torch.float32) * (2.0 * math.pi / n)
+        rad = R * (1.0 + _u(gen, n, lo=-jitter, hi=jitter))
+        pts = torch.stack([c[0] + rad * torch.cos(ang), c[1] + rad * torch.sin(ang)], 1).contiguous()
+        shapes.append(mod.Path(num_control_points=torch.full((nseg,), 2, dtype=torch.int32),
+                               points=pts, is_closed=True, stroke_width=torch.tensor(1.0)))
+        kind = i % 4
+        if kind in (0, 1):
+            fill = _u(gen, 4)
+        elif kind == 2:
+            fill = mod.LinearGradient(begin=c - R, end=c + R, offsets=torch.tensor([0.0, 0.5, 1.0]),
+                                      stop_colors=_u(gen, 3, 4))
+        else:
+            fill = mod.RadialGradient(center=c.clone(), radius=torch.tensor([R, R]),
+                                      offsets=torch.tensor([0.0, 0.5, 1.0]), stop_colors=_u(gen, 3, 4))
+        stroke = None
+        if float(_u(gen, 1)[0]) < stroke_fraction:
+            shapes[-1].stroke_width = _u(gen, 1, lo=width_range[0], hi=width_range[1])[0]
+            stroke = _u(gen, 4)
+        groups.append(mod.ShapeGroup(shape_ids=torch.tensor([i]), fill_color=fill, stroke_color=stroke))
+    return canvas, canvas, shapes, groups
+
+
+def batched_scenes(mod, seeds=range(100, 164), canvases=(64, 128, 256, 512), path_range=(16, 1024)):
+    """Config 4: independent stroke scenes of uneven size.
+
+    Per scene (seed s): canvas U{canvases}, path count log-uniform in
+    path_range, then stroke_scene(seed=s) with the step scaled by canvas/512."""
+    out = []
+    for s in seeds:
+        gen = torch.Generator().manual_seed(int(s))
+        canvas = canvases[int(torch.randint(0, len(canvases), (1,), generator=gen)[0])]
+        lo, hi = math.log(path_range[0]), math.log(path_range[1])
+        npaths = int(round(math.exp(lo + (hi - lo) * float(torch.rand(1, generator=gen)[0]))))
+        out.append(stroke_scene(mod, seed=int(s) * 7919 + 1, num_paths=npaths, canvas=canvas,
+                                step=20.0 * canvas / 512.0))
+    return out

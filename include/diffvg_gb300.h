@@ -1,0 +1,166 @@
+/*
+ * diffvg_gb300 — C ABI of the GB300-native render path of diffvg.
+ *
+ * The library renders 2-D vector scenes (circles, ellipses, rects, paths of
+ * line / quadratic / cubic segments, grouped into shape groups with constant,
+ * linear-gradient or radial-gradient paint) with per-sample pcg32 jitter, a
+ * pixel filter and optional analytic prefiltering, and back-propagates an
+ * image gradient to every scene parameter (interior + edge-sampling terms).
+ *
+ * Data model.  A scene is split in two:
+ *   - its TOPOLOGY (shape kinds, point / segment counts, group membership,
+ *     paint kinds) is uploaded once by dvg_scene_create() and stays resident;
+ *   - its PARAMETERS are one flat fp32 arena whose layout is the order in
+ *     which pydiffvg's RenderFunction.serialize_scene lists its differentiable
+ *     tensors (reference: pydiffvg/render_pytorch.py:22-172).  The gradient
+ *     arena written by dvg_render_backward() has the same layout, so the
+ *     gradient of every input tensor is a view into it.
+ *
+ * Per-shape parameter layout at shape_info[SHAPE_PARAM_OFF]:
+ *   circle : radius, cx, cy                 (render_pytorch.py:47-50)
+ *   ellipse: rx, ry, cx, cy                 (render_pytorch.py:51-56)
+ *   path   : points[2*num_points]           (render_pytorch.py:57-72)
+ *            + thickness[num_points] at SHAPE_THICKNESS_OFF when present
+ *   rect   : pmin_x, pmin_y, pmax_x, pmax_y (render_pytorch.py:86-91)
+ *   stroke width: one float at SHAPE_STROKE_WIDTH_OFF (render_pytorch.py:94-97)
+ * Per-paint layout at group_info[GROUP_FILL_OFF / GROUP_STROKE_OFF]:
+ *   constant: r, g, b, a
+ *   linear  : begin_x, begin_y, end_x, end_y, offsets[k], stop_colors[4k]
+ *   radial  : center_x, center_y, radius_x, radius_y, offsets[k], stop_colors[4k]
+ * Group transform: 9 floats (row-major 3x3 shape_to_canvas) at GROUP_XFORM_OFF.
+ * Filter radius: one float at filter_radius_off.
+ *
+ * All functions return DVG_OK (0) or a negative DvgStatus; the message of the
+ * last failure on the calling thread is returned by dvg_last_error().  No
+ * function aborts the process (the reference asserts / exit(1)s instead:
+ * cuda_utils.h:11-16, diffvg.cpp:542,847).
+ *
+ * Threading: calls are stream-ordered on the caller's cudaStream_t (passed as
+ * void*).  A DvgScene owns its scratch arenas, so one scene must not be used
+ * by two streams at once; distinct scenes are independent.
+ */
+#ifndef DIFFVG_GB300_H
+#define DIFFVG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Shape kinds: values of diffvg.ShapeType (shape.h:9-14). */
+enum DvgShapeKind { DVG_CIRCLE = 0, DVG_ELLIPSE = 1, DVG_PATH = 2, DVG_RECT = 3 };
+/* Paint kinds: values of diffvg.ColorType (color.h:7-11); -1 = no paint. */
+enum DvgPaintKind { DVG_PAINT_NONE = -1, DVG_CONSTANT = 0, DVG_LINEAR = 1, DVG_RADIAL = 2 };
+/* Pixel filters: values of diffvg.FilterType (filter.h:6-11). */
+enum DvgFilterKind { DVG_BOX = 0, DVG_TENT = 1, DVG_PARABOLIC = 2, DVG_HANN = 3 };
+
+enum DvgStatus {
+  DVG_OK = 0,
+  DVG_ERR_INVALID = -1,      /* malformed scene or arguments                    */
+  DVG_ERR_CUDA = -2,         /* a CUDA runtime call failed                       */
+  DVG_ERR_CAPACITY = -3,     /* a per-sample fragment list overflowed            */
+  DVG_ERR_UNSUPPORTED = -4,  /* the reference aborts on this input (e.g. ellipse stroke) */
+  DVG_ERR_SCENE = -5         /* degenerate scene (zero / NaN total boundary length) */
+};
+
+/* shape_info record (DVG_SHAPE_INFO_STRIDE int32 per shape). */
+#define DVG_SHAPE_INFO_STRIDE 8
+#define DVG_SHAPE_KIND 0
+#define DVG_SHAPE_PARAM_OFF 1
+#define DVG_SHAPE_NUM_POINTS 2
+#define DVG_SHAPE_NUM_SEGMENTS 3
+#define DVG_SHAPE_SEG_OFF 4          /* first entry of this path in segment_ctrl */
+#define DVG_SHAPE_THICKNESS_OFF 5    /* -1 when the path has no per-point thickness */
+#define DVG_SHAPE_FLAGS 6            /* bit0 is_closed, bit1 use_distance_approx */
+#define DVG_SHAPE_STROKE_WIDTH_OFF 7
+
+/* group_info record (DVG_GROUP_INFO_STRIDE int32 per shape group). */
+#define DVG_GROUP_INFO_STRIDE 12
+#define DVG_GROUP_NUM_SHAPES 0
+#define DVG_GROUP_SHAPES_OFF 1       /* first entry of this group in group_shapes */
+#define DVG_GROUP_FILL_KIND 2
+#define DVG_GROUP_FILL_OFF 3
+#define DVG_GROUP_FILL_STOPS 4
+#define DVG_GROUP_STROKE_KIND 5
+#define DVG_GROUP_STROKE_OFF 6
+#define DVG_GROUP_STROKE_STOPS 7
+#define DVG_GROUP_EVEN_ODD 8
+#define DVG_GROUP_XFORM_OFF 9
+
+/* Host-side description of a scene's topology (all pointers are host memory).
+ * Replaces the arguments of diffvg.Scene(...) (diffvg.cpp:1777-1789,
+ * scene.cpp:919-998) minus the parameter values. */
+typedef struct DvgSceneDesc {
+  int32_t canvas_width;
+  int32_t canvas_height;
+  int32_t num_shapes;
+  int32_t num_groups;
+  int32_t num_params;            /* floats in the parameter arena            */
+  int32_t total_segments;        /* entries in segment_ctrl                  */
+  int32_t total_group_shapes;    /* entries in group_shapes                  */
+  int32_t filter_type;           /* DvgFilterKind                            */
+  int32_t filter_radius_off;     /* parameter offset of the filter radius    */
+  const int32_t *shape_info;     /* [num_shapes * DVG_SHAPE_INFO_STRIDE]     */
+  const int32_t *segment_ctrl;   /* [total_segments] control points per segment: 0 line, 1 quadratic, 2 cubic */
+  const int32_t *group_info;     /* [num_groups * DVG_GROUP_INFO_STRIDE]     */
+  const int32_t *group_shapes;   /* [total_group_shapes] shape ids           */
+} DvgSceneDesc;
+
+/* Per-call render arguments (device pointers unless stated).
+ * Mirrors the scalar arguments of diffvg.render (diffvg.cpp:1477-1492). */
+typedef struct DvgRenderArgs {
+  int32_t width;                 /* output image size (pixels)               */
+  int32_t height;
+  int32_t num_samples_x;
+  int32_t num_samples_y;
+  uint64_t seed;
+  int32_t use_prefiltering;
+  int32_t num_eval_positions;    /* >0: SDF at eval_positions instead of an image */
+  const float *params;           /* [num_params] parameter arena             */
+  const float *background;       /* [height*width*4] or NULL                 */
+  const float *eval_positions;   /* [num_eval_positions*2] or NULL           */
+} DvgRenderArgs;
+
+typedef struct DvgScene DvgScene;
+
+/* Uploads the topology and allocates the scene's resident arenas.
+ * Replaces diffvg.Scene(...) (diffvg.cpp:1777-1789; scene.cpp:919-998). */
+int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene);
+
+/* Frees a scene and its arenas.  Replaces Scene::~Scene (scene.cpp:1000-1023). */
+int dvg_scene_destroy(DvgScene *scene);
+
+/* Forward render.  Exactly one of image / sdf is non-NULL:
+ *   image: [height*width*4] colour output (OutputType.color)
+ *   sdf  : [height*width] or [num_eval_positions] signed distance (OutputType.sdf)
+ * Replaces diffvg.render(...) called with render_image / render_sdf
+ * (diffvg.cpp:1477-1649; render_pytorch.py:394-409). */
+int dvg_render_forward(DvgScene *scene, const DvgRenderArgs *args,
+                       float *image, float *sdf, void *stream);
+
+/* Backward render: accumulates (+=) the gradient of <d_image, image> (or of
+ * <d_sdf, sdf>) into d_params (same layout as params), d_background
+ * ([height*width*4] or NULL) and d_translation ([height*width*2] or NULL).
+ * The caller zeroes the outputs.  Replaces diffvg.render(...) called with
+ * d_render_image / d_render_sdf / d_translation (diffvg.cpp:1477-1649;
+ * render_pytorch.py:692-707 and 633-650) plus the gradient read-back of
+ * Scene::get_d_shape / get_d_shape_group / get_d_filter_radius
+ * (scene.cpp:1025-1035). */
+int dvg_render_backward(DvgScene *scene, const DvgRenderArgs *args,
+                        const float *d_image, const float *d_sdf,
+                        float *d_params, float *d_background,
+                        float *d_translation, void *stream);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *dvg_last_error(void);
+
+/* Library version string. */
+const char *dvg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIFFVG_GB300_H */
