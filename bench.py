@@ -1,0 +1,410 @@
+"""Benchmark of the render hot path: fwd+bwd Msamples/s.
+
+Workload (the stroke-heavy plain-method configuration): canvas 512x512,
+2x2 samples per pixel, box filter radius 0.5, seed 1; 2048 open paths of 4
+cubic segments (13 control points, first point uniform in the canvas, each
+later point a uniform [-20, 20]^2 step), stroke half-width U[1, 4], stroke
+RGBA U[0, 1]^4, no fill.  Loss: MSE against the render of the same
+generator with seed 2.  One step = forward + loss gradient + backward
+(interior and boundary terms) = 1,048,576 samples.
+
+Lines printed (one JSON line, rank 0):
+  value  device-resident throughput: parameters, target and buffers live in
+         HBM; each step is timed with CUDA events on the launching stream,
+         the L2 is flushed (a 256 MiB write) between steps outside the timed
+         events.
+  e2e    the same metric through the public API a user calls
+         (RenderFunction.serialize_scene / apply / backward) with the scene
+         tensors in host memory: host-to-device copy of the parameters, the
+         render, the loss, the backward, the gradients copied back to host
+         tensors and the loss read back are all inside the timed region.
+  roofline  the dominant kernel's algorithmic bytes per launch over its
+         CUDA-event time, against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle port (oracle/, all host cores) on one full
+         step of the same workload.
+
+--impl reference times the reference algorithm on the host cores (the
+oracle port; the reference's own CPU module cannot be built on the GPU
+host) and prints the same line with "impl": "reference".
+Under torchrun (N > 1) every rank renders its own replica of the workload
+(no collective on the data path); the timed region is bracketed by barriers
+and the slowest rank's time is used.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(canvas=512, num_paths=2048, spp=(2, 2), seed=1, target_seed=2, filter='box', radius=0.5)
+METRIC = 'fwd+bwd Msamples/s'
+UNIT = 'Msamples/s'
+PREP_KERNELS = 7  # kernels launched by one scene preparation
+
+
+def _dist():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+def _workload_config():
+    return {'workload': 'stroke-heavy plain method: 512x512 canvas, 2x2 spp, box r=0.5, 2048 open cubic paths '
+                        '(4 segments, 13 points), stroke half-width U[1,4], seed 1; MSE vs seed-2 target',
+            'canvas': [512, 512], 'num_paths': 2048, 'samples_per_step': 512 * 512 * 4,
+            'l2': 'flushed between timed steps (256 MiB write)', 'parallelism': 'replicas'}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.FIELDS,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(',')]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        sm.sort()
+        return {'sm_mhz': sm[len(sm) // 2] if sm else None, 'sm_max_mhz': smax, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            p = json.load(f)
+        return float(p['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+def _ncu_traffic():
+    """Per-launch DRAM bytes per kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, 'profiles', 'ncu_traffic.json')) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def build_workload(mod, device):
+    import torch
+    from diffvg_gb300 import workloads
+    w, h, shapes, groups = workloads.stroke_scene(mod, seed=WORKLOAD['seed'], num_paths=WORKLOAD['num_paths'],
+                                                  canvas=WORKLOAD['canvas'])
+    tw, th, tshapes, tgroups = workloads.stroke_scene(mod, seed=WORKLOAD['target_seed'],
+                                                      num_paths=WORKLOAD['num_paths'], canvas=WORKLOAD['canvas'])
+    return (w, h, shapes, groups), (tw, th, tshapes, tgroups)
+
+
+def algorithmic_bytes(kernel, packed, w, h, spp):
+    """Unique bytes a launch must move: scene data read, per-pixel / per-sample
+    inputs read, outputs written."""
+    scene = 4 * packed.num_params + 4 * (packed.shape_info.size + packed.segment_ctrl.size +
+                                         packed.group_info.size + packed.group_shapes.size)
+    npx, n = w * h, w * h * spp
+    if kernel == 'sample_fwd':
+        return scene + 16 * n                      # sample colours out
+    if kernel == 'resolve':
+        return 16 * n + 4 * npx + 16 * npx         # samples + weights in, image out
+    if kernel == 'weight':
+        return 4 * npx
+    if kernel == 'sample_bwd':
+        return scene + 16 * npx + 4 * npx + 4 * packed.num_params   # d_image, weights in; d_params out
+    if kernel == 'edge':
+        return scene + 16 * npx + 4 * npx + 4 * packed.num_params
+    return scene
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import _native
+    from diffvg_gb300.packing import pack_scene
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    dvg.set_device(dev)
+    if ws > 1:
+        dist.init_process_group('nccl', device_id=dev)
+    (w, h, shapes, groups), (tw, th, tshapes, tgroups) = build_workload(dvg, dev)
+    nsx, nsy = WORKLOAD['spp']
+    spp = nsx * nsy
+    n_samples = w * h * spp
+    seed = WORKLOAD['seed']
+
+    # ---------------- device-resident step through the C ABI ----------------
+    sargs = dvg.RenderFunction.serialize_scene(w, h, shapes, groups)
+    packed = pack_scene(sargs)
+    scene = _native.NativeScene(packed)
+    arena = packed.param_arena(dev).contiguous()
+    targs = dvg.RenderFunction.serialize_scene(tw, th, tshapes, tgroups)
+    tpacked = pack_scene(targs)
+    tscene = _native.NativeScene(tpacked)
+    tarena = tpacked.param_arena(dev).contiguous()
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    target = torch.empty(h, w, 4, device=dev)
+    ra = _native.RenderArgs(w, h, nsx, nsy, seed, 0, 0, tarena.data_ptr(), None, None, 0)
+    tscene.forward(ra, image_ptr=target.data_ptr(), stream=sptr)
+    img = torch.empty(h, w, 4, device=dev)
+    d_img = torch.empty_like(img)
+    d_params = torch.zeros(packed.num_params, device=dev)
+    fwd_args = _native.RenderArgs(w, h, nsx, nsy, seed, 0, 0, arena.data_ptr(), None, None, _native.DVG_FLAG_NO_SYNC)
+    bwd_args = _native.RenderArgs(w, h, nsx, nsy, seed, 0, 0, arena.data_ptr(), None, None,
+                                  _native.DVG_FLAG_NO_SYNC | _native.DVG_FLAG_REUSE_PREP)
+    scale = 2.0 / img.numel()
+    loss_buf = torch.zeros((), device=dev)
+
+    def step():
+        scene.forward(fwd_args, image_ptr=img.data_ptr(), stream=sptr)
+        torch.sub(img, target, out=d_img)
+        torch.sum(d_img * d_img, out=loss_buf)
+        d_img.mul_(scale)
+        d_params.zero_()
+        scene.backward(bwd_args, d_image_ptr=d_img.data_ptr(), d_params_ptr=d_params.data_ptr(), stream=sptr)
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    scene.sync(sptr)
+    torch.cuda.synchronize(dev)
+    # forward / backward split, measured once on a warm step
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    flush.fill_(1.0)
+    e0.record(stream)
+    scene.forward(fwd_args, image_ptr=img.data_ptr(), stream=sptr)
+    e1.record(stream)
+    d_params.zero_()
+    scene.backward(bwd_args, d_image_ptr=d_img.data_ptr(), d_params_ptr=d_params.data_ptr(), stream=sptr)
+    e2.record(stream)
+    torch.cuda.synchronize(dev)
+    fwd_ms, bwd_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
+
+    clocks = ClockSampler(local)
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    scene.profile(True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.fill_(float(i))          # L2 flush, outside the timed events
+        starts[i].record(stream)
+        step()
+        ends[i].record(stream)
+    torch.cuda.synchronize(dev)
+    clock_info = clocks.stop()
+    scene.sync(sptr)
+    kernels = scene.profile_read()
+    scene.profile(False)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    value = ws * n_samples * args.steps / (total_ms / 1e3) / 1e6
+    gpu_launches = 0
+    for name, (cnt, _) in kernels.items():
+        gpu_launches += cnt * (PREP_KERNELS if name == 'prepare' else 1)
+
+    # ---------------- roofline of the dominant kernel ----------------
+    peak, peak_kind = _peaks()
+    dom = max((k for k in kernels if k != 'prepare'), key=lambda k: kernels[k][1])
+    dom_cnt, dom_ms = kernels[dom]
+    avg_s = dom_ms / dom_cnt / 1e3
+    alg = algorithmic_bytes(dom, packed, w, h, spp)
+    achieved = alg / avg_s / 1e9
+    traffic = _ncu_traffic().get(dom)
+    roofline = {'bound': 'hbm', 'kernel': dom, 'achieved': round(achieved, 3), 'peak': peak,
+                'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 6),
+                'traffic': traffic, 'algorithmic_bytes': alg, 'avg_launch_ms': round(avg_s * 1e3, 4),
+                'note': 'the path is FP32/FP64-issue bound (no dense contraction); the HBM fraction is small by '
+                        'construction'}
+
+    # ---------------- end to end through the public API ----------------
+    e2e = run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samples, ws)
+
+    out = {'metric': METRIC, 'value': round(value, 3), 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
+           'warmup': max(args.warmup, 3), 'ms_per_step': round(total_ms / args.steps, 4), 'higher_is_better': True,
+           'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 (fp64 root solves)', 'data': 'synthetic',
+           'config': _workload_config(), 'e2e': e2e, 'roofline': roofline, 'clocks': clock_info,
+           'gpu_launches': gpu_launches, 'fwd_ms': round(fwd_ms, 4), 'bwd_ms': round(bwd_ms, 4),
+           'kernels_ms_per_launch': {k: round(v[1] / v[0], 4) for k, v in kernels.items()},
+           'loss': float(loss_buf.item())}
+    if rank == 0 and not args.no_cpu_baseline:
+        out['cpu_baseline'] = cpu_baseline(packed, oracle_params(packed), w, h, nsx, nsy, seed, target.cpu().numpy())
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samples, ws):
+    """Same metric through RenderFunction with host-resident scene tensors."""
+    import torch
+    params = []
+    for s in shapes:
+        s.points.requires_grad_(True)
+        s.stroke_width.requires_grad_(True)
+        params += [s.points, s.stroke_width]
+    for g in groups:
+        g.stroke_color.requires_grad_(True)
+        params.append(g.stroke_color)
+    h2d = 4 * sum(p.numel() for p in params) + 4 * (len(groups) * 9 + 1)
+    d2h = 4 * sum(p.numel() for p in params) + 4
+
+    def step():
+        for p in params:
+            p.grad = None
+        sargs = dvg.RenderFunction.serialize_scene(w, h, shapes, groups)
+        img = dvg.RenderFunction.apply(w, h, nsx, nsy, seed, None, *sargs)
+        loss = ((img - target) ** 2).mean()
+        loss.backward()
+        return float(loss.item())
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(dev)
+    k = max(1, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        step()
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t0
+    return {'value': round(ws * n_samples * k / dt / 1e6, 3), 'unit': UNIT, 'h2d_bytes_per_step': h2d,
+            'd2h_bytes_per_step': d2h, 'steps': k, 'ms_per_step': round(dt / k * 1e3, 3),
+            'api': 'RenderFunction.serialize_scene + apply + MSE + backward, scene tensors in host memory'}
+
+
+def oracle_params(packed):
+    import oracle
+    return oracle.params_of(packed)
+
+
+def cpu_baseline(packed, P, w, h, nsx, nsy, seed, target, threads=None):
+    """One full step of the workload on the host cores with the oracle port."""
+    import numpy as np
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    fwd = oracle.render(packed, P, w, h, nsx, nsy, seed, num_threads=threads)
+    d_img = (2.0 / fwd['image'].size) * (fwd['image'] - target)
+    oracle.render(packed, P, w, h, nsx, nsy, seed, forward=False, d_image=d_img.astype(np.float32),
+                  num_threads=threads)
+    dt = time.perf_counter() - t0
+    return {'value': round(w * h * nsx * nsy / dt / 1e6, 4), 'unit': UNIT, 'cores': threads, 'kind': 'port',
+            'sample': 'one full fwd+bwd step of the workload (1,048,576 samples), %.2f s' % dt}
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    import diffvg_gb300 as dvg
+    from diffvg_gb300.packing import pack_scene
+    import oracle
+    (w, h, shapes, groups), (tw, th, tshapes, tgroups) = build_workload(dvg, None)
+    nsx, nsy = WORKLOAD['spp']
+    seed = WORKLOAD['seed']
+    packed = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups))
+    P = oracle.params_of(packed)
+    tpacked = pack_scene(dvg.RenderFunction.serialize_scene(tw, th, tshapes, tgroups))
+    threads = os.cpu_count() or 1
+    target = oracle.render(tpacked, oracle.params_of(tpacked), w, h, nsx, nsy, seed, num_threads=threads)['image']
+    cpu_baseline(packed, P, w, h, nsx, nsy, seed, target, threads)  # one untimed warm-up step
+    budget_s = 120.0
+    times = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cpu_baseline(packed, P, w, h, nsx, nsy, seed, target, threads)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > budget_s:
+            break
+    total = sum(times)
+    n = w * h * nsx * nsy
+    value = n * len(times) / total / 1e6
+    out = {'metric': METRIC, 'value': round(value, 4), 'unit': UNIT, 'n_gpus': ws, 'steps': len(times),
+           'warmup': 1, 'ms_per_step': round(total / len(times) * 1e3, 2), 'higher_is_better': True,
+           'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 (fp64 root solves)', 'data': 'synthetic',
+           'config': _workload_config(), 'impl': 'reference',
+           'cpu_baseline': {'value': round(value, 4), 'unit': UNIT, 'cores': threads, 'kind': 'port',
+                            'sample': 'full fwd+bwd steps of the workload on all host cores; the timed loop '
+                                      'stops after %d s' % int(budget_s)},
+           'e2e': {'value': round(value, 4), 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+           'note': "the reference's own CPU module needs pybind11 and the reference checkout, neither of which "
+                   "exists on the GPU host; the oracle port (oracle/dvg_oracle.c) restates its algorithm"}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,19 @@
+"""diffvg_gb300: a GB300-native (sm_103a) implementation of diffvg's render
+hot path behind pydiffvg's API.
+
+``import diffvg_gb300 as pydiffvg`` gives the scene classes (Circle,
+Ellipse, Path, Polygon, Rect, ShapeGroup), paints (LinearGradient,
+RadialGradient), PixelFilter, the device switches and RenderFunction with
+pydiffvg's signatures.  Rendering runs the hand-written CUDA kernels of
+libdiffvg_gb300.so through its C ABI (include/diffvg_gb300.h); there is no
+CPU fallback.
+"""
+from .device import set_use_gpu, get_use_gpu, set_device, get_device
+from .shape import Circle, Ellipse, Path, Polygon, Rect, ShapeGroup
+from .color import LinearGradient, RadialGradient
+from .pixel_filter import PixelFilter
+from .diffvg import ShapeType, ColorType, FilterType
+from .render_pytorch import RenderFunction, OutputType, set_print_timing, clear_scene_cache
+from . import diffvg
+
+__version__ = '0.1.0'

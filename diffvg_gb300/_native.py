@@ -1,0 +1,186 @@
+"""ctypes binding of libdiffvg_gb300.so (include/diffvg_gb300.h).
+
+The library is the only implementation of the render path: there is no CPU
+fallback, and loading fails loudly when the library is missing or when no
+CUDA device is present.
+"""
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+_FP = ctypes.POINTER(ctypes.c_float)
+_IP = ctypes.POINTER(ctypes.c_int32)
+
+DVG_OK = 0
+DVG_ERR_INVALID = -1
+DVG_ERR_CUDA = -2
+DVG_ERR_CAPACITY = -3
+DVG_ERR_UNSUPPORTED = -4
+DVG_ERR_SCENE = -5
+
+DVG_FLAG_NO_SYNC = 1
+DVG_FLAG_REUSE_PREP = 2
+
+EXPORTS = ('dvg_scene_create', 'dvg_scene_destroy', 'dvg_render_forward', 'dvg_render_backward',
+           'dvg_scene_sync', 'dvg_scene_profile', 'dvg_scene_profile_read', 'dvg_last_error', 'dvg_version')
+
+
+class KernelTime(ctypes.Structure):
+    _fields_ = [('name', ctypes.c_char_p), ('launches', ctypes.c_int64), ('total_ms', ctypes.c_double)]
+
+
+class SceneDesc(ctypes.Structure):
+    _fields_ = [
+        ('canvas_width', ctypes.c_int32), ('canvas_height', ctypes.c_int32),
+        ('num_shapes', ctypes.c_int32), ('num_groups', ctypes.c_int32),
+        ('num_params', ctypes.c_int32), ('total_segments', ctypes.c_int32),
+        ('total_group_shapes', ctypes.c_int32), ('filter_type', ctypes.c_int32),
+        ('filter_radius_off', ctypes.c_int32),
+        ('shape_info', _IP), ('segment_ctrl', _IP), ('group_info', _IP), ('group_shapes', _IP),
+    ]
+
+
+class RenderArgs(ctypes.Structure):
+    _fields_ = [
+        ('width', ctypes.c_int32), ('height', ctypes.c_int32),
+        ('num_samples_x', ctypes.c_int32), ('num_samples_y', ctypes.c_int32),
+        ('seed', ctypes.c_uint64), ('use_prefiltering', ctypes.c_int32),
+        ('num_eval_positions', ctypes.c_int32),
+        ('params', ctypes.c_void_p), ('background', ctypes.c_void_p), ('eval_positions', ctypes.c_void_p),
+        ('flags', ctypes.c_int32),
+    ]
+
+
+class RenderError(RuntimeError):
+    """A failed call of the native library; `status` is the DvgStatus."""
+
+    def __init__(self, status, msg):
+        super().__init__(msg)
+        self.status = status
+
+
+class SceneCapacityError(RenderError):
+    pass
+
+
+class UnsupportedSceneError(RenderError):
+    pass
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path():
+    return _build.LIB_PATH
+
+
+def load(build_if_missing=True):
+    """Loads the native library (building it first if it is missing or stale
+    and nvcc is available)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB_PATH
+        if build_if_missing and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError('libdiffvg_gb300.so is not built (run diffvg_gb300.build.build())')
+        lib = ctypes.CDLL(path)
+        lib.dvg_scene_create.argtypes = [ctypes.POINTER(SceneDesc), ctypes.POINTER(ctypes.c_void_p)]
+        lib.dvg_scene_create.restype = ctypes.c_int
+        lib.dvg_scene_destroy.argtypes = [ctypes.c_void_p]
+        lib.dvg_scene_destroy.restype = ctypes.c_int
+        lib.dvg_render_forward.argtypes = [ctypes.c_void_p, ctypes.POINTER(RenderArgs), ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p]
+        lib.dvg_render_forward.restype = ctypes.c_int
+        lib.dvg_render_backward.argtypes = [ctypes.c_void_p, ctypes.POINTER(RenderArgs), ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p]
+        lib.dvg_render_backward.restype = ctypes.c_int
+        lib.dvg_scene_sync.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        lib.dvg_scene_sync.restype = ctypes.c_int
+        lib.dvg_scene_profile.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.dvg_scene_profile.restype = ctypes.c_int
+        lib.dvg_scene_profile_read.argtypes = [ctypes.c_void_p, ctypes.POINTER(KernelTime), ctypes.c_int,
+                                               ctypes.POINTER(ctypes.c_int)]
+        lib.dvg_scene_profile_read.restype = ctypes.c_int
+        lib.dvg_last_error.argtypes = []
+        lib.dvg_last_error.restype = ctypes.c_char_p
+        lib.dvg_version.argtypes = []
+        lib.dvg_version.restype = ctypes.c_char_p
+        _lib = lib
+        return lib
+
+
+def check(status):
+    if status == DVG_OK:
+        return
+    msg = load().dvg_last_error().decode(errors='replace')
+    if status == DVG_ERR_CAPACITY:
+        raise SceneCapacityError(status, msg)
+    if status == DVG_ERR_UNSUPPORTED:
+        raise UnsupportedSceneError(status, msg)
+    if status == DVG_ERR_INVALID:
+        raise ValueError(msg)
+    raise RenderError(status, msg)
+
+
+class NativeScene:
+    """Owns a DvgScene handle: the resident topology of a packed scene."""
+
+    def __init__(self, packed):
+        lib = load()
+        self._lib = lib
+        si = np.ascontiguousarray(packed.shape_info.reshape(-1), dtype=np.int32)
+        sc = np.ascontiguousarray(packed.segment_ctrl, dtype=np.int32)
+        gi = np.ascontiguousarray(packed.group_info.reshape(-1), dtype=np.int32)
+        gs = np.ascontiguousarray(packed.group_shapes, dtype=np.int32)
+        keep = [np.zeros(1, np.int32) if x.size == 0 else x for x in (si, sc, gi, gs)]
+        desc = SceneDesc(packed.canvas_width, packed.canvas_height, packed.num_shapes, packed.num_groups,
+                         max(packed.num_params, 1), int(sc.size), int(gs.size), int(packed.filter_type),
+                         int(packed.filter_radius_off),
+                         keep[0].ctypes.data_as(_IP), keep[1].ctypes.data_as(_IP),
+                         keep[2].ctypes.data_as(_IP), keep[3].ctypes.data_as(_IP))
+        h = ctypes.c_void_p()
+        check(lib.dvg_scene_create(ctypes.byref(desc), ctypes.byref(h)))
+        self.handle = h
+        self.num_params = max(packed.num_params, 1)
+
+    def close(self):
+        if getattr(self, 'handle', None):
+            self._lib.dvg_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, args, image_ptr=None, sdf_ptr=None, stream=0):
+        check(self._lib.dvg_render_forward(self.handle, ctypes.byref(args), image_ptr, sdf_ptr, stream))
+
+    def backward(self, args, d_image_ptr=None, d_sdf_ptr=None, d_params_ptr=None, d_background_ptr=None,
+                 d_translation_ptr=None, stream=0):
+        check(self._lib.dvg_render_backward(self.handle, ctypes.byref(args), d_image_ptr, d_sdf_ptr, d_params_ptr,
+                                            d_background_ptr, d_translation_ptr, stream))
+
+    def sync(self, stream=0):
+        check(self._lib.dvg_scene_sync(self.handle, stream))
+
+    def profile(self, enable):
+        """Starts (clearing the table) or stops per-kernel CUDA-event timing."""
+        check(self._lib.dvg_scene_profile(self.handle, 1 if enable else 0))
+
+    def profile_read(self):
+        """{kernel name: (launches, total milliseconds)} since profile(True)."""
+        arr = (KernelTime * 16)()
+        n = ctypes.c_int()
+        check(self._lib.dvg_scene_profile_read(self.handle, arr, 16, ctypes.byref(n)))
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(min(n.value, 16))}

@@ -1,0 +1,611 @@
+// C ABI of libdiffvg_gb300 (include/diffvg_gb300.h): scene handles that keep
+// the topology and all scratch arenas resident on the device, and the
+// forward / backward entry points that replace diffvg.Scene + diffvg.render
+// (diffvg.cpp:1477-1649, 1777-1789; scene.cpp:919-1035).
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dvg_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string &msg) {
+  g_last_error = msg;
+  return status;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(DVG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// grow-only device buffer
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need) {
+    if (need <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    size_t nb = need + need / 4 + 256;
+    cudaError_t e = cudaMalloc(&ptr, nb);
+    if (e == cudaSuccess) bytes = nb;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+};
+
+}  // namespace
+
+struct DvgScene {
+  int device = 0;
+  DvgSceneDesc d{};
+  int tiles_x = 1, tiles_y = 1;
+  int num_total = 0;
+  DevBuf topo, derived, tiles;
+  int tile_cap = 0;
+  // carved from `topo`
+  int *shape_info = nullptr, *segment_ctrl = nullptr, *seg_point = nullptr, *group_info = nullptr;
+  int *group_shapes = nullptr, *smp_shape = nullptr, *smp_group = nullptr;
+  // carved from `derived`
+  float *c2s = nullptr, *g_max_radius = nullptr, *s_length = nullptr;
+  float4 *g_local_box = nullptr, *g_canvas_box = nullptr, *s_box = nullptr, *seg_box = nullptr;
+  float *seg_r = nullptr, *seg_pmf = nullptr, *seg_cdf = nullptr, *smp_cdf = nullptr, *smp_pmf = nullptr;
+  int *seg_order = nullptr, *tile_start = nullptr, *tile_count = nullptr, *scratch = nullptr;
+  int4 *g_tile_range = nullptr;
+  unsigned *err = nullptr;  // [0] status bits, [1] tile-list length
+  // image-sized arenas
+  DevBuf weight, samples, dbg_val, dbg_flag;
+  unsigned *h_status = nullptr;  // pinned mirror of err[0..1]
+  bool prepared = false;
+  // per-kernel timing (dvg_scene_profile)
+  bool profiling = false;
+  struct Pending { int kid; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  double total_ms[16] = {0};
+  long long launches[16] = {0};
+};
+
+namespace {
+
+template <typename T>
+T *carve(char *&p, size_t n) {
+  uintptr_t a = (reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255);
+  T *r = reinterpret_cast<T *>(a);
+  p = reinterpret_cast<char *>(a + sizeof(T) * (n > 0 ? n : 1));
+  return r;
+}
+
+size_t carve_size(const std::vector<size_t> &bytes) {
+  size_t s = 0;
+  for (size_t b : bytes) s += ((b > 0 ? b : 4) + 255) / 256 * 256 + 256;
+  return s + 256;
+}
+
+enum { K_PREPARE, K_WEIGHT, K_SAMPLE_FWD, K_RESOLVE, K_SAMPLE_BWD, K_BG_COMBINE, K_EDGE, K_SDF, K_COUNT };
+const char *const kKernelNames[K_COUNT] = {"prepare", "weight", "sample_fwd", "resolve",
+                                           "sample_bwd", "bg_combine", "edge", "sdf"};
+
+cudaEvent_t take_event(DvgScene *sc) {
+  if (!sc->event_pool.empty()) {
+    cudaEvent_t e = sc->event_pool.back();
+    sc->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+// Runs `launch` (kernel launches on st); with profiling on, brackets it with
+// two events on the same stream.
+template <class F>
+void timed(DvgScene *sc, int kid, cudaStream_t st, F launch) {
+  if (!sc->profiling) { launch(); return; }
+  cudaEvent_t a = take_event(sc), b = take_event(sc);
+  if (a) cudaEventRecord(a, st);
+  launch();
+  if (b) cudaEventRecord(b, st);
+  if (a && b) sc->pending.push_back({kid, a, b});
+}
+
+int validate_desc(const DvgSceneDesc *d, std::vector<int> &seg_point) {
+  if (!d) return fail(DVG_ERR_INVALID, "scene description is NULL");
+  if (d->canvas_width <= 0 || d->canvas_height <= 0) return fail(DVG_ERR_INVALID, "canvas size must be positive");
+  if (d->num_shapes < 0 || d->num_groups < 0 || d->num_params < 1 || d->total_segments < 0 ||
+      d->total_group_shapes < 0)
+    return fail(DVG_ERR_INVALID, "negative counts in scene description");
+  if ((d->num_shapes > 0 && !d->shape_info) || (d->num_groups > 0 && !d->group_info) ||
+      (d->total_segments > 0 && !d->segment_ctrl) || (d->total_group_shapes > 0 && !d->group_shapes))
+    return fail(DVG_ERR_INVALID, "missing topology array");
+  if (d->filter_type < DVG_BOX || d->filter_type > DVG_HANN) return fail(DVG_ERR_INVALID, "unknown filter type");
+  auto in_params = [&](long long off, long long n) { return off >= 0 && n >= 0 && off + n <= d->num_params; };
+  if (!in_params(d->filter_radius_off, 1)) return fail(DVG_ERR_INVALID, "filter radius offset out of range");
+  seg_point.assign((size_t)(d->total_segments > 0 ? d->total_segments : 1), 0);
+  for (int s = 0; s < d->num_shapes; s++) {
+    const int32_t *si = d->shape_info + (size_t)s * DVG_SHAPE_INFO_STRIDE;
+    int kind = si[DVG_SHAPE_KIND], po = si[DVG_SHAPE_PARAM_OFF];
+    if (!in_params(si[DVG_SHAPE_STROKE_WIDTH_OFF], 1))
+      return fail(DVG_ERR_INVALID, "shape " + std::to_string(s) + ": stroke width offset out of range");
+    if (kind == DVG_CIRCLE) {
+      if (!in_params(po, 3)) return fail(DVG_ERR_INVALID, "circle parameters out of range");
+    } else if (kind == DVG_ELLIPSE || kind == DVG_RECT) {
+      if (!in_params(po, 4)) return fail(DVG_ERR_INVALID, "shape parameters out of range");
+    } else if (kind == DVG_PATH) {
+      int np = si[DVG_SHAPE_NUM_POINTS], nseg = si[DVG_SHAPE_NUM_SEGMENTS], so = si[DVG_SHAPE_SEG_OFF];
+      int th = si[DVG_SHAPE_THICKNESS_OFF];
+      if (np < 0 || nseg < 0 || so < 0 || (long long)so + nseg > d->total_segments)
+        return fail(DVG_ERR_INVALID, "path " + std::to_string(s) + ": segment range out of bounds");
+      if (!in_params(po, 2LL * np)) return fail(DVG_ERR_INVALID, "path points out of range");
+      if (th >= 0 && !in_params(th, np)) return fail(DVG_ERR_INVALID, "path thickness out of range");
+      if (nseg > 0 && np < 1) return fail(DVG_ERR_INVALID, "path with segments but no points");
+      int pid = 0;
+      for (int i = 0; i < nseg; i++) {
+        int nc = d->segment_ctrl[so + i];
+        if (nc < 0 || nc > 2) return fail(DVG_ERR_INVALID, "num_control_points entries must be 0, 1 or 2");
+        if (pid + nc >= np) return fail(DVG_ERR_INVALID, "num_control_points does not fit the number of points");
+        seg_point[(size_t)so + i] = pid;
+        pid += nc + 1;
+      }
+    } else {
+      return fail(DVG_ERR_INVALID, "unknown shape kind " + std::to_string(kind));
+    }
+  }
+  for (int g = 0; g < d->num_groups; g++) {
+    const int32_t *gi = d->group_info + (size_t)g * DVG_GROUP_INFO_STRIDE;
+    int nsh = gi[DVG_GROUP_NUM_SHAPES], off = gi[DVG_GROUP_SHAPES_OFF];
+    if (nsh < 1 || off < 0 || (long long)off + nsh > d->total_group_shapes)
+      return fail(DVG_ERR_INVALID, "group " + std::to_string(g) + ": shape list out of range");
+    for (int k = 0; k < nsh; k++) {
+      int s = d->group_shapes[off + k];
+      if (s < 0 || s >= d->num_shapes) return fail(DVG_ERR_INVALID, "group refers to a shape id out of range");
+    }
+    for (int which = 0; which < 2; which++) {
+      int kind = gi[which ? DVG_GROUP_STROKE_KIND : DVG_GROUP_FILL_KIND];
+      int po = gi[which ? DVG_GROUP_STROKE_OFF : DVG_GROUP_FILL_OFF];
+      int k = gi[which ? DVG_GROUP_STROKE_STOPS : DVG_GROUP_FILL_STOPS];
+      if (kind == DVG_PAINT_NONE) continue;
+      if (kind == DVG_CONSTANT) {
+        if (!in_params(po, 4)) return fail(DVG_ERR_INVALID, "constant paint out of range");
+      } else if (kind == DVG_LINEAR || kind == DVG_RADIAL) {
+        if (k < 1 || !in_params(po, 4 + 5LL * k)) return fail(DVG_ERR_INVALID, "gradient paint out of range");
+      } else {
+        return fail(DVG_ERR_INVALID, "unknown paint kind");
+      }
+    }
+    if (!in_params(gi[DVG_GROUP_XFORM_OFF], 9)) return fail(DVG_ERR_INVALID, "group transform out of range");
+  }
+  return DVG_OK;
+}
+
+DevScene make_dev(DvgScene *sc, const float *params) {
+  DevScene S;
+  S.W = sc->d.canvas_width;
+  S.H = sc->d.canvas_height;
+  S.num_shapes = sc->d.num_shapes;
+  S.num_groups = sc->d.num_groups;
+  S.num_segments = sc->d.total_segments;
+  S.num_total = sc->num_total;
+  S.shape_info = sc->shape_info;
+  S.segment_ctrl = sc->segment_ctrl;
+  S.seg_point = sc->seg_point;
+  S.group_info = sc->group_info;
+  S.group_shapes = sc->group_shapes;
+  S.smp_shape = sc->smp_shape;
+  S.smp_group = sc->smp_group;
+  S.P = params;
+  S.c2s = sc->c2s;
+  S.g_local_box = sc->g_local_box;
+  S.g_canvas_box = sc->g_canvas_box;
+  S.g_max_radius = sc->g_max_radius;
+  S.s_box = sc->s_box;
+  S.s_length = sc->s_length;
+  S.seg_box = sc->seg_box;
+  S.seg_r = sc->seg_r;
+  S.seg_pmf = sc->seg_pmf;
+  S.seg_cdf = sc->seg_cdf;
+  S.seg_order = sc->seg_order;
+  S.smp_cdf = sc->smp_cdf;
+  S.smp_pmf = sc->smp_pmf;
+  S.tiles_x = sc->tiles_x;
+  S.tiles_y = sc->tiles_y;
+  S.tile_start = sc->tile_start;
+  S.tile_list = reinterpret_cast<int *>(sc->tiles.ptr);
+  S.scratch = sc->scratch;
+  S.err = sc->err;
+  return S;
+}
+
+int check_args(DvgScene *sc, const DvgRenderArgs *a) {
+  if (!sc) return fail(DVG_ERR_INVALID, "scene is NULL");
+  if (!a) return fail(DVG_ERR_INVALID, "render arguments are NULL");
+  if (a->width <= 0 || a->height <= 0 || a->num_samples_x <= 0 || a->num_samples_y <= 0)
+    return fail(DVG_ERR_INVALID, "image size and sample counts must be positive");
+  if ((long long)a->width * a->height * a->num_samples_x * a->num_samples_y > 0x7fffffffLL)
+    return fail(DVG_ERR_INVALID, "more than 2^31-1 samples per call (the reference indexes samples with int)");
+  if (!a->params) return fail(DVG_ERR_INVALID, "params is NULL");
+  if (a->background && (reinterpret_cast<uintptr_t>(a->background) & 15u))
+    return fail(DVG_ERR_INVALID, "background must be 16-byte aligned");
+  return DVG_OK;
+}
+
+DevRender make_render(DvgScene *sc, const DvgRenderArgs *a) {
+  DevRender R;
+  R.w = a->width;
+  R.h = a->height;
+  R.nsx = a->num_samples_x;
+  R.nsy = a->num_samples_y;
+  R.spp = R.nsx * R.nsy;
+  R.seed = a->seed;
+  R.prefilter = a->use_prefiltering ? 1 : 0;
+  R.ftype = sc->d.filter_type;
+  R.fr_ptr = a->params + sc->d.filter_radius_off;
+  R.fr = 0.f;  // read on the device (load_filter)
+  R.ri = 0;
+  R.background = a->background;
+  R.weight = reinterpret_cast<float *>(sc->weight.ptr);
+  R.d_image = nullptr;
+  R.d_params = nullptr;
+  R.d_background = nullptr;
+  R.d_translation = nullptr;
+  R.filter_radius_off = sc->d.filter_radius_off;
+  return R;
+}
+
+// scoped device switch
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+int prepare(DvgScene *sc, const DevScene &S, const DvgRenderArgs *a, cudaStream_t st) {
+  cudaError_t e;
+  if (!(a->flags & DVG_FLAG_NO_SYNC)) {
+    // a synchronous call reports only its own failures; with NO_SYNC the
+    // bits stay latched until dvg_scene_sync()
+    e = cudaMemsetAsync(sc->err, 0, 2 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return cuda_fail(e, "clearing the status word");
+  }
+  if ((a->flags & DVG_FLAG_REUSE_PREP) && sc->prepared) return DVG_OK;
+  timed(sc, K_PREPARE, st, [&] {
+    e = dvg::launch_prepare(S, sc->tile_cap, reinterpret_cast<int *>(sc->err + 1), sc->g_tile_range, sc->tile_count,
+                            st);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "scene preparation launch");
+  sc->prepared = true;
+  return DVG_OK;
+}
+
+// Waits for the stream and maps the device status word to a DvgStatus.
+// Returns 1 when the tile lists overflowed and were grown (the caller
+// repeats the call).
+int finish(DvgScene *sc, cudaStream_t st, bool *retry) {
+  *retry = false;
+  cudaError_t e = cudaMemcpyAsync(sc->h_status, sc->err, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "render");
+  unsigned bits = sc->h_status[0];
+  if (bits & DVG_EFLAG_SCENE_ZERO)
+    return fail(DVG_ERR_SCENE, "The total length of the shape boundaries in the scene is equal or less than 0.");
+  if (bits & DVG_EFLAG_SCENE_NAN)
+    return fail(DVG_ERR_SCENE, "The total length of the shape boundaries in the scene is not a number.");
+  if (bits & DVG_EFLAG_BIN_OVERFLOW) {
+    size_t need = (size_t)sc->h_status[1];
+    size_t cap = need + need / 2 + 1024;
+    if (cap > 0x7fffffffu) return fail(DVG_ERR_CAPACITY, "tile candidate lists exceed 2^31 entries");
+    e = sc->tiles.ensure(cap * sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "growing the tile lists");
+    sc->tile_cap = (int)(sc->tiles.bytes / sizeof(int));
+    sc->prepared = false;
+    *retry = true;
+    return DVG_OK;
+  }
+  if (bits & DVG_EFLAG_FILTER) return fail(DVG_ERR_INVALID, "filter radius must be in [0, 64]");
+  if (bits & DVG_EFLAG_CAPACITY)
+    return fail(DVG_ERR_CAPACITY,
+                "a sample has more fragments than the reference's per-sample limit (256, or 64 with prefiltering)");
+  if (bits & DVG_EFLAG_UNSUPPORTED)
+    return fail(DVG_ERR_UNSUPPORTED,
+                "unsupported input (the reference asserts on it): ellipse stroke/prefilter, prefiltered circle "
+                "stroke, or a rotated rect edge");
+  return DVG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *dvg_last_error(void) { return g_last_error.c_str(); }
+
+const char *dvg_version(void) { return "diffvg_gb300 0.1 (sm_103a)"; }
+
+int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
+  g_last_error.clear();
+  if (!out_scene) return fail(DVG_ERR_INVALID, "out_scene is NULL");
+  *out_scene = nullptr;
+  std::vector<int> seg_point;
+  int st = validate_desc(desc, seg_point);
+  if (st != DVG_OK) return st;
+  DvgScene *sc = new DvgScene();
+  sc->d = *desc;
+  sc->d.shape_info = nullptr;
+  sc->d.segment_ctrl = nullptr;
+  sc->d.group_info = nullptr;
+  sc->d.group_shapes = nullptr;
+  cudaGetDevice(&sc->device);
+  int S = desc->num_shapes, G = desc->num_groups, NSEG = desc->total_segments, NGS = desc->total_group_shapes;
+  sc->tiles_x = (desc->canvas_width + DVG_TILE - 1) / DVG_TILE;
+  sc->tiles_y = (desc->canvas_height + DVG_TILE - 1) / DVG_TILE;
+  int T = sc->tiles_x * sc->tiles_y;
+  // (group, shape) pairs of the boundary CDF, in group order (scene.cpp:207-246)
+  std::vector<int> smp_shape, smp_group;
+  for (int g = 0; g < G; g++) {
+    const int32_t *gi = desc->group_info + (size_t)g * DVG_GROUP_INFO_STRIDE;
+    for (int k = 0; k < gi[DVG_GROUP_NUM_SHAPES]; k++) {
+      smp_shape.push_back(desc->group_shapes[gi[DVG_GROUP_SHAPES_OFF] + k]);
+      smp_group.push_back(g);
+    }
+  }
+  sc->num_total = (int)smp_shape.size();
+  int NT = sc->num_total;
+  cudaError_t e;
+  // topology
+  std::vector<size_t> tb = {sizeof(int) * S * DVG_SHAPE_INFO_STRIDE, sizeof(int) * NSEG, sizeof(int) * NSEG,
+                            sizeof(int) * G * DVG_GROUP_INFO_STRIDE, sizeof(int) * NGS, sizeof(int) * NT,
+                            sizeof(int) * NT};
+  e = sc->topo.ensure(carve_size(tb));
+  if (e != cudaSuccess) { delete sc; return cuda_fail(e, "allocating the scene topology"); }
+  char *p = reinterpret_cast<char *>(sc->topo.ptr);
+  sc->shape_info = carve<int>(p, (size_t)S * DVG_SHAPE_INFO_STRIDE);
+  sc->segment_ctrl = carve<int>(p, NSEG);
+  sc->seg_point = carve<int>(p, NSEG);
+  sc->group_info = carve<int>(p, (size_t)G * DVG_GROUP_INFO_STRIDE);
+  sc->group_shapes = carve<int>(p, NGS);
+  sc->smp_shape = carve<int>(p, NT);
+  sc->smp_group = carve<int>(p, NT);
+  struct Up { void *dst; const void *src; size_t n; } ups[] = {
+      {sc->shape_info, desc->shape_info, sizeof(int) * S * DVG_SHAPE_INFO_STRIDE},
+      {sc->segment_ctrl, desc->segment_ctrl, sizeof(int) * NSEG},
+      {sc->seg_point, seg_point.data(), sizeof(int) * NSEG},
+      {sc->group_info, desc->group_info, sizeof(int) * G * DVG_GROUP_INFO_STRIDE},
+      {sc->group_shapes, desc->group_shapes, sizeof(int) * NGS},
+      {sc->smp_shape, smp_shape.data(), sizeof(int) * NT},
+      {sc->smp_group, smp_group.data(), sizeof(int) * NT}};
+  for (auto &u : ups) {
+    if (u.n == 0) continue;
+    e = cudaMemcpy(u.dst, u.src, u.n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "uploading the scene topology"); }
+  }
+  // derived arrays
+  std::vector<size_t> db = {
+      sizeof(float) * 9 * G, sizeof(float4) * G, sizeof(float4) * G, sizeof(float) * G,    // c2s, boxes, radius
+      sizeof(float4) * S, sizeof(float) * S,                                              // s_box, s_length
+      sizeof(float4) * NSEG, sizeof(float) * NSEG, sizeof(float) * NSEG, sizeof(float) * NSEG,
+      sizeof(int) * NSEG,                                                                  // seg_*
+      sizeof(float) * NT, sizeof(float) * NT,                                              // smp cdf/pmf
+      sizeof(int) * (T + 1), sizeof(int) * T, sizeof(int4) * G,                           // tiles
+      sizeof(int) * (10 * (size_t)NSEG + 8 * (size_t)S + 8),                              // scratch
+      sizeof(unsigned) * 4};
+  e = sc->derived.ensure(carve_size(db));
+  if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "allocating scene arenas"); }
+  p = reinterpret_cast<char *>(sc->derived.ptr);
+  sc->c2s = carve<float>(p, 9 * (size_t)G);
+  sc->g_local_box = carve<float4>(p, G);
+  sc->g_canvas_box = carve<float4>(p, G);
+  sc->g_max_radius = carve<float>(p, G);
+  sc->s_box = carve<float4>(p, S);
+  sc->s_length = carve<float>(p, S);
+  sc->seg_box = carve<float4>(p, NSEG);
+  sc->seg_r = carve<float>(p, NSEG);
+  sc->seg_pmf = carve<float>(p, NSEG);
+  sc->seg_cdf = carve<float>(p, NSEG);
+  sc->seg_order = carve<int>(p, NSEG);
+  sc->smp_cdf = carve<float>(p, NT);
+  sc->smp_pmf = carve<float>(p, NT);
+  sc->tile_start = carve<int>(p, (size_t)T + 1);
+  sc->tile_count = carve<int>(p, T);
+  sc->g_tile_range = carve<int4>(p, G);
+  sc->scratch = carve<int>(p, 10 * (size_t)NSEG + 8 * (size_t)S + 8);
+  sc->err = carve<unsigned>(p, 4);
+  e = cudaMemset(sc->derived.ptr, 0, sc->derived.bytes);
+  if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "clearing scene arenas"); }
+  size_t cap = (size_t)T * 32;
+  if (cap < 65536) cap = 65536;
+  e = sc->tiles.ensure(cap * sizeof(int));
+  if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "allocating tile lists"); }
+  sc->tile_cap = (int)(sc->tiles.bytes / sizeof(int));
+  e = cudaMallocHost(&sc->h_status, 4 * sizeof(unsigned));
+  if (e != cudaSuccess) { sc->h_status = nullptr; dvg_scene_destroy(sc); return cuda_fail(e, "pinned status"); }
+  *out_scene = sc;
+  return DVG_OK;
+}
+
+int dvg_scene_destroy(DvgScene *sc) {
+  if (!sc) return DVG_OK;
+  DeviceGuard guard(sc->device);
+  sc->topo.release();
+  sc->derived.release();
+  sc->tiles.release();
+  sc->weight.release();
+  sc->samples.release();
+  sc->dbg_val.release();
+  sc->dbg_flag.release();
+  if (sc->h_status) cudaFreeHost(sc->h_status);
+  for (auto &p : sc->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+  for (auto ev : sc->event_pool) cudaEventDestroy(ev);
+  delete sc;
+  return DVG_OK;
+}
+
+int dvg_scene_profile(DvgScene *sc, int enable) {
+  g_last_error.clear();
+  if (!sc) return fail(DVG_ERR_INVALID, "scene is NULL");
+  DeviceGuard guard(sc->device);
+  for (auto &p : sc->pending) { sc->event_pool.push_back(p.a); sc->event_pool.push_back(p.b); }
+  sc->pending.clear();
+  for (int k = 0; k < 16; k++) { sc->total_ms[k] = 0; sc->launches[k] = 0; }
+  sc->profiling = enable != 0;
+  return DVG_OK;
+}
+
+int dvg_scene_profile_read(DvgScene *sc, DvgKernelTime *out, int max_entries, int *num_entries) {
+  g_last_error.clear();
+  if (!sc || !num_entries) return fail(DVG_ERR_INVALID, "scene / num_entries is NULL");
+  DeviceGuard guard(sc->device);
+  for (auto &p : sc->pending) {
+    cudaError_t e = cudaEventSynchronize(p.b);
+    if (e != cudaSuccess) return cuda_fail(e, "reading kernel timings");
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      sc->total_ms[p.kid] += ms;
+      sc->launches[p.kid] += 1;
+    }
+    sc->event_pool.push_back(p.a);
+    sc->event_pool.push_back(p.b);
+  }
+  sc->pending.clear();
+  int n = 0;
+  for (int k = 0; k < K_COUNT; k++) {
+    if (sc->launches[k] == 0) continue;
+    if (out && n < max_entries) {
+      out[n].name = kKernelNames[k];
+      out[n].launches = sc->launches[k];
+      out[n].total_ms = sc->total_ms[k];
+    }
+    n++;
+  }
+  *num_entries = n;
+  return DVG_OK;
+}
+
+int dvg_scene_sync(DvgScene *sc, void *stream) {
+  g_last_error.clear();
+  if (!sc) return fail(DVG_ERR_INVALID, "scene is NULL");
+  DeviceGuard guard(sc->device);
+  bool retry = false;
+  int st = finish(sc, reinterpret_cast<cudaStream_t>(stream), &retry);
+  cudaMemsetAsync(sc->err, 0, 2 * sizeof(unsigned), reinterpret_cast<cudaStream_t>(stream));
+  if (st == DVG_OK && retry)
+    return fail(DVG_ERR_CAPACITY, "tile candidate lists overflowed and were grown; repeat the affected calls");
+  return st;
+}
+
+int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float *sdf, void *stream) {
+  g_last_error.clear();
+  int st = check_args(sc, a);
+  if (st != DVG_OK) return st;
+  if ((image == nullptr) == (sdf == nullptr)) return fail(DVG_ERR_INVALID, "exactly one of image / sdf must be set");
+  if (image && a->num_eval_positions > 0) return fail(DVG_ERR_INVALID, "eval_positions apply to the sdf output only");
+  if (image && (reinterpret_cast<uintptr_t>(image) & 15u)) return fail(DVG_ERR_INVALID, "image must be 16-byte aligned");
+  DeviceGuard guard(sc->device);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  size_t npx = (size_t)a->width * a->height, n = npx * a->num_samples_x * a->num_samples_y;
+  cudaError_t e = sc->weight.ensure(npx * sizeof(float));
+  if (e == cudaSuccess && image) e = sc->samples.ensure(n * sizeof(float4));
+  if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
+  if (sc->d.num_groups == 0 && image) {
+    // empty scene: the background (or transparent black), unfiltered
+    e = a->background ? cudaMemcpyAsync(image, a->background, npx * 4 * sizeof(float), cudaMemcpyDeviceToDevice, s)
+                      : cudaMemsetAsync(image, 0, npx * 4 * sizeof(float), s);
+    if (e == cudaSuccess && !(a->flags & DVG_FLAG_NO_SYNC)) e = cudaStreamSynchronize(s);
+    return e == cudaSuccess ? DVG_OK : cuda_fail(e, "empty-scene forward");
+  }
+  for (int attempt = 0; attempt < 3; attempt++) {
+    DevScene S = make_dev(sc, a->params);
+    if ((st = prepare(sc, S, a, s)) != DVG_OK) return st;
+    DevRender R = make_render(sc, a);
+    if (image) {
+      float4 *samples = reinterpret_cast<float4 *>(sc->samples.ptr);
+      timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
+      timed(sc, K_SAMPLE_FWD, s, [&] { dvg::launch_sample_fwd(S, R, samples, s); });
+      timed(sc, K_RESOLVE, s, [&] { dvg::launch_resolve(R, samples, image, s); });
+      e = cudaGetLastError();
+    } else {
+      size_t nout = a->num_eval_positions > 0 ? (size_t)a->num_eval_positions : npx;
+      e = cudaMemsetAsync(sdf, 0, nout * sizeof(float), s);
+      if (e == cudaSuccess) {
+        timed(sc, K_SDF, s, [&] {
+          dvg::launch_sdf(S, R, a->num_eval_positions > 0 ? a->eval_positions : nullptr, a->num_eval_positions, sdf,
+                          nullptr, s);
+        });
+        e = cudaGetLastError();
+      }
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "forward launch");
+    if (a->flags & DVG_FLAG_NO_SYNC) return DVG_OK;
+    bool retry = false;
+    if ((st = finish(sc, s, &retry)) != DVG_OK) return st;
+    if (!retry) return DVG_OK;
+  }
+  return fail(DVG_ERR_CAPACITY, "tile candidate lists kept overflowing");
+}
+
+int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_image, const float *d_sdf,
+                        float *d_params, float *d_background, float *d_translation, void *stream) {
+  g_last_error.clear();
+  int st = check_args(sc, a);
+  if (st != DVG_OK) return st;
+  if ((d_image == nullptr) == (d_sdf == nullptr)) return fail(DVG_ERR_INVALID, "exactly one of d_image / d_sdf must be set");
+  if (!d_params) return fail(DVG_ERR_INVALID, "d_params is NULL");
+  if (d_image && a->num_eval_positions > 0) return fail(DVG_ERR_INVALID, "eval_positions apply to the sdf output only");
+  if ((d_image && (reinterpret_cast<uintptr_t>(d_image) & 15u)) ||
+      (d_background && (reinterpret_cast<uintptr_t>(d_background) & 15u)))
+    return fail(DVG_ERR_INVALID, "d_image and d_background must be 16-byte aligned");
+  if (d_background && !a->background) d_background = nullptr;  // no background, no background gradient
+  if (sc->d.num_groups == 0) return DVG_OK;                       // empty scene: nothing to differentiate
+  DeviceGuard guard(sc->device);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  size_t npx = (size_t)a->width * a->height, n = npx * a->num_samples_x * a->num_samples_y;
+  cudaError_t e = sc->weight.ensure(npx * sizeof(float));
+  if (e == cudaSuccess && d_background) e = sc->dbg_val.ensure(n * sizeof(float4));
+  if (e == cudaSuccess && d_background) e = sc->dbg_flag.ensure(n * sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
+  for (int attempt = 0; attempt < 3; attempt++) {
+    DevScene S = make_dev(sc, a->params);
+    if ((st = prepare(sc, S, a, s)) != DVG_OK) return st;
+    DevRender R = make_render(sc, a);
+    R.d_params = d_params;
+    R.d_translation = d_translation;
+    if (d_image) {
+      R.d_image = d_image;
+      R.d_background = d_background;
+      float4 *dbg_val = reinterpret_cast<float4 *>(sc->dbg_val.ptr);
+      int *dbg_flag = reinterpret_cast<int *>(sc->dbg_flag.ptr);
+      timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
+      timed(sc, K_SAMPLE_BWD, s, [&] { dvg::launch_sample_bwd(S, R, dbg_val, dbg_flag, s); });
+      if (d_background) timed(sc, K_BG_COMBINE, s, [&] { dvg::launch_bg_combine(S, R, dbg_val, dbg_flag, s); });
+      if (!a->use_prefiltering) timed(sc, K_EDGE, s, [&] { dvg::launch_edge(S, R, s); });
+    } else {
+      timed(sc, K_SDF, s, [&] {
+        dvg::launch_sdf(S, R, a->num_eval_positions > 0 ? a->eval_positions : nullptr, a->num_eval_positions,
+                        nullptr, d_sdf, s);
+      });
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "backward launch");
+    if (a->flags & DVG_FLAG_NO_SYNC) return DVG_OK;
+    bool retry = false;
+    if ((st = finish(sc, s, &retry)) != DVG_OK) return st;
+    if (!retry) return DVG_OK;
+  }
+  return fail(DVG_ERR_CAPACITY, "tile candidate lists kept overflowing");
+}
+
+}  // extern "C"

@@ -1,0 +1,881 @@
+// Device-side scene representation and per-sample geometry of the GB300
+// render path.
+//
+// Everything here is __device__ code evaluated per sample (or per boundary
+// sample).  Arithmetic follows the reference's evaluation order and
+// precision (fp32 where it computes in float, fp64 where it promotes to
+// double) so that sample classification (inside / outside, within stroke or
+// not) agrees with the reference CPU build; the library is compiled with
+// --fmad=false for the same reason.  Each function cites the reference
+// file:line whose semantics it implements.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/diffvg_gb300.h"
+
+#define DVG_TILE 16
+#define DVG_MAX_FRAGMENTS 256          // diffvg.cpp:542
+#define DVG_MAX_PREFILTER_FRAGMENTS 64 // diffvg.cpp:847
+#define DVG_PI 3.14159265358979323846
+
+// error bits of the per-scene device status word
+enum {
+  DVG_EFLAG_CAPACITY = 1u,     // fragment list above the reference's cap
+  DVG_EFLAG_UNSUPPORTED = 2u,  // input on which the reference asserts
+  DVG_EFLAG_SCENE_ZERO = 4u,   // total boundary length <= 0
+  DVG_EFLAG_SCENE_NAN = 8u,    // total boundary length not finite
+  DVG_EFLAG_FILTER = 16u,      // filter radius outside [0, 64]
+};
+
+// Resident scene: topology (uploaded once) + per-call derived arrays.
+struct DevScene {
+  int W, H;  // canvas size
+  int num_shapes, num_groups, num_segments, num_total;
+  const int *shape_info;    // [S * DVG_SHAPE_INFO_STRIDE]
+  const int *segment_ctrl;  // [NSEG]
+  const int *seg_point;     // [NSEG] first point of each segment within its path
+  const int *group_info;    // [G * DVG_GROUP_INFO_STRIDE]
+  const int *group_shapes;  // [sum of group sizes]
+  const int *smp_shape;     // [num_total] (group, shape) pairs of the boundary CDF
+  const int *smp_group;
+  const float *P;           // parameter arena
+  // derived per call from P
+  float *c2s;               // [G*9] canvas_to_shape
+  float4 *g_local_box;      // [G] (lo.x, lo.y, hi.x, hi.y) in shape space
+  float4 *g_canvas_box;     // [G] in canvas space
+  float *g_max_radius;      // [G]
+  float4 *s_box;            // [S]
+  float *s_length;          // [S]
+  float4 *seg_box;          // [NSEG]
+  float *seg_r, *seg_pmf, *seg_cdf;
+  int *seg_order;           // [NSEG] per-path visiting order (local indices)
+  float *smp_cdf, *smp_pmf; // [num_total]
+  int tiles_x, tiles_y;
+  int *tile_start;          // [tiles+1]
+  int *tile_list;           // candidate groups per tile, ascending
+  int *scratch;             // [8*NSEG + 8*S] path leaf-order scratch
+  unsigned *err;            // status word (DVG_EFLAG_*)
+};
+
+// Per-call render settings (image space).
+struct DevRender {
+  int w, h, nsx, nsy, spp;
+  uint64_t seed;
+  int prefilter;
+  int ftype;
+  const float *fr_ptr;       // filter radius in the parameter arena
+  float fr;                  // *fr_ptr, loaded on the device (load_filter)
+  int ri;                    // ceil(fr)
+  const float *background;   // [h*w*4] or null
+  float *weight;             // [h*w]
+  const float *d_image;      // [h*w*4] or null
+  float *d_params;           // gradient arena or null
+  float *d_background;       // [h*w*4] or null
+  float *d_translation;      // [h*w*2] or null
+  int filter_radius_off;
+};
+
+typedef float2 v2;
+
+#define DI __device__ __forceinline__
+
+DI v2 V2(float x, float y) { return make_float2(x, y); }
+DI v2 add2(v2 a, v2 b) { return V2(a.x + b.x, a.y + b.y); }
+DI v2 sub2(v2 a, v2 b) { return V2(a.x - b.x, a.y - b.y); }
+DI v2 mul2(v2 a, v2 b) { return V2(a.x * b.x, a.y * b.y); }
+DI v2 scl2(float s, v2 a) { return V2(s * a.x, s * a.y); }
+DI v2 div2s(v2 a, float s) { return V2(a.x / s, a.y / s); }
+DI v2 neg2(v2 a) { return V2(-a.x, -a.y); }
+DI float sum2(v2 a) { return a.x + a.y; }
+DI float dot2(v2 a, v2 b) { return a.x * b.x + a.y * b.y; }
+DI float lensq2(v2 a) { return a.x * a.x + a.y * a.y; }
+DI float len2(v2 a) { return sqrtf(lensq2(a)); }
+DI float dist2(v2 a, v2 b) { return len2(sub2(b, a)); }
+DI float distsq2(v2 a, v2 b) { return lensq2(sub2(b, a)); }
+DI v2 normalize2(v2 a) { float l = len2(a); return V2(a.x / l, a.y / l); }
+DI float4 F4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
+DI float4 add4(float4 a, float4 b) { return F4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+DI float4 sub4(float4 a, float4 b) { return F4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+DI float4 scl4(float s, float4 a) { return F4(s * a.x, s * a.y, s * a.z, s * a.w); }
+DI float dot4(float4 a, float4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+DI float rmin(float a, float b) { return a < b ? a : b; }
+DI float rmax(float a, float b) { return a > b ? a : b; }
+DI float sq(float x) { return x * x; }
+DI float clampf_(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
+DI float det2(v2 a, v2 b) { return a.x * b.y - b.x * a.y; }
+
+// boxes are float4 (lo.x, lo.y, hi.x, hi.y); aabb.h:15-40, 62-66
+DI float4 box_empty() { return F4(INFINITY, INFINITY, -INFINITY, -INFINITY); }
+DI float4 box_add(float4 b, v2 p) { return F4(rmin(p.x, b.x), rmin(p.y, b.y), rmax(p.x, b.z), rmax(p.y, b.w)); }
+DI float4 box_union(float4 a, float4 b) {
+  return F4(rmin(a.x, b.x), rmin(a.y, b.y), rmax(a.z, b.z), rmax(a.w, b.w));
+}
+DI bool box_in(float4 b, v2 p) { return p.x >= b.x && p.x <= b.z && p.y >= b.y && p.y <= b.w; }
+DI bool box_in_r(float4 b, v2 p, float r) {
+  return p.x >= b.x - r && p.x <= b.z + r && p.y >= b.y - r && p.y <= b.w + r;
+}
+// winding-ray box test (winding_number.h:33-42)
+DI bool box_ray(float4 b, v2 p) {
+  if (p.y < b.y || p.y > b.w) return false;
+  if (p.x > b.z) return false;
+  return true;
+}
+
+// 3x3 row-major transforms (matrix.h:209-229, 504-544)
+DI v2 xform_pt(const float *m, v2 p) {
+  float t0 = m[0] * p.x + m[1] * p.y + m[2];
+  float t1 = m[3] * p.x + m[4] * p.y + m[5];
+  float t2 = m[6] * p.x + m[7] * p.y + m[8];
+  return V2(t0 / t2, t1 / t2);
+}
+DI void d_xform_pt(const float *m, v2 pt, v2 d_out, float *d_m, v2 *d_pt) {
+  float t0 = m[0] * pt.x + m[1] * pt.y + m[2];
+  float t1 = m[3] * pt.x + m[4] * pt.y + m[5];
+  float t2 = m[6] * pt.x + m[7] * pt.y + m[8];
+  v2 out = V2(t0 / t2, t1 / t2);
+  float dt0 = d_out.x / t2, dt1 = d_out.y / t2;
+  float dt2 = -(d_out.x * out.x + d_out.y * out.y) / t2;
+  d_m[0] += dt0 * pt.x; d_m[1] += dt0 * pt.y; d_m[2] += dt0;
+  d_m[3] += dt1 * pt.x; d_m[4] += dt1 * pt.y; d_m[5] += dt1;
+  d_m[6] += dt2 * pt.x; d_m[7] += dt2 * pt.y; d_m[8] += dt2;
+  d_pt->x += dt0 * m[0] + dt1 * m[3] + dt2 * m[6];
+  d_pt->y += dt0 * m[1] + dt1 * m[4] + dt2 * m[7];
+}
+DI v2 xform_normal(const float *m_inv, v2 n) {
+  return normalize2(V2(m_inv[0] * n.x + m_inv[3] * n.y, m_inv[1] * n.x + m_inv[4] * n.y));
+}
+DI void inverse3(const float *m, float *r) {
+#define M(i, j) m[3 * (i) + (j)]
+  float det = M(0, 0) * (M(1, 1) * M(2, 2) - M(2, 1) * M(1, 2)) -
+              M(0, 1) * (M(1, 0) * M(2, 2) - M(1, 2) * M(2, 0)) +
+              M(0, 2) * (M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0));
+  float invdet = 1 / det;
+  r[0] = (M(1, 1) * M(2, 2) - M(2, 1) * M(1, 2)) * invdet;
+  r[1] = (M(0, 2) * M(2, 1) - M(0, 1) * M(2, 2)) * invdet;
+  r[2] = (M(0, 1) * M(1, 2) - M(0, 2) * M(1, 1)) * invdet;
+  r[3] = (M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2)) * invdet;
+  r[4] = (M(0, 0) * M(2, 2) - M(0, 2) * M(2, 0)) * invdet;
+  r[5] = (M(1, 0) * M(0, 2) - M(0, 0) * M(1, 2)) * invdet;
+  r[6] = (M(1, 0) * M(2, 1) - M(2, 0) * M(1, 1)) * invdet;
+  r[7] = (M(2, 0) * M(0, 1) - M(0, 0) * M(2, 1)) * invdet;
+  r[8] = (M(0, 0) * M(1, 1) - M(1, 0) * M(0, 1)) * invdet;
+#undef M
+}
+
+// ---------------------------------------------------------------------------
+// pcg32 (pcg.h:11-40): one stream per sample index, XSH-RR output.
+struct Pcg { uint64_t state, inc; };
+DI uint32_t pcg_next(Pcg &r) {
+  uint64_t old = r.state;
+  r.state = old * 6364136223846793005ULL + (r.inc | 1ULL);
+  uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+  uint32_t rot = (uint32_t)(old >> 59u);
+  return __funnelshift_r(xs, xs, rot);
+}
+DI float pcg_float(Pcg &r) { return __uint_as_float((pcg_next(r) >> 9) | 0x3f800000u) - 1.0f; }
+DI Pcg pcg_init(int32_t idx, uint64_t seed) {
+  Pcg s;
+  s.inc = (((uint64_t)(int64_t)idx + 1ULL) << 1u) | 1ULL;
+  // state = 0; next(); state += K + seed; next();  (the first output is unused)
+  s.state = s.inc + (0x853c49e6748fea9bULL + seed);
+  s.state = s.state * 6364136223846793005ULL + s.inc;
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// root solvers (solve.h:5-59)
+DI bool solve_quadratic_f(float a, float b, float c, float *t0, float *t1) {
+  float discrim = b * b - 4 * a * c;
+  if (discrim < 0) return false;
+  float root = sqrtf(discrim);
+  float q = (b < 0) ? -0.5f * (b - root) : -0.5f * (b + root);
+  *t0 = q / a;
+  *t1 = c / q;
+  if (*t0 > *t1) { float tmp = *t0; *t0 = *t1; *t1 = tmp; }
+  return true;
+}
+DI bool solve_quadratic_d(double a, double b, double c, double *t0, double *t1) {
+  double discrim = b * b - 4 * a * c;
+  if (discrim < 0) return false;
+  double root = sqrt(discrim);
+  double q = (b < 0) ? -0.5f * (b - root) : -0.5f * (b + root);
+  *t0 = q / a;
+  *t1 = c / q;
+  if (*t0 > *t1) { double tmp = *t0; *t0 = *t1; *t1 = tmp; }
+  return true;
+}
+DI int solve_cubic_d(double a, double b, double c, double d, double t[3]) {
+  if (fabs(a) < 1e-6f) return solve_quadratic_d(b, c, d, &t[0], &t[1]) ? 2 : 0;
+  b /= a; c /= a; d /= a;
+  double Q = (b * b - 3 * c) / 9.f;
+  double R = (2 * b * b * b - 9 * b * c + 27 * d) / 54.f;
+  if (R * R < Q * Q * Q) {
+    double theta = acos(R / sqrt(Q * Q * Q));
+    double sQ = sqrt(Q);
+    t[0] = -2.f * sQ * cos(theta / 3.f) - b / 3.f;
+    t[1] = -2.f * sQ * cos((theta + 2.f * DVG_PI) / 3.f) - b / 3.f;
+    t[2] = -2.f * sQ * cos((theta - 2.f * DVG_PI) / 3.f) - b / 3.f;
+    return 3;
+  } else {
+    double A = R > 0 ? -pow(R + sqrt(R * R - Q * Q * Q), (double)(1. / 3.))
+                     : pow(-R + sqrt(R * R - Q * Q * Q), (double)(1. / 3.));
+    double B = fabs(A) > 1e-6f ? Q / A : 0.0;
+    t[0] = (A + B) - b / 3.0;
+    return 1;
+  }
+}
+// solve_cubic<float>: the reference's unqualified sqrt/acos/cos/pow bind to
+// the double-precision functions, so intermediates are double until stored
+// back into a float.
+DI int solve_cubic_f(float a, float b, float c, float d, float t[3]) {
+  if (fabsf(a) < 1e-6f) return solve_quadratic_f(b, c, d, &t[0], &t[1]) ? 2 : 0;
+  b /= a; c /= a; d /= a;
+  float Q = (b * b - 3 * c) / 9.f;
+  float R = (2 * b * b * b - 9 * b * c + 27 * d) / 54.f;
+  if (R * R < Q * Q * Q) {
+    float theta = (float)acos((double)R / sqrt((double)(Q * Q * Q)));
+    double sQ = sqrt((double)Q);
+    t[0] = (float)(-2.f * sQ * cos((double)(theta / 3.f)) - (double)(b / 3.f));
+    t[1] = (float)(-2.f * sQ * cos((double)((theta + 2.f * (float)DVG_PI) / 3.f)) - (double)(b / 3.f));
+    t[2] = (float)(-2.f * sQ * cos((double)((theta - 2.f * (float)DVG_PI) / 3.f)) - (double)(b / 3.f));
+    return 3;
+  } else {
+    double third = (double)(float)(1. / 3.);
+    float A = R > 0 ? (float)(-pow((double)R + sqrt((double)(R * R - Q * Q * Q)), third))
+                    : (float)pow((double)(-R) + sqrt((double)(R * R - Q * Q * Q)), third);
+    float B = fabsf(A) > 1e-6f ? Q / A : 0.f;
+    t[0] = (A + B) - b / 3.f;
+    return 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pixel filters (filter.h:22-106)
+DI float filter_weight(int type, float r, float dx, float dy) {
+  if (fabsf(dx) > r || fabsf(dy) > r) return 0;
+  if (type == DVG_BOX) return 1.f / sq(2 * r);
+  if (type == DVG_TENT) return (r - fabsf(dx)) * (r - fabsf(dy)) / sq(sq(r));
+  if (type == DVG_PARABOLIC) return (4.f / 3.f) * (1 - sq(dx / r)) * (4.f / 3.f) * (1 - sq(dy / r));
+  float ndx = (dx / (2 * r)) + 0.5f, ndy = (dy / (2 * r)) + 0.5f;
+  return 0.5f * (1.f - cosf((float)(2 * DVG_PI) * ndx)) * 0.5f * (1.f - cosf((float)(2 * DVG_PI) * ndy)) / sq(r);
+}
+DI float d_filter_weight(int type, float r, float dx, float dy, float d_ret) {
+  if (type == DVG_BOX) {
+    return d_ret * (-2) * 2 * r / ((2 * r) * (2 * r) * (2 * r));
+  } else if (type == DVG_TENT) {
+    float fx = r - fabsf(dx), fy = r - fabsf(dy);
+    float norm = 1 / sq(r);
+    float d_fx = d_ret * fy * norm, d_fy = d_ret * fx * norm, d_norm = d_ret * fx * fy;
+    return d_fx + d_fy + (-4) * d_norm / (float)pow((double)r, 5.0);
+  } else if (type == DVG_PARABOLIC) {
+    float r3 = r * r * r;
+    return -(2 * sq(dx) + 2 * sq(dy)) / r3;
+  } else {
+    float ndx = (dx / (2 * r)) + 0.5f, ndy = (dy / (2 * r)) + 0.5f;
+    float fx = 0.5f * (1.f - cosf((float)(2 * DVG_PI) * ndx));
+    float fy = 0.5f * (1.f - cosf((float)(2 * DVG_PI) * ndy));
+    float norm = 1 / sq(r);
+    float d_fx = d_ret * fy * norm, d_fy = d_ret * fx * norm, d_norm = d_ret * fx * fy;
+    float d_ndx = d_fx * 0.5f * sinf((float)(2 * DVG_PI) * ndx) * (float)(2 * DVG_PI);
+    float d_ndy = d_fy * 0.5f * sinf((float)(2 * DVG_PI) * ndy) * (float)(2 * DVG_PI);
+    return d_ndx * (-2 * dx / sq(2 * r)) + d_ndy * (-2 * dy / sq(2 * r)) + (-2) * d_norm / (r * r * r);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// scene accessors
+#define SI(S, s, f) __ldg(&(S).shape_info[(s) * DVG_SHAPE_INFO_STRIDE + (f)])
+#define GI(S, g, f) __ldg(&(S).group_info[(g) * DVG_GROUP_INFO_STRIDE + (f)])
+
+DI v2 path_pt(const DevScene &S, int po, int i) {
+  return V2(__ldg(&S.P[po + 2 * i]), __ldg(&S.P[po + 2 * i + 1]));
+}
+DI float pget(const DevScene &S, int off) { return __ldg(&S.P[off]); }
+DI float stroke_width(const DevScene &S, int s) { return pget(S, SI(S, s, DVG_SHAPE_STROKE_WIDTH_OFF)); }
+DI void flag_error(const DevScene &S, unsigned bit) { atomicOr(S.err, bit); }
+
+DI v2 eval_quad(v2 p0, v2 p1, v2 p2, float t) {
+  float tt = 1 - t;
+  return add2(add2(scl2(tt * tt, p0), scl2(2 * tt * t, p1)), scl2(t * t, p2));
+}
+DI v2 eval_cubic(v2 p0, v2 p1, v2 p2, v2 p3, float t) {
+  float tt = 1 - t;
+  return add2(add2(add2(scl2(tt * tt * tt, p0), scl2(3 * tt * tt * t, p1)), scl2(3 * tt * t * t, p2)),
+              scl2(t * t * t, p3));
+}
+
+// Candidate groups for a canvas-space point: the point's tile list, or all
+// groups outside the tile grid.  Returns true when the tile list is used.
+DI bool cand_range(const DevScene &S, v2 pt, int &begin, int &end) {
+  float fx = floorf(pt.x / DVG_TILE), fy = floorf(pt.y / DVG_TILE);
+  if (fx >= 0 && fy >= 0 && fx < S.tiles_x && fy < S.tiles_y) {
+    int t = (int)fy * S.tiles_x + (int)fx;
+    begin = __ldg(&S.tile_start[t]);
+    end = __ldg(&S.tile_start[t + 1]);
+    return true;
+  }
+  begin = 0;
+  end = S.num_groups;
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// winding numbers (winding_number.h:9-202)
+DI int winding_segment(const DevScene &S, int po, int np, int nc, int i0, v2 pt) {
+  int w = 0;
+  if (nc == 0) {
+    v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, (i0 + 1) % np);
+    if (p1.y != p0.y) {
+      float t = (pt.y - p0.y) / (p1.y - p0.y);
+      if (t >= 0 && t <= 1) {
+        float tp = p0.x - pt.x + t * (p1.x - p0.x);
+        if (tp >= 0) w += (p1.y - p0.y > 0) ? 1 : -1;
+      }
+    }
+  } else if (nc == 1) {
+    v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, (i0 + 2) % np);
+    float t[2];
+    if (solve_quadratic_f(p0.y - 2 * p1.y + p2.y, -2 * p0.y + 2 * p1.y, p0.y - pt.y, &t[0], &t[1])) {
+      for (int j = 0; j < 2; j++) {
+        if (t[j] >= 0 && t[j] <= 1) {
+          float tp = (p0.x - 2 * p1.x + p2.x) * t[j] * t[j] + (-2 * p0.x + 2 * p1.x) * t[j] + p0.x - pt.x;
+          if (tp >= 0) w += (2 * (p0.y - 2 * p1.y + p2.y) * t[j] + (-2 * p0.y + 2 * p1.y) > 0) ? 1 : -1;
+        }
+      }
+    }
+  } else {
+    v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, i0 + 2),
+       p3 = path_pt(S, po, (i0 + 3) % np);
+    double t[3];
+    int n = solve_cubic_d((double)(-p0.y + 3 * p1.y - 3 * p2.y + p3.y), (double)(3 * p0.y - 6 * p1.y + 3 * p2.y),
+                          (double)(-3 * p0.y + 3 * p1.y), (double)(p0.y - pt.y), t);
+    for (int j = 0; j < n; j++) {
+      if (t[j] >= 0 && t[j] <= 1) {
+        double tp = (-p0.x + 3 * p1.x - 3 * p2.x + p3.x) * t[j] * t[j] * t[j] +
+                    (3 * p0.x - 6 * p1.x + 3 * p2.x) * t[j] * t[j] + (-3 * p0.x + 3 * p1.x) * t[j] + p0.x - pt.x;
+        if (tp > 0) {
+          w += (3 * (-p0.y + 3 * p1.y - 3 * p2.y + p3.y) * t[j] * t[j] +
+                    2 * (3 * p0.y - 6 * p1.y + 3 * p2.y) * t[j] + (-3 * p0.y + 3 * p1.y) > 0)
+                   ? 1 : -1;
+        }
+      }
+    }
+  }
+  return w;
+}
+
+DI int winding_shape(const DevScene &S, int s, v2 pt) {
+  int kind = SI(S, s, DVG_SHAPE_KIND);
+  int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
+  if (kind == DVG_CIRCLE) {
+    v2 c = V2(pget(S, po + 1), pget(S, po + 2));
+    float r = pget(S, po);
+    return distsq2(c, pt) < r * r ? 1 : 0;
+  } else if (kind == DVG_ELLIPSE) {
+    v2 r = V2(pget(S, po), pget(S, po + 1)), c = V2(pget(S, po + 2), pget(S, po + 3));
+    return (sq(c.x - pt.x) / sq(r.x) + sq(c.y - pt.y) / sq(r.y) < 1) ? 1 : 0;
+  } else if (kind == DVG_RECT) {
+    return (pt.x > pget(S, po) && pt.x < pget(S, po + 2) && pt.y > pget(S, po + 1) && pt.y < pget(S, po + 3)) ? 1 : 0;
+  }
+  int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
+  int w = 0;
+  for (int i = 0; i < nseg; i++) {
+    if (nseg > 1 && !box_ray(S.seg_box[so + i], pt)) continue;
+    w += winding_segment(S, po, np, __ldg(&S.segment_ctrl[so + i]), __ldg(&S.seg_point[so + i]), pt);
+  }
+  return w;
+}
+
+struct EdgeQ { int group, shape, hit; };
+
+// is_inside (diffvg.cpp:33-87)
+DI bool group_inside(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
+  v2 lp = xform_pt(S.c2s + 9 * g, pt);
+  if (!box_in(S.g_local_box[g], lp)) return false;
+  int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
+  int eo = GI(S, g, DVG_GROUP_EVEN_ODD);
+  int w = 0;
+  for (int k = 0; k < nsh; k++) {
+    int s = __ldg(&S.group_shapes[off + k]);
+    if (nsh > 1 && !box_in(S.s_box[s], lp)) continue;
+    int ws = winding_shape(S, s, lp);
+    w += ws;
+    if (eq && eq->group == g && eq->shape == s) {
+      if ((eo && abs(ws) % 2 == 1) || (!eo && ws != 0)) eq->hit = 1;
+    }
+  }
+  return eo ? (abs(w) % 2 == 1) : (w != 0);
+}
+
+// ---------------------------------------------------------------------------
+// stroke coverage (within_distance.h:8-446)
+
+// quadratic_closest_pt_approx (vector.h:787-817)
+DI v2 quad_closest_approx(v2 b0, v2 b1, v2 b2, v2 pt, float *t_out) {
+  b0 = sub2(b0, pt); b1 = sub2(b1, pt); b2 = sub2(b2, pt);
+  float a = det2(b0, b2), b = 2 * det2(b1, b0), d = 2 * det2(b2, b1);
+  float f = b * d - a * a;
+  v2 d21 = sub2(b2, b1), d10 = sub2(b1, b0), d20 = sub2(b2, b0);
+  v2 gf = scl2(2, add2(add2(scl2(b, d21), scl2(d, d10)), scl2(a, d20)));
+  gf = V2(gf.y, -gf.x);
+  v2 pp = div2s(scl2(-f, gf), dot2(gf, gf));
+  v2 d0p = sub2(b0, pp);
+  float ap = det2(d0p, d20), bp = 2 * det2(d10, d0p);
+  float t = clampf_((ap + bp) / (2 * a + b + d), 0.f, 1.f);
+  float tt = 1 - t;
+  if (t_out) *t_out = t;
+  return add2(add2(add2(scl2(tt * tt, b0), scl2(2 * tt * t, b1)), scl2(t * t, b2)), pt);
+}
+
+// distance quintic of a cubic segment (within_distance.h:150-167), normalised
+struct Quintic { double A, B, C, D, E, F; };
+DI Quintic cubic_quintic(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
+  v2 a = add2(sub2(add2(neg2(p0), scl2(3, p1)), scl2(3, p2)), p3);
+  v2 b = add2(sub2(scl2(3, p0), scl2(6, p1)), scl2(3, p2));
+  v2 c = add2(scl2(-3, p0), scl2(3, p1));
+  v2 e = sub2(p0, pt);
+  Quintic q;
+  q.A = (double)(3 * sum2(mul2(a, a)));
+  q.B = (double)(5 * sum2(mul2(a, b)));
+  q.C = (double)(4 * sum2(mul2(a, c)) + 2 * sum2(mul2(b, b)));
+  q.D = (double)(3 * (sum2(mul2(b, c)) + sum2(mul2(a, e))));
+  q.E = (double)(sum2(mul2(c, c)) + 2 * sum2(mul2(e, b)));
+  q.F = (double)(sum2(mul2(e, c)));
+  q.B /= q.A; q.C /= q.A; q.D /= q.A; q.E /= q.A; q.F /= q.A;
+  return q;
+}
+DI double quintic_eval(const Quintic &q, double t) {
+  return t * t * t * t * t + q.B * t * t * t * t + q.C * t * t * t + q.D * t * t + q.E * t + q.F;
+}
+DI double quintic_deriv(const Quintic &q, double t) {
+  return 5 * t * t * t * t + 4 * q.B * t * t * t + 3 * q.C * t * t + 2 * q.D * t + q.E;
+}
+// isolator intervals (within_distance.h:181-236); a slot that the reference
+// leaves uninitialised when -B/5 is outside [0,1] holds -1 (skipped).
+DI int quintic_intervals(const Quintic &q, float iv[4]) {
+  double p1A = (2 / 5.f) * q.C - (4 / 25.f) * q.B * q.B;
+  double p1B = (3 / 5.f) * q.D - (3 / 25.f) * q.B * q.C;
+  double p1C = (4 / 5.f) * q.E - (2 / 25.f) * q.B * q.D;
+  double p1D = q.F - q.B * q.E / 25.f;
+  double q_root = -q.B / 5.f;
+  double pr[3];
+  int ns = solve_cubic_d(p1A, p1B, p1C, p1D, pr);
+  iv[0] = (q_root >= 0 && q_root <= 1) ? (float)q_root : -1.0f;
+  for (int j = 0; j < ns; j++) iv[j + 1] = (float)pr[j];
+  int n = 1 + ns;
+  for (int j = 1; j < n; j++)
+    for (int k = j; k > 0 && iv[k - 1] > iv[k]; k--) { float tmp = iv[k]; iv[k] = iv[k - 1]; iv[k - 1] = tmp; }
+  return n;
+}
+// safeguarded Newton / bisection in one bracket (within_distance.h:251-269)
+DI float quintic_root(const Quintic &q, float lb, float ub) {
+  float t = 0.5f * (lb + ub);
+  for (int it = 0; it < 20; it++) {
+    if (!(t >= lb && t <= ub)) t = 0.5f * (lb + ub);
+    double value = quintic_eval(q, t);
+    if (fabs(value) < 1e-5f || it == 19) break;
+    if (value > 0.f) ub = t; else lb = t;
+    double derivative = quintic_deriv(q, t);
+    t = (float)(t - value / derivative);
+  }
+  return t;
+}
+
+// 1: within, 0: not, -1: the path reports "not within" (approx quadratics)
+DI int within_segment(const DevScene &S, int s, int po, int np, int th, int flags, int nc, int i0, v2 pt, float r) {
+  if (nc == 0) {
+    int i1 = (i0 + 1) % np;
+    v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1);
+    float t = dot2(sub2(pt, p0), sub2(p1, p0)) / dot2(sub2(p1, p0), sub2(p1, p0));
+    float r0 = r, r1 = r;
+    if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); }
+    if (t < 0) return distsq2(p0, pt) < r0 * r0 ? 1 : 0;
+    if (t > 1) return distsq2(p1, pt) < r1 * r1 ? 1 : 0;
+    float rr = r0 + t * (r1 - r0);
+    return distsq2(add2(p0, scl2(t, sub2(p1, p0))), pt) < rr * rr ? 1 : 0;
+  } else if (nc == 1) {
+    int i1 = i0 + 1, i2 = (i0 + 2) % np;
+    v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2);
+    if (flags & 2) {
+      v2 cp = quad_closest_approx(p0, p1, p2, pt, nullptr);
+      return distsq2(cp, pt) < r * r ? 1 : -1;
+    }
+    float r0 = r, r1 = r, r2 = r;
+    if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); }
+    if (distsq2(eval_quad(p0, p1, p2, 0), pt) < r0 * r0) return 1;
+    if (distsq2(eval_quad(p0, p1, p2, 1), pt) < r2 * r2) return 1;
+    v2 v = add2(sub2(p0, scl2(2, p1)), p2), w = add2(neg2(p0), p1);
+    float A = sum2(mul2(v, v));
+    float B = sum2(mul2(scl2(3, v), w));
+    float C = sum2(add2(mul2(scl2(2, w), w), mul2(v, sub2(p0, pt))));
+    float D = sum2(mul2(w, sub2(p0, pt)));
+    float t[3];
+    int n = solve_cubic_f(A, B, C, D, t);
+    for (int j = 0; j < n; j++) {
+      if (t[j] >= 0 && t[j] <= 1) {
+        float tt = 1 - t[j];
+        float rr = (tt * tt) * r0 + (2 * tt * t[j]) * r1 + (t[j] * t[j]) * r2;
+        if (distsq2(eval_quad(p0, p1, p2, t[j]), pt) < rr * rr) return 1;
+      }
+    }
+    return 0;
+  }
+  int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
+  v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2), p3 = path_pt(S, po, i3);
+  float r0 = r, r1 = r, r2 = r, r3 = r;
+  if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); r3 = pget(S, th + i3); }
+  if (distsq2(eval_cubic(p0, p1, p2, p3, 0), pt) < r0 * r0) return 1;
+  if (distsq2(eval_cubic(p0, p1, p2, p3, 1), pt) < r3 * r3) return 1;
+  Quintic q = cubic_quintic(p0, p1, p2, p3, pt);
+  float iv[4];
+  int ni = quintic_intervals(q, iv);
+  float lower = 0.f;
+  for (int j = 0; j < ni + 1; j++) {
+    if (j < ni && iv[j] < 0.f) continue;
+    float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
+    float lb = lower, ub = upper;
+    double lbe = quintic_eval(q, lb), ube = quintic_eval(q, ub);
+    if (lbe * ube > 0) continue;
+    if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
+    float t = quintic_root(q, lb, ub);
+    float tt = 1 - t;
+    float rr = (tt * tt * tt) * r0 + (3 * tt * tt * t) * r1 + (3 * tt * t * t) * r2 + (t * t * t) * r3;
+    if (distsq2(eval_cubic(p0, p1, p2, p3, t), pt) < rr * rr) return 1;
+    if (upper >= 1.f) break;
+    lower = upper;
+  }
+  return 0;
+}
+
+DI bool within_shape(const DevScene &S, int s, v2 pt, float r) {
+  int kind = SI(S, s, DVG_SHAPE_KIND);
+  int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
+  if (kind == DVG_CIRCLE) {
+    float dc = dist2(V2(pget(S, po + 1), pget(S, po + 2)), pt);
+    return fabsf(dc - pget(S, po)) < r;
+  } else if (kind == DVG_ELLIPSE) {
+    flag_error(S, DVG_EFLAG_UNSUPPORTED);  // within_distance.h:343-345 asserts
+    return false;
+  } else if (kind == DVG_RECT) {
+    v2 lt = V2(pget(S, po), pget(S, po + 1)), rt = V2(pget(S, po + 2), pget(S, po + 1));
+    v2 lb = V2(pget(S, po), pget(S, po + 3)), rb = V2(pget(S, po + 2), pget(S, po + 3));
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      v2 a = k == 0 ? lt : (k == 1 ? lt : (k == 2 ? rt : lb));
+      v2 b = k == 0 ? lb : (k == 1 ? rt : rb);
+      float t = dot2(sub2(pt, a), sub2(b, a)) / dot2(sub2(b, a), sub2(b, a));
+      if (t < 0) { if (distsq2(a, pt) < r * r) return true; }
+      else if (t > 1) { if (distsq2(b, pt) < r * r) return true; }
+      else { if (distsq2(add2(a, scl2(t, sub2(b, a))), pt) < r * r) return true; }
+    }
+    return false;
+  }
+  int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF);
+  int np = SI(S, s, DVG_SHAPE_NUM_POINTS), th = SI(S, s, DVG_SHAPE_THICKNESS_OFF), flags = SI(S, s, DVG_SHAPE_FLAGS);
+  for (int k = 0; k < nseg; k++) {
+    int seg = S.seg_order[so + k];
+    if (nseg > 1 && !box_in_r(S.seg_box[so + seg], pt, S.seg_r[so + seg])) continue;
+    int h = within_segment(S, s, po, np, th, flags, __ldg(&S.segment_ctrl[so + seg]), __ldg(&S.seg_point[so + seg]),
+                           pt, r);
+    if (h == 1) return true;
+    if (h == -1) return false;
+  }
+  return false;
+}
+
+// within_distance(scene, group, pt, edge_query) (within_distance.h:355-446)
+DI bool group_stroke(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
+  v2 lp = xform_pt(S.c2s + 9 * g, pt);
+  int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
+  bool ret = false;
+  for (int k = 0; k < nsh; k++) {
+    int s = __ldg(&S.group_shapes[off + k]);
+    float r = stroke_width(S, s);
+    if (nsh > 1 && !box_in_r(S.s_box[s], lp, r)) continue;
+    if (within_shape(S, s, lp, r)) {
+      if (!eq || eq->group != g) return true;
+      ret = true;
+      if (s == eq->shape) eq->hit = 1;
+    }
+  }
+  return ret;
+}
+
+// ---------------------------------------------------------------------------
+// closest point / distance (compute_distance.h:12-439)
+struct PathInfo { int base_point_id, point_id; float t_root; };
+
+DI bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
+  int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
+  int po = SI(S, s, DVG_SHAPE_PARAM_OFF), flags = SI(S, s, DVG_SHAPE_FLAGS);
+  float min_dist = max_radius;
+  v2 ret = V2(0, 0);
+  bool found = false;
+  for (int k = 0; k < nseg; k++) {
+    int seg = S.seg_order[so + k];
+    if (nseg > 1 && !box_in_r(S.seg_box[so + seg], pt, min_dist)) continue;
+    int nc = __ldg(&S.segment_ctrl[so + seg]), i0 = __ldg(&S.seg_point[so + seg]);
+    float dist = 0.f, t_root = 0.f;
+    v2 cp = V2(0, 0);
+    if (nc == 0) {
+      v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, (i0 + 1) % np);
+      float t = dot2(sub2(pt, p0), sub2(p1, p0)) / dot2(sub2(p1, p0), sub2(p1, p0));
+      if (t < 0) { dist = dist2(p0, pt); cp = p0; t_root = 0; }
+      else if (t > 1) { dist = dist2(p1, pt); cp = p1; t_root = 1; }
+      else {
+        dist = dist2(add2(p0, scl2(t, sub2(p1, p0))), pt);
+        cp = add2(p0, scl2(t, sub2(p1, p0)));
+        t_root = t;
+      }
+    } else if (nc == 1) {
+      v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, (i0 + 2) % np);
+      if (flags & 2) {
+        cp = quad_closest_approx(p0, p1, p2, pt, &t_root);
+        dist = dist2(cp, pt);
+      } else {
+        v2 pt0 = eval_quad(p0, p1, p2, 0), pt1 = eval_quad(p0, p1, p2, 1);
+        float d0 = dist2(pt0, pt), d1 = dist2(pt1, pt);
+        dist = d0; cp = pt0; t_root = 0;
+        if (d1 < dist) { dist = d1; cp = pt1; t_root = 1; }
+        v2 v = add2(sub2(p0, scl2(2, p1)), p2), w = add2(neg2(p0), p1);
+        float A = sum2(mul2(v, v));
+        float B = sum2(mul2(scl2(3, v), w));
+        float C = sum2(add2(mul2(scl2(2, w), w), mul2(v, sub2(p0, pt))));
+        float D = sum2(mul2(w, sub2(p0, pt)));
+        float t[3];
+        int n = solve_cubic_f(A, B, C, D, t);
+        for (int j = 0; j < n; j++) {
+          if (t[j] >= 0 && t[j] <= 1) {
+            v2 p = eval_quad(p0, p1, p2, t[j]);
+            float dp = dist2(p, pt);
+            if (dp < dist) { dist = dp; cp = p; t_root = t[j]; }
+          }
+        }
+      }
+    } else {
+      v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, i0 + 2),
+         p3 = path_pt(S, po, (i0 + 3) % np);
+      v2 pt0 = eval_cubic(p0, p1, p2, p3, 0), pt1 = eval_cubic(p0, p1, p2, p3, 1);
+      float d0 = dist2(pt0, pt), d1 = dist2(pt1, pt);
+      dist = d0; cp = pt0; t_root = 0;
+      if (d1 < dist) { dist = d1; cp = pt1; t_root = 1; }
+      Quintic q = cubic_quintic(p0, p1, p2, p3, pt);
+      float iv[4];
+      int ni = quintic_intervals(q, iv);
+      float lower = 0.f;
+      for (int j = 0; j < ni + 1; j++) {
+        if (j < ni && iv[j] < 0.f) continue;
+        float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
+        float lb = lower, ub = upper;
+        double lbe = quintic_eval(q, lb), ube = quintic_eval(q, ub);
+        if (lbe * ube > 0) continue;
+        if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
+        float t = quintic_root(q, lb, ub);
+        v2 p = eval_cubic(p0, p1, p2, p3, t);
+        float dp = dist2(p, pt);
+        if (dp < dist) { dist = dp; cp = p; t_root = t; }
+        if (upper >= 1.f) break;
+        lower = upper;
+      }
+    }
+    if (dist < min_dist) {
+      min_dist = dist;
+      ret = cp;
+      info->base_point_id = seg;
+      info->point_id = i0;
+      info->t_root = t_root;
+      found = true;
+    }
+  }
+  *result = ret;
+  return found;
+}
+
+DI bool closest_shape(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
+  int kind = SI(S, s, DVG_SHAPE_KIND);
+  int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
+  if (kind == DVG_CIRCLE) {
+    // compute_distance.h:18-24 computes the point but reports "not found"
+    v2 c = V2(pget(S, po + 1), pget(S, po + 2));
+    *result = add2(c, scl2(pget(S, po), normalize2(sub2(pt, c))));
+    return false;
+  } else if (kind == DVG_ELLIPSE) {
+    flag_error(S, DVG_EFLAG_UNSUPPORTED);  // compute_distance.h:362-365 asserts
+    return false;
+  } else if (kind == DVG_RECT) {
+    v2 lt = V2(pget(S, po), pget(S, po + 1)), rt = V2(pget(S, po + 2), pget(S, po + 1));
+    v2 lb = V2(pget(S, po), pget(S, po + 3)), rb = V2(pget(S, po + 2), pget(S, po + 3));
+    float min_dist = 0.f;
+    v2 cp = V2(0, 0);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      v2 a = k == 0 ? lt : (k == 1 ? lt : (k == 2 ? rt : lb));
+      v2 b = k == 0 ? lb : (k == 1 ? rt : rb);
+      bool first = (k == 0);
+      float t = dot2(sub2(pt, a), sub2(b, a)) / dot2(sub2(b, a), sub2(b, a));
+      if (t < 0) { float dd = dist2(a, pt); if (first || dd < min_dist) { min_dist = dd; cp = a; } }
+      else if (t > 1) { float dd = dist2(b, pt); if (first || dd < min_dist) { min_dist = dd; cp = b; } }
+      else {
+        // compute_distance.h:333-338 stores p0, not the projection
+        float dd = dist2(add2(a, scl2(t, sub2(b, a))), pt);
+        if (first || dd < min_dist) { min_dist = dd; cp = a; }
+      }
+    }
+    *result = cp;
+    return true;
+  }
+  return closest_path(S, s, pt, max_radius, info, result);
+}
+
+// compute_distance (compute_distance.h:373-439)
+DI bool group_distance(const DevScene &S, int g, v2 pt, float max_radius, int *min_shape, v2 *closest,
+                       PathInfo *info, float *result) {
+  v2 lp = xform_pt(S.c2s + 9 * g, pt);
+  const float *s2c = S.P + GI(S, g, DVG_GROUP_XFORM_OFF);
+  int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
+  float min_dist = max_radius;
+  bool found = false;
+  for (int k = 0; k < nsh; k++) {
+    int s = __ldg(&S.group_shapes[off + k]);
+    if (nsh > 1 && !box_in_r(S.s_box[s], lp, max_radius)) continue;
+    PathInfo li;
+    li.base_point_id = -1; li.point_id = -1; li.t_root = 0;
+    v2 lcp = V2(0, 0);
+    if (closest_shape(S, s, lp, max_radius, &li, &lcp)) {
+      v2 cp = xform_pt(s2c, lcp);
+      float dist = dist2(cp, pt);
+      if (!found || dist < min_dist) {
+        found = true;
+        min_dist = dist;
+        if (min_shape) *min_shape = s;
+        if (closest) *closest = cp;
+        if (info) *info = li;
+      }
+    }
+  }
+  *result = min_dist;
+  return found;
+}
+
+// ---------------------------------------------------------------------------
+// paint (diffvg.cpp:276-368)
+DI float4 stop_color(const DevScene &S, int co, int i) {
+  return F4(pget(S, co + 4 * i), pget(S, co + 4 * i + 1), pget(S, co + 4 * i + 2), pget(S, co + 4 * i + 3));
+}
+DI float4 paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt) {
+  if (kind == DVG_CONSTANT) return F4(pget(S, off), pget(S, off + 1), pget(S, off + 2), pget(S, off + 3));
+  float t;
+  if (kind == DVG_LINEAR) {
+    v2 beg = V2(pget(S, off), pget(S, off + 1)), end = V2(pget(S, off + 2), pget(S, off + 3));
+    t = dot2(sub2(pt, beg), sub2(end, beg)) / rmax(dot2(sub2(end, beg), sub2(end, beg)), 1e-3f);
+  } else {
+    v2 cen = V2(pget(S, off), pget(S, off + 1)), rad = V2(pget(S, off + 2), pget(S, off + 3));
+    v2 o = sub2(pt, cen);
+    v2 no = V2(o.x / rad.x, o.y / rad.y);
+    t = len2(no);
+  }
+  int oo = off + 4, co = off + 4 + nstops;
+  if (t < pget(S, oo)) return stop_color(S, co, 0);
+  for (int i = 0; i < nstops - 1; i++) {
+    float oc = pget(S, oo + i), on = pget(S, oo + i + 1);
+    if (t >= oc && t < on) {
+      float4 cc = stop_color(S, co, i), cn = stop_color(S, co, i + 1);
+      float tt = (t - oc) / (on - oc);
+      return add4(scl4(1 - tt, cc), scl4(tt, cn));
+    }
+  }
+  return stop_color(S, co, nstops - 1);
+}
+
+DI void gadd(float *dp, int off, float v) { atomicAdd(dp + off, v); }
+
+// d_sample_color (diffvg.cpp:370-504)
+DI void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, float4 d_color, float *dp,
+                      float *d_translation) {
+  if (kind == DVG_CONSTANT) {
+    gadd(dp, off + 0, d_color.x); gadd(dp, off + 1, d_color.y);
+    gadd(dp, off + 2, d_color.z); gadd(dp, off + 3, d_color.w);
+    return;
+  }
+  int oo = off + 4, co = off + 4 + nstops;
+  float t;
+  v2 beg = V2(0, 0), end = V2(0, 0), cen = V2(0, 0), rad = V2(0, 0), no = V2(0, 0), o2 = V2(0, 0);
+  if (kind == DVG_LINEAR) {
+    beg = V2(pget(S, off), pget(S, off + 1)); end = V2(pget(S, off + 2), pget(S, off + 3));
+    t = dot2(sub2(pt, beg), sub2(end, beg)) / rmax(dot2(sub2(end, beg), sub2(end, beg)), 1e-3f);
+  } else {
+    cen = V2(pget(S, off), pget(S, off + 1)); rad = V2(pget(S, off + 2), pget(S, off + 3));
+    o2 = sub2(pt, cen);
+    no = V2(o2.x / rad.x, o2.y / rad.y);
+    t = len2(no);
+  }
+  if (t < pget(S, oo)) {
+    gadd(dp, co + 0, d_color.x); gadd(dp, co + 1, d_color.y); gadd(dp, co + 2, d_color.z); gadd(dp, co + 3, d_color.w);
+    return;
+  }
+  for (int i = 0; i < nstops - 1; i++) {
+    float oc = pget(S, oo + i), on = pget(S, oo + i + 1);
+    if (t >= oc && t < on) {
+      float4 cc = stop_color(S, co, i), cn = stop_color(S, co, i + 1);
+      float tt = (t - oc) / (on - oc);
+      float4 dcc = scl4(1 - tt, d_color), dcn = scl4(tt, d_color);
+      float4 diff = sub4(cn, cc);
+      float d_tt = d_color.x * diff.x + d_color.y * diff.y + d_color.z * diff.z + d_color.w * diff.w;
+      float d_on = -d_tt * tt / (on - oc);
+      float d_oc = d_tt * ((tt - 1.f) / (on - oc));
+      float d_t = d_tt / (on - oc);
+      gadd(dp, co + 4 * i + 0, dcc.x); gadd(dp, co + 4 * i + 1, dcc.y);
+      gadd(dp, co + 4 * i + 2, dcc.z); gadd(dp, co + 4 * i + 3, dcc.w);
+      gadd(dp, co + 4 * (i + 1) + 0, dcn.x); gadd(dp, co + 4 * (i + 1) + 1, dcn.y);
+      gadd(dp, co + 4 * (i + 1) + 2, dcn.z); gadd(dp, co + 4 * (i + 1) + 3, dcn.w);
+      gadd(dp, oo + i, d_oc); gadd(dp, oo + i + 1, d_on);
+      if (kind == DVG_LINEAR) {
+        float l = rmax(dot2(sub2(end, beg), sub2(end, beg)), 1e-3f);
+        v2 d_beg = div2s(scl2(d_t, sub2(neg2(sub2(pt, beg)), sub2(end, beg))), l);
+        v2 d_end = div2s(scl2(d_t, sub2(pt, beg)), l);
+        float d_l = -d_t * t / l;
+        if (dot2(sub2(end, beg), sub2(end, beg)) > 1e-3f) {
+          d_beg = add2(d_beg, scl2(2 * d_l, sub2(beg, end)));
+          d_end = add2(d_end, scl2(2 * d_l, sub2(end, beg)));
+        }
+        gadd(dp, off + 0, d_beg.x); gadd(dp, off + 1, d_beg.y); gadd(dp, off + 2, d_end.x); gadd(dp, off + 3, d_end.y);
+        if (d_translation) {
+          atomicAdd(d_translation + 0, d_beg.x + d_end.x);
+          atomicAdd(d_translation + 1, d_beg.y + d_end.y);
+        }
+        return;
+      } else {
+        float l = sqrtf(lensq2(no));
+        float d_l_sq = 0.5f * d_t / l;
+        v2 d_no = scl2(2 * d_l_sq, no);
+        v2 d_off = V2(d_no.x / rad.x, d_no.y / rad.y);
+        v2 d_rad = V2(-d_no.x * o2.x / (rad.x * rad.x), -d_no.y * o2.y / (rad.y * rad.y));
+        v2 d_cen = neg2(d_off);
+        gadd(dp, off + 0, d_cen.x); gadd(dp, off + 1, d_cen.y); gadd(dp, off + 2, d_rad.x); gadd(dp, off + 3, d_rad.y);
+        if (d_translation) {
+          atomicAdd(d_translation + 0, d_cen.x);
+          atomicAdd(d_translation + 1, d_cen.y);
+        }
+        // diffvg.cpp:491-498: no return, the last stop also receives d_color
+      }
+    }
+  }
+  int last = co + 4 * (nstops - 1);
+  gadd(dp, last + 0, d_color.x); gadd(dp, last + 1, d_color.y); gadd(dp, last + 2, d_color.z); gadd(dp, last + 3, d_color.w);
+}
+
+// d_length / d_normalize (vector.h:496-503, 591-601)
+DI v2 d_length2(v2 v, float d_l) {
+  float l = sqrtf(lensq2(v));
+  float d_l_sq = 0.5f * d_l / l;
+  return scl2(2 * d_l_sq, v);
+}
+DI v2 d_normalize2(v2 v, v2 d_n) {
+  float l = len2(v);
+  v2 n = div2s(v, l);
+  v2 dv = div2s(d_n, l);
+  float d_l = -dot2(d_n, n) / l;
+  return add2(dv, d_length2(v, d_l));
+}

@@ -1,0 +1,35 @@
+// Host-side launchers shared by the translation units of libdiffvg_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dvg_device.cuh"
+
+namespace dvg {
+
+// Scene preparation from the parameter arena: transforms, boxes, segment
+// order, boundary CDFs and the per-tile candidate group lists.
+// tile_cap is the capacity of S.tile_list; bin_total receives the list
+// length.  On overflow the lists are emptied and DVG_EFLAG_BIN_OVERFLOW is
+// raised in S.err.
+cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4 *g_tile_range, int *tile_count,
+                           cudaStream_t st);
+
+// One launcher per render kernel; the C ABI sequences them (and can record
+// CUDA events between them for per-kernel timing).
+void launch_weight(const DevScene &S, const DevRender &R, cudaStream_t st);
+void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, cudaStream_t st);
+void launch_resolve(const DevRender &R, const float4 *samples, float *image, cudaStream_t st);
+// dbg_val / dbg_flag: per-sample background adjoint scratch (only written
+// when R.d_background is set).
+void launch_sample_bwd(const DevScene &S, const DevRender &R, float4 *dbg_val, int *dbg_flag, cudaStream_t st);
+void launch_bg_combine(const DevScene &S, const DevRender &R, const float4 *dbg_val, const int *dbg_flag,
+                       cudaStream_t st);
+void launch_edge(const DevScene &S, const DevRender &R, cudaStream_t st);
+// Signed distance output (forward: sdf, backward: d_sdf).
+void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
+                const float *d_sdf, cudaStream_t st);
+
+}  // namespace dvg
+
+#define DVG_EFLAG_BIN_OVERFLOW 0x100u

@@ -1,0 +1,351 @@
+// Scene preparation kernels of the GB300 render path.
+//
+// The reference rebuilds its scene on the host on every call
+// (scene.cpp:919-998: boxes, per-path segment BVHs, group BVHs, length
+// CDFs).  Here the topology stays resident on the device and everything
+// that depends on the parameter values is derived by these kernels from the
+// parameter arena, so an optimisation step never leaves the GPU:
+//   k_group_xform   canvas_to_shape = inverse(shape_to_canvas)   (shape.h:123)
+//   k_shape_prep    shape / segment boxes and stroke radii, the per-path
+//                   segment visiting order, boundary lengths and per-path
+//                   segment CDFs (scene.cpp:113-333, 495-625)
+//   k_group_prep    group boxes, max stroke radius, tile range (scene.cpp:627-684)
+//   k_sampling_cdf  the (group, shape) boundary-length CDF (scene.cpp:207-246)
+//   k_bin_count / k_bin_scan / k_bin_fill
+//                   per-16x16-tile candidate group lists in ascending group
+//                   id, replacing the reference's top-level group BVH.
+#include "dvg_internal.h"
+
+namespace dvg {
+
+__global__ void k_group_xform(DevScene S) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= S.num_groups) return;
+  float m[9], r[9];
+  int xo = GI(S, g, DVG_GROUP_XFORM_OFF);
+  for (int i = 0; i < 9; i++) m[i] = S.P[xo + i];
+  inverse3(m, r);
+  for (int i = 0; i < 9; i++) S.c2s[9 * g + i] = r[i];
+}
+
+// Stable bottom-up merge sort of idx[0..n) by key[idx] (ties keep index order).
+__device__ void sort_by_key_stable(int *idx, int *tmp, const float *key, int n) {
+  for (int width = 1; width < n; width *= 2) {
+    for (int lo = 0; lo < n; lo += 2 * width) {
+      int mid = min(lo + width, n), hi = min(lo + 2 * width, n);
+      int a = lo, b = mid, o = lo;
+      while (a < mid && b < hi) {
+        if (key[idx[b]] < key[idx[a]]) tmp[o++] = idx[b++];
+        else tmp[o++] = idx[a++];
+      }
+      while (a < mid) tmp[o++] = idx[a++];
+      while (b < hi) tmp[o++] = idx[b++];
+    }
+    for (int i = 0; i < n; i++) idx[i] = tmp[i];
+  }
+}
+
+// Visiting order of a path's segments: segments sorted by box y-centre and
+// paired bottom-up into a binary tree (scene.cpp:439-494, 602-620), leaves
+// visited depth-first with child1 before child0 (the stack discipline of
+// winding_number.h:44-172).  scratch holds 10*n + 8 ints.
+__device__ void path_leaf_order(const float4 *boxes, int n, int *out, int *scratch) {
+  int *idx = scratch;
+  float *key = reinterpret_cast<float *>(scratch + n);
+  int *tmp = scratch + 2 * n;
+  int *c0 = scratch + 3 * n;
+  int *c1 = scratch + 5 * n;
+  int *stack = scratch + 7 * n;
+  for (int i = 0; i < n; i++) { idx[i] = i; key[i] = 0.5f * (boxes[i].y + boxes[i].w); }
+  sort_by_key_stable(idx, tmp, key, n);
+  if (n == 1) { out[0] = idx[0]; return; }
+  int size = 2 * n - 1;
+  for (int i = 0; i < size; i++) { c0[i] = -1; c1[i] = -1; }
+  int prev_beg = 0, prev_end = n;
+  int leftover = prev_end % 2 == 0 ? -1 : prev_end - 1;
+  while (prev_end - prev_beg >= 1 || leftover != -1) {
+    int length = (prev_end - prev_beg) / 2;
+    if ((prev_end - prev_beg) % 2 == 1 && leftover != -1 && leftover != prev_end - 1) length += 1;
+    for (int i = 0; i < length; i++) {
+      int a = prev_beg + 2 * i, b = prev_beg + 2 * i + 1;
+      if (b >= prev_end) { b = leftover; leftover = -1; }
+      c0[prev_end + i] = a;
+      c1[prev_end + i] = b;
+    }
+    if (length == 1 && leftover == -1) break;
+    prev_beg = prev_end;
+    prev_end = prev_beg + length;
+    if (length % 2 == 1 && leftover == -1) leftover = prev_end - 1;
+  }
+  int sp = 0, k = 0;
+  stack[sp++] = size - 1;
+  while (sp > 0 && k < n) {
+    int node = stack[--sp];
+    if (node < n) { out[k++] = idx[node]; continue; }
+    if (sp + 2 > 3 * n) break;  // cannot happen for a tree of 2n-1 nodes
+    stack[sp++] = c0[node];
+    stack[sp++] = c1[node];
+  }
+}
+
+__global__ void k_shape_prep(DevScene S) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S.num_shapes) return;
+  int kind = SI(S, s, DVG_SHAPE_KIND);
+  int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
+  const float *p = S.P + po;
+  float L = 0.f;
+  if (kind == DVG_CIRCLE) {
+    float r = p[0];
+    v2 c = V2(p[1], p[2]);
+    S.s_box[s] = F4(c.x - r, c.y - r, c.x + r, c.y + r);
+    L += (float)(2.f * DVG_PI) * r;
+  } else if (kind == DVG_ELLIPSE) {
+    v2 r = V2(p[0], p[1]), c = V2(p[2], p[3]);
+    S.s_box[s] = F4(c.x - r.x, c.y - r.y, c.x + r.x, c.y + r.y);
+    float a = r.x, b = r.y;
+    L += (float)((float)DVG_PI * (3 * (a + b) - sqrt((double)((3 * a + b) * (a + 3 * b)))));
+  } else if (kind == DVG_RECT) {
+    S.s_box[s] = F4(p[0], p[1], p[2], p[3]);
+    L += 2 * (p[2] - p[0] + p[3] - p[1]);
+  } else {
+    int np = SI(S, s, DVG_SHAPE_NUM_POINTS), nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);
+    int so = SI(S, s, DVG_SHAPE_SEG_OFF), th = SI(S, s, DVG_SHAPE_THICKNESS_OFF);
+    float4 b = box_empty();
+    if (np > 0) { v2 q = path_pt(S, po, 0); b = F4(q.x, q.y, q.x, q.y); }
+    for (int i = 1; i < np; i++) b = box_add(b, path_pt(S, po, i));
+    S.s_box[s] = b;
+    float r = stroke_width(S, s);
+    for (int i = 0; i < nseg; i++) {
+      int nc = S.segment_ctrl[so + i], pid = S.seg_point[so + i];
+      float4 sb = box_empty();
+      float rr = r;
+      for (int k = 0; k <= nc + 1; k++) {
+        int id = (k == nc + 1) ? (pid + k) % np : pid + k;
+        sb = box_add(sb, path_pt(S, po, id));
+        if (th >= 0) {
+          float rk = S.P[th + id];
+          rr = (k == 0) ? rk : rmax(rr, rk);
+        }
+      }
+      S.seg_box[so + i] = sb;
+      S.seg_r[so + i] = rr;
+    }
+    if (nseg > 0) path_leaf_order(S.seg_box + so, nseg, S.seg_order + so, S.scratch + 10 * so + 8 * s);
+    float len = 0.f;
+    for (int i = 0; i < nseg; i++) {
+      int nc = S.segment_ctrl[so + i], i0 = S.seg_point[so + i];
+      if (nc == 0) {
+        len += dist2(path_pt(S, po, (i0 + 1) % np), path_pt(S, po, i0));
+      } else if (nc == 1) {
+        v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, (i0 + 2) % np);
+        v2 v1 = eval_quad(p0, p1, p2, 0.5f);
+        len += dist2(v1, p0) + dist2(v1, p2);
+      } else {
+        v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, i0 + 2),
+           p3 = path_pt(S, po, (i0 + 3) % np);
+        v2 v1 = eval_cubic(p0, p1, p2, p3, 1.f / 3.f), v2_ = eval_cubic(p0, p1, p2, p3, 2.f / 3.f);
+        len += dist2(v1, p0) + dist2(v1, v2_) + dist2(v2_, p3);
+      }
+    }
+    L += len;
+    float inv = 1.f / L;
+    float cdf = 0.f;
+    for (int i = 0; i < nseg; i++) {
+      int nc = S.segment_ctrl[so + i], i0 = S.seg_point[so + i];
+      float dd;
+      if (nc == 0) {
+        dd = dist2(path_pt(S, po, i0), path_pt(S, po, (i0 + 1) % np)) * inv;
+      } else if (nc == 1) {
+        v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, (i0 + 2) % np);
+        v2 v1 = eval_quad(p0, p1, p2, 0.5f);
+        dd = (dist2(p0, v1) + dist2(v1, p2)) * inv;
+      } else {
+        v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, i0 + 2),
+           p3 = path_pt(S, po, (i0 + 3) % np);
+        v2 v1 = eval_cubic(p0, p1, p2, p3, 1.f / 3.f), v2_ = eval_cubic(p0, p1, p2, p3, 2.f / 3.f);
+        dd = (dist2(v1, p0) + dist2(v1, v2_) + dist2(v2_, p3)) * inv;
+      }
+      S.seg_pmf[so + i] = dd;
+      cdf = (i == 0) ? dd : dd + cdf;
+      S.seg_cdf[so + i] = cdf;
+    }
+  }
+  S.s_length[s] = L;
+}
+
+__device__ __forceinline__ int clamp_tile(double f, int hi, bool lower) {
+  // clamps a floored tile coordinate to the grid (first / last tile)
+  if (lower) return f < 0 ? 0 : (f > hi - 1 ? hi : (int)f);
+  return f > hi - 1 ? hi - 1 : (f < 0 ? -1 : (int)f);
+}
+
+__global__ void k_group_prep(DevScene S, int4 *g_tile_range) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= S.num_groups) return;
+  int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
+  float4 b = box_empty();
+  float max_r = 0.f;
+  for (int k = 0; k < nsh; k++) {
+    int s = S.group_shapes[off + k];
+    b = (k == 0) ? S.s_box[s] : box_union(b, S.s_box[s]);
+    float r = stroke_width(S, s);
+    if (SI(S, s, DVG_SHAPE_KIND) == DVG_PATH && SI(S, s, DVG_SHAPE_THICKNESS_OFF) >= 0 &&
+        SI(S, s, DVG_SHAPE_NUM_SEGMENTS) > 0) {
+      // the reference reads node 0 of the path BVH: the leaf with the lowest y-centre
+      int so = SI(S, s, DVG_SHAPE_SEG_OFF), nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);
+      int best = 0;
+      float bk = 0.5f * (S.seg_box[so].y + S.seg_box[so].w);
+      for (int i = 1; i < nseg; i++) {
+        float ki = 0.5f * (S.seg_box[so + i].y + S.seg_box[so + i].w);
+        if (ki < bk) { bk = ki; best = i; }
+      }
+      r = S.seg_r[so + best];
+    }
+    max_r = (k == 0) ? r : (max_r < r ? r : max_r);
+  }
+  S.g_local_box[g] = b;
+  const float *m = S.P + GI(S, g, DVG_GROUP_XFORM_OFF);
+  float mm[9];
+  for (int i = 0; i < 9; i++) mm[i] = m[i];
+  float4 cb = box_empty();
+  cb = box_add(cb, xform_pt(mm, V2(b.x, b.y)));
+  cb = box_add(cb, xform_pt(mm, V2(b.x, b.w)));
+  cb = box_add(cb, xform_pt(mm, V2(b.z, b.y)));
+  cb = box_add(cb, xform_pt(mm, V2(b.z, b.w)));
+  S.g_canvas_box[g] = cb;
+  float r = GI(S, g, DVG_GROUP_STROKE_KIND) == DVG_PAINT_NONE ? 0.f : max_r;
+  S.g_max_radius[g] = r;
+  // tiles touched by the box grown by the stroke radius and one pixel
+  int4 tr;
+  if (S.num_groups == 1) {
+    tr = make_int4(0, S.tiles_x - 1, 0, S.tiles_y - 1);
+  } else {
+    double fx0 = floor(((double)cb.x - r - 1.0) / DVG_TILE), fx1 = floor(((double)cb.z + r + 1.0) / DVG_TILE);
+    double fy0 = floor(((double)cb.y - r - 1.0) / DVG_TILE), fy1 = floor(((double)cb.w + r + 1.0) / DVG_TILE);
+    if (!(fx0 <= fx1) || !(fy0 <= fy1)) {
+      tr = make_int4(1, 0, 1, 0);
+    } else {
+      tr = make_int4(clamp_tile(fx0, S.tiles_x, true), clamp_tile(fx1, S.tiles_x, false),
+                     clamp_tile(fy0, S.tiles_y, true), clamp_tile(fy1, S.tiles_y, false));
+    }
+  }
+  g_tile_range[g] = tr;
+}
+
+// Boundary-length CDF over (group, shape) pairs in group order, normalised
+// (scene.cpp:207-246).  One thread: the running sum keeps the reference's
+// summation order.
+__global__ void k_sampling_cdf(DevScene S) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int nt = S.num_total;
+  float cdf = 0.f;
+  for (int k = 0; k < nt; k++) {
+    float len = S.s_length[S.smp_shape[k]];
+    cdf = (k == 0) ? len : len + cdf;
+    S.smp_cdf[k] = cdf;
+    S.smp_pmf[k] = len;
+  }
+  if (nt > 0) {
+    float norm = cdf;
+    if (norm <= 0) { atomicOr(S.err, DVG_EFLAG_SCENE_ZERO); return; }
+    if (!isfinite(norm)) { atomicOr(S.err, DVG_EFLAG_SCENE_NAN); return; }
+    for (int i = 0; i < nt; i++) { S.smp_cdf[i] /= norm; S.smp_pmf[i] /= norm; }
+  }
+}
+
+__device__ __forceinline__ bool tile_hit(int4 r, int tx, int ty) {
+  return tx >= r.x && tx <= r.y && ty >= r.z && ty <= r.w;
+}
+
+// one block per tile: number of candidate groups
+__global__ void k_bin_count(DevScene S, const int4 *g_tile_range, int *tile_count) {
+  int t = blockIdx.x;
+  int tx = t % S.tiles_x, ty = t / S.tiles_x;
+  int c = 0;
+  for (int g = threadIdx.x; g < S.num_groups; g += blockDim.x) c += tile_hit(g_tile_range[g], tx, ty) ? 1 : 0;
+  __shared__ int red[32];
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int sum = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) sum += red[w];
+    tile_count[t] = sum;
+  }
+}
+
+// exclusive scan of the tile counts (one block of 1024 threads)
+__global__ void k_bin_scan(DevScene S, const int *tile_count, int tile_cap, int *bin_total) {
+  int T = S.tiles_x * S.tiles_y;
+  __shared__ int part[1024];
+  int per = (T + blockDim.x - 1) / blockDim.x;
+  int lo = threadIdx.x * per, hi = min(lo + per, T);
+  int sum = 0;
+  for (int i = lo; i < hi; i++) sum += tile_count[i];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+    int v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int total = part[blockDim.x - 1];
+  bool overflow = total > tile_cap;
+  int run = threadIdx.x > 0 ? part[threadIdx.x - 1] : 0;
+  for (int i = lo; i < hi; i++) {
+    S.tile_start[i] = overflow ? 0 : run;
+    run += tile_count[i];
+  }
+  if (threadIdx.x == 0) {
+    S.tile_start[T] = overflow ? 0 : total;
+    *bin_total = total;
+    if (overflow) atomicOr(S.err, DVG_EFLAG_BIN_OVERFLOW);
+  }
+}
+
+// one block per tile: ordered (ascending group id) compaction of the hits
+__global__ void k_bin_fill(DevScene S, const int4 *g_tile_range) {
+  if (*(volatile unsigned *)S.err & DVG_EFLAG_BIN_OVERFLOW) return;
+  int t = blockIdx.x;
+  int tx = t % S.tiles_x, ty = t / S.tiles_x;
+  __shared__ int warp_cnt[32];
+  __shared__ int base_sh;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) base_sh = S.tile_start[t];
+  __syncthreads();
+  for (int g0 = 0; g0 < S.num_groups; g0 += blockDim.x) {
+    int g = g0 + threadIdx.x;
+    bool hit = g < S.num_groups && tile_hit(g_tile_range[g], tx, ty);
+    unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) warp_cnt[wid] = __popc(m);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < nw; w++) {
+      int c = warp_cnt[w];
+      if (w < wid) before += c;
+      total += c;
+    }
+    if (hit) S.tile_list[base_sh + before + __popc(m & ((1u << lane) - 1u))] = g;
+    __syncthreads();
+    if (threadIdx.x == 0) base_sh += total;
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4 *g_tile_range, int *tile_count,
+                           cudaStream_t st) {
+  int G = S.num_groups, NS = S.num_shapes;
+  int T = S.tiles_x * S.tiles_y;
+  if (G > 0) k_group_xform<<<(G + 127) / 128, 128, 0, st>>>(S);
+  if (NS > 0) k_shape_prep<<<(NS + 63) / 64, 64, 0, st>>>(S);
+  if (G > 0) k_group_prep<<<(G + 127) / 128, 128, 0, st>>>(S, g_tile_range);
+  k_sampling_cdf<<<1, 32, 0, st>>>(S);
+  k_bin_count<<<T, 128, 0, st>>>(S, g_tile_range, tile_count);
+  k_bin_scan<<<1, 1024, 0, st>>>(S, tile_count, tile_cap, bin_total);
+  k_bin_fill<<<T, 128, 0, st>>>(S, g_tile_range);
+  return cudaGetLastError();
+}
+
+}  // namespace dvg

@@ -1,0 +1,285 @@
+// Render kernels of the GB300 path: weight image, per-sample colour,
+// filtered resolve, interior adjoint, boundary (edge-sampling) adjoint and
+// the signed-distance output.
+//
+// Work decomposition.  Colour kernels run one CTA per 16x16 image tile and
+// sub-sample index (blockIdx.y), one thread per pixel, so a warp covers two
+// adjacent pixel rows and shares its candidate list.  Sample colours go to a
+// per-sample buffer and are filtered by a gather pass per pixel (the
+// reference splats them with float atomics, diffvg.cpp:1218-1249); the
+// image is written once, atomic-free and deterministic.  The boundary pass
+// runs one thread per boundary sample (diffvg.cpp:1325-1475).
+#include "dvg_internal.h"
+#include "dvg_sample.cuh"
+
+namespace dvg {
+
+// Kernels that accumulate into caller-visible outputs do nothing when the
+// tile lists overflowed their capacity; the host then grows the lists and
+// runs the call again, so nothing is counted twice.
+__device__ __forceinline__ bool bins_overflowed(const DevScene &S) {
+  return (*(volatile const unsigned *)S.err & DVG_EFLAG_BIN_OVERFLOW) != 0u;
+}
+
+// Filter radius and support read from the parameter arena on the device, so
+// that no call waits for a host read of a parameter.
+__device__ __forceinline__ DevRender load_filter(const DevRender &R0, const DevScene *S) {
+  DevRender R = R0;
+  float fr = __ldg(R0.fr_ptr);
+  bool ok = fr >= 0.f && fr <= 64.f;
+  if (!ok && S && threadIdx.x == 0 && blockIdx.x == 0 && blockIdx.y == 0) atomicOr(S->err, (unsigned)DVG_EFLAG_FILTER);
+  R.fr = ok ? fr : 0.f;
+  R.ri = ok ? (int)ceilf(fr) : 0;
+  return R;
+}
+
+// weight image (weight_kernel, diffvg.cpp:1115-1158), gathered per pixel.
+// The reference never passes use_prefiltering to it (diffvg.cpp:1525-1533),
+// so the weights always use the jittered positions.
+__global__ void __launch_bounds__(256) k_weight(DevRender R0, DevScene S) {
+  DevRender R = load_filter(R0, &S);
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= R.w * R.h) return;
+  int px = p % R.w, py = p / R.w;
+  float ws = 0.f;
+  for (int ny = py - R.ri; ny <= py + R.ri; ny++) {
+    if (ny < 0 || ny >= R.h) continue;
+    for (int nx = px - R.ri; nx <= px + R.ri; nx++) {
+      if (nx < 0 || nx >= R.w) continue;
+      for (int k = 0; k < R.spp; k++) {
+        int idx = (ny * R.w + nx) * R.spp + k, x, y;
+        v2 pt = sample_pos(R, idx, false, x, y);
+        ws += filter_weight(R.ftype, R.fr, (px + 0.5f) - pt.x, (py + 0.5f) - pt.y);
+      }
+    }
+  }
+  R.weight[p] = ws;
+}
+
+template <bool PREFILTER>
+__global__ void __launch_bounds__(256) k_sample_fwd(DevScene S, DevRender R, float4 *samples) {
+  int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
+  int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  int px = tx * DVG_TILE + (threadIdx.x & (DVG_TILE - 1)), py = ty * DVG_TILE + (threadIdx.x / DVG_TILE);
+  if (px >= R.w || py >= R.h) return;
+  int idx = (py * R.w + px) * R.spp + blockIdx.y;
+  int x, y;
+  v2 pt = sample_pos(R, idx, PREFILTER, x, y);
+  v2 npt = V2(pt.x / R.w, pt.y / R.h);
+  const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
+  float4 c = PREFILTER ? sample_color_prefiltered_fwd(S, bg, npt) : sample_color_fwd(S, bg, npt, nullptr);
+  samples[idx] = c;
+}
+
+// filtered pixel colour from the sample colours around it
+__global__ void __launch_bounds__(256) k_resolve(DevRender R0, const float4 *samples, float *image) {
+  DevRender R = load_filter(R0, nullptr);
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= R.w * R.h) return;
+  int px = p % R.w, py = p / R.w;
+  float ws = R.weight[p];
+  float4 acc = F4(0, 0, 0, 0);
+  if (ws > 0) {
+    for (int ny = py - R.ri; ny <= py + R.ri; ny++) {
+      if (ny < 0 || ny >= R.h) continue;
+      for (int nx = px - R.ri; nx <= px + R.ri; nx++) {
+        if (nx < 0 || nx >= R.w) continue;
+        for (int k = 0; k < R.spp; k++) {
+          int idx = (ny * R.w + nx) * R.spp + k, x, y;
+          v2 pt = sample_pos(R, idx, R.prefilter != 0, x, y);
+          float fw = filter_weight(R.ftype, R.fr, (px + 0.5f) - pt.x, (py + 0.5f) - pt.y);
+          float4 c = samples[idx];
+          acc = add4(acc, F4(fw * c.x / ws, fw * c.y / ws, fw * c.z / ws, fw * c.w / ws));
+        }
+      }
+    }
+  }
+  reinterpret_cast<float4 *>(image)[p] = acc;
+}
+
+__device__ __forceinline__ float block_sum(float v) {
+  __shared__ float red[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float s = 0.f;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+  return s;
+}
+
+// interior adjoint (render_kernel with d_render_image, diffvg.cpp:1160-1268)
+template <bool PREFILTER>
+__global__ void __launch_bounds__(256) k_sample_bwd(DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
+  DevRender R = load_filter(R0, nullptr);
+  int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
+  int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  int px = tx * DVG_TILE + (threadIdx.x & (DVG_TILE - 1)), py = ty * DVG_TILE + (threadIdx.x / DVG_TILE);
+  bool active = px < R.w && py < R.h && !bins_overflowed(S);
+  float dfr = 0.f;
+  if (active) {
+    int idx = (py * R.w + px) * R.spp + blockIdx.y;
+    int x, y;
+    v2 pt = sample_pos(R, idx, PREFILTER, x, y);
+    v2 npt = V2(pt.x / R.w, pt.y / R.h);
+    float4 d_color = gather_d_color(R, pt);
+    const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
+    float4 dbg = F4(0, 0, 0, 0);
+    int assign = 0;
+    float *d_tr = R.d_translation ? R.d_translation + 2 * (y * R.w + x) : nullptr;
+    float4 *dbgp = R.d_background ? &dbg : nullptr;
+    float4 color = PREFILTER ? sample_color_prefiltered_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params)
+                             : sample_color_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params);
+    if (R.d_background) { dbg_val[idx] = dbg; dbg_flag[idx] = assign; }
+    // d filter radius (diffvg.cpp:1250-1268)
+    for (int dy = -R.ri; dy <= R.ri; dy++)
+      for (int dx = -R.ri; dx <= R.ri; dx++) {
+        int xx = x + dx, yy = y + dy;
+        if (xx >= 0 && xx < R.w && yy >= 0 && yy < R.h && R.weight[yy * R.w + xx] > 0) {
+          float ws = R.weight[yy * R.w + xx];
+          float xc = xx + 0.5f, yc = yy + 0.5f;
+          float fw = filter_weight(R.ftype, R.fr, xc - pt.x, yc - pt.y);
+          float4 di = __ldg(reinterpret_cast<const float4 *>(R.d_image) + (yy * R.w + xx));
+          float dd = dot4(di, color);
+          float d_weight = (dd * ws - fw * dd * (ws - fw)) / (ws * ws);
+          dfr += d_filter_weight(R.ftype, R.fr, xc - pt.x, yc - pt.y, d_weight);
+        }
+      }
+  }
+  float tot = block_sum(dfr);
+  if (threadIdx.x == 0 && tot != 0.f) atomicAdd(R.d_params + R.filter_radius_off, tot);
+}
+
+// Background adjoint in sample order per pixel: a sample without fragments
+// overwrites the pixel's value with its d_color, the others add to it
+// (diffvg.cpp:596-604, 699-704).
+__global__ void k_bg_combine(DevScene S, DevRender R, const float4 *dbg_val, const int *dbg_flag) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= R.w * R.h || bins_overflowed(S)) return;
+  float4 *dst = reinterpret_cast<float4 *>(R.d_background) + p;
+  float4 v = *dst;
+  for (int k = 0; k < R.spp; k++) {
+    int idx = p * R.spp + k;
+    float4 c = dbg_val[idx];
+    v = dbg_flag[idx] ? c : add4(v, c);
+  }
+  *dst = v;
+}
+
+// boundary adjoint (sample_boundary_kernel + render_edge_kernel,
+// diffvg.cpp:1325-1475); the reference's Morton sort of the boundary samples
+// only reorders atomics and is not needed for the result.
+__global__ void __launch_bounds__(256) k_edge(DevScene S, DevRender R0) {
+  DevRender R = load_filter(R0, nullptr);
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = R.w * R.h * R.spp;
+  if (idx >= n || S.num_total <= 0 || bins_overflowed(S)) return;
+  Pcg rng = pcg_init(idx, R.seed);
+  float u = pcg_float(rng);
+  int sid = cdf_sample(S.smp_cdf, S.num_total, u, nullptr);
+  int s = S.smp_shape[sid], g = S.smp_group[sid];
+  // diffvg.cpp:1343 indexes the pmf by shape id
+  float pmf = s < S.num_total ? S.smp_pmf[s] : 0.f;
+  if (pmf <= 0) return;
+  float pdf = 0.f;
+  v2 normal = V2(0, 0);
+  float t = pcg_float(rng);
+  BData bd = {0, 0, 0.f, 0};
+  v2 lpt = sample_boundary(S, g, s, t, &normal, &pdf, &bd);
+  if (pdf <= 0) return;
+  int xo = GI(S, g, DVG_GROUP_XFORM_OFF);
+  float s2c[9], c2s[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) { s2c[i] = pget(S, xo + i); c2s[i] = S.c2s[9 * g + i]; }
+  v2 bpt = xform_pt(s2c, lpt);
+  normal = xform_normal(c2s, normal);
+  bpt.x /= S.W;
+  bpt.y /= S.H;
+  pdf = pmf * pdf;
+  int bx = (int)(bpt.x * R.w), by = (int)(bpt.y * R.h);
+  if (bx < 0 || bx >= R.w || by < 0 || by >= R.h) return;
+  EdgeQ qin = {g, s, 0}, qout = {g, s, 0};
+  const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (by * R.w + bx) : nullptr;
+  float4 cin = sample_color_fwd(S, bg, sub2(bpt, scl2(1e-4f, normal)), &qin);
+  float4 cout = sample_color_fwd(S, bg, add2(bpt, scl2(1e-4f, normal)), &qout);
+  if (!qin.hit && !qout.hit) return;
+  if (!qin.hit) {
+    normal = neg2(normal);
+    float4 tmp = cin; cin = cout; cout = tmp;
+  }
+  v2 sbpt = V2(bpt.x * R.w, bpt.y * R.h);
+  float4 dc = gather_d_color(R, sbpt);
+  float norm = (float)(S.W * S.H);
+  dc = F4(dc.x / norm, dc.y / norm, dc.z / norm, dc.w / norm);
+  float contrib = dot4(sub4(cin, cout), dc) / pdf;
+  accumulate_boundary_gradient(S, g, s, contrib, t, normal, bd, lpt, R.d_params);
+  if (R.d_translation) {
+    atomicAdd(&R.d_translation[2 * (by * R.w + bx) + 0], normal.x * contrib);
+    atomicAdd(&R.d_translation[2 * (by * R.w + bx) + 1], normal.y * contrib);
+  }
+}
+
+// signed distance output (render_kernel's sdf branch, diffvg.cpp:1273-1293)
+__global__ void __launch_bounds__(256) k_sdf(DevScene S, DevRender R, const float *eval_positions, int num_eval,
+                                             float *sdf, const float *d_sdf) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = eval_positions ? num_eval : R.w * R.h * R.spp;
+  if (idx >= n || bins_overflowed(S)) return;
+  int x, y;
+  v2 pt;
+  if (eval_positions) {
+    pt = V2(eval_positions[2 * idx], eval_positions[2 * idx + 1]);
+    x = (int)pt.x;
+    y = (int)pt.y;
+  } else {
+    pt = sample_pos(R, idx, R.prefilter != 0, x, y);
+  }
+  v2 npt = V2(pt.x / R.w, pt.y / R.h);
+  float d_dist = 0.f;
+  if (d_sdf) d_dist = eval_positions ? d_sdf[idx] : d_sdf[y * R.w + x];
+  float weight = eval_positions ? 1.f : 1.f / R.spp;
+  bool in_image = x >= 0 && x < R.w && y >= 0 && y < R.h;
+  float *d_tr = (R.d_translation && in_image) ? R.d_translation + 2 * (y * R.w + x) : nullptr;
+  float dist = sample_distance(S, npt, weight, d_sdf ? &d_dist : nullptr, d_tr, R.d_params);
+  if (sdf) {
+    if (eval_positions) sdf[idx] += dist;
+    else atomicAdd(&sdf[y * R.w + x], dist);
+  }
+}
+
+static inline int tiles_of(const DevRender &R) {
+  return ((R.w + DVG_TILE - 1) / DVG_TILE) * ((R.h + DVG_TILE - 1) / DVG_TILE);
+}
+static inline unsigned blocks_of(long long n) { return (unsigned)((n + 255) / 256); }
+
+void launch_weight(const DevScene &S, const DevRender &R, cudaStream_t st) {
+  k_weight<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(R, S);
+}
+void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, cudaStream_t st) {
+  dim3 grid(tiles_of(R), R.spp);
+  if (R.prefilter) k_sample_fwd<true><<<grid, 256, 0, st>>>(S, R, samples);
+  else k_sample_fwd<false><<<grid, 256, 0, st>>>(S, R, samples);
+}
+void launch_resolve(const DevRender &R, const float4 *samples, float *image, cudaStream_t st) {
+  k_resolve<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(R, samples, image);
+}
+void launch_sample_bwd(const DevScene &S, const DevRender &R, float4 *dbg_val, int *dbg_flag, cudaStream_t st) {
+  dim3 grid(tiles_of(R), R.spp);
+  if (R.prefilter) k_sample_bwd<true><<<grid, 256, 0, st>>>(S, R, dbg_val, dbg_flag);
+  else k_sample_bwd<false><<<grid, 256, 0, st>>>(S, R, dbg_val, dbg_flag);
+}
+void launch_bg_combine(const DevScene &S, const DevRender &R, const float4 *dbg_val, const int *dbg_flag,
+                       cudaStream_t st) {
+  k_bg_combine<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(S, R, dbg_val, dbg_flag);
+}
+void launch_edge(const DevScene &S, const DevRender &R, cudaStream_t st) {
+  k_edge<<<blocks_of((long long)R.w * R.h * R.spp), 256, 0, st>>>(S, R);
+}
+void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
+                const float *d_sdf, cudaStream_t st) {
+  long long n = eval_positions ? num_eval : (long long)R.w * R.h * R.spp;
+  if (n <= 0) return;
+  k_sdf<<<blocks_of(n), 256, 0, st>>>(S, R, eval_positions, num_eval, sdf, d_sdf);
+}
+
+}  // namespace dvg

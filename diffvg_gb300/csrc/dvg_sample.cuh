@@ -1,0 +1,380 @@
+// Per-sample colour evaluation of the GB300 render path: the forward blend,
+// its reverse-mode adjoint, the prefiltered (analytic coverage) variant and
+// the signed distance query (diffvg.cpp:525-833, 835-1113, 709-775).
+//
+// Candidate groups come from the sample's 16x16 canvas tile list in
+// ascending group id, which is the reference's back-to-front fragment order
+// (it sorts fragments by group id, diffvg.cpp:605-615), so the forward pass
+// blends each fragment as soon as it is found and keeps no fragment list.
+// The adjoint re-evaluates the fragments of its sample (the forward pass
+// stores nothing per sample) into a per-thread list and walks it in
+// reverse.
+#pragma once
+
+#include "dvg_adjoint.cuh"
+
+// Sample position of sample idx (diffvg.cpp:1164-1180).
+DI v2 sample_pos(const DevRender &R, int idx, bool prefilter, int &x, int &y) {
+  Pcg rng = pcg_init(idx, R.seed);
+  int sx = idx % R.nsx;
+  int sy = (idx / R.nsx) % R.nsy;
+  x = (idx / (R.nsx * R.nsy)) % R.w;
+  y = (idx / (R.nsx * R.nsy * R.w));
+  float rx = pcg_float(rng), ry = pcg_float(rng);
+  if (prefilter) { rx = 0.5f; ry = 0.5f; }
+  return V2(x + ((float)sx + rx) / R.nsx, y + ((float)sy + ry) / R.nsy);
+}
+
+// gather_d_color (diffvg.cpp:777-815)
+DI float4 gather_d_color(const DevRender &R, v2 pt) {
+  int x = (int)pt.x, y = (int)pt.y;
+  float4 d = F4(0, 0, 0, 0);
+  for (int dy = -R.ri; dy <= R.ri; dy++)
+    for (int dx = -R.ri; dx <= R.ri; dx++) {
+      int xx = x + dx, yy = y + dy;
+      if (xx >= 0 && xx < R.w && yy >= 0 && yy < R.h) {
+        float xc = xx + 0.5f, yc = yy + 0.5f;
+        float fw = filter_weight(R.ftype, R.fr, xc - pt.x, yc - pt.y);
+        float ws = R.weight[yy * R.w + xx];
+        if (ws > 0) {
+          float4 di = __ldg(reinterpret_cast<const float4 *>(R.d_image) + (yy * R.w + xx));
+          d = add4(d, scl4(fw / ws, di));
+        }
+      }
+    }
+  return d;
+}
+
+DI void blend(float4 &acc, float4 c) {
+  float na = c.w;
+  acc.x = acc.x * (1 - na) + na * c.x;
+  acc.y = acc.y * (1 - na) + na * c.y;
+  acc.z = acc.z * (1 - na) + na * c.z;
+  acc.w = acc.w * (1 - na) + na;
+}
+
+DI float4 finish_color(float4 acc) {
+  if (acc.w > 1e-6f) { acc.x /= acc.w; acc.y /= acc.w; acc.z /= acc.w; }
+  return acc;
+}
+
+// Forward colour of one sample (sample_color, diffvg.cpp:525-655).  With an
+// EdgeQuery the hit flag follows the reference's rule: the last fragment
+// that is either of the queried group (sets it) or opaque (clears it)
+// decides; without such a fragment the flag keeps what the coverage tests
+// of the queried shape set (diffvg.cpp:624-633).
+DI float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq) {
+  if (eq) eq->hit = 0;
+  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+  int b, e;
+  bool list = cand_range(S, pt, b, e);
+  float4 acc = bg ? *bg : F4(0, 0, 0, 0);
+  int nf = 0, ev = -1;
+  int G = S.num_groups;
+  for (int k = b; k < e; k++) {
+    int g = list ? __ldg(&S.tile_list[k]) : k;
+    if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
+    int sk = GI(S, g, DVG_GROUP_STROKE_KIND), fk = GI(S, g, DVG_GROUP_FILL_KIND);
+    if (sk != DVG_PAINT_NONE && group_stroke(S, g, pt, eq)) {
+      float4 c = paint_color(S, sk, GI(S, g, DVG_GROUP_STROKE_OFF), GI(S, g, DVG_GROUP_STROKE_STOPS), pt);
+      if (eq) ev = (eq->group == g) ? 1 : (c.w >= 1.f ? 0 : ev);
+      blend(acc, c);
+      nf++;
+    }
+    if (fk != DVG_PAINT_NONE && group_inside(S, g, pt, eq)) {
+      float4 c = paint_color(S, fk, GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS), pt);
+      if (eq) ev = (eq->group == g) ? 1 : (c.w >= 1.f ? 0 : ev);
+      blend(acc, c);
+      nf++;
+    }
+  }
+  if (nf > DVG_MAX_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
+  if (eq && ev >= 0) eq->hit = ev;
+  if (nf <= 0) return bg ? *bg : F4(0, 0, 0, 0);
+  return finish_color(acc);
+}
+
+// Adjoint of sample_color (diffvg.cpp:525-707 with d_color != nullptr).
+// d_bg receives the background adjoint with the reference's semantics:
+// *assign = 1 when the sample has no fragment (the reference then
+// overwrites the pixel's background gradient with d_color).
+DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color, float4 *d_bg,
+                           int *assign, float *d_tr, float *dp) {
+  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+  int b, e;
+  bool list = cand_range(S, pt, b, e);
+  float4 cols[DVG_MAX_FRAGMENTS];
+  float4 accs[DVG_MAX_FRAGMENTS];
+  int keys[DVG_MAX_FRAGMENTS];
+  float4 first = bg ? *bg : F4(0, 0, 0, 0);
+  float4 acc = first;
+  int nf = 0;
+  bool overflow = false;
+  int G = S.num_groups;
+  for (int k = b; k < e && !overflow; k++) {
+    int g = list ? __ldg(&S.tile_list[k]) : k;
+    if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
+    int sk = GI(S, g, DVG_GROUP_STROKE_KIND), fk = GI(S, g, DVG_GROUP_FILL_KIND);
+    if (sk != DVG_PAINT_NONE && group_stroke(S, g, pt, nullptr)) {
+      if (nf >= DVG_MAX_FRAGMENTS) { overflow = true; break; }
+      float4 c = paint_color(S, sk, GI(S, g, DVG_GROUP_STROKE_OFF), GI(S, g, DVG_GROUP_STROKE_STOPS), pt);
+      blend(acc, c);
+      cols[nf] = c; accs[nf] = acc; keys[nf] = 2 * g + 1;
+      nf++;
+    }
+    if (fk != DVG_PAINT_NONE && group_inside(S, g, pt, nullptr)) {
+      if (nf >= DVG_MAX_FRAGMENTS) { overflow = true; break; }
+      float4 c = paint_color(S, fk, GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS), pt);
+      blend(acc, c);
+      cols[nf] = c; accs[nf] = acc; keys[nf] = 2 * g;
+      nf++;
+    }
+  }
+  if (overflow) {
+    flag_error(S, DVG_EFLAG_CAPACITY);
+    return F4(0, 0, 0, 0);
+  }
+  if (nf <= 0) {
+    if (bg) {
+      if (d_bg) { *d_bg = d_color; *assign = 1; }
+      return *bg;
+    }
+    return F4(0, 0, 0, 0);
+  }
+  float4 fin = finish_color(acc);
+  float dcr = d_color.x, dcg = d_color.y, dcb = d_color.z, dca = d_color.w;
+  if (acc.w > 1e-6f) {
+    float fa = acc.w;
+    float nr = d_color.x / fa, ng = d_color.y / fa, nb = d_color.z / fa;
+    dca -= (d_color.x * fin.x + d_color.y * fin.y + d_color.z * fin.z) / fa;
+    dcr = nr; dcg = ng; dcb = nb;
+  }
+  for (int i = nf - 1; i >= 0; i--) {
+    float4 f = cols[i];
+    float4 p = i > 0 ? accs[i - 1] : first;
+    float d_pa = dca * (1.f - f.w);
+    float d_ai = dca * (1.f - p.w);
+    d_ai += dcr * (f.x - p.x) + dcg * (f.y - p.y) + dcb * (f.z - p.z);
+    float d_pr = dcr * (1 - f.w), d_pg = dcg * (1 - f.w), d_pb = dcb * (1 - f.w);
+    float4 dci = F4(dcr * f.w, dcg * f.w, dcb * f.w, d_ai);
+    int g = keys[i] >> 1;
+    if (keys[i] & 1)
+      d_paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
+                    GI(S, g, DVG_GROUP_STROKE_STOPS), pt, dci, dp, d_tr);
+    else
+      d_paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS),
+                    pt, dci, dp, d_tr);
+    dcr = d_pr; dcg = d_pg; dcb = d_pb; dca = d_pa;
+  }
+  if (d_bg) { d_bg->x += dcr; d_bg->y += dcg; d_bg->z += dcb; d_bg->w += dca; }
+  return fin;
+}
+
+// smoothstep / d_smoothstep (diffvg.cpp:817-833)
+DI float smoothstep(float d) {
+  float t = clampf_((d + 1.f) / 2.f, 0.f, 1.f);
+  return t * t * (3 - 2 * t);
+}
+DI float d_smoothstep(float d, float d_ret) {
+  if (d < -1.f || d > 1.f) return 0.f;
+  float t = (d + 1.f) / 2.f;
+  float d_t = d_ret * (6 * t - 6 * t * t);
+  return d_t / 2.f;
+}
+
+struct PFrag {
+  float4 c;
+  int group_stroke;  // 2*group + stroke
+  int shape;
+  float distance;
+  v2 closest;
+  PathInfo info;
+  int within;
+};
+
+// Coverage fragments of one group at pt (diffvg.cpp:851-905).  Returns the
+// number of fragments written (0..2).
+DI int prefilter_group(const DevScene &S, int g, v2 pt, PFrag *out) {
+  int n = 0;
+  int sk = GI(S, g, DVG_GROUP_STROKE_KIND), fk = GI(S, g, DVG_GROUP_FILL_KIND);
+  if (sk != DVG_PAINT_NONE) {
+    int ms = -1;
+    v2 cp = V2(0, 0);
+    PathInfo li = {-1, -1, 0.f};
+    float d = INFINITY;
+    group_distance(S, g, pt, INFINITY, &ms, &cp, &li, &d);
+    if (ms == -1) {
+      flag_error(S, DVG_EFLAG_UNSUPPORTED);  // diffvg.cpp:867 asserts
+    } else {
+      float sw = stroke_width(S, ms);
+      float w = smoothstep(fabsf(d) + sw) - smoothstep(fabsf(d) - sw);
+      if (w > 0) {
+        float4 c = paint_color(S, sk, GI(S, g, DVG_GROUP_STROKE_OFF), GI(S, g, DVG_GROUP_STROKE_STOPS), pt);
+        PFrag &f = out[n++];
+        f.c = F4(c.x, c.y, c.z, c.w * w);
+        f.group_stroke = 2 * g + 1; f.shape = ms; f.distance = d; f.closest = cp; f.info = li; f.within = 1;
+      }
+    }
+  }
+  if (fk != DVG_PAINT_NONE) {
+    int ms = -1;
+    v2 cp = V2(0, 0);
+    PathInfo li = {-1, -1, 0.f};
+    float d = INFINITY;
+    bool found = group_distance(S, g, pt, 1.f, &ms, &cp, &li, &d);
+    bool ins = group_inside(S, g, pt, nullptr);
+    if (found || ins) {
+      if (!ins) d = -d;
+      float w = smoothstep(d);
+      if (w > 0) {
+        float4 c = paint_color(S, fk, GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS), pt);
+        PFrag &f = out[n++];
+        f.c = F4(c.x, c.y, c.z, c.w * w);
+        f.group_stroke = 2 * g; f.shape = ms; f.distance = d; f.closest = cp; f.info = li; f.within = found ? 1 : 0;
+      }
+    }
+  }
+  return n;
+}
+
+// sample_color_prefiltered, forward only (diffvg.cpp:835-960)
+DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 screen_pt) {
+  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+  int b, e;
+  bool list = cand_range(S, pt, b, e);
+  float4 acc = bg ? *bg : F4(0, 0, 0, 0);
+  int nf = 0;
+  int G = S.num_groups;
+  for (int k = b; k < e; k++) {
+    int g = list ? __ldg(&S.tile_list[k]) : k;
+    if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
+    PFrag fr[2];
+    int n = prefilter_group(S, g, pt, fr);
+    for (int j = 0; j < n; j++) { blend(acc, fr[j].c); nf++; }
+  }
+  if (nf > DVG_MAX_PREFILTER_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
+  if (nf <= 0) return bg ? *bg : F4(0, 0, 0, 0);
+  return finish_color(acc);
+}
+
+// Adjoint of sample_color_prefiltered (diffvg.cpp:960-1113)
+DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color,
+                                       float4 *d_bg, int *assign, float *d_tr, float *dp) {
+  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+  int b, e;
+  bool list = cand_range(S, pt, b, e);
+  PFrag frags[DVG_MAX_PREFILTER_FRAGMENTS];
+  float4 accs[DVG_MAX_PREFILTER_FRAGMENTS];
+  float4 first = bg ? *bg : F4(0, 0, 0, 0);
+  float4 acc = first;
+  int nf = 0;
+  bool overflow = false;
+  int G = S.num_groups;
+  for (int k = b; k < e; k++) {
+    int g = list ? __ldg(&S.tile_list[k]) : k;
+    if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
+    PFrag fr[2];
+    int n = prefilter_group(S, g, pt, fr);
+    if (nf + n > DVG_MAX_PREFILTER_FRAGMENTS) { overflow = true; break; }
+    for (int j = 0; j < n; j++) {
+      blend(acc, fr[j].c);
+      frags[nf] = fr[j];
+      accs[nf] = acc;
+      nf++;
+    }
+  }
+  if (overflow) {
+    flag_error(S, DVG_EFLAG_CAPACITY);
+    return F4(0, 0, 0, 0);
+  }
+  if (nf <= 0) {
+    if (bg) {
+      if (d_bg) { *d_bg = d_color; *assign = 1; }
+      return *bg;
+    }
+    return F4(0, 0, 0, 0);
+  }
+  float4 fin = finish_color(acc);
+  float dcr = d_color.x, dcg = d_color.y, dcb = d_color.z, dca = d_color.w;
+  if (acc.w > 1e-6f) {
+    float fa = acc.w;
+    float nr = d_color.x / fa, ng = d_color.y / fa, nb = d_color.z / fa;
+    dca -= (d_color.x * fin.x + d_color.y * fin.y + d_color.z * fin.z) / fa;
+    dcr = nr; dcg = ng; dcb = nb;
+  }
+  for (int i = nf - 1; i >= 0; i--) {
+    const PFrag &f = frags[i];
+    float4 p = i > 0 ? accs[i - 1] : first;
+    float d_pa = dca * (1.f - f.c.w);
+    float d_ai = dca * (1.f - p.w);
+    d_ai += dcr * (f.c.x - p.x) + dcg * (f.c.y - p.y) + dcb * (f.c.z - p.z);
+    float d_pr = dcr * (1 - f.c.w), d_pg = dcg * (1 - f.c.w), d_pb = dcb * (1 - f.c.w);
+    float dcir = dcr * f.c.w, dcig = dcg * f.c.w, dcib = dcb * f.c.w;
+    int g = f.group_stroke >> 1;
+    if (f.group_stroke & 1) {
+      float d = f.distance;
+      float sw = stroke_width(S, f.shape);
+      float apw = fabsf(d) + sw, amw = fabsf(d) - sw;
+      float w = smoothstep(apw) - smoothstep(amw);
+      if (w != 0) {
+        float d_w = w > 0 ? (f.c.w / w) * d_ai : 0.f;
+        d_ai *= w;
+        d_paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
+                      GI(S, g, DVG_GROUP_STROKE_STOPS), pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr);
+        float d_apw = d_smoothstep(apw, d_w);
+        float d_amw = -d_smoothstep(amw, d_w);
+        float d_d = d_apw + d_amw;
+        if (d < 0) d_d = -d_d;
+        float d_sw = d_apw - d_amw;
+        if (fabsf(d_d) > 1e-10f) d_group_distance(S, g, f.shape, pt, f.closest, f.info, d_d, dp, d_tr);
+        gadd(dp, SI(S, f.shape, DVG_SHAPE_STROKE_WIDTH_OFF), d_sw);
+      }
+    } else {
+      float d = f.distance;
+      float w = smoothstep(d);
+      if (w != 0) {
+        float d_w = w > 0 ? (f.c.w / w) * d_ai : 0.f;
+        d_ai *= w;
+        d_paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS),
+                      pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr);
+        float d_d = d_smoothstep(d, d_w);
+        if (d < 0) d_d = -d_d;
+        if (fabsf(d_d) > 1e-10f && f.within) d_group_distance(S, g, f.shape, pt, f.closest, f.info, d_d, dp, d_tr);
+      }
+    }
+    dcr = d_pr; dcg = d_pg; dcb = d_pb; dca = d_pa;
+  }
+  if (d_bg) { d_bg->x += dcr; d_bg->y += dcg; d_bg->z += dcb; d_bg->w += dca; }
+  return fin;
+}
+
+// sample_distance (diffvg.cpp:709-775): signed distance to the closest
+// group boundary, negative inside a filled group.
+DI float sample_distance(const DevScene &S, v2 screen_pt, float weight, const float *d_dist, float *d_tr, float *dp) {
+  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+  int min_g = -1, min_s = -1;
+  float min_d = 0.f;
+  v2 cpt = V2(0, 0);
+  PathInfo minfo = {-1, -1, 0.f};
+  for (int g = S.num_groups - 1; g >= 0; g--) {
+    int s = -1;
+    v2 p = V2(0, 0);
+    PathInfo li = {-1, -1, 0.f};
+    float d = INFINITY;
+    if (group_distance(S, g, pt, INFINITY, &s, &p, &li, &d)) {
+      if (min_g == -1 || d < min_d) { min_d = d; min_g = g; min_s = s; cpt = p; minfo = li; }
+    }
+  }
+  if (min_g == -1) return min_d;
+  min_d *= weight;
+  bool ins = false;
+  if (GI(S, min_g, DVG_GROUP_FILL_KIND) != DVG_PAINT_NONE) {
+    ins = group_inside(S, min_g, pt, nullptr);
+    if (ins) min_d = -min_d;
+  }
+  if (d_dist) {
+    float d_abs = ins ? -(*d_dist) : (*d_dist);
+    d_group_distance(S, min_g, min_s, pt, cpt, minfo, d_abs, dp, d_tr);
+  }
+  return min_d;
+}

@@ -63,8 +63,11 @@ class PackedScene:
         """The parameter values as one contiguous fp32 tensor on `device`."""
         if not self.tensors:
             return torch.zeros(1, dtype=torch.float32, device=device)
-        flat = [t.detach().reshape(-1).to(device=device, dtype=torch.float32) for t in self.tensors]
-        return torch.cat(flat)
+        flat = [t.detach().reshape(-1).to(dtype=torch.float32) for t in self.tensors]
+        if len({t.device for t in flat}) == 1:
+            # one concatenation where the tensors live, then one copy
+            return torch.cat(flat).to(device=device)
+        return torch.cat([t.to(device=device) for t in flat])
 
 
 def _as_tensor(x):

@@ -1,0 +1,275 @@
+"""PyTorch front end of the GB300 render path: pydiffvg's RenderFunction.
+
+Drop-in for pydiffvg.RenderFunction (reference: pydiffvg/render_pytorch.py):
+``serialize_scene`` builds the same flat argument list, ``apply`` takes
+``(width, height, num_samples_x, num_samples_y, seed, background_image,
+*args)`` and returns the ``[H, W, 4]`` image (or the ``[H, W, 1]`` /
+``[N, 1]`` signed distance), ``backward`` returns one gradient per argument
+(None where the reference returns None) and ``render_grad`` returns the
+``[H, W, 2]`` translation gradient image.
+
+Differences from the reference that a caller can observe:
+  * tensors keep their device: serialize_scene does not copy them to the
+    host, and gradients come back on the device of each input tensor;
+  * the scene topology (shape kinds, segment counts, group membership) is
+    uploaded once and cached on the device by its hash, so an optimisation
+    loop re-sends only the parameter values (one concatenated fp32 arena);
+  * there is no CPU path: rendering requires a CUDA device.
+"""
+from collections import OrderedDict
+from enum import IntEnum
+import itertools
+import threading
+import warnings
+
+import torch
+
+from . import device as _device
+from . import _native
+from .diffvg import ShapeType, ColorType, FilterType
+from .packing import pack_scene
+from .pixel_filter import PixelFilter
+from . import shape as _shape
+from . import color as _color
+
+print_timing = False
+
+
+def set_print_timing(val):
+    global print_timing
+    print_timing = val
+
+
+class OutputType(IntEnum):
+    color = 1
+    sdf = 2
+
+
+_SCENE_CACHE_SIZE = 64
+_cache_lock = threading.Lock()
+_scene_cache = OrderedDict()
+_token = itertools.count(1)
+
+
+def _native_scene(packed, device):
+    """Resident device scene for this topology (cached, LRU)."""
+    key = (packed.topology_key, device.index)
+    with _cache_lock:
+        sc = _scene_cache.get(key)
+        if sc is not None:
+            _scene_cache.move_to_end(key)
+            return sc
+    with torch.cuda.device(device):
+        sc = _native.NativeScene(packed)
+    sc.last_token = None
+    with _cache_lock:
+        _scene_cache[key] = sc
+        while len(_scene_cache) > _SCENE_CACHE_SIZE:
+            _, old = _scene_cache.popitem(last=False)
+            old.close()
+    return sc
+
+
+def clear_scene_cache():
+    with _cache_lock:
+        for sc in _scene_cache.values():
+            sc.close()
+        _scene_cache.clear()
+
+
+def _render_device():
+    dev = _device.get_device()
+    if dev.type != 'cuda':
+        raise RuntimeError('diffvg_gb300 renders on CUDA only; set_use_gpu(False) has no CPU path here')
+    if not torch.cuda.is_available():
+        raise RuntimeError('diffvg_gb300 needs a CUDA device')
+    if dev.index is None:
+        dev = torch.device('cuda', torch.cuda.current_device())
+    return dev
+
+
+def _background(background_image, height, width, device, strict=True):
+    if background_image is None:
+        return None
+    bg = background_image.to(device=device, dtype=torch.float32)
+    if bg.shape[2] == 3:
+        if strict:
+            raise NotImplementedError('Background image must have 4 channels, not 3. Add a fourth channel with '
+                                      'all ones via torch.ones().')
+        bg = torch.cat((bg, torch.ones(bg.shape[0], bg.shape[1], 1, device=device)), dim=2)
+    bg = bg.contiguous()
+    assert bg.shape[0] == height and bg.shape[1] == width and bg.shape[2] == 4
+    return bg
+
+
+def _render_args(packed, width, height, nsx, nsy, seed, arena, bg, eval_positions, flags=0):
+    n_eval = 0 if eval_positions is None else int(eval_positions.shape[0])
+    return _native.RenderArgs(int(width), int(height), int(nsx), int(nsy), int(seed) & (2 ** 64 - 1),
+                              1 if packed.use_prefiltering else 0, n_eval, arena.data_ptr(),
+                              None if bg is None else bg.data_ptr(),
+                              None if n_eval == 0 else eval_positions.data_ptr(), int(flags))
+
+
+def _eval_positions(packed, device):
+    ev = packed.eval_positions
+    if ev is None or ev.numel() == 0:
+        return None
+    return ev.to(device=device, dtype=torch.float32).reshape(-1, 2).contiguous()
+
+
+class RenderFunction(torch.autograd.Function):
+    """The PyTorch interface of the renderer (render_pytorch.py:18-868)."""
+
+    @staticmethod
+    def serialize_scene(canvas_width, canvas_height, shapes, shape_groups,
+                        filter=None, output_type=OutputType.color, use_prefiltering=False,
+                        eval_positions=None):
+        """Flattens a scene into RenderFunction.apply's argument list, in the
+        reference's order (render_pytorch.py:22-172)."""
+        if filter is None:
+            filter = PixelFilter(type=FilterType.box, radius=torch.tensor(0.5))
+        if eval_positions is None:
+            eval_positions = torch.tensor([])
+        args = [canvas_width, canvas_height, len(shapes), len(shape_groups), output_type, use_prefiltering,
+                eval_positions]
+        for shp in shapes:
+            use_thickness = False
+            if isinstance(shp, _shape.Circle) or type(shp).__name__ == 'Circle':
+                args += [ShapeType.circle, shp.radius, shp.center]
+            elif isinstance(shp, _shape.Ellipse) or type(shp).__name__ == 'Ellipse':
+                args += [ShapeType.ellipse, shp.radius, shp.center]
+            elif isinstance(shp, _shape.Path) or type(shp).__name__ == 'Path':
+                assert shp.points.shape[1] == 2
+                assert torch.isfinite(shp.points).all()
+                args += [ShapeType.path, shp.num_control_points.to(torch.int32), shp.points]
+                sw = shp.stroke_width
+                if len(sw.shape) > 0 and sw.shape[0] > 1:
+                    assert torch.isfinite(sw).all()
+                    use_thickness = True
+                    args.append(sw)
+                else:
+                    args.append(None)
+                args += [shp.is_closed, getattr(shp, 'use_distance_approx', False)]
+            elif isinstance(shp, _shape.Polygon) or type(shp).__name__ == 'Polygon':
+                assert shp.points.shape[1] == 2
+                n = shp.points.shape[0] if shp.is_closed else shp.points.shape[0] - 1
+                args += [ShapeType.path, torch.zeros(n, dtype=torch.int32), shp.points, None, shp.is_closed, False]
+            elif isinstance(shp, _shape.Rect) or type(shp).__name__ == 'Rect':
+                args += [ShapeType.rect, shp.p_min, shp.p_max]
+            else:
+                raise TypeError('unknown shape type %r' % type(shp))
+            args.append(torch.tensor(0.0) if use_thickness else shp.stroke_width)
+        for grp in shape_groups:
+            args.append(grp.shape_ids.to(torch.int32))
+            for paint in (grp.fill_color, grp.stroke_color):
+                if paint is None:
+                    args.append(None)
+                elif isinstance(paint, torch.Tensor):
+                    args += [ColorType.constant, paint]
+                elif hasattr(paint, 'begin'):
+                    args += [ColorType.linear_gradient, paint.begin, paint.end, paint.offsets, paint.stop_colors]
+                elif hasattr(paint, 'center'):
+                    args += [ColorType.radial_gradient, paint.center, paint.radius, paint.offsets, paint.stop_colors]
+                else:
+                    raise TypeError('unknown paint type %r' % type(paint))
+                if paint is grp.fill_color and paint is not None:
+                    for sid in grp.shape_ids.tolist():
+                        s = shapes[sid]
+                        if type(s).__name__ == 'Path' and not s.is_closed:
+                            warnings.warn('Detected non-closed paths with fill color. This might causes '
+                                          'unexpected results.', Warning)
+            args.append(grp.use_even_odd_rule)
+            args.append(grp.shape_to_canvas.contiguous())
+        args.append(filter.type)
+        args.append(filter.radius)
+        return args
+
+    @staticmethod
+    def forward(ctx, width, height, num_samples_x, num_samples_y, seed, background_image, *args):
+        device = _render_device()
+        packed = pack_scene(args)
+        scene = _native_scene(packed, device)
+        arena = packed.param_arena(device).contiguous()
+        ev = _eval_positions(packed, device)
+        if packed.output_type == OutputType.color:
+            assert ev is None, 'eval_positions apply to the sdf output only'
+            out = torch.empty(height, width, 4, device=device)
+        else:
+            out = torch.empty((height, width, 1) if ev is None else (ev.shape[0], 1), device=device)
+        bg = _background(background_image, out.shape[0], out.shape[1], device)
+        token = next(_token)
+        rargs = _render_args(packed, width, height, num_samples_x, num_samples_y, seed, arena, bg, ev)
+        stream = torch.cuda.current_stream(device).cuda_stream
+        with torch.cuda.device(device):
+            if packed.output_type == OutputType.color:
+                scene.forward(rargs, image_ptr=out.data_ptr(), stream=stream)
+            else:
+                scene.forward(rargs, sdf_ptr=out.data_ptr(), stream=stream)
+        scene.last_token = token
+        ctx.packed = packed
+        ctx.scene = scene
+        ctx.arena = arena
+        ctx.token = token
+        ctx.background_image = bg
+        ctx.bg_requested = background_image is not None
+        ctx.eval_positions = ev
+        ctx.dims = (width, height, num_samples_x, num_samples_y, seed)
+        ctx.device = device
+        ctx.num_args = len(args)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_img):
+        packed, scene, device = ctx.packed, ctx.scene, ctx.device
+        width, height, nsx, nsy, seed = ctx.dims
+        grad = grad_img.to(device=device, dtype=torch.float32).contiguous()
+        d_arena = torch.zeros(max(packed.num_params, 1), device=device)
+        bg = ctx.background_image
+        d_bg = torch.zeros_like(bg) if bg is not None else None
+        flags = _native.DVG_FLAG_REUSE_PREP if scene.last_token == ctx.token else 0
+        rargs = _render_args(packed, width, height, nsx, nsy, seed, ctx.arena, bg, ctx.eval_positions, flags)
+        stream = torch.cuda.current_stream(device).cuda_stream
+        with torch.cuda.device(device):
+            if packed.output_type == OutputType.color:
+                scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
+                               d_background_ptr=None if d_bg is None else d_bg.data_ptr(), stream=stream)
+            else:
+                scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(), stream=stream)
+        scene.last_token = ctx.token
+        d_args = [None] * ctx.num_args
+        for slot, t in zip(packed.slots, packed.tensors):
+            if not slot.differentiable:
+                continue
+            g = d_arena[slot.offset:slot.offset + slot.numel].reshape(slot.shape)
+            d_args[slot.arg_index] = g.to(device=t.device, dtype=t.dtype) if isinstance(t, torch.Tensor) else g
+        return (None, None, None, None, None, d_bg if ctx.bg_requested else None) + tuple(d_args)
+
+    @staticmethod
+    def render_grad(grad_img, width, height, num_samples_x, num_samples_y, seed, background_image, *args):
+        """Gradient of <grad_img, render> with respect to a screen-space
+        translation of every pixel's content: a [H, W, 2] image
+        (render_pytorch.py:430-666)."""
+        device = _render_device()
+        packed = pack_scene(args)
+        scene = _native_scene(packed, device)
+        arena = packed.param_arena(device).contiguous()
+        ev = _eval_positions(packed, device)
+        grad = grad_img.to(device=device, dtype=torch.float32).contiguous()
+        if packed.output_type == OutputType.color:
+            assert grad.shape[2] == 4
+        else:
+            assert grad.shape[2] == 1
+        bg = _background(background_image, height, width, device, strict=False)
+        d_translation = torch.zeros(height, width, 2, device=device)
+        d_arena = torch.zeros(max(packed.num_params, 1), device=device)
+        rargs = _render_args(packed, width, height, num_samples_x, num_samples_y, seed, arena, bg, ev)
+        stream = torch.cuda.current_stream(device).cuda_stream
+        with torch.cuda.device(device):
+            if packed.output_type == OutputType.color:
+                scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
+                               d_translation_ptr=d_translation.data_ptr(), stream=stream)
+            else:
+                scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
+                               d_translation_ptr=d_translation.data_ptr(), stream=stream)
+        scene.last_token = None
+        return d_translation

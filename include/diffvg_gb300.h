@@ -121,7 +121,21 @@ typedef struct DvgRenderArgs {
   const float *params;           /* [num_params] parameter arena             */
   const float *background;       /* [height*width*4] or NULL                 */
   const float *eval_positions;   /* [num_eval_positions*2] or NULL           */
+  int32_t flags;                 /* DVG_FLAG_* bits                          */
 } DvgRenderArgs;
+
+/* DvgRenderArgs.flags.
+ * DVG_FLAG_NO_SYNC: return right after enqueueing the work on the stream;
+ *   device-side failures (fragment-list capacity, unsupported input, tile
+ *   list overflow) are latched in the scene and reported by the next call
+ *   without this flag or by dvg_scene_sync().  Without the flag every call
+ *   waits for its stream, like the reference (diffvg.cpp:1639-1641).
+ * DVG_FLAG_REUSE_PREP: the parameter values are those of the previous call
+ *   on this scene, so the derived scene data (boxes, CDFs, tile lists) is
+ *   reused instead of recomputed (the autograd backward right after its
+ *   forward). */
+#define DVG_FLAG_NO_SYNC 1
+#define DVG_FLAG_REUSE_PREP 2
 
 typedef struct DvgScene DvgScene;
 
@@ -152,6 +166,27 @@ int dvg_render_backward(DvgScene *scene, const DvgRenderArgs *args,
                         const float *d_image, const float *d_sdf,
                         float *d_params, float *d_background,
                         float *d_translation, void *stream);
+
+/* Waits for `stream` and reports any failure latched by calls made with
+ * DVG_FLAG_NO_SYNC since the last check; clears the latch.  A tile-list
+ * overflow grows the lists and returns DVG_ERR_CAPACITY: the affected calls
+ * produced no gradient and must be repeated.  No reference counterpart (the
+ * reference is synchronous). */
+int dvg_scene_sync(DvgScene *scene, void *stream);
+
+/* Per-kernel GPU time of the calls on a scene, measured with CUDA events
+ * recorded on the call's stream around each kernel (no reference
+ * counterpart; the reference only has a wall-clock print_timing flag,
+ * render_pytorch.py:8-12).  dvg_scene_profile(scene, 1) clears the table
+ * and starts recording, 0 stops; dvg_scene_profile_read() waits for the
+ * recorded events and returns one entry per kernel that ran. */
+typedef struct DvgKernelTime {
+  const char *name;              /* prepare, weight, sample_fwd, resolve, sample_bwd, bg_combine, edge, sdf */
+  int64_t launches;
+  double total_ms;
+} DvgKernelTime;
+int dvg_scene_profile(DvgScene *scene, int enable);
+int dvg_scene_profile_read(DvgScene *scene, DvgKernelTime *out, int max_entries, int *num_entries);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *dvg_last_error(void);

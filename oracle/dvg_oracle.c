@@ -74,6 +74,11 @@ static inline float dot4(v4 a, v4 b) { return a.x * b.x + a.y * b.y + a.z * b.z 
 static inline float rmin(float a, float b) { return a < b ? a : b; }
 static inline float rmax(float a, float b) { return a > b ? a : b; }
 static inline float sq(float x) { return x * x; }
+/* The reference's unqualified cos / sin calls on float arguments bind to the
+ * double-precision libm functions (the CPU build imports cos / sin / sincos),
+ * so the argument is widened and the result stays double until stored. */
+static inline double dcos(float x) { return cos((double)x); }
+static inline double dsin(float x) { return sin((double)x); }
 
 static inline box2 box_empty(void) { box2 b; b.lo = V2(INFINITY, INFINITY); b.hi = V2(-INFINITY, -INFINITY); return b; }
 /* merge(box, p) (aabb.h:15-20) */
@@ -1732,15 +1737,15 @@ static v2 sample_shape_boundary(const Scene *S, int s, float t, v2 *normal, floa
   float sr = stroke_width(S, s);
   if (kind == DVG_CIRCLE) {
     float r = p[0]; v2 c = V2(p[1], p[2]);
-    v2 off = V2(r * cosf(2 * (float)M_PI * t), r * sinf(2 * (float)M_PI * t));
+    v2 off = V2((float)(r * dcos(2 * (float)M_PI * t)), (float)(r * dsin(2 * (float)M_PI * t)));
     *normal = normalize2(off);
     *pdf /= (2 * (float)M_PI * r);
     return perturb(add2(c, off), normal, dir, sr);
   } else if (kind == DVG_ELLIPSE) {
     v2 r = V2(p[0], p[1]), c = V2(p[2], p[3]);
-    v2 off = V2(r.x * cosf(2 * (float)M_PI * t), r.y * sinf(2 * (float)M_PI * t));
-    float dxdt = -r.x * sinf(2 * (float)M_PI * t) * 2 * (float)M_PI;
-    float dydt = r.y * cosf(2 * (float)M_PI * t) * 2 * (float)M_PI;
+    v2 off = V2((float)(r.x * dcos(2 * (float)M_PI * t)), (float)(r.y * dsin(2 * (float)M_PI * t)));
+    float dxdt = (float)(-r.x * dsin(2 * (float)M_PI * t) * 2 * (float)M_PI);
+    float dydt = (float)(r.y * dcos(2 * (float)M_PI * t) * 2 * (float)M_PI);
     *normal = normalize2(V2(dydt, -dxdt));
     *pdf /= sqrtf(sq(dxdt) + sq(dydt));
     return perturb(add2(c, off), normal, dir, sr);
@@ -1785,14 +1790,14 @@ static v2 sample_shape_boundary(const Scene *S, int s, float t, v2 *normal, floa
       if (th >= 0) { r0 = P[th]; r1 = P[th + np - 1]; }
       if (dir < 0) {
         v2 p0 = path_pt(S, s, 0);
-        v2 off = V2(r0 * cosf(2 * (float)M_PI * t), r0 * sinf(2 * (float)M_PI * t));
+        v2 off = V2((float)(r0 * dcos(2 * (float)M_PI * t)), (float)(r0 * dsin(2 * (float)M_PI * t)));
         *normal = normalize2(off);
         *pdf /= (2 * (float)M_PI * r0);
         bd->base_point_id = 0; bd->point_id = 0; bd->t = 0;
         return add2(p0, off);
       } else {
         v2 p0 = path_pt(S, s, np - 1);
-        v2 off = V2(r1 * cosf(2 * (float)M_PI * t), r1 * sinf(2 * (float)M_PI * t));
+        v2 off = V2((float)(r1 * dcos(2 * (float)M_PI * t)), (float)(r1 * dsin(2 * (float)M_PI * t)));
         *normal = normalize2(off);
         *pdf /= (2 * (float)M_PI * r1);
         bd->base_point_id = nseg - 1;
@@ -1918,8 +1923,8 @@ static void accumulate_boundary_gradient(const Scene *S, int g, int s, float con
     gadd(G, po + 0, contrib);
   } else if (kind == DVG_ELLIPSE) {
     gadd(G, po + 2, normal.x * contrib); gadd(G, po + 3, normal.y * contrib);
-    gadd(G, po + 0, cosf(2 * (float)M_PI * t) * normal.x * contrib);
-    gadd(G, po + 1, sinf(2 * (float)M_PI * t) * normal.y * contrib);
+    gadd(G, po + 0, (float)(dcos(2 * (float)M_PI * t) * normal.x * contrib));
+    gadd(G, po + 1, (float)(dsin(2 * (float)M_PI * t) * normal.y * contrib));
   } else if (kind == DVG_PATH) {
     int i0 = bd->point_id;
     float tt = bd->t;
