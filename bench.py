@@ -208,7 +208,7 @@ def run_ours(args):
     def step():
         scene.forward(fwd_args, image_ptr=img.data_ptr(), stream=sptr)
         torch.sub(img, target, out=d_img)
-        torch.sum(d_img * d_img, out=loss_buf)
+        loss_buf.copy_(torch.sum(d_img * d_img))
         d_img.mul_(scale)
         d_params.zero_()
         scene.backward(bwd_args, d_image_ptr=d_img.data_ptr(), d_params_ptr=d_params.data_ptr(), stream=sptr)

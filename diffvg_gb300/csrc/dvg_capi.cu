@@ -63,7 +63,7 @@ struct DvgScene {
   int4 *g_tile_range = nullptr;
   unsigned *err = nullptr;  // [0] status bits, [1] tile-list length
   // image-sized arenas
-  DevBuf weight, samples, dbg_val, dbg_flag;
+  DevBuf weight, samples, dbg_val, dbg_flag, edge;
   unsigned *h_status = nullptr;  // pinned mirror of err[0..1]
   bool prepared = false;
   // per-kernel timing (dvg_scene_profile)
@@ -293,6 +293,28 @@ int prepare(DvgScene *sc, const DevScene &S, const DvgRenderArgs *a, cudaStream_
   return DVG_OK;
 }
 
+size_t edge_bytes(DvgScene *sc, size_t n) {
+  size_t T = (size_t)sc->tiles_x * sc->tiles_y;
+  return carve_size({n * sizeof(float4), n * sizeof(float4), n * sizeof(int4), n * sizeof(float2), n * sizeof(int),
+                     n * sizeof(int), n * sizeof(int), T * sizeof(int), (T + 1) * sizeof(int)});
+}
+
+EdgeRecords edge_records(DvgScene *sc, size_t n) {
+  size_t T = (size_t)sc->tiles_x * sc->tiles_y;
+  char *p = reinterpret_cast<char *>(sc->edge.ptr);
+  EdgeRecords E;
+  E.a = carve<float4>(p, n);
+  E.b = carve<float4>(p, n);
+  E.c = carve<int4>(p, n);
+  E.d = carve<float2>(p, n);
+  E.key = carve<int>(p, n);
+  E.rank = carve<int>(p, n);
+  E.order = carve<int>(p, n);
+  E.tile_count = carve<int>(p, T);
+  E.tile_start = carve<int>(p, T + 1);
+  return E;
+}
+
 // Waits for the stream and maps the device status word to a DvgStatus.
 // Returns 1 when the tile lists overflowed and were grown (the caller
 // repeats the call).
@@ -447,6 +469,7 @@ int dvg_scene_destroy(DvgScene *sc) {
   sc->samples.release();
   sc->dbg_val.release();
   sc->dbg_flag.release();
+  sc->edge.release();
   if (sc->h_status) cudaFreeHost(sc->h_status);
   for (auto &p : sc->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   for (auto ev : sc->event_pool) cudaEventDestroy(ev);
@@ -576,6 +599,7 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
   cudaError_t e = sc->weight.ensure(npx * sizeof(float));
   if (e == cudaSuccess && d_background) e = sc->dbg_val.ensure(n * sizeof(float4));
   if (e == cudaSuccess && d_background) e = sc->dbg_flag.ensure(n * sizeof(int));
+  if (e == cudaSuccess && d_image && !a->use_prefiltering) e = sc->edge.ensure(edge_bytes(sc, n));
   if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
   for (int attempt = 0; attempt < 3; attempt++) {
     DevScene S = make_dev(sc, a->params);
@@ -591,7 +615,10 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
       timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
       timed(sc, K_SAMPLE_BWD, s, [&] { dvg::launch_sample_bwd(S, R, dbg_val, dbg_flag, s); });
       if (d_background) timed(sc, K_BG_COMBINE, s, [&] { dvg::launch_bg_combine(S, R, dbg_val, dbg_flag, s); });
-      if (!a->use_prefiltering) timed(sc, K_EDGE, s, [&] { dvg::launch_edge(S, R, s); });
+      if (!a->use_prefiltering) {
+        EdgeRecords E = edge_records(sc, n);
+        timed(sc, K_EDGE, s, [&] { dvg::launch_edge(S, R, E, s); });
+      }
     } else {
       timed(sc, K_SDF, s, [&] {
         dvg::launch_sdf(S, R, a->num_eval_positions > 0 ? a->eval_positions : nullptr, a->num_eval_positions,

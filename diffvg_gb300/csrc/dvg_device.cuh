@@ -77,6 +77,17 @@ struct DevRender {
   int filter_radius_off;
 };
 
+// Boundary samples filed by canvas tile (edge-sampling pass), n entries
+// each; tile_count / tile_start have one entry per canvas tile (+1).
+struct EdgeRecords {
+  float4 *a;        // boundary point (normalised canvas), normal
+  float4 *b;        // local point, pdf, t
+  int4 *c;          // group, shape, segment, first point
+  float2 *d;        // segment t, is_stroke
+  int *key, *rank, *order;
+  int *tile_count, *tile_start;
+};
+
 typedef float2 v2;
 
 #define DI __device__ __forceinline__
@@ -483,8 +494,181 @@ DI float quintic_root(const Quintic &q, float lb, float ub) {
   return t;
 }
 
-// 1: within, 0: not, -1: the path reports "not within" (approx quadratics)
-DI int within_segment(const DevScene &S, int s, int po, int np, int th, int flags, int nc, int i0, v2 pt, float r) {
+// ---------------------------------------------------------------------------
+// Conservative fp32 distance bounds that skip fp64 root solves whose outcome
+// is already decided.  A Bezier curve lies in the convex hull of its control
+// points, and the hull lies in the capsule of radius max_i dist(p_i, chord)
+// around the chord p0-pn, so
+//     dist(pt, curve) >= dist(pt, chord) - max_i dist(p_i, chord).
+// Splitting at t = 1/2 (de Casteljau) shrinks the capsule radius 4x per
+// level; two levels are tried.  far_margin() covers the fp32 rounding of the
+// bound and of the reference's own fp32 distance evaluation, so a segment
+// reported far is one on which the reference's test fails as well.
+DI v2 mid2(v2 a, v2 b) { return V2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y)); }
+DI float dist_to_seg(v2 a, v2 b, v2 p) {
+  v2 ab = sub2(b, a);
+  float l2 = dot2(ab, ab);
+  float t = l2 > 0.f ? clampf_(dot2(sub2(p, a), ab) / l2, 0.f, 1.f) : 0.f;
+  return len2(sub2(add2(a, scl2(t, ab)), p));
+}
+DI float far_margin(float m) { return 1e-5f * m + 1e-4f; }
+DI float absmax2(v2 a) { return fmaxf(fabsf(a.x), fabsf(a.y)); }
+DI float cubic_lb(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
+  return dist_to_seg(p0, p3, pt) - fmaxf(dist_to_seg(p0, p3, p1), dist_to_seg(p0, p3, p2));
+}
+DI bool cubic_half_far(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float thr) {
+  if (cubic_lb(p0, p1, p2, p3, pt) > thr) return true;
+  v2 a01 = mid2(p0, p1), a12 = mid2(p1, p2), a23 = mid2(p2, p3);
+  v2 b0 = mid2(a01, a12), b1 = mid2(a12, a23), c = mid2(b0, b1);
+  return cubic_lb(p0, a01, b0, c, pt) > thr && cubic_lb(c, b1, a23, p3, pt) > thr;
+}
+// true when every point of the cubic is farther than thr from pt
+DI bool cubic_far(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float thr) {
+  if (cubic_lb(p0, p1, p2, p3, pt) > thr) return true;
+  v2 a01 = mid2(p0, p1), a12 = mid2(p1, p2), a23 = mid2(p2, p3);
+  v2 b0 = mid2(a01, a12), b1 = mid2(a12, a23), c = mid2(b0, b1);
+  return cubic_half_far(p0, a01, b0, c, pt, thr) && cubic_half_far(c, b1, a23, p3, pt, thr);
+}
+DI float quad_lb(v2 p0, v2 p1, v2 p2, v2 pt) { return dist_to_seg(p0, p2, pt) - dist_to_seg(p0, p2, p1); }
+DI bool quad_far(v2 p0, v2 p1, v2 p2, v2 pt, float thr) {
+  if (quad_lb(p0, p1, p2, pt) > thr) return true;
+  v2 a01 = mid2(p0, p1), a12 = mid2(p1, p2), c = mid2(a01, a12);
+  if (quad_lb(p0, a01, c, pt) > thr && quad_lb(c, a12, p2, pt) > thr) return true;
+  v2 l1 = mid2(p0, a01), l2 = mid2(a01, c), lc = mid2(l1, l2);
+  v2 r1 = mid2(c, a12), r2 = mid2(a12, p2), rc = mid2(r1, r2);
+  return quad_lb(p0, l1, lc, pt) > thr && quad_lb(lc, l2, c, pt) > thr && quad_lb(c, r1, rc, pt) > thr &&
+         quad_lb(rc, r2, p2, pt) > thr;
+}
+
+// Certified fp32 stroke classification of one Bezier segment.  The segment
+// is subdivided (stackless depth-first walk of the binary subdivision tree,
+// sub-pieces from blossoms of the original control points) and a piece whose
+// capsule bound is farther than r_out + m is pruned.  Returns 0 when every
+// piece is pruned: no point of the curve is within the stroke radius, so the
+// reference's candidates (end points and quintic roots, all on the curve)
+// fail its test as well.  Otherwise returns -2 and the caller runs the
+// reference's fp64 root solve.
+//   An inside proof (a curve point closer than r - m) is available through
+// r_in > 0 but is not used by the renderer: the reference's quintic root
+// isolation can miss the closest root (two roots in one isolation interval)
+// and then reports "outside" for a sample that is geometrically inside, and
+// the renderer reproduces the reference, not the geometry.
+#define DVG_SUBDIV_DEPTH 8
+DI v2 lerp2(v2 a, v2 b, float u) { return V2(a.x + u * (b.x - a.x), a.y + u * (b.y - a.y)); }
+DI v2 cubic_blossom(v2 p0, v2 p1, v2 p2, v2 p3, float u, float v, float w) {
+  v2 a0 = lerp2(p0, p1, u), a1 = lerp2(p1, p2, u), a2 = lerp2(p2, p3, u);
+  v2 b0 = lerp2(a0, a1, v), b1 = lerp2(a1, a2, v);
+  return lerp2(b0, b1, w);
+}
+DI v2 quad_blossom(v2 p0, v2 p1, v2 p2, float u, float v) {
+  return lerp2(lerp2(p0, p1, u), lerp2(p1, p2, u), v);
+}
+DI int cubic_stroke_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float r_in, float r_out, float m) {
+  float thr_out = r_out + m;
+  float in = r_in - m;
+  float in2 = in > 0.f ? in * in : -1.f;
+  unsigned node = 1;
+  for (int guard = 0; guard < (2 << DVG_SUBDIV_DEPTH) + 2; guard++) {
+    int d = 31 - __clz(node);
+    float scale = __int_as_float((127 - d) << 23);  // 2^-d, exact
+    float ta = (float)(node - (1u << d)) * scale, tb = ta + scale;
+    v2 q0 = cubic_blossom(p0, p1, p2, p3, ta, ta, ta), q3 = cubic_blossom(p0, p1, p2, p3, tb, tb, tb);
+    if (distsq2(q0, pt) < in2 || distsq2(q3, pt) < in2) return 1;
+    v2 q1 = cubic_blossom(p0, p1, p2, p3, ta, ta, tb), q2 = cubic_blossom(p0, p1, p2, p3, ta, tb, tb);
+    if (cubic_lb(q0, q1, q2, q3, pt) <= thr_out) {
+      if (d >= DVG_SUBDIV_DEPTH) return -2;
+      node <<= 1;
+      continue;
+    }
+    while (node & 1u) node >>= 1;
+    if (node == 0u) return 0;
+    node += 1;
+  }
+  return -2;
+}
+DI int quad_stroke_fast(v2 p0, v2 p1, v2 p2, v2 pt, float r_in, float r_out, float m) {
+  float thr_out = r_out + m;
+  float in = r_in - m;
+  float in2 = in > 0.f ? in * in : -1.f;
+  unsigned node = 1;
+  for (int guard = 0; guard < (2 << DVG_SUBDIV_DEPTH) + 2; guard++) {
+    int d = 31 - __clz(node);
+    float scale = __int_as_float((127 - d) << 23);
+    float ta = (float)(node - (1u << d)) * scale, tb = ta + scale;
+    v2 q0 = quad_blossom(p0, p1, p2, ta, ta), q2 = quad_blossom(p0, p1, p2, tb, tb);
+    if (distsq2(q0, pt) < in2 || distsq2(q2, pt) < in2) return 1;
+    v2 q1 = quad_blossom(p0, p1, p2, ta, tb);
+    if (quad_lb(q0, q1, q2, pt) <= thr_out) {
+      if (d >= DVG_SUBDIV_DEPTH) return -2;
+      node <<= 1;
+      continue;
+    }
+    while (node & 1u) node >>= 1;
+    if (node == 0u) return 0;
+    node += 1;
+  }
+  return -2;
+}
+
+// Root-solve part of the stroke test of one quadratic (nc = 1) or cubic
+// (nc = 2) segment, for a point whose end-point checks failed: the
+// quadratic's cubic and the cubic's distance quintic, solved as the
+// reference does (within_distance.h:95-118, 150-272).  Out of line: it is
+// the one fp64-heavy routine, shared by every caller.
+static __device__ __noinline__ int segment_root_test(const DevScene &S, int po, int np, int th, int nc, int i0, v2 pt,
+                                              float r) {
+  if (nc == 1) {
+    int i1 = i0 + 1, i2 = (i0 + 2) % np;
+    v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2);
+    float r0 = r, r1 = r, r2 = r;
+    if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); }
+    v2 v = add2(sub2(p0, scl2(2, p1)), p2), w = add2(neg2(p0), p1);
+    float A = sum2(mul2(v, v));
+    float B = sum2(mul2(scl2(3, v), w));
+    float C = sum2(add2(mul2(scl2(2, w), w), mul2(v, sub2(p0, pt))));
+    float D = sum2(mul2(w, sub2(p0, pt)));
+    float t[3];
+    int n = solve_cubic_f(A, B, C, D, t);
+    for (int j = 0; j < n; j++) {
+      if (t[j] >= 0 && t[j] <= 1) {
+        float tt = 1 - t[j];
+        float rr = (tt * tt) * r0 + (2 * tt * t[j]) * r1 + (t[j] * t[j]) * r2;
+        if (distsq2(eval_quad(p0, p1, p2, t[j]), pt) < rr * rr) return 1;
+      }
+    }
+    return 0;
+  }
+  int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
+  v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2), p3 = path_pt(S, po, i3);
+  float r0 = r, r1 = r, r2 = r, r3 = r;
+  if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); r3 = pget(S, th + i3); }
+  Quintic q = cubic_quintic(p0, p1, p2, p3, pt);
+  float iv[4];
+  int ni = quintic_intervals(q, iv);
+  float lower = 0.f;
+  for (int j = 0; j < ni + 1; j++) {
+    if (j < ni && iv[j] < 0.f) continue;
+    float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
+    float lb = lower, ub = upper;
+    double lbe = quintic_eval(q, lb), ube = quintic_eval(q, ub);
+    if (lbe * ube > 0) continue;
+    if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
+    float t = quintic_root(q, lb, ub);
+    float tt = 1 - t;
+    float rr = (tt * tt * tt) * r0 + (3 * tt * tt * t) * r1 + (3 * tt * t * t) * r2 + (t * t * t) * r3;
+    if (distsq2(eval_cubic(p0, p1, p2, p3, t), pt) < rr * rr) return 1;
+    if (upper >= 1.f) break;
+    lower = upper;
+  }
+  return 0;
+}
+
+// Cheap part of the stroke test of one segment (within_distance.h:20-272):
+// lines exactly, quadratic / cubic end points exactly, then the fp32
+// outside proof.  1: within, 0: not, -1: the path reports "not within"
+// (distance-approximated quadratics), 2: undecided, the root solve
+// (segment_root_test) decides.
+DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, int nc, int i0, v2 pt, float r) {
   if (nc == 0) {
     int i1 = (i0 + 1) % np;
     v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1);
@@ -506,21 +690,8 @@ DI int within_segment(const DevScene &S, int s, int po, int np, int th, int flag
     if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); }
     if (distsq2(eval_quad(p0, p1, p2, 0), pt) < r0 * r0) return 1;
     if (distsq2(eval_quad(p0, p1, p2, 1), pt) < r2 * r2) return 1;
-    v2 v = add2(sub2(p0, scl2(2, p1)), p2), w = add2(neg2(p0), p1);
-    float A = sum2(mul2(v, v));
-    float B = sum2(mul2(scl2(3, v), w));
-    float C = sum2(add2(mul2(scl2(2, w), w), mul2(v, sub2(p0, pt))));
-    float D = sum2(mul2(w, sub2(p0, pt)));
-    float t[3];
-    int n = solve_cubic_f(A, B, C, D, t);
-    for (int j = 0; j < n; j++) {
-      if (t[j] >= 0 && t[j] <= 1) {
-        float tt = 1 - t[j];
-        float rr = (tt * tt) * r0 + (2 * tt * t[j]) * r1 + (t[j] * t[j]) * r2;
-        if (distsq2(eval_quad(p0, p1, p2, t[j]), pt) < rr * rr) return 1;
-      }
-    }
-    return 0;
+    float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(absmax2(p2), absmax2(pt)));
+    return quad_stroke_fast(p0, p1, p2, pt, 0.f, fmaxf(r0, fmaxf(r1, r2)), far_margin(m)) == 0 ? 0 : 2;
   }
   int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
   v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2), p3 = path_pt(S, po, i3);
@@ -528,25 +699,15 @@ DI int within_segment(const DevScene &S, int s, int po, int np, int th, int flag
   if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); r3 = pget(S, th + i3); }
   if (distsq2(eval_cubic(p0, p1, p2, p3, 0), pt) < r0 * r0) return 1;
   if (distsq2(eval_cubic(p0, p1, p2, p3, 1), pt) < r3 * r3) return 1;
-  Quintic q = cubic_quintic(p0, p1, p2, p3, pt);
-  float iv[4];
-  int ni = quintic_intervals(q, iv);
-  float lower = 0.f;
-  for (int j = 0; j < ni + 1; j++) {
-    if (j < ni && iv[j] < 0.f) continue;
-    float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
-    float lb = lower, ub = upper;
-    double lbe = quintic_eval(q, lb), ube = quintic_eval(q, ub);
-    if (lbe * ube > 0) continue;
-    if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
-    float t = quintic_root(q, lb, ub);
-    float tt = 1 - t;
-    float rr = (tt * tt * tt) * r0 + (3 * tt * tt * t) * r1 + (3 * tt * t * t) * r2 + (t * t * t) * r3;
-    if (distsq2(eval_cubic(p0, p1, p2, p3, t), pt) < rr * rr) return 1;
-    if (upper >= 1.f) break;
-    lower = upper;
-  }
-  return 0;
+  float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
+  return cubic_stroke_fast(p0, p1, p2, p3, pt, 0.f, fmaxf(fmaxf(r0, r1), fmaxf(r2, r3)), far_margin(m)) == 0 ? 0 : 2;
+}
+
+// 1: within, 0: not, -1: the path reports "not within" (approx quadratics)
+DI int within_segment(const DevScene &S, int s, int po, int np, int th, int flags, int nc, int i0, v2 pt, float r) {
+  int f = within_segment_pre(S, po, np, th, flags, nc, i0, pt, r);
+  if (f == 2) f = segment_root_test(S, po, np, th, nc, i0, pt, r);
+  return f;
 }
 
 DI bool within_shape(const DevScene &S, int s, v2 pt, float r) {
@@ -635,6 +796,8 @@ DI bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
         cp = quad_closest_approx(p0, p1, p2, pt, &t_root);
         dist = dist2(cp, pt);
       } else {
+        float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(absmax2(p2), absmax2(pt)));
+        if (quad_far(p0, p1, p2, pt, min_dist + far_margin(m))) continue;  // cannot improve the best
         v2 pt0 = eval_quad(p0, p1, p2, 0), pt1 = eval_quad(p0, p1, p2, 1);
         float d0 = dist2(pt0, pt), d1 = dist2(pt1, pt);
         dist = d0; cp = pt0; t_root = 0;
@@ -657,6 +820,10 @@ DI bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
     } else {
       v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, i0 + 2),
          p3 = path_pt(S, po, (i0 + 3) % np);
+      {
+        float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
+        if (cubic_far(p0, p1, p2, p3, pt, min_dist + far_margin(m))) continue;  // cannot improve the best
+      }
       v2 pt0 = eval_cubic(p0, p1, p2, p3, 0), pt1 = eval_cubic(p0, p1, p2, p3, 1);
       float d0 = dist2(pt0, pt), d1 = dist2(pt1, pt);
       dist = d0; cp = pt0; t_root = 0;

@@ -25,7 +25,7 @@ void launch_resolve(const DevRender &R, const float4 *samples, float *image, cud
 void launch_sample_bwd(const DevScene &S, const DevRender &R, float4 *dbg_val, int *dbg_flag, cudaStream_t st);
 void launch_bg_combine(const DevScene &S, const DevRender &R, const float4 *dbg_val, const int *dbg_flag,
                        cudaStream_t st);
-void launch_edge(const DevScene &S, const DevRender &R, cudaStream_t st);
+void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st);
 // Signed distance output (forward: sdf, backward: d_sdf).
 void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
                 const float *d_sdf, cudaStream_t st);

@@ -234,24 +234,45 @@ __global__ void k_group_prep(DevScene S, int4 *g_tile_range) {
 }
 
 // Boundary-length CDF over (group, shape) pairs in group order, normalised
-// (scene.cpp:207-246).  One thread: the running sum keeps the reference's
-// summation order.
+// (scene.cpp:207-246).  The running sum keeps the reference's sequential
+// summation order: the block stages the lengths in shared memory and one
+// thread accumulates them; normalisation is parallel.
 __global__ void k_sampling_cdf(DevScene S) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ float buf[1024];
+  __shared__ float carry;
+  __shared__ int bad;
   int nt = S.num_total;
-  float cdf = 0.f;
-  for (int k = 0; k < nt; k++) {
-    float len = S.s_length[S.smp_shape[k]];
-    cdf = (k == 0) ? len : len + cdf;
-    S.smp_cdf[k] = cdf;
-    S.smp_pmf[k] = len;
+  if (threadIdx.x == 0) { carry = 0.f; bad = 0; }
+  for (int base = 0; base < nt; base += 1024) {
+    int m = min(1024, nt - base);
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) buf[j] = S.s_length[S.smp_shape[base + j]];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float cdf = carry;
+      for (int j = 0; j < m; j++) {
+        float len = buf[j];
+        cdf = (base + j == 0) ? len : len + cdf;
+        buf[j] = cdf;
+      }
+      carry = cdf;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+      S.smp_cdf[base + j] = buf[j];
+      S.smp_pmf[base + j] = S.s_length[S.smp_shape[base + j]];
+    }
   }
-  if (nt > 0) {
-    float norm = cdf;
-    if (norm <= 0) { atomicOr(S.err, DVG_EFLAG_SCENE_ZERO); return; }
-    if (!isfinite(norm)) { atomicOr(S.err, DVG_EFLAG_SCENE_NAN); return; }
-    for (int i = 0; i < nt; i++) { S.smp_cdf[i] /= norm; S.smp_pmf[i] /= norm; }
+  __syncthreads();
+  if (nt <= 0) return;
+  float norm = carry;
+  if (threadIdx.x == 0) {
+    if (norm <= 0) { atomicOr(S.err, DVG_EFLAG_SCENE_ZERO); bad = 1; }
+    else if (!isfinite(norm)) { atomicOr(S.err, DVG_EFLAG_SCENE_NAN); bad = 1; }
   }
+  __syncthreads();
+  if (bad) return;
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) { S.smp_cdf[i] /= norm; S.smp_pmf[i] /= norm; }
 }
 
 __device__ __forceinline__ bool tile_hit(int4 r, int tx, int ty) {
@@ -341,7 +362,7 @@ cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4
   if (G > 0) k_group_xform<<<(G + 127) / 128, 128, 0, st>>>(S);
   if (NS > 0) k_shape_prep<<<(NS + 63) / 64, 64, 0, st>>>(S);
   if (G > 0) k_group_prep<<<(G + 127) / 128, 128, 0, st>>>(S, g_tile_range);
-  k_sampling_cdf<<<1, 32, 0, st>>>(S);
+  k_sampling_cdf<<<1, 256, 0, st>>>(S);
   k_bin_count<<<T, 128, 0, st>>>(S, g_tile_range, tile_count);
   k_bin_scan<<<1, 1024, 0, st>>>(S, tile_count, tile_cap, bin_total);
   k_bin_fill<<<T, 128, 0, st>>>(S, g_tile_range);

@@ -58,17 +58,21 @@ __global__ void __launch_bounds__(256) k_weight(DevRender R0, DevScene S) {
 
 template <bool PREFILTER>
 __global__ void __launch_bounds__(256) k_sample_fwd(DevScene S, DevRender R, float4 *samples) {
+  __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
   int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
   int px = tx * DVG_TILE + (threadIdx.x & (DVG_TILE - 1)), py = ty * DVG_TILE + (threadIdx.x / DVG_TILE);
-  if (px >= R.w || py >= R.h) return;
-  int idx = (py * R.w + px) * R.spp + blockIdx.y;
+  bool active = px < R.w && py < R.h;
+  if (PREFILTER && !active) return;
+  int idx = active ? (py * R.w + px) * R.spp + blockIdx.y : 0;
   int x, y;
   v2 pt = sample_pos(R, idx, PREFILTER, x, y);
   v2 npt = V2(pt.x / R.w, pt.y / R.h);
   const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
-  float4 c = PREFILTER ? sample_color_prefiltered_fwd(S, bg, npt) : sample_color_fwd(S, bg, npt, nullptr);
-  samples[idx] = c;
+  float4 c;
+  if (PREFILTER) c = sample_color_prefiltered_fwd(S, bg, npt);
+  else c = sample_color_fwd(S, bg, npt, nullptr, active, &wq[threadIdx.x >> 5], threadIdx.x & 31);
+  if (active) samples[idx] = c;
 }
 
 // filtered pixel colour from the sample colours around it
@@ -111,25 +115,32 @@ __device__ __forceinline__ float block_sum(float v) {
 // interior adjoint (render_kernel with d_render_image, diffvg.cpp:1160-1268)
 template <bool PREFILTER>
 __global__ void __launch_bounds__(256) k_sample_bwd(DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
+  __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
   DevRender R = load_filter(R0, nullptr);
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
   int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
   int px = tx * DVG_TILE + (threadIdx.x & (DVG_TILE - 1)), py = ty * DVG_TILE + (threadIdx.x / DVG_TILE);
   bool active = px < R.w && py < R.h && !bins_overflowed(S);
   float dfr = 0.f;
+  int idx = active ? (py * R.w + px) * R.spp + blockIdx.y : 0;
+  int x, y;
+  v2 pt = sample_pos(R, idx, PREFILTER, x, y);
+  v2 npt = V2(pt.x / R.w, pt.y / R.h);
+  float4 d_color = active ? gather_d_color(R, pt) : F4(0, 0, 0, 0);
+  const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
+  float4 dbg = F4(0, 0, 0, 0);
+  int assign = 0;
+  float *d_tr = R.d_translation ? R.d_translation + 2 * (y * R.w + x) : nullptr;
+  float4 *dbgp = R.d_background ? &dbg : nullptr;
+  float4 color;
+  if (PREFILTER) {
+    color = active ? sample_color_prefiltered_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params)
+                   : F4(0, 0, 0, 0);
+  } else {
+    color = sample_color_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params, active, &wq[threadIdx.x >> 5],
+                             threadIdx.x & 31);
+  }
   if (active) {
-    int idx = (py * R.w + px) * R.spp + blockIdx.y;
-    int x, y;
-    v2 pt = sample_pos(R, idx, PREFILTER, x, y);
-    v2 npt = V2(pt.x / R.w, pt.y / R.h);
-    float4 d_color = gather_d_color(R, pt);
-    const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
-    float4 dbg = F4(0, 0, 0, 0);
-    int assign = 0;
-    float *d_tr = R.d_translation ? R.d_translation + 2 * (y * R.w + x) : nullptr;
-    float4 *dbgp = R.d_background ? &dbg : nullptr;
-    float4 color = PREFILTER ? sample_color_prefiltered_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params)
-                             : sample_color_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params);
     if (R.d_background) { dbg_val[idx] = dbg; dbg_flag[idx] = assign; }
     // d filter radius (diffvg.cpp:1250-1268)
     for (int dy = -R.ri; dy <= R.ri; dy++)
@@ -166,14 +177,22 @@ __global__ void k_bg_combine(DevScene S, DevRender R, const float4 *dbg_val, con
   *dst = v;
 }
 
-// boundary adjoint (sample_boundary_kernel + render_edge_kernel,
-// diffvg.cpp:1325-1475); the reference's Morton sort of the boundary samples
-// only reorders atomics and is not needed for the result.
-__global__ void __launch_bounds__(256) k_edge(DevScene S, DevRender R0) {
-  DevRender R = load_filter(R0, nullptr);
+// Boundary adjoint (sample_boundary_kernel + render_edge_kernel,
+// diffvg.cpp:1325-1475) in three passes:
+//   k_edge_sample  draws every boundary sample (same pcg streams and CDFs as
+//                  the reference) and files it under its canvas tile;
+//   k_edge_order   turns the per-tile counts into a tile-sorted order;
+//   k_edge_eval    evaluates the two sides of each boundary point in tile
+//                  order, so that a warp's samples share a candidate list.
+// The reference sorts its boundary samples by Morton code for the same
+// coherence (diffvg.cpp:1594-1599); the order only changes the order of the
+// gradient atomics.
+__global__ void __launch_bounds__(256) k_edge_sample(DevScene S, DevRender R, EdgeRecords E) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   int n = R.w * R.h * R.spp;
-  if (idx >= n || S.num_total <= 0 || bins_overflowed(S)) return;
+  if (idx >= n) return;
+  E.key[idx] = -1;
+  if (S.num_total <= 0 || bins_overflowed(S)) return;
   Pcg rng = pcg_init(idx, R.seed);
   float u = pcg_float(rng);
   int sid = cdf_sample(S.smp_cdf, S.num_total, u, nullptr);
@@ -198,11 +217,72 @@ __global__ void __launch_bounds__(256) k_edge(DevScene S, DevRender R0) {
   pdf = pmf * pdf;
   int bx = (int)(bpt.x * R.w), by = (int)(bpt.y * R.h);
   if (bx < 0 || bx >= R.w || by < 0 || by >= R.h) return;
+  // canvas tile of the boundary point (clamped into the grid)
+  float cx = bpt.x * S.W, cy = bpt.y * S.H;
+  int tx = min(max((int)floorf(cx / DVG_TILE), 0), S.tiles_x - 1);
+  int ty = min(max((int)floorf(cy / DVG_TILE), 0), S.tiles_y - 1);
+  int key = ty * S.tiles_x + tx;
+  E.key[idx] = key;
+  E.rank[idx] = atomicAdd(&E.tile_count[key], 1);
+  E.a[idx] = F4(bpt.x, bpt.y, normal.x, normal.y);
+  E.b[idx] = F4(lpt.x, lpt.y, pdf, t);
+  E.c[idx] = make_int4(g, s, bd.base_point_id, bd.point_id);
+  E.d[idx] = make_float2(bd.t, (float)bd.is_stroke);
+}
+
+// exclusive scan of the per-tile sample counts (one block of 1024 threads)
+__global__ void k_edge_scan(DevScene S, EdgeRecords E) {
+  int T = S.tiles_x * S.tiles_y;
+  __shared__ int part[1024];
+  int per = (T + blockDim.x - 1) / blockDim.x;
+  int lo = threadIdx.x * per, hi = min(lo + per, T);
+  int sum = 0;
+  for (int i = lo; i < hi; i++) sum += E.tile_count[i];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+    int v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = threadIdx.x > 0 ? part[threadIdx.x - 1] : 0;
+  for (int i = lo; i < hi; i++) {
+    E.tile_start[i] = run;
+    run += E.tile_count[i];
+  }
+  if (threadIdx.x == 0) E.tile_start[T] = part[blockDim.x - 1];
+}
+
+__global__ void k_edge_order(EdgeRecords E, int n) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  int key = E.key[idx];
+  if (key >= 0) E.order[E.tile_start[key] + E.rank[idx]] = idx;
+}
+
+__global__ void __launch_bounds__(256) k_edge_eval(DevScene S, DevRender R0, EdgeRecords E) {
+  __shared__ WarpQueue wq[8];
+  DevRender R = load_filter(R0, nullptr);
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int T = S.tiles_x * S.tiles_y;
+  bool active = i < E.tile_start[T] && !bins_overflowed(S);
+  int idx = active ? E.order[i] : 0;
+  float4 a = active ? E.a[idx] : F4(0.5f, 0.5f, 1.f, 0.f), b = active ? E.b[idx] : F4(0, 0, 1, 0);
+  int4 c = active ? E.c[idx] : make_int4(0, 0, 0, 0);
+  float2 d = active ? E.d[idx] : make_float2(0.f, 0.f);
+  v2 bpt = V2(a.x, a.y), normal = V2(a.z, a.w), lpt = V2(b.x, b.y);
+  float pdf = b.z, t = b.w;
+  int g = c.x, s = c.y;
+  BData bd = {c.z, c.w, d.x, d.y != 0.f ? 1 : 0};
+  int bx = min(max((int)(bpt.x * R.w), 0), R.w - 1), by = min(max((int)(bpt.y * R.h), 0), R.h - 1);
   EdgeQ qin = {g, s, 0}, qout = {g, s, 0};
   const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (by * R.w + bx) : nullptr;
-  float4 cin = sample_color_fwd(S, bg, sub2(bpt, scl2(1e-4f, normal)), &qin);
-  float4 cout = sample_color_fwd(S, bg, add2(bpt, scl2(1e-4f, normal)), &qout);
-  if (!qin.hit && !qout.hit) return;
+  WarpQueue *q = &wq[threadIdx.x >> 5];
+  int lane = threadIdx.x & 31;
+  float4 cin = sample_color_fwd(S, bg, sub2(bpt, scl2(1e-4f, normal)), &qin, active, q, lane);
+  float4 cout = sample_color_fwd(S, bg, add2(bpt, scl2(1e-4f, normal)), &qout, active, q, lane);
+  if (!active || (!qin.hit && !qout.hit)) return;
   if (!qin.hit) {
     normal = neg2(normal);
     float4 tmp = cin; cin = cout; cout = tmp;
@@ -272,8 +352,13 @@ void launch_bg_combine(const DevScene &S, const DevRender &R, const float4 *dbg_
                        cudaStream_t st) {
   k_bg_combine<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(S, R, dbg_val, dbg_flag);
 }
-void launch_edge(const DevScene &S, const DevRender &R, cudaStream_t st) {
-  k_edge<<<blocks_of((long long)R.w * R.h * R.spp), 256, 0, st>>>(S, R);
+void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
+  long long n = (long long)R.w * R.h * R.spp;
+  cudaMemsetAsync(E.tile_count, 0, sizeof(int) * S.tiles_x * S.tiles_y, st);
+  k_edge_sample<<<blocks_of(n), 256, 0, st>>>(S, R, E);
+  k_edge_scan<<<1, 1024, 0, st>>>(S, E);
+  k_edge_order<<<blocks_of(n), 256, 0, st>>>(E, (int)n);
+  k_edge_eval<<<blocks_of(n), 256, 0, st>>>(S, R, E);
 }
 void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
                 const float *d_sdf, cudaStream_t st) {

@@ -58,39 +58,191 @@ DI float4 finish_color(float4 acc) {
   return acc;
 }
 
-// Forward colour of one sample (sample_color, diffvg.cpp:525-655).  With an
-// EdgeQuery the hit flag follows the reference's rule: the last fragment
-// that is either of the queried group (sets it) or opaque (clears it)
-// decides; without such a fragment the flag keeps what the coverage tests
-// of the queried shape set (diffvg.cpp:624-633).
-DI float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq) {
-  if (eq) eq->hit = 0;
-  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+// ---------------------------------------------------------------------------
+// Warp-batched root solves.  Each lane first runs the cheap part of every
+// stroke test of its sample (exact end-point and line checks, fp32 outside
+// proofs); segments that stay undecided become jobs in the warp's queue in
+// shared memory.  The warp then solves all queued jobs together, one job per
+// lane, so the fp64 root solves run with full warps instead of the few lanes
+// whose sample happens to sit near a curve.  Each lane finally blends its
+// fragments in group order with the solved results.  Every lane of the warp
+// must call the batched functions (inactive lanes pass active = false).
+#define DVG_LANE_JOBS 8
+struct SegJob { int shape, seg; float x, y, r; };
+struct WarpQueue {
+  SegJob job[32][DVG_LANE_JOBS];
+  unsigned result[32];
+  int offs[33];
+};
+
+// candidate fragment of a sample: key = 2 * group + is_stroke; meta bit 31
+// = decided hit, else bits 0-7 / 8-15 = the lane's job range whose results
+// decide it
+struct FragRef { int key, meta; };
+#define DVG_META_HIT (1 << 31)
+
+DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
+  const unsigned full = 0xffffffffu;
+  int incl = njobs;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int v = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += v;
+  }
+  int total = __shfl_sync(full, incl, 31);
+  q->offs[lane] = incl - njobs;
+  if (lane == 31) q->offs[32] = total;
+  q->result[lane] = 0u;
+  __syncwarp();
+  for (int j = lane; j < total; j += 32) {
+    int lo = 0, hi = 31;  // owner: last lane with offs <= j
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (q->offs[mid] <= j) lo = mid; else hi = mid - 1;
+    }
+    int idx = j - q->offs[lo];
+    SegJob jb = q->job[lo][idx];
+    int s = jb.shape;
+    int hit = segment_root_test(S, SI(S, s, DVG_SHAPE_PARAM_OFF), SI(S, s, DVG_SHAPE_NUM_POINTS),
+                                SI(S, s, DVG_SHAPE_THICKNESS_OFF), __ldg(&S.segment_ctrl[jb.seg]),
+                                __ldg(&S.seg_point[jb.seg]), V2(jb.x, jb.y), jb.r);
+    if (hit) atomicOr(&q->result[lo], 1u << idx);
+  }
+  __syncwarp();
+}
+
+// Stroke test of one shape with undecided path segments queued.
+// 1: hit, 0: miss, 2: pending on the jobs [njobs_before, njobs).
+DI int shape_stroke_status(const DevScene &S, int s, v2 lp, float r, WarpQueue *q, int lane, int &njobs,
+                           unsigned *mark) {
+  int kind = SI(S, s, DVG_SHAPE_KIND);
+  int flags = kind == DVG_PATH ? SI(S, s, DVG_SHAPE_FLAGS) : 0;
+  if (kind != DVG_PATH || (flags & 2)) return within_shape(S, s, lp, r) ? 1 : 0;
+  int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF);
+  int np = SI(S, s, DVG_SHAPE_NUM_POINTS), th = SI(S, s, DVG_SHAPE_THICKNESS_OFF);
+  int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
+  int lo = njobs;
+  for (int k = 0; k < nseg; k++) {
+    int seg = S.seg_order[so + k];
+    if (nseg > 1 && !box_in_r(S.seg_box[so + seg], lp, S.seg_r[so + seg])) continue;
+    int nc = __ldg(&S.segment_ctrl[so + seg]), i0 = __ldg(&S.seg_point[so + seg]);
+    int f = within_segment_pre(S, po, np, th, flags, nc, i0, lp, r);
+    if (f == 2) {
+      if (njobs < DVG_LANE_JOBS) {
+        q->job[lane][njobs] = SegJob{s, so + seg, lp.x, lp.y, r};
+        if (mark) *mark |= 1u << njobs;
+        njobs++;
+        continue;
+      }
+      f = segment_root_test(S, po, np, th, nc, i0, lp, r);  // queue full: solve now
+    }
+    if (f == 1) {
+      if (mark) *mark &= (1u << lo) - 1u;
+      njobs = lo;  // decided: drop this shape's queued jobs
+      return 1;
+    }
+  }
+  return njobs > lo ? 2 : 0;
+}
+
+// group_stroke (within_distance.h:355-446) with queued segments; for the
+// group of an edge query every shape is tested and the queried shape's jobs
+// are marked in eq_jobs.
+DI int group_stroke_status(const DevScene &S, int g, v2 pt, WarpQueue *q, int lane, int &njobs, EdgeQ *eq,
+                           unsigned &eq_jobs) {
+  v2 lp = xform_pt(S.c2s + 9 * g, pt);
+  int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
+  bool is_eq = eq && eq->group == g;
+  int lo = njobs;
+  bool ret = false;
+  for (int k = 0; k < nsh; k++) {
+    int s = __ldg(&S.group_shapes[off + k]);
+    float r = stroke_width(S, s);
+    if (nsh > 1 && !box_in_r(S.s_box[s], lp, r)) continue;
+    int st = shape_stroke_status(S, s, lp, r, q, lane, njobs, (is_eq && s == eq->shape) ? &eq_jobs : nullptr);
+    if (st == 1) {
+      if (!is_eq) {
+        njobs = lo;
+        return 1;
+      }
+      ret = true;
+      if (s == eq->shape) eq->hit = 1;
+    }
+  }
+  if (ret) return 1;
+  return njobs > lo ? 2 : 0;
+}
+
+// Pass 1 of a sample: candidate fragments in group order, undecided stroke
+// segments queued.  Returns the number of candidate fragments (capped).
+DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q, int lane, int &njobs, EdgeQ *eq,
+                         unsigned &eq_jobs, bool &overflow) {
   int b, e;
   bool list = cand_range(S, pt, b, e);
-  float4 acc = bg ? *bg : F4(0, 0, 0, 0);
-  int nf = 0, ev = -1;
+  int nf = 0;
   int G = S.num_groups;
   for (int k = b; k < e; k++) {
     int g = list ? __ldg(&S.tile_list[k]) : k;
     if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
     int sk = GI(S, g, DVG_GROUP_STROKE_KIND), fk = GI(S, g, DVG_GROUP_FILL_KIND);
-    if (sk != DVG_PAINT_NONE && group_stroke(S, g, pt, eq)) {
-      float4 c = paint_color(S, sk, GI(S, g, DVG_GROUP_STROKE_OFF), GI(S, g, DVG_GROUP_STROKE_STOPS), pt);
-      if (eq) ev = (eq->group == g) ? 1 : (c.w >= 1.f ? 0 : ev);
-      blend(acc, c);
-      nf++;
+    if (sk != DVG_PAINT_NONE) {
+      int lo = njobs;
+      int st = group_stroke_status(S, g, pt, q, lane, njobs, eq, eq_jobs);
+      if (st != 0) {
+        if (nf < DVG_MAX_FRAGMENTS) frags[nf++] = FragRef{2 * g + 1, st == 1 ? DVG_META_HIT : (lo | (njobs << 8))};
+        else overflow = true;
+      }
     }
     if (fk != DVG_PAINT_NONE && group_inside(S, g, pt, eq)) {
-      float4 c = paint_color(S, fk, GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS), pt);
-      if (eq) ev = (eq->group == g) ? 1 : (c.w >= 1.f ? 0 : ev);
-      blend(acc, c);
-      nf++;
+      if (nf < DVG_MAX_FRAGMENTS) frags[nf++] = FragRef{2 * g, DVG_META_HIT};
+      else overflow = true;
     }
   }
-  if (nf > DVG_MAX_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
+  return nf;
+}
+
+DI bool frag_hit(int meta, unsigned res) {
+  if (meta & DVG_META_HIT) return true;
+  int lo = meta & 255, hi = (meta >> 8) & 255;
+  unsigned mask = (hi - lo >= 32) ? 0xffffffffu : ((1u << (hi - lo)) - 1u);
+  return ((res >> lo) & mask) != 0u;
+}
+
+// Forward colour of one sample (sample_color, diffvg.cpp:525-655).  With an
+// EdgeQuery the hit flag follows the reference's rule: the last fragment
+// that is either of the queried group (sets it) or opaque (clears it)
+// decides; without such a fragment the flag keeps what the coverage tests
+// of the queried shape set (diffvg.cpp:624-633).
+DI float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq, bool active, WarpQueue *q,
+                           int lane) {
+  FragRef frags[DVG_MAX_FRAGMENTS];
+  int nf = 0, njobs = 0;
+  unsigned eq_jobs = 0;
+  bool overflow = false;
+  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+  if (eq) eq->hit = 0;
+  if (active) nf = collect_fragments(S, pt, frags, q, lane, njobs, eq, eq_jobs, overflow);
+  warp_solve(S, q, lane, njobs);
+  if (!active) return F4(0, 0, 0, 0);
+  unsigned res = q->result[lane];
+  if (eq && (res & eq_jobs)) eq->hit = 1;
+  float4 acc = bg ? *bg : F4(0, 0, 0, 0);
+  int nhit = 0, ev = -1;
+  for (int i = 0; i < nf; i++) {
+    if (!frag_hit(frags[i].meta, res)) continue;
+    int g = frags[i].key >> 1;
+    float4 c = (frags[i].key & 1)
+                   ? paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
+                                 GI(S, g, DVG_GROUP_STROKE_STOPS), pt)
+                   : paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF),
+                                 GI(S, g, DVG_GROUP_FILL_STOPS), pt);
+    if (eq) ev = (eq->group == g) ? 1 : (c.w >= 1.f ? 0 : ev);
+    blend(acc, c);
+    nhit++;
+  }
+  if (overflow || nhit > DVG_MAX_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
   if (eq && ev >= 0) eq->hit = ev;
-  if (nf <= 0) return bg ? *bg : F4(0, 0, 0, 0);
+  if (nhit <= 0) return bg ? *bg : F4(0, 0, 0, 0);
   return finish_color(acc);
 }
 
@@ -99,42 +251,39 @@ DI float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, Ed
 // *assign = 1 when the sample has no fragment (the reference then
 // overwrites the pixel's background gradient with d_color).
 DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color, float4 *d_bg,
-                           int *assign, float *d_tr, float *dp) {
+                           int *assign, float *d_tr, float *dp, bool active, WarpQueue *q, int lane) {
+  FragRef frags[DVG_MAX_FRAGMENTS];
+  int nf = 0, njobs = 0;
+  unsigned eq_jobs = 0;
+  bool overflow = false;
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
-  int b, e;
-  bool list = cand_range(S, pt, b, e);
+  if (active) nf = collect_fragments(S, pt, frags, q, lane, njobs, nullptr, eq_jobs, overflow);
+  warp_solve(S, q, lane, njobs);
+  if (!active) return F4(0, 0, 0, 0);
+  if (overflow) {
+    flag_error(S, DVG_EFLAG_CAPACITY);
+    return F4(0, 0, 0, 0);
+  }
+  unsigned res = q->result[lane];
   float4 cols[DVG_MAX_FRAGMENTS];
   float4 accs[DVG_MAX_FRAGMENTS];
   int keys[DVG_MAX_FRAGMENTS];
   float4 first = bg ? *bg : F4(0, 0, 0, 0);
   float4 acc = first;
-  int nf = 0;
-  bool overflow = false;
-  int G = S.num_groups;
-  for (int k = b; k < e && !overflow; k++) {
-    int g = list ? __ldg(&S.tile_list[k]) : k;
-    if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
-    int sk = GI(S, g, DVG_GROUP_STROKE_KIND), fk = GI(S, g, DVG_GROUP_FILL_KIND);
-    if (sk != DVG_PAINT_NONE && group_stroke(S, g, pt, nullptr)) {
-      if (nf >= DVG_MAX_FRAGMENTS) { overflow = true; break; }
-      float4 c = paint_color(S, sk, GI(S, g, DVG_GROUP_STROKE_OFF), GI(S, g, DVG_GROUP_STROKE_STOPS), pt);
-      blend(acc, c);
-      cols[nf] = c; accs[nf] = acc; keys[nf] = 2 * g + 1;
-      nf++;
-    }
-    if (fk != DVG_PAINT_NONE && group_inside(S, g, pt, nullptr)) {
-      if (nf >= DVG_MAX_FRAGMENTS) { overflow = true; break; }
-      float4 c = paint_color(S, fk, GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS), pt);
-      blend(acc, c);
-      cols[nf] = c; accs[nf] = acc; keys[nf] = 2 * g;
-      nf++;
-    }
+  int nh = 0;
+  for (int i = 0; i < nf; i++) {
+    if (!frag_hit(frags[i].meta, res)) continue;
+    int g = frags[i].key >> 1;
+    float4 c = (frags[i].key & 1)
+                   ? paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
+                                 GI(S, g, DVG_GROUP_STROKE_STOPS), pt)
+                   : paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF),
+                                 GI(S, g, DVG_GROUP_FILL_STOPS), pt);
+    blend(acc, c);
+    cols[nh] = c; accs[nh] = acc; keys[nh] = frags[i].key;
+    nh++;
   }
-  if (overflow) {
-    flag_error(S, DVG_EFLAG_CAPACITY);
-    return F4(0, 0, 0, 0);
-  }
-  if (nf <= 0) {
+  if (nh <= 0) {
     if (bg) {
       if (d_bg) { *d_bg = d_color; *assign = 1; }
       return *bg;
@@ -149,7 +298,7 @@ DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, fl
     dca -= (d_color.x * fin.x + d_color.y * fin.y + d_color.z * fin.z) / fa;
     dcr = nr; dcg = ng; dcb = nb;
   }
-  for (int i = nf - 1; i >= 0; i--) {
+  for (int i = nh - 1; i >= 0; i--) {
     float4 f = cols[i];
     float4 p = i > 0 ? accs[i - 1] : first;
     float d_pa = dca * (1.f - f.w);

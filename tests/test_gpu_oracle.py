@@ -60,3 +60,17 @@ def test_fill_scene_prefiltered_small():
 def test_fill_scene_sampled_small():
     from diffvg_gb300 import workloads
     _run(lambda m: workloads.fill_scene(m, seed=3, num_paths=48, canvas=256), 2, 3)
+
+
+def test_stroke_scene_full_size():
+    """The benchmark's stroke-heavy scene at full size (512x512, 2048 paths,
+    2x2 spp): 1,048,576 samples."""
+    from diffvg_gb300 import workloads
+    _run(lambda m: workloads.stroke_scene(m, seed=1), 2, 1)
+
+
+def test_fill_scene_full_size_prefiltered():
+    """The fill-heavy scene at full size (1024x1024, 512 closed paths with
+    constant / linear / radial fills, 10% stroked, prefiltered, 1 spp)."""
+    from diffvg_gb300 import workloads
+    _run(lambda m: workloads.fill_scene(m, seed=3), 1, 3, prefilter=True)
