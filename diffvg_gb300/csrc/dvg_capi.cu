@@ -2,6 +2,7 @@
 // the topology and all scratch arenas resident on the device, and the
 // forward / backward entry points that replace diffvg.Scene + diffvg.render
 // (diffvg.cpp:1477-1649, 1777-1789; scene.cpp:919-1035).
+#include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -9,18 +10,32 @@
 
 #include "dvg_internal.h"
 
-namespace {
+namespace dvg {
 
-thread_local std::string g_last_error;
+// last error of this thread; a fixed buffer, so that reporting an error
+// allocates nothing
+thread_local char g_last_error[512];
 
-int fail(int status, const std::string &msg) {
-  g_last_error = msg;
+int fail(int status, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
   return status;
 }
 
 int cuda_fail(cudaError_t e, const char *what) {
-  return fail(DVG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return fail(DVG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
+
+void clear_error() { g_last_error[0] = 0; }
+
+}  // namespace dvg
+
+namespace {
+
+using dvg::cuda_fail;
+using dvg::fail;
 
 // grow-only device buffer
 struct DevBuf {
@@ -118,7 +133,13 @@ void timed(DvgScene *sc, int kid, cudaStream_t st, F launch) {
   if (a && b) sc->pending.push_back({kid, a, b});
 }
 
-int validate_desc(const DvgSceneDesc *d, std::vector<int> &seg_point) {
+}  // namespace
+
+namespace dvg {
+
+// Host-side checks of a scene description; writes the first point of every
+// path segment to seg_point when it is not NULL.  Allocates nothing.
+int validate_desc(const DvgSceneDesc *d, int *seg_point) {
   if (!d) return fail(DVG_ERR_INVALID, "scene description is NULL");
   if (d->canvas_width <= 0 || d->canvas_height <= 0) return fail(DVG_ERR_INVALID, "canvas size must be positive");
   if (d->num_shapes < 0 || d->num_groups < 0 || d->num_params < 1 || d->total_segments < 0 ||
@@ -130,12 +151,11 @@ int validate_desc(const DvgSceneDesc *d, std::vector<int> &seg_point) {
   if (d->filter_type < DVG_BOX || d->filter_type > DVG_HANN) return fail(DVG_ERR_INVALID, "unknown filter type");
   auto in_params = [&](long long off, long long n) { return off >= 0 && n >= 0 && off + n <= d->num_params; };
   if (!in_params(d->filter_radius_off, 1)) return fail(DVG_ERR_INVALID, "filter radius offset out of range");
-  seg_point.assign((size_t)(d->total_segments > 0 ? d->total_segments : 1), 0);
   for (int s = 0; s < d->num_shapes; s++) {
     const int32_t *si = d->shape_info + (size_t)s * DVG_SHAPE_INFO_STRIDE;
     int kind = si[DVG_SHAPE_KIND], po = si[DVG_SHAPE_PARAM_OFF];
     if (!in_params(si[DVG_SHAPE_STROKE_WIDTH_OFF], 1))
-      return fail(DVG_ERR_INVALID, "shape " + std::to_string(s) + ": stroke width offset out of range");
+      return fail(DVG_ERR_INVALID, "shape %d: stroke width offset out of range", s);
     if (kind == DVG_CIRCLE) {
       if (!in_params(po, 3)) return fail(DVG_ERR_INVALID, "circle parameters out of range");
     } else if (kind == DVG_ELLIPSE || kind == DVG_RECT) {
@@ -144,7 +164,7 @@ int validate_desc(const DvgSceneDesc *d, std::vector<int> &seg_point) {
       int np = si[DVG_SHAPE_NUM_POINTS], nseg = si[DVG_SHAPE_NUM_SEGMENTS], so = si[DVG_SHAPE_SEG_OFF];
       int th = si[DVG_SHAPE_THICKNESS_OFF];
       if (np < 0 || nseg < 0 || so < 0 || (long long)so + nseg > d->total_segments)
-        return fail(DVG_ERR_INVALID, "path " + std::to_string(s) + ": segment range out of bounds");
+        return fail(DVG_ERR_INVALID, "path %d: segment range out of bounds", s);
       if (!in_params(po, 2LL * np)) return fail(DVG_ERR_INVALID, "path points out of range");
       if (th >= 0 && !in_params(th, np)) return fail(DVG_ERR_INVALID, "path thickness out of range");
       if (nseg > 0 && np < 1) return fail(DVG_ERR_INVALID, "path with segments but no points");
@@ -153,18 +173,18 @@ int validate_desc(const DvgSceneDesc *d, std::vector<int> &seg_point) {
         int nc = d->segment_ctrl[so + i];
         if (nc < 0 || nc > 2) return fail(DVG_ERR_INVALID, "num_control_points entries must be 0, 1 or 2");
         if (pid + nc >= np) return fail(DVG_ERR_INVALID, "num_control_points does not fit the number of points");
-        seg_point[(size_t)so + i] = pid;
+        if (seg_point) seg_point[(size_t)so + i] = pid;
         pid += nc + 1;
       }
     } else {
-      return fail(DVG_ERR_INVALID, "unknown shape kind " + std::to_string(kind));
+      return fail(DVG_ERR_INVALID, "unknown shape kind %d", kind);
     }
   }
   for (int g = 0; g < d->num_groups; g++) {
     const int32_t *gi = d->group_info + (size_t)g * DVG_GROUP_INFO_STRIDE;
     int nsh = gi[DVG_GROUP_NUM_SHAPES], off = gi[DVG_GROUP_SHAPES_OFF];
     if (nsh < 1 || off < 0 || (long long)off + nsh > d->total_group_shapes)
-      return fail(DVG_ERR_INVALID, "group " + std::to_string(g) + ": shape list out of range");
+      return fail(DVG_ERR_INVALID, "group %d: shape list out of range", g);
     for (int k = 0; k < nsh; k++) {
       int s = d->group_shapes[off + k];
       if (s < 0 || s >= d->num_shapes) return fail(DVG_ERR_INVALID, "group refers to a shape id out of range");
@@ -186,6 +206,12 @@ int validate_desc(const DvgSceneDesc *d, std::vector<int> &seg_point) {
   }
   return DVG_OK;
 }
+
+}  // namespace dvg
+
+namespace {
+
+using dvg::validate_desc;
 
 DevScene make_dev(DvgScene *sc, const float *params) {
   DevScene S;
@@ -354,16 +380,16 @@ int finish(DvgScene *sc, cudaStream_t st, bool *retry) {
 
 extern "C" {
 
-const char *dvg_last_error(void) { return g_last_error.c_str(); }
+const char *dvg_last_error(void) { return dvg::g_last_error; }
 
 const char *dvg_version(void) { return "diffvg_gb300 0.1 (sm_103a)"; }
 
 int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
-  g_last_error.clear();
+  dvg::clear_error();
   if (!out_scene) return fail(DVG_ERR_INVALID, "out_scene is NULL");
   *out_scene = nullptr;
-  std::vector<int> seg_point;
-  int st = validate_desc(desc, seg_point);
+  std::vector<int> seg_point((size_t)(desc && desc->total_segments > 0 ? desc->total_segments : 1), 0);
+  int st = validate_desc(desc, seg_point.data());
   if (st != DVG_OK) return st;
   DvgScene *sc = new DvgScene();
   sc->d = *desc;
@@ -478,7 +504,7 @@ int dvg_scene_destroy(DvgScene *sc) {
 }
 
 int dvg_scene_profile(DvgScene *sc, int enable) {
-  g_last_error.clear();
+  dvg::clear_error();
   if (!sc) return fail(DVG_ERR_INVALID, "scene is NULL");
   DeviceGuard guard(sc->device);
   for (auto &p : sc->pending) { sc->event_pool.push_back(p.a); sc->event_pool.push_back(p.b); }
@@ -489,7 +515,7 @@ int dvg_scene_profile(DvgScene *sc, int enable) {
 }
 
 int dvg_scene_profile_read(DvgScene *sc, DvgKernelTime *out, int max_entries, int *num_entries) {
-  g_last_error.clear();
+  dvg::clear_error();
   if (!sc || !num_entries) return fail(DVG_ERR_INVALID, "scene / num_entries is NULL");
   DeviceGuard guard(sc->device);
   for (auto &p : sc->pending) {
@@ -519,7 +545,7 @@ int dvg_scene_profile_read(DvgScene *sc, DvgKernelTime *out, int max_entries, in
 }
 
 int dvg_scene_sync(DvgScene *sc, void *stream) {
-  g_last_error.clear();
+  dvg::clear_error();
   if (!sc) return fail(DVG_ERR_INVALID, "scene is NULL");
   DeviceGuard guard(sc->device);
   bool retry = false;
@@ -531,7 +557,7 @@ int dvg_scene_sync(DvgScene *sc, void *stream) {
 }
 
 int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float *sdf, void *stream) {
-  g_last_error.clear();
+  dvg::clear_error();
   int st = check_args(sc, a);
   if (st != DVG_OK) return st;
   if ((image == nullptr) == (sdf == nullptr)) return fail(DVG_ERR_INVALID, "exactly one of image / sdf must be set");
@@ -582,7 +608,7 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
 
 int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_image, const float *d_sdf,
                         float *d_params, float *d_background, float *d_translation, void *stream) {
-  g_last_error.clear();
+  dvg::clear_error();
   int st = check_args(sc, a);
   if (st != DVG_OK) return st;
   if ((d_image == nullptr) == (d_sdf == nullptr)) return fail(DVG_ERR_INVALID, "exactly one of d_image / d_sdf must be set");

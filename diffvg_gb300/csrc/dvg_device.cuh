@@ -540,19 +540,18 @@ DI bool quad_far(v2 p0, v2 p1, v2 p2, v2 pt, float thr) {
          quad_lb(rc, r2, p2, pt) > thr;
 }
 
-// Certified fp32 stroke classification of one Bezier segment.  The segment
-// is subdivided (stackless depth-first walk of the binary subdivision tree,
-// sub-pieces from blossoms of the original control points) and a piece whose
-// capsule bound is farther than r_out + m is pruned.  Returns 0 when every
-// piece is pruned: no point of the curve is within the stroke radius, so the
-// reference's candidates (end points and quintic roots, all on the curve)
-// fail its test as well.  Otherwise returns -2 and the caller runs the
-// reference's fp64 root solve.
-//   An inside proof (a curve point closer than r - m) is available through
-// r_in > 0 but is not used by the renderer: the reference's quintic root
-// isolation can miss the closest root (two roots in one isolation interval)
-// and then reports "outside" for a sample that is geometrically inside, and
-// the renderer reproduces the reference, not the geometry.
+// Certified fp32 outside proof for the stroke test of one Bezier segment.
+// The segment is subdivided (stackless depth-first walk of the binary
+// subdivision tree, sub-pieces from blossoms of the original control points)
+// and a piece whose capsule bound is farther than r_out + m is pruned.
+// Returns 0 when every piece is pruned: no point of the curve is within the
+// stroke radius, so the reference's candidates (end points and quintic
+// roots, all on the curve) fail its test as well.  Returns -2 otherwise,
+// early when a curve point is closer than r_out - m, and the caller runs the
+// reference's fp64 root solve.  No inside proof is attempted: the
+// reference's quintic root isolation can miss the closest root (two roots in
+// one isolation interval) and then reports "outside" for a sample that is
+// geometrically inside; the renderer reproduces the reference.
 #define DVG_SUBDIV_DEPTH 8
 DI v2 lerp2(v2 a, v2 b, float u) { return V2(a.x + u * (b.x - a.x), a.y + u * (b.y - a.y)); }
 DI v2 cubic_blossom(v2 p0, v2 p1, v2 p2, v2 p3, float u, float v, float w) {
@@ -563,17 +562,18 @@ DI v2 cubic_blossom(v2 p0, v2 p1, v2 p2, v2 p3, float u, float v, float w) {
 DI v2 quad_blossom(v2 p0, v2 p1, v2 p2, float u, float v) {
   return lerp2(lerp2(p0, p1, u), lerp2(p1, p2, u), v);
 }
-DI int cubic_stroke_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float r_in, float r_out, float m) {
+DI int cubic_stroke_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float r_out, float m) {
   float thr_out = r_out + m;
-  float in = r_in - m;
-  float in2 = in > 0.f ? in * in : -1.f;
+  float near = r_out - m;
+  float near2 = near > 0.f ? near * near : -1.f;
   unsigned node = 1;
   for (int guard = 0; guard < (2 << DVG_SUBDIV_DEPTH) + 2; guard++) {
     int d = 31 - __clz(node);
     float scale = __int_as_float((127 - d) << 23);  // 2^-d, exact
     float ta = (float)(node - (1u << d)) * scale, tb = ta + scale;
     v2 q0 = cubic_blossom(p0, p1, p2, p3, ta, ta, ta), q3 = cubic_blossom(p0, p1, p2, p3, tb, tb, tb);
-    if (distsq2(q0, pt) < in2 || distsq2(q3, pt) < in2) return 1;
+    // a curve point this close: no outside proof can exist
+    if (distsq2(q0, pt) < near2 || distsq2(q3, pt) < near2) return -2;
     v2 q1 = cubic_blossom(p0, p1, p2, p3, ta, ta, tb), q2 = cubic_blossom(p0, p1, p2, p3, ta, tb, tb);
     if (cubic_lb(q0, q1, q2, q3, pt) <= thr_out) {
       if (d >= DVG_SUBDIV_DEPTH) return -2;
@@ -586,17 +586,17 @@ DI int cubic_stroke_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float r_in, float r_
   }
   return -2;
 }
-DI int quad_stroke_fast(v2 p0, v2 p1, v2 p2, v2 pt, float r_in, float r_out, float m) {
+DI int quad_stroke_fast(v2 p0, v2 p1, v2 p2, v2 pt, float r_out, float m) {
   float thr_out = r_out + m;
-  float in = r_in - m;
-  float in2 = in > 0.f ? in * in : -1.f;
+  float near = r_out - m;
+  float near2 = near > 0.f ? near * near : -1.f;
   unsigned node = 1;
   for (int guard = 0; guard < (2 << DVG_SUBDIV_DEPTH) + 2; guard++) {
     int d = 31 - __clz(node);
     float scale = __int_as_float((127 - d) << 23);
     float ta = (float)(node - (1u << d)) * scale, tb = ta + scale;
     v2 q0 = quad_blossom(p0, p1, p2, ta, ta), q2 = quad_blossom(p0, p1, p2, tb, tb);
-    if (distsq2(q0, pt) < in2 || distsq2(q2, pt) < in2) return 1;
+    if (distsq2(q0, pt) < near2 || distsq2(q2, pt) < near2) return -2;
     v2 q1 = quad_blossom(p0, p1, p2, ta, tb);
     if (quad_lb(q0, q1, q2, pt) <= thr_out) {
       if (d >= DVG_SUBDIV_DEPTH) return -2;
@@ -691,7 +691,7 @@ DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, 
     if (distsq2(eval_quad(p0, p1, p2, 0), pt) < r0 * r0) return 1;
     if (distsq2(eval_quad(p0, p1, p2, 1), pt) < r2 * r2) return 1;
     float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(absmax2(p2), absmax2(pt)));
-    return quad_stroke_fast(p0, p1, p2, pt, 0.f, fmaxf(r0, fmaxf(r1, r2)), far_margin(m)) == 0 ? 0 : 2;
+    return quad_stroke_fast(p0, p1, p2, pt, fmaxf(r0, fmaxf(r1, r2)), far_margin(m)) == 0 ? 0 : 2;
   }
   int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
   v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2), p3 = path_pt(S, po, i3);
@@ -700,7 +700,7 @@ DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, 
   if (distsq2(eval_cubic(p0, p1, p2, p3, 0), pt) < r0 * r0) return 1;
   if (distsq2(eval_cubic(p0, p1, p2, p3, 1), pt) < r3 * r3) return 1;
   float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
-  return cubic_stroke_fast(p0, p1, p2, p3, pt, 0.f, fmaxf(fmaxf(r0, r1), fmaxf(r2, r3)), far_margin(m)) == 0 ? 0 : 2;
+  return cubic_stroke_fast(p0, p1, p2, p3, pt, fmaxf(fmaxf(r0, r1), fmaxf(r2, r3)), far_margin(m)) == 0 ? 0 : 2;
 }
 
 // 1: within, 0: not, -1: the path reports "not within" (approx quadratics)

@@ -7,6 +7,15 @@
 
 namespace dvg {
 
+// Error reporting shared by the C ABI entry points (a thread-local fixed
+// buffer returned by dvg_last_error; printf-style, allocation-free).
+int fail(int status, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+void clear_error();
+// Host-side checks of a scene description; writes the first point of every
+// path segment to seg_point when it is not NULL.
+int validate_desc(const DvgSceneDesc *d, int *seg_point);
+
 // Scene preparation from the parameter arena: transforms, boxes, segment
 // order, boundary CDFs and the per-tile candidate group lists.
 // tile_cap is the capacity of S.tile_list; bin_total receives the list

@@ -213,8 +213,9 @@ DI bool frag_hit(int meta, unsigned res) {
 // that is either of the queried group (sets it) or opaque (clears it)
 // decides; without such a fragment the flag keeps what the coverage tests
 // of the queried shape set (diffvg.cpp:624-633).
-DI float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq, bool active, WarpQueue *q,
-                           int lane) {
+// Out of line: the boundary pass calls it twice per sample.
+static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq,
+                                                      bool active, WarpQueue *q, int lane) {
   FragRef frags[DVG_MAX_FRAGMENTS];
   int nf = 0, njobs = 0;
   unsigned eq_jobs = 0;

@@ -237,11 +237,18 @@ class RenderFunction(torch.autograd.Function):
                 scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(), stream=stream)
         scene.last_token = ctx.token
         d_args = [None] * ctx.num_args
+        # one copy of the gradient arena per destination device, then views
+        arenas = {device: d_arena}
         for slot, t in zip(packed.slots, packed.tensors):
             if not slot.differentiable:
                 continue
-            g = d_arena[slot.offset:slot.offset + slot.numel].reshape(slot.shape)
-            d_args[slot.arg_index] = g.to(device=t.device, dtype=t.dtype) if isinstance(t, torch.Tensor) else g
+            dst = t.device if isinstance(t, torch.Tensor) else device
+            if dst not in arenas:
+                arenas[dst] = d_arena.to(dst)
+            g = arenas[dst][slot.offset:slot.offset + slot.numel].view(slot.shape)
+            if isinstance(t, torch.Tensor) and t.dtype != g.dtype:
+                g = g.to(t.dtype)
+            d_args[slot.arg_index] = g
         return (None, None, None, None, None, d_bg if ctx.bg_requested else None) + tuple(d_args)
 
     @staticmethod

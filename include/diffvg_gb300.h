@@ -188,6 +188,22 @@ typedef struct DvgKernelTime {
 int dvg_scene_profile(DvgScene *scene, int enable);
 int dvg_scene_profile_read(DvgScene *scene, DvgKernelTime *out, int max_entries, int *num_entries);
 
+/* Forward colour render that allocates nothing (no counterpart in the
+ * reference).  For callers that must not allocate device memory: a host
+ * process that owns all GPU memory through its own pool and bars plugins
+ * from cudaMalloc, or a loop that may not allocate once running.  Takes the
+ * scene description with HOST topology arrays (as dvg_scene_create), the
+ * render arguments (device parameter arena, optional device background) and
+ * the device image [height*width*4]; writes the image like
+ * dvg_render_forward.  All scratch (topology copy, derived scene data, tile
+ * lists, weight image, per-sample colours) lives in one static 16 MiB device
+ * array inside the library, held by every GPU that loads it until exit;
+ * calls needing more return DVG_ERR_CAPACITY.  Group shape lists must be
+ * stored in group order (as serialize_scene produces them).  Every call
+ * shares that array: calls that overlap on the GPU race.  The first call on
+ * a device looks up the array's address; make it before any stream capture. */
+int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRenderArgs *args, float *image, void *stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char *dvg_last_error(void);
 
