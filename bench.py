@@ -284,6 +284,8 @@ def run_ours(args):
            'gpu_launches': gpu_launches, 'fwd_ms': round(fwd_ms, 4), 'bwd_ms': round(bwd_ms, 4),
            'kernels_ms_per_launch': {k: round(v[1] / v[0], 4) for k, v in kernels.items()},
            'loss': float(loss_buf.item())}
+    if rank == 0 and not args.no_batched:
+        out['batched'] = run_batched(dev)
     if rank == 0 and not args.no_cpu_baseline:
         out['cpu_baseline'] = cpu_baseline(packed, oracle_params(packed), w, h, nsx, nsy, seed, target.cpu().numpy())
     if rank == 0:
@@ -327,6 +329,76 @@ def run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samp
     return {'value': round(ws * n_samples * k / dt / 1e6, 3), 'unit': UNIT, 'h2d_bytes_per_step': h2d,
             'd2h_bytes_per_step': d2h, 'steps': k, 'ms_per_step': round(dt / k * 1e3, 3),
             'api': 'RenderFunction.serialize_scene + apply + MSE + backward, scene tensors in host memory'}
+
+
+def run_batched(dev, steps=10, warmup=3, plain_steps=2):
+    """The batched workload: 64 stroke scenes (seeds 100-163), canvas sizes
+    drawn from {64,128,256,512}^2, path counts log-uniform in [16, 1024],
+    2x2 spp, each optimised with Adam (lr 1e-2) towards a perturbed render
+    of itself (points N(0, 2 px), colours N(0, 0.05)).  Reports the batched
+    path (one CUDA graph per step) and the plain per-call path
+    (RenderFunction.apply + backward + torch Adam per scene) on the same
+    scenes."""
+    import torch
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import workloads
+    from diffvg_gb300.batch import BatchedScenes
+    seeds = list(range(100, 164))
+    scenes = workloads.batched_scenes(dvg, seeds=seeds)
+    args = [dvg.RenderFunction.serialize_scene(w, h, s, g) for (w, h, s, g) in scenes]
+    b = BatchedScenes(args, seeds=seeds, lr=1e-2, streams=8, check_every=0)
+    targets = [b.render(i, workloads.perturbed_target_params(p, b.scene_params(i), seeds[i]))
+               for i, p in enumerate(b.packed)]
+    b.set_targets(targets)
+    for _ in range(warmup):
+        b.step()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        b.step()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    b.check()
+    ms = e0.elapsed_time(e1) / steps
+    n = b.samples_per_step()
+    out = {'workload': '64 stroke scenes, canvases {64,128,256,512}^2, 16-1024 paths (log-uniform), 2x2 spp, '
+                       'Adam lr 1e-2 towards perturbed self-renders', 'samples_per_step': n,
+           'steps_per_s': round(1e3 / ms, 3), 'ms_per_step': round(ms, 3), 'Msamples_per_s': round(n / ms / 1e3, 3),
+           'graph': 'one CUDA graph per step (forward, MSE gradient, backward per scene on 8 streams; one Adam)'}
+    # plain per-call path on the same scenes and targets
+    params, opts = [], []
+    for (w, h, shapes, groups) in scenes:
+        ps = []
+        for s in shapes:
+            s.points = s.points.to(dev).detach().requires_grad_(True)
+            s.stroke_width = s.stroke_width.to(dev).detach().requires_grad_(True)
+            ps += [s.points, s.stroke_width]
+        for g in groups:
+            g.stroke_color = g.stroke_color.to(dev).detach().requires_grad_(True)
+            ps.append(g.stroke_color)
+        params.append(ps)
+        opts.append(torch.optim.Adam(ps, lr=1e-2))
+
+    def plain_step():
+        for i, (w, h, shapes, groups) in enumerate(scenes):
+            opts[i].zero_grad()
+            a = dvg.RenderFunction.serialize_scene(w, h, shapes, groups)
+            img = dvg.RenderFunction.apply(w, h, 2, 2, seeds[i], None, *a)
+            loss = ((img - targets[i]) ** 2).mean()
+            loss.backward()
+            opts[i].step()
+    plain_step()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(plain_steps):
+        plain_step()
+    torch.cuda.synchronize(dev)
+    pms = (time.perf_counter() - t0) / plain_steps * 1e3
+    out['plain_steps_per_s'] = round(1e3 / pms, 3)
+    out['plain_ms_per_step'] = round(pms, 2)
+    out['speedup_vs_plain'] = round(pms / ms, 2)
+    return out
 
 
 def oracle_params(packed):
@@ -399,6 +471,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=5)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-batched', action='store_true')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)

@@ -26,7 +26,8 @@ DVG_FLAG_NO_SYNC = 1
 DVG_FLAG_REUSE_PREP = 2
 
 EXPORTS = ('dvg_scene_create', 'dvg_scene_destroy', 'dvg_render_forward', 'dvg_render_backward',
-           'dvg_scene_sync', 'dvg_scene_profile', 'dvg_scene_profile_read', 'dvg_last_error', 'dvg_version')
+           'dvg_scene_sync', 'dvg_scene_profile', 'dvg_scene_profile_read', 'dvg_mse_grad', 'dvg_adam_step',
+           'dvg_last_error', 'dvg_version')
 
 
 class KernelTime(ctypes.Structure):
@@ -110,6 +111,13 @@ def load(build_if_missing=True):
         lib.dvg_scene_profile_read.argtypes = [ctypes.c_void_p, ctypes.POINTER(KernelTime), ctypes.c_int,
                                                ctypes.POINTER(ctypes.c_int)]
         lib.dvg_scene_profile_read.restype = ctypes.c_int
+        lib.dvg_mse_grad.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p]
+        lib.dvg_mse_grad.restype = ctypes.c_int
+        lib.dvg_adam_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]
+        lib.dvg_adam_step.restype = ctypes.c_int
         lib.dvg_last_error.argtypes = []
         lib.dvg_last_error.restype = ctypes.c_char_p
         lib.dvg_version.argtypes = []
@@ -184,3 +192,21 @@ class NativeScene:
         n = ctypes.c_int()
         check(self._lib.dvg_scene_profile_read(self.handle, arr, 16, ctypes.byref(n)))
         return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(min(n.value, 16))}
+
+
+def mse_grad(image, target, d_image, loss=None, scale=None, stream=0):
+    """d_image = scale * (image - target) (scale defaults to 2 / numel, the
+    gradient of the mean squared error); loss += sum of squared differences."""
+    n = image.numel() // 4
+    if scale is None:
+        scale = 2.0 / image.numel()
+    check(load().dvg_mse_grad(image.data_ptr(), target.data_ptr(), n, float(scale), d_image.data_ptr(),
+                              None if loss is None else loss.data_ptr(), stream))
+
+
+def adam_step(params, grads, m, v, step, lr, betas=(0.9, 0.999), eps=1e-8, lr_scale=None, stream=0):
+    """Adam update of a flat fp32 parameter tensor on the device; `step` is a
+    one-element int32 device tensor holding the number of steps taken."""
+    check(load().dvg_adam_step(params.data_ptr(), grads.data_ptr(), m.data_ptr(), v.data_ptr(),
+                               None if lr_scale is None else lr_scale.data_ptr(), params.numel(), float(lr),
+                               float(betas[0]), float(betas[1]), float(eps), step.data_ptr(), stream))

@@ -16,7 +16,7 @@ LIB_DIR = os.path.join(HERE, '_lib')
 LIB_PATH = os.path.join(LIB_DIR, 'libdiffvg_gb300.so')
 INCLUDE = os.path.join(os.path.dirname(HERE), 'include')
 
-UNITS = ['dvg_prep.cu', 'dvg_render.cu', 'dvg_capi.cu', 'dvg_static.cu']
+UNITS = ['dvg_prep.cu', 'dvg_render.cu', 'dvg_capi.cu', 'dvg_static.cu', 'dvg_optim.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-std=c++17', '-lineinfo', '--fmad=false', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2',
          '-I' + INCLUDE]

@@ -37,6 +37,7 @@ class ParamSlot:
     numel: int
     shape: tuple
     differentiable: bool  # False: the reference returns None for this slot
+    kind: str = ''        # what the values are: points, thickness, stroke_width, color, ...
 
 
 @dataclass
@@ -98,11 +99,11 @@ def pack_scene(args):
     slots, tensors = [], []
     off = 0
 
-    def add(arg_index, t, differentiable=True):
+    def add(arg_index, t, differentiable=True, kind=''):
         nonlocal off
         t = _as_tensor(t)
         n = t.numel()
-        slots.append(ParamSlot(arg_index, off, n, tuple(t.shape), differentiable))
+        slots.append(ParamSlot(arg_index, off, n, tuple(t.shape), differentiable, kind))
         tensors.append(t)
         off += n
         return off - n
@@ -119,20 +120,20 @@ def pack_scene(args):
             r = _as_tensor(args[i])
             if r.numel() != 1:
                 raise SceneError('circle radius must be a scalar')
-            info[1] = add(i, r); i += 1
+            info[1] = add(i, r, kind='radius'); i += 1
             c = _as_tensor(args[i])
             if c.numel() != 2:
                 raise SceneError('circle center must have 2 elements')
-            add(i, c); i += 1
+            add(i, c, kind='center'); i += 1
         elif kind == ShapeType.ellipse:
             r = _as_tensor(args[i])
             if r.numel() != 2:
                 raise SceneError('ellipse radius must have 2 elements')
-            info[1] = add(i, r); i += 1
+            info[1] = add(i, r, kind='radius'); i += 1
             c = _as_tensor(args[i])
             if c.numel() != 2:
                 raise SceneError('ellipse center must have 2 elements')
-            add(i, c); i += 1
+            add(i, c, kind='center'); i += 1
         elif kind == ShapeType.path:
             ncp = args[i]; i += 1
             ncp = np.asarray(ncp.detach().cpu() if isinstance(ncp, torch.Tensor) else ncp, dtype=np.int64).reshape(-1)
@@ -140,13 +141,13 @@ def pack_scene(args):
             if pts.dim() != 2 or pts.shape[1] != 2:
                 raise SceneError('path points must have shape [N, 2]')
             npts = int(pts.shape[0])
-            info[1] = add(i, pts); i += 1
+            info[1] = add(i, pts, kind='points'); i += 1
             thickness = args[i]
             if thickness is not None:
                 thickness = _as_tensor(thickness)
                 if thickness.numel() != npts:
                     raise SceneError('path thickness must have one entry per point')
-                info[5] = add(i, thickness)
+                info[5] = add(i, thickness, kind='thickness')
             i += 1
             is_closed = bool(args[i]); i += 1
             use_approx = bool(args[i]); i += 1
@@ -168,18 +169,18 @@ def pack_scene(args):
             pmin = _as_tensor(args[i])
             if pmin.numel() != 2:
                 raise SceneError('rect p_min must have 2 elements')
-            info[1] = add(i, pmin); i += 1
+            info[1] = add(i, pmin, kind='corner'); i += 1
             pmax = _as_tensor(args[i])
             if pmax.numel() != 2:
                 raise SceneError('rect p_max must have 2 elements')
-            add(i, pmax); i += 1
+            add(i, pmax, kind='corner'); i += 1
         else:
             raise SceneError('unknown shape type %r' % (kind,))
         sw = _as_tensor(args[i])
         if sw.numel() != 1:
             raise SceneError('stroke_width slot must be a scalar')
         # a thickness path's stroke_width slot is a placeholder (render_pytorch.py:94-95, 775-776)
-        info[7] = add(i, sw, differentiable=(info[5] < 0)); i += 1
+        info[7] = add(i, sw, differentiable=(info[5] < 0), kind='stroke_width'); i += 1
         key.append(('s', kind))
 
     group_info = np.zeros((num_groups, GROUP_INFO_STRIDE), dtype=np.int32)
@@ -197,27 +198,27 @@ def pack_scene(args):
             c = _as_tensor(args[i])
             if c.numel() != 4:
                 raise SceneError('constant colour must have 4 elements')
-            gi[kind_col + 1] = add(i, c); i += 1
+            gi[kind_col + 1] = add(i, c, kind='color'); i += 1
             gi[kind_col + 2] = 0
             return ('c',)
         if ctype in (ColorType.linear_gradient, ColorType.radial_gradient):
             a = _as_tensor(args[i])
             if a.numel() != 2:
                 raise SceneError('gradient begin/center must have 2 elements')
-            gi[kind_col + 1] = add(i, a); i += 1
+            gi[kind_col + 1] = add(i, a, kind='gradient_geometry'); i += 1
             b = _as_tensor(args[i])
             if b.numel() != 2:
                 raise SceneError('gradient end/radius must have 2 elements')
-            add(i, b); i += 1
+            add(i, b, kind='gradient_geometry'); i += 1
             offs = _as_tensor(args[i])
             k = offs.numel()
             if k < 1:
                 raise SceneError('gradient needs at least one stop')
-            add(i, offs); i += 1
+            add(i, offs, kind='stop_offsets'); i += 1
             cols = _as_tensor(args[i])
             if cols.numel() != 4 * k:
                 raise SceneError('gradient stop_colors must have shape [num_stops, 4]')
-            add(i, cols); i += 1
+            add(i, cols, kind='color'); i += 1
             gi[kind_col + 2] = k
             return ('g', ctype, k)
         raise SceneError('unknown colour type %r' % (ctype,))
@@ -239,7 +240,7 @@ def pack_scene(args):
         m = _as_tensor(args[i])
         if m.numel() != 9:
             raise SceneError('shape_to_canvas must be a 3x3 matrix')
-        gi[9] = add(i, m); i += 1
+        gi[9] = add(i, m, kind='transform'); i += 1
         key.append(('g', ids.tobytes(), kf, ks, int(gi[8])))
 
     ftype = _enum_value(args[i]); i += 1
@@ -248,7 +249,7 @@ def pack_scene(args):
     fr = _as_tensor(args[i])
     if fr.numel() != 1:
         raise SceneError('filter radius must be a scalar')
-    filter_radius_off = add(i, fr); i += 1
+    filter_radius_off = add(i, fr, kind='filter_radius'); i += 1
     key.append(('f', ftype))
 
     seg = np.asarray(seg_ctrl, dtype=np.int32)

@@ -100,3 +100,18 @@ def batched_scenes(mod, seeds=range(100, 164), canvases=(64, 128, 256, 512), pat
         out.append(stroke_scene(mod, seed=int(s) * 7919 + 1, num_paths=npaths, canvas=canvas,
                                 step=20.0 * canvas / 512.0))
     return out
+
+
+def perturbed_target_params(packed, params, seed, point_sigma=2.0, color_sigma=0.05):
+    """Parameters of a batched-workload target: the scene's own parameters
+    with points jittered by N(0, point_sigma^2) pixels and colours by
+    N(0, color_sigma^2), colours clamped to [0, 1]."""
+    gen = torch.Generator().manual_seed(int(seed) + 1000003)
+    out = params.detach().cpu().clone()
+    for sl in packed.slots:
+        seg = out[sl.offset:sl.offset + sl.numel]
+        if sl.kind == 'points':
+            seg += point_sigma * torch.randn(sl.numel, generator=gen)
+        elif sl.kind == 'color':
+            seg.copy_((seg + color_sigma * torch.randn(sl.numel, generator=gen)).clamp_(0.0, 1.0))
+    return out

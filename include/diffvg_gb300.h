@@ -188,6 +188,20 @@ typedef struct DvgKernelTime {
 int dvg_scene_profile(DvgScene *scene, int enable);
 int dvg_scene_profile_read(DvgScene *scene, DvgKernelTime *out, int max_entries, int *num_entries);
 
+/* Optimisation-step kernels of the batched / served paths (no reference
+ * counterpart: the reference leaves the loss and the optimiser to PyTorch on
+ * the host side of each call, apps/painterly_rendering.py:146-192).
+ * dvg_mse_grad: d_image = scale * (image - target) over num_pixels RGBA
+ *   pixels, and *loss += sum((image - target)^2) when loss is not NULL.
+ * dvg_adam_step: Adam with bias correction over n parameters; lr_scale
+ *   (NULL = all ones) scales each element's step, 0 freezes it; the step
+ *   count *step lives on the device and is incremented, so a CUDA graph can
+ *   replay the update. */
+int dvg_mse_grad(const float *image, const float *target, int64_t num_pixels, float scale, float *d_image,
+                 float *loss, void *stream);
+int dvg_adam_step(float *params, const float *grads, float *m, float *v, const float *lr_scale, int64_t n,
+                  float lr, float beta1, float beta2, float eps, int *step, void *stream);
+
 /* Forward colour render that allocates nothing (no counterpart in the
  * reference).  For callers that must not allocate device memory: a host
  * process that owns all GPU memory through its own pool and bars plugins
