@@ -286,6 +286,7 @@ def run_ours(args):
            'loss': float(loss_buf.item())}
     if rank == 0 and not args.no_batched:
         out['batched'] = run_batched(dev)
+        out['served'] = run_served(dev)
     if rank == 0 and not args.no_cpu_baseline:
         out['cpu_baseline'] = cpu_baseline(packed, oracle_params(packed), w, h, nsx, nsy, seed, target.cpu().numpy())
     if rank == 0:
@@ -399,6 +400,82 @@ def run_batched(dev, steps=10, warmup=3, plain_steps=2):
     out['plain_ms_per_step'] = round(pms, 2)
     out['speedup_vs_plain'] = round(pms / ms, 2)
     return out
+
+
+def run_served(dev, num_requests=12, rate=20.0, step_range=(10, 30), path_range=(64, 1024), plain_steps=3):
+    """The served workload, scaled down to finish in seconds: requests with
+    canvas {128,256,512}^2, path_range paths of mixed open strokes and closed
+    fills, step_range Adam steps (lr 1e-2) towards a different seeded scene
+    plus N(0, 0.02) pixel noise, Poisson arrivals at `rate` requests/s,
+    admission under a 150 GB device budget.  Reports p50 / p99 per-step
+    latency and aggregate steps/s of the continuous-batching server, and
+    steps/s of the plain per-call path (RenderFunction + torch Adam, one
+    request at a time) on the same requests."""
+    import torch
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import serve, workloads
+    specs = workloads.served_requests(dvg, num_requests, path_range=path_range, step_range=step_range)
+    gen = torch.Generator().manual_seed(7)
+    gaps = torch.empty(num_requests).exponential_(rate, generator=gen).tolist()
+    reqs, scenes = [], []
+    for sp in specs:
+        w, h, shapes, groups = workloads.mixed_scene(dvg, sp['seed'], sp['canvas'], sp['num_paths'])
+        tw, th, ts, tg = workloads.mixed_scene(dvg, sp['target_seed'], sp['canvas'], sp['num_paths'])
+        targs = dvg.RenderFunction.serialize_scene(tw, th, ts, tg)
+        target = workloads.noisy_target(dvg.RenderFunction.apply(tw, th, 2, 2, sp['seed'], None, *targs).detach(),
+                                        sp['seed'])
+        scenes.append((w, h, shapes, groups, target, sp))
+        reqs.append(serve.Request(dvg.RenderFunction.serialize_scene(w, h, shapes, groups), target, sp['steps'],
+                                  seed=sp['seed']))
+    srv = serve.Server(device=dev, memory_budget=150 * 10 ** 9)
+    t0 = time.perf_counter()
+    t = t0
+    for r, g in zip(reqs, gaps):
+        t += g
+        r.arrival = t
+        srv.submit(r)
+    srv.run()
+    st = srv.stats()
+    # plain per-call path, one request at a time, a few steps each
+    done, t_plain, loss_plain = 0, 0.0, None
+    for k, (w, h, shapes, groups, target, sp) in enumerate(scenes):
+        ps = []
+        for sh in shapes:
+            sh.points = sh.points.to(dev).detach().requires_grad_(True)
+            sh.stroke_width = sh.stroke_width.to(dev).detach().requires_grad_(True)
+            ps += [sh.points, sh.stroke_width]
+        for g in groups:
+            for attr in ('fill_color', 'stroke_color'):
+                c = getattr(g, attr)
+                if isinstance(c, torch.Tensor):
+                    setattr(g, attr, c.to(dev).detach().requires_grad_(True))
+                    ps.append(getattr(g, attr))
+        opt = torch.optim.Adam(ps, lr=1e-2)
+        torch.cuda.synchronize(dev)
+        t1 = time.perf_counter()
+        for _ in range(plain_steps):
+            opt.zero_grad()
+            a = dvg.RenderFunction.serialize_scene(w, h, shapes, groups)
+            img = dvg.RenderFunction.apply(w, h, 2, 2, sp['seed'], None, *a)
+            loss = ((img - target) ** 2).mean()
+            loss.backward()
+            opt.step()
+            if k == 0:
+                loss_plain = float(loss)
+        torch.cuda.synchronize(dev)
+        t_plain += time.perf_counter() - t1
+        done += plain_steps
+    return {'workload': '%d requests, canvases {128,256,512}^2, %d-%d paths (half open strokes, half closed fills), '
+                        '%d-%d Adam steps each, Poisson arrivals at %.0f req/s, 150 GB admission budget; scaled down '
+                        'from 64-2048 paths and 100-500 steps to keep the run short'
+                        % (num_requests, path_range[0], path_range[1], step_range[0], step_range[1], rate),
+            'p50_step_ms': round(st['p50_step_ms'], 3), 'p99_step_ms': round(st['p99_step_ms'], 3),
+            'steps_per_s': round(st['steps_per_s'], 2), 'requests': st['requests'], 'ticks': st['ticks'],
+            'plain_steps_per_s': round(done / t_plain, 2),
+            'speedup_vs_plain': round(st['steps_per_s'] / (done / t_plain), 2),
+            'equal_error_check': {'request0_loss_after_%d_steps' % plain_steps:
+                                  {'served': round(reqs[0].losses[plain_steps - 1], 6),
+                                   'plain': round(loss_plain, 6)}}}
 
 
 def oracle_params(packed):

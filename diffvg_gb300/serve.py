@@ -1,0 +1,292 @@
+"""Serving loop: continuous batching of render-and-optimise requests.
+
+A request is a scene (RenderFunction.serialize_scene argument list), a
+target image and a number of Adam steps.  The server keeps a set of active
+slots on the device.  A slot holds everything a request needs between its
+steps: the DvgScene handle (topology, derived scene data, tile lists,
+per-sample and boundary-sample arenas), the parameter arena, its gradient,
+the Adam moments, the rendered / target / adjoint images, and a CUDA graph
+of one optimisation step (forward, MSE gradient, backward, Adam), captured
+when the slot is admitted.
+
+The loop runs in ticks.  Each tick replays the graph of every active slot,
+spread over several streams so that the slots' kernels overlap on the GPU,
+and waits for all of them; every active request advances by one step.
+Between ticks, requests that have arrived are admitted while slots and the
+device-memory budget allow (each request's device bytes are estimated from
+its scene and image size before anything is allocated), and finished
+requests are retired, which frees their memory for the next admissions.
+A request admitted while others are mid-way joins the next tick.
+
+Per-step latency is the duration of the tick a step ran in (CUDA events);
+the server reports p50 / p99 over all request-steps and aggregate steps/s.
+"""
+import collections
+import threading
+import time
+
+import torch
+
+from . import _native
+from .batch import DEFAULT_TRAINABLE
+from .packing import pack_scene
+
+
+def estimate_device_bytes(packed, width, height, spp):
+    """Device bytes a request holds while resident."""
+    npx, n = width * height, width * height * spp
+    P = max(packed.num_params, 1)
+    nseg, ns, ng = packed.segment_ctrl.size, packed.num_shapes, packed.num_groups
+    tiles = ((packed.canvas_width + 15) // 16) * ((packed.canvas_height + 15) // 16)
+    params = 4 * P * 6                              # params, grads, m, v, lr scale, spare
+    images = 16 * npx * 3 + 4 * npx                 # image, adjoint, target; weight image
+    samples = 16 * n                                # forward sample colours
+    edges = 68 * n                                  # boundary-sample records and ordering
+    scene = 4 * (8 * ns + 12 * ng + 2 * nseg + 2 * ng) + 64 * ng + 40 * ns + 48 * nseg + 4 * (10 * nseg + 8 * ns)
+    tile_lists = 4 * max(65536, 32 * tiles) * 5 // 4 + 8 * tiles
+    return int(params + images + samples + edges + scene + tile_lists + (1 << 20))
+
+
+class Request:
+    """A render-and-optimise request."""
+
+    _ids = 0
+
+    def __init__(self, scene_args, target, steps, num_samples=(2, 2), seed=0, lr=1e-2, betas=(0.9, 0.999),
+                 eps=1e-8, trainable=DEFAULT_TRAINABLE, size=None, arrival=None):
+        Request._ids += 1
+        self.id = Request._ids
+        self.scene_args = scene_args
+        self.target = target
+        self.steps = int(steps)
+        self.num_samples = num_samples
+        self.seed = seed
+        self.lr, self.betas, self.eps = lr, betas, eps
+        self.trainable = trainable
+        self.packed = pack_scene(scene_args)
+        self.size = size or (self.packed.canvas_width, self.packed.canvas_height)
+        self.arrival = arrival
+        self.admitted = None
+        self.finished = None
+        self.losses = []
+        self.result = None       # final parameter arena (host tensor)
+        self.step_ms = []
+
+    def device_bytes(self):
+        return estimate_device_bytes(self.packed, self.size[0], self.size[1],
+                                     self.num_samples[0] * self.num_samples[1])
+
+
+class Slot:
+    """The resident state of one admitted request."""
+
+    def __init__(self, req, device, stream):
+        self.req = req
+        self.device = device
+        w, h = req.size
+        p = req.packed
+        with torch.cuda.device(device):
+            self.scene = _native.NativeScene(p)
+        n = max(p.num_params, 1)
+        self.params = p.param_arena(device)[:n].contiguous().clone()
+        self.grads = torch.zeros(n, device=device)
+        self.m = torch.zeros(n, device=device)
+        self.v = torch.zeros(n, device=device)
+        self.lr_scale = torch.zeros(n, device=device)
+        for sl in p.slots:
+            if sl.differentiable and sl.kind in req.trainable:
+                self.lr_scale[sl.offset:sl.offset + sl.numel] = 1.0
+        self.step_count = torch.zeros(1, dtype=torch.int32, device=device)
+        self.image = torch.zeros(h, w, 4, device=device)
+        self.d_image = torch.zeros(h, w, 4, device=device)
+        self.target = req.target.to(device=device, dtype=torch.float32).reshape(h, w, 4).contiguous()
+        self.loss = torch.zeros(1, device=device)
+        self.stream = stream
+        self.graph = None
+        self.done = 0
+        self._capture()
+
+    def _args(self, flags):
+        w, h = self.req.size
+        nsx, nsy = self.req.num_samples
+        return _native.RenderArgs(w, h, nsx, nsy, int(self.req.seed) & (2 ** 64 - 1),
+                                  1 if self.req.packed.use_prefiltering else 0, 0, self.params.data_ptr(), None, None,
+                                  flags)
+
+    def _body(self):
+        sp = torch.cuda.current_stream(self.device).cuda_stream
+        self.loss.zero_()
+        self.scene.forward(self._args(_native.DVG_FLAG_NO_SYNC), image_ptr=self.image.data_ptr(), stream=sp)
+        _native.mse_grad(self.image, self.target, self.d_image, self.loss, stream=sp)
+        self.grads.zero_()
+        self.scene.backward(self._args(_native.DVG_FLAG_NO_SYNC | _native.DVG_FLAG_REUSE_PREP),
+                            d_image_ptr=self.d_image.data_ptr(), d_params_ptr=self.grads.data_ptr(), stream=sp)
+        _native.adam_step(self.params, self.grads, self.m, self.v, self.step_count, self.req.lr, self.req.betas,
+                          self.req.eps, lr_scale=self.lr_scale, stream=sp)
+
+    def _capture(self):
+        dev = self.device
+        with torch.cuda.device(dev), torch.cuda.stream(self.stream):
+            # a synchronous forward sizes the arenas and tile lists before capture
+            self.scene.forward(self._args(0), image_ptr=self.image.data_ptr(), stream=self.stream.cuda_stream)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=self.stream):
+                self._body()
+            self.graph = g
+
+    def launch(self):
+        with torch.cuda.stream(self.stream):
+            self.graph.replay()
+
+    def check(self):
+        try:
+            self.scene.sync(self.stream.cuda_stream)
+        except _native.SceneCapacityError as e:
+            if 'grown' not in str(e):
+                raise
+            # a tile list outgrew its capacity (shapes moved) and was grown:
+            # the graph is captured again.  The steps since the last check
+            # rendered this slot without gradient (their Adam updates used
+            # the moments only) and are not counted as done.
+            self.graph = None
+            self._capture()
+            return False
+        return True
+
+    def release(self):
+        self.scene.close()
+        self.graph = None
+
+
+class Server:
+    """Continuous-batching request loop on one GPU."""
+
+    def __init__(self, device=None, memory_budget=150 * 10 ** 9, max_slots=64, streams=8, check_every=8):
+        self.device = device or torch.device('cuda', torch.cuda.current_device())
+        self.budget = int(memory_budget)
+        self.max_slots = max_slots
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(streams)]
+        self.check_every = check_every
+        self.pending = collections.deque()
+        self.lock = threading.Lock()
+        self.active = []
+        self.bytes_in_use = 0
+        self.completed = []
+        self.rejected = []
+        self.tick_ms = []
+        self.ticks = 0
+        self._rr = 0
+
+    def submit(self, req):
+        """Queues a request; it is admitted at the next tick that has room.
+        A request whose estimated bytes exceed the whole budget is rejected."""
+        if req.device_bytes() > self.budget:
+            self.rejected.append(req)
+            return False
+        if req.arrival is None:
+            req.arrival = time.perf_counter()
+        with self.lock:
+            self.pending.append(req)
+        return True
+
+    def _admit(self, now):
+        with self.lock:
+            while self.pending and len(self.active) < self.max_slots:
+                req = self.pending[0]
+                if req.arrival is not None and req.arrival > now:
+                    break
+                b = req.device_bytes()
+                if self.bytes_in_use + b > self.budget:
+                    break
+                self.pending.popleft()
+                stream = self.streams[self._rr % len(self.streams)]
+                self._rr += 1
+                req.admitted = now
+                req.bytes = b
+                self.active.append(Slot(req, self.device, stream))
+                self.bytes_in_use += b
+
+    def _retire(self, now):
+        keep = []
+        for sl in self.active:
+            if sl.done >= sl.req.steps:
+                sl.req.result = sl.params.detach().cpu()
+                sl.req.finished = now
+                self.bytes_in_use -= sl.req.bytes
+                sl.release()
+                self.completed.append(sl.req)
+            else:
+                keep.append(sl)
+        self.active = keep
+
+    def tick(self):
+        """Admits what fits, runs one step of every active request, retires
+        finished requests.  Returns the number of steps run."""
+        now = time.perf_counter()
+        self._admit(now)
+        if not self.active:
+            return 0
+        main = torch.cuda.current_stream(self.device)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(main)
+        for st in self.streams:
+            st.wait_stream(main)
+        for sl in self.active:
+            sl.launch()
+        for st in self.streams:
+            main.wait_stream(st)
+        end.record(main)
+        losses = torch.cat([sl.loss for sl in self.active]).cpu()  # waits for the tick
+        ms = start.elapsed_time(end)
+        self.ticks += 1
+        self.tick_ms.append(ms)
+        redo = set()
+        if self.check_every and self.ticks % self.check_every == 0:
+            for sl in self.active:
+                if not sl.check():
+                    redo.add(id(sl))
+        for sl, l in zip(self.active, losses.tolist()):
+            if id(sl) in redo:
+                continue
+            sl.done += 1
+            sl.req.step_ms.append(ms)
+            sl.req.losses.append(l / sl.image.numel())
+        n = len(self.active) - len(redo)
+        self._retire(time.perf_counter())
+        return n
+
+    def run(self, until_idle=True, max_seconds=None):
+        """Ticks until every submitted request is done (or time runs out)."""
+        t0 = time.perf_counter()
+        steps = 0
+        while True:
+            if max_seconds is not None and time.perf_counter() - t0 > max_seconds:
+                break
+            n = self.tick()
+            steps += n
+            if n == 0:
+                with self.lock:
+                    idle = not self.pending
+                if idle and not self.active and until_idle:
+                    break
+                if not idle:
+                    nxt = self.pending[0].arrival
+                    delay = (nxt - time.perf_counter()) if nxt is not None else 0
+                    if delay > 0:
+                        time.sleep(min(delay, 0.01))
+        return steps
+
+    def stats(self):
+        lat = sorted(ms for r in self.completed for ms in r.step_ms)
+
+        def pct(q):
+            if not lat:
+                return None
+            return lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+        total_steps = sum(len(r.step_ms) for r in self.completed)
+        span = None
+        if self.completed:
+            span = max(r.finished for r in self.completed) - min(r.admitted for r in self.completed)
+        return {'requests': len(self.completed), 'rejected': len(self.rejected), 'steps': total_steps,
+                'p50_step_ms': pct(0.5), 'p99_step_ms': pct(0.99),
+                'steps_per_s': (total_steps / span) if span else None, 'ticks': self.ticks}

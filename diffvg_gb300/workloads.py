@@ -115,3 +115,48 @@ def perturbed_target_params(packed, params, seed, point_sigma=2.0, color_sigma=0
         elif sl.kind == 'color':
             seg.copy_((seg + color_sigma * torch.randn(sl.numel, generator=gen)).clamp_(0.0, 1.0))
     return out
+
+
+def mixed_scene(mod, seed, canvas, num_paths):
+    """Served-request scene: half open cubic strokes drawn like the
+    stroke-heavy configuration (step scaled by canvas / 512), half closed
+    star-shaped cubic fills with constant colours drawn like the fill-heavy
+    configuration (radius range scaled by canvas / 1024)."""
+    n_strokes = num_paths // 2
+    w, h, s_shapes, s_groups = stroke_scene(mod, seed=seed, num_paths=n_strokes, canvas=canvas,
+                                            step=20.0 * canvas / 512.0)
+    _, _, f_shapes, f_groups = fill_scene(mod, seed=seed + 7, num_paths=num_paths - n_strokes, canvas=canvas,
+                                          radius_range=(10.0 * canvas / 1024.0, 120.0 * canvas / 1024.0),
+                                          stroke_fraction=0.0)
+    shapes = s_shapes + f_shapes
+    groups = list(s_groups)
+    for k, g in enumerate(f_groups):
+        fill = g.fill_color if isinstance(g.fill_color, torch.Tensor) else torch.rand(
+            4, generator=torch.Generator().manual_seed(seed * 31 + k))
+        groups.append(mod.ShapeGroup(shape_ids=torch.tensor([n_strokes + k]), fill_color=fill, stroke_color=None))
+    return w, h, shapes, groups
+
+
+def served_requests(mod, num_requests, seed0=500, canvases=(128, 256, 512), path_range=(64, 2048),
+                    step_range=(100, 500)):
+    """Request parameters of the served workload: per request (seed s)
+    canvas U{canvases}, path count log-uniform in path_range, Adam step
+    count U{step_range}; the target is a different seeded scene (seed
+    s + 50000) of the same size."""
+    out = []
+    for r in range(num_requests):
+        s = seed0 + r
+        gen = torch.Generator().manual_seed(s)
+        canvas = canvases[int(torch.randint(0, len(canvases), (1,), generator=gen)[0])]
+        lo, hi = math.log(path_range[0]), math.log(path_range[1])
+        npaths = int(round(math.exp(lo + (hi - lo) * float(torch.rand(1, generator=gen)[0]))))
+        steps = int(torch.randint(step_range[0], step_range[1] + 1, (1,), generator=gen)[0])
+        out.append(dict(seed=s, canvas=canvas, num_paths=npaths, steps=steps, target_seed=s + 50000))
+    return out
+
+
+def noisy_target(image, seed, sigma=0.02):
+    """Target image: a render plus N(0, sigma^2) pixel noise."""
+    gen = torch.Generator().manual_seed(int(seed))
+    noise = sigma * torch.randn(tuple(image.shape), generator=gen)
+    return image + noise.to(image.device)
