@@ -152,11 +152,16 @@ class BatchedScenes:
         return grown
 
     def warmup(self):
-        """Synchronous calls that size every scene's arenas and tile lists."""
+        """Synchronous calls that size every scene's arenas and tile lists
+        (nothing may be allocated while the graph is captured)."""
         with torch.cuda.device(self.device):
+            sp = torch.cuda.current_stream(self.device).cuda_stream
             for i, sc in enumerate(self.scenes):
-                sc.forward(self._args(i, 0), image_ptr=self.images[i].data_ptr(),
-                           stream=torch.cuda.current_stream(self.device).cuda_stream)
+                o, n = self.offsets[i], self.packed[i].num_params
+                sc.forward(self._args(i, 0), image_ptr=self.images[i].data_ptr(), stream=sp)
+                sc.backward(self._args(i, 0), d_image_ptr=self.d_images[i].data_ptr(),
+                            d_params_ptr=self.grads[o:o + n].data_ptr(), stream=sp)
+            self.grads.zero_()
             torch.cuda.synchronize(self.device)
 
     def capture(self):

@@ -127,8 +127,13 @@ class Slot:
     def _capture(self):
         dev = self.device
         with torch.cuda.device(dev), torch.cuda.stream(self.stream):
-            # a synchronous forward sizes the arenas and tile lists before capture
-            self.scene.forward(self._args(0), image_ptr=self.image.data_ptr(), stream=self.stream.cuda_stream)
+            # synchronous calls size every arena and the tile lists before
+            # capture (nothing may be allocated while the graph is captured)
+            sp = self.stream.cuda_stream
+            self.scene.forward(self._args(0), image_ptr=self.image.data_ptr(), stream=sp)
+            self.scene.backward(self._args(0), d_image_ptr=self.d_image.data_ptr(), d_params_ptr=self.grads.data_ptr(),
+                                stream=sp)
+            self.grads.zero_()
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g, stream=self.stream):
                 self._body()
