@@ -158,7 +158,9 @@ def algorithmic_bytes(kernel, packed, w, h, spp):
     if kernel == 'sample_bwd':
         return scene + 16 * npx + 4 * npx + 4 * packed.num_params   # d_image, weights in; d_params out
     if kernel == 'edge':
-        return scene + 16 * npx + 4 * npx + 4 * packed.num_params
+        # the boundary pass: records written and read back once (56 B per boundary sample, as the
+        # reference's BoundarySample), d_image and weights in, d_params out
+        return scene + 2 * 56 * n + 16 * npx + 4 * npx + 4 * packed.num_params
     return scene
 
 
@@ -275,7 +277,8 @@ def run_ours(args):
                         'construction'}
 
     # ---------------- end to end through the public API ----------------
-    e2e = run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samples, ws)
+    e2e = None if getattr(args, 'no_e2e', False) else run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx,
+                                                              nsy, seed, n_samples, ws)
 
     out = {'metric': METRIC, 'value': round(value, 3), 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
            'warmup': max(args.warmup, 3), 'ms_per_step': round(total_ms / args.steps, 4), 'higher_is_better': True,
@@ -549,7 +552,12 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-batched', action='store_true')
+    ap.add_argument('--profile', action='store_true',
+                    help='only the device-resident steps (for ncu captures): no e2e, batched, served or CPU legs')
     args = ap.parse_args()
+    if args.profile:
+        args.no_batched = args.no_cpu_baseline = True
+        args.no_e2e = True
     if args.impl == 'reference':
         run_reference(args)
     else:

@@ -116,6 +116,7 @@ DI float rmax(float a, float b) { return a > b ? a : b; }
 DI float sq(float x) { return x * x; }
 DI float clampf_(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
 DI float det2(v2 a, v2 b) { return a.x * b.y - b.x * a.y; }
+DI float absmax2(v2 a) { return fmaxf(fabsf(a.x), fabsf(a.y)); }
 
 // boxes are float4 (lo.x, lo.y, hi.x, hi.y); aabb.h:15-40, 62-66
 DI float4 box_empty() { return F4(INFINITY, INFINITY, -INFINITY, -INFINITY); }
@@ -334,6 +335,71 @@ DI bool cand_range(const DevScene &S, v2 pt, int &begin, int &end) {
 
 // ---------------------------------------------------------------------------
 // winding numbers (winding_number.h:9-202)
+
+// Certified fp32 winding contribution of one cubic segment for the +x ray
+// from pt.  y(t) is split at its extrema into monotone pieces; a piece whose
+// end values straddle pt.y holds exactly one simple crossing, found by
+// bisection, and counts +-1 when the crossing lies right of pt.  Every
+// decision (end values against pt.y, crossing x against pt.x) must clear a
+// rounding margin; otherwise DVG_WINDING_UNDECIDED is returned and the caller
+// runs the reference's fp64 cubic solve.  With every decision clear of the
+// margin the reference's closed-form roots are simple roots at the same
+// crossings, so both count the same.
+#define DVG_WINDING_UNDECIDED (-1000)
+DI float cubic_y(float a, float b, float c, float d, float t) { return ((a * t + b) * t + c) * t + d; }
+DI int winding_cubic_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
+  float m = 2e-5f * fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt))) + 1e-4f;
+  float ay = -p0.y + 3 * p1.y - 3 * p2.y + p3.y, by = 3 * p0.y - 6 * p1.y + 3 * p2.y, cy = -3 * p0.y + 3 * p1.y,
+        dy = p0.y - pt.y;
+  float ax = -p0.x + 3 * p1.x - 3 * p2.x + p3.x, bx = 3 * p0.x - 6 * p1.x + 3 * p2.x, cx = -3 * p0.x + 3 * p1.x,
+        dx = p0.x - pt.x;
+  // split points: roots of y'(t) = 3 ay t^2 + 2 by t + cy inside (0, 1)
+  float ts[4];
+  int nt = 0;
+  ts[nt++] = 0.f;
+  {
+    float qa = 3 * ay, qb = 2 * by, qc = cy;
+    float e0 = -1.f, e1 = -1.f;
+    if (fabsf(qa) > 1e-12f) {
+      float disc = qb * qb - 4 * qa * qc;
+      if (disc >= 0.f) {
+        float sq_ = sqrtf(disc);
+        float q = qb < 0 ? -0.5f * (qb - sq_) : -0.5f * (qb + sq_);
+        e0 = q / qa;
+        e1 = q != 0.f ? qc / q : -1.f;
+      }
+    } else if (fabsf(qb) > 1e-12f) {
+      e0 = -qc / qb;
+    }
+    if (e0 > e1) { float tmp = e0; e0 = e1; e1 = tmp; }
+    if (e0 > 0.f && e0 < 1.f) ts[nt++] = e0;
+    if (e1 > 0.f && e1 < 1.f && e1 != e0) ts[nt++] = e1;
+  }
+  ts[nt++] = 1.f;
+  float span = fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(cx), 1.f));
+  int w = 0;
+  float ya = cubic_y(ay, by, cy, dy, ts[0]);
+  if (fabsf(ya) <= m) return DVG_WINDING_UNDECIDED;
+  for (int k = 1; k < nt; k++) {
+    float yb = cubic_y(ay, by, cy, dy, ts[k]);
+    if (fabsf(yb) <= m) return DVG_WINDING_UNDECIDED;
+    if ((ya < 0.f) != (yb < 0.f)) {
+      float lo = ts[k - 1], hi = ts[k];
+      bool up = yb > ya;
+      for (int it = 0; it < 26; it++) {
+        float mid = 0.5f * (lo + hi);
+        float ym = cubic_y(ay, by, cy, dy, mid);
+        if ((ym > 0.f) == up) hi = mid; else lo = mid;
+      }
+      float xs = cubic_y(ax, bx, cx, dx, 0.5f * (lo + hi));
+      if (fabsf(xs) <= 4.f * m + 1e-6f * span) return DVG_WINDING_UNDECIDED;
+      if (xs > 0.f) w += up ? 1 : -1;
+    }
+    ya = yb;
+  }
+  return w;
+}
+
 DI int winding_segment(const DevScene &S, int po, int np, int nc, int i0, v2 pt) {
   int w = 0;
   if (nc == 0) {
@@ -359,6 +425,8 @@ DI int winding_segment(const DevScene &S, int po, int np, int nc, int i0, v2 pt)
   } else {
     v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, i0 + 2),
        p3 = path_pt(S, po, (i0 + 3) % np);
+    int fw = winding_cubic_fast(p0, p1, p2, p3, pt);
+    if (fw != DVG_WINDING_UNDECIDED) return fw;
     double t[3];
     int n = solve_cubic_d((double)(-p0.y + 3 * p1.y - 3 * p2.y + p3.y), (double)(3 * p0.y - 6 * p1.y + 3 * p2.y),
                           (double)(-3 * p0.y + 3 * p1.y), (double)(p0.y - pt.y), t);
@@ -512,7 +580,6 @@ DI float dist_to_seg(v2 a, v2 b, v2 p) {
   return len2(sub2(add2(a, scl2(t, ab)), p));
 }
 DI float far_margin(float m) { return 1e-5f * m + 1e-4f; }
-DI float absmax2(v2 a) { return fmaxf(fabsf(a.x), fabsf(a.y)); }
 DI float cubic_lb(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
   return dist_to_seg(p0, p3, pt) - fmaxf(dist_to_seg(p0, p3, p1), dist_to_seg(p0, p3, p2));
 }
