@@ -548,7 +548,11 @@ DI int quintic_intervals(const Quintic &q, float iv[4]) {
     for (int k = j; k > 0 && iv[k - 1] > iv[k]; k--) { float tmp = iv[k]; iv[k] = iv[k - 1]; iv[k - 1] = tmp; }
   return n;
 }
-// safeguarded Newton / bisection in one bracket (within_distance.h:251-269)
+// safeguarded Newton / bisection in one bracket (within_distance.h:251-269).
+// When the caller swapped the bracket ends (q decreasing), lb > ub holds for
+// the whole loop, the test t in [lb, ub] always fails and every iteration
+// restarts from the midpoint: the reference's Newton update is dead work
+// there and is skipped, which leaves every result unchanged.
 DI float quintic_root(const Quintic &q, float lb, float ub) {
   float t = 0.5f * (lb + ub);
   for (int it = 0; it < 20; it++) {
@@ -556,10 +560,20 @@ DI float quintic_root(const Quintic &q, float lb, float ub) {
     double value = quintic_eval(q, t);
     if (fabs(value) < 1e-5f || it == 19) break;
     if (value > 0.f) ub = t; else lb = t;
+    if (lb > ub) continue;  // the next iteration restarts from the midpoint
     double derivative = quintic_deriv(q, t);
     t = (float)(t - value / derivative);
   }
   return t;
+}
+
+// quintic value at a bracket end; consecutive brackets share an end, so the
+// previous value is reused (same argument, same result)
+DI double quintic_eval_cached(const Quintic &q, float t, float &ct, double &cv) {
+  if (t == ct) return cv;
+  ct = t;
+  cv = quintic_eval(q, t);
+  return cv;
 }
 
 // ---------------------------------------------------------------------------
@@ -713,11 +727,13 @@ static __device__ __noinline__ int segment_root_test(const DevScene &S, int po, 
   float iv[4];
   int ni = quintic_intervals(q, iv);
   float lower = 0.f;
+  float ct = NAN;
+  double cv = 0.0;
   for (int j = 0; j < ni + 1; j++) {
     if (j < ni && iv[j] < 0.f) continue;
     float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
     float lb = lower, ub = upper;
-    double lbe = quintic_eval(q, lb), ube = quintic_eval(q, ub);
+    double lbe = quintic_eval_cached(q, lb, ct, cv), ube = quintic_eval_cached(q, ub, ct, cv);
     if (lbe * ube > 0) continue;
     if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
     float t = quintic_root(q, lb, ub);
@@ -899,11 +915,13 @@ DI bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
       float iv[4];
       int ni = quintic_intervals(q, iv);
       float lower = 0.f;
+      float ct = NAN;
+      double cv = 0.0;
       for (int j = 0; j < ni + 1; j++) {
         if (j < ni && iv[j] < 0.f) continue;
         float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
         float lb = lower, ub = upper;
-        double lbe = quintic_eval(q, lb), ube = quintic_eval(q, ub);
+        double lbe = quintic_eval_cached(q, lb, ct, cv), ube = quintic_eval_cached(q, ub, ct, cv);
         if (lbe * ube > 0) continue;
         if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
         float t = quintic_root(q, lb, ub);

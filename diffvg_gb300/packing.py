@@ -13,8 +13,10 @@ module performs that unpacking once per call and splits the result in two:
     tensor lives in the arena so that its gradient is a view of the gradient
     arena.
 """
+from collections import OrderedDict
 from dataclasses import dataclass, field
 import hashlib
+import threading
 
 import numpy as np
 import torch
@@ -59,16 +61,33 @@ class PackedScene:
     slots: list = field(default_factory=list)
     tensors: list = field(default_factory=list)
     topology_key: bytes = b''
+    _pinned: object = None
+    _copied: object = None
 
     def param_arena(self, device):
         """The parameter values as one contiguous fp32 tensor on `device`."""
         if not self.tensors:
             return torch.zeros(1, dtype=torch.float32, device=device)
-        flat = [t.detach().reshape(-1).to(dtype=torch.float32) for t in self.tensors]
-        if len({t.device for t in flat}) == 1:
-            # one concatenation where the tensors live, then one copy
-            return torch.cat(flat).to(device=device)
-        return torch.cat([t.to(device=device) for t in flat])
+        flat = [t.detach().reshape(-1) for t in self.tensors]
+        if any(t.dtype != torch.float32 for t in flat):
+            flat = [t.to(torch.float32) for t in flat]
+        devs = {t.device for t in flat}
+        if len(devs) != 1:
+            return torch.cat([t.to(device=device) for t in flat])
+        src = next(iter(devs))
+        if src.type == 'cpu' and device.type == 'cuda':
+            # one concatenation into a reused pinned buffer, one asynchronous copy
+            if self._pinned is None or self._pinned.numel() != self.num_params:
+                self._pinned = torch.empty(self.num_params, dtype=torch.float32, pin_memory=True)
+                self._copied = None
+            if self._copied is not None:
+                self._copied.synchronize()  # the previous copy out of the buffer has finished
+            torch.cat(flat, out=self._pinned)
+            out = self._pinned.to(device=device, non_blocking=True)
+            self._copied = torch.cuda.Event()
+            self._copied.record(torch.cuda.current_stream(device))
+            return out
+        return torch.cat(flat).to(device=device)
 
 
 def _as_tensor(x):
@@ -79,6 +98,44 @@ def _as_tensor(x):
 
 def _enum_value(v):
     return int(v.value) if hasattr(v, 'value') else int(v)
+
+
+_cache_lock = threading.Lock()
+_pack_cache = OrderedDict()
+_PACK_CACHE_SIZE = 32
+
+
+def _structure_key(args):
+    """Cheap identity of an argument list's structure: floating-point tensors
+    by identity and shape (their values are parameters, read later),
+    integer tensors (segment counts, shape ids) by identity and version
+    counter (an in-place edit changes the version), everything else by
+    value."""
+    T = torch.Tensor
+    return tuple(((id(a), a.shape) if a.is_floating_point() else (id(a), a._version)) if isinstance(a, T) else a
+                 for a in args)
+
+
+def pack_scene_cached(args):
+    """pack_scene with a cache for optimisation loops, which call
+    serialize_scene with the same shape objects on every step.  An entry
+    keeps its argument objects alive, so identities in the key cannot be
+    reused while it is cached.  On a hit the packed topology and parameter
+    slots are reused; parameter values are read when the arena is built.
+    Integer tensors that are converted anew on every call (e.g. by a
+    serialize_scene that copies them) simply miss the cache."""
+    key = _structure_key(args)
+    with _cache_lock:
+        hit = _pack_cache.get(key)
+        if hit is not None:
+            _pack_cache.move_to_end(key)
+            return hit[1]
+    packed = pack_scene(args)
+    with _cache_lock:
+        _pack_cache[key] = (list(args), packed)
+        while len(_pack_cache) > _PACK_CACHE_SIZE:
+            _pack_cache.popitem(last=False)
+    return packed
 
 
 def pack_scene(args):

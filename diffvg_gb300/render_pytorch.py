@@ -27,7 +27,7 @@ import torch
 from . import device as _device
 from . import _native
 from .diffvg import ShapeType, ColorType, FilterType
-from .packing import pack_scene
+from .packing import pack_scene, pack_scene_cached
 from .pixel_filter import PixelFilter
 from . import shape as _shape
 from . import color as _color
@@ -46,6 +46,11 @@ class OutputType(IntEnum):
 
 
 _SCENE_CACHE_SIZE = 64
+# shared defaults, so that repeated serialize_scene calls produce the same
+# argument objects (the packed-scene cache keys on tensor identity)
+_EMPTY_EVAL = torch.tensor([])
+_DEFAULT_FILTER = PixelFilter(type=FilterType.box, radius=torch.tensor(0.5))
+_THICKNESS_PLACEHOLDER = torch.tensor(0.0)
 _cache_lock = threading.Lock()
 _scene_cache = OrderedDict()
 _token = itertools.count(1)
@@ -127,9 +132,9 @@ class RenderFunction(torch.autograd.Function):
         """Flattens a scene into RenderFunction.apply's argument list, in the
         reference's order (render_pytorch.py:22-172)."""
         if filter is None:
-            filter = PixelFilter(type=FilterType.box, radius=torch.tensor(0.5))
+            filter = _DEFAULT_FILTER
         if eval_positions is None:
-            eval_positions = torch.tensor([])
+            eval_positions = _EMPTY_EVAL
         args = [canvas_width, canvas_height, len(shapes), len(shape_groups), output_type, use_prefiltering,
                 eval_positions]
         for shp in shapes:
@@ -140,11 +145,9 @@ class RenderFunction(torch.autograd.Function):
                 args += [ShapeType.ellipse, shp.radius, shp.center]
             elif isinstance(shp, _shape.Path) or type(shp).__name__ == 'Path':
                 assert shp.points.shape[1] == 2
-                assert torch.isfinite(shp.points).all()
                 args += [ShapeType.path, shp.num_control_points.to(torch.int32), shp.points]
                 sw = shp.stroke_width
                 if len(sw.shape) > 0 and sw.shape[0] > 1:
-                    assert torch.isfinite(sw).all()
                     use_thickness = True
                     args.append(sw)
                 else:
@@ -158,9 +161,9 @@ class RenderFunction(torch.autograd.Function):
                 args += [ShapeType.rect, shp.p_min, shp.p_max]
             else:
                 raise TypeError('unknown shape type %r' % type(shp))
-            args.append(torch.tensor(0.0) if use_thickness else shp.stroke_width)
+            args.append(_THICKNESS_PLACEHOLDER if use_thickness else shp.stroke_width)
         for grp in shape_groups:
-            args.append(grp.shape_ids.to(torch.int32))
+            args.append(grp.shape_ids)
             for paint in (grp.fill_color, grp.stroke_color):
                 if paint is None:
                     args.append(None)
@@ -187,7 +190,7 @@ class RenderFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, width, height, num_samples_x, num_samples_y, seed, background_image, *args):
         device = _render_device()
-        packed = pack_scene(args)
+        packed = pack_scene_cached(args)
         scene = _native_scene(packed, device)
         arena = packed.param_arena(device).contiguous()
         ev = _eval_positions(packed, device)
@@ -197,6 +200,8 @@ class RenderFunction(torch.autograd.Function):
         else:
             out = torch.empty((height, width, 1) if ev is None else (ev.shape[0], 1), device=device)
         bg = _background(background_image, out.shape[0], out.shape[1], device)
+        if not bool(torch.isfinite(arena).all()):
+            raise ValueError('scene parameters contain a non-finite value')
         token = next(_token)
         rargs = _render_args(packed, width, height, num_samples_x, num_samples_y, seed, arena, bg, ev)
         stream = torch.cuda.current_stream(device).cuda_stream
