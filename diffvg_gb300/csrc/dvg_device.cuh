@@ -691,6 +691,252 @@ DI int quad_stroke_fast(v2 p0, v2 p1, v2 p2, v2 pt, float r_out, float m) {
   return -2;
 }
 
+// ---------------------------------------------------------------------------
+// fp32 decision of the reference's cubic-segment stroke test.
+//
+// The reference decides a point against a cubic segment by isolating the
+// roots of the normalised distance quintic Q (breakpoints: -B/5 and the roots
+// of the isolator cubic Q - (t/5 + B/25) Q', within_distance.h:181-236),
+// walking the brackets whose ends change sign (the lower end stays put
+// through brackets without a sign change, within_distance.h:237-240), running
+// a safeguarded Newton iteration in each that stops where |Q| < 1e-5 or after
+// 20 steps (within_distance.h:244-261), and testing the distance at the
+// stopping point against the interpolated radius.  All of it runs in fp64
+// there.  cubic_stroke_decide repeats the same structure in fp32 with error
+// enclosures: every breakpoint carries a certified radius, every sign the
+// reference reads must be certain, each sign-change bracket must hold one
+// simple root (Bernstein bounds of Q' on subdivided pieces) and no other
+// place where the Newton iteration could stop, and the distance at the root
+// must clear the radius by a margin that covers where in the stopping window
+// the reference lands.  Returns 1 or 0 when that decides the outcome, 2 when
+// any enclosure is inconclusive (the fp64 solve then runs).
+DI float emu_p3(float c3, float c2, float c1, float c0, float t) { return ((c3 * t + c2) * t + c1) * t + c0; }
+DI float emu_q(const float n[6], float t) { return ((((t + n[1]) * t + n[2]) * t + n[3]) * t + n[4]) * t + n[5]; }
+// Bernstein coefficients on [l,u] of the quartic with [0,1]-Bernstein coefficients b (blossoming)
+DI void emu_blossom4(const float b[5], float l, float u, float c[5]) {
+#pragma unroll
+  for (int k = 0; k < 5; k++) {
+    float w[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) w[i] = b[i];
+#pragma unroll
+    for (int lev = 0; lev < 4; lev++) {
+      float t = lev < 4 - k ? l : u;
+#pragma unroll
+      for (int i = 0; i < 4 - lev; i++) w[i] = w[i] + t * (w[i + 1] - w[i]);
+    }
+    c[k] = w[0];
+  }
+}
+// roots in (0,1) of c3 t^3 + c2 t^2 + c1 t + c0 with certified enclosure
+// radii (sign change certain at root +- rad); the count, or -1 when a
+// stationary point or an end sits within del of zero
+DI int emu_cubic_roots01(float c3, float c2, float c1, float c0, float del, float root[3], float rad[3]) {
+  float ts[4];
+  int nt = 0;
+  ts[nt++] = 0.f;
+  float qa = 3 * c3, qb = 2 * c2, qc = c1, e0 = -1.f, e1 = -1.f;
+  float sc = fabsf(qa) + fabsf(qb) + fabsf(qc);
+  if (fabsf(qa) > 1e-7f * sc) {
+    float disc = qb * qb - 4 * qa * qc;
+    if (disc >= 0.f) {
+      float s = sqrtf(disc);
+      float q = qb < 0 ? -0.5f * (qb - s) : -0.5f * (qb + s);
+      e0 = q / qa;
+      e1 = q != 0.f ? qc / q : -1.f;
+    }
+  } else if (fabsf(qb) > 1e-7f * sc) {
+    e0 = -qc / qb;
+  }
+  if (e0 > e1) { float tmp = e0; e0 = e1; e1 = tmp; }
+  if (e0 > 0.f && e0 < 1.f) ts[nt++] = e0;
+  if (e1 > 0.f && e1 < 1.f && e1 != e0) ts[nt++] = e1;
+  ts[nt++] = 1.f;
+  int n = 0;
+  float ya = emu_p3(c3, c2, c1, c0, ts[0]);
+  if (fabsf(ya) <= del) return -1;
+  for (int k = 1; k < nt; k++) {
+    float yb = emu_p3(c3, c2, c1, c0, ts[k]);
+    if (fabsf(yb) <= del) return -1;
+    if ((ya < 0) != (yb < 0)) {
+      float lo = ts[k - 1], hi = ts[k];
+      bool up = yb > ya;
+      for (int it = 0; it < 32; it++) {
+        float m = 0.5f * (lo + hi);
+        if (m <= lo || m >= hi) break;
+        if ((emu_p3(c3, c2, c1, c0, m) > 0) == up) hi = m; else lo = m;
+      }
+      float r = 0.5f * (lo + hi);
+      float dp = fabsf((3 * c3 * r + 2 * c2) * r + c1);
+      if (!(dp > 0.f)) return -1;
+      float eps = fmaxf(4e-7f, 4.f * del / dp);
+      float ym = emu_p3(c3, c2, c1, c0, r - eps), yp = emu_p3(c3, c2, c1, c0, r + eps);
+      if (!(fabsf(ym) > del && fabsf(yp) > del && ((ym < 0) != (yp < 0)))) return -1;
+      root[n] = r;
+      rad[n] = eps;
+      n++;
+    }
+    ya = yb;
+  }
+  return n;
+}
+// Root structure of Q on [l,u] (Q(l), Q(u) of certain opposite signs): 1
+// with the piece [ra,rb] that holds the one simple root and mu = min |Q'|
+// on it; 0 when another root may exist or |Q| may drop to the stopping
+// tolerance away from the root piece.  Q' bounds come from its Bernstein
+// coefficients on each piece (qb: on [0,1]); dQ, dQp bound the fp32 error of
+// Q and Q'.
+DI int emu_unique_root(const float n[6], const float qb[5], float l, float u, float ql, float qu, float dQ, float dQp,
+                       float stop, float *ra, float *rb, float *mu_out) {
+  float sa[8], sb[8], sqa[8], sqb[8];
+  int sd[8];
+  int sp = 1;
+  sa[0] = l; sb[0] = u; sqa[0] = ql; sqb[0] = qu; sd[0] = 0;
+  int nroot = 0;
+  while (sp > 0) {
+    sp--;
+    float a = sa[sp], b = sb[sp], qa = sqa[sp], qbv = sqb[sp];
+    int d = sd[sp];
+    float c[5];
+    emu_blossom4(qb, a, b, c);
+    float mn = c[0], mx = c[0], amax = fabsf(c[0]);
+#pragma unroll
+    for (int k = 1; k < 5; k++) { mn = fminf(mn, c[k]); mx = fmaxf(mx, c[k]); amax = fmaxf(amax, fabsf(c[k])); }
+    if (mn > dQp || mx < -dQp) {  // Q monotone on the piece
+      float mu = (mn > dQp) ? mn - dQp : -mx - dQp;
+      if ((qa < 0) != (qbv < 0)) {
+        if (++nroot > 1) return 0;
+        *ra = a; *rb = b; *mu_out = mu;
+      } else if (fminf(fabsf(qa), fabsf(qbv)) <= stop + dQ) {
+        return 0;
+      }
+      continue;
+    }
+    float m = 0.5f * (a + b);
+    float qm = emu_q(n, m);
+    float lip = amax + dQp;
+    if (fabsf(qm) - lip * 0.5f * (b - a) > stop + dQ) continue;  // no root, |Q| above the stopping tolerance
+    if (d >= 6 || sp + 2 > 8) return 0;
+    if (fabsf(qm) <= dQ) return 0;
+    sa[sp] = m; sb[sp] = b; sqa[sp] = qm; sqb[sp] = qbv; sd[sp] = d + 1; sp++;
+    sa[sp] = a; sb[sp] = m; sqa[sp] = qa; sqb[sp] = qm; sd[sp] = d + 1; sp++;
+  }
+  return nroot == 1;
+}
+static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float r0, float r1,
+                                                       float r2, float r3) {
+  // distance quintic coefficients exactly as the reference forms them in fp32 (within_distance.h:150-167)
+  v2 a = add2(sub2(add2(neg2(p0), scl2(3, p1)), scl2(3, p2)), p3);
+  v2 b = add2(sub2(scl2(3, p0), scl2(6, p1)), scl2(3, p2));
+  v2 c = add2(scl2(-3, p0), scl2(3, p1));
+  v2 e = sub2(p0, pt);
+  float A = 3 * sum2(mul2(a, a)), B = 5 * sum2(mul2(a, b)), C = 4 * sum2(mul2(a, c)) + 2 * sum2(mul2(b, b));
+  float D = 3 * (sum2(mul2(b, c)) + sum2(mul2(a, e))), E = sum2(mul2(c, c)) + 2 * sum2(mul2(e, b));
+  float F = sum2(mul2(e, c));
+  float sabs = fabsf(A) + fabsf(B) + fabsf(C) + fabsf(D) + fabsf(E) + fabsf(F);
+  if (!(A > 1e-5f * sabs)) return 2;
+  float n[6] = {1.f, B / A, C / A, D / A, E / A, F / A};
+  float ns = 1.f + fabsf(n[1]) + fabsf(n[2]) + fabsf(n[3]) + fabsf(n[4]) + fabsf(n[5]);
+  float dQ = 1.5e-6f * ns;  // |Q (fp32 here) - Q (fp64 there)| on [0,1]
+  float qbz[5];             // Bernstein coefficients of Q' on [0,1]
+  {
+    float a0 = n[4], a1 = 2 * n[3], a2 = 3 * n[2], a3 = 4 * n[1], a4 = 5.f;
+    qbz[0] = a0;
+    qbz[1] = a0 + a1 / 4;
+    qbz[2] = a0 + a1 / 2 + a2 / 6;
+    qbz[3] = a0 + 3 * a1 / 4 + a2 / 2 + a3 / 4;
+    qbz[4] = a0 + a1 + a2 + a3 + a4;
+  }
+  float dQp = 2e-6f * (5 + 4 * fabsf(n[1]) + 3 * fabsf(n[2]) + 2 * fabsf(n[3]) + fabsf(n[4]));
+  // isolator cubic and the bound of its evaluation error
+  float mA = 0.4f * fabsf(n[2]) + 0.16f * n[1] * n[1], mB = 0.6f * fabsf(n[3]) + 0.12f * fabsf(n[1] * n[2]);
+  float mC = 0.8f * fabsf(n[4]) + 0.08f * fabsf(n[1] * n[3]), mD = fabsf(n[5]) + fabsf(n[1] * n[4]) / 25.f;
+  float pA = 0.4f * n[2] - 0.16f * n[1] * n[1], pB = 0.6f * n[3] - 0.12f * n[1] * n[2];
+  float pC = 0.8f * n[4] - 0.08f * n[1] * n[3], pD = n[5] - n[1] * n[4] / 25.f;
+  float del = 1e-6f * (mA + mB + mC + mD) + 1e-30f;
+  if (fabsf(pA) <= 1e-6f + 2e-6f * mA) {  // the reference's solver may take its quadratic branch
+    del += fabsf(pA) + 2e-6f * mA + 1e-6f;
+    pA = 0.f;
+  }
+  float bp[4], br[4];
+  int nb = 0;
+  float qr = -n[1] / 5.f, eq = 3e-7f * fabsf(qr) + 1e-7f;
+  if (fabsf(qr) <= eq || fabsf(qr - 1.f) <= eq) return 2;
+  if (qr > 0.f && qr < 1.f) { bp[nb] = qr; br[nb] = eq; nb++; }
+  float rts[3], rrad[3];
+  int nr = emu_cubic_roots01(pA, pB, pC, pD, del, rts, rrad);
+  if (nr < 0) return 2;
+  for (int k = 0; k < nr; k++) {
+    float rad = rrad[k] + 1.2e-7f;
+    if (rts[k] - rad <= 0.f || rts[k] + rad >= 1.f) return 2;
+    bp[nb] = rts[k];
+    br[nb] = rad;
+    nb++;
+  }
+  for (int j = 1; j < nb; j++)
+    for (int k = j; k > 0 && bp[k - 1] > bp[k]; k--) {
+      float t = bp[k]; bp[k] = bp[k - 1]; bp[k - 1] = t;
+      t = br[k]; br[k] = br[k - 1]; br[k - 1] = t;
+    }
+  for (int j = 1; j < nb; j++)
+    if (bp[j] - bp[j - 1] <= br[j] + br[j - 1]) return 2;
+  // bracket ends, Q there, and |Q'| within the enclosure of each breakpoint
+  float ends[6], val[6], qloc[6];
+  int ne = 0;
+  float qpp = 20 + 12 * fabsf(n[1]) + 6 * fabsf(n[2]) + 2 * fabsf(n[3]);  // |Q''| on [0,1]
+  ends[ne] = 0.f; val[ne] = n[5]; qloc[ne] = 0.f; ne++;
+  for (int j = 0; j < nb; j++) {
+    float t = bp[j];
+    float qd = (((5 * t + 4 * n[1]) * t + 3 * n[2]) * t + 2 * n[3]) * t + n[4];
+    ends[ne] = t;
+    val[ne] = emu_q(n, t);
+    qloc[ne] = fabsf(qd) + dQp + qpp * br[j];
+    if (fabsf(val[ne]) <= dQ + qloc[ne] * br[j]) return 2;  // the sign the reference reads is not certain
+    ne++;
+  }
+  ends[ne] = 1.f; val[ne] = emu_q(n, 1.f); qloc[ne] = 0.f; ne++;
+  if (fabsf(val[0]) <= dQ || fabsf(val[ne - 1]) <= dQ) return 2;
+  float bmax = 3 * fmaxf(fmaxf(dist2(p0, p1), dist2(p1, p2)), dist2(p2, p3));    // |cubic'|
+  float rmaxd = 3 * fmaxf(fmaxf(fabsf(r1 - r0), fabsf(r2 - r1)), fabsf(r3 - r2));  // |radius'|
+  float M = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
+  bool unsure = false;
+  int lj = 0;  // lower bracket end: kept through brackets without a sign change
+  for (int j = 0; j + 1 < ne; j++) {
+    if ((val[j] < 0) == (val[j + 1] < 0)) continue;
+    int i0 = lj;
+    lj = j + 1;
+    // the reference's bracket ends sit within br of ours: the certain part of the bracket
+    float rl = i0 > 0 ? br[i0 - 1] : 0.f, ru = j + 1 < ne - 1 ? br[j] : 0.f;
+    float l = ends[i0] + rl, u = ends[j + 1] - ru;
+    // the iteration may stop right at an end where |Q| < 1e-5
+    if (fabsf(val[i0]) <= 1e-5f + dQ + 2.f * qloc[i0] * rl || fabsf(val[j + 1]) <= 1e-5f + dQ + 2.f * qloc[j + 1] * ru) {
+      unsure = true;
+      continue;
+    }
+    float ql = emu_q(n, l), qu = emu_q(n, u);
+    if (fabsf(ql) <= dQ || fabsf(qu) <= dQ || ((ql < 0) == (qu < 0))) { unsure = true; continue; }
+    float ra, rb, mu;
+    if (!emu_unique_root(n, qbz, l, u, ql, qu, dQ, dQp, 1e-5f, &ra, &rb, &mu)) { unsure = true; continue; }
+    bool up = emu_q(n, rb) > emu_q(n, ra);
+    float lo = ra, hi = rb;
+    for (int it = 0; it < 32; it++) {
+      float m = 0.5f * (lo + hi);
+      if (m <= lo || m >= hi) break;
+      if ((emu_q(n, m) > 0) == up) hi = m; else lo = m;
+    }
+    float ts = 0.5f * (lo + hi);
+    // where the reference may stop: |Q| < 1e-5 around the root, or the 20-step bisection window
+    float eps_t = (1e-5f + dQ) / mu + (ends[j + 1] - ends[i0]) * 4e-6f + 1e-6f;
+    float margin = (bmax + rmaxd) * eps_t + far_margin(M);
+    float tt = 1 - ts;
+    float rr = (tt * tt * tt) * r0 + (3 * tt * tt * ts) * r1 + (3 * tt * ts * ts) * r2 + (ts * ts * ts) * r3;
+    float dd = dist2(eval_cubic(p0, p1, p2, p3, ts), pt);
+    if (dd < rr - margin) return 1;  // the reference returns 1 here or at an earlier bracket
+    if (dd <= rr + margin) unsure = true;
+  }
+  return unsure ? 2 : 0;
+}
+
 // Root-solve part of the stroke test of one quadratic (nc = 1) or cubic
 // (nc = 2) segment, for a point whose end-point checks failed: the
 // quadratic's cubic and the cubic's distance quintic, solved as the
@@ -749,8 +995,7 @@ static __device__ __noinline__ int segment_root_test(const DevScene &S, int po, 
 // Cheap part of the stroke test of one segment (within_distance.h:20-272):
 // lines exactly, quadratic / cubic end points exactly, then the fp32
 // outside proof.  1: within, 0: not, -1: the path reports "not within"
-// (distance-approximated quadratics), 2: undecided, the root solve
-// (segment_root_test) decides.
+// (distance-approximated quadratics), 2: undecided (segment_solve decides).
 DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, int nc, int i0, v2 pt, float r) {
   if (nc == 0) {
     int i1 = (i0 + 1) % np;
@@ -786,10 +1031,27 @@ DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, 
   return cubic_stroke_fast(p0, p1, p2, p3, pt, fmaxf(fmaxf(r0, r1), fmaxf(r2, r3)), far_margin(m)) == 0 ? 0 : 2;
 }
 
+// fp32 decision of an undecided segment (cubics: cubic_stroke_decide); 2
+// when it stays undecided
+DI int segment_decide(const DevScene &S, int po, int np, int th, int nc, int i0, v2 pt, float r) {
+  if (nc != 2) return 2;
+  int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
+  v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2), p3 = path_pt(S, po, i3);
+  float r0 = r, r1 = r, r2 = r, r3 = r;
+  if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); r3 = pget(S, th + i3); }
+  return cubic_stroke_decide(p0, p1, p2, p3, pt, r0, r1, r2, r3);
+}
+
+// an undecided segment, decided: fp32 where that suffices, else the fp64 solve
+DI int segment_solve(const DevScene &S, int po, int np, int th, int nc, int i0, v2 pt, float r) {
+  int f = segment_decide(S, po, np, th, nc, i0, pt, r);
+  return f != 2 ? f : segment_root_test(S, po, np, th, nc, i0, pt, r);
+}
+
 // 1: within, 0: not, -1: the path reports "not within" (approx quadratics)
 DI int within_segment(const DevScene &S, int s, int po, int np, int th, int flags, int nc, int i0, v2 pt, float r) {
   int f = within_segment_pre(S, po, np, th, flags, nc, i0, pt, r);
-  if (f == 2) f = segment_root_test(S, po, np, th, nc, i0, pt, r);
+  if (f == 2) f = segment_solve(S, po, np, th, nc, i0, pt, r);
   return f;
 }
 

@@ -12,6 +12,12 @@
 #include "dvg_internal.h"
 #include "dvg_sample.cuh"
 
+// resident blocks per SM the sample kernels are compiled for (sets their
+// register budget: 65536 / (256 * blocks))
+#ifndef DVG_SAMPLE_MIN_BLOCKS
+#define DVG_SAMPLE_MIN_BLOCKS 2
+#endif
+
 namespace dvg {
 
 // Kernels that accumulate into caller-visible outputs do nothing when the
@@ -57,7 +63,7 @@ __global__ void __launch_bounds__(256) k_weight(DevRender R0, DevScene S) {
 }
 
 template <bool PREFILTER>
-__global__ void __launch_bounds__(256) k_sample_fwd(DevScene S, DevRender R, float4 *samples) {
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_sample_fwd(DevScene S, DevRender R, float4 *samples) {
   __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
   int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
@@ -114,7 +120,7 @@ __device__ __forceinline__ float block_sum(float v) {
 
 // interior adjoint (render_kernel with d_render_image, diffvg.cpp:1160-1268)
 template <bool PREFILTER>
-__global__ void __launch_bounds__(256) k_sample_bwd(DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_sample_bwd(DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
   __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
   DevRender R = load_filter(R0, nullptr);
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
@@ -261,7 +267,7 @@ __global__ void k_edge_order(EdgeRecords E, int n) {
   if (key >= 0) E.order[E.tile_start[key] + E.rank[idx]] = idx;
 }
 
-__global__ void __launch_bounds__(256) k_edge_eval(DevScene S, DevRender R0, EdgeRecords E) {
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_edge_eval(DevScene S, DevRender R0, EdgeRecords E) {
   __shared__ WarpQueue wq[8];
   DevRender R = load_filter(R0, nullptr);
   int i = blockIdx.x * blockDim.x + threadIdx.x;

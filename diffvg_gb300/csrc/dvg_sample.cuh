@@ -73,7 +73,9 @@ struct WarpQueue {
   SegJob job[32][DVG_LANE_JOBS];
   unsigned result[32];
   int offs[33];
+  unsigned char pend[32 * DVG_LANE_JOBS];  // jobs the fp32 decision left open
 };
+static_assert(32 * DVG_LANE_JOBS <= 256, "job numbers are stored in bytes");
 
 // candidate fragment of a sample: key = 2 * group + is_stroke; meta bit 31
 // = decided hit, else bits 0-7 / 8-15 = the lane's job range whose results
@@ -81,6 +83,21 @@ struct WarpQueue {
 struct FragRef { int key, meta; };
 #define DVG_META_HIT (1 << 31)
 
+// owner lane and slot of the warp's j-th queued job
+DI const SegJob &warp_job(const WarpQueue *q, int j, int &owner, int &idx) {
+  int lo = 0, hi = 31;  // last lane with offs <= j
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (q->offs[mid] <= j) lo = mid; else hi = mid - 1;
+  }
+  owner = lo;
+  idx = j - q->offs[lo];
+  return q->job[lo][idx];
+}
+
+// Decide every queued job of the warp, spread over its lanes: the fp32
+// decision first, then the fp64 solve of the jobs it left open, compacted so
+// that the lanes run those together.
 DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
   const unsigned full = 0xffffffffu;
   int incl = njobs;
@@ -94,108 +111,169 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
   if (lane == 31) q->offs[32] = total;
   q->result[lane] = 0u;
   __syncwarp();
-  for (int j = lane; j < total; j += 32) {
-    int lo = 0, hi = 31;  // owner: last lane with offs <= j
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (q->offs[mid] <= j) lo = mid; else hi = mid - 1;
+  int npend = 0;
+  for (int base = 0; base < total; base += 32) {  // warp-uniform trip count
+    int j = base + lane;
+    bool pending = false;
+    if (j < total) {
+      int owner, idx;
+      SegJob jb = warp_job(q, j, owner, idx);
+      int s = jb.shape;
+      int f = segment_decide(S, SI(S, s, DVG_SHAPE_PARAM_OFF), SI(S, s, DVG_SHAPE_NUM_POINTS),
+                             SI(S, s, DVG_SHAPE_THICKNESS_OFF), __ldg(&S.segment_ctrl[jb.seg]),
+                             __ldg(&S.seg_point[jb.seg]), V2(jb.x, jb.y), jb.r);
+      if (f == 1) atomicOr(&q->result[owner], 1u << idx);
+      pending = f == 2;
     }
-    int idx = j - q->offs[lo];
-    SegJob jb = q->job[lo][idx];
+    unsigned bal = __ballot_sync(full, pending);
+    if (pending) q->pend[npend + __popc(bal & ((1u << lane) - 1u))] = (unsigned char)j;
+    npend += __popc(bal);
+  }
+  __syncwarp();
+  for (int k = lane; k < npend; k += 32) {
+    int owner, idx;
+    SegJob jb = warp_job(q, q->pend[k], owner, idx);
     int s = jb.shape;
     int hit = segment_root_test(S, SI(S, s, DVG_SHAPE_PARAM_OFF), SI(S, s, DVG_SHAPE_NUM_POINTS),
                                 SI(S, s, DVG_SHAPE_THICKNESS_OFF), __ldg(&S.segment_ctrl[jb.seg]),
                                 __ldg(&S.seg_point[jb.seg]), V2(jb.x, jb.y), jb.r);
-    if (hit) atomicOr(&q->result[lo], 1u << idx);
+    if (hit) atomicOr(&q->result[owner], 1u << idx);
   }
   __syncwarp();
 }
 
-// Stroke test of one shape with undecided path segments queued.
-// 1: hit, 0: miss, 2: pending on the jobs [njobs_before, njobs).
-DI int shape_stroke_status(const DevScene &S, int s, v2 lp, float r, WarpQueue *q, int lane, int &njobs,
-                           unsigned *mark) {
-  int kind = SI(S, s, DVG_SHAPE_KIND);
-  int flags = kind == DVG_PATH ? SI(S, s, DVG_SHAPE_FLAGS) : 0;
-  if (kind != DVG_PATH || (flags & 2)) return within_shape(S, s, lp, r) ? 1 : 0;
-  int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF);
-  int np = SI(S, s, DVG_SHAPE_NUM_POINTS), th = SI(S, s, DVG_SHAPE_THICKNESS_OFF);
-  int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
-  int lo = njobs;
-  for (int k = 0; k < nseg; k++) {
-    int seg = S.seg_order[so + k];
-    if (nseg > 1 && !box_in_r(S.seg_box[so + seg], lp, S.seg_r[so + seg])) continue;
-    int nc = __ldg(&S.segment_ctrl[so + seg]), i0 = __ldg(&S.seg_point[so + seg]);
-    int f = within_segment_pre(S, po, np, th, flags, nc, i0, lp, r);
-    if (f == 2) {
-      if (njobs < DVG_LANE_JOBS) {
-        q->job[lane][njobs] = SegJob{s, so + seg, lp.x, lp.y, r};
-        if (mark) *mark |= 1u << njobs;
-        njobs++;
-        continue;
-      }
-      f = segment_root_test(S, po, np, th, nc, i0, lp, r);  // queue full: solve now
-    }
-    if (f == 1) {
-      if (mark) *mark &= (1u << lo) - 1u;
-      njobs = lo;  // decided: drop this shape's queued jobs
-      return 1;
-    }
-  }
-  return njobs > lo ? 2 : 0;
-}
-
-// group_stroke (within_distance.h:355-446) with queued segments; for the
-// group of an edge query every shape is tested and the queried shape's jobs
-// are marked in eq_jobs.
-DI int group_stroke_status(const DevScene &S, int g, v2 pt, WarpQueue *q, int lane, int &njobs, EdgeQ *eq,
-                           unsigned &eq_jobs) {
-  v2 lp = xform_pt(S.c2s + 9 * g, pt);
-  int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
-  bool is_eq = eq && eq->group == g;
-  int lo = njobs;
-  bool ret = false;
-  for (int k = 0; k < nsh; k++) {
-    int s = __ldg(&S.group_shapes[off + k]);
-    float r = stroke_width(S, s);
-    if (nsh > 1 && !box_in_r(S.s_box[s], lp, r)) continue;
-    int st = shape_stroke_status(S, s, lp, r, q, lane, njobs, (is_eq && s == eq->shape) ? &eq_jobs : nullptr);
-    if (st == 1) {
-      if (!is_eq) {
-        njobs = lo;
-        return 1;
-      }
-      ret = true;
-      if (s == eq->shape) eq->hit = 1;
-    }
-  }
-  if (ret) return 1;
-  return njobs > lo ? 2 : 0;
-}
-
 // Pass 1 of a sample: candidate fragments in group order, undecided stroke
 // segments queued.  Returns the number of candidate fragments (capped).
+//
+// All 32 lanes of the warp call it (lanes without a sample pass active =
+// false).  Each lane walks its own candidate list: tile groups, their
+// shapes, the shapes' segments, with the bounding-box culls, as the nested
+// loops of within_distance (within_distance.h:355-446) and sample_color
+// (diffvg.cpp:525-585) do.  The walk stops at each segment that needs a
+// test, and the segment tests of all lanes then run together, so that the
+// lanes that passed their culls at different groups still test in lockstep.
+// A shape that hits ends its own walk (and its group's, outside the group of
+// an edge query) as the reference's early returns do.
 DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q, int lane, int &njobs, EdgeQ *eq,
-                         unsigned &eq_jobs, bool &overflow) {
-  int b, e;
-  bool list = cand_range(S, pt, b, e);
+                         unsigned &eq_jobs, bool &overflow, bool active) {
+  int k = 0, e = 0;
+  bool list = true;
+  if (active) list = cand_range(S, pt, k, e);
+  const int G = S.num_groups;
   int nf = 0;
-  int G = S.num_groups;
-  for (int k = b; k < e; k++) {
-    int g = list ? __ldg(&S.tile_list[k]) : k;
-    if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
-    int sk = GI(S, g, DVG_GROUP_STROKE_KIND), fk = GI(S, g, DVG_GROUP_FILL_KIND);
-    if (sk != DVG_PAINT_NONE) {
-      int lo = njobs;
-      int st = group_stroke_status(S, g, pt, q, lane, njobs, eq, eq_jobs);
-      if (st != 0) {
-        if (nf < DVG_MAX_FRAGMENTS) frags[nf++] = FragRef{2 * g + 1, st == 1 ? DVG_META_HIT : (lo | (njobs << 8))};
-        else overflow = true;
+  // stroke part of the group in progress
+  int g = 0, nsh = 0, off = 0, si = 0, glo = 0;
+  bool in_group = false, is_eq = false, gret = false;
+  v2 lp = pt;
+  // path shape in progress
+  int s = 0, po = 0, np = 0, th = 0, sflags = 0, nseg = 0, so = 0, sg = 0, slo = 0;
+  float r = 0.f;
+  bool in_shape = false, mark = false;
+  auto emit = [&](int key, int meta) {
+    if (nf < DVG_MAX_FRAGMENTS) frags[nf++] = FragRef{key, meta};
+    else overflow = true;
+  };
+  auto fill = [&](int gg) {
+    if (GI(S, gg, DVG_GROUP_FILL_KIND) != DVG_PAINT_NONE && group_inside(S, gg, pt, eq)) emit(2 * gg, DVG_META_HIT);
+  };
+  while (true) {
+    // advance this lane to its next segment test (or a shape decided without one)
+    int nc = 0, i0 = 0, segi = 0;
+    bool have = false, shape_hit = false;
+    while (true) {
+      if (in_shape) {
+        if (sg < nseg) {
+          int seg = __ldg(&S.seg_order[so + sg]);
+          sg++;
+          if (nseg > 1 && !box_in_r(S.seg_box[so + seg], lp, S.seg_r[so + seg])) continue;
+          nc = __ldg(&S.segment_ctrl[so + seg]);
+          i0 = __ldg(&S.seg_point[so + seg]);
+          segi = so + seg;
+          have = true;
+          break;
+        }
+        in_shape = false;  // no segment hit: its queued jobs decide the shape
+        continue;
+      }
+      if (in_group) {
+        if (si < nsh) {
+          s = __ldg(&S.group_shapes[off + si]);
+          si++;
+          r = stroke_width(S, s);
+          if (nsh > 1 && !box_in_r(S.s_box[s], lp, r)) continue;
+          int kind = SI(S, s, DVG_SHAPE_KIND);
+          sflags = kind == DVG_PATH ? SI(S, s, DVG_SHAPE_FLAGS) : 0;
+          if (kind != DVG_PATH || (sflags & 2)) {
+            if (within_shape(S, s, lp, r)) {
+              slo = njobs;
+              mark = false;
+              shape_hit = true;
+              break;
+            }
+            continue;
+          }
+          po = SI(S, s, DVG_SHAPE_PARAM_OFF);
+          np = SI(S, s, DVG_SHAPE_NUM_POINTS);
+          th = SI(S, s, DVG_SHAPE_THICKNESS_OFF);
+          nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);
+          so = SI(S, s, DVG_SHAPE_SEG_OFF);
+          sg = 0;
+          slo = njobs;
+          mark = is_eq && s == eq->shape;
+          in_shape = true;
+          continue;
+        }
+        in_group = false;  // the group's stroke is decided up to its queued jobs
+        if (gret) emit(2 * g + 1, DVG_META_HIT);
+        else if (njobs > glo) emit(2 * g + 1, glo | (njobs << 8));
+        fill(g);
+        continue;
+      }
+      if (k >= e) break;
+      g = list ? __ldg(&S.tile_list[k]) : k;
+      k++;
+      if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
+      if (GI(S, g, DVG_GROUP_STROKE_KIND) != DVG_PAINT_NONE) {
+        lp = xform_pt(S.c2s + 9 * g, pt);
+        nsh = GI(S, g, DVG_GROUP_NUM_SHAPES);
+        off = GI(S, g, DVG_GROUP_SHAPES_OFF);
+        si = 0;
+        glo = njobs;
+        gret = false;
+        is_eq = eq && eq->group == g;
+        in_group = true;
+        continue;
+      }
+      fill(g);
+    }
+    if (!__any_sync(0xffffffffu, have || shape_hit)) break;
+    int f = shape_hit ? 1 : 0;
+    if (have) {
+      f = within_segment_pre(S, po, np, th, sflags, nc, i0, lp, r);  // the lanes' tests run together
+      if (f == 2) {
+        if (njobs < DVG_LANE_JOBS) {
+          q->job[lane][njobs] = SegJob{s, segi, lp.x, lp.y, r};
+          if (mark) eq_jobs |= 1u << njobs;
+          njobs++;
+          f = 0;
+        } else {
+          f = segment_solve(S, po, np, th, nc, i0, lp, r);  // queue full: solve now
+        }
       }
     }
-    if (fk != DVG_PAINT_NONE && group_inside(S, g, pt, eq)) {
-      if (nf < DVG_MAX_FRAGMENTS) frags[nf++] = FragRef{2 * g, DVG_META_HIT};
-      else overflow = true;
+    if (f == 1) {  // the shape hits
+      if (mark) eq_jobs &= (1u << slo) - 1u;
+      njobs = slo;  // its queued jobs are moot
+      in_shape = false;
+      if (!is_eq) {
+        njobs = glo;
+        in_group = false;
+        emit(2 * g + 1, DVG_META_HIT);
+        fill(g);
+      } else {
+        gret = true;
+        if (s == eq->shape) eq->hit = 1;
+      }
     }
   }
   return nf;
@@ -222,7 +300,7 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
   bool overflow = false;
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   if (eq) eq->hit = 0;
-  if (active) nf = collect_fragments(S, pt, frags, q, lane, njobs, eq, eq_jobs, overflow);
+  nf = collect_fragments(S, pt, frags, q, lane, njobs, eq, eq_jobs, overflow, active);
   warp_solve(S, q, lane, njobs);
   if (!active) return F4(0, 0, 0, 0);
   unsigned res = q->result[lane];
@@ -258,7 +336,7 @@ DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, fl
   unsigned eq_jobs = 0;
   bool overflow = false;
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
-  if (active) nf = collect_fragments(S, pt, frags, q, lane, njobs, nullptr, eq_jobs, overflow);
+  nf = collect_fragments(S, pt, frags, q, lane, njobs, nullptr, eq_jobs, overflow, active);
   warp_solve(S, q, lane, njobs);
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) {
