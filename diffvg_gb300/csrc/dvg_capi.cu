@@ -79,6 +79,13 @@ struct DvgScene {
   unsigned *err = nullptr;  // [0] status bits, [1] tile-list length
   // image-sized arenas
   DevBuf weight, samples, dbg_val, dbg_flag, edge;
+  // fragment cache of the last image forward (no prefiltering): per-sample
+  // hit keys and counts, a copy of its parameters and the stale flag the
+  // backward sets when its parameters differ
+  DevBuf hits;
+  bool hit_live = false;
+  int hit_w = 0, hit_h = 0, hit_nsx = 0, hit_nsy = 0;
+  uint64_t hit_seed = 0;
   unsigned *h_status = nullptr;  // pinned mirror of err[0..1]
   bool prepared = false;
   // per-kernel timing (dvg_scene_profile)
@@ -319,6 +326,27 @@ int prepare(DvgScene *sc, const DevScene &S, const DvgRenderArgs *a, cudaStream_
   return DVG_OK;
 }
 
+struct HitArena { int *keys; unsigned char *cnt; float *params; unsigned *stale; };
+
+size_t hit_bytes(DvgScene *sc, size_t n) {
+  return carve_size({DVG_HIT_SLOTS * n * sizeof(int), n, (size_t)sc->d.num_params * sizeof(float), sizeof(unsigned)});
+}
+
+HitArena hit_arena(DvgScene *sc, size_t n) {
+  char *p = reinterpret_cast<char *>(sc->hits.ptr);
+  HitArena h;
+  h.keys = carve<int>(p, DVG_HIT_SLOTS * n);
+  h.cnt = carve<unsigned char>(p, n);
+  h.params = carve<float>(p, sc->d.num_params);
+  h.stale = carve<unsigned>(p, 1);
+  return h;
+}
+
+bool hit_matches(const DvgScene *sc, const DvgRenderArgs *a) {
+  return sc->hit_live && sc->hit_w == a->width && sc->hit_h == a->height && sc->hit_nsx == a->num_samples_x &&
+         sc->hit_nsy == a->num_samples_y && sc->hit_seed == a->seed;
+}
+
 size_t edge_bytes(DvgScene *sc, size_t n) {
   size_t T = (size_t)sc->tiles_x * sc->tiles_y;
   return carve_size({n * sizeof(float4), n * sizeof(float4), n * sizeof(int4), n * sizeof(float2), n * sizeof(int),
@@ -496,6 +524,7 @@ int dvg_scene_destroy(DvgScene *sc) {
   sc->dbg_val.release();
   sc->dbg_flag.release();
   sc->edge.release();
+  sc->hits.release();
   if (sc->h_status) cudaFreeHost(sc->h_status);
   for (auto &p : sc->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   for (auto ev : sc->event_pool) cudaEventDestroy(ev);
@@ -566,8 +595,11 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
   DeviceGuard guard(sc->device);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   size_t npx = (size_t)a->width * a->height, n = npx * a->num_samples_x * a->num_samples_y;
+  sc->hit_live = false;
+  bool cache = image && !a->use_prefiltering;
   cudaError_t e = sc->weight.ensure(npx * sizeof(float));
   if (e == cudaSuccess && image) e = sc->samples.ensure(n * sizeof(float4));
+  if (e == cudaSuccess && cache) e = sc->hits.ensure(hit_bytes(sc, n));
   if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
   if (sc->d.num_groups == 0 && image) {
     // empty scene: the background (or transparent black), unfiltered
@@ -582,10 +614,26 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
     DevRender R = make_render(sc, a);
     if (image) {
       float4 *samples = reinterpret_cast<float4 *>(sc->samples.ptr);
+      HitArena h{};
+      if (cache) {
+        h = hit_arena(sc, n);
+        R.hit_keys = h.keys;
+        R.hit_cnt = h.cnt;
+      }
       timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
       timed(sc, K_SAMPLE_FWD, s, [&] { dvg::launch_sample_fwd(S, R, samples, s); });
       timed(sc, K_RESOLVE, s, [&] { dvg::launch_resolve(R, samples, image, s); });
       e = cudaGetLastError();
+      if (e == cudaSuccess && cache && sc->d.num_params > 0)
+        e = cudaMemcpyAsync(h.params, a->params, (size_t)sc->d.num_params * sizeof(float), cudaMemcpyDeviceToDevice, s);
+      if (e == cudaSuccess && cache) {
+        sc->hit_live = true;
+        sc->hit_w = a->width;
+        sc->hit_h = a->height;
+        sc->hit_nsx = a->num_samples_x;
+        sc->hit_nsy = a->num_samples_y;
+        sc->hit_seed = a->seed;
+      }
     } else {
       size_t nout = a->num_eval_positions > 0 ? (size_t)a->num_eval_positions : npx;
       e = cudaMemsetAsync(sdf, 0, nout * sizeof(float), s);
@@ -638,6 +686,15 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
       R.d_background = d_background;
       float4 *dbg_val = reinterpret_cast<float4 *>(sc->dbg_val.ptr);
       int *dbg_flag = reinterpret_cast<int *>(sc->dbg_flag.ptr);
+      if (!a->use_prefiltering && hit_matches(sc, a)) {
+        HitArena h = hit_arena(sc, n);
+        e = cudaMemsetAsync(h.stale, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return cuda_fail(e, "backward launch");
+        if (sc->d.num_params > 0) dvg::launch_hit_check(a->params, h.params, sc->d.num_params, h.stale, s);
+        R.hit_keys = h.keys;
+        R.hit_cnt = h.cnt;
+        R.hit_stale = h.stale;
+      }
       timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
       timed(sc, K_SAMPLE_BWD, s, [&] { dvg::launch_sample_bwd(S, R, dbg_val, dbg_flag, s); });
       if (d_background) timed(sc, K_BG_COMBINE, s, [&] { dvg::launch_bg_combine(S, R, dbg_val, dbg_flag, s); });

@@ -75,7 +75,15 @@ struct DevRender {
   float *d_background;       // [h*w*4] or null
   float *d_translation;      // [h*w*2] or null
   int filter_radius_off;
+  // fragment cache from the forward pass to the backward pass of the same
+  // parameters: the keys of each sample's hit fragments in blend order
+  // ([DVG_HIT_SLOTS][samples]) and their count (DVG_HIT_NONE: not cached)
+  int *hit_keys = nullptr;
+  unsigned char *hit_cnt = nullptr;
+  const unsigned *hit_stale = nullptr;  // backward: nonzero when the parameters differ from the forward's
 };
+#define DVG_HIT_SLOTS 8
+#define DVG_HIT_NONE 255
 
 // Boundary samples filed by canvas tile (edge-sampling pass), n entries
 // each; tile_count / tile_start have one entry per canvas tile (+1).

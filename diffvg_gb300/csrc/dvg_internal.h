@@ -28,6 +28,7 @@ cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4
 // CUDA events between them for per-kernel timing).
 void launch_weight(const DevScene &S, const DevRender &R, cudaStream_t st);
 void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, cudaStream_t st);
+void launch_hit_check(const float *params, const float *fwd_params, int n, unsigned *stale, cudaStream_t st);
 void launch_resolve(const DevRender &R, const float4 *samples, float *image, cudaStream_t st);
 // dbg_val / dbg_flag: per-sample background adjoint scratch (only written
 // when R.d_background is set).

@@ -77,7 +77,13 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_sample_fwd(DevSc
   const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
   float4 c;
   if (PREFILTER) c = sample_color_prefiltered_fwd(S, bg, npt);
-  else c = sample_color_fwd(S, bg, npt, nullptr, active, &wq[threadIdx.x >> 5], threadIdx.x & 31);
+  else {
+    int n = R.w * R.h * R.spp;
+    bool cache = R.hit_keys && !bins_overflowed(S);
+    if (active && R.hit_cnt && !cache) R.hit_cnt[idx] = DVG_HIT_NONE;
+    c = sample_color_fwd(S, bg, npt, nullptr, active, &wq[threadIdx.x >> 5], threadIdx.x & 31,
+                         cache ? R.hit_keys : nullptr, cache ? R.hit_cnt : nullptr, n, idx);
+  }
   if (active) samples[idx] = c;
 }
 
@@ -143,8 +149,13 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_sample_bwd(DevSc
     color = active ? sample_color_prefiltered_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params)
                    : F4(0, 0, 0, 0);
   } else {
+    int cached = -1;
+    if (active && R.hit_cnt && *R.hit_stale == 0u) {
+      int c = R.hit_cnt[idx];
+      if (c != DVG_HIT_NONE) cached = c;
+    }
     color = sample_color_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params, active, &wq[threadIdx.x >> 5],
-                             threadIdx.x & 31);
+                             threadIdx.x & 31, R.hit_keys, R.w * R.h * R.spp, idx, cached);
   }
   if (active) {
     if (R.d_background) { dbg_val[idx] = dbg; dbg_flag[idx] = assign; }
@@ -333,6 +344,14 @@ __global__ void __launch_bounds__(256) k_sdf(DevScene S, DevRender R, const floa
   }
 }
 
+// bitwise comparison of the parameter arena with the forward pass's copy
+__global__ void k_hit_check(const float *params, const float *fwd_params, int n, unsigned *stale) {
+  const unsigned *a = reinterpret_cast<const unsigned *>(params), *b = reinterpret_cast<const unsigned *>(fwd_params);
+  bool diff = false;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) diff |= a[i] != b[i];
+  if (__syncthreads_or(diff) && threadIdx.x == 0) atomicOr(stale, 1u);
+}
+
 static inline int tiles_of(const DevRender &R) {
   return ((R.w + DVG_TILE - 1) / DVG_TILE) * ((R.h + DVG_TILE - 1) / DVG_TILE);
 }
@@ -345,6 +364,10 @@ void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, c
   dim3 grid(tiles_of(R), R.spp);
   if (R.prefilter) k_sample_fwd<true><<<grid, 256, 0, st>>>(S, R, samples);
   else k_sample_fwd<false><<<grid, 256, 0, st>>>(S, R, samples);
+}
+void launch_hit_check(const float *params, const float *fwd_params, int n, unsigned *stale, cudaStream_t st) {
+  int blocks = (n + 255) / 256;
+  k_hit_check<<<blocks < 1 ? 1 : (blocks > 1216 ? 1216 : blocks), 256, 0, st>>>(params, fwd_params, n, stale);
 }
 void launch_resolve(const DevRender &R, const float4 *samples, float *image, cudaStream_t st) {
   k_resolve<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(R, samples, image);

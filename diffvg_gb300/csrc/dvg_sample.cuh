@@ -292,8 +292,11 @@ DI bool frag_hit(int meta, unsigned res) {
 // decides; without such a fragment the flag keeps what the coverage tests
 // of the queried shape set (diffvg.cpp:624-633).
 // Out of line: the boundary pass calls it twice per sample.
+// With hit_keys set, the sample's hit fragment keys (blend order) and their
+// count are stored for the backward pass (sample idx of n).
 static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq,
-                                                      bool active, WarpQueue *q, int lane) {
+                                                      bool active, WarpQueue *q, int lane, int *hit_keys = nullptr,
+                                                      unsigned char *hit_cnt = nullptr, int n = 0, int idx = 0) {
   FragRef frags[DVG_MAX_FRAGMENTS];
   int nf = 0, njobs = 0;
   unsigned eq_jobs = 0;
@@ -317,8 +320,10 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
                                  GI(S, g, DVG_GROUP_FILL_STOPS), pt);
     if (eq) ev = (eq->group == g) ? 1 : (c.w >= 1.f ? 0 : ev);
     blend(acc, c);
+    if (hit_keys && nhit < DVG_HIT_SLOTS) hit_keys[(size_t)nhit * n + idx] = frags[i].key;
     nhit++;
   }
+  if (hit_cnt) hit_cnt[idx] = (overflow || nhit > DVG_HIT_SLOTS) ? DVG_HIT_NONE : (unsigned char)nhit;
   if (overflow || nhit > DVG_MAX_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
   if (eq && ev >= 0) eq->hit = ev;
   if (nhit <= 0) return bg ? *bg : F4(0, 0, 0, 0);
@@ -329,14 +334,21 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
 // d_bg receives the background adjoint with the reference's semantics:
 // *assign = 1 when the sample has no fragment (the reference then
 // overwrites the pixel's background gradient with d_color).
+// cached >= 0: the forward pass's hit fragments of this sample (cached of
+// them, keys in hit_keys) stand in for collecting and deciding them again.
 DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color, float4 *d_bg,
-                           int *assign, float *d_tr, float *dp, bool active, WarpQueue *q, int lane) {
+                           int *assign, float *d_tr, float *dp, bool active, WarpQueue *q, int lane,
+                           const int *hit_keys, int n, int idx, int cached) {
   FragRef frags[DVG_MAX_FRAGMENTS];
   int nf = 0, njobs = 0;
   unsigned eq_jobs = 0;
   bool overflow = false;
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
-  nf = collect_fragments(S, pt, frags, q, lane, njobs, nullptr, eq_jobs, overflow, active);
+  nf = collect_fragments(S, pt, frags, q, lane, njobs, nullptr, eq_jobs, overflow, active && cached < 0);
+  if (active && cached >= 0) {
+    nf = cached;
+    for (int i = 0; i < nf; i++) frags[i] = FragRef{__ldg(&hit_keys[(size_t)i * n + idx]), DVG_META_HIT};
+  }
   warp_solve(S, q, lane, njobs);
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) {

@@ -40,6 +40,15 @@ def _run(builder, spp, seed, prefilter=False):
     den = np.linalg.norm(rb['d_params'])
     print('d_params rel L2 %.3g' % (num / den))
     assert num / den <= GRAD_TOL
+    # forward then backward on one scene handle: the backward takes the
+    # forward's fragment cache
+    from diffvg_gb300 import _native
+    sc = _native.NativeScene(packed)
+    nu.render(packed, P, w, h, spp, spp, seed, scene=sc)
+    mc = nu.render(packed, P, w, h, spp, spp, seed, d_out=d_img, scene=sc)
+    num = np.linalg.norm(mc['d_params'] - rb['d_params'])
+    print('d_params rel L2 (after forward) %.3g' % (num / den))
+    assert num / den <= GRAD_TOL
 
 
 def test_circle_scene():
