@@ -76,6 +76,8 @@ struct DvgScene {
   float *seg_r = nullptr, *seg_pmf = nullptr, *seg_cdf = nullptr, *smp_cdf = nullptr, *smp_pmf = nullptr;
   int *seg_order = nullptr, *tile_start = nullptr, *tile_count = nullptr, *scratch = nullptr;
   int4 *g_tile_range = nullptr;
+  float2 *seg_tpts = nullptr;
+  float *seg_th = nullptr;
   unsigned *err = nullptr;  // [0] status bits, [1] tile-list length
   // image-sized arenas
   DevBuf weight, samples, dbg_val, dbg_flag, edge;
@@ -244,6 +246,8 @@ DevScene make_dev(DvgScene *sc, const float *params) {
   S.s_length = sc->s_length;
   S.seg_box = sc->seg_box;
   S.seg_r = sc->seg_r;
+  S.seg_tpts = sc->seg_tpts;
+  S.seg_th = sc->seg_th;
   S.seg_pmf = sc->seg_pmf;
   S.seg_cdf = sc->seg_cdf;
   S.seg_order = sc->seg_order;
@@ -478,7 +482,8 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
       sizeof(float) * NT, sizeof(float) * NT,                                              // smp cdf/pmf
       sizeof(int) * (T + 1), sizeof(int) * T, sizeof(int4) * G,                           // tiles
       sizeof(int) * (10 * (size_t)NSEG + 8 * (size_t)S + 8),                              // scratch
-      sizeof(unsigned) * 4};
+      sizeof(unsigned) * 4,
+      sizeof(float2) * DVG_TREE_PTS * (size_t)NSEG, sizeof(float) * DVG_TREE_NODES * (size_t)NSEG};  // trees
   e = sc->derived.ensure(carve_size(db));
   if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "allocating scene arenas"); }
   p = reinterpret_cast<char *>(sc->derived.ptr);
@@ -500,6 +505,8 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   sc->g_tile_range = carve<int4>(p, G);
   sc->scratch = carve<int>(p, 10 * (size_t)NSEG + 8 * (size_t)S + 8);
   sc->err = carve<unsigned>(p, 4);
+  sc->seg_tpts = carve<float2>(p, DVG_TREE_PTS * (size_t)NSEG);
+  sc->seg_th = carve<float>(p, DVG_TREE_NODES * (size_t)NSEG);
   e = cudaMemset(sc->derived.ptr, 0, sc->derived.bytes);
   if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "clearing scene arenas"); }
   size_t cap = (size_t)T * 32;

@@ -56,6 +56,8 @@ struct DevScene {
   int *tile_start;          // [tiles+1]
   int *tile_list;           // candidate groups per tile, ascending
   int *scratch;             // [8*NSEG + 8*S] path leaf-order scratch
+  float2 *seg_tpts = nullptr;  // [NSEG * DVG_TREE_PTS] tabulated subdivision trees (curved segments), or null
+  float *seg_th = nullptr;     // [NSEG * DVG_TREE_NODES]
   unsigned *err;            // status word (DVG_EFLAG_*)
 };
 
@@ -629,18 +631,6 @@ DI bool quad_far(v2 p0, v2 p1, v2 p2, v2 pt, float thr) {
          quad_lb(rc, r2, p2, pt) > thr;
 }
 
-// Certified fp32 outside proof for the stroke test of one Bezier segment.
-// The segment is subdivided (stackless depth-first walk of the binary
-// subdivision tree, sub-pieces from blossoms of the original control points)
-// and a piece whose capsule bound is farther than r_out + m is pruned.
-// Returns 0 when every piece is pruned: no point of the curve is within the
-// stroke radius, so the reference's candidates (end points and quintic
-// roots, all on the curve) fail its test as well.  Returns -2 otherwise,
-// early when a curve point is closer than r_out - m, and the caller runs the
-// reference's fp64 root solve.  No inside proof is attempted: the
-// reference's quintic root isolation can miss the closest root (two roots in
-// one isolation interval) and then reports "outside" for a sample that is
-// geometrically inside; the renderer reproduces the reference.
 #define DVG_SUBDIV_DEPTH 8
 DI v2 lerp2(v2 a, v2 b, float u) { return V2(a.x + u * (b.x - a.x), a.y + u * (b.y - a.y)); }
 DI v2 cubic_blossom(v2 p0, v2 p1, v2 p2, v2 p3, float u, float v, float w) {
@@ -651,43 +641,80 @@ DI v2 cubic_blossom(v2 p0, v2 p1, v2 p2, v2 p3, float u, float v, float w) {
 DI v2 quad_blossom(v2 p0, v2 p1, v2 p2, float u, float v) {
   return lerp2(lerp2(p0, p1, u), lerp2(p1, p2, u), v);
 }
-DI int cubic_stroke_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float r_out, float m) {
-  float thr_out = r_out + m;
-  float near = r_out - m;
-  float near2 = near > 0.f ? near * near : -1.f;
-  unsigned node = 1;
-  for (int guard = 0; guard < (2 << DVG_SUBDIV_DEPTH) + 2; guard++) {
-    int d = 31 - __clz(node);
-    float scale = __int_as_float((127 - d) << 23);  // 2^-d, exact
-    float ta = (float)(node - (1u << d)) * scale, tb = ta + scale;
-    v2 q0 = cubic_blossom(p0, p1, p2, p3, ta, ta, ta), q3 = cubic_blossom(p0, p1, p2, p3, tb, tb, tb);
-    // a curve point this close: no outside proof can exist
-    if (distsq2(q0, pt) < near2 || distsq2(q3, pt) < near2) return -2;
-    v2 q1 = cubic_blossom(p0, p1, p2, p3, ta, ta, tb), q2 = cubic_blossom(p0, p1, p2, p3, ta, tb, tb);
-    if (cubic_lb(q0, q1, q2, q3, pt) <= thr_out) {
-      if (d >= DVG_SUBDIV_DEPTH) return -2;
-      node <<= 1;
-      continue;
-    }
-    while (node & 1u) node >>= 1;
-    if (node == 0u) return 0;
-    node += 1;
+// Levels 0..DVG_TREE_DEPTH of each curved segment's subdivision tree are
+// tabulated per call (k_seg_tree): the curve points at t = k / 2^D (the end
+// points of every tabulated piece) and each piece's hull width, the largest
+// distance of its inner control points from its chord.  Deeper pieces are
+// formed from blossoms on the fly.  Tabulated and on-the-fly pieces hold the
+// same fp32 values.
+#define DVG_TREE_DEPTH 5
+#define DVG_TREE_PTS ((1 << DVG_TREE_DEPTH) + 1)
+#define DVG_TREE_NODES (2 << DVG_TREE_DEPTH)  // heap order, entry 0 unused
+
+// distance from p to the segment ab greater than T (T >= 0), without roots or divisions
+DI bool seg_far(v2 a, v2 b, v2 p, float T) {
+  v2 ab = sub2(b, a), ap = sub2(p, a);
+  float T2 = T * T;
+  float dt = dot2(ap, ab);
+  if (dt <= 0.f) return dot2(ap, ap) > T2;
+  float l2 = dot2(ab, ab);
+  if (dt >= l2) {
+    v2 bp = sub2(p, b);
+    return dot2(bp, bp) > T2;
   }
-  return -2;
+  float cr = ap.x * ab.y - ap.y * ab.x;
+  return cr * cr > T2 * l2;
 }
-DI int quad_stroke_fast(v2 p0, v2 p1, v2 p2, v2 pt, float r_out, float m) {
+DI float cubic_hull_width(v2 q0, v2 q1, v2 q2, v2 q3) { return fmaxf(dist_to_seg(q0, q3, q1), dist_to_seg(q0, q3, q2)); }
+DI float quad_hull_width(v2 q0, v2 q1, v2 q2) { return dist_to_seg(q0, q2, q1); }
+
+// Certified fp32 outside proof for the stroke test of one Bezier segment
+// (nc = 1 quadratic: p3 unused; nc = 2 cubic).  The segment is subdivided
+// (stackless depth-first walk of the binary subdivision tree) and a piece
+// whose capsule bound (distance to its chord less its hull width) is farther
+// than r_out + m is pruned.  tp / th: the segment's tabulated tree, or null.
+// Returns 0 when every piece is pruned: no point of the curve is within the
+// stroke radius, so the reference's candidates (end points and quintic or
+// cubic roots, all on the curve) fail its test as well.  Returns -2
+// otherwise, early when a curve point is closer than r_out - m, and the
+// caller runs the root-walk decision.  No inside proof is attempted: the
+// reference's quintic root isolation can miss the closest root (two roots in
+// one isolation interval) and then reports "outside" for a sample that is
+// geometrically inside; the renderer reproduces the reference.
+template <int NC>
+DI int curve_stroke_fast(v2 p0, v2 p1, v2 p2, v2 p3, const float2 *tp, const float *th, v2 pt, float r_out,
+                         float m) {
   float thr_out = r_out + m;
   float near = r_out - m;
   float near2 = near > 0.f ? near * near : -1.f;
   unsigned node = 1;
   for (int guard = 0; guard < (2 << DVG_SUBDIV_DEPTH) + 2; guard++) {
     int d = 31 - __clz(node);
-    float scale = __int_as_float((127 - d) << 23);
-    float ta = (float)(node - (1u << d)) * scale, tb = ta + scale;
-    v2 q0 = quad_blossom(p0, p1, p2, ta, ta), q2 = quad_blossom(p0, p1, p2, tb, tb);
-    if (distsq2(q0, pt) < near2 || distsq2(q2, pt) < near2) return -2;
-    v2 q1 = quad_blossom(p0, p1, p2, ta, tb);
-    if (quad_lb(q0, q1, q2, pt) <= thr_out) {
+    v2 q0, qe;
+    float h;
+    if (tp && d <= DVG_TREE_DEPTH) {
+      unsigned k = node - (1u << d);
+      int sh = DVG_TREE_DEPTH - d;
+      q0 = tp[k << sh];
+      qe = tp[(k + 1) << sh];
+      h = th[node];
+    } else {
+      float scale = __int_as_float((127 - d) << 23);  // 2^-d, exact
+      float ta = (float)(node - (1u << d)) * scale, tb = ta + scale;
+      if (NC == 2) {
+        q0 = cubic_blossom(p0, p1, p2, p3, ta, ta, ta);
+        qe = cubic_blossom(p0, p1, p2, p3, tb, tb, tb);
+        h = cubic_hull_width(q0, cubic_blossom(p0, p1, p2, p3, ta, ta, tb), cubic_blossom(p0, p1, p2, p3, ta, tb, tb),
+                             qe);
+      } else {
+        q0 = quad_blossom(p0, p1, p2, ta, ta);
+        qe = quad_blossom(p0, p1, p2, tb, tb);
+        h = quad_hull_width(q0, quad_blossom(p0, p1, p2, ta, tb), qe);
+      }
+    }
+    // a curve point this close: no outside proof can exist
+    if (distsq2(q0, pt) < near2 || distsq2(qe, pt) < near2) return -2;
+    if (!seg_far(q0, qe, pt, thr_out + h)) {
       if (d >= DVG_SUBDIV_DEPTH) return -2;
       node <<= 1;
       continue;
@@ -1004,7 +1031,8 @@ static __device__ __noinline__ int segment_root_test(const DevScene &S, int po, 
 // lines exactly, quadratic / cubic end points exactly, then the fp32
 // outside proof.  1: within, 0: not, -1: the path reports "not within"
 // (distance-approximated quadratics), 2: undecided (segment_solve decides).
-DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, int nc, int i0, v2 pt, float r) {
+DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, int nc, int i0, int segi, v2 pt,
+                          float r) {
   if (nc == 0) {
     int i1 = (i0 + 1) % np;
     v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1);
@@ -1027,7 +1055,9 @@ DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, 
     if (distsq2(eval_quad(p0, p1, p2, 0), pt) < r0 * r0) return 1;
     if (distsq2(eval_quad(p0, p1, p2, 1), pt) < r2 * r2) return 1;
     float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(absmax2(p2), absmax2(pt)));
-    return quad_stroke_fast(p0, p1, p2, pt, fmaxf(r0, fmaxf(r1, r2)), far_margin(m)) == 0 ? 0 : 2;
+    const float2 *tp = S.seg_tpts ? S.seg_tpts + (size_t)segi * DVG_TREE_PTS : nullptr;
+    const float *tw = S.seg_th ? S.seg_th + (size_t)segi * DVG_TREE_NODES : nullptr;
+    return curve_stroke_fast<1>(p0, p1, p2, p2, tp, tw, pt, fmaxf(r0, fmaxf(r1, r2)), far_margin(m)) == 0 ? 0 : 2;
   }
   int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
   v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2), p3 = path_pt(S, po, i3);
@@ -1036,7 +1066,10 @@ DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, 
   if (distsq2(eval_cubic(p0, p1, p2, p3, 0), pt) < r0 * r0) return 1;
   if (distsq2(eval_cubic(p0, p1, p2, p3, 1), pt) < r3 * r3) return 1;
   float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
-  return cubic_stroke_fast(p0, p1, p2, p3, pt, fmaxf(fmaxf(r0, r1), fmaxf(r2, r3)), far_margin(m)) == 0 ? 0 : 2;
+  const float2 *tp = S.seg_tpts ? S.seg_tpts + (size_t)segi * DVG_TREE_PTS : nullptr;
+  const float *tw = S.seg_th ? S.seg_th + (size_t)segi * DVG_TREE_NODES : nullptr;
+  return curve_stroke_fast<2>(p0, p1, p2, p3, tp, tw, pt, fmaxf(fmaxf(r0, r1), fmaxf(r2, r3)), far_margin(m)) == 0 ? 0
+                                                                                                               : 2;
 }
 
 // fp32 decision of an undecided segment (cubics: cubic_stroke_decide); 2
@@ -1057,8 +1090,9 @@ DI int segment_solve(const DevScene &S, int po, int np, int th, int nc, int i0, 
 }
 
 // 1: within, 0: not, -1: the path reports "not within" (approx quadratics)
-DI int within_segment(const DevScene &S, int s, int po, int np, int th, int flags, int nc, int i0, v2 pt, float r) {
-  int f = within_segment_pre(S, po, np, th, flags, nc, i0, pt, r);
+DI int within_segment(const DevScene &S, int s, int po, int np, int th, int flags, int nc, int i0, int segi, v2 pt,
+                      float r) {
+  int f = within_segment_pre(S, po, np, th, flags, nc, i0, segi, pt, r);
   if (f == 2) f = segment_solve(S, po, np, th, nc, i0, pt, r);
   return f;
 }
@@ -1092,7 +1126,7 @@ DI bool within_shape(const DevScene &S, int s, v2 pt, float r) {
     int seg = S.seg_order[so + k];
     if (nseg > 1 && !box_in_r(S.seg_box[so + seg], pt, S.seg_r[so + seg])) continue;
     int h = within_segment(S, s, po, np, th, flags, __ldg(&S.segment_ctrl[so + seg]), __ldg(&S.seg_point[so + seg]),
-                           pt, r);
+                           so + seg, pt, r);
     if (h == 1) return true;
     if (h == -1) return false;
   }

@@ -180,6 +180,43 @@ __device__ __forceinline__ int clamp_tile(double f, int hi, bool lower) {
   return f > hi - 1 ? hi - 1 : (f < 0 ? -1 : (int)f);
 }
 
+// Tabulated subdivision trees of the curved path segments (one warp per
+// shape, lanes over its segments): the curve points at t = k / 2^D and the
+// hull width of every piece of levels 0..D, formed exactly as the outside
+// proof forms them (curve_stroke_fast).
+__global__ void k_seg_tree(DevScene S) {
+  int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (s >= S.num_shapes || !S.seg_tpts || SI(S, s, DVG_SHAPE_KIND) != DVG_PATH) return;
+  int po = SI(S, s, DVG_SHAPE_PARAM_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
+  int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF);
+  for (int i = lane; i < nseg; i += 32) {
+    int nc = S.segment_ctrl[so + i], i0 = S.seg_point[so + i];
+    if (nc != 1 && nc != 2) continue;
+    float2 *tp = S.seg_tpts + (size_t)(so + i) * DVG_TREE_PTS;
+    float *th = S.seg_th + (size_t)(so + i) * DVG_TREE_NODES;
+    v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1);
+    v2 p2 = path_pt(S, po, nc == 2 ? i0 + 2 : (i0 + 2) % np), p3 = nc == 2 ? path_pt(S, po, (i0 + 3) % np) : p2;
+    const float step = __int_as_float((127 - DVG_TREE_DEPTH) << 23);  // 2^-D
+    for (int k = 0; k < DVG_TREE_PTS; k++) {
+      float t = (float)k * step;
+      tp[k] = nc == 2 ? cubic_blossom(p0, p1, p2, p3, t, t, t) : quad_blossom(p0, p1, p2, t, t);
+    }
+    th[0] = 0.f;
+    for (unsigned node = 1; node < DVG_TREE_NODES; node++) {
+      int d = 31 - __clz(node);
+      float scale = __int_as_float((127 - d) << 23);
+      float ta = (float)(node - (1u << d)) * scale, tb = ta + scale;
+      th[node] = nc == 2 ? cubic_hull_width(cubic_blossom(p0, p1, p2, p3, ta, ta, ta),
+                                            cubic_blossom(p0, p1, p2, p3, ta, ta, tb),
+                                            cubic_blossom(p0, p1, p2, p3, ta, tb, tb),
+                                            cubic_blossom(p0, p1, p2, p3, tb, tb, tb))
+                         : quad_hull_width(quad_blossom(p0, p1, p2, ta, ta), quad_blossom(p0, p1, p2, ta, tb),
+                                           quad_blossom(p0, p1, p2, tb, tb));
+    }
+  }
+}
+
 __global__ void k_group_prep(DevScene S, int4 *g_tile_range) {
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= S.num_groups) return;
@@ -361,6 +398,7 @@ cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4
   int T = S.tiles_x * S.tiles_y;
   if (G > 0) k_group_xform<<<(G + 127) / 128, 128, 0, st>>>(S);
   if (NS > 0) k_shape_prep<<<(NS + 63) / 64, 64, 0, st>>>(S);
+  if (NS > 0 && S.seg_tpts) k_seg_tree<<<(NS + 3) / 4, 128, 0, st>>>(S);
   if (G > 0) k_group_prep<<<(G + 127) / 128, 128, 0, st>>>(S, g_tile_range);
   k_sampling_cdf<<<1, 256, 0, st>>>(S);
   k_bin_count<<<T, 128, 0, st>>>(S, g_tile_range, tile_count);

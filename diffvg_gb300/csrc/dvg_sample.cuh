@@ -249,7 +249,7 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
     if (!__any_sync(0xffffffffu, have || shape_hit)) break;
     int f = shape_hit ? 1 : 0;
     if (have) {
-      f = within_segment_pre(S, po, np, th, sflags, nc, i0, lp, r);  // the lanes' tests run together
+      f = within_segment_pre(S, po, np, th, sflags, nc, i0, segi, lp, r);  // the lanes' tests run together
       if (f == 2) {
         if (njobs < DVG_LANE_JOBS) {
           q->job[lane][njobs] = SegJob{s, segi, lp.x, lp.y, r};

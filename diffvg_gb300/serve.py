@@ -43,6 +43,7 @@ def estimate_device_bytes(packed, width, height, spp):
     samples = 16 * n                                # forward sample colours
     edges = 68 * n                                  # boundary-sample records and ordering
     scene = 4 * (8 * ns + 12 * ng + 2 * nseg + 2 * ng) + 64 * ng + 40 * ns + 48 * nseg + 4 * (10 * nseg + 8 * ns)
+    scene += (8 * 33 + 4 * 64) * nseg                # tabulated subdivision trees of the segments
     tile_lists = 4 * max(65536, 32 * tiles) * 5 // 4 + 8 * tiles
     return int(params + images + samples + edges + scene + tile_lists + (1 << 20))
 
