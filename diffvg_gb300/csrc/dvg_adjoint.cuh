@@ -12,7 +12,7 @@ DI double dcos(float x) { return cos((double)x); }
 DI double dsin(float x) { return sin((double)x); }
 
 // d_closest_point for paths (compute_distance.h:442-897)
-DI void d_closest_path(const DevScene &S, int s, v2 pt, v2 d_cp, const PathInfo &info, float *dp, v2 *d_pt) {
+DN void d_closest_path(const DevScene &S, int s, v2 pt, v2 d_cp, const PathInfo &info, float *dp, v2 *d_pt) {
   int np = SI(S, s, DVG_SHAPE_NUM_POINTS), so = SI(S, s, DVG_SHAPE_SEG_OFF);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
   int bp = info.base_point_id, i0 = info.point_id;
@@ -277,7 +277,7 @@ DI v2 perturb(v2 ret, v2 *normal, float dir, float r) {
 }
 
 // per-shape boundary samplers (sample_boundary.h:20-384)
-DI v2 sample_shape_boundary(const DevScene &S, int s, float t, v2 *normal, float *pdf, BData *bd, float dir) {
+DN v2 sample_shape_boundary(const DevScene &S, int s, float t, v2 *normal, float *pdf, BData *bd, float dir) {
   int kind = SI(S, s, DVG_SHAPE_KIND);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
   float sr = stroke_width(S, s);
@@ -441,7 +441,7 @@ DI v2 sample_boundary(const DevScene &S, int g, int s, float t, v2 *normal, floa
 }
 
 // accumulate_boundary_gradient (diffvg.cpp:89-274)
-DI void accumulate_boundary_gradient(const DevScene &S, int g, int s, float contrib, float t, v2 normal,
+DN void accumulate_boundary_gradient(const DevScene &S, int g, int s, float contrib, float t, v2 normal,
                                      const BData &bd, v2 local_pt, float *dp) {
   int kind = SI(S, s, DVG_SHAPE_KIND), po = SI(S, s, DVG_SHAPE_PARAM_OFF);
   int th = kind == DVG_PATH ? SI(S, s, DVG_SHAPE_THICKNESS_OFF) : -1;

@@ -101,6 +101,8 @@ struct EdgeRecords {
 typedef float2 v2;
 
 #define DI __device__ __forceinline__
+// out of line: large routines that would otherwise be copied into every caller
+#define DN static __device__ __noinline__
 
 DI v2 V2(float x, float y) { return make_float2(x, y); }
 DI v2 add2(v2 a, v2 b) { return V2(a.x + b.x, a.y + b.y); }
@@ -228,7 +230,7 @@ DI bool solve_quadratic_d(double a, double b, double c, double *t0, double *t1) 
   if (*t0 > *t1) { double tmp = *t0; *t0 = *t1; *t1 = tmp; }
   return true;
 }
-DI int solve_cubic_d(double a, double b, double c, double d, double t[3]) {
+DN int solve_cubic_d(double a, double b, double c, double d, double t[3]) {
   if (fabs(a) < 1e-6f) return solve_quadratic_d(b, c, d, &t[0], &t[1]) ? 2 : 0;
   b /= a; c /= a; d /= a;
   double Q = (b * b - 3 * c) / 9.f;
@@ -480,12 +482,13 @@ DI int winding_shape(const DevScene &S, int s, v2 pt) {
 struct EdgeQ { int group, shape, hit; };
 
 // is_inside (diffvg.cpp:33-87)
-DI bool group_inside(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
+DN bool group_inside(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
   v2 lp = xform_pt(S.c2s + 9 * g, pt);
   if (!box_in(S.g_local_box[g], lp)) return false;
   int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
   int eo = GI(S, g, DVG_GROUP_EVEN_ODD);
   int w = 0;
+  #pragma unroll 1
   for (int k = 0; k < nsh; k++) {
     int s = __ldg(&S.group_shapes[off + k]);
     if (nsh > 1 && !box_in(S.s_box[s], lp)) continue;
@@ -502,7 +505,7 @@ DI bool group_inside(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
 // stroke coverage (within_distance.h:8-446)
 
 // quadratic_closest_pt_approx (vector.h:787-817)
-DI v2 quad_closest_approx(v2 b0, v2 b1, v2 b2, v2 pt, float *t_out) {
+DN v2 quad_closest_approx(v2 b0, v2 b1, v2 b2, v2 pt, float *t_out) {
   b0 = sub2(b0, pt); b1 = sub2(b1, pt); b2 = sub2(b2, pt);
   float a = det2(b0, b2), b = 2 * det2(b1, b0), d = 2 * det2(b2, b1);
   float f = b * d - a * a;
@@ -565,6 +568,7 @@ DI int quintic_intervals(const Quintic &q, float iv[4]) {
 // there and is skipped, which leaves every result unchanged.
 DI float quintic_root(const Quintic &q, float lb, float ub) {
   float t = 0.5f * (lb + ub);
+  #pragma unroll 1
   for (int it = 0; it < 20; it++) {
     if (!(t >= lb && t <= ub)) t = 0.5f * (lb + ub);
     double value = quintic_eval(q, t);
@@ -682,12 +686,13 @@ DI float quad_hull_width(v2 q0, v2 q1, v2 q2) { return dist_to_seg(q0, q2, q1); 
 // one isolation interval) and then reports "outside" for a sample that is
 // geometrically inside; the renderer reproduces the reference.
 template <int NC>
-DI int curve_stroke_fast(v2 p0, v2 p1, v2 p2, v2 p3, const float2 *tp, const float *th, v2 pt, float r_out,
+DN int curve_stroke_fast(v2 p0, v2 p1, v2 p2, v2 p3, const float2 *tp, const float *th, v2 pt, float r_out,
                          float m) {
   float thr_out = r_out + m;
   float near = r_out - m;
   float near2 = near > 0.f ? near * near : -1.f;
   unsigned node = 1;
+  #pragma unroll 1
   for (int guard = 0; guard < (2 << DVG_SUBDIV_DEPTH) + 2; guard++) {
     int d = 31 - __clz(node);
     v2 q0, qe;
@@ -745,6 +750,7 @@ DI int curve_stroke_fast(v2 p0, v2 p1, v2 p2, v2 p3, const float2 *tp, const flo
 // must clear the radius by a margin that covers where in the stopping window
 // the reference lands.  Returns 1 or 0 when that decides the outcome, 2 when
 // any enclosure is inconclusive (the fp64 solve then runs).
+#define DVG_EMU_NEWTON 6  // Newton steps per root (each root is certified afterwards)
 DI float emu_p3(float c3, float c2, float c1, float c0, float t) { return ((c3 * t + c2) * t + c1) * t + c0; }
 DI float emu_q(const float n[6], float t) { return ((((t + n[1]) * t + n[2]) * t + n[3]) * t + n[4]) * t + n[5]; }
 // Bernstein coefficients on [l,u] of the quartic with [0,1]-Bernstein coefficients b (blossoming)
@@ -790,21 +796,24 @@ DI int emu_cubic_roots01(float c3, float c2, float c1, float c0, float del, floa
   int n = 0;
   float ya = emu_p3(c3, c2, c1, c0, ts[0]);
   if (fabsf(ya) <= del) return -1;
+#pragma unroll 1
   for (int k = 1; k < nt; k++) {
     float yb = emu_p3(c3, c2, c1, c0, ts[k]);
     if (fabsf(yb) <= del) return -1;
     if ((ya < 0) != (yb < 0)) {
       float lo = ts[k - 1], hi = ts[k];
       bool up = yb > ya;
-      for (int it = 0; it < 32; it++) {
-        float m = 0.5f * (lo + hi);
-        if (m <= lo || m >= hi) break;
-        if ((emu_p3(c3, c2, c1, c0, m) > 0) == up) hi = m; else lo = m;
-      }
       float r = 0.5f * (lo + hi);
+#pragma unroll 1
+      for (int it = 0; it < DVG_EMU_NEWTON; it++) {  // Newton kept inside the bracket
+        float y = emu_p3(c3, c2, c1, c0, r), dy = (3 * c3 * r + 2 * c2) * r + c1;
+        if ((y > 0) == up) hi = r; else lo = r;
+        float nr = r - __fdividef(y, dy);
+        r = (nr >= lo && nr <= hi) ? nr : 0.5f * (lo + hi);
+      }
       float dp = fabsf((3 * c3 * r + 2 * c2) * r + c1);
       if (!(dp > 0.f)) return -1;
-      float eps = fmaxf(4e-7f, 4.f * del / dp);
+      float eps = fmaxf(4e-7f, __fdividef(4.f * del, dp));
       float ym = emu_p3(c3, c2, c1, c0, r - eps), yp = emu_p3(c3, c2, c1, c0, r + eps);
       if (!(fabsf(ym) > del && fabsf(yp) > del && ((ym < 0) != (yp < 0)))) return -1;
       root[n] = r;
@@ -870,24 +879,25 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
   float F = sum2(mul2(e, c));
   float sabs = fabsf(A) + fabsf(B) + fabsf(C) + fabsf(D) + fabsf(E) + fabsf(F);
   if (!(A > 1e-5f * sabs)) return 2;
-  float n[6] = {1.f, B / A, C / A, D / A, E / A, F / A};
+  float ia = 1.f / A;
+  float n[6] = {1.f, B * ia, C * ia, D * ia, E * ia, F * ia};
   float ns = 1.f + fabsf(n[1]) + fabsf(n[2]) + fabsf(n[3]) + fabsf(n[4]) + fabsf(n[5]);
   float dQ = 1.5e-6f * ns;  // |Q (fp32 here) - Q (fp64 there)| on [0,1]
   float qbz[5];             // Bernstein coefficients of Q' on [0,1]
   {
     float a0 = n[4], a1 = 2 * n[3], a2 = 3 * n[2], a3 = 4 * n[1], a4 = 5.f;
     qbz[0] = a0;
-    qbz[1] = a0 + a1 / 4;
-    qbz[2] = a0 + a1 / 2 + a2 / 6;
-    qbz[3] = a0 + 3 * a1 / 4 + a2 / 2 + a3 / 4;
+    qbz[1] = a0 + a1 * 0.25f;
+    qbz[2] = a0 + a1 * 0.5f + a2 * (1.f / 6.f);
+    qbz[3] = a0 + 3 * a1 * 0.25f + a2 * 0.5f + a3 * 0.25f;
     qbz[4] = a0 + a1 + a2 + a3 + a4;
   }
   float dQp = 2e-6f * (5 + 4 * fabsf(n[1]) + 3 * fabsf(n[2]) + 2 * fabsf(n[3]) + fabsf(n[4]));
   // isolator cubic and the bound of its evaluation error
   float mA = 0.4f * fabsf(n[2]) + 0.16f * n[1] * n[1], mB = 0.6f * fabsf(n[3]) + 0.12f * fabsf(n[1] * n[2]);
-  float mC = 0.8f * fabsf(n[4]) + 0.08f * fabsf(n[1] * n[3]), mD = fabsf(n[5]) + fabsf(n[1] * n[4]) / 25.f;
+  float mC = 0.8f * fabsf(n[4]) + 0.08f * fabsf(n[1] * n[3]), mD = fabsf(n[5]) + fabsf(n[1] * n[4]) * 0.04f;
   float pA = 0.4f * n[2] - 0.16f * n[1] * n[1], pB = 0.6f * n[3] - 0.12f * n[1] * n[2];
-  float pC = 0.8f * n[4] - 0.08f * n[1] * n[3], pD = n[5] - n[1] * n[4] / 25.f;
+  float pC = 0.8f * n[4] - 0.08f * n[1] * n[3], pD = n[5] - n[1] * n[4] * 0.04f;
   float del = 1e-6f * (mA + mB + mC + mD) + 1e-30f;
   if (fabsf(pA) <= 1e-6f + 2e-6f * mA) {  // the reference's solver may take its quadratic branch
     del += fabsf(pA) + 2e-6f * mA + 1e-6f;
@@ -895,12 +905,13 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
   }
   float bp[4], br[4];
   int nb = 0;
-  float qr = -n[1] / 5.f, eq = 3e-7f * fabsf(qr) + 1e-7f;
+  float qr = -n[1] * 0.2f, eq = 3e-7f * fabsf(qr) + 1e-7f;
   if (fabsf(qr) <= eq || fabsf(qr - 1.f) <= eq) return 2;
   if (qr > 0.f && qr < 1.f) { bp[nb] = qr; br[nb] = eq; nb++; }
   float rts[3], rrad[3];
   int nr = emu_cubic_roots01(pA, pB, pC, pD, del, rts, rrad);
   if (nr < 0) return 2;
+  #pragma unroll 1
   for (int k = 0; k < nr; k++) {
     float rad = rrad[k] + 1.2e-7f;
     if (rts[k] - rad <= 0.f || rts[k] + rad >= 1.f) return 2;
@@ -908,11 +919,14 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
     br[nb] = rad;
     nb++;
   }
+  #pragma unroll 1
   for (int j = 1; j < nb; j++)
+    #pragma unroll 1
     for (int k = j; k > 0 && bp[k - 1] > bp[k]; k--) {
       float t = bp[k]; bp[k] = bp[k - 1]; bp[k - 1] = t;
       t = br[k]; br[k] = br[k - 1]; br[k - 1] = t;
     }
+  #pragma unroll 1
   for (int j = 1; j < nb; j++)
     if (bp[j] - bp[j - 1] <= br[j] + br[j - 1]) return 2;
   // bracket ends, Q there, and |Q'| within the enclosure of each breakpoint
@@ -920,6 +934,7 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
   int ne = 0;
   float qpp = 20 + 12 * fabsf(n[1]) + 6 * fabsf(n[2]) + 2 * fabsf(n[3]);  // |Q''| on [0,1]
   ends[ne] = 0.f; val[ne] = n[5]; qloc[ne] = 0.f; ne++;
+  #pragma unroll 1
   for (int j = 0; j < nb; j++) {
     float t = bp[j];
     float qd = (((5 * t + 4 * n[1]) * t + 3 * n[2]) * t + 2 * n[3]) * t + n[4];
@@ -936,6 +951,7 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
   float M = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
   bool unsure = false;
   int lj = 0;  // lower bracket end: kept through brackets without a sign change
+  #pragma unroll 1
   for (int j = 0; j + 1 < ne; j++) {
     if ((val[j] < 0) == (val[j + 1] < 0)) continue;
     int i0 = lj;
@@ -953,15 +969,24 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
     float ra, rb, mu;
     if (!emu_unique_root(n, qbz, l, u, ql, qu, dQ, dQp, 1e-5f, &ra, &rb, &mu)) { unsure = true; continue; }
     bool up = emu_q(n, rb) > emu_q(n, ra);
-    float lo = ra, hi = rb;
-    for (int it = 0; it < 32; it++) {
-      float m = 0.5f * (lo + hi);
-      if (m <= lo || m >= hi) break;
-      if ((emu_q(n, m) > 0) == up) hi = m; else lo = m;
+    float lo = ra, hi = rb, ts = 0.5f * (ra + rb);
+#pragma unroll 1
+    for (int it = 0; it < DVG_EMU_NEWTON; it++) {  // Newton kept inside the root piece
+      float y = emu_q(n, ts), dy = (((5 * ts + 4 * n[1]) * ts + 3 * n[2]) * ts + 2 * n[3]) * ts + n[4];
+      if ((y > 0) == up) hi = ts; else lo = ts;
+      float nt = ts - __fdividef(y, dy);
+      ts = (nt >= lo && nt <= hi) ? nt : 0.5f * (lo + hi);
     }
-    float ts = 0.5f * (lo + hi);
+    // how far the root can be from ts: a certified sign change around ts, else the piece
+    float er = hi - lo;
+    {
+      float dts = (((5 * ts + 4 * n[1]) * ts + 3 * n[2]) * ts + 2 * n[3]) * ts + n[4];
+      float e = fmaxf(2e-7f, __fdividef(2.f * (fabsf(emu_q(n, ts)) + dQ), fmaxf(fabsf(dts), mu)));
+      float qm = emu_q(n, ts - e), qp = emu_q(n, ts + e);
+      if (fabsf(qm) > dQ && fabsf(qp) > dQ && ((qm < 0) != (qp < 0))) er = fminf(er, e);
+    }
     // where the reference may stop: |Q| < 1e-5 around the root, or the 20-step bisection window
-    float eps_t = (1e-5f + dQ) / mu + (ends[j + 1] - ends[i0]) * 4e-6f + 1e-6f;
+    float eps_t = __fdividef(1e-5f + dQ, mu) * 1.000001f + er + (ends[j + 1] - ends[i0]) * 4e-6f + 1e-6f;
     float margin = (bmax + rmaxd) * eps_t + far_margin(M);
     float tt = 1 - ts;
     float rr = (tt * tt * tt) * r0 + (3 * tt * tt * ts) * r1 + (3 * tt * ts * ts) * r2 + (ts * ts * ts) * r3;
@@ -1010,6 +1035,7 @@ static __device__ __noinline__ int segment_root_test(const DevScene &S, int po, 
   float lower = 0.f;
   float ct = NAN;
   double cv = 0.0;
+  #pragma unroll 1
   for (int j = 0; j < ni + 1; j++) {
     if (j < ni && iv[j] < 0.f) continue;
     float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
@@ -1031,7 +1057,7 @@ static __device__ __noinline__ int segment_root_test(const DevScene &S, int po, 
 // lines exactly, quadratic / cubic end points exactly, then the fp32
 // outside proof.  1: within, 0: not, -1: the path reports "not within"
 // (distance-approximated quadratics), 2: undecided (segment_solve decides).
-DI int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, int nc, int i0, int segi, v2 pt,
+DN int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, int nc, int i0, int segi, v2 pt,
                           float r) {
   if (nc == 0) {
     int i1 = (i0 + 1) % np;
@@ -1097,7 +1123,7 @@ DI int within_segment(const DevScene &S, int s, int po, int np, int th, int flag
   return f;
 }
 
-DI bool within_shape(const DevScene &S, int s, v2 pt, float r) {
+DN bool within_shape(const DevScene &S, int s, v2 pt, float r) {
   int kind = SI(S, s, DVG_SHAPE_KIND);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
   if (kind == DVG_CIRCLE) {
@@ -1122,6 +1148,7 @@ DI bool within_shape(const DevScene &S, int s, v2 pt, float r) {
   }
   int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF);
   int np = SI(S, s, DVG_SHAPE_NUM_POINTS), th = SI(S, s, DVG_SHAPE_THICKNESS_OFF), flags = SI(S, s, DVG_SHAPE_FLAGS);
+  #pragma unroll 1
   for (int k = 0; k < nseg; k++) {
     int seg = S.seg_order[so + k];
     if (nseg > 1 && !box_in_r(S.seg_box[so + seg], pt, S.seg_r[so + seg])) continue;
@@ -1138,6 +1165,7 @@ DI bool group_stroke(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
   v2 lp = xform_pt(S.c2s + 9 * g, pt);
   int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
   bool ret = false;
+  #pragma unroll 1
   for (int k = 0; k < nsh; k++) {
     int s = __ldg(&S.group_shapes[off + k]);
     float r = stroke_width(S, s);
@@ -1155,12 +1183,13 @@ DI bool group_stroke(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
 // closest point / distance (compute_distance.h:12-439)
 struct PathInfo { int base_point_id, point_id; float t_root; };
 
-DI bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
+DN bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
   int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF), flags = SI(S, s, DVG_SHAPE_FLAGS);
   float min_dist = max_radius;
   v2 ret = V2(0, 0);
   bool found = false;
+  #pragma unroll 1
   for (int k = 0; k < nseg; k++) {
     int seg = S.seg_order[so + k];
     if (nseg > 1 && !box_in_r(S.seg_box[so + seg], pt, min_dist)) continue;
@@ -1221,6 +1250,7 @@ DI bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
       float lower = 0.f;
       float ct = NAN;
       double cv = 0.0;
+      #pragma unroll 1
       for (int j = 0; j < ni + 1; j++) {
         if (j < ni && iv[j] < 0.f) continue;
         float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
@@ -1249,7 +1279,7 @@ DI bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
   return found;
 }
 
-DI bool closest_shape(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
+DN bool closest_shape(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
   int kind = SI(S, s, DVG_SHAPE_KIND);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
   if (kind == DVG_CIRCLE) {
@@ -1293,6 +1323,7 @@ DI bool group_distance(const DevScene &S, int g, v2 pt, float max_radius, int *m
   int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
   float min_dist = max_radius;
   bool found = false;
+  #pragma unroll 1
   for (int k = 0; k < nsh; k++) {
     int s = __ldg(&S.group_shapes[off + k]);
     if (nsh > 1 && !box_in_r(S.s_box[s], lp, max_radius)) continue;
@@ -1320,7 +1351,7 @@ DI bool group_distance(const DevScene &S, int g, v2 pt, float max_radius, int *m
 DI float4 stop_color(const DevScene &S, int co, int i) {
   return F4(pget(S, co + 4 * i), pget(S, co + 4 * i + 1), pget(S, co + 4 * i + 2), pget(S, co + 4 * i + 3));
 }
-DI float4 paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt) {
+DN float4 paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt) {
   if (kind == DVG_CONSTANT) return F4(pget(S, off), pget(S, off + 1), pget(S, off + 2), pget(S, off + 3));
   float t;
   if (kind == DVG_LINEAR) {
@@ -1348,7 +1379,7 @@ DI float4 paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt) {
 DI void gadd(float *dp, int off, float v) { atomicAdd(dp + off, v); }
 
 // d_sample_color (diffvg.cpp:370-504)
-DI void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, float4 d_color, float *dp,
+DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, float4 d_color, float *dp,
                       float *d_translation) {
   if (kind == DVG_CONSTANT) {
     gadd(dp, off + 0, d_color.x); gadd(dp, off + 1, d_color.y);

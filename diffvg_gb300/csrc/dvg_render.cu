@@ -42,7 +42,7 @@ __device__ __forceinline__ DevRender load_filter(const DevRender &R0, const DevS
 // weight image (weight_kernel, diffvg.cpp:1115-1158), gathered per pixel.
 // The reference never passes use_prefiltering to it (diffvg.cpp:1525-1533),
 // so the weights always use the jittered positions.
-__global__ void __launch_bounds__(256) k_weight(DevRender R0, DevScene S) {
+__global__ void __launch_bounds__(256) k_weight(DevRender R0, const __grid_constant__ DevScene S) {
   DevRender R = load_filter(R0, &S);
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= R.w * R.h) return;
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_sample_bwd(DevSc
 // Background adjoint in sample order per pixel: a sample without fragments
 // overwrites the pixel's value with its d_color, the others add to it
 // (diffvg.cpp:596-604, 699-704).
-__global__ void k_bg_combine(DevScene S, DevRender R, const float4 *dbg_val, const int *dbg_flag) {
+__global__ void k_bg_combine(const __grid_constant__ DevScene S, DevRender R, const float4 *dbg_val, const int *dbg_flag) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= R.w * R.h || bins_overflowed(S)) return;
   float4 *dst = reinterpret_cast<float4 *>(R.d_background) + p;
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(256) k_edge_sample(DevScene S, DevRender R, Ed
 }
 
 // exclusive scan of the per-tile sample counts (one block of 1024 threads)
-__global__ void k_edge_scan(DevScene S, EdgeRecords E) {
+__global__ void k_edge_scan(const __grid_constant__ DevScene S, EdgeRecords E) {
   int T = S.tiles_x * S.tiles_y;
   __shared__ int part[1024];
   int per = (T + blockDim.x - 1) / blockDim.x;

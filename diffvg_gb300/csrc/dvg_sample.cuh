@@ -112,6 +112,7 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
   q->result[lane] = 0u;
   __syncwarp();
   int npend = 0;
+  #pragma unroll 1
   for (int base = 0; base < total; base += 32) {  // warp-uniform trip count
     int j = base + lane;
     bool pending = false;
@@ -130,6 +131,7 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
     npend += __popc(bal);
   }
   __syncwarp();
+  #pragma unroll 1
   for (int k = lane; k < npend; k += 32) {
     int owner, idx;
     SegJob jb = warp_job(q, q->pend[k], owner, idx);
@@ -310,6 +312,7 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
   if (eq && (res & eq_jobs)) eq->hit = 1;
   float4 acc = bg ? *bg : F4(0, 0, 0, 0);
   int nhit = 0, ev = -1;
+  #pragma unroll 1
   for (int i = 0; i < nf; i++) {
     if (!frag_hit(frags[i].meta, res)) continue;
     int g = frags[i].key >> 1;
@@ -362,6 +365,7 @@ DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, fl
   float4 first = bg ? *bg : F4(0, 0, 0, 0);
   float4 acc = first;
   int nh = 0;
+  #pragma unroll 1
   for (int i = 0; i < nf; i++) {
     if (!frag_hit(frags[i].meta, res)) continue;
     int g = frags[i].key >> 1;
