@@ -76,6 +76,11 @@ struct DvgScene {
   float *seg_r = nullptr, *seg_pmf = nullptr, *seg_cdf = nullptr, *smp_cdf = nullptr, *smp_pmf = nullptr;
   int *seg_order = nullptr, *tile_start = nullptr, *tile_count = nullptr, *scratch = nullptr;
   int4 *g_tile_range = nullptr;
+  int num_records = 0;  // stroke records (k_rec_fill)
+  int2 *g_rec = nullptr;
+  float4 *rec_box = nullptr;
+  int4 *rec_a = nullptr, *rec_b = nullptr;
+  float *rec_r = nullptr;
   float2 *seg_tpts = nullptr;
   float *seg_th = nullptr;
   unsigned *err = nullptr;  // [0] status bits, [1] tile-list length
@@ -216,6 +221,23 @@ int validate_desc(const DvgSceneDesc *d, int *seg_point) {
   return DVG_OK;
 }
 
+// Number of stroke records of a (validated) description: per stroke group
+// and shape, one per path segment, or one for a shape that is not tested
+// segment by segment (k_rec_fill).  Allocates nothing.
+int count_stroke_records(const DvgSceneDesc *d) {
+  long long n = 0;
+  for (int g = 0; g < d->num_groups; g++) {
+    const int32_t *gi = d->group_info + (size_t)g * DVG_GROUP_INFO_STRIDE;
+    if (gi[DVG_GROUP_STROKE_KIND] == DVG_PAINT_NONE) continue;
+    for (int k = 0; k < gi[DVG_GROUP_NUM_SHAPES]; k++) {
+      const int32_t *si = d->shape_info + (size_t)d->group_shapes[gi[DVG_GROUP_SHAPES_OFF] + k] * DVG_SHAPE_INFO_STRIDE;
+      bool per_segment = si[DVG_SHAPE_KIND] == DVG_PATH && !(si[DVG_SHAPE_FLAGS] & 2);
+      n += per_segment ? si[DVG_SHAPE_NUM_SEGMENTS] : 1;
+    }
+  }
+  return (int)n;
+}
+
 }  // namespace dvg
 
 namespace {
@@ -246,6 +268,11 @@ DevScene make_dev(DvgScene *sc, const float *params) {
   S.s_length = sc->s_length;
   S.seg_box = sc->seg_box;
   S.seg_r = sc->seg_r;
+  S.g_rec = sc->g_rec;
+  S.rec_box = sc->rec_box;
+  S.rec_a = sc->rec_a;
+  S.rec_b = sc->rec_b;
+  S.rec_r = sc->rec_r;
   S.seg_tpts = sc->seg_tpts;
   S.seg_th = sc->seg_th;
   S.seg_pmf = sc->seg_pmf;
@@ -445,6 +472,8 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   }
   sc->num_total = (int)smp_shape.size();
   int NT = sc->num_total;
+  sc->num_records = dvg::count_stroke_records(desc);
+  int NR = sc->num_records;
   cudaError_t e;
   // topology
   std::vector<size_t> tb = {sizeof(int) * S * DVG_SHAPE_INFO_STRIDE, sizeof(int) * NSEG, sizeof(int) * NSEG,
@@ -483,7 +512,8 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
       sizeof(int) * (T + 1), sizeof(int) * T, sizeof(int4) * G,                           // tiles
       sizeof(int) * (10 * (size_t)NSEG + 8 * (size_t)S + 8),                              // scratch
       sizeof(unsigned) * 4,
-      sizeof(float2) * DVG_TREE_PTS * (size_t)NSEG, sizeof(float) * DVG_TREE_NODES * (size_t)NSEG};  // trees
+      sizeof(float2) * DVG_TREE_PTS * (size_t)NSEG, sizeof(float) * DVG_TREE_NODES * (size_t)NSEG,  // trees
+      sizeof(int2) * G, sizeof(float4) * NR, sizeof(int4) * NR, sizeof(int4) * NR, sizeof(float) * NR};  // records
   e = sc->derived.ensure(carve_size(db));
   if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "allocating scene arenas"); }
   p = reinterpret_cast<char *>(sc->derived.ptr);
@@ -507,6 +537,11 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   sc->err = carve<unsigned>(p, 4);
   sc->seg_tpts = carve<float2>(p, DVG_TREE_PTS * (size_t)NSEG);
   sc->seg_th = carve<float>(p, DVG_TREE_NODES * (size_t)NSEG);
+  sc->g_rec = carve<int2>(p, G);
+  sc->rec_box = carve<float4>(p, NR);
+  sc->rec_a = carve<int4>(p, NR);
+  sc->rec_b = carve<int4>(p, NR);
+  sc->rec_r = carve<float>(p, NR);
   e = cudaMemset(sc->derived.ptr, 0, sc->derived.bytes);
   if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "clearing scene arenas"); }
   size_t cap = (size_t)T * 32;

@@ -56,6 +56,11 @@ struct DevScene {
   int *tile_start;          // [tiles+1]
   int *tile_list;           // candidate groups per tile, ascending
   int *scratch;             // [8*NSEG + 8*S] path leaf-order scratch
+  int2 *g_rec;              // [G] range of each group's stroke records
+  float4 *rec_box;          // [records] cull box (empty test: infinite box)
+  int4 *rec_a;              // {segment (so + seg; -1: whole-shape record), shape, nc, first point}
+  int4 *rec_b;              // {param offset, point count, thickness offset, first record of the next shape}
+  float *rec_r;             // stroke radius of the record's shape
   float2 *seg_tpts = nullptr;  // [NSEG * DVG_TREE_PTS] tabulated subdivision trees (curved segments), or null
   float *seg_th = nullptr;     // [NSEG * DVG_TREE_NODES]
   unsigned *err;            // status word (DVG_EFLAG_*)

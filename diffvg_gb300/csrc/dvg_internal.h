@@ -15,6 +15,7 @@ void clear_error();
 // Host-side checks of a scene description; writes the first point of every
 // path segment to seg_point when it is not NULL.
 int validate_desc(const DvgSceneDesc *d, int *seg_point);
+int count_stroke_records(const DvgSceneDesc *d);
 
 // Scene preparation from the parameter arena: transforms, boxes, segment
 // order, boundary CDFs and the per-tile candidate group lists.

@@ -217,6 +217,87 @@ __global__ void k_seg_tree(DevScene S) {
   }
 }
 
+// Stroke records: the stroke tests of every stroke group flattened into one
+// array, group after group, each group's shapes in order and each path's
+// segments in visiting order (seg_order), one record per segment; a shape
+// that is not a path, or a path with distance-approximated segments, gets
+// one record for the whole shape.  A record holds the cull box (the
+// segment's box grown by its stroke radius, or the shape's when a cull
+// applies to the whole shape), the indices a test needs and the first record
+// of the next shape, so that the sample loops test segments without
+// following indices through the scene tables.
+DI int stroke_record_count(const DevScene &S, int g) {
+  if (GI(S, g, DVG_GROUP_STROKE_KIND) == DVG_PAINT_NONE) return 0;
+  int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF), n = 0;
+  for (int k = 0; k < nsh; k++) {
+    int s = S.group_shapes[off + k];
+    bool per_segment = SI(S, s, DVG_SHAPE_KIND) == DVG_PATH && !(SI(S, s, DVG_SHAPE_FLAGS) & 2);
+    n += per_segment ? SI(S, s, DVG_SHAPE_NUM_SEGMENTS) : 1;
+  }
+  return n;
+}
+
+// exclusive scan of the per-group record counts (one block of 1024 threads)
+__global__ void k_rec_scan(DevScene S) {
+  int G = S.num_groups;
+  __shared__ int part[1024];
+  int per = (G + blockDim.x - 1) / blockDim.x;
+  int lo = threadIdx.x * per, hi = min(lo + per, G);
+  int sum = 0;
+  for (int g = lo; g < hi; g++) sum += stroke_record_count(S, g);
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+    int v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = threadIdx.x > 0 ? part[threadIdx.x - 1] : 0;
+  for (int g = lo; g < hi; g++) {
+    int c = stroke_record_count(S, g);
+    S.g_rec[g] = make_int2(run, run + c);
+    run += c;
+  }
+}
+
+__global__ void k_rec_fill(DevScene S) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= S.num_groups) return;
+  int j = S.g_rec[g].x;
+  if (S.g_rec[g].y <= j) return;
+  const float4 all = F4(-INFINITY, -INFINITY, INFINITY, INFINITY);
+  int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
+  for (int k = 0; k < nsh; k++) {
+    int s = S.group_shapes[off + k];
+    float r = stroke_width(S, s);
+    int po = SI(S, s, DVG_SHAPE_PARAM_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
+    int th = SI(S, s, DVG_SHAPE_THICKNESS_OFF);
+    bool per_segment = SI(S, s, DVG_SHAPE_KIND) == DVG_PATH && !(SI(S, s, DVG_SHAPE_FLAGS) & 2);
+    float4 sb = S.s_box[s];
+    float4 shape_cull = nsh > 1 ? F4(sb.x - r, sb.y - r, sb.z + r, sb.w + r) : all;
+    if (!per_segment) {
+      S.rec_box[j] = shape_cull;
+      S.rec_a[j] = make_int4(-1, s, 0, 0);
+      S.rec_b[j] = make_int4(po, np, th, j + 1);
+      S.rec_r[j] = r;
+      j++;
+      continue;
+    }
+    int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF);
+    int next = j + nseg;
+    for (int m = 0; m < nseg; m++, j++) {
+      int seg = S.seg_order[so + m];
+      float4 b = S.seg_box[so + seg];
+      float rr = S.seg_r[so + seg];
+      S.rec_box[j] = nseg > 1 ? F4(b.x - rr, b.y - rr, b.z + rr, b.w + rr) : shape_cull;
+      S.rec_a[j] = make_int4(so + seg, s, S.segment_ctrl[so + seg], S.seg_point[so + seg]);
+      S.rec_b[j] = make_int4(po, np, th, next);
+      S.rec_r[j] = r;
+    }
+  }
+}
+
 __global__ void k_group_prep(DevScene S, int4 *g_tile_range) {
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= S.num_groups) return;
@@ -400,6 +481,10 @@ cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4
   if (NS > 0) k_shape_prep<<<(NS + 63) / 64, 64, 0, st>>>(S);
   if (NS > 0 && S.seg_tpts) k_seg_tree<<<(NS + 3) / 4, 128, 0, st>>>(S);
   if (G > 0) k_group_prep<<<(G + 127) / 128, 128, 0, st>>>(S, g_tile_range);
+  if (G > 0) {
+    k_rec_scan<<<1, 1024, 0, st>>>(S);
+    k_rec_fill<<<(G + 127) / 128, 128, 0, st>>>(S);
+  }
   k_sampling_cdf<<<1, 256, 0, st>>>(S);
   k_bin_count<<<T, 128, 0, st>>>(S, g_tile_range, tile_count);
   k_bin_scan<<<1, 1024, 0, st>>>(S, tile_count, tile_cap, bin_total);

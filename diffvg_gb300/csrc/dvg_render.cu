@@ -63,7 +63,8 @@ __global__ void __launch_bounds__(256) k_weight(DevRender R0, const __grid_const
 }
 
 template <bool PREFILTER>
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_sample_fwd(DevScene S, DevRender R, float4 *samples) {
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+    k_sample_fwd(const __grid_constant__ DevScene S, DevRender R, float4 *samples) {
   __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
   int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
@@ -126,7 +127,8 @@ __device__ __forceinline__ float block_sum(float v) {
 
 // interior adjoint (render_kernel with d_render_image, diffvg.cpp:1160-1268)
 template <bool PREFILTER>
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_sample_bwd(DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+    k_sample_bwd(const __grid_constant__ DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
   __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
   DevRender R = load_filter(R0, nullptr);
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
@@ -181,7 +183,8 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_sample_bwd(DevSc
 // Background adjoint in sample order per pixel: a sample without fragments
 // overwrites the pixel's value with its d_color, the others add to it
 // (diffvg.cpp:596-604, 699-704).
-__global__ void k_bg_combine(const __grid_constant__ DevScene S, DevRender R, const float4 *dbg_val, const int *dbg_flag) {
+__global__ void k_bg_combine(const __grid_constant__ DevScene S, DevRender R, const float4 *dbg_val,
+                             const int *dbg_flag) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= R.w * R.h || bins_overflowed(S)) return;
   float4 *dst = reinterpret_cast<float4 *>(R.d_background) + p;
@@ -204,7 +207,7 @@ __global__ void k_bg_combine(const __grid_constant__ DevScene S, DevRender R, co
 // The reference sorts its boundary samples by Morton code for the same
 // coherence (diffvg.cpp:1594-1599); the order only changes the order of the
 // gradient atomics.
-__global__ void __launch_bounds__(256) k_edge_sample(DevScene S, DevRender R, EdgeRecords E) {
+__global__ void __launch_bounds__(256) k_edge_sample(const __grid_constant__ DevScene S, DevRender R, EdgeRecords E) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   int n = R.w * R.h * R.spp;
   if (idx >= n) return;
@@ -278,7 +281,8 @@ __global__ void k_edge_order(EdgeRecords E, int n) {
   if (key >= 0) E.order[E.tile_start[key] + E.rank[idx]] = idx;
 }
 
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_edge_eval(DevScene S, DevRender R0, EdgeRecords E) {
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+    k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, EdgeRecords E) {
   __shared__ WarpQueue wq[8];
   DevRender R = load_filter(R0, nullptr);
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -317,8 +321,9 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS) k_edge_eval(DevSce
 }
 
 // signed distance output (render_kernel's sdf branch, diffvg.cpp:1273-1293)
-__global__ void __launch_bounds__(256) k_sdf(DevScene S, DevRender R, const float *eval_positions, int num_eval,
-                                             float *sdf, const float *d_sdf) {
+__global__ void __launch_bounds__(256) k_sdf(const __grid_constant__ DevScene S, DevRender R,
+                                             const float *eval_positions, int num_eval, float *sdf,
+                                             const float *d_sdf) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   int n = eval_positions ? num_eval : R.w * R.h * R.spp;
   if (idx >= n || bins_overflowed(S)) return;

@@ -148,12 +148,11 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
 // segments queued.  Returns the number of candidate fragments (capped).
 //
 // All 32 lanes of the warp call it (lanes without a sample pass active =
-// false).  Each lane walks its own candidate list: tile groups, their
-// shapes, the shapes' segments, with the bounding-box culls, as the nested
-// loops of within_distance (within_distance.h:355-446) and sample_color
-// (diffvg.cpp:525-585) do.  The walk stops at each segment that needs a
-// test, and the segment tests of all lanes then run together, so that the
-// lanes that passed their culls at different groups still test in lockstep.
+// false).  Each lane walks its own candidates: the tile's groups, then each
+// stroke group's records (its shapes' segments with their cull boxes, in
+// the order of the nested loops of within_distance, within_distance.h:355-446,
+// and sample_color, diffvg.cpp:525-585).  The walk stops at each segment
+// that needs a test, and the segment tests of all lanes then run together.
 // A shape that hits ends its own walk (and its group's, outside the group of
 // an edge query) as the reference's early returns do.
 DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q, int lane, int &njobs, EdgeQ *eq,
@@ -163,14 +162,13 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
   if (active) list = cand_range(S, pt, k, e);
   const int G = S.num_groups;
   int nf = 0;
-  // stroke part of the group in progress
-  int g = 0, nsh = 0, off = 0, si = 0, glo = 0;
-  bool in_group = false, is_eq = false, gret = false;
+  // stroke records of the group in progress
+  int g = 0, j = 0, jend = 0, glo = 0, cs = -1, slo = 0;
+  bool in_group = false, is_eq = false, gret = false, mark = false;
   v2 lp = pt;
-  // path shape in progress
-  int s = 0, po = 0, np = 0, th = 0, sflags = 0, nseg = 0, so = 0, sg = 0, slo = 0;
+  // the test the walk stopped at
+  int s = 0, po = 0, np = 0, th = 0, nc = 0, i0 = 0, segi = 0, jnext = 0;
   float r = 0.f;
-  bool in_shape = false, mark = false;
   auto emit = [&](int key, int meta) {
     if (nf < DVG_MAX_FRAGMENTS) frags[nf++] = FragRef{key, meta};
     else overflow = true;
@@ -179,51 +177,41 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
     if (GI(S, gg, DVG_GROUP_FILL_KIND) != DVG_PAINT_NONE && group_inside(S, gg, pt, eq)) emit(2 * gg, DVG_META_HIT);
   };
   while (true) {
-    // advance this lane to its next segment test (or a shape decided without one)
-    int nc = 0, i0 = 0, segi = 0;
     bool have = false, shape_hit = false;
+    #pragma unroll 1
     while (true) {
-      if (in_shape) {
-        if (sg < nseg) {
-          int seg = __ldg(&S.seg_order[so + sg]);
-          sg++;
-          if (nseg > 1 && !box_in_r(S.seg_box[so + seg], lp, S.seg_r[so + seg])) continue;
-          nc = __ldg(&S.segment_ctrl[so + seg]);
-          i0 = __ldg(&S.seg_point[so + seg]);
-          segi = so + seg;
-          have = true;
-          break;
-        }
-        in_shape = false;  // no segment hit: its queued jobs decide the shape
-        continue;
-      }
       if (in_group) {
-        if (si < nsh) {
-          s = __ldg(&S.group_shapes[off + si]);
-          si++;
-          r = stroke_width(S, s);
-          if (nsh > 1 && !box_in_r(S.s_box[s], lp, r)) continue;
-          int kind = SI(S, s, DVG_SHAPE_KIND);
-          sflags = kind == DVG_PATH ? SI(S, s, DVG_SHAPE_FLAGS) : 0;
-          if (kind != DVG_PATH || (sflags & 2)) {
+        if (j < jend) {
+          float4 b = __ldg(&S.rec_box[j]);
+          if (!(lp.x >= b.x && lp.x <= b.z && lp.y >= b.y && lp.y <= b.w)) {
+            j++;
+            continue;
+          }
+          int4 a = __ldg(&S.rec_a[j]), c = __ldg(&S.rec_b[j]);
+          r = __ldg(&S.rec_r[j]);
+          j++;
+          s = a.y;
+          jnext = c.w;
+          if (s != cs) {  // the walk enters the next shape: its jobs start here
+            cs = s;
+            slo = njobs;
+            mark = is_eq && s == eq->shape;
+          }
+          if (a.x < 0) {
             if (within_shape(S, s, lp, r)) {
-              slo = njobs;
-              mark = false;
               shape_hit = true;
               break;
             }
             continue;
           }
-          po = SI(S, s, DVG_SHAPE_PARAM_OFF);
-          np = SI(S, s, DVG_SHAPE_NUM_POINTS);
-          th = SI(S, s, DVG_SHAPE_THICKNESS_OFF);
-          nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);
-          so = SI(S, s, DVG_SHAPE_SEG_OFF);
-          sg = 0;
-          slo = njobs;
-          mark = is_eq && s == eq->shape;
-          in_shape = true;
-          continue;
+          segi = a.x;
+          nc = a.z;
+          i0 = a.w;
+          po = c.x;
+          np = c.y;
+          th = c.z;
+          have = true;
+          break;
         }
         in_group = false;  // the group's stroke is decided up to its queued jobs
         if (gret) emit(2 * g + 1, DVG_META_HIT);
@@ -235,14 +223,15 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
       g = list ? __ldg(&S.tile_list[k]) : k;
       k++;
       if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
-      if (GI(S, g, DVG_GROUP_STROKE_KIND) != DVG_PAINT_NONE) {
+      int2 rg = __ldg(&S.g_rec[g]);
+      if (rg.y > rg.x) {
+        j = rg.x;
+        jend = rg.y;
         lp = xform_pt(S.c2s + 9 * g, pt);
-        nsh = GI(S, g, DVG_GROUP_NUM_SHAPES);
-        off = GI(S, g, DVG_GROUP_SHAPES_OFF);
-        si = 0;
         glo = njobs;
         gret = false;
         is_eq = eq && eq->group == g;
+        cs = -1;
         in_group = true;
         continue;
       }
@@ -251,7 +240,7 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
     if (!__any_sync(0xffffffffu, have || shape_hit)) break;
     int f = shape_hit ? 1 : 0;
     if (have) {
-      f = within_segment_pre(S, po, np, th, sflags, nc, i0, segi, lp, r);  // the lanes' tests run together
+      f = within_segment_pre(S, po, np, th, 0, nc, i0, segi, lp, r);  // the lanes' tests run together
       if (f == 2) {
         if (njobs < DVG_LANE_JOBS) {
           q->job[lane][njobs] = SegJob{s, segi, lp.x, lp.y, r};
@@ -266,7 +255,7 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
     if (f == 1) {  // the shape hits
       if (mark) eq_jobs &= (1u << slo) - 1u;
       njobs = slo;  // its queued jobs are moot
-      in_shape = false;
+      j = jnext;
       if (!is_eq) {
         njobs = glo;
         in_group = false;

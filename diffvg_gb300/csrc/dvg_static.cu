@@ -123,6 +123,9 @@ extern "C" int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRen
          o_smppmf = c.take<float>(NGS), o_tstart = c.take<int>((size_t)T + 1), o_tcount = c.take<int>((size_t)T),
          o_trange = c.take<int4>(G), o_scratch = c.take<int>(10 * (size_t)NSEG + 8 * (size_t)NS + 8),
          o_err = c.take<unsigned>(4), o_weight = c.take<float>((size_t)npx), o_samples = c.take<float4>((size_t)n);
+  int NR = dvg::count_stroke_records(desc);
+  size_t o_grec = c.take<int2>(G), o_rbox = c.take<float4>(NR), o_ra = c.take<int4>(NR), o_rb = c.take<int4>(NR),
+         o_rr = c.take<float>(NR);
   size_t o_tiles = c.take<int>(0);
   c.off = o_tiles;
   if (o_tiles + 256 * sizeof(int) > DVG_STATIC_SCRATCH_BYTES)
@@ -180,6 +183,11 @@ extern "C" int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRen
   S.tile_list = reinterpret_cast<int *>(base + o_tiles);
   S.scratch = reinterpret_cast<int *>(base + o_scratch);
   S.err = reinterpret_cast<unsigned *>(base + o_err);
+  S.g_rec = reinterpret_cast<int2 *>(base + o_grec);
+  S.rec_box = reinterpret_cast<float4 *>(base + o_rbox);
+  S.rec_a = reinterpret_cast<int4 *>(base + o_ra);
+  S.rec_b = reinterpret_cast<int4 *>(base + o_rb);
+  S.rec_r = reinterpret_cast<float *>(base + o_rr);
 
   if (G == 0) {
     e = a->background ? cudaMemcpyAsync(image, a->background, (size_t)npx * 4 * sizeof(float), cudaMemcpyDeviceToDevice, s)
