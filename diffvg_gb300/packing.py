@@ -62,32 +62,46 @@ class PackedScene:
     tensors: list = field(default_factory=list)
     topology_key: bytes = b''
     _pinned: object = None
+    _pinned_views: object = None
     _copied: object = None
+    _staged: object = None
+    _staged_views: object = None
+
+    def _slot_views(self, buf):
+        return [buf[sl.offset:sl.offset + sl.numel].view(sl.shape) for sl in self.slots]
 
     def param_arena(self, device):
         """The parameter values as one contiguous fp32 tensor on `device`."""
         if not self.tensors:
             return torch.zeros(1, dtype=torch.float32, device=device)
-        flat = [t.detach().reshape(-1) for t in self.tensors]
-        if any(t.dtype != torch.float32 for t in flat):
-            flat = [t.to(torch.float32) for t in flat]
-        devs = {t.device for t in flat}
+        devs = {t.device for t in self.tensors}
         if len(devs) != 1:
-            return torch.cat([t.to(device=device) for t in flat])
+            return torch.cat([t.detach().reshape(-1).to(device=device, dtype=torch.float32) for t in self.tensors])
         src = next(iter(devs))
-        if src.type == 'cpu' and device.type == 'cuda':
-            # one concatenation into a reused pinned buffer, one asynchronous copy
-            if self._pinned is None or self._pinned.numel() != self.num_params:
-                self._pinned = torch.empty(self.num_params, dtype=torch.float32, pin_memory=True)
-                self._copied = None
-            if self._copied is not None:
-                self._copied.synchronize()  # the previous copy out of the buffer has finished
-            torch.cat(flat, out=self._pinned)
-            out = self._pinned.to(device=device, non_blocking=True)
-            self._copied = torch.cuda.Event()
-            self._copied.record(torch.cuda.current_stream(device))
-            return out
-        return torch.cat(flat).to(device=device)
+        with torch.no_grad():
+            if src.type == 'cpu' and device.type == 'cuda':
+                # one gather into a reused pinned buffer (a single multi-tensor
+                # copy), one asynchronous upload
+                if self._pinned is None or self._pinned.numel() != self.num_params:
+                    self._pinned = torch.empty(self.num_params, dtype=torch.float32, pin_memory=True)
+                    self._pinned_views = self._slot_views(self._pinned)
+                    self._copied = None
+                if self._copied is not None:
+                    self._copied.synchronize()  # the previous upload out of the buffer has finished
+                torch._foreach_copy_(self._pinned_views, self.tensors)
+                out = self._pinned.to(device=device, non_blocking=True)
+                self._copied = torch.cuda.Event()
+                self._copied.record(torch.cuda.current_stream(device))
+                return out
+            if src == device and device.type == 'cuda':
+                # device-resident tensors: a multi-tensor copy into a staging
+                # buffer, then a copy the caller owns
+                if self._staged is None or self._staged.device != device or self._staged.numel() != self.num_params:
+                    self._staged = torch.empty(self.num_params, dtype=torch.float32, device=device)
+                    self._staged_views = self._slot_views(self._staged)
+                torch._foreach_copy_(self._staged_views, self.tensors)
+                return self._staged.clone()
+            return torch.cat([t.detach().reshape(-1).to(torch.float32) for t in self.tensors]).to(device=device)
 
 
 def _as_tensor(x):
@@ -105,34 +119,57 @@ _pack_cache = OrderedDict()
 _PACK_CACHE_SIZE = 32
 
 
-def _structure_key(args):
-    """Cheap identity of an argument list's structure: floating-point tensors
-    by identity and shape (their values are parameters, read later),
-    integer tensors (segment counts, shape ids) by identity and version
-    counter (an in-place edit changes the version), everything else by
-    value."""
+def _mutable_state(args):
+    """What can change inside the argument objects without changing their
+    identity: the shapes of floating-point tensors (their values are
+    parameters, read when the arena is built) and the version counters of
+    integer tensors (segment counts, shape ids; an in-place edit bumps it)."""
     T = torch.Tensor
-    return tuple(((id(a), a.shape) if a.is_floating_point() else (id(a), a._version)) if isinstance(a, T) else a
-                 for a in args)
+    ts = [a for a in args if isinstance(a, T)]
+    fl = [t for t in ts if t.is_floating_point()]
+    it = [t for t in ts if not t.is_floating_point()]
+    return fl, [t.shape for t in fl], it, [t._version for t in it]
+
+
+def _same_args(old, new):
+    """The same argument list: identical tensors, equal other values."""
+    if len(old) != len(new):
+        return False
+    T = torch.Tensor
+    for a, b in zip(old, new):
+        if a is not b and (isinstance(a, T) or isinstance(b, T) or type(a) is not type(b) or a != b):
+            return False
+    return True
 
 
 def pack_scene_cached(args):
     """pack_scene with a cache for optimisation loops, which call
-    serialize_scene with the same shape objects on every step.  An entry
-    keeps its argument objects alive, so identities in the key cannot be
-    reused while it is cached.  On a hit the packed topology and parameter
-    slots are reused; parameter values are read when the arena is built.
-    Integer tensors that are converted anew on every call (e.g. by a
-    serialize_scene that copies them) simply miss the cache."""
-    key = _structure_key(args)
+    serialize_scene with the same shape objects on every step.  Entries are
+    found by a hash of the argument list (tensors hash by identity) and
+    confirmed by _same_args and by the tensors' mutable state
+    (_mutable_state); an entry keeps its argument objects alive, so tensor
+    identities cannot be reused while it is cached.  On a hit the packed
+    topology and parameter slots are reused; parameter values are read when
+    the arena is built.  Integer tensors that are converted anew on every
+    call (e.g. by a serialize_scene that copies them) simply miss the
+    cache."""
+    try:
+        key = hash(tuple(args))
+    except TypeError:  # an unhashable argument: no caching
+        return pack_scene(args)
     with _cache_lock:
         hit = _pack_cache.get(key)
-        if hit is not None:
-            _pack_cache.move_to_end(key)
-            return hit[1]
+    if hit is not None:
+        old, packed, fl, shapes, it, versions = hit
+        if (_same_args(old, args) and [t.shape for t in fl] == shapes and
+                [t._version for t in it] == versions):
+            with _cache_lock:
+                if key in _pack_cache:
+                    _pack_cache.move_to_end(key)
+            return packed
     packed = pack_scene(args)
     with _cache_lock:
-        _pack_cache[key] = (list(args), packed)
+        _pack_cache[key] = (list(args), packed) + tuple(_mutable_state(args))
         while len(_pack_cache) > _PACK_CACHE_SIZE:
             _pack_cache.popitem(last=False)
     return packed

@@ -231,29 +231,57 @@ class RenderFunction(torch.autograd.Function):
         d_arena = torch.zeros(max(packed.num_params, 1), device=device)
         bg = ctx.background_image
         d_bg = torch.zeros_like(bg) if bg is not None else None
-        flags = _native.DVG_FLAG_REUSE_PREP if scene.last_token == ctx.token else 0
-        rargs = _render_args(packed, width, height, nsx, nsy, seed, ctx.arena, bg, ctx.eval_positions, flags)
+        reuse = _native.DVG_FLAG_REUSE_PREP if scene.last_token == ctx.token else 0
         stream = torch.cuda.current_stream(device).cuda_stream
-        with torch.cuda.device(device):
-            if packed.output_type == OutputType.color:
-                scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
-                               d_background_ptr=None if d_bg is None else d_bg.data_ptr(), stream=stream)
-            else:
-                scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(), stream=stream)
+
+        def launch(flags):
+            rargs = _render_args(packed, width, height, nsx, nsy, seed, ctx.arena, bg, ctx.eval_positions, flags)
+            with torch.cuda.device(device):
+                if packed.output_type == OutputType.color:
+                    scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
+                                   d_background_ptr=None if d_bg is None else d_bg.data_ptr(), stream=stream)
+                else:
+                    scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(), stream=stream)
+
+        # the kernels run while the host lays out the gradient views; the
+        # status is checked once the gradient has been read back
+        launch(reuse | _native.DVG_FLAG_NO_SYNC)
         scene.last_token = ctx.token
+        slots = packed.slots
+        dst_of = [t.device if isinstance(t, torch.Tensor) else device for t in packed.tensors]
+        bufs = {device: d_arena}
+        for dst in set(dst_of):
+            if dst != device:
+                bufs[dst] = torch.empty(d_arena.shape, dtype=torch.float32, device=dst)
+        sizes = [sl.numel for sl in slots]
+        parts = {dst: torch.split(b[:sum(sizes)], sizes) for dst, b in bufs.items()}
         d_args = [None] * ctx.num_args
-        # one copy of the gradient arena per destination device, then views
-        arenas = {device: d_arena}
-        for slot, t in zip(packed.slots, packed.tensors):
+        for k, (slot, t) in enumerate(zip(slots, packed.tensors)):
             if not slot.differentiable:
                 continue
-            dst = t.device if isinstance(t, torch.Tensor) else device
-            if dst not in arenas:
-                arenas[dst] = d_arena.to(dst)
-            g = arenas[dst][slot.offset:slot.offset + slot.numel].view(slot.shape)
+            g = parts[dst_of[k]][k]
+            if len(slot.shape) != 1:
+                g = g.view(slot.shape)
             if isinstance(t, torch.Tensor) and t.dtype != g.dtype:
                 g = g.to(t.dtype)
             d_args[slot.arg_index] = g
+        for dst, b in bufs.items():
+            if dst != device:
+                b.copy_(d_arena)  # waits for the kernels
+        try:
+            scene.sync(stream)
+        except _native.SceneCapacityError as e:
+            if 'grown' not in str(e):
+                raise
+            # the tile lists outgrew their capacity and were grown: the
+            # gradient is computed again, synchronously
+            d_arena.zero_()
+            if d_bg is not None:
+                d_bg.zero_()
+            launch(0)
+            for dst, b in bufs.items():
+                if dst != device:
+                    b.copy_(d_arena)
         return (None, None, None, None, None, d_bg if ctx.bg_requested else None) + tuple(d_args)
 
     @staticmethod
