@@ -81,6 +81,7 @@ struct DvgScene {
   float4 *rec_box = nullptr;
   int4 *rec_a = nullptr, *rec_b = nullptr;
   float *rec_r = nullptr;
+  float4 *rec_cbox = nullptr;
   float2 *seg_tpts = nullptr;
   float *seg_th = nullptr;
   unsigned *err = nullptr;  // [0] status bits, [1] tile-list length
@@ -273,6 +274,7 @@ DevScene make_dev(DvgScene *sc, const float *params) {
   S.rec_a = sc->rec_a;
   S.rec_b = sc->rec_b;
   S.rec_r = sc->rec_r;
+  S.rec_cbox = sc->rec_cbox;
   S.seg_tpts = sc->seg_tpts;
   S.seg_th = sc->seg_th;
   S.seg_pmf = sc->seg_pmf;
@@ -284,6 +286,7 @@ DevScene make_dev(DvgScene *sc, const float *params) {
   S.tiles_y = sc->tiles_y;
   S.tile_start = sc->tile_start;
   S.tile_list = reinterpret_cast<int *>(sc->tiles.ptr);
+  S.tile_mask = reinterpret_cast<unsigned *>(sc->tiles.ptr) + sc->tile_cap;
   S.scratch = sc->scratch;
   S.err = sc->err;
   return S;
@@ -417,9 +420,9 @@ int finish(DvgScene *sc, cudaStream_t st, bool *retry) {
     size_t need = (size_t)sc->h_status[1];
     size_t cap = need + need / 2 + 1024;
     if (cap > 0x7fffffffu) return fail(DVG_ERR_CAPACITY, "tile candidate lists exceed 2^31 entries");
-    e = sc->tiles.ensure(cap * sizeof(int));
+    e = sc->tiles.ensure(cap * 2 * sizeof(int));
     if (e != cudaSuccess) return cuda_fail(e, "growing the tile lists");
-    sc->tile_cap = (int)(sc->tiles.bytes / sizeof(int));
+    sc->tile_cap = (int)(sc->tiles.bytes / (2 * sizeof(int)));
     sc->prepared = false;
     *retry = true;
     return DVG_OK;
@@ -513,7 +516,8 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
       sizeof(int) * (10 * (size_t)NSEG + 8 * (size_t)S + 8),                              // scratch
       sizeof(unsigned) * 4,
       sizeof(float2) * DVG_TREE_PTS * (size_t)NSEG, sizeof(float) * DVG_TREE_NODES * (size_t)NSEG,  // trees
-      sizeof(int2) * G, sizeof(float4) * NR, sizeof(int4) * NR, sizeof(int4) * NR, sizeof(float) * NR};  // records
+      sizeof(int2) * G, sizeof(float4) * NR, sizeof(int4) * NR, sizeof(int4) * NR, sizeof(float) * NR,  // records
+      sizeof(float4) * NR};
   e = sc->derived.ensure(carve_size(db));
   if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "allocating scene arenas"); }
   p = reinterpret_cast<char *>(sc->derived.ptr);
@@ -542,13 +546,14 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   sc->rec_a = carve<int4>(p, NR);
   sc->rec_b = carve<int4>(p, NR);
   sc->rec_r = carve<float>(p, NR);
+  sc->rec_cbox = carve<float4>(p, NR);
   e = cudaMemset(sc->derived.ptr, 0, sc->derived.bytes);
   if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "clearing scene arenas"); }
   size_t cap = (size_t)T * 32;
   if (cap < 65536) cap = 65536;
-  e = sc->tiles.ensure(cap * sizeof(int));
+  e = sc->tiles.ensure(cap * 2 * sizeof(int));
   if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "allocating tile lists"); }
-  sc->tile_cap = (int)(sc->tiles.bytes / sizeof(int));
+  sc->tile_cap = (int)(sc->tiles.bytes / (2 * sizeof(int)));
   e = cudaMallocHost(&sc->h_status, 4 * sizeof(unsigned));
   if (e != cudaSuccess) { sc->h_status = nullptr; dvg_scene_destroy(sc); return cuda_fail(e, "pinned status"); }
   *out_scene = sc;

@@ -55,12 +55,15 @@ struct DevScene {
   int tiles_x, tiles_y;
   int *tile_start;          // [tiles+1]
   int *tile_list;           // candidate groups per tile, ascending
+  unsigned *tile_mask;      // per tile-list entry: bit i (< 31) set when the group's stroke record i may
+                            // reach the tile, bit 31 when any record from 31 on may
   int *scratch;             // [8*NSEG + 8*S] path leaf-order scratch
   int2 *g_rec;              // [G] range of each group's stroke records
   float4 *rec_box;          // [records] cull box (empty test: infinite box)
   int4 *rec_a;              // {segment (so + seg; -1: whole-shape record), shape, nc, first point}
   int4 *rec_b;              // {param offset, point count, thickness offset, first record of the next shape}
   float *rec_r;             // stroke radius of the record's shape
+  float4 *rec_cbox;         // canvas box of the record's cull box (one pixel wider), for tile binning
   float2 *seg_tpts = nullptr;  // [NSEG * DVG_TREE_PTS] tabulated subdivision trees (curved segments), or null
   float *seg_th = nullptr;     // [NSEG * DVG_TREE_NODES]
   unsigned *err;            // status word (DVG_EFLAG_*)

@@ -261,12 +261,28 @@ __global__ void k_rec_scan(DevScene S) {
   }
 }
 
+// canvas box of a shape-space box under the group's shape_to_canvas, one
+// pixel wider (the group boxes of k_group_prep are formed the same way)
+DI float4 canvas_box_of(const float *m, float4 b) {
+  if (!(b.x > -INFINITY && b.y > -INFINITY && b.z < INFINITY && b.w < INFINITY))
+    return F4(-INFINITY, -INFINITY, INFINITY, INFINITY);
+  float4 cb = box_empty();
+  cb = box_add(cb, xform_pt(m, V2(b.x, b.y)));
+  cb = box_add(cb, xform_pt(m, V2(b.x, b.w)));
+  cb = box_add(cb, xform_pt(m, V2(b.z, b.y)));
+  cb = box_add(cb, xform_pt(m, V2(b.z, b.w)));
+  return F4(cb.x - 1.f, cb.y - 1.f, cb.z + 1.f, cb.w + 1.f);
+}
+
 __global__ void k_rec_fill(DevScene S) {
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= S.num_groups) return;
   int j = S.g_rec[g].x;
   if (S.g_rec[g].y <= j) return;
   const float4 all = F4(-INFINITY, -INFINITY, INFINITY, INFINITY);
+  float m9[9];
+  const float *xm = S.P + GI(S, g, DVG_GROUP_XFORM_OFF);
+  for (int i = 0; i < 9; i++) m9[i] = xm[i];
   int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
   for (int k = 0; k < nsh; k++) {
     int s = S.group_shapes[off + k];
@@ -278,6 +294,7 @@ __global__ void k_rec_fill(DevScene S) {
     float4 shape_cull = nsh > 1 ? F4(sb.x - r, sb.y - r, sb.z + r, sb.w + r) : all;
     if (!per_segment) {
       S.rec_box[j] = shape_cull;
+      S.rec_cbox[j] = canvas_box_of(m9, shape_cull);
       S.rec_a[j] = make_int4(-1, s, 0, 0);
       S.rec_b[j] = make_int4(po, np, th, j + 1);
       S.rec_r[j] = r;
@@ -291,6 +308,7 @@ __global__ void k_rec_fill(DevScene S) {
       float4 b = S.seg_box[so + seg];
       float rr = S.seg_r[so + seg];
       S.rec_box[j] = nseg > 1 ? F4(b.x - rr, b.y - rr, b.z + rr, b.w + rr) : shape_cull;
+      S.rec_cbox[j] = canvas_box_of(m9, S.rec_box[j]);
       S.rec_a[j] = make_int4(so + seg, s, S.segment_ctrl[so + seg], S.seg_point[so + seg]);
       S.rec_b[j] = make_int4(po, np, th, next);
       S.rec_r[j] = r;
@@ -398,11 +416,36 @@ __device__ __forceinline__ bool tile_hit(int4 r, int tx, int ty) {
 }
 
 // one block per tile: number of candidate groups
+// Whether group g enters the candidate list of tile (tx, ty), and the mask
+// of its stroke records that may reach the tile (tile_mask).  A group whose
+// box reaches the tile enters unless it has no fill and none of its stroke
+// records reaches the tile.
+DI bool tile_keep(const DevScene &S, const int4 *g_tile_range, int g, int tx, int ty, unsigned *mask) {
+  *mask = 0u;
+  if (!tile_hit(g_tile_range[g], tx, ty)) return false;
+  int2 rg = S.g_rec[g];
+  float x0 = (float)(tx * DVG_TILE), y0 = (float)(ty * DVG_TILE);
+  float x1 = x0 + (float)DVG_TILE, y1 = y0 + (float)DVG_TILE;
+  unsigned m = 0u;
+  for (int j = rg.x; j < rg.y; j++) {
+    int rel = j - rg.x;
+    if (rel >= 31) {
+      m |= 1u << 31;
+      break;
+    }
+    float4 b = S.rec_cbox[j];
+    if (b.x <= x1 && b.z >= x0 && b.y <= y1 && b.w >= y0) m |= 1u << rel;
+  }
+  *mask = m;
+  return m != 0u || GI(S, g, DVG_GROUP_FILL_KIND) != DVG_PAINT_NONE;
+}
+
 __global__ void k_bin_count(DevScene S, const int4 *g_tile_range, int *tile_count) {
   int t = blockIdx.x;
   int tx = t % S.tiles_x, ty = t / S.tiles_x;
   int c = 0;
-  for (int g = threadIdx.x; g < S.num_groups; g += blockDim.x) c += tile_hit(g_tile_range[g], tx, ty) ? 1 : 0;
+  unsigned mask;
+  for (int g = threadIdx.x; g < S.num_groups; g += blockDim.x) c += tile_keep(S, g_tile_range, g, tx, ty, &mask) ? 1 : 0;
   __shared__ int red[32];
   for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
@@ -456,7 +499,8 @@ __global__ void k_bin_fill(DevScene S, const int4 *g_tile_range) {
   __syncthreads();
   for (int g0 = 0; g0 < S.num_groups; g0 += blockDim.x) {
     int g = g0 + threadIdx.x;
-    bool hit = g < S.num_groups && tile_hit(g_tile_range[g], tx, ty);
+    unsigned mask = 0u;
+    bool hit = g < S.num_groups && tile_keep(S, g_tile_range, g, tx, ty, &mask);
     unsigned m = __ballot_sync(0xffffffffu, hit);
     if (lane == 0) warp_cnt[wid] = __popc(m);
     __syncthreads();
@@ -466,7 +510,11 @@ __global__ void k_bin_fill(DevScene S, const int4 *g_tile_range) {
       if (w < wid) before += c;
       total += c;
     }
-    if (hit) S.tile_list[base_sh + before + __popc(m & ((1u << lane) - 1u))] = g;
+    if (hit) {
+      int at = base_sh + before + __popc(m & ((1u << lane) - 1u));
+      S.tile_list[at] = g;
+      S.tile_mask[at] = mask;
+    }
     __syncthreads();
     if (threadIdx.x == 0) base_sh += total;
     __syncthreads();

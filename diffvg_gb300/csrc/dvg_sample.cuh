@@ -162,8 +162,9 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
   if (active) list = cand_range(S, pt, k, e);
   const int G = S.num_groups;
   int nf = 0;
-  // stroke records of the group in progress
-  int g = 0, j = 0, jend = 0, glo = 0, cs = -1, slo = 0;
+  // stroke records of the group in progress (gmask: tile_mask of its entry)
+  int g = 0, j = 0, jb = 0, jend = 0, glo = 0, cs = -1, slo = 0;
+  unsigned gmask = 0xffffffffu;
   bool in_group = false, is_eq = false, gret = false, mark = false;
   v2 lp = pt;
   // the test the walk stopped at
@@ -182,6 +183,15 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
     while (true) {
       if (in_group) {
         if (j < jend) {
+          int rel = j - jb;
+          if (rel < 31) {  // skip the records that cannot reach the tile
+            unsigned m = (gmask & 0x7fffffffu) >> rel;
+            if (m == 0u) {
+              j = (gmask >> 31) ? jb + 31 : jend;
+              continue;
+            }
+            j += __ffs(m) - 1;
+          }
           float4 b = __ldg(&S.rec_box[j]);
           if (!(lp.x >= b.x && lp.x <= b.z && lp.y >= b.y && lp.y <= b.w)) {
             j++;
@@ -221,11 +231,12 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
       }
       if (k >= e) break;
       g = list ? __ldg(&S.tile_list[k]) : k;
+      gmask = list ? __ldg(&S.tile_mask[k]) : 0xffffffffu;
       k++;
       if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
       int2 rg = __ldg(&S.g_rec[g]);
-      if (rg.y > rg.x) {
-        j = rg.x;
+      if (rg.y > rg.x && gmask != 0u) {
+        j = jb = rg.x;
         jend = rg.y;
         lp = xform_pt(S.c2s + 9 * g, pt);
         glo = njobs;

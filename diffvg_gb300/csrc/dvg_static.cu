@@ -125,14 +125,14 @@ extern "C" int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRen
          o_err = c.take<unsigned>(4), o_weight = c.take<float>((size_t)npx), o_samples = c.take<float4>((size_t)n);
   int NR = dvg::count_stroke_records(desc);
   size_t o_grec = c.take<int2>(G), o_rbox = c.take<float4>(NR), o_ra = c.take<int4>(NR), o_rb = c.take<int4>(NR),
-         o_rr = c.take<float>(NR);
+         o_rr = c.take<float>(NR), o_rcb = c.take<float4>(NR);
   size_t o_tiles = c.take<int>(0);
   c.off = o_tiles;
   if (o_tiles + 256 * sizeof(int) > DVG_STATIC_SCRATCH_BYTES)
     return dvg::fail(DVG_ERR_CAPACITY,
                      "scene and image need %zu bytes of scratch; the allocation-free render has %u",
                      o_tiles + 256 * sizeof(int), (unsigned)DVG_STATIC_SCRATCH_BYTES);
-  int tile_cap = (int)((DVG_STATIC_SCRATCH_BYTES - o_tiles) / sizeof(int));
+  int tile_cap = (int)((DVG_STATIC_SCRATCH_BYTES - o_tiles) / (2 * sizeof(int)));  // tile lists and masks
 
   void *base_v = nullptr;
   if ((st = static_scratch(&base_v)) != DVG_OK) return st;
@@ -181,6 +181,7 @@ extern "C" int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRen
   S.tiles_y = tiles_y;
   S.tile_start = reinterpret_cast<int *>(base + o_tstart);
   S.tile_list = reinterpret_cast<int *>(base + o_tiles);
+  S.tile_mask = reinterpret_cast<unsigned *>(base + o_tiles) + tile_cap;
   S.scratch = reinterpret_cast<int *>(base + o_scratch);
   S.err = reinterpret_cast<unsigned *>(base + o_err);
   S.g_rec = reinterpret_cast<int2 *>(base + o_grec);
@@ -188,6 +189,7 @@ extern "C" int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRen
   S.rec_a = reinterpret_cast<int4 *>(base + o_ra);
   S.rec_b = reinterpret_cast<int4 *>(base + o_rb);
   S.rec_r = reinterpret_cast<float *>(base + o_rr);
+  S.rec_cbox = reinterpret_cast<float4 *>(base + o_rcb);
 
   if (G == 0) {
     e = a->background ? cudaMemcpyAsync(image, a->background, (size_t)npx * 4 * sizeof(float), cudaMemcpyDeviceToDevice, s)
