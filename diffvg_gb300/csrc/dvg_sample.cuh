@@ -148,28 +148,24 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
 // segments queued.  Returns the number of candidate fragments (capped).
 //
 // All 32 lanes of the warp call it (lanes without a sample pass active =
-// false).  Each lane walks its own candidates: the tile's groups, then each
-// stroke group's records (its shapes' segments with their cull boxes, in
-// the order of the nested loops of within_distance, within_distance.h:355-446,
-// and sample_color, diffvg.cpp:525-585).  The walk stops at each segment
-// that needs a test, and the segment tests of all lanes then run together.
-// A shape that hits ends its own walk (and its group's, outside the group of
-// an edge query) as the reference's early returns do.
+// false) and walk the candidates together: the groups of the lanes' tile
+// lists in ascending order (a merge of the lists: the lanes of a warp mostly
+// share one tile), and inside a stroke group its records (its shapes'
+// segments with their cull boxes, in the order of the nested loops of
+// within_distance, within_distance.h:355-446, and sample_color,
+// diffvg.cpp:525-585).  Each lane tests its own point; the records' loads and
+// the loop control are shared, and the segment tests of the lanes whose
+// culls pass run together.  A shape that hits ends the lane's walk of that
+// shape (and of its group, outside the group of an edge query) as the
+// reference's early returns do.
 DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q, int lane, int &njobs, EdgeQ *eq,
                          unsigned &eq_jobs, bool &overflow, bool active) {
+  const unsigned full = 0xffffffffu;
   int k = 0, e = 0;
   bool list = true;
   if (active) list = cand_range(S, pt, k, e);
   const int G = S.num_groups;
   int nf = 0;
-  // stroke records of the group in progress (gmask: tile_mask of its entry)
-  int g = 0, j = 0, jb = 0, jend = 0, glo = 0, cs = -1, slo = 0;
-  unsigned gmask = 0xffffffffu;
-  bool in_group = false, is_eq = false, gret = false, mark = false;
-  v2 lp = pt;
-  // the test the walk stopped at
-  int s = 0, po = 0, np = 0, th = 0, nc = 0, i0 = 0, segi = 0, jnext = 0;
-  float r = 0.f;
   auto emit = [&](int key, int meta) {
     if (nf < DVG_MAX_FRAGMENTS) frags[nf++] = FragRef{key, meta};
     else overflow = true;
@@ -177,105 +173,89 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
   auto fill = [&](int gg) {
     if (GI(S, gg, DVG_GROUP_FILL_KIND) != DVG_PAINT_NONE && group_inside(S, gg, pt, eq)) emit(2 * gg, DVG_META_HIT);
   };
+  #pragma unroll 1
   while (true) {
-    bool have = false, shape_hit = false;
+    int myg = k < e ? (list ? __ldg(&S.tile_list[k]) : k) : 0x7fffffff;
+    int g = __reduce_min_sync(full, myg);
+    if (g == 0x7fffffff) break;
+    bool act = myg == g;
+    unsigned tmask = act ? (list ? __ldg(&S.tile_mask[k]) : full) : 0u;
+    if (act) k++;
+    if (act && G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) act = false;
+    if (!__any_sync(full, act)) continue;
+    int2 rg = __ldg(&S.g_rec[g]);
+    unsigned um = __reduce_or_sync(full, act ? tmask : 0u);
+    if (rg.y <= rg.x || um == 0u) {  // no stroke record of the group reaches these tiles
+      if (act) fill(g);
+      continue;
+    }
+    // stroke records of g, walked together
+    v2 lp = act ? xform_pt(S.c2s + 9 * g, pt) : pt;
+    int glo = njobs, cs = -1, slo = njobs, skip_to = rg.x;
+    bool live = act, gret = false, mark = false;
+    bool is_eq = act && eq && eq->group == g;
+    int jb = rg.x, j = rg.x;
     #pragma unroll 1
-    while (true) {
-      if (in_group) {
-        if (j < jend) {
-          int rel = j - jb;
-          if (rel < 31) {  // skip the records that cannot reach the tile
-            unsigned m = (gmask & 0x7fffffffu) >> rel;
-            if (m == 0u) {
-              j = (gmask >> 31) ? jb + 31 : jend;
-              continue;
-            }
-            j += __ffs(m) - 1;
-          }
-          float4 b = __ldg(&S.rec_box[j]);
-          if (!(lp.x >= b.x && lp.x <= b.z && lp.y >= b.y && lp.y <= b.w)) {
-            j++;
-            continue;
-          }
-          int4 a = __ldg(&S.rec_a[j]), c = __ldg(&S.rec_b[j]);
-          r = __ldg(&S.rec_r[j]);
-          j++;
-          s = a.y;
-          jnext = c.w;
-          if (s != cs) {  // the walk enters the next shape: its jobs start here
-            cs = s;
-            slo = njobs;
-            mark = is_eq && s == eq->shape;
-          }
-          if (a.x < 0) {
-            if (within_shape(S, s, lp, r)) {
-              shape_hit = true;
-              break;
-            }
-            continue;
-          }
-          segi = a.x;
-          nc = a.z;
-          i0 = a.w;
-          po = c.x;
-          np = c.y;
-          th = c.z;
-          have = true;
-          break;
+    while (j < rg.y) {
+      int rel = j - jb;
+      if (rel < 31) {  // skip the records that cannot reach the lanes' tiles
+        unsigned m = (um & 0x7fffffffu) >> rel;
+        if (m == 0u) {
+          if (!(um >> 31)) break;
+          j = jb + 31;
+          continue;
         }
-        in_group = false;  // the group's stroke is decided up to its queued jobs
-        if (gret) emit(2 * g + 1, DVG_META_HIT);
-        else if (njobs > glo) emit(2 * g + 1, glo | (njobs << 8));
-        fill(g);
-        continue;
+        j += __ffs(m) - 1;
       }
-      if (k >= e) break;
-      g = list ? __ldg(&S.tile_list[k]) : k;
-      gmask = list ? __ldg(&S.tile_mask[k]) : 0xffffffffu;
-      k++;
-      if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
-      int2 rg = __ldg(&S.g_rec[g]);
-      if (rg.y > rg.x && gmask != 0u) {
-        j = jb = rg.x;
-        jend = rg.y;
-        lp = xform_pt(S.c2s + 9 * g, pt);
-        glo = njobs;
-        gret = false;
-        is_eq = eq && eq->group == g;
-        cs = -1;
-        in_group = true;
-        continue;
+      float4 b = __ldg(&S.rec_box[j]);
+      bool test = live && j >= skip_to && lp.x >= b.x && lp.x <= b.z && lp.y >= b.y && lp.y <= b.w;
+      if (__any_sync(full, test)) {
+        int4 a = __ldg(&S.rec_a[j]), c = __ldg(&S.rec_b[j]);
+        float r = __ldg(&S.rec_r[j]);
+        int s = a.y;
+        if (test && s != cs) {  // the lane enters the next shape: its jobs start here
+          cs = s;
+          slo = njobs;
+          mark = is_eq && s == eq->shape;
+        }
+        int f = 0;
+        if (a.x < 0) {
+          if (test) f = within_shape(S, s, lp, r) ? 1 : 0;
+        } else if (test) {
+          f = within_segment_pre(S, c.x, c.y, c.z, 0, a.z, a.w, a.x, lp, r);  // the lanes' tests run together
+          if (f == 2) {
+            if (njobs < DVG_LANE_JOBS) {
+              q->job[lane][njobs] = SegJob{s, a.x, lp.x, lp.y, r};
+              if (mark) eq_jobs |= 1u << njobs;
+              njobs++;
+              f = 0;
+            } else {
+              f = segment_solve(S, c.x, c.y, c.z, a.z, a.w, lp, r);  // queue full: solve now
+            }
+          }
+        }
+        if (f == 1) {  // the shape hits
+          if (mark) eq_jobs &= (1u << slo) - 1u;
+          njobs = slo;  // its queued jobs are moot
+          skip_to = c.w;
+          if (!is_eq) {
+            njobs = glo;
+            live = false;
+            emit(2 * g + 1, DVG_META_HIT);
+            fill(g);
+          } else {
+            gret = true;
+            if (s == eq->shape) eq->hit = 1;
+          }
+        }
+        if (!__any_sync(full, live)) break;
       }
+      j++;
+    }
+    if (live) {  // the group's stroke is decided up to its queued jobs
+      if (gret) emit(2 * g + 1, DVG_META_HIT);
+      else if (njobs > glo) emit(2 * g + 1, glo | (njobs << 8));
       fill(g);
-    }
-    if (!__any_sync(0xffffffffu, have || shape_hit)) break;
-    int f = shape_hit ? 1 : 0;
-    if (have) {
-      f = within_segment_pre(S, po, np, th, 0, nc, i0, segi, lp, r);  // the lanes' tests run together
-      if (f == 2) {
-        if (njobs < DVG_LANE_JOBS) {
-          q->job[lane][njobs] = SegJob{s, segi, lp.x, lp.y, r};
-          if (mark) eq_jobs |= 1u << njobs;
-          njobs++;
-          f = 0;
-        } else {
-          f = segment_solve(S, po, np, th, nc, i0, lp, r);  // queue full: solve now
-        }
-      }
-    }
-    if (f == 1) {  // the shape hits
-      if (mark) eq_jobs &= (1u << slo) - 1u;
-      njobs = slo;  // its queued jobs are moot
-      j = jnext;
-      if (!is_eq) {
-        njobs = glo;
-        in_group = false;
-        emit(2 * g + 1, DVG_META_HIT);
-        fill(g);
-      } else {
-        gret = true;
-        if (s == eq->shape) eq->hit = 1;
-      }
     }
   }
   return nf;
