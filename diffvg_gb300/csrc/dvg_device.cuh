@@ -777,13 +777,11 @@ DI void emu_blossom4(const float b[5], float l, float u, float c[5]) {
     c[k] = w[0];
   }
 }
-// roots in (0,1) of c3 t^3 + c2 t^2 + c1 t + c0 with certified enclosure
-// radii (sign change certain at root +- rad); the count, or -1 when a
-// stationary point or an end sits within del of zero
-DI int emu_cubic_roots01(float c3, float c2, float c1, float c0, float del, float root[3], float rad[3]) {
-  float ts[4];
-  int nt = 0;
-  ts[nt++] = 0.f;
+// roots in (0,1) of c3 t^3 + c2 t^2 + c1 t + c0, one slot per monotone piece
+// (split at the stationary points), each with a certified enclosure radius
+// (the sign change at root +- rad is certain); false when a stationary
+// point or an end sits within del of zero, or an enclosure fails
+DI bool emu_cubic_roots3(float c3, float c2, float c1, float c0, float del, float root[3], float rad[3], bool has[3]) {
   float qa = 3 * c3, qb = 2 * c2, qc = c1, e0 = -1.f, e1 = -1.f;
   float sc = fabsf(qa) + fabsf(qb) + fabsf(qc);
   if (fabsf(qa) > 1e-7f * sc) {
@@ -798,21 +796,23 @@ DI int emu_cubic_roots01(float c3, float c2, float c1, float c0, float del, floa
     e0 = -qc / qb;
   }
   if (e0 > e1) { float tmp = e0; e0 = e1; e1 = tmp; }
-  if (e0 > 0.f && e0 < 1.f) ts[nt++] = e0;
-  if (e1 > 0.f && e1 < 1.f && e1 != e0) ts[nt++] = e1;
-  ts[nt++] = 1.f;
-  int n = 0;
+  bool h0 = e0 > 0.f && e0 < 1.f, h1 = e1 > 0.f && e1 < 1.f && e1 != e0;
+  float ts[4] = {0.f, h0 ? e0 : (h1 ? e1 : 1.f), (h0 && h1) ? e1 : 1.f, 1.f};
+  bool ok = true;
   float ya = emu_p3(c3, c2, c1, c0, ts[0]);
-  if (fabsf(ya) <= del) return -1;
-#pragma unroll 1
-  for (int k = 1; k < nt; k++) {
+  ok = ok && fabsf(ya) > del;
+#pragma unroll
+  for (int k = 1; k < 4; k++) {
     float yb = emu_p3(c3, c2, c1, c0, ts[k]);
-    if (fabsf(yb) <= del) return -1;
-    if ((ya < 0) != (yb < 0)) {
+    ok = ok && fabsf(yb) > del;
+    has[k - 1] = false;
+    root[k - 1] = 0.f;
+    rad[k - 1] = 0.f;
+    if (ok && (ya < 0) != (yb < 0)) {
       float lo = ts[k - 1], hi = ts[k];
       bool up = yb > ya;
       float r = 0.5f * (lo + hi);
-#pragma unroll 1
+      #pragma unroll 1
       for (int it = 0; it < DVG_EMU_NEWTON; it++) {  // Newton kept inside the bracket
         float y = emu_p3(c3, c2, c1, c0, r), dy = (3 * c3 * r + 2 * c2) * r + c1;
         if ((y > 0) == up) hi = r; else lo = r;
@@ -820,17 +820,30 @@ DI int emu_cubic_roots01(float c3, float c2, float c1, float c0, float del, floa
         r = (nr >= lo && nr <= hi) ? nr : 0.5f * (lo + hi);
       }
       float dp = fabsf((3 * c3 * r + 2 * c2) * r + c1);
-      if (!(dp > 0.f)) return -1;
       float eps = fmaxf(4e-7f, __fdividef(4.f * del, dp));
       float ym = emu_p3(c3, c2, c1, c0, r - eps), yp = emu_p3(c3, c2, c1, c0, r + eps);
-      if (!(fabsf(ym) > del && fabsf(yp) > del && ((ym < 0) != (yp < 0)))) return -1;
-      root[n] = r;
-      rad[n] = eps;
-      n++;
+      ok = ok && dp > 0.f && fabsf(ym) > del && fabsf(yp) > del && ((ym < 0) != (yp < 0));
+      has[k - 1] = true;
+      root[k - 1] = r;
+      rad[k - 1] = eps;
     }
     ya = yb;
   }
-  return n;
+  return ok;
+}
+// v[i] for an index known only at run time, from values kept in registers
+DI float emu_pick6(const float v[6], int i) {
+  float r = v[0];
+#pragma unroll
+  for (int k = 1; k < 6; k++) r = i == k ? v[k] : r;
+  return r;
+}
+// compare-exchange of (key, payload) pairs
+DI void emu_cx(float &a, float &ra, float &b, float &rb) {
+  if (a > b) {
+    float t = a; a = b; b = t;
+    t = ra; ra = rb; rb = t;
+  }
 }
 // Root structure of Q on [l,u] (Q(l), Q(u) of certain opposite signs): 1
 // with the piece [ra,rb] that holds the one simple root and mu = min |Q'|
@@ -875,8 +888,12 @@ DI int emu_unique_root(const float n[6], const float qb[5], float l, float u, fl
   }
   return nroot == 1;
 }
-static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float r0, float r1,
-                                                       float r2, float r3) {
+// Called with uniform = true by all 32 lanes of a warp together (lanes
+// without a test pass valid = false): the bracket loop then runs a
+// warp-wide trip count so the lanes' brackets are decided in step.
+static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform, v2 p0, v2 p1, v2 p2, v2 p3, v2 pt,
+                                                       float r0, float r1, float r2, float r3) {
+  int res = valid ? -1 : 2;  // -1: not decided yet
   // distance quintic coefficients exactly as the reference forms them in fp32 (within_distance.h:150-167)
   v2 a = add2(sub2(add2(neg2(p0), scl2(3, p1)), scl2(3, p2)), p3);
   v2 b = add2(sub2(scl2(3, p0), scl2(6, p1)), scl2(3, p2));
@@ -886,7 +903,7 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
   float D = 3 * (sum2(mul2(b, c)) + sum2(mul2(a, e))), E = sum2(mul2(c, c)) + 2 * sum2(mul2(e, b));
   float F = sum2(mul2(e, c));
   float sabs = fabsf(A) + fabsf(B) + fabsf(C) + fabsf(D) + fabsf(E) + fabsf(F);
-  if (!(A > 1e-5f * sabs)) return 2;
+  if (!(A > 1e-5f * sabs)) res = 2;
   float ia = 1.f / A;
   float n[6] = {1.f, B * ia, C * ia, D * ia, E * ia, F * ia};
   float ns = 1.f + fabsf(n[1]) + fabsf(n[2]) + fabsf(n[3]) + fabsf(n[4]) + fabsf(n[5]);
@@ -911,64 +928,82 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
     del += fabsf(pA) + 2e-6f * mA + 1e-6f;
     pA = 0.f;
   }
-  float bp[4], br[4];
-  int nb = 0;
+  // breakpoints: -B/5 and the isolator's roots, each with its enclosure radius (absent: +inf)
   float qr = -n[1] * 0.2f, eq = 3e-7f * fabsf(qr) + 1e-7f;
-  if (fabsf(qr) <= eq || fabsf(qr - 1.f) <= eq) return 2;
-  if (qr > 0.f && qr < 1.f) { bp[nb] = qr; br[nb] = eq; nb++; }
-  float rts[3], rrad[3];
-  int nr = emu_cubic_roots01(pA, pB, pC, pD, del, rts, rrad);
-  if (nr < 0) return 2;
-  #pragma unroll 1
-  for (int k = 0; k < nr; k++) {
-    float rad = rrad[k] + 1.2e-7f;
-    if (rts[k] - rad <= 0.f || rts[k] + rad >= 1.f) return 2;
-    bp[nb] = rts[k];
-    br[nb] = rad;
-    nb++;
-  }
-  #pragma unroll 1
-  for (int j = 1; j < nb; j++)
-    #pragma unroll 1
-    for (int k = j; k > 0 && bp[k - 1] > bp[k]; k--) {
-      float t = bp[k]; bp[k] = bp[k - 1]; bp[k - 1] = t;
-      t = br[k]; br[k] = br[k - 1]; br[k - 1] = t;
+  if (fabsf(qr) <= eq || fabsf(qr - 1.f) <= eq) res = 2;
+  float bp[5], br[5];
+  bool hq = qr > 0.f && qr < 1.f;
+  bp[0] = hq ? qr : INFINITY;
+  br[0] = hq ? eq : 0.f;
+  int nb = hq ? 1 : 0;
+  {
+    float rts[3], rrad[3];
+    bool has[3];
+    if (!emu_cubic_roots3(pA, pB, pC, pD, del, rts, rrad, has)) res = 2;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      float rad = rrad[k] + 1.2e-7f;
+      if (has[k] && (rts[k] - rad <= 0.f || rts[k] + rad >= 1.f)) res = 2;
+      bp[k + 1] = has[k] ? rts[k] : INFINITY;
+      br[k + 1] = has[k] ? rad : 0.f;
+      nb += has[k] ? 1 : 0;
     }
-  #pragma unroll 1
-  for (int j = 1; j < nb; j++)
-    if (bp[j] - bp[j - 1] <= br[j] + br[j - 1]) return 2;
-  // bracket ends, Q there, and |Q'| within the enclosure of each breakpoint
-  float ends[6], val[6], qloc[6];
-  int ne = 0;
-  float qpp = 20 + 12 * fabsf(n[1]) + 6 * fabsf(n[2]) + 2 * fabsf(n[3]);  // |Q''| on [0,1]
-  ends[ne] = 0.f; val[ne] = n[5]; qloc[ne] = 0.f; ne++;
-  #pragma unroll 1
-  for (int j = 0; j < nb; j++) {
-    float t = bp[j];
-    float qd = (((5 * t + 4 * n[1]) * t + 3 * n[2]) * t + 2 * n[3]) * t + n[4];
-    ends[ne] = t;
-    val[ne] = emu_q(n, t);
-    qloc[ne] = fabsf(qd) + dQp + qpp * br[j];
-    if (fabsf(val[ne]) <= dQ + qloc[ne] * br[j]) return 2;  // the sign the reference reads is not certain
-    ne++;
   }
-  ends[ne] = 1.f; val[ne] = emu_q(n, 1.f); qloc[ne] = 0.f; ne++;
-  if (fabsf(val[0]) <= dQ || fabsf(val[ne - 1]) <= dQ) return 2;
+  bp[4] = 1.f;  // the end t = 1 sorts after every breakpoint, before the absent ones
+  br[4] = 0.f;
+  // sorting network on the five entries
+  emu_cx(bp[0], br[0], bp[1], br[1]); emu_cx(bp[3], br[3], bp[4], br[4]); emu_cx(bp[2], br[2], bp[4], br[4]);
+  emu_cx(bp[2], br[2], bp[3], br[3]); emu_cx(bp[0], br[0], bp[3], br[3]); emu_cx(bp[0], br[0], bp[2], br[2]);
+  emu_cx(bp[1], br[1], bp[4], br[4]); emu_cx(bp[1], br[1], bp[3], br[3]); emu_cx(bp[1], br[1], bp[2], br[2]);
+#pragma unroll
+  for (int j = 1; j < 4; j++)
+    if (j < nb && bp[j] - bp[j - 1] <= br[j] + br[j - 1]) res = 2;
+  // bracket ends (slot 0: t = 0; slots 1..nb: breakpoints; slot nb + 1: t = 1), Q there, and |Q'| within
+  // the enclosure of each breakpoint
+  int ne = nb + 2;
+  float ends[6], val[6], qloc[6], bre[6];
+  float qpp = 20 + 12 * fabsf(n[1]) + 6 * fabsf(n[2]) + 2 * fabsf(n[3]);  // |Q''| on [0,1]
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    float t = j == 0 ? 0.f : bp[j - 1];
+    float rj = j == 0 ? 0.f : br[j - 1];
+    float qd = (((5 * t + 4 * n[1]) * t + 3 * n[2]) * t + 2 * n[3]) * t + n[4];
+    ends[j] = t;
+    bre[j] = rj;
+    val[j] = j == 0 ? n[5] : emu_q(n, t);
+    qloc[j] = rj > 0.f ? fabsf(qd) + dQp + qpp * rj : 0.f;
+    // the sign the reference reads is not certain
+    if (j < ne && fabsf(val[j]) <= dQ + qloc[j] * rj) res = 2;
+  }
+  // brackets whose ends change sign (bit j: slots j, j + 1)
+  unsigned sc = 0u;
+#pragma unroll
+  for (int j = 0; j < 5; j++)
+    if (j + 1 < ne && (val[j] < 0) != (val[j + 1] < 0)) sc |= 1u << j;
   float bmax = 3 * fmaxf(fmaxf(dist2(p0, p1), dist2(p1, p2)), dist2(p2, p3));    // |cubic'|
   float rmaxd = 3 * fmaxf(fmaxf(fabsf(r1 - r0), fabsf(r2 - r1)), fabsf(r3 - r2));  // |radius'|
   float M = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
   bool unsure = false;
-  int lj = 0;  // lower bracket end: kept through brackets without a sign change
+  int cnt = res < 0 ? __popc(sc) : 0;
+  int rounds = uniform ? __reduce_max_sync(0xffffffffu, cnt) : cnt;
+  unsigned rem = sc;
   #pragma unroll 1
-  for (int j = 0; j + 1 < ne; j++) {
-    if ((val[j] < 0) == (val[j + 1] < 0)) continue;
-    int i0 = lj;
-    lj = j + 1;
-    // the reference's bracket ends sit within br of ours: the certain part of the bracket
-    float rl = i0 > 0 ? br[i0 - 1] : 0.f, ru = j + 1 < ne - 1 ? br[j] : 0.f;
-    float l = ends[i0] + rl, u = ends[j + 1] - ru;
+  for (int it = 0; it < rounds; it++) {
+    if (res >= 0 || it >= cnt) continue;
+    int j = __ffs(rem) - 1;
+    rem &= rem - 1u;
+    // lower bracket end: the end of the previous sign-change bracket (the reference keeps its lower end
+    // through brackets without a sign change, within_distance.h:237-240)
+    unsigned below = sc & ((1u << j) - 1u);
+    int i0 = below ? 32 - __clz(below) : 0;
+    float el = emu_pick6(ends, i0), eu = emu_pick6(ends, j + 1);
+    float vl = emu_pick6(val, i0), vu = emu_pick6(val, j + 1);
+    float rl = emu_pick6(bre, i0), ru = emu_pick6(bre, j + 1);
+    float ql0 = emu_pick6(qloc, i0), qu0 = emu_pick6(qloc, j + 1);
+    // the reference's bracket ends sit within the enclosures of ours: the certain part of the bracket
+    float l = el + rl, u = eu - ru;
     // the iteration may stop right at an end where |Q| < 1e-5
-    if (fabsf(val[i0]) <= 1e-5f + dQ + 2.f * qloc[i0] * rl || fabsf(val[j + 1]) <= 1e-5f + dQ + 2.f * qloc[j + 1] * ru) {
+    if (fabsf(vl) <= 1e-5f + dQ + 2.f * ql0 * rl || fabsf(vu) <= 1e-5f + dQ + 2.f * qu0 * ru) {
       unsure = true;
       continue;
     }
@@ -978,8 +1013,8 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
     if (!emu_unique_root(n, qbz, l, u, ql, qu, dQ, dQp, 1e-5f, &ra, &rb, &mu)) { unsure = true; continue; }
     bool up = emu_q(n, rb) > emu_q(n, ra);
     float lo = ra, hi = rb, ts = 0.5f * (ra + rb);
-#pragma unroll 1
-    for (int it = 0; it < DVG_EMU_NEWTON; it++) {  // Newton kept inside the root piece
+    #pragma unroll 1
+    for (int k = 0; k < DVG_EMU_NEWTON; k++) {  // Newton kept inside the root piece
       float y = emu_q(n, ts), dy = (((5 * ts + 4 * n[1]) * ts + 3 * n[2]) * ts + 2 * n[3]) * ts + n[4];
       if ((y > 0) == up) hi = ts; else lo = ts;
       float nt = ts - __fdividef(y, dy);
@@ -989,20 +1024,21 @@ static __device__ __noinline__ int cubic_stroke_decide(v2 p0, v2 p1, v2 p2, v2 p
     float er = hi - lo;
     {
       float dts = (((5 * ts + 4 * n[1]) * ts + 3 * n[2]) * ts + 2 * n[3]) * ts + n[4];
-      float e = fmaxf(2e-7f, __fdividef(2.f * (fabsf(emu_q(n, ts)) + dQ), fmaxf(fabsf(dts), mu)));
-      float qm = emu_q(n, ts - e), qp = emu_q(n, ts + e);
-      if (fabsf(qm) > dQ && fabsf(qp) > dQ && ((qm < 0) != (qp < 0))) er = fminf(er, e);
+      float e2 = fmaxf(2e-7f, __fdividef(2.f * (fabsf(emu_q(n, ts)) + dQ), fmaxf(fabsf(dts), mu)));
+      float qm = emu_q(n, ts - e2), qp = emu_q(n, ts + e2);
+      if (fabsf(qm) > dQ && fabsf(qp) > dQ && ((qm < 0) != (qp < 0))) er = fminf(er, e2);
     }
     // where the reference may stop: |Q| < 1e-5 around the root, or the 20-step bisection window
-    float eps_t = __fdividef(1e-5f + dQ, mu) * 1.000001f + er + (ends[j + 1] - ends[i0]) * 4e-6f + 1e-6f;
+    float eps_t = __fdividef(1e-5f + dQ, mu) * 1.000001f + er + (eu - el) * 4e-6f + 1e-6f;
     float margin = (bmax + rmaxd) * eps_t + far_margin(M);
     float tt = 1 - ts;
     float rr = (tt * tt * tt) * r0 + (3 * tt * tt * ts) * r1 + (3 * tt * ts * ts) * r2 + (ts * ts * ts) * r3;
     float dd = dist2(eval_cubic(p0, p1, p2, p3, ts), pt);
-    if (dd < rr - margin) return 1;  // the reference returns 1 here or at an earlier bracket
-    if (dd <= rr + margin) unsure = true;
+    if (dd < rr - margin) res = 1;  // the reference returns 1 here or at an earlier bracket
+    else if (dd <= rr + margin) unsure = true;
   }
-  return unsure ? 2 : 0;
+  if (res < 0) res = unsure ? 2 : 0;
+  return res;
 }
 
 // Root-solve part of the stroke test of one quadratic (nc = 1) or cubic
@@ -1108,13 +1144,20 @@ DN int within_segment_pre(const DevScene &S, int po, int np, int th, int flags, 
 
 // fp32 decision of an undecided segment (cubics: cubic_stroke_decide); 2
 // when it stays undecided
-DI int segment_decide(const DevScene &S, int po, int np, int th, int nc, int i0, v2 pt, float r) {
-  if (nc != 2) return 2;
-  int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
-  v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2), p3 = path_pt(S, po, i3);
+// uniform: all 32 lanes of the warp call together (valid = false for lanes without a test)
+DI int segment_decide(const DevScene &S, int po, int np, int th, int nc, int i0, v2 pt, float r, bool valid = true,
+                      bool uniform = false) {
+  bool cubic = valid && nc == 2;
+  if (!uniform && !cubic) return 2;
+  v2 p0 = V2(0.f, 0.f), p1 = p0, p2 = p0, p3 = p0;
   float r0 = r, r1 = r, r2 = r, r3 = r;
-  if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); r3 = pget(S, th + i3); }
-  return cubic_stroke_decide(p0, p1, p2, p3, pt, r0, r1, r2, r3);
+  if (cubic) {
+    int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
+    p0 = path_pt(S, po, i0); p1 = path_pt(S, po, i1); p2 = path_pt(S, po, i2); p3 = path_pt(S, po, i3);
+    if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); r3 = pget(S, th + i3); }
+  }
+  int f = cubic_stroke_decide(cubic, uniform, p0, p1, p2, p3, pt, r0, r1, r2, r3);
+  return cubic ? f : 2;
 }
 
 // an undecided segment, decided: fp32 where that suffices, else the fp64 solve

@@ -115,17 +115,16 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
   #pragma unroll 1
   for (int base = 0; base < total; base += 32) {  // warp-uniform trip count
     int j = base + lane;
-    bool pending = false;
-    if (j < total) {
-      int owner, idx;
-      SegJob jb = warp_job(q, j, owner, idx);
-      int s = jb.shape;
-      int f = segment_decide(S, SI(S, s, DVG_SHAPE_PARAM_OFF), SI(S, s, DVG_SHAPE_NUM_POINTS),
-                             SI(S, s, DVG_SHAPE_THICKNESS_OFF), __ldg(&S.segment_ctrl[jb.seg]),
-                             __ldg(&S.seg_point[jb.seg]), V2(jb.x, jb.y), jb.r);
-      if (f == 1) atomicOr(&q->result[owner], 1u << idx);
-      pending = f == 2;
-    }
+    bool valid = j < total;
+    int owner = 0, idx = 0;
+    SegJob jb = valid ? warp_job(q, j, owner, idx) : SegJob{0, 0, 0.f, 0.f, 0.f};
+    int s = jb.shape;
+    int f = segment_decide(S, valid ? SI(S, s, DVG_SHAPE_PARAM_OFF) : 0, valid ? SI(S, s, DVG_SHAPE_NUM_POINTS) : 1,
+                           valid ? SI(S, s, DVG_SHAPE_THICKNESS_OFF) : -1,
+                           valid ? __ldg(&S.segment_ctrl[jb.seg]) : 0, valid ? __ldg(&S.seg_point[jb.seg]) : 0,
+                           V2(jb.x, jb.y), jb.r, valid, true);  // all lanes: the decisions run in step
+    if (valid && f == 1) atomicOr(&q->result[owner], 1u << idx);
+    bool pending = valid && f == 2;
     unsigned bal = __ballot_sync(full, pending);
     if (pending) q->pend[npend + __popc(bal & ((1u << lane) - 1u))] = (unsigned char)j;
     npend += __popc(bal);
