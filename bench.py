@@ -288,6 +288,7 @@ def run_ours(args):
            'kernels_ms_per_launch': {k: round(v[1] / v[0], 4) for k, v in kernels.items()},
            'loss': float(loss_buf.item())}
     if rank == 0 and not args.no_batched:
+        out['configs'] = run_configs(dev)
         out['batched'] = run_batched(dev)
         out['served'] = run_served(dev)
     if rank == 0 and not args.no_cpu_baseline:
@@ -333,6 +334,72 @@ def run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samp
     return {'value': round(ws * n_samples * k / dt / 1e6, 3), 'unit': UNIT, 'h2d_bytes_per_step': h2d,
             'd2h_bytes_per_step': d2h, 'steps': k, 'ms_per_step': round(dt / k * 1e3, 3),
             'api': 'RenderFunction.serialize_scene + apply + MSE + backward, scene tensors in host memory'}
+
+
+def run_configs(dev, steps=5, warmup=3):
+    """Device-resident fwd+bwd Msamples/s of the other single-scene
+    configurations, through the C ABI like the headline leg: the single
+    circle (256x256, 2x2 spp; target: the circle at (120,140), radius 48,
+    colour (0.7,0.2,0.4,1)) and the fill-heavy prefiltered scene (1024x1024,
+    1 spp, 512 closed paths, seed 3; target: the same generator with seed 4).
+    L2 flushed between steps, CUDA events per step."""
+    import torch
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import _native, workloads
+    from diffvg_gb300.packing import pack_scene
+    cases = {
+        'circle_256_2x2': (workloads.circle_scene(dvg),
+                           workloads.circle_scene(dvg, center=(120.0, 140.0), radius=48.0,
+                                                  color=(0.7, 0.2, 0.4, 1.0)), (2, 2), 0, False),
+        'fill_prefiltered_1024_1x1': (workloads.fill_scene(dvg, seed=3), workloads.fill_scene(dvg, seed=4), (1, 1),
+                                      3, True),
+    }
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)
+    out = {}
+    for name, ((w, h, shapes, groups), (tw, th, ts, tg), (nsx, nsy), seed, pf) in cases.items():
+        packed = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=pf))
+        tpacked = pack_scene(dvg.RenderFunction.serialize_scene(tw, th, ts, tg, use_prefiltering=pf))
+        scene, tscene = _native.NativeScene(packed), _native.NativeScene(tpacked)
+        arena, tarena = packed.param_arena(dev).contiguous(), tpacked.param_arena(dev).contiguous()
+        target = torch.empty(h, w, 4, device=dev)
+        tscene.forward(_native.RenderArgs(w, h, nsx, nsy, seed, int(pf), 0, tarena.data_ptr(), None, None, 0),
+                       image_ptr=target.data_ptr(), stream=sptr)
+        img, d_img = torch.empty(h, w, 4, device=dev), torch.empty(h, w, 4, device=dev)
+        d_params = torch.zeros(max(packed.num_params, 1), device=dev)
+        fa = _native.RenderArgs(w, h, nsx, nsy, seed, int(pf), 0, arena.data_ptr(), None, None,
+                                _native.DVG_FLAG_NO_SYNC)
+        ba = _native.RenderArgs(w, h, nsx, nsy, seed, int(pf), 0, arena.data_ptr(), None, None,
+                                _native.DVG_FLAG_NO_SYNC | _native.DVG_FLAG_REUSE_PREP)
+        scale = 2.0 / img.numel()
+
+        def step():
+            scene.forward(fa, image_ptr=img.data_ptr(), stream=sptr)
+            torch.sub(img, target, out=d_img)
+            d_img.mul_(scale)
+            d_params.zero_()
+            scene.backward(ba, d_image_ptr=d_img.data_ptr(), d_params_ptr=d_params.data_ptr(), stream=sptr)
+
+        for _ in range(warmup):
+            step()
+        scene.sync(sptr)
+        torch.cuda.synchronize(dev)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i, (a, b) in enumerate(ev):
+            flush.fill_(float(i))
+            a.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        scene.sync(sptr)
+        ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+        n = w * h * nsx * nsy
+        out[name] = {'Msamples_per_s': round(n / (ms / 1e3) / 1e6, 3), 'ms_per_step': round(ms, 4),
+                     'samples_per_step': n, 'prefiltered': pf, 'steps': steps}
+        scene.close()
+        tscene.close()
+    return out
 
 
 def run_batched(dev, steps=10, warmup=3, plain_steps=2):
