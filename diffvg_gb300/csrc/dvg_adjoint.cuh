@@ -472,12 +472,13 @@ DN void accumulate_boundary_gradient(const DevScene &S, int g, int s, float cont
     }
   }
   if (kind == DVG_CIRCLE) {
-    gadd(dp, po + 1, normal.x * contrib); gadd(dp, po + 2, normal.y * contrib);
-    gadd(dp, po + 0, contrib);
+    const float d[3] = {contrib, normal.x * contrib, normal.y * contrib};
+    gadd_shared<3>(dp, po, d);
   } else if (kind == DVG_ELLIPSE) {
-    gadd(dp, po + 2, normal.x * contrib); gadd(dp, po + 3, normal.y * contrib);
-    gadd(dp, po + 0, (float)(dcos(2 * (float)DVG_PI * t) * normal.x * contrib));
-    gadd(dp, po + 1, (float)(dsin(2 * (float)DVG_PI * t) * normal.y * contrib));
+    const float d[4] = {(float)(dcos(2 * (float)DVG_PI * t) * normal.x * contrib),
+                        (float)(dsin(2 * (float)DVG_PI * t) * normal.y * contrib), normal.x * contrib,
+                        normal.y * contrib};
+    gadd_shared<4>(dp, po, d);
   } else if (kind == DVG_PATH) {
     int i0 = bd.point_id;
     float tt = bd.t;
@@ -519,6 +520,10 @@ DN void accumulate_boundary_gradient(const DevScene &S, int g, int s, float cont
 #pragma unroll
   for (int i = 0; i < 9; i++) s2c[i] = pget(S, xo + i);
   d_xform_pt(s2c, local_pt, scl2(contrib, normal), d_s2c, &d_local);
+  if (kind == DVG_PATH) {  // paths: samples spread over many shapes and groups
 #pragma unroll
-  for (int i = 0; i < 9; i++) gadd(dp, xo + i, d_s2c[i]);
+    for (int i = 0; i < 9; i++) gadd(dp, xo + i, d_s2c[i]);
+  } else {  // one circle, ellipse or rectangle takes every sample of its boundary
+    gadd_shared<9>(dp, xo, d_s2c);
+  }
 }

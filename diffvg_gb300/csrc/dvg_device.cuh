@@ -1428,13 +1428,45 @@ DN float4 paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt) {
 }
 
 DI void gadd(float *dp, int off, float v) { atomicAdd(dp + off, v); }
+// Accumulation of N consecutive parameters that every sample of a warp may
+// hit at once (a circle's, ellipse's or rectangle's parameters and its group
+// transform in the boundary pass): the lanes that add to the same block at
+// this point sum their values first and one of them adds the sums.  Where
+// the lanes' targets mostly differ (path points, paints) the plain atomics
+// are faster.
+template <int N>
+DI void gadd_shared(float *dp, int off, const float *v) {
+  unsigned peers = __match_any_sync(__activemask(), off);
+  if (__popc(peers) == 1) {
+#pragma unroll
+    for (int k = 0; k < N; k++) atomicAdd(dp + off + k, v[k]);
+    return;
+  }
+  float sum[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) sum[k] = 0.f;
+  for (unsigned m = peers; m; m &= m - 1u) {
+    int src = __ffs(m) - 1;
+#pragma unroll
+    for (int k = 0; k < N; k++) sum[k] += __shfl_sync(peers, v[k], src);
+  }
+  if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+#pragma unroll
+    for (int k = 0; k < N; k++) atomicAdd(dp + off + k, sum[k]);
+  }
+}
+DI void gadd4(float *dp, int off, float4 v) {
+  gadd(dp, off + 0, v.x);
+  gadd(dp, off + 1, v.y);
+  gadd(dp, off + 2, v.z);
+  gadd(dp, off + 3, v.w);
+}
 
 // d_sample_color (diffvg.cpp:370-504)
 DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, float4 d_color, float *dp,
                       float *d_translation) {
   if (kind == DVG_CONSTANT) {
-    gadd(dp, off + 0, d_color.x); gadd(dp, off + 1, d_color.y);
-    gadd(dp, off + 2, d_color.z); gadd(dp, off + 3, d_color.w);
+    gadd4(dp, off, d_color);
     return;
   }
   int oo = off + 4, co = off + 4 + nstops;
@@ -1450,7 +1482,7 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
     t = len2(no);
   }
   if (t < pget(S, oo)) {
-    gadd(dp, co + 0, d_color.x); gadd(dp, co + 1, d_color.y); gadd(dp, co + 2, d_color.z); gadd(dp, co + 3, d_color.w);
+    gadd4(dp, co, d_color);
     return;
   }
   for (int i = 0; i < nstops - 1; i++) {
@@ -1464,11 +1496,10 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
       float d_on = -d_tt * tt / (on - oc);
       float d_oc = d_tt * ((tt - 1.f) / (on - oc));
       float d_t = d_tt / (on - oc);
-      gadd(dp, co + 4 * i + 0, dcc.x); gadd(dp, co + 4 * i + 1, dcc.y);
-      gadd(dp, co + 4 * i + 2, dcc.z); gadd(dp, co + 4 * i + 3, dcc.w);
-      gadd(dp, co + 4 * (i + 1) + 0, dcn.x); gadd(dp, co + 4 * (i + 1) + 1, dcn.y);
-      gadd(dp, co + 4 * (i + 1) + 2, dcn.z); gadd(dp, co + 4 * (i + 1) + 3, dcn.w);
-      gadd(dp, oo + i, d_oc); gadd(dp, oo + i + 1, d_on);
+      gadd4(dp, co + 4 * i, dcc);
+      gadd4(dp, co + 4 * (i + 1), dcn);
+      gadd(dp, oo + i, d_oc);
+      gadd(dp, oo + i + 1, d_on);
       if (kind == DVG_LINEAR) {
         float l = rmax(dot2(sub2(end, beg), sub2(end, beg)), 1e-3f);
         v2 d_beg = div2s(scl2(d_t, sub2(neg2(sub2(pt, beg)), sub2(end, beg))), l);
@@ -1478,7 +1509,7 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
           d_beg = add2(d_beg, scl2(2 * d_l, sub2(beg, end)));
           d_end = add2(d_end, scl2(2 * d_l, sub2(end, beg)));
         }
-        gadd(dp, off + 0, d_beg.x); gadd(dp, off + 1, d_beg.y); gadd(dp, off + 2, d_end.x); gadd(dp, off + 3, d_end.y);
+        gadd4(dp, off, F4(d_beg.x, d_beg.y, d_end.x, d_end.y));
         if (d_translation) {
           atomicAdd(d_translation + 0, d_beg.x + d_end.x);
           atomicAdd(d_translation + 1, d_beg.y + d_end.y);
@@ -1491,7 +1522,7 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
         v2 d_off = V2(d_no.x / rad.x, d_no.y / rad.y);
         v2 d_rad = V2(-d_no.x * o2.x / (rad.x * rad.x), -d_no.y * o2.y / (rad.y * rad.y));
         v2 d_cen = neg2(d_off);
-        gadd(dp, off + 0, d_cen.x); gadd(dp, off + 1, d_cen.y); gadd(dp, off + 2, d_rad.x); gadd(dp, off + 3, d_rad.y);
+        gadd4(dp, off, F4(d_cen.x, d_cen.y, d_rad.x, d_rad.y));
         if (d_translation) {
           atomicAdd(d_translation + 0, d_cen.x);
           atomicAdd(d_translation + 1, d_cen.y);
@@ -1501,7 +1532,7 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
     }
   }
   int last = co + 4 * (nstops - 1);
-  gadd(dp, last + 0, d_color.x); gadd(dp, last + 1, d_color.y); gadd(dp, last + 2, d_color.z); gadd(dp, last + 3, d_color.w);
+  gadd4(dp, last, d_color);
 }
 
 // d_length / d_normalize (vector.h:496-503, 591-601)
