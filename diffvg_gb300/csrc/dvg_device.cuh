@@ -218,67 +218,78 @@ DI Pcg pcg_init(int32_t idx, uint64_t seed) {
 
 // ---------------------------------------------------------------------------
 // root solvers (solve.h:5-59)
+// IEEE divisions out of line for the rarely run solver paths (each inline
+// division expands to ~100 instructions without fused multiply-add)
+DN float fdiv(float a, float b) { return a / b; }
+DN double ddiv(double a, double b) { return a / b; }
+DN double dsqrt(double a) { return sqrt(a); }
+
 DI bool solve_quadratic_f(float a, float b, float c, float *t0, float *t1) {
   float discrim = b * b - 4 * a * c;
   if (discrim < 0) return false;
   float root = sqrtf(discrim);
   float q = (b < 0) ? -0.5f * (b - root) : -0.5f * (b + root);
-  *t0 = q / a;
-  *t1 = c / q;
+  *t0 = fdiv(q, a);
+  *t1 = fdiv(c, q);
   if (*t0 > *t1) { float tmp = *t0; *t0 = *t1; *t1 = tmp; }
   return true;
 }
 DI bool solve_quadratic_d(double a, double b, double c, double *t0, double *t1) {
   double discrim = b * b - 4 * a * c;
   if (discrim < 0) return false;
-  double root = sqrt(discrim);
+  double root = dsqrt(discrim);
   double q = (b < 0) ? -0.5f * (b - root) : -0.5f * (b + root);
-  *t0 = q / a;
-  *t1 = c / q;
+  *t0 = ddiv(q, a);
+  *t1 = ddiv(c, q);
   if (*t0 > *t1) { double tmp = *t0; *t0 = *t1; *t1 = tmp; }
   return true;
 }
+// solve_cubic<double> (solve.h:24-58).  The three trigonometric roots share
+// one cos call (theta + 0 = theta for theta = acos(.) >= 0), and the one-root
+// branch's two pow calls one (R + s for R > 0, -R + s otherwise, is |R| + s).
 DN int solve_cubic_d(double a, double b, double c, double d, double t[3]) {
   if (fabs(a) < 1e-6f) return solve_quadratic_d(b, c, d, &t[0], &t[1]) ? 2 : 0;
-  b /= a; c /= a; d /= a;
-  double Q = (b * b - 3 * c) / 9.f;
-  double R = (2 * b * b * b - 9 * b * c + 27 * d) / 54.f;
+  b = ddiv(b, a); c = ddiv(c, a); d = ddiv(d, a);
+  double Q = ddiv(b * b - 3 * c, 9.f);
+  double R = ddiv(2 * b * b * b - 9 * b * c + 27 * d, 54.f);
   if (R * R < Q * Q * Q) {
-    double theta = acos(R / sqrt(Q * Q * Q));
-    double sQ = sqrt(Q);
-    t[0] = -2.f * sQ * cos(theta / 3.f) - b / 3.f;
-    t[1] = -2.f * sQ * cos((theta + 2.f * DVG_PI) / 3.f) - b / 3.f;
-    t[2] = -2.f * sQ * cos((theta - 2.f * DVG_PI) / 3.f) - b / 3.f;
+    double theta = acos(ddiv(R, dsqrt(Q * Q * Q)));
+    double sQ = dsqrt(Q);
+    double b3 = ddiv(b, 3.f);
+    const double off[3] = {0.0, 2.f * DVG_PI, -(2.f * DVG_PI)};
+    #pragma unroll 1
+    for (int k = 0; k < 3; k++) t[k] = -2.f * sQ * cos(ddiv(theta + off[k], 3.f)) - b3;
     return 3;
   } else {
-    double A = R > 0 ? -pow(R + sqrt(R * R - Q * Q * Q), (double)(1. / 3.))
-                     : pow(-R + sqrt(R * R - Q * Q * Q), (double)(1. / 3.));
-    double B = fabs(A) > 1e-6f ? Q / A : 0.0;
-    t[0] = (A + B) - b / 3.0;
+    double pw = pow(fabs(R) + dsqrt(R * R - Q * Q * Q), (double)(1. / 3.));
+    double A = R > 0 ? -pw : pw;
+    double B = fabs(A) > 1e-6f ? ddiv(Q, A) : 0.0;
+    t[0] = (A + B) - ddiv(b, 3.0);
     return 1;
   }
 }
 // solve_cubic<float>: the reference's unqualified sqrt/acos/cos/pow bind to
 // the double-precision functions, so intermediates are double until stored
 // back into a float.
-DI int solve_cubic_f(float a, float b, float c, float d, float t[3]) {
+DN int solve_cubic_f(float a, float b, float c, float d, float t[3]) {
   if (fabsf(a) < 1e-6f) return solve_quadratic_f(b, c, d, &t[0], &t[1]) ? 2 : 0;
-  b /= a; c /= a; d /= a;
-  float Q = (b * b - 3 * c) / 9.f;
-  float R = (2 * b * b * b - 9 * b * c + 27 * d) / 54.f;
+  b = fdiv(b, a); c = fdiv(c, a); d = fdiv(d, a);
+  float Q = fdiv(b * b - 3 * c, 9.f);
+  float R = fdiv(2 * b * b * b - 9 * b * c + 27 * d, 54.f);
   if (R * R < Q * Q * Q) {
-    float theta = (float)acos((double)R / sqrt((double)(Q * Q * Q)));
-    double sQ = sqrt((double)Q);
-    t[0] = (float)(-2.f * sQ * cos((double)(theta / 3.f)) - (double)(b / 3.f));
-    t[1] = (float)(-2.f * sQ * cos((double)((theta + 2.f * (float)DVG_PI) / 3.f)) - (double)(b / 3.f));
-    t[2] = (float)(-2.f * sQ * cos((double)((theta - 2.f * (float)DVG_PI) / 3.f)) - (double)(b / 3.f));
+    float theta = (float)acos(ddiv((double)R, dsqrt((double)(Q * Q * Q))));
+    double sQ = dsqrt((double)Q);
+    double b3 = (double)fdiv(b, 3.f);
+    const float off[3] = {0.f, 2.f * (float)DVG_PI, -(2.f * (float)DVG_PI)};
+    #pragma unroll 1
+    for (int k = 0; k < 3; k++) t[k] = (float)(-2.f * sQ * cos((double)fdiv(theta + off[k], 3.f)) - b3);
     return 3;
   } else {
     double third = (double)(float)(1. / 3.);
-    float A = R > 0 ? (float)(-pow((double)R + sqrt((double)(R * R - Q * Q * Q)), third))
-                    : (float)pow((double)(-R) + sqrt((double)(R * R - Q * Q * Q)), third);
-    float B = fabsf(A) > 1e-6f ? Q / A : 0.f;
-    t[0] = (A + B) - b / 3.f;
+    double pw = pow((double)fabsf(R) + dsqrt((double)(R * R - Q * Q * Q)), third);
+    float A = R > 0 ? (float)(-pw) : (float)pw;
+    float B = fabsf(A) > 1e-6f ? fdiv(Q, A) : 0.f;
+    t[0] = (A + B) - fdiv(b, 3.f);
     return 1;
   }
 }
