@@ -91,7 +91,7 @@ struct DvgScene {
   // hit keys and counts, a copy of its parameters and the stale flag the
   // backward sets when its parameters differ
   DevBuf hits;
-  bool hit_live = false;
+  bool hit_live = false, hit_pf = false;
   int hit_w = 0, hit_h = 0, hit_nsx = 0, hit_nsy = 0;
   uint64_t hit_seed = 0;
   unsigned *h_status = nullptr;  // pinned mirror of err[0..1]
@@ -362,14 +362,17 @@ int prepare(DvgScene *sc, const DevScene &S, const DvgRenderArgs *a, cudaStream_
 
 struct HitArena { int *keys; unsigned char *cnt; float *params; unsigned *stale; };
 
-size_t hit_bytes(DvgScene *sc, size_t n) {
-  return carve_size({DVG_HIT_SLOTS * n * sizeof(int), n, (size_t)sc->d.num_params * sizeof(float), sizeof(unsigned)});
+// per sample: DVG_HIT_SLOTS fragment keys, or with prefiltering DVG_PF_SLOTS whole fragments
+size_t hit_slot_bytes(bool prefilter) { return prefilter ? DVG_PF_SLOTS * DVG_PF_BYTES : DVG_HIT_SLOTS * sizeof(int); }
+
+size_t hit_bytes(DvgScene *sc, size_t n, bool prefilter) {
+  return carve_size({hit_slot_bytes(prefilter) * n, n, (size_t)sc->d.num_params * sizeof(float), sizeof(unsigned)});
 }
 
-HitArena hit_arena(DvgScene *sc, size_t n) {
+HitArena hit_arena(DvgScene *sc, size_t n, bool prefilter) {
   char *p = reinterpret_cast<char *>(sc->hits.ptr);
   HitArena h;
-  h.keys = carve<int>(p, DVG_HIT_SLOTS * n);
+  h.keys = carve<int>(p, hit_slot_bytes(prefilter) * n / sizeof(int));
   h.cnt = carve<unsigned char>(p, n);
   h.params = carve<float>(p, sc->d.num_params);
   h.stale = carve<unsigned>(p, 1);
@@ -377,8 +380,9 @@ HitArena hit_arena(DvgScene *sc, size_t n) {
 }
 
 bool hit_matches(const DvgScene *sc, const DvgRenderArgs *a) {
-  return sc->hit_live && sc->hit_w == a->width && sc->hit_h == a->height && sc->hit_nsx == a->num_samples_x &&
-         sc->hit_nsy == a->num_samples_y && sc->hit_seed == a->seed;
+  return sc->hit_live && sc->hit_pf == (a->use_prefiltering != 0) && sc->hit_w == a->width &&
+         sc->hit_h == a->height && sc->hit_nsx == a->num_samples_x && sc->hit_nsy == a->num_samples_y &&
+         sc->hit_seed == a->seed;
 }
 
 size_t edge_bytes(DvgScene *sc, size_t n) {
@@ -643,10 +647,11 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   size_t npx = (size_t)a->width * a->height, n = npx * a->num_samples_x * a->num_samples_y;
   sc->hit_live = false;
-  bool cache = image && !a->use_prefiltering;
+  bool cache = image != nullptr;
+  bool pf = a->use_prefiltering != 0;
   cudaError_t e = sc->weight.ensure(npx * sizeof(float));
   if (e == cudaSuccess && image) e = sc->samples.ensure(n * sizeof(float4));
-  if (e == cudaSuccess && cache) e = sc->hits.ensure(hit_bytes(sc, n));
+  if (e == cudaSuccess && cache) e = sc->hits.ensure(hit_bytes(sc, n, pf));
   if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
   if (sc->d.num_groups == 0 && image) {
     // empty scene: the background (or transparent black), unfiltered
@@ -663,8 +668,9 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
       float4 *samples = reinterpret_cast<float4 *>(sc->samples.ptr);
       HitArena h{};
       if (cache) {
-        h = hit_arena(sc, n);
-        R.hit_keys = h.keys;
+        h = hit_arena(sc, n, pf);
+        if (pf) R.pf_frags = h.keys;
+        else R.hit_keys = h.keys;
         R.hit_cnt = h.cnt;
       }
       timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
@@ -675,6 +681,7 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
         e = cudaMemcpyAsync(h.params, a->params, (size_t)sc->d.num_params * sizeof(float), cudaMemcpyDeviceToDevice, s);
       if (e == cudaSuccess && cache) {
         sc->hit_live = true;
+        sc->hit_pf = pf;
         sc->hit_w = a->width;
         sc->hit_h = a->height;
         sc->hit_nsx = a->num_samples_x;
@@ -733,12 +740,14 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
       R.d_background = d_background;
       float4 *dbg_val = reinterpret_cast<float4 *>(sc->dbg_val.ptr);
       int *dbg_flag = reinterpret_cast<int *>(sc->dbg_flag.ptr);
-      if (!a->use_prefiltering && hit_matches(sc, a)) {
-        HitArena h = hit_arena(sc, n);
+      if (hit_matches(sc, a)) {
+        bool pf = a->use_prefiltering != 0;
+        HitArena h = hit_arena(sc, n, pf);
         e = cudaMemsetAsync(h.stale, 0, sizeof(unsigned), s);
         if (e != cudaSuccess) return cuda_fail(e, "backward launch");
         if (sc->d.num_params > 0) dvg::launch_hit_check(a->params, h.params, sc->d.num_params, h.stale, s);
-        R.hit_keys = h.keys;
+        if (pf) R.pf_frags = h.keys;
+        else R.hit_keys = h.keys;
         R.hit_cnt = h.cnt;
         R.hit_stale = h.stale;
       }

@@ -89,11 +89,14 @@ struct DevRender {
   // parameters: the keys of each sample's hit fragments in blend order
   // ([DVG_HIT_SLOTS][samples]) and their count (DVG_HIT_NONE: not cached)
   int *hit_keys = nullptr;
+  void *pf_frags = nullptr;  // prefiltered: [DVG_PF_SLOTS][samples] fragments instead of keys
   unsigned char *hit_cnt = nullptr;
   const unsigned *hit_stale = nullptr;  // backward: nonzero when the parameters differ from the forward's
 };
 #define DVG_HIT_SLOTS 8
 #define DVG_HIT_NONE 255
+#define DVG_PF_SLOTS 12   // prefiltered fragments cached per sample
+#define DVG_PF_BYTES 64   // bytes per cached prefiltered fragment
 
 // Boundary samples filed by canvas tile (edge-sampling pass), n entries
 // each; tile_count / tile_start have one entry per canvas tile (+1).

@@ -77,7 +77,13 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   v2 npt = V2(pt.x / R.w, pt.y / R.h);
   const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
   float4 c;
-  if (PREFILTER) c = sample_color_prefiltered_fwd(S, bg, npt);
+  if (PREFILTER) {
+    int n = R.w * R.h * R.spp;
+    bool cache = R.pf_frags && !bins_overflowed(S);
+    if (R.hit_cnt && !cache) R.hit_cnt[idx] = DVG_HIT_NONE;
+    c = sample_color_prefiltered_fwd(S, bg, npt, cache ? static_cast<PFrag *>(R.pf_frags) : nullptr,
+                                     cache ? R.hit_cnt : nullptr, n, idx);
+  }
   else {
     int n = R.w * R.h * R.spp;
     bool cache = R.hit_keys && !bins_overflowed(S);
@@ -148,7 +154,14 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   float4 *dbgp = R.d_background ? &dbg : nullptr;
   float4 color;
   if (PREFILTER) {
-    color = active ? sample_color_prefiltered_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params)
+    int cached = -1;
+    if (active && R.pf_frags && R.hit_cnt && *R.hit_stale == 0u) {
+      int c = R.hit_cnt[idx];
+      if (c != DVG_HIT_NONE) cached = c;
+    }
+    color = active ? sample_color_prefiltered_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params,
+                                                  static_cast<const PFrag *>(R.pf_frags), R.w * R.h * R.spp, idx,
+                                                  cached)
                    : F4(0, 0, 0, 0);
   } else {
     int cached = -1;

@@ -414,6 +414,7 @@ struct PFrag {
   PathInfo info;
   int within;
 };
+static_assert(sizeof(PFrag) <= DVG_PF_BYTES, "prefiltered fragment cache entries");
 
 // Coverage fragments of one group at pt (diffvg.cpp:851-905).  Returns the
 // number of fragments written (0..2).
@@ -461,7 +462,10 @@ DI int prefilter_group(const DevScene &S, int g, v2 pt, PFrag *out) {
 }
 
 // sample_color_prefiltered, forward only (diffvg.cpp:835-960)
-DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 screen_pt) {
+// With cache set, the sample's fragments (blend order) and their count are
+// stored for the backward pass (sample idx of n).
+DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, PFrag *cache = nullptr,
+                                       unsigned char *cache_cnt = nullptr, int n = 0, int idx = 0) {
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   int b, e;
   bool list = cand_range(S, pt, b, e);
@@ -472,17 +476,25 @@ DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 s
     int g = list ? __ldg(&S.tile_list[k]) : k;
     if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
     PFrag fr[2];
-    int n = prefilter_group(S, g, pt, fr);
-    for (int j = 0; j < n; j++) { blend(acc, fr[j].c); nf++; }
+    int m = prefilter_group(S, g, pt, fr);
+    for (int j = 0; j < m; j++) {
+      blend(acc, fr[j].c);
+      if (cache && nf < DVG_PF_SLOTS) cache[(size_t)nf * n + idx] = fr[j];
+      nf++;
+    }
   }
+  if (cache_cnt) cache_cnt[idx] = nf > DVG_PF_SLOTS ? DVG_HIT_NONE : (unsigned char)nf;
   if (nf > DVG_MAX_PREFILTER_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
   if (nf <= 0) return bg ? *bg : F4(0, 0, 0, 0);
   return finish_color(acc);
 }
 
 // Adjoint of sample_color_prefiltered (diffvg.cpp:960-1113)
+// cached >= 0: the forward pass's fragments of this sample (cached of them,
+// in cache) stand in for computing them again.
 DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color,
-                                       float4 *d_bg, int *assign, float *d_tr, float *dp) {
+                                       float4 *d_bg, int *assign, float *d_tr, float *dp,
+                                       const PFrag *cache = nullptr, int n = 0, int idx = 0, int cached = -1) {
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   int b, e;
   bool list = cand_range(S, pt, b, e);
@@ -493,6 +505,15 @@ DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 s
   int nf = 0;
   bool overflow = false;
   int G = S.num_groups;
+  if (cached >= 0) {
+    for (int j = 0; j < cached; j++) {
+      frags[j] = cache[(size_t)j * n + idx];
+      blend(acc, frags[j].c);
+      accs[j] = acc;
+    }
+    nf = cached;
+    e = b;  // the walk below has nothing left to do
+  }
   for (int k = b; k < e; k++) {
     int g = list ? __ldg(&S.tile_list[k]) : k;
     if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;

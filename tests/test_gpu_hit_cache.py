@@ -74,3 +74,31 @@ def test_other_seed_does_not_use_the_cache():
     nu.render(packed, P, w, h, 2, 2, 7, scene=sc)
     after_other = nu.render(packed, P, w, h, 2, 2, 9, d_out=d, scene=sc)['d_params']
     assert _rel(after_other, fresh) <= TOL
+
+
+def _fill_scene(prefilter):
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import workloads
+    from diffvg_gb300.packing import pack_scene
+    w, h, shapes, groups = workloads.fill_scene(dvg, seed=3, num_paths=40, canvas=192)
+    return w, h, pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=prefilter))
+
+
+def test_prefiltered_cache_matches_fresh_and_goes_stale():
+    import native_util as nu
+    from diffvg_gb300 import _native
+    w, h, packed = _fill_scene(True)
+    P0 = _params(packed)
+    P1 = P0.copy()
+    P1 += np.random.default_rng(1).normal(0, 0.75, P1.shape).astype(np.float32) * (np.abs(P0) > 1.0)
+    d = _d_img(h, w)
+    fresh0 = nu.render(packed, P0, w, h, 1, 1, 3, d_out=d)['d_params']
+    fresh1 = nu.render(packed, P1, w, h, 1, 1, 3, d_out=d)['d_params']
+    sc = _native.NativeScene(packed)
+    nu.render(packed, P0, w, h, 1, 1, 3, scene=sc)
+    cached = nu.render(packed, P0, w, h, 1, 1, 3, d_out=d, scene=sc)['d_params']
+    nu.render(packed, P0, w, h, 1, 1, 3, scene=sc)
+    after_other = nu.render(packed, P1, w, h, 1, 1, 3, d_out=d, scene=sc)['d_params']
+    assert _rel(cached, fresh0) <= TOL
+    assert _rel(fresh0, fresh1) > 100 * TOL
+    assert _rel(after_other, fresh1) <= TOL
