@@ -4,9 +4,10 @@ Drop-in for pydiffvg.RenderFunction (reference: pydiffvg/render_pytorch.py):
 ``serialize_scene`` builds the same flat argument list, ``apply`` takes
 ``(width, height, num_samples_x, num_samples_y, seed, background_image,
 *args)`` and returns the ``[H, W, 4]`` image (or the ``[H, W, 1]`` /
-``[N, 1]`` signed distance), ``backward`` returns one gradient per argument
-(None where the reference returns None) and ``render_grad`` returns the
-``[H, W, 2]`` translation gradient image.
+``[N, 1]`` signed distance), autograd delivers a gradient to every argument
+tensor that requires grad (the reference's backward returns None for the
+non-differentiable ones) and ``render_grad`` returns the ``[H, W, 2]``
+translation gradient image.
 
 Differences from the reference that a caller can observe:
   * tensors keep their device: serialize_scene does not copy them to the
@@ -122,7 +123,7 @@ def _eval_positions(packed, device):
     return ev.to(device=device, dtype=torch.float32).reshape(-1, 2).contiguous()
 
 
-class RenderFunction(torch.autograd.Function):
+class RenderFunction:
     """The PyTorch interface of the renderer (render_pytorch.py:18-868)."""
 
     @staticmethod
@@ -188,101 +189,17 @@ class RenderFunction(torch.autograd.Function):
         return args
 
     @staticmethod
-    def forward(ctx, width, height, num_samples_x, num_samples_y, seed, background_image, *args):
-        device = _render_device()
+    def apply(width, height, num_samples_x, num_samples_y, seed, background_image, *args):
+        """Renders the serialized scene; differentiable with respect to every
+        tensor of ``args`` (and ``background_image``) that requires grad.
+        Autograd sees only those tensors, so a step over thousands of shapes
+        does not pay per-argument bookkeeping for the rest of the list."""
         packed = pack_scene_cached(args)
-        scene = _native_scene(packed, device)
-        arena = packed.param_arena(device).contiguous()
-        ev = _eval_positions(packed, device)
-        if packed.output_type == OutputType.color:
-            assert ev is None, 'eval_positions apply to the sdf output only'
-            out = torch.empty(height, width, 4, device=device)
-        else:
-            out = torch.empty((height, width, 1) if ev is None else (ev.shape[0], 1), device=device)
-        bg = _background(background_image, out.shape[0], out.shape[1], device)
-        if not bool(torch.isfinite(arena).all()):
-            raise ValueError('scene parameters contain a non-finite value')
-        token = next(_token)
-        rargs = _render_args(packed, width, height, num_samples_x, num_samples_y, seed, arena, bg, ev)
-        stream = torch.cuda.current_stream(device).cuda_stream
-        with torch.cuda.device(device):
-            if packed.output_type == OutputType.color:
-                scene.forward(rargs, image_ptr=out.data_ptr(), stream=stream)
-            else:
-                scene.forward(rargs, sdf_ptr=out.data_ptr(), stream=stream)
-        scene.last_token = token
-        ctx.packed = packed
-        ctx.scene = scene
-        ctx.arena = arena
-        ctx.token = token
-        ctx.background_image = bg
-        ctx.bg_requested = background_image is not None
-        ctx.eval_positions = ev
-        ctx.dims = (width, height, num_samples_x, num_samples_y, seed)
-        ctx.device = device
-        ctx.num_args = len(args)
-        return out
-
-    @staticmethod
-    def backward(ctx, grad_img):
-        packed, scene, device = ctx.packed, ctx.scene, ctx.device
-        width, height, nsx, nsy, seed = ctx.dims
-        grad = grad_img.to(device=device, dtype=torch.float32).contiguous()
-        d_arena = torch.zeros(max(packed.num_params, 1), device=device)
-        bg = ctx.background_image
-        d_bg = torch.zeros_like(bg) if bg is not None else None
-        reuse = _native.DVG_FLAG_REUSE_PREP if scene.last_token == ctx.token else 0
-        stream = torch.cuda.current_stream(device).cuda_stream
-
-        def launch(flags):
-            rargs = _render_args(packed, width, height, nsx, nsy, seed, ctx.arena, bg, ctx.eval_positions, flags)
-            with torch.cuda.device(device):
-                if packed.output_type == OutputType.color:
-                    scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
-                                   d_background_ptr=None if d_bg is None else d_bg.data_ptr(), stream=stream)
-                else:
-                    scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(), stream=stream)
-
-        # the kernels run while the host lays out the gradient views; the
-        # status is checked once the gradient has been read back
-        launch(reuse | _native.DVG_FLAG_NO_SYNC)
-        scene.last_token = ctx.token
-        slots = packed.slots
-        dst_of = [t.device if isinstance(t, torch.Tensor) else device for t in packed.tensors]
-        bufs = {device: d_arena}
-        for dst in set(dst_of):
-            if dst != device:
-                bufs[dst] = torch.empty(d_arena.shape, dtype=torch.float32, device=dst)
-        sizes = [sl.numel for sl in slots]
-        parts = {dst: torch.split(b[:sum(sizes)], sizes) for dst, b in bufs.items()}
-        d_args = [None] * ctx.num_args
-        for k, (slot, t) in enumerate(zip(slots, packed.tensors)):
-            if not slot.differentiable:
-                continue
-            g = parts[dst_of[k]][k]
-            if len(slot.shape) != 1:
-                g = g.view(slot.shape)
-            if isinstance(t, torch.Tensor) and t.dtype != g.dtype:
-                g = g.to(t.dtype)
-            d_args[slot.arg_index] = g
-        for dst, b in bufs.items():
-            if dst != device:
-                b.copy_(d_arena)  # waits for the kernels
-        try:
-            scene.sync(stream)
-        except _native.SceneCapacityError as e:
-            if 'grown' not in str(e):
-                raise
-            # the tile lists outgrew their capacity and were grown: the
-            # gradient is computed again, synchronously
-            d_arena.zero_()
-            if d_bg is not None:
-                d_bg.zero_()
-            launch(0)
-            for dst, b in bufs.items():
-                if dst != device:
-                    b.copy_(d_arena)
-        return (None, None, None, None, None, d_bg if ctx.bg_requested else None) + tuple(d_args)
+        T = torch.Tensor
+        grad_slots = [k for k, (sl, t) in enumerate(zip(packed.slots, packed.tensors))
+                      if sl.differentiable and isinstance(t, T) and t.requires_grad]
+        call = _RenderCall((width, height, num_samples_x, num_samples_y, seed), packed, grad_slots)
+        return _RenderCore.apply(call, background_image, *[packed.tensors[k] for k in grad_slots])
 
     @staticmethod
     def render_grad(grad_img, width, height, num_samples_x, num_samples_y, seed, background_image, *args):
@@ -313,3 +230,116 @@ class RenderFunction(torch.autograd.Function):
                                d_translation_ptr=d_translation.data_ptr(), stream=stream)
         scene.last_token = None
         return d_translation
+
+
+class _RenderCall:
+    """What one RenderFunction.apply call renders: image size, sample
+    counts, seed, the packed scene and the slots whose tensors autograd
+    tracks."""
+    __slots__ = ('dims', 'packed', 'grad_slots')
+
+    def __init__(self, dims, packed, grad_slots):
+        self.dims, self.packed, self.grad_slots = dims, packed, grad_slots
+
+
+class _RenderCore(torch.autograd.Function):
+    """Forward and backward of one render (render_pytorch.py:186-428 and
+    668-868): inputs are the tensors that require grad, in slot order."""
+
+    @staticmethod
+    def forward(ctx, call, background_image, *grad_tensors):
+        width, height, num_samples_x, num_samples_y, seed = call.dims
+        packed = call.packed
+        device = _render_device()
+        scene = _native_scene(packed, device)
+        arena = packed.param_arena(device).contiguous()
+        ev = _eval_positions(packed, device)
+        if packed.output_type == OutputType.color:
+            assert ev is None, 'eval_positions apply to the sdf output only'
+            out = torch.empty(height, width, 4, device=device)
+        else:
+            out = torch.empty((height, width, 1) if ev is None else (ev.shape[0], 1), device=device)
+        bg = _background(background_image, out.shape[0], out.shape[1], device)
+        if not bool(torch.isfinite(arena).all()):
+            raise ValueError('scene parameters contain a non-finite value')
+        token = next(_token)
+        rargs = _render_args(packed, width, height, num_samples_x, num_samples_y, seed, arena, bg, ev)
+        stream = torch.cuda.current_stream(device).cuda_stream
+        with torch.cuda.device(device):
+            if packed.output_type == OutputType.color:
+                scene.forward(rargs, image_ptr=out.data_ptr(), stream=stream)
+            else:
+                scene.forward(rargs, sdf_ptr=out.data_ptr(), stream=stream)
+        scene.last_token = token
+        ctx.packed = packed
+        ctx.scene = scene
+        ctx.arena = arena
+        ctx.token = token
+        ctx.background_image = bg
+        ctx.bg_requested = background_image is not None
+        ctx.eval_positions = ev
+        ctx.dims = call.dims
+        ctx.device = device
+        ctx.grad_slots = call.grad_slots
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_img):
+        packed, scene, device = ctx.packed, ctx.scene, ctx.device
+        width, height, nsx, nsy, seed = ctx.dims
+        grad = grad_img.to(device=device, dtype=torch.float32).contiguous()
+        d_arena = torch.zeros(max(packed.num_params, 1), device=device)
+        bg = ctx.background_image
+        d_bg = torch.zeros_like(bg) if bg is not None else None
+        reuse = _native.DVG_FLAG_REUSE_PREP if scene.last_token == ctx.token else 0
+        stream = torch.cuda.current_stream(device).cuda_stream
+
+        def launch(flags):
+            rargs = _render_args(packed, width, height, nsx, nsy, seed, ctx.arena, bg, ctx.eval_positions, flags)
+            with torch.cuda.device(device):
+                if packed.output_type == OutputType.color:
+                    scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
+                                   d_background_ptr=None if d_bg is None else d_bg.data_ptr(), stream=stream)
+                else:
+                    scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(), stream=stream)
+
+        # the kernels run while the host lays out the gradient views; the
+        # status is checked once the gradient has been read back
+        launch(reuse | _native.DVG_FLAG_NO_SYNC)
+        scene.last_token = ctx.token
+        slots, tensors = packed.slots, packed.tensors
+        ks = ctx.grad_slots
+        dst_of = [tensors[k].device for k in ks]
+        bufs = {device: d_arena}
+        for dst in set(dst_of):
+            if dst != device:
+                bufs[dst] = torch.empty(d_arena.shape, dtype=torch.float32, device=dst)
+        sizes = [sl.numel for sl in slots]
+        parts = {dst: torch.split(bufs[dst][:sum(sizes)], sizes) for dst in set(dst_of)}
+        grads = []
+        for k, dst in zip(ks, dst_of):
+            slot, t = slots[k], tensors[k]
+            g = parts[dst][k]
+            if len(slot.shape) != 1:
+                g = g.view(slot.shape)
+            if t.dtype != g.dtype:
+                g = g.to(t.dtype)
+            grads.append(g)
+        for dst, b in bufs.items():
+            if dst != device:
+                b.copy_(d_arena)  # waits for the kernels
+        try:
+            scene.sync(stream)
+        except _native.SceneCapacityError as e:
+            if 'grown' not in str(e):
+                raise
+            # the tile lists outgrew their capacity and were grown: the
+            # gradient is computed again, synchronously
+            d_arena.zero_()
+            if d_bg is not None:
+                d_bg.zero_()
+            launch(0)
+            for dst, b in bufs.items():
+                if dst != device:
+                    b.copy_(d_arena)
+        return (None, d_bg if ctx.bg_requested else None) + tuple(grads)
