@@ -54,6 +54,21 @@ def _dist():
     return ws, rank, local
 
 
+def aggregate_throughput(total_ms, n_samples, steps, ws, device=None):
+    """Whole-job Msamples/s of replicas: every rank rendered n_samples per
+    step for `steps` steps, and the job took as long as the slowest rank
+    (max over ranks; the caller's process group: NCCL on the GPUs, gloo in
+    the CPU tests).  Returns (value, max total_ms)."""
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    return ws * n_samples * steps / (total_ms / 1e3) / 1e6, total_ms
+
+
 def _workload_config():
     return {'workload': 'stroke-heavy plain method: 512x512 canvas, 2x2 spp, box r=0.5, 2048 open cubic paths '
                         '(4 segments, 13 points), stroke half-width U[1,4], seed 1; MSE vs seed-2 target',
@@ -251,13 +266,7 @@ def run_ours(args):
     kernels = scene.profile_read()
     scene.profile(False)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(sum(step_ms))
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        dist.barrier()
-    value = ws * n_samples * args.steps / (total_ms / 1e3) / 1e6
+    value, total_ms = aggregate_throughput(float(sum(step_ms)), n_samples, args.steps, ws, dev)
     gpu_launches = 0
     for name, (cnt, _) in kernels.items():
         gpu_launches += cnt * (PREP_KERNELS if name == 'prepare' else 1)
