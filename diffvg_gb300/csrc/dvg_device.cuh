@@ -557,7 +557,7 @@ DI Quintic cubic_quintic(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
   q.D = (double)(3 * (sum2(mul2(b, c)) + sum2(mul2(a, e))));
   q.E = (double)(sum2(mul2(c, c)) + 2 * sum2(mul2(e, b)));
   q.F = (double)(sum2(mul2(e, c)));
-  q.B /= q.A; q.C /= q.A; q.D /= q.A; q.E /= q.A; q.F /= q.A;
+  q.B = ddiv(q.B, q.A); q.C = ddiv(q.C, q.A); q.D = ddiv(q.D, q.A); q.E = ddiv(q.E, q.A); q.F = ddiv(q.F, q.A);
   return q;
 }
 DI double quintic_eval(const Quintic &q, double t) {
@@ -572,8 +572,8 @@ DI int quintic_intervals(const Quintic &q, float iv[4]) {
   double p1A = (2 / 5.f) * q.C - (4 / 25.f) * q.B * q.B;
   double p1B = (3 / 5.f) * q.D - (3 / 25.f) * q.B * q.C;
   double p1C = (4 / 5.f) * q.E - (2 / 25.f) * q.B * q.D;
-  double p1D = q.F - q.B * q.E / 25.f;
-  double q_root = -q.B / 5.f;
+  double p1D = q.F - ddiv(q.B * q.E, 25.f);
+  double q_root = ddiv(-q.B, 5.f);
   double pr[3];
   int ns = solve_cubic_d(p1A, p1B, p1C, p1D, pr);
   iv[0] = (q_root >= 0 && q_root <= 1) ? (float)q_root : -1.0f;
@@ -598,7 +598,7 @@ DI float quintic_root(const Quintic &q, float lb, float ub) {
     if (value > 0.f) ub = t; else lb = t;
     if (lb > ub) continue;  // the next iteration restarts from the midpoint
     double derivative = quintic_deriv(q, t);
-    t = (float)(t - value / derivative);
+    t = (float)(t - ddiv(value, derivative));
   }
   return t;
 }
