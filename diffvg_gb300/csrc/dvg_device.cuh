@@ -796,6 +796,8 @@ DI void emu_blossom4(const float b[5], float l, float u, float c[5]) {
 // (the sign change at root +- rad is certain); false when a stationary
 // point or an end sits within del of zero, or an enclosure fails
 DI bool emu_cubic_roots3(float c3, float c2, float c1, float c0, float del, float root[3], float rad[3], bool has[3]) {
+  // stationary points (their rounding is covered by the end checks below: a
+  // piece's end within del of zero makes the result uncertain)
   float qa = 3 * c3, qb = 2 * c2, qc = c1, e0 = -1.f, e1 = -1.f;
   float sc = fabsf(qa) + fabsf(qb) + fabsf(qc);
   if (fabsf(qa) > 1e-7f * sc) {
@@ -803,27 +805,27 @@ DI bool emu_cubic_roots3(float c3, float c2, float c1, float c0, float del, floa
     if (disc >= 0.f) {
       float s = sqrtf(disc);
       float q = qb < 0 ? -0.5f * (qb - s) : -0.5f * (qb + s);
-      e0 = q / qa;
-      e1 = q != 0.f ? qc / q : -1.f;
+      e0 = __fdividef(q, qa);
+      e1 = q != 0.f ? __fdividef(qc, q) : -1.f;
     }
   } else if (fabsf(qb) > 1e-7f * sc) {
-    e0 = -qc / qb;
+    e0 = __fdividef(-qc, qb);
   }
   if (e0 > e1) { float tmp = e0; e0 = e1; e1 = tmp; }
   bool h0 = e0 > 0.f && e0 < 1.f, h1 = e1 > 0.f && e1 < 1.f && e1 != e0;
-  float ts[4] = {0.f, h0 ? e0 : (h1 ? e1 : 1.f), (h0 && h1) ? e1 : 1.f, 1.f};
+  float t1 = h0 ? e0 : (h1 ? e1 : 1.f), t2 = (h0 && h1) ? e1 : 1.f;
+  float rr[3] = {0.f, 0.f, 0.f}, ee[3] = {0.f, 0.f, 0.f};
+  bool hh[3] = {false, false, false};
   bool ok = true;
-  float ya = emu_p3(c3, c2, c1, c0, ts[0]);
+  float ta = 0.f, ya = emu_p3(c3, c2, c1, c0, 0.f);
   ok = ok && fabsf(ya) > del;
-#pragma unroll
-  for (int k = 1; k < 4; k++) {
-    float yb = emu_p3(c3, c2, c1, c0, ts[k]);
+  #pragma unroll 1
+  for (int k = 1; k < 4; k++) {  // the monotone pieces [0,t1], [t1,t2], [t2,1]
+    float tb = k == 1 ? t1 : (k == 2 ? t2 : 1.f);
+    float yb = emu_p3(c3, c2, c1, c0, tb);
     ok = ok && fabsf(yb) > del;
-    has[k - 1] = false;
-    root[k - 1] = 0.f;
-    rad[k - 1] = 0.f;
     if (ok && (ya < 0) != (yb < 0)) {
-      float lo = ts[k - 1], hi = ts[k];
+      float lo = ta, hi = tb;
       bool up = yb > ya;
       float r = 0.5f * (lo + hi);
       #pragma unroll 1
@@ -837,11 +839,19 @@ DI bool emu_cubic_roots3(float c3, float c2, float c1, float c0, float del, floa
       float eps = fmaxf(4e-7f, __fdividef(4.f * del, dp));
       float ym = emu_p3(c3, c2, c1, c0, r - eps), yp = emu_p3(c3, c2, c1, c0, r + eps);
       ok = ok && dp > 0.f && fabsf(ym) > del && fabsf(yp) > del && ((ym < 0) != (yp < 0));
-      has[k - 1] = true;
-      root[k - 1] = r;
-      rad[k - 1] = eps;
+      // slot k - 1, kept in registers
+      rr[0] = k == 1 ? r : rr[0]; rr[1] = k == 2 ? r : rr[1]; rr[2] = k == 3 ? r : rr[2];
+      ee[0] = k == 1 ? eps : ee[0]; ee[1] = k == 2 ? eps : ee[1]; ee[2] = k == 3 ? eps : ee[2];
+      hh[0] = hh[0] || k == 1; hh[1] = hh[1] || k == 2; hh[2] = hh[2] || k == 3;
     }
+    ta = tb;
     ya = yb;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    root[k] = rr[k];
+    rad[k] = ee[k];
+    has[k] = hh[k];
   }
   return ok;
 }
@@ -994,7 +1004,7 @@ static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform,
 #pragma unroll
   for (int j = 0; j < 5; j++)
     if (j + 1 < ne && (val[j] < 0) != (val[j + 1] < 0)) sc |= 1u << j;
-  float bmax = 3 * fmaxf(fmaxf(dist2(p0, p1), dist2(p1, p2)), dist2(p2, p3));    // |cubic'|
+  float bmax = 3 * sqrtf(fmaxf(fmaxf(distsq2(p0, p1), distsq2(p1, p2)), distsq2(p2, p3)));  // |cubic'|
   float rmaxd = 3 * fmaxf(fmaxf(fabsf(r1 - r0), fabsf(r2 - r1)), fabsf(r3 - r2));  // |radius'|
   float M = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
   bool unsure = false;
