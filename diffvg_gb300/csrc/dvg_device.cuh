@@ -915,9 +915,18 @@ DI int emu_unique_root(const float n[6], const float qb[5], float l, float u, fl
 // Called with uniform = true by all 32 lanes of a warp together (lanes
 // without a test pass valid = false): the bracket loop then runs a
 // warp-wide trip count so the lanes' brackets are decided in step.
-static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform, v2 p0, v2 p1, v2 p2, v2 p3, v2 pt,
-                                                       float r0, float r1, float r2, float r3) {
-  int res = valid ? -1 : 2;  // -1: not decided yet
+// Root structure of the cubic's distance quintic as the reference's walk
+// sees it (within_distance.h:150-240): coefficients, breakpoints with
+// enclosures, bracket ends and their certain signs.  false when any of it is
+// uncertain.
+struct EmuRoots {
+  float A, n[6], dQ, dQp, qbz[5];
+  float ends[6], val[6], qloc[6], bre[6];
+  int ne;
+  unsigned sc;  // bit j: the bracket of slots j, j + 1 changes sign
+};
+DI bool emu_root_structure(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, EmuRoots &R) {
+  bool ok = true;
   // distance quintic coefficients exactly as the reference forms them in fp32 (within_distance.h:150-167)
   v2 a = add2(sub2(add2(neg2(p0), scl2(3, p1)), scl2(3, p2)), p3);
   v2 b = add2(sub2(scl2(3, p0), scl2(6, p1)), scl2(3, p2));
@@ -927,7 +936,7 @@ static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform,
   float D = 3 * (sum2(mul2(b, c)) + sum2(mul2(a, e))), E = sum2(mul2(c, c)) + 2 * sum2(mul2(e, b));
   float F = sum2(mul2(e, c));
   float sabs = fabsf(A) + fabsf(B) + fabsf(C) + fabsf(D) + fabsf(E) + fabsf(F);
-  if (!(A > 1e-5f * sabs)) res = 2;
+  if (!(A > 1e-5f * sabs)) ok = false;
   float ia = 1.f / A;
   float n[6] = {1.f, B * ia, C * ia, D * ia, E * ia, F * ia};
   float ns = 1.f + fabsf(n[1]) + fabsf(n[2]) + fabsf(n[3]) + fabsf(n[4]) + fabsf(n[5]);
@@ -954,7 +963,7 @@ static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform,
   }
   // breakpoints: -B/5 and the isolator's roots, each with its enclosure radius (absent: +inf)
   float qr = -n[1] * 0.2f, eq = 3e-7f * fabsf(qr) + 1e-7f;
-  if (fabsf(qr) <= eq || fabsf(qr - 1.f) <= eq) res = 2;
+  if (fabsf(qr) <= eq || fabsf(qr - 1.f) <= eq) ok = false;
   float bp[5], br[5];
   bool hq = qr > 0.f && qr < 1.f;
   bp[0] = hq ? qr : INFINITY;
@@ -963,11 +972,11 @@ static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform,
   {
     float rts[3], rrad[3];
     bool has[3];
-    if (!emu_cubic_roots3(pA, pB, pC, pD, del, rts, rrad, has)) res = 2;
+    if (!emu_cubic_roots3(pA, pB, pC, pD, del, rts, rrad, has)) ok = false;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       float rad = rrad[k] + 1.2e-7f;
-      if (has[k] && (rts[k] - rad <= 0.f || rts[k] + rad >= 1.f)) res = 2;
+      if (has[k] && (rts[k] - rad <= 0.f || rts[k] + rad >= 1.f)) ok = false;
       bp[k + 1] = has[k] ? rts[k] : INFINITY;
       br[k + 1] = has[k] ? rad : 0.f;
       nb += has[k] ? 1 : 0;
@@ -981,7 +990,7 @@ static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform,
   emu_cx(bp[1], br[1], bp[4], br[4]); emu_cx(bp[1], br[1], bp[3], br[3]); emu_cx(bp[1], br[1], bp[2], br[2]);
 #pragma unroll
   for (int j = 1; j < 4; j++)
-    if (j < nb && bp[j] - bp[j - 1] <= br[j] + br[j - 1]) res = 2;
+    if (j < nb && bp[j] - bp[j - 1] <= br[j] + br[j - 1]) ok = false;
   // bracket ends (slot 0: t = 0; slots 1..nb: breakpoints; slot nb + 1: t = 1), Q there, and |Q'| within
   // the enclosure of each breakpoint
   int ne = nb + 2;
@@ -997,13 +1006,83 @@ static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform,
     val[j] = j == 0 ? n[5] : emu_q(n, t);
     qloc[j] = rj > 0.f ? fabsf(qd) + dQp + qpp * rj : 0.f;
     // the sign the reference reads is not certain
-    if (j < ne && fabsf(val[j]) <= dQ + qloc[j] * rj) res = 2;
+    if (j < ne && fabsf(val[j]) <= dQ + qloc[j] * rj) ok = false;
   }
   // brackets whose ends change sign (bit j: slots j, j + 1)
   unsigned sc = 0u;
 #pragma unroll
   for (int j = 0; j < 5; j++)
     if (j + 1 < ne && (val[j] < 0) != (val[j + 1] < 0)) sc |= 1u << j;
+  R.A = A;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    R.n[k] = n[k];
+    R.ends[k] = ends[k];
+    R.val[k] = val[k];
+    R.qloc[k] = qloc[k];
+    R.bre[k] = bre[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 5; k++) R.qbz[k] = qbz[k];
+  R.dQ = dQ;
+  R.dQp = dQp;
+  R.ne = ne;
+  R.sc = sc;
+  return ok;
+}
+
+// The root of Q in the sign-change bracket ending at slot j + 1 of R, as the
+// reference's safeguarded Newton iteration finds it (within_distance.h:
+// 237-261): ts and a bound eps_t on the distance from ts to where the
+// reference stops.  false when the bracket may hold more than one root or
+// the iteration may stop next to an end.
+DI bool emu_bracket_root(const EmuRoots &R, int j, float &ts, float &eps_t) {
+  const float *n = R.n, *qbz = R.qbz;
+  float dQ = R.dQ, dQp = R.dQp;
+  // lower bracket end: the end of the previous sign-change bracket (the reference keeps its lower end
+  // through brackets without a sign change, within_distance.h:237-240)
+  unsigned below = R.sc & ((1u << j) - 1u);
+  int i0 = below ? 32 - __clz(below) : 0;
+  float el = emu_pick6(R.ends, i0), eu = emu_pick6(R.ends, j + 1);
+  float vl = emu_pick6(R.val, i0), vu = emu_pick6(R.val, j + 1);
+  float rl = emu_pick6(R.bre, i0), ru = emu_pick6(R.bre, j + 1);
+  float ql0 = emu_pick6(R.qloc, i0), qu0 = emu_pick6(R.qloc, j + 1);
+  // the reference's bracket ends sit within the enclosures of ours: the certain part of the bracket
+  float l = el + rl, u = eu - ru;
+  // the iteration may stop right at an end where |Q| < 1e-5
+  if (fabsf(vl) <= 1e-5f + dQ + 2.f * ql0 * rl || fabsf(vu) <= 1e-5f + dQ + 2.f * qu0 * ru) return false;
+  float ql = emu_q(n, l), qu = emu_q(n, u);
+  if (fabsf(ql) <= dQ || fabsf(qu) <= dQ || ((ql < 0) == (qu < 0))) return false;
+  float ra, rb, mu;
+  if (!emu_unique_root(n, qbz, l, u, ql, qu, dQ, dQp, 1e-5f, &ra, &rb, &mu)) return false;
+  bool up = emu_q(n, rb) > emu_q(n, ra);
+  float lo = ra, hi = rb;
+  ts = 0.5f * (ra + rb);
+  #pragma unroll 1
+  for (int k = 0; k < DVG_EMU_NEWTON; k++) {  // Newton kept inside the root piece
+    float y = emu_q(n, ts), dy = (((5 * ts + 4 * n[1]) * ts + 3 * n[2]) * ts + 2 * n[3]) * ts + n[4];
+    if ((y > 0) == up) hi = ts; else lo = ts;
+    float nt = ts - __fdividef(y, dy);
+    ts = (nt >= lo && nt <= hi) ? nt : 0.5f * (lo + hi);
+  }
+  // how far the root can be from ts: a certified sign change around ts, else the piece
+  float er = hi - lo;
+  {
+    float dts = (((5 * ts + 4 * n[1]) * ts + 3 * n[2]) * ts + 2 * n[3]) * ts + n[4];
+    float e2 = fmaxf(2e-7f, __fdividef(2.f * (fabsf(emu_q(n, ts)) + dQ), fmaxf(fabsf(dts), mu)));
+    float qm = emu_q(n, ts - e2), qp = emu_q(n, ts + e2);
+    if (fabsf(qm) > dQ && fabsf(qp) > dQ && ((qm < 0) != (qp < 0))) er = fminf(er, e2);
+  }
+  // where the reference may stop: |Q| < 1e-5 around the root, or the 20-step bisection window
+  eps_t = __fdividef(1e-5f + dQ, mu) * 1.000001f + er + (eu - el) * 4e-6f + 1e-6f;
+  return true;
+}
+
+static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform, v2 p0, v2 p1, v2 p2, v2 p3, v2 pt,
+                                                       float r0, float r1, float r2, float r3) {
+  EmuRoots R;
+  int res = emu_root_structure(p0, p1, p2, p3, pt, R) && valid ? -1 : 2;  // -1: not decided yet
+  unsigned sc = R.sc;
   float bmax = 3 * sqrtf(fmaxf(fmaxf(distsq2(p0, p1), distsq2(p1, p2)), distsq2(p2, p3)));  // |cubic'|
   float rmaxd = 3 * fmaxf(fmaxf(fabsf(r1 - r0), fabsf(r2 - r1)), fabsf(r3 - r2));  // |radius'|
   float M = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
@@ -1016,44 +1095,11 @@ static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform,
     if (res >= 0 || it >= cnt) continue;
     int j = __ffs(rem) - 1;
     rem &= rem - 1u;
-    // lower bracket end: the end of the previous sign-change bracket (the reference keeps its lower end
-    // through brackets without a sign change, within_distance.h:237-240)
-    unsigned below = sc & ((1u << j) - 1u);
-    int i0 = below ? 32 - __clz(below) : 0;
-    float el = emu_pick6(ends, i0), eu = emu_pick6(ends, j + 1);
-    float vl = emu_pick6(val, i0), vu = emu_pick6(val, j + 1);
-    float rl = emu_pick6(bre, i0), ru = emu_pick6(bre, j + 1);
-    float ql0 = emu_pick6(qloc, i0), qu0 = emu_pick6(qloc, j + 1);
-    // the reference's bracket ends sit within the enclosures of ours: the certain part of the bracket
-    float l = el + rl, u = eu - ru;
-    // the iteration may stop right at an end where |Q| < 1e-5
-    if (fabsf(vl) <= 1e-5f + dQ + 2.f * ql0 * rl || fabsf(vu) <= 1e-5f + dQ + 2.f * qu0 * ru) {
+    float ts, eps_t;
+    if (!emu_bracket_root(R, j, ts, eps_t)) {
       unsure = true;
       continue;
     }
-    float ql = emu_q(n, l), qu = emu_q(n, u);
-    if (fabsf(ql) <= dQ || fabsf(qu) <= dQ || ((ql < 0) == (qu < 0))) { unsure = true; continue; }
-    float ra, rb, mu;
-    if (!emu_unique_root(n, qbz, l, u, ql, qu, dQ, dQp, 1e-5f, &ra, &rb, &mu)) { unsure = true; continue; }
-    bool up = emu_q(n, rb) > emu_q(n, ra);
-    float lo = ra, hi = rb, ts = 0.5f * (ra + rb);
-    #pragma unroll 1
-    for (int k = 0; k < DVG_EMU_NEWTON; k++) {  // Newton kept inside the root piece
-      float y = emu_q(n, ts), dy = (((5 * ts + 4 * n[1]) * ts + 3 * n[2]) * ts + 2 * n[3]) * ts + n[4];
-      if ((y > 0) == up) hi = ts; else lo = ts;
-      float nt = ts - __fdividef(y, dy);
-      ts = (nt >= lo && nt <= hi) ? nt : 0.5f * (lo + hi);
-    }
-    // how far the root can be from ts: a certified sign change around ts, else the piece
-    float er = hi - lo;
-    {
-      float dts = (((5 * ts + 4 * n[1]) * ts + 3 * n[2]) * ts + 2 * n[3]) * ts + n[4];
-      float e2 = fmaxf(2e-7f, __fdividef(2.f * (fabsf(emu_q(n, ts)) + dQ), fmaxf(fabsf(dts), mu)));
-      float qm = emu_q(n, ts - e2), qp = emu_q(n, ts + e2);
-      if (fabsf(qm) > dQ && fabsf(qp) > dQ && ((qm < 0) != (qp < 0))) er = fminf(er, e2);
-    }
-    // where the reference may stop: |Q| < 1e-5 around the root, or the 20-step bisection window
-    float eps_t = __fdividef(1e-5f + dQ, mu) * 1.000001f + er + (eu - el) * 4e-6f + 1e-6f;
     float margin = (bmax + rmaxd) * eps_t + far_margin(M);
     float tt = 1 - ts;
     float rr = (tt * tt * tt) * r0 + (3 * tt * tt * ts) * r1 + (3 * tt * ts * ts) * r2 + (ts * ts * ts) * r3;
