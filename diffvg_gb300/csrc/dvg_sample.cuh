@@ -416,6 +416,44 @@ struct PFrag {
 };
 static_assert(sizeof(PFrag) <= DVG_PF_BYTES, "prefiltered fragment cache entries");
 
+// Shape-space search radius for a prefiltered stroke's closest point that
+// leaves its fragment unchanged.  The coverage smoothstep(|d| + sw) -
+// smoothstep(|d| - sw) is exactly 0 once |d| - sw >= 1 in fp32 (both terms
+// clamp to 1), so a group whose closest point lies farther than sw_max + 1
+// from pt in canvas space gives no fragment.  Under an affine
+// canvas-to-shape transform (2x2 part L, corner c8) a canvas distance d is
+// at most |L|_F d / |c8| in shape space; the closest-point search keeps the
+// same segment and shape whenever the unbounded search's answer lies inside
+// the radius, because it only drops candidates that cannot come under it.
+// The radius carries a margin for the rounding of both transforms.  Returns
+// INFINITY (the unbounded search of compute_distance) for projective or
+// ill-conditioned transforms, for groups holding an ellipse (whose distance
+// query raises an error), and for groups in which no shape reports a closest
+// point (circles, empty paths), where the unbounded search decides the error.
+DI float stroke_search_radius(const DevScene &S, int g, v2 pt) {
+  const float *c = S.c2s + 9 * g;
+  const float *m = S.P + GI(S, g, DVG_GROUP_XFORM_OFF);
+  if (c[6] != 0.f || c[7] != 0.f || m[6] != 0.f || m[7] != 0.f) return INFINITY;
+  int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
+  float sw = 0.f;
+  bool reports = false;
+  #pragma unroll 1
+  for (int k = 0; k < nsh; k++) {
+    int s = __ldg(&S.group_shapes[off + k]);
+    int kind = SI(S, s, DVG_SHAPE_KIND);
+    if (kind == DVG_ELLIPSE) return INFINITY;
+    reports |= kind == DVG_RECT || (kind == DVG_PATH && SI(S, s, DVG_SHAPE_NUM_SEGMENTS) > 0);
+    sw = fmaxf(sw, stroke_width(S, s));
+  }
+  if (!reports) return INFINITY;
+  float fl = sqrtf(sq(c[0]) + sq(c[1]) + sq(c[3]) + sq(c[4])) / fabsf(c[8]);
+  float fm = sqrtf(sq(m[0]) + sq(m[1]) + sq(m[3]) + sq(m[4])) / fabsf(m[8]);
+  if (!(fl * fm <= 64.f)) return INFINITY;  // also rejects inf / NaN
+  float shift = (fabsf(c[2]) + fabsf(c[5])) / fabsf(c[8]);
+  float r = fl * ((sw + 1.f) * 1.01f + 1e-4f * (absmax2(pt) + 1.f)) + 1e-4f * shift + 1e-3f;
+  return r < INFINITY ? r : INFINITY;
+}
+
 // Coverage fragments of one group at pt (diffvg.cpp:851-905).  Returns the
 // number of fragments written (0..2).
 DI int prefilter_group(const DevScene &S, int g, v2 pt, PFrag *out) {
@@ -426,9 +464,11 @@ DI int prefilter_group(const DevScene &S, int g, v2 pt, PFrag *out) {
     v2 cp = V2(0, 0);
     PathInfo li = {-1, -1, 0.f};
     float d = INFINITY;
-    group_distance(S, g, pt, INFINITY, &ms, &cp, &li, &d);
+    float lim = stroke_search_radius(S, g, pt);
+    group_distance(S, g, pt, lim, &ms, &cp, &li, &d);
     if (ms == -1) {
-      flag_error(S, DVG_EFLAG_UNSUPPORTED);  // diffvg.cpp:867 asserts
+      // with a finite radius: nothing within reach, so the coverage is 0
+      if (lim == INFINITY) flag_error(S, DVG_EFLAG_UNSUPPORTED);  // diffvg.cpp:867 asserts
     } else {
       float sw = stroke_width(S, ms);
       float w = smoothstep(fabsf(d) + sw) - smoothstep(fabsf(d) - sw);

@@ -9,7 +9,8 @@ the render settings, the forward output, and the reference's gradients
 deterministic adjoint image tests/scenes.d_image_pattern.
 
 Usage (in a container that has the reference checkout):
-    python tests/golden/make_golden.py [reference_dir]
+    python tests/golden/make_golden.py [reference_dir [case ...]]
+With case names given, only those fixtures are written.
 """
 import os
 import sys
@@ -76,8 +77,11 @@ def run_case(pyd, case):
 
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else ref_loader.DEFAULT_REF
+    only = set(sys.argv[2:])
     pyd, _ = ref_loader.load(ref)
     for builder in scenes.CASES:
+        if only and builder.__name__ not in only:
+            continue
         case = builder(pyd)
         rec = run_case(pyd, case)
         path = os.path.join(HERE, builder.__name__ + '.npz')

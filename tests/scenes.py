@@ -219,6 +219,24 @@ def prefilter_strokes(m):
     return c
 
 
+def prefilter_transformed_strokes(m):
+    """Prefiltered strokes under rotated, anisotropically scaled group
+    transforms; the second group strokes two shapes (a cubic and a rect)."""
+    c = transformed_group(m)
+    a = -0.3
+    xf = _t([[0.9 * math.cos(a), -1.3 * math.sin(a), 26.0], [0.9 * math.sin(a), 1.3 * math.cos(a), 24.0],
+             [0.0, 0.0, 1.0]])
+    c['shapes'].append(m.Path(num_control_points=torch.tensor([2], dtype=torch.int32),
+                              points=_t([[-14.0, 6.0], [-4.0, -16.0], [8.0, 14.0], [16.0, -6.0]]),
+                              is_closed=False, stroke_width=_t(1.5)))
+    c['shapes'].append(m.Rect(p_min=_t([-6.0, -5.0]), p_max=_t([7.0, 9.0]), stroke_width=_t(0.8)))
+    c['groups'].append(m.ShapeGroup(shape_ids=torch.tensor([1, 2]), fill_color=None,
+                                    stroke_color=_t([0.1, 0.3, 0.9, 0.9]), shape_to_canvas=xf))
+    c['use_prefiltering'] = True
+    c['spp'] = 1
+    return c
+
+
 def sdf_image(m):
     c = overlapping_groups(m)
     c['output'] = 'sdf'
@@ -244,6 +262,7 @@ CASES = [circle_fill, circle_stroke, ellipse_fill, rect_fill_stroke, polygon_fil
          overlapping_groups, _with_filter(overlapping_groups, 'tent', 1.0),
          _with_filter(overlapping_groups, 'parabolic', 1.0), _with_filter(overlapping_groups, 'hann', 1.5),
          background_image, render_size_differs, distance_approx_stroke, prefilter_fills, prefilter_strokes,
+         prefilter_transformed_strokes,
          sdf_image, sdf_eval_positions]
 
 CASE_BY_NAME = {f.__name__: f for f in CASES}
