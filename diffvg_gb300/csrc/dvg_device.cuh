@@ -414,12 +414,14 @@ DI int winding_cubic_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
   int w = 0;
   float ya = cubic_y(ay, by, cy, dy, ts[0]);
   if (fabsf(ya) <= m) return DVG_WINDING_UNDECIDED;
+  #pragma unroll 1
   for (int k = 1; k < nt; k++) {
     float yb = cubic_y(ay, by, cy, dy, ts[k]);
     if (fabsf(yb) <= m) return DVG_WINDING_UNDECIDED;
     if ((ya < 0.f) != (yb < 0.f)) {
       float lo = ts[k - 1], hi = ts[k];
       bool up = yb > ya;
+      #pragma unroll 1
       for (int it = 0; it < 26; it++) {
         float mid = 0.5f * (lo + hi);
         float ym = cubic_y(ay, by, cy, dy, mid);
@@ -494,6 +496,7 @@ DI int winding_shape(const DevScene &S, int s, v2 pt) {
   }
   int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
   int w = 0;
+  #pragma unroll 1
   for (int i = 0; i < nseg; i++) {
     if (nseg > 1 && !box_ray(S.seg_box[so + i], pt)) continue;
     w += winding_segment(S, po, np, __ldg(&S.segment_ctrl[so + i]), __ldg(&S.seg_point[so + i]), pt);
@@ -619,10 +622,10 @@ DI double quintic_eval_cached(const Quintic &q, float t, float &ct, double &cv) 
 // around the chord p0-pn, so
 //     dist(pt, curve) >= dist(pt, chord) - max_i dist(p_i, chord).
 // Splitting at t = 1/2 (de Casteljau) shrinks the capsule radius 4x per
-// level; two levels are tried.  far_margin() covers the fp32 rounding of the
-// bound and of the reference's own fp32 distance evaluation, so a segment
-// reported far is one on which the reference's test fails as well.
-DI v2 mid2(v2 a, v2 b) { return V2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y)); }
+// level; curve_stroke_fast walks the subdivision tree.  far_margin() covers
+// the fp32 rounding of the bound and of the reference's own fp32 distance
+// evaluation, so a segment reported far is one on which the reference's test
+// fails as well (the stroke test and the closest-point search use it alike).
 DI float dist_to_seg(v2 a, v2 b, v2 p) {
   v2 ab = sub2(b, a);
   float l2 = dot2(ab, ab);
@@ -630,33 +633,6 @@ DI float dist_to_seg(v2 a, v2 b, v2 p) {
   return len2(sub2(add2(a, scl2(t, ab)), p));
 }
 DI float far_margin(float m) { return 1e-5f * m + 1e-4f; }
-DI float cubic_lb(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
-  return dist_to_seg(p0, p3, pt) - fmaxf(dist_to_seg(p0, p3, p1), dist_to_seg(p0, p3, p2));
-}
-DI bool cubic_half_far(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float thr) {
-  if (cubic_lb(p0, p1, p2, p3, pt) > thr) return true;
-  v2 a01 = mid2(p0, p1), a12 = mid2(p1, p2), a23 = mid2(p2, p3);
-  v2 b0 = mid2(a01, a12), b1 = mid2(a12, a23), c = mid2(b0, b1);
-  return cubic_lb(p0, a01, b0, c, pt) > thr && cubic_lb(c, b1, a23, p3, pt) > thr;
-}
-// true when every point of the cubic is farther than thr from pt
-DI bool cubic_far(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt, float thr) {
-  if (cubic_lb(p0, p1, p2, p3, pt) > thr) return true;
-  v2 a01 = mid2(p0, p1), a12 = mid2(p1, p2), a23 = mid2(p2, p3);
-  v2 b0 = mid2(a01, a12), b1 = mid2(a12, a23), c = mid2(b0, b1);
-  return cubic_half_far(p0, a01, b0, c, pt, thr) && cubic_half_far(c, b1, a23, p3, pt, thr);
-}
-DI float quad_lb(v2 p0, v2 p1, v2 p2, v2 pt) { return dist_to_seg(p0, p2, pt) - dist_to_seg(p0, p2, p1); }
-DI bool quad_far(v2 p0, v2 p1, v2 p2, v2 pt, float thr) {
-  if (quad_lb(p0, p1, p2, pt) > thr) return true;
-  v2 a01 = mid2(p0, p1), a12 = mid2(p1, p2), c = mid2(a01, a12);
-  if (quad_lb(p0, a01, c, pt) > thr && quad_lb(c, a12, p2, pt) > thr) return true;
-  v2 l1 = mid2(p0, a01), l2 = mid2(a01, c), lc = mid2(l1, l2);
-  v2 r1 = mid2(c, a12), r2 = mid2(a12, p2), rc = mid2(r1, r2);
-  return quad_lb(p0, l1, lc, pt) > thr && quad_lb(lc, l2, c, pt) > thr && quad_lb(c, r1, rc, pt) > thr &&
-         quad_lb(rc, r2, p2, pt) > thr;
-}
-
 #define DVG_SUBDIV_DEPTH 8
 DI v2 lerp2(v2 a, v2 b, float u) { return V2(a.x + u * (b.x - a.x), a.y + u * (b.y - a.y)); }
 DI v2 cubic_blossom(v2 p0, v2 p1, v2 p2, v2 p3, float u, float v, float w) {
@@ -1334,7 +1310,9 @@ DN bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
         dist = dist2(cp, pt);
       } else {
         float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(absmax2(p2), absmax2(pt)));
-        if (quad_far(p0, p1, p2, pt, min_dist + far_margin(m))) continue;  // cannot improve the best
+        const float2 *tp = S.seg_tpts ? S.seg_tpts + (size_t)(so + seg) * DVG_TREE_PTS : nullptr;
+        const float *tw = S.seg_th ? S.seg_th + (size_t)(so + seg) * DVG_TREE_NODES : nullptr;
+        if (curve_stroke_fast<1>(p0, p1, p2, p2, tp, tw, pt, min_dist, far_margin(m)) == 0) continue;  // cannot improve the best
         v2 pt0 = eval_quad(p0, p1, p2, 0), pt1 = eval_quad(p0, p1, p2, 1);
         float d0 = dist2(pt0, pt), d1 = dist2(pt1, pt);
         dist = d0; cp = pt0; t_root = 0;
@@ -1359,7 +1337,9 @@ DN bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
          p3 = path_pt(S, po, (i0 + 3) % np);
       {
         float m = fmaxf(fmaxf(absmax2(p0), absmax2(p1)), fmaxf(fmaxf(absmax2(p2), absmax2(p3)), absmax2(pt)));
-        if (cubic_far(p0, p1, p2, p3, pt, min_dist + far_margin(m))) continue;  // cannot improve the best
+        const float2 *tp = S.seg_tpts ? S.seg_tpts + (size_t)(so + seg) * DVG_TREE_PTS : nullptr;
+        const float *tw = S.seg_th ? S.seg_th + (size_t)(so + seg) * DVG_TREE_NODES : nullptr;
+        if (curve_stroke_fast<2>(p0, p1, p2, p3, tp, tw, pt, min_dist, far_margin(m)) == 0) continue;  // cannot improve the best
       }
       v2 pt0 = eval_cubic(p0, p1, p2, p3, 0), pt1 = eval_cubic(p0, p1, p2, p3, 1);
       float d0 = dist2(pt0, pt), d1 = dist2(pt1, pt);
