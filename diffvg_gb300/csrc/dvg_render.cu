@@ -120,15 +120,12 @@ __global__ void __launch_bounds__(256) k_resolve(DevRender R0, const float4 *sam
   reinterpret_cast<float4 *>(image)[p] = acc;
 }
 
-__device__ __forceinline__ float block_sum(float v) {
-  __shared__ float red[32];
+// warp total in lane 0; no block barrier, so a warp that finishes its
+// samples early leaves the SM to other blocks instead of waiting for the
+// slowest warp of its tile
+__device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  float s = 0.f;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
-  return s;
+  return v;
 }
 
 // interior adjoint (render_kernel with d_render_image, diffvg.cpp:1160-1268)
@@ -189,8 +186,8 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
         }
       }
   }
-  float tot = block_sum(dfr);
-  if (threadIdx.x == 0 && tot != 0.f) atomicAdd(R.d_params + R.filter_radius_off, tot);
+  float tot = warp_sum(dfr);
+  if ((threadIdx.x & 31) == 0 && tot != 0.f) atomicAdd(R.d_params + R.filter_radius_off, tot);
 }
 
 // Background adjoint in sample order per pixel: a sample without fragments

@@ -6,9 +6,10 @@
 // ascending group id, which is the reference's back-to-front fragment order
 // (it sorts fragments by group id, diffvg.cpp:605-615), so the forward pass
 // blends each fragment as soon as it is found and keeps no fragment list.
-// The adjoint re-evaluates the fragments of its sample (the forward pass
-// stores nothing per sample) into a per-thread list and walks it in
-// reverse.
+// The adjoint gathers the fragments of its sample into a per-thread list and
+// walks it in reverse; it takes them from the forward pass's per-sample
+// cache when that is valid for the current parameters and re-evaluates them
+// otherwise.
 #pragma once
 
 #include "dvg_adjoint.cuh"
@@ -502,36 +503,46 @@ DI int prefilter_group(const DevScene &S, int g, v2 pt, PFrag *out) {
 }
 
 // sample_color_prefiltered, forward only (diffvg.cpp:835-960)
-// With cache set, the sample's fragments (blend order) and their count are
-// stored for the backward pass (sample idx of n).
+// With cache set, the sample's fragments (blend order) are stored for the
+// backward pass (sample idx of n): all of them, or, when they do not fit,
+// those of the leading groups that fit whole, with DVG_PF_PARTIAL set in the
+// count; the backward pass then resumes the walk after the last stored group.
+#define DVG_PF_PARTIAL 0x80
 DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, PFrag *cache = nullptr,
                                        unsigned char *cache_cnt = nullptr, int n = 0, int idx = 0) {
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   int b, e;
   bool list = cand_range(S, pt, b, e);
   float4 acc = bg ? *bg : F4(0, 0, 0, 0);
-  int nf = 0;
+  int nf = 0, nc = 0;
+  bool caching = cache != nullptr;
   int G = S.num_groups;
   for (int k = b; k < e; k++) {
     int g = list ? __ldg(&S.tile_list[k]) : k;
     if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
     PFrag fr[2];
     int m = prefilter_group(S, g, pt, fr);
-    for (int j = 0; j < m; j++) {
-      blend(acc, fr[j].c);
-      if (cache && nf < DVG_PF_SLOTS) cache[(size_t)nf * n + idx] = fr[j];
-      nf++;
+    if (caching && m > 0) {
+      if (nc + m <= DVG_PF_SLOTS) {
+        for (int j = 0; j < m; j++) cache[(size_t)(nc + j) * n + idx] = fr[j];
+        nc += m;
+      } else {
+        caching = false;
+      }
     }
+    for (int j = 0; j < m; j++) blend(acc, fr[j].c);
+    nf += m;
   }
-  if (cache_cnt) cache_cnt[idx] = nf > DVG_PF_SLOTS ? DVG_HIT_NONE : (unsigned char)nf;
+  if (cache_cnt) cache_cnt[idx] = (unsigned char)(caching ? nc : (nc | DVG_PF_PARTIAL));
   if (nf > DVG_MAX_PREFILTER_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
   if (nf <= 0) return bg ? *bg : F4(0, 0, 0, 0);
   return finish_color(acc);
 }
 
 // Adjoint of sample_color_prefiltered (diffvg.cpp:960-1113)
-// cached >= 0: the forward pass's fragments of this sample (cached of them,
-// in cache) stand in for computing them again.
+// cached >= 0: the forward pass's cache entry of this sample (a count, with
+// DVG_PF_PARTIAL when only the leading groups' fragments were stored); the
+// stored fragments stand in for computing them again.
 DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color,
                                        float4 *d_bg, int *assign, float *d_tr, float *dp,
                                        const PFrag *cache = nullptr, int n = 0, int idx = 0, int cached = -1) {
@@ -545,17 +556,21 @@ DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 s
   int nf = 0;
   bool overflow = false;
   int G = S.num_groups;
+  int g_done = -1;  // groups up to this id are in the cache
   if (cached >= 0) {
-    for (int j = 0; j < cached; j++) {
+    int nc = cached & ~DVG_PF_PARTIAL;
+    for (int j = 0; j < nc; j++) {
       frags[j] = cache[(size_t)j * n + idx];
       blend(acc, frags[j].c);
       accs[j] = acc;
     }
-    nf = cached;
-    e = b;  // the walk below has nothing left to do
+    nf = nc;
+    if (cached & DVG_PF_PARTIAL) g_done = nc > 0 ? frags[nc - 1].group_stroke >> 1 : -1;
+    else e = b;  // the walk below has nothing left to do
   }
   for (int k = b; k < e; k++) {
     int g = list ? __ldg(&S.tile_list[k]) : k;
+    if (g <= g_done) continue;  // candidates run in ascending group id
     if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
     PFrag fr[2];
     int n = prefilter_group(S, g, pt, fr);
