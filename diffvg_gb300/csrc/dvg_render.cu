@@ -291,11 +291,23 @@ __global__ void k_edge_order(EdgeRecords E, int n) {
   if (key >= 0) E.order[E.tile_start[key] + E.rank[idx]] = idx;
 }
 
+// Boundary samples (render_edge_kernel, diffvg.cpp:1388-1475).  With PAIRS
+// set, the two colour queries of a sample (just inside and just outside the
+// boundary) run in adjacent lanes: their points are 2e-4 canvas widths apart,
+// so the two lanes walk the same candidates and tests, and a warp spreads its
+// divergence over 16 samples instead of 32 walked twice; the even lane
+// finishes the sample.  Without PAIRS one lane runs both queries: for scenes
+// of few shapes the walks are short and the gradient atomics, aggregated per
+// warp, are what costs.
+template <bool PAIRS>
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
     k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, EdgeRecords E) {
   __shared__ WarpQueue wq[8];
+  const unsigned full = 0xffffffffu;
   DevRender R = load_filter(R0, nullptr);
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int i = (int)(PAIRS ? gi >> 1 : gi);
+  bool outside = PAIRS && (gi & 1);
   int T = S.tiles_x * S.tiles_y;
   bool active = i < E.tile_start[T] && !bins_overflowed(S);
   int idx = active ? E.order[i] : 0;
@@ -307,14 +319,25 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   int g = c.x, s = c.y;
   BData bd = {c.z, c.w, d.x, d.y != 0.f ? 1 : 0};
   int bx = min(max((int)(bpt.x * R.w), 0), R.w - 1), by = min(max((int)(bpt.y * R.h), 0), R.h - 1);
-  EdgeQ qin = {g, s, 0}, qout = {g, s, 0};
+  EdgeQ qq = {g, s, 0};
   const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (by * R.w + bx) : nullptr;
   WarpQueue *q = &wq[threadIdx.x >> 5];
   int lane = threadIdx.x & 31;
-  float4 cin = sample_color_fwd(S, bg, sub2(bpt, scl2(1e-4f, normal)), &qin, active, q, lane);
-  float4 cout = sample_color_fwd(S, bg, add2(bpt, scl2(1e-4f, normal)), &qout, active, q, lane);
-  if (!active || (!qin.hit && !qout.hit)) return;
-  if (!qin.hit) {
+  v2 qpt = outside ? add2(bpt, scl2(1e-4f, normal)) : sub2(bpt, scl2(1e-4f, normal));
+  float4 cin = sample_color_fwd(S, bg, qpt, &qq, active, q, lane), cout;
+  int hin = qq.hit, hout;
+  if (PAIRS) {
+    cout = F4(__shfl_xor_sync(full, cin.x, 1), __shfl_xor_sync(full, cin.y, 1), __shfl_xor_sync(full, cin.z, 1),
+              __shfl_xor_sync(full, cin.w, 1));
+    hout = __shfl_xor_sync(full, hin, 1);
+  } else {
+    EdgeQ qo = {g, s, 0};
+    cout = sample_color_fwd(S, bg, add2(bpt, scl2(1e-4f, normal)), &qo, active, q, lane);
+    hout = qo.hit;
+  }
+  if (outside || !active) return;
+  if (!hin && !hout) return;
+  if (!hin) {
     normal = neg2(normal);
     float4 tmp = cin; cin = cout; cout = tmp;
   }
@@ -402,7 +425,8 @@ void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cu
   k_edge_sample<<<blocks_of(n), 256, 0, st>>>(S, R, E);
   k_edge_scan<<<1, 1024, 0, st>>>(S, E);
   k_edge_order<<<blocks_of(n), 256, 0, st>>>(E, (int)n);
-  k_edge_eval<<<blocks_of(n), 256, 0, st>>>(S, R, E);
+  if (S.num_groups >= 8) k_edge_eval<true><<<blocks_of(2 * (long long)n), 256, 0, st>>>(S, R, E);  // two lanes per sample
+  else k_edge_eval<false><<<blocks_of(n), 256, 0, st>>>(S, R, E);
 }
 void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
                 const float *d_sdf, cudaStream_t st) {
