@@ -93,7 +93,7 @@ struct DevRender {
   unsigned char *hit_cnt = nullptr;
   const unsigned *hit_stale = nullptr;  // backward: nonzero when the parameters differ from the forward's
 };
-#define DVG_HIT_SLOTS 8
+#define DVG_HIT_SLOTS 16
 #define DVG_HIT_NONE 255
 #define DVG_PF_SLOTS 12   // prefiltered fragments cached per sample
 #define DVG_PF_BYTES 64   // bytes per cached prefiltered fragment
