@@ -386,13 +386,13 @@ bool hit_matches(const DvgScene *sc, const DvgRenderArgs *a) {
 }
 
 size_t edge_bytes(DvgScene *sc, size_t n) {
-  size_t T = (size_t)sc->tiles_x * sc->tiles_y;
+  size_t T = (size_t)sc->tiles_x * sc->tiles_y * DVG_EDGE_CELLS;
   return carve_size({n * sizeof(float4), n * sizeof(float4), n * sizeof(int4), n * sizeof(float2), n * sizeof(int),
                      n * sizeof(int), n * sizeof(int), T * sizeof(int), (T + 1) * sizeof(int)});
 }
 
 EdgeRecords edge_records(DvgScene *sc, size_t n) {
-  size_t T = (size_t)sc->tiles_x * sc->tiles_y;
+  size_t T = (size_t)sc->tiles_x * sc->tiles_y * DVG_EDGE_CELLS;
   char *p = reinterpret_cast<char *>(sc->edge.ptr);
   EdgeRecords E;
   E.a = carve<float4>(p, n);

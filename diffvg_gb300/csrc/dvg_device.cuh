@@ -106,8 +106,11 @@ struct EdgeRecords {
   int4 *c;          // group, shape, segment, first point
   float2 *d;        // segment t, is_stroke
   int *key, *rank, *order;
-  int *tile_count, *tile_start;
+  int *tile_count, *tile_start;  // per ordering cell: [tiles * DVG_EDGE_CELLS] (+1)
 };
+// Boundary samples are ordered by canvas tile and, inside a tile, by 4x4
+// pixel cell in Morton order.
+#define DVG_EDGE_CELLS 16
 
 typedef float2 v2;
 

@@ -210,10 +210,12 @@ __global__ void k_bg_combine(const __grid_constant__ DevScene S, DevRender R, co
 // Boundary adjoint (sample_boundary_kernel + render_edge_kernel,
 // diffvg.cpp:1325-1475) in three passes:
 //   k_edge_sample  draws every boundary sample (same pcg streams and CDFs as
-//                  the reference) and files it under its canvas tile;
-//   k_edge_order   turns the per-tile counts into a tile-sorted order;
-//   k_edge_eval    evaluates the two sides of each boundary point in tile
-//                  order, so that a warp's samples share a candidate list.
+//                  the reference) and files it under its canvas tile and
+//                  4x4-pixel cell;
+//   k_edge_order   turns the per-cell counts into a cell-sorted order;
+//   k_edge_eval    evaluates the two sides of each boundary point in that
+//                  order, so that a warp's samples share a candidate list
+//                  and mostly the same segment tests.
 // The reference sorts its boundary samples by Morton code for the same
 // coherence (diffvg.cpp:1594-1599); the order only changes the order of the
 // gradient atomics.
@@ -247,11 +249,15 @@ __global__ void __launch_bounds__(256) k_edge_sample(const __grid_constant__ Dev
   pdf = pmf * pdf;
   int bx = (int)(bpt.x * R.w), by = (int)(bpt.y * R.h);
   if (bx < 0 || bx >= R.w || by < 0 || by >= R.h) return;
-  // canvas tile of the boundary point (clamped into the grid)
+  // canvas tile of the boundary point (clamped into the grid), then its 4x4
+  // pixel cell inside the tile
   float cx = bpt.x * S.W, cy = bpt.y * S.H;
   int tx = min(max((int)floorf(cx / DVG_TILE), 0), S.tiles_x - 1);
   int ty = min(max((int)floorf(cy / DVG_TILE), 0), S.tiles_y - 1);
-  int key = ty * S.tiles_x + tx;
+  int lx = min(max((int)floorf(cx) - tx * DVG_TILE, 0), DVG_TILE - 1) >> 2;
+  int ly = min(max((int)floorf(cy) - ty * DVG_TILE, 0), DVG_TILE - 1) >> 2;
+  int cell = (lx & 1) | ((ly & 1) << 1) | ((lx & 2) << 1) | ((ly & 2) << 2);
+  int key = (ty * S.tiles_x + tx) * DVG_EDGE_CELLS + cell;
   E.key[idx] = key;
   E.rank[idx] = atomicAdd(&E.tile_count[key], 1);
   E.a[idx] = F4(bpt.x, bpt.y, normal.x, normal.y);
@@ -260,9 +266,9 @@ __global__ void __launch_bounds__(256) k_edge_sample(const __grid_constant__ Dev
   E.d[idx] = make_float2(bd.t, (float)bd.is_stroke);
 }
 
-// exclusive scan of the per-tile sample counts (one block of 1024 threads)
+// exclusive scan of the per-cell sample counts (one block of 1024 threads)
 __global__ void k_edge_scan(const __grid_constant__ DevScene S, EdgeRecords E) {
-  int T = S.tiles_x * S.tiles_y;
+  int T = S.tiles_x * S.tiles_y * DVG_EDGE_CELLS;
   __shared__ int part[1024];
   int per = (T + blockDim.x - 1) / blockDim.x;
   int lo = threadIdx.x * per, hi = min(lo + per, T);
@@ -308,7 +314,7 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int i = (int)(PAIRS ? gi >> 1 : gi);
   bool outside = PAIRS && (gi & 1);
-  int T = S.tiles_x * S.tiles_y;
+  int T = S.tiles_x * S.tiles_y * DVG_EDGE_CELLS;
   bool active = i < E.tile_start[T] && !bins_overflowed(S);
   int idx = active ? E.order[i] : 0;
   float4 a = active ? E.a[idx] : F4(0.5f, 0.5f, 1.f, 0.f), b = active ? E.b[idx] : F4(0, 0, 1, 0);
@@ -421,7 +427,7 @@ void launch_bg_combine(const DevScene &S, const DevRender &R, const float4 *dbg_
 }
 void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
   long long n = (long long)R.w * R.h * R.spp;
-  cudaMemsetAsync(E.tile_count, 0, sizeof(int) * S.tiles_x * S.tiles_y, st);
+  cudaMemsetAsync(E.tile_count, 0, sizeof(int) * S.tiles_x * S.tiles_y * DVG_EDGE_CELLS, st);
   k_edge_sample<<<blocks_of(n), 256, 0, st>>>(S, R, E);
   k_edge_scan<<<1, 1024, 0, st>>>(S, E);
   k_edge_order<<<blocks_of(n), 256, 0, st>>>(E, (int)n);
