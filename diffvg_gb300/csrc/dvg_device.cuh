@@ -108,9 +108,10 @@ struct EdgeRecords {
   int *key, *rank, *order;
   int *tile_count, *tile_start;  // per ordering cell: [tiles * DVG_EDGE_CELLS] (+1)
 };
-// Boundary samples are ordered by canvas tile and, inside a tile, by 4x4
-// pixel cell in Morton order.
-#define DVG_EDGE_CELLS 16
+// Boundary samples are ordered by canvas tile and, inside a tile, by
+// 2^DVG_EDGE_CELL_SHIFT-pixel square cell in Morton order.
+#define DVG_EDGE_CELL_SHIFT 2
+#define DVG_EDGE_CELLS ((DVG_TILE >> DVG_EDGE_CELL_SHIFT) * (DVG_TILE >> DVG_EDGE_CELL_SHIFT))
 
 typedef float2 v2;
 

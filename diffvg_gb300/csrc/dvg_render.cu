@@ -211,7 +211,7 @@ __global__ void k_bg_combine(const __grid_constant__ DevScene S, DevRender R, co
 // diffvg.cpp:1325-1475) in three passes:
 //   k_edge_sample  draws every boundary sample (same pcg streams and CDFs as
 //                  the reference) and files it under its canvas tile and
-//                  4x4-pixel cell;
+//                  its cell of 4x4 pixels in the tile;
 //   k_edge_order   turns the per-cell counts into a cell-sorted order;
 //   k_edge_eval    evaluates the two sides of each boundary point in that
 //                  order, so that a warp's samples share a candidate list
@@ -249,14 +249,16 @@ __global__ void __launch_bounds__(256) k_edge_sample(const __grid_constant__ Dev
   pdf = pmf * pdf;
   int bx = (int)(bpt.x * R.w), by = (int)(bpt.y * R.h);
   if (bx < 0 || bx >= R.w || by < 0 || by >= R.h) return;
-  // canvas tile of the boundary point (clamped into the grid), then its 4x4
-  // pixel cell inside the tile
+  // canvas tile of the boundary point (clamped into the grid), then its cell
+  // inside the tile
   float cx = bpt.x * S.W, cy = bpt.y * S.H;
   int tx = min(max((int)floorf(cx / DVG_TILE), 0), S.tiles_x - 1);
   int ty = min(max((int)floorf(cy / DVG_TILE), 0), S.tiles_y - 1);
-  int lx = min(max((int)floorf(cx) - tx * DVG_TILE, 0), DVG_TILE - 1) >> 2;
-  int ly = min(max((int)floorf(cy) - ty * DVG_TILE, 0), DVG_TILE - 1) >> 2;
-  int cell = (lx & 1) | ((ly & 1) << 1) | ((lx & 2) << 1) | ((ly & 2) << 2);
+  int lx = min(max((int)floorf(cx) - tx * DVG_TILE, 0), DVG_TILE - 1) >> DVG_EDGE_CELL_SHIFT;
+  int ly = min(max((int)floorf(cy) - ty * DVG_TILE, 0), DVG_TILE - 1) >> DVG_EDGE_CELL_SHIFT;
+  int cell = 0;
+  #pragma unroll
+  for (int bit = 0; bit < 4; bit++) cell |= (((lx >> bit) & 1) << (2 * bit)) | (((ly >> bit) & 1) << (2 * bit + 1));
   int key = (ty * S.tiles_x + tx) * DVG_EDGE_CELLS + cell;
   E.key[idx] = key;
   E.rank[idx] = atomicAdd(&E.tile_count[key], 1);
