@@ -61,12 +61,24 @@ DN void d_closest_path(const DevScene &S, int s, v2 pt, v2 d_cp, const PathInfo 
     if (t == 0) d0 = add2(d0, d_cp);
     else if (t == 1) d3 = add2(d3, d_cp);
     else {
-      Quintic q = cubic_quintic(p0, p1, p2, p3, pt);
+      // The quintic's normalised coefficients and the implicit-function
+      // terms below divide by A and by Q'(t) in fp64; one reciprocal of each
+      // stands in for the reference's separate divisions (the adjoint moves
+      // by fp64 rounding only, far inside the gradient tolerance, and the
+      // fp64 divisions are what this routine spends its time on).
       v2 a = add2(sub2(add2(neg2(p0), scl2(3, p1)), scl2(3, p2)), p3);
       v2 b = add2(sub2(scl2(3, p0), scl2(6, p1)), scl2(3, p2));
       v2 c = add2(scl2(-3, p0), scl2(3, p1));
       v2 e = sub2(p0, pt);
       double A = (double)(3 * sum2(mul2(a, a)));
+      double inv_a = ddiv(1.0, A);
+      Quintic q;
+      q.A = A;
+      q.B = (double)(5 * sum2(mul2(a, b))) * inv_a;
+      q.C = (double)(4 * sum2(mul2(a, c)) + 2 * sum2(mul2(b, b))) * inv_a;
+      q.D = (double)(3 * (sum2(mul2(b, c)) + sum2(mul2(a, e)))) * inv_a;
+      q.E = (double)(sum2(mul2(c, c)) + 2 * sum2(mul2(e, b))) * inv_a;
+      q.F = (double)(sum2(mul2(e, c))) * inv_a;
       v2 d_p = d_cp;
       float tt = 1 - t;
       float d_tt = 3 * tt * tt * dot2(d_p, p0) + 6 * tt * t * dot2(d_p, p1) + 3 * t * t * dot2(d_p, p2);
@@ -77,13 +89,10 @@ DN void d_closest_path(const DevScene &S, int s, v2 pt, v2 d_cp, const PathInfo 
       d3 = add2(d3, scl2(t * t * t, d_p));
       double pd = quintic_deriv(q, t);
       if (fabs(pd) > 1e-10f) {
-        double dB = -(d_t / pd) * t * t * t * t;
-        double dC = -(d_t / pd) * t * t * t;
-        double dD = -(d_t / pd) * t * t;
-        double dE = -(d_t / pd) * t;
-        double dF = -(d_t / pd);
-        double dA = -dB * q.B / A - dC * q.C / A - dD * q.D / A - dE * q.E / A - dF * q.F / A;
-        dB /= A; dC /= A; dD /= A; dE /= A; dF /= A;
+        double u = -ddiv(d_t, pd);
+        double dF = u, dE = u * t, dD = dE * t, dC = dD * t, dB = dC * t;
+        double dA = -(dB * q.B + dC * q.C + dD * q.D + dE * q.E + dF * q.F) * inv_a;
+        dB *= inv_a; dC *= inv_a; dD *= inv_a; dE *= inv_a; dF *= inv_a;
         // float += double updates round after every term
 #define ACC(dst, sc, vec) do { (dst).x = (float)((double)(dst).x + (sc) * (double)(vec).x); \
                                (dst).y = (float)((double)(dst).y + (sc) * (double)(vec).y); } while (0)
@@ -240,8 +249,7 @@ DI void d_group_distance(const DevScene &S, int g, int s, v2 pt, v2 closest, con
       for (int k = 0; k < 3; k++) acc += tmp[3 * i + k] * t[3 * k + j];
       d_s2c[3 * i + j] += acc;
     }
-#pragma unroll
-  for (int i = 0; i < 9; i++) gadd(dp, xo + i, d_s2c[i]);
+  gadd_shared<9>(dp, xo, d_s2c);  // the group's transform: every lane of a coherent warp adds here
   if (d_translation) {
     atomicAdd(d_translation + 0, -d_pt.x);
     atomicAdd(d_translation + 1, -d_pt.y);

@@ -95,7 +95,7 @@ struct DevRender {
 };
 #define DVG_HIT_SLOTS 16
 #define DVG_HIT_NONE 255
-#define DVG_PF_SLOTS 12   // prefiltered fragments cached per sample
+#define DVG_PF_SLOTS 16   // prefiltered fragments cached per sample
 #define DVG_PF_BYTES 64   // bytes per cached prefiltered fragment
 
 // Boundary samples filed by canvas tile (edge-sampling pass), n entries
@@ -1516,11 +1516,23 @@ DI void gadd4(float *dp, int off, float4 v) {
   gadd(dp, off + 3, v.w);
 }
 
-// d_sample_color (diffvg.cpp:370-504)
+// 4 consecutive parameters; with agg, the lanes of the warp that reach this
+// point with the same target sum first (gadd_shared)
+DI void gadd4_agg(float *dp, int off, float4 v, bool agg) {
+  if (agg) {
+    float a[4] = {v.x, v.y, v.z, v.w};
+    gadd_shared<4>(dp, off, a);
+  } else {
+    gadd4(dp, off, v);
+  }
+}
+
+// d_sample_color (diffvg.cpp:370-504).  agg: the samples of the calling warp
+// are neighbouring pixels (interior passes), which mostly hit the same paints
 DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, float4 d_color, float *dp,
-                      float *d_translation) {
+                      float *d_translation, bool agg) {
   if (kind == DVG_CONSTANT) {
-    gadd4(dp, off, d_color);
+    gadd4_agg(dp, off, d_color, agg);
     return;
   }
   int oo = off + 4, co = off + 4 + nstops;
@@ -1536,7 +1548,7 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
     t = len2(no);
   }
   if (t < pget(S, oo)) {
-    gadd4(dp, co, d_color);
+    gadd4_agg(dp, co, d_color, agg);
     return;
   }
   for (int i = 0; i < nstops - 1; i++) {
@@ -1550,10 +1562,15 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
       float d_on = -d_tt * tt / (on - oc);
       float d_oc = d_tt * ((tt - 1.f) / (on - oc));
       float d_t = d_tt / (on - oc);
-      gadd4(dp, co + 4 * i, dcc);
-      gadd4(dp, co + 4 * (i + 1), dcn);
-      gadd(dp, oo + i, d_oc);
-      gadd(dp, oo + i + 1, d_on);
+      gadd4_agg(dp, co + 4 * i, dcc, agg);
+      gadd4_agg(dp, co + 4 * (i + 1), dcn, agg);
+      if (agg) {
+        float o2v[2] = {d_oc, d_on};
+        gadd_shared<2>(dp, oo + i, o2v);
+      } else {
+        gadd(dp, oo + i, d_oc);
+        gadd(dp, oo + i + 1, d_on);
+      }
       if (kind == DVG_LINEAR) {
         float l = rmax(dot2(sub2(end, beg), sub2(end, beg)), 1e-3f);
         v2 d_beg = div2s(scl2(d_t, sub2(neg2(sub2(pt, beg)), sub2(end, beg))), l);
@@ -1563,7 +1580,7 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
           d_beg = add2(d_beg, scl2(2 * d_l, sub2(beg, end)));
           d_end = add2(d_end, scl2(2 * d_l, sub2(end, beg)));
         }
-        gadd4(dp, off, F4(d_beg.x, d_beg.y, d_end.x, d_end.y));
+        gadd4_agg(dp, off, F4(d_beg.x, d_beg.y, d_end.x, d_end.y), agg);
         if (d_translation) {
           atomicAdd(d_translation + 0, d_beg.x + d_end.x);
           atomicAdd(d_translation + 1, d_beg.y + d_end.y);
@@ -1576,7 +1593,7 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
         v2 d_off = V2(d_no.x / rad.x, d_no.y / rad.y);
         v2 d_rad = V2(-d_no.x * o2.x / (rad.x * rad.x), -d_no.y * o2.y / (rad.y * rad.y));
         v2 d_cen = neg2(d_off);
-        gadd4(dp, off, F4(d_cen.x, d_cen.y, d_rad.x, d_rad.y));
+        gadd4_agg(dp, off, F4(d_cen.x, d_cen.y, d_rad.x, d_rad.y), agg);
         if (d_translation) {
           atomicAdd(d_translation + 0, d_cen.x);
           atomicAdd(d_translation + 1, d_cen.y);
@@ -1586,7 +1603,7 @@ DN void d_paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt, f
     }
   }
   int last = co + 4 * (nstops - 1);
-  gadd4(dp, last, d_color);
+  gadd4_agg(dp, last, d_color, agg);
 }
 
 // d_length / d_normalize (vector.h:496-503, 591-601)

@@ -384,10 +384,10 @@ DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, fl
     int g = keys[i] >> 1;
     if (keys[i] & 1)
       d_paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
-                    GI(S, g, DVG_GROUP_STROKE_STOPS), pt, dci, dp, d_tr);
+                    GI(S, g, DVG_GROUP_STROKE_STOPS), pt, dci, dp, d_tr, true);
     else
       d_paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS),
-                    pt, dci, dp, d_tr);
+                    pt, dci, dp, d_tr, true);
     dcr = d_pr; dcg = d_pg; dcb = d_pb; dca = d_pa;
   }
   if (d_bg) { d_bg->x += dcr; d_bg->y += dcg; d_bg->z += dcb; d_bg->w += dca; }
@@ -556,16 +556,18 @@ DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 s
   int nf = 0;
   bool overflow = false;
   int G = S.num_groups;
+  // cached fragments stay in the cache (read again by the reverse walk);
+  // only the recomputed ones go to the per-thread list
   int g_done = -1;  // groups up to this id are in the cache
+  int nc = 0;
   if (cached >= 0) {
-    int nc = cached & ~DVG_PF_PARTIAL;
+    nc = cached & ~DVG_PF_PARTIAL;
     for (int j = 0; j < nc; j++) {
-      frags[j] = cache[(size_t)j * n + idx];
-      blend(acc, frags[j].c);
+      blend(acc, cache[(size_t)j * n + idx].c);
       accs[j] = acc;
     }
     nf = nc;
-    if (cached & DVG_PF_PARTIAL) g_done = nc > 0 ? frags[nc - 1].group_stroke >> 1 : -1;
+    if (cached & DVG_PF_PARTIAL) g_done = nc > 0 ? cache[(size_t)(nc - 1) * n + idx].group_stroke >> 1 : -1;
     else e = b;  // the walk below has nothing left to do
   }
   for (int k = b; k < e; k++) {
@@ -602,7 +604,7 @@ DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 s
     dcr = nr; dcg = ng; dcb = nb;
   }
   for (int i = nf - 1; i >= 0; i--) {
-    const PFrag &f = frags[i];
+    const PFrag f = i < nc ? cache[(size_t)i * n + idx] : frags[i];
     float4 p = i > 0 ? accs[i - 1] : first;
     float d_pa = dca * (1.f - f.c.w);
     float d_ai = dca * (1.f - p.w);
@@ -619,7 +621,7 @@ DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 s
         float d_w = w > 0 ? (f.c.w / w) * d_ai : 0.f;
         d_ai *= w;
         d_paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
-                      GI(S, g, DVG_GROUP_STROKE_STOPS), pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr);
+                      GI(S, g, DVG_GROUP_STROKE_STOPS), pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr, true);
         float d_apw = d_smoothstep(apw, d_w);
         float d_amw = -d_smoothstep(amw, d_w);
         float d_d = d_apw + d_amw;
@@ -635,7 +637,7 @@ DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 s
         float d_w = w > 0 ? (f.c.w / w) * d_ai : 0.f;
         d_ai *= w;
         d_paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS),
-                      pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr);
+                      pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr, true);
         float d_d = d_smoothstep(d, d_w);
         if (d < 0) d_d = -d_d;
         if (fabsf(d_d) > 1e-10f && f.within) d_group_distance(S, g, f.shape, pt, f.closest, f.info, d_d, dp, d_tr);

@@ -41,8 +41,8 @@ def estimate_device_bytes(packed, width, height, spp):
     params = 4 * P * 6                              # params, grads, m, v, lr scale, spare
     images = 16 * npx * 3 + 4 * npx                 # image, adjoint, target; weight image
     # forward sample colours; fragment cache per sample: 16 hit keys, or with
-    # prefiltering 12 fragments of 64 B, and a count
-    samples = 16 * n + ((12 * 64 if packed.use_prefiltering else 16 * 4) + 1) * n
+    # prefiltering 16 fragments of 64 B, and a count
+    samples = 16 * n + ((16 * 64 if packed.use_prefiltering else 16 * 4) + 1) * n
     edges = 68 * n                                  # boundary-sample records and ordering
     scene = 4 * (8 * ns + 12 * ng + 2 * nseg + 2 * ng) + 64 * ng + 40 * ns + 48 * nseg + 4 * (10 * nseg + 8 * ns)
     scene += (8 * 33 + 4 * 64) * nseg                # tabulated subdivision trees of the segments
