@@ -1483,11 +1483,12 @@ DN float4 paint_color(const DevScene &S, int kind, int off, int nstops, v2 pt) {
 
 DI void gadd(float *dp, int off, float v) { atomicAdd(dp + off, v); }
 // Accumulation of N consecutive parameters that many samples of a warp may
-// hit at once (a shape's parameters, a segment's points, a paint, a group
-// transform, where the warp's samples are neighbours): the lanes that add to
-// the same block at this point sum their values first and one of them adds
-// the sums.  Where the lanes' targets mostly differ the plain atomics are
-// faster.
+// hit at once (a circle's, ellipse's or rectangle's parameters and group
+// transform in the boundary pass; paints and group transforms in the
+// interior adjoints, whose warps hold neighbouring pixels): the lanes that
+// add to the same block at this point sum their values first and one of them
+// adds the sums.  Where the lanes' targets mostly differ (path points in the
+// boundary pass) the plain atomics are faster.
 template <int N>
 DI void gadd_shared(float *dp, int off, const float *v) {
   unsigned peers = __match_any_sync(__activemask(), off);
