@@ -345,7 +345,7 @@ def run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samp
             'api': 'RenderFunction.serialize_scene + apply + MSE + backward, scene tensors in host memory'}
 
 
-def run_configs(dev, steps=5, warmup=3):
+def run_configs(dev, steps=5, warmup=3, only=None):
     """Device-resident fwd+bwd Msamples/s of the other single-scene
     configurations, through the C ABI like the headline leg: the single
     circle (256x256, 2x2 spp; target: the circle at (120,140), radius 48,
@@ -368,6 +368,8 @@ def run_configs(dev, steps=5, warmup=3):
     flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)
     out = {}
     for name, ((w, h, shapes, groups), (tw, th, ts, tg), (nsx, nsy), seed, pf) in cases.items():
+        if only is not None and name != only:
+            continue
         packed = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=pf))
         tpacked = pack_scene(dvg.RenderFunction.serialize_scene(tw, th, ts, tg, use_prefiltering=pf))
         scene, tscene = _native.NativeScene(packed), _native.NativeScene(tpacked)
@@ -630,7 +632,14 @@ def main():
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--profile', action='store_true',
                     help='only the device-resident steps (for ncu captures): no e2e, batched, served or CPU legs')
+    ap.add_argument('--config', choices=['circle_256_2x2', 'fill_prefiltered_1024_1x1'],
+                    help='only this single-scene configuration (for ncu captures): target render, 3 warm-up '
+                         'and 5 timed fwd+bwd steps')
     args = ap.parse_args()
+    if args.config:
+        import torch
+        print(json.dumps({'configs': run_configs(torch.device('cuda', 0), only=args.config)}))
+        return
     if args.profile:
         args.no_batched = args.no_cpu_baseline = True
         args.no_e2e = True
