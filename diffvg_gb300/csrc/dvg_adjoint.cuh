@@ -93,35 +93,37 @@ DN void d_closest_path(const DevScene &S, int s, v2 pt, v2 d_cp, const PathInfo 
         double dF = u, dE = u * t, dD = dE * t, dC = dD * t, dB = dC * t;
         double dA = -(dB * q.B + dC * q.C + dD * q.D + dE * q.E + dF * q.F) * inv_a;
         dB *= inv_a; dC *= inv_a; dD *= inv_a; dE *= inv_a; dF *= inv_a;
-        // float += double updates round after every term
-#define ACC(dst, sc, vec) do { (dst).x = (float)((double)(dst).x + (sc) * (double)(vec).x); \
-                               (dst).y = (float)((double)(dst).y + (sc) * (double)(vec).y); } while (0)
-#define ACC2(dst, s0, v0, s1, v1) do { \
-    (dst).x = (float)((double)(dst).x + ((s0) * (double)(v0).x + (s1) * (double)(v1).x)); \
-    (dst).y = (float)((double)(dst).y + ((s0) * (double)(v0).y + (s1) * (double)(v1).y)); } while (0)
-        ACC(d0, dA * 3 * (-1) * 2, a);
-        ACC(d1, dA * 3 * 3 * 2, a);
-        ACC(d2, dA * 3 * (-3) * 2, a);
-        ACC(d3, dA * 3 * 1 * 2, a);
-        ACC(d0, dB * 5, add2(scl2(-1, b), scl2(3, a)));
-        ACC(d1, dB * 5, add2(scl2(3, b), scl2(-6, a)));
-        ACC(d2, dB * 5, add2(scl2(-3, b), scl2(3, a)));
-        ACC(d3, dB * 5, b);
-        ACC2(d0, dC * 4, add2(scl2(-1, c), scl2(-3, a)), dC * 2, scl2(3 * 2, b));
-        ACC2(d1, dC * 4, add2(scl2(3, c), scl2(3, a)), dC * 2, scl2(-6 * 2, b));
-        ACC2(d2, dC * 4, scl2(-3, c), dC * 2, scl2(3 * 2, b));
-        ACC(d3, dC * 4, c);
-        ACC2(d0, dD * 3, add2(scl2(3, c), scl2(-3, b)), dD * 3, add2(scl2(-1, e), scl2(1, a)));
-        ACC2(d1, dD * 3, add2(scl2(-6, c), scl2(3, b)), dD * 3, scl2(3, e));
-        ACC2(d2, dD * 3, scl2(3, c), dD * 3, scl2(-3, e));
-        ACC(*d_pt, dD * 3, scl2(-1, a));
-        ACC2(d0, dE, scl2(-3 * 2, c), dE * 2, add2(scl2(1, b), scl2(3, e)));
-        ACC2(d1, dE, scl2(3 * 2, c), dE * 2, scl2(-6, e));
-        ACC(d2, dE * 2, scl2(3, e));
-        ACC(*d_pt, dE * 2, scl2(-1, b));
-        ACC2(d0, dF, scl2(1, c), dF, scl2(-3, e));
-        ACC(d1, dF, scl2(3, e));
-        ACC(*d_pt, dF, scl2(-1, c));
+        // The control-point terms accumulate in fp32 (the reference adds double
+        // products to float accumulators; the two differ by fp32 rounding only,
+        // far inside the gradient tolerance, and fp64 runs at a small fraction
+        // of the fp32 rate here).
+        float fA = (float)dA, fB = (float)dB, fC = (float)dC, fD = (float)dD, fE = (float)dE, fF = (float)dF;
+#define ACC(dst, sc, vec) do { float s_ = (sc); (dst).x += s_ * (vec).x; (dst).y += s_ * (vec).y; } while (0)
+#define ACC2(dst, s0, v0, s1, v1) do { float a_ = (s0), b_ = (s1); \
+    (dst).x += a_ * (v0).x + b_ * (v1).x; (dst).y += a_ * (v0).y + b_ * (v1).y; } while (0)
+        ACC(d0, fA * 3 * (-1) * 2, a);
+        ACC(d1, fA * 3 * 3 * 2, a);
+        ACC(d2, fA * 3 * (-3) * 2, a);
+        ACC(d3, fA * 3 * 1 * 2, a);
+        ACC(d0, fB * 5, add2(scl2(-1, b), scl2(3, a)));
+        ACC(d1, fB * 5, add2(scl2(3, b), scl2(-6, a)));
+        ACC(d2, fB * 5, add2(scl2(-3, b), scl2(3, a)));
+        ACC(d3, fB * 5, b);
+        ACC2(d0, fC * 4, add2(scl2(-1, c), scl2(-3, a)), fC * 2, scl2(3 * 2, b));
+        ACC2(d1, fC * 4, add2(scl2(3, c), scl2(3, a)), fC * 2, scl2(-6 * 2, b));
+        ACC2(d2, fC * 4, scl2(-3, c), fC * 2, scl2(3 * 2, b));
+        ACC(d3, fC * 4, c);
+        ACC2(d0, fD * 3, add2(scl2(3, c), scl2(-3, b)), fD * 3, add2(scl2(-1, e), scl2(1, a)));
+        ACC2(d1, fD * 3, add2(scl2(-6, c), scl2(3, b)), fD * 3, scl2(3, e));
+        ACC2(d2, fD * 3, scl2(3, c), fD * 3, scl2(-3, e));
+        ACC(*d_pt, fD * 3, scl2(-1, a));
+        ACC2(d0, fE, scl2(-3 * 2, c), fE * 2, add2(scl2(1, b), scl2(3, e)));
+        ACC2(d1, fE, scl2(3 * 2, c), fE * 2, scl2(-6, e));
+        ACC(d2, fE * 2, scl2(3, e));
+        ACC(*d_pt, fE * 2, scl2(-1, b));
+        ACC2(d0, fF, scl2(1, c), fF, scl2(-3, e));
+        ACC(d1, fF, scl2(3, e));
+        ACC(*d_pt, fF, scl2(-1, c));
 #undef ACC
 #undef ACC2
       }
