@@ -2,9 +2,10 @@
 // filtered resolve, interior adjoint, boundary (edge-sampling) adjoint and
 // the signed-distance output.
 //
-// Work decomposition.  Colour kernels run one CTA per 16x16 image tile and
-// sub-sample index (blockIdx.y), one thread per pixel, so a warp covers two
-// adjacent pixel rows and shares its candidate list.  Sample colours go to a
+// Work decomposition.  Colour kernels run spp CTAs of 256 threads per 16x16
+// image tile; the tile's samples are numbered pixel-major with the pixels in
+// Morton order, so a warp holds all sub-samples of a compact pixel block
+// (4x2 pixels at 2x2 spp, 8x4 at 1 spp) and shares its candidate list.  Sample colours go to a
 // per-sample buffer and are filtered by a gather pass per pixel (the
 // reference splats them with float atomics, diffvg.cpp:1218-1249); the
 // image is written once, atomic-free and deterministic.  The boundary pass
@@ -62,11 +63,18 @@ __global__ void __launch_bounds__(256) k_weight(DevRender R0, const __grid_const
   R.weight[p] = ws;
 }
 
-// Pixel of thread i inside its 16x16 tile: each warp takes an 8x4 block
-// (the tile is 2 x 4 of them), a tighter patch than two 16-pixel rows, so
-// that the lanes of a warp meet more of the same segments.
-__device__ __forceinline__ int tile_px(int i) { return ((i >> 5) & 1) * 8 + (i & 7); }
-__device__ __forceinline__ int tile_py(int i) { return (i >> 6) * 4 + ((i >> 3) & 3); }
+// Sample of thread threadIdx.x in CTA blockIdx.y of its tile: the tile's
+// 256 * spp samples are numbered pixel-major, pixels in Morton order, so the
+// lanes of a warp hold neighbouring samples and meet the same segments.
+__device__ __forceinline__ int morton_x(int k) { return (k & 1) | ((k >> 1) & 2) | ((k >> 2) & 4) | ((k >> 3) & 8); }
+__device__ __forceinline__ int morton_y(int k) { return ((k >> 1) & 1) | ((k >> 2) & 2) | ((k >> 3) & 4) | ((k >> 4) & 8); }
+__device__ __forceinline__ void tile_sample(int spp, int &dx, int &dy, int &sub) {
+  int j = blockIdx.y * blockDim.x + threadIdx.x;
+  int k = j / spp;
+  sub = j - k * spp;
+  dx = morton_x(k);
+  dy = morton_y(k);
+}
 
 template <bool PREFILTER>
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
@@ -74,10 +82,12 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
   int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-  int px = tx * DVG_TILE + tile_px(threadIdx.x), py = ty * DVG_TILE + tile_py(threadIdx.x);
+  int dx, dy, sub;
+  tile_sample(R.spp, dx, dy, sub);
+  int px = tx * DVG_TILE + dx, py = ty * DVG_TILE + dy;
   bool active = px < R.w && py < R.h;
   if (PREFILTER && !active) return;
-  int idx = active ? (py * R.w + px) * R.spp + blockIdx.y : 0;
+  int idx = active ? (py * R.w + px) * R.spp + sub : 0;
   int x, y;
   v2 pt = sample_pos(R, idx, PREFILTER, x, y);
   v2 npt = V2(pt.x / R.w, pt.y / R.h);
@@ -142,10 +152,12 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   DevRender R = load_filter(R0, nullptr);
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
   int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-  int px = tx * DVG_TILE + tile_px(threadIdx.x), py = ty * DVG_TILE + tile_py(threadIdx.x);
+  int dx, dy, sub;
+  tile_sample(R.spp, dx, dy, sub);
+  int px = tx * DVG_TILE + dx, py = ty * DVG_TILE + dy;
   bool active = px < R.w && py < R.h && !bins_overflowed(S);
   float dfr = 0.f;
-  int idx = active ? (py * R.w + px) * R.spp + blockIdx.y : 0;
+  int idx = active ? (py * R.w + px) * R.spp + sub : 0;
   int x, y;
   v2 pt = sample_pos(R, idx, PREFILTER, x, y);
   v2 npt = V2(pt.x / R.w, pt.y / R.h);
