@@ -9,7 +9,7 @@
 // per-sample buffer and are filtered by a gather pass per pixel (the
 // reference splats them with float atomics, diffvg.cpp:1218-1249); the
 // image is written once, atomic-free and deterministic.  The boundary pass
-// runs one thread per boundary sample (diffvg.cpp:1325-1475).
+// runs one or two threads per boundary sample (diffvg.cpp:1325-1475).
 #include "dvg_internal.h"
 #include "dvg_sample.cuh"
 
