@@ -73,6 +73,18 @@ def test_estimate_grows_with_image_and_scene():
     assert a.device_bytes() < b.device_bytes() < c.device_bytes()
 
 
+def test_estimate_counts_the_prefiltered_fragment_cache():
+    """A prefiltered request caches 16 whole fragments of 64 B per sample for
+    its backward pass, a sampled one 16 fragment keys of 4 B."""
+    from diffvg_gb300.packing import pack_scene
+    w, h, shapes, groups = workloads.fill_scene(dvg, seed=3, num_paths=8, canvas=128)
+    plain = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups))
+    pref = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=True))
+    n = w * h
+    diff = serve.estimate_device_bytes(pref, w, h, 1) - serve.estimate_device_bytes(plain, w, h, 1)
+    assert diff == (16 * 64 - 16 * 4) * n
+
+
 def test_budget_serialises_requests_and_all_complete(server):
     reqs = [_req(i, 64, 8, 3) for i in range(4)]
     s = server(budget=int(reqs[0].device_bytes() * 1.5))
