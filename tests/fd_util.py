@@ -1,0 +1,124 @@
+"""Finite-difference checks of the renderer's gradients, shared by the oracle
+(CPU) and CUDA-path (GPU) tests.
+
+The image of a Monte-Carlo renderer is piecewise constant in the geometry at
+a fixed seed, so a raw finite difference of it is noise.  The estimators
+here are therefore explicit:
+
+- colour parameters: the image is smooth in them at a fixed seed, so one
+  central difference (h = 1e-2, loss summed in float64) is compared with the
+  analytic gradient at a 1e-3 relative tolerance;
+- geometry through the boundary (edge-sampling) term: central differences
+  with a step of a quarter pixel, with the same seed on both sides (the same
+  sample positions, so the difference counts the samples the boundary
+  sweeps), averaged over several seeds, against the analytic gradient
+  averaged over the same seeds;
+- prefiltered coverage: deterministic and smooth in the geometry, so one
+  central difference per parameter.
+
+The loss is L = sum(image * weights) with a fixed smooth weight image, whose
+gradient is the backward pass with d_image = weights.
+"""
+import numpy as np
+
+
+def weight_image(h, w):
+    """Smooth per-pixel, per-channel loss weights (a ramp, so that
+    translations of a shape change the loss)."""
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    ramp = 1.0 + x / w + 2.0 * y / h
+    ch = np.array([1.0, 0.5, 0.25, 0.1])
+    return (ramp[:, :, None] * ch[None, None, :]).astype(np.float32)
+
+
+def loss(image, weights):
+    return float(np.sum(image.astype(np.float64) * weights.astype(np.float64)))
+
+
+def slot_offset(packed, arg_index):
+    """Parameter-arena offset of the argument list entry arg_index."""
+    for sl in packed.slots:
+        if sl.arg_index == arg_index:
+            return sl.offset
+    raise KeyError(arg_index)
+
+
+def central_fd(fwd, P, index, h, weights, seeds):
+    """Mean over seeds of (L(P + h e_i) - L(P - h e_i)) / 2h."""
+    vals = []
+    for seed in seeds:
+        Pp = P.copy()
+        Pm = P.copy()
+        Pp[index] += h
+        Pm[index] -= h
+        vals.append((loss(fwd(Pp, seed), weights) - loss(fwd(Pm, seed), weights)) / (2.0 * h))
+    return float(np.mean(vals))
+
+
+def analytic(bwd, P, weights, seeds):
+    """Mean over seeds of the backward pass's gradient of L."""
+    return np.mean([bwd(P, seed, weights).astype(np.float64) for seed in seeds], axis=0)
+
+
+def rel_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def slot_of(packed, kind, nth=0):
+    """Arena offset of the nth parameter slot of the given kind."""
+    found = [sl for sl in packed.slots if sl.kind == kind]
+    return found[nth].offset
+
+
+def circle_case(m):
+    """A filled circle inside a 48x48 canvas, 4x4 spp."""
+    import torch
+    shapes = [m.Circle(radius=torch.tensor(12.0), center=torch.tensor([22.0, 25.0]))]
+    groups = [m.ShapeGroup(shape_ids=torch.tensor([0]), fill_color=torch.tensor([0.3, 0.6, 0.3, 1.0]))]
+    return 48, 48, shapes, groups, False, 4
+
+
+def prefiltered_polygon_case(m):
+    """A filled pentagon (lines) under prefiltering, 1 spp at pixel centres."""
+    import math
+    import torch
+    pts = [[24.0 + 15.0 * math.cos(0.3 + 2 * math.pi * k / 5), 24.0 + 13.0 * math.sin(0.3 + 2 * math.pi * k / 5)]
+           for k in range(5)]
+    shapes = [m.Polygon(points=torch.tensor(pts), is_closed=True)]
+    groups = [m.ShapeGroup(shape_ids=torch.tensor([0]), fill_color=torch.tensor([0.8, 0.3, 0.2, 1.0]))]
+    return 48, 48, shapes, groups, True, 1
+
+
+def run_checks(make_backend):
+    """Runs the three finite-difference checks through a backend factory:
+    make_backend(case_builder) -> (packed, P, fwd(P, seed) -> image,
+    bwd(P, seed, d_image) -> d_params).  Returns the relative errors."""
+    out = {}
+    # colour gradients of the circle at one seed
+    packed, P, fwd, bwd = make_backend(circle_case)
+    wts = weight_image(48, 48)
+    co = slot_of(packed, 'color')
+    g = analytic(bwd, P, wts, [1])
+    fd = [central_fd(fwd, P, co + k, 1e-2, wts, [1]) for k in range(4)]
+    out['color'] = rel_err(fd, g[co:co + 4])
+    # radius and centre through the boundary term, averaged over seeds
+    seeds = list(range(1, 9))
+    ro, ce = slot_of(packed, 'radius'), slot_of(packed, 'center')
+    g = analytic(bwd, P, wts, seeds)
+    idx = [ro, ce, ce + 1]
+    fd = [central_fd(fwd, P, i, 0.25, wts, seeds) for i in idx]
+    out['geometry'] = rel_err(fd, g[idx])
+    # prefiltered polygon: every vertex coordinate, deterministic.  Alpha
+    # only: the output colour is un-premultiplied, so a pixel's rgb jumps from
+    # 0 to the paint colour where its coverage leaves 0 (alpha is smooth).
+    packed, P, fwd, bwd = make_backend(prefiltered_polygon_case)
+    po = slot_of(packed, 'points')
+    wa = wts.copy()
+    wa[:, :, :3] = 0.0
+    g = analytic(bwd, P, wa, [0])
+    idx = list(range(po, po + 10))
+    fd = [central_fd(fwd, P, i, 1e-2, wa, [0]) for i in idx]
+    out['prefiltered_points'] = rel_err(fd, g[idx])
+    return out

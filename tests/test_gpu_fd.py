@@ -1,0 +1,36 @@
+"""The CUDA path's gradients against finite differences of its own forward
+pass, with the estimators and tolerances of the oracle's test
+(test_oracle_fd.py, fd_util): colour gradients at one seed, circle radius
+and centre through the boundary term averaged over 8 seeds, and the
+prefiltered coverage's vertex gradients."""
+import pytest
+
+import fd_util
+from test_oracle_fd import COLOR_TOL, GEOMETRY_TOL, PREFILTER_TOL
+
+pytestmark = pytest.mark.gpu
+
+
+def _cuda_backend(builder):
+    import diffvg_gb300 as dvg
+    from diffvg_gb300.packing import pack_scene
+    import oracle
+    import native_util as nu
+    w, h, shapes, groups, pf, spp = builder(dvg)
+    packed = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=pf))
+    P = oracle.params_of(packed)
+
+    def fwd(Pv, seed):
+        return nu.render(packed, Pv, w, h, spp, spp, seed)['image']
+
+    def bwd(Pv, seed, d):
+        return nu.render(packed, Pv, w, h, spp, spp, seed, d_out=d)['d_params']
+    return packed, P, fwd, bwd
+
+
+def test_cuda_gradients_match_finite_differences():
+    err = fd_util.run_checks(_cuda_backend)
+    print(err)
+    assert err['color'] <= COLOR_TOL
+    assert err['geometry'] <= GEOMETRY_TOL
+    assert err['prefiltered_points'] <= PREFILTER_TOL
