@@ -139,6 +139,20 @@ def _peaks():
         return 6800.0, 'fallback'
 
 
+def issue_roofline(warp_instructions, avg_launch_s, num_sms, sm_mhz):
+    """Issue-slot roofline of an instruction-bound kernel: warp instructions
+    per launch (from an ncu capture of the same workload) over the live
+    launch time, against 4 schedulers x 1 warp instruction per cycle per SM
+    at the sampled SM clock.  None when an input is missing."""
+    if not warp_instructions or not avg_launch_s or not num_sms or not sm_mhz:
+        return None
+    achieved = warp_instructions / avg_launch_s / 1e9
+    peak = 4.0 * num_sms * sm_mhz / 1e3
+    return {'achieved': round(achieved, 2), 'peak': round(peak, 2), 'unit': 'G warp instructions/s',
+            'frac': round(achieved / peak, 4), 'warp_instructions': int(warp_instructions),
+            'source': 'profiles/ncu_traffic.json (ncu smsp__inst_executed.sum per launch)'}
+
+
 def _ncu_traffic():
     """Per-launch DRAM bytes per kernel from the committed ncu summary."""
     try:
@@ -283,7 +297,13 @@ def run_ours(args):
                 'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 6),
                 'traffic': traffic, 'algorithmic_bytes': alg, 'avg_launch_ms': round(avg_s * 1e3, 4),
                 'note': 'the path is FP32/FP64-issue bound (no dense contraction); the HBM fraction is small by '
-                        'construction'}
+                        'construction, the issue-slot fraction is the binding one'}
+    try:
+        sm_mhz = clock_info.get('sm_mhz') or clock_info.get('sm_max_mhz') or 2070.0
+        roofline['issue'] = issue_roofline(_ncu_traffic().get(dom + '_warp_instructions'), avg_s,
+                                           torch.cuda.get_device_properties(dev).multi_processor_count, sm_mhz)
+    except Exception:
+        roofline['issue'] = None
 
     # ---------------- end to end through the public API ----------------
     e2e = None if getattr(args, 'no_e2e', False) else run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx,

@@ -48,3 +48,18 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setenv('WORLD_SIZE', '2')
     assert bench.run_reference(None) is None
     assert capsys.readouterr().out == ''
+
+
+def test_issue_roofline_arithmetic():
+    import bench
+    r = bench.issue_roofline(4.2e9, 13.8e-3, 152, 2070.0)
+    assert r['peak'] == pytest.approx(4 * 152 * 2.07)              # G warp instructions / s
+    assert r['achieved'] == pytest.approx(4.2e9 / 13.8e-3 / 1e9, rel=1e-3)
+    assert r['frac'] == pytest.approx(r['achieved'] / r['peak'], rel=1e-3)
+    assert bench.issue_roofline(None, 13.8e-3, 152, 2070.0) is None
+
+
+def test_committed_profile_figures_are_present():
+    import bench
+    t = bench._ncu_traffic()
+    assert t.get('edge', 0) > 0 and t.get('edge_warp_instructions', 0) > 0
