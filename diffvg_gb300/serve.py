@@ -75,6 +75,16 @@ class Request:
         self.result = None       # final parameter arena (host tensor)
         self.step_ms = []
 
+    @classmethod
+    def from_svg(cls, filename, target, steps, use_prefiltering=False, **kw):
+        """A request whose scene is read from an SVG file (svg_to_scene); the
+        other arguments are those of Request."""
+        from .parse_svg import svg_to_scene
+        from .render_pytorch import RenderFunction
+        w, h, shapes, groups = svg_to_scene(filename)
+        args = RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=use_prefiltering)
+        return cls(args, target, steps, **kw)
+
     def device_bytes(self):
         return estimate_device_bytes(self.packed, self.size[0], self.size[1],
                                      self.num_samples[0] * self.num_samples[1])

@@ -126,3 +126,17 @@ def test_slot_limit(server):
     for i in range(5):
         s.submit(_req(i, 64, 8, 2))
     assert s.tick() == 2
+
+
+def test_request_from_svg_is_served(server, tmp_path):
+    """A request read from an SVG file goes through admission and completes."""
+    svg = tmp_path / 'req.svg'
+    svg.write_text('<svg xmlns="http://www.w3.org/2000/svg" width="32" height="24">'
+                   '<path d="M2 2 C10 0 20 8 28 20" fill="none" stroke="#ff0000" stroke-width="3"/>'
+                   '<circle cx="16" cy="12" r="5" fill="blue"/></svg>')
+    req = serve.Request.from_svg(str(svg), torch.zeros(24, 32, 4), 2)
+    assert req.size == (32, 24) and req.packed.num_shapes == 2
+    srv = server(budget=1 << 40)
+    assert srv.submit(req)
+    srv.run()
+    assert srv.completed == [req] and len(req.step_ms) == 2
