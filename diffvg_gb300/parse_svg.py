@@ -342,9 +342,10 @@ def parse_shape(node, transform, fill_color, shapes, shape_groups, defs):
             p.id = '{}-{}'.format(name, k) if len(paths) > 1 else name
         shapes = _group(shapes, shape_groups, paths, fill, stroke, even_odd, xform, name, with_xform=False)
     elif tag == 'polygon':
-        items = [x for x in node.attrib['points'].strip().split(' ') if x]
-        pts = [[float(v) for v in re.split(',| ', x)] for x in items]
-        poly = Polygon(torch.tensor(pts, dtype=torch.float32).view(-1, 2), fill is not None)
+        # coordinates separated by spaces and / or commas, read in pairs (the
+        # reference reads "x,y x,y ..." and "x y x y ..." the same way)
+        nums = [float(v) for v in re.split(r'[\s,]+', node.attrib['points'].strip()) if v]
+        poly = Polygon(torch.tensor(nums, dtype=torch.float32).view(-1, 2), fill is not None)
         poly.stroke_width = width
         shapes = _group(shapes, shape_groups, [poly], fill, stroke, even_odd, xform, name)
     elif tag == 'line':

@@ -203,3 +203,41 @@ def test_parsed_scene_renders_like_the_hand_built_one(tmp_path):
         imgs.append(oracle.render(packed, oracle.params_of(packed), w, h, 2, 2, 5)['image'])
     assert np.array_equal(imgs[0], imgs[1])
     assert imgs[0][..., 3].max() > 0.9
+
+
+def test_transforms_viewbox_and_inheritance(tmp_path):
+    svg = ('<svg xmlns="http://www.w3.org/2000/svg" viewBox="0 0 40 30" width="400">'
+           '<g fill="rgb(255,128,0)" transform="matrix(1 0 0 1 2 3)">'
+           '<g transform="scale(2)"><path d="M0 0 L1 0 L1 1 Z M5 5 L6 5 L6 6 Z" stroke="#000" stroke-opacity="0.25"/></g>'
+           '<polygon points="0 0,4 0 4,4" transform="skewX(45)"/></g>'
+           '<circle cx="1" cy="2" r="3" fill="chartreuse"/></svg>')
+    with pytest.warns(UserWarning):
+        w, h, shapes, groups = dvg.svg_to_scene(_write(tmp_path, svg))
+    assert (w, h) == (40, 30)                                   # the viewBox wins over width
+    # one path element with two subpaths: two shapes in one group, points in canvas space
+    assert groups[0].shape_ids.tolist() == [0, 1]
+    assert _pts(shapes[0]) == [[2.0, 3.0], [4.0, 3.0], [4.0, 5.0]]
+    assert _pts(shapes[1])[0] == [12.0, 13.0]
+    assert groups[0].fill_color.tolist() == pytest.approx([1.0, 128 / 255, 0.0, 1.0])
+    assert groups[0].stroke_color.tolist() == pytest.approx([0.0, 0.0, 0.0, 0.25])
+    # the polygon's group carries matrix x skewX; its points stay local
+    m = groups[1].shape_to_canvas.numpy()
+    assert np.allclose(m, [[1.0, 1.0, 2.0], [0.0, 1.0, 3.0], [0.0, 0.0, 1.0]], atol=1e-6)
+    assert _pts(shapes[2]) == [[0.0, 0.0], [4.0, 0.0], [4.0, 4.0]] and shapes[2].is_closed
+    # an unknown colour name warns and stays black
+    assert groups[2].fill_color.tolist() == [0.0, 0.0, 0.0, 1.0]
+
+
+def test_save_svg_gamma_and_path_commands(tmp_path):
+    shapes = [dvg.Path(num_control_points=torch.tensor([0, 1, 2], dtype=torch.int32),
+                       points=torch.tensor([[0.0, 0.0], [4.0, 0.0], [6.0, 2.0], [4.0, 4.0], [2.0, 6.0], [0.0, 5.0]]),
+                       is_closed=True)]
+    groups = [dvg.ShapeGroup(shape_ids=torch.tensor([0]), fill_color=torch.tensor([0.0, 0.0, 1.0, 1.0]))]
+    f = str(tmp_path / 'g.svg')
+    dvg.save_svg(f, 8, 8, shapes, groups, use_gamma=True)
+    text = open(f).read()
+    assert 'feComponentTransfer' in text and 'filter:url(#gamma)' in text
+    assert 'M 0.0 0.0 L 4.0 0.0 Q 6.0 2.0 4.0 4.0 C 2.0 6.0 0.0 5.0 0.0 0.0' in text
+    w, h, s2, g2 = dvg.svg_to_scene(f)
+    assert s2[0].num_control_points.tolist() == [0, 1, 2] and s2[0].is_closed
+    assert _pts(s2[0]) == _pts(shapes[0])
