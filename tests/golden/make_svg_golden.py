@@ -2,7 +2,9 @@
 
 Runs the reference's pydiffvg/parse_svg.py (its svg_to_scene and, through
 pydiffvg/shape.py, its from_svg_path) on the documents of tests/svg_cases.py
-and stores each parsed scene as plain lists.  The reference imports three
+and stores each parsed scene as plain lists; runs the reference's
+pydiffvg/save_svg.py on the scenes of svg_cases.save_scenes and stores the
+documents it writes (tests/golden/svg_saved.json).  The reference imports three
 packages that are not installed here; they are stood in for:
 
 - svgpathtools: path data is read by diffvg_gb300.svg_path, wrapped in the
@@ -111,9 +113,20 @@ def load_reference_reader(ref_dir):
     return mod
 
 
+def load_reference_writer(ref_dir):
+    path = os.path.join(ref_dir, 'pydiffvg', 'save_svg.py')
+    spec = importlib.util.spec_from_file_location('pydiffvg.save_svg', path)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules['pydiffvg.save_svg'] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else ref_loader.DEFAULT_REF
     reader = load_reference_reader(ref)
+    writer = load_reference_writer(ref)
+    pyd = sys.modules['pydiffvg']
     out = {}
     with tempfile.TemporaryDirectory() as d:
         for name, text in svg_cases.CASES.items():
@@ -121,10 +134,20 @@ def main():
             with open(f, 'w') as fh:
                 fh.write(text)
             out[name] = svg_cases.describe(*reader.svg_to_scene(f))
+        saved = {}
+        for name, (w, h, shapes, groups, gamma) in svg_cases.save_scenes(pyd).items():
+            f = os.path.join(d, 'saved_' + name + '.svg')
+            writer.save_svg(f, w, h, shapes, groups, use_gamma=gamma)
+            with open(f) as fh:
+                saved[name] = fh.read()
     path = os.path.join(HERE, 'svg_scenes.json')
     with open(path, 'w') as fh:
         json.dump(out, fh, indent=1)
     print('%s: %d scenes, %d bytes' % (path, len(out), os.path.getsize(path)))
+    path = os.path.join(HERE, 'svg_saved.json')
+    with open(path, 'w') as fh:
+        json.dump(saved, fh, indent=1)
+    print('%s: %d documents, %d bytes' % (path, len(saved), os.path.getsize(path)))
 
 
 if __name__ == '__main__':

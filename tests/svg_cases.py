@@ -79,3 +79,25 @@ def describe(width, height, shapes, groups):
                               'stroke': _paint(g.stroke_color), 'even_odd': bool(g.use_even_odd_rule),
                               'shape_to_canvas': _t(g.shape_to_canvas)})
     return out
+
+
+def save_scenes(m):
+    """Scenes for the writer's parity fixtures, built with module m's classes:
+    name -> (width, height, shapes, shape_groups, use_gamma)."""
+    import torch
+    t = torch.tensor
+    shapes = [m.Circle(radius=t(10.0), center=t([20.0, 22.0]), stroke_width=t(1.5)),
+              m.Path(num_control_points=t([0, 1, 2], dtype=torch.int32),
+                     points=t([[0.0, 0.0], [4.0, 0.0], [6.0, 2.0], [4.0, 4.0], [2.0, 6.0], [0.0, 5.0]]),
+                     is_closed=True, stroke_width=t(0.5)),
+              m.Polygon(points=t([[1.0, 2.0], [30.0, 4.0], [5.0, 30.0]]), is_closed=True, stroke_width=t(1.0)),
+              m.Rect(p_min=t([3.0, 4.0]), p_max=t([13.0, 24.0]), stroke_width=t(2.0)),
+              m.Ellipse(radius=t([6.0, 3.0]), center=t([30.0, 10.0]))]
+    groups = [m.ShapeGroup(shape_ids=t([0]), fill_color=t([0.2, 0.4, 0.6, 0.8]), stroke_color=t([1.0, 0.0, 0.0, 1.0])),
+              m.ShapeGroup(shape_ids=t([1]),
+                           fill_color=m.LinearGradient(begin=t([0.0, 0.0]), end=t([10.0, 10.0]), offsets=t([0.0, 1.0]),
+                                                       stop_colors=t([[1.0, 0.0, 0.0, 1.0], [0.0, 0.0, 1.0, 0.5]]))),
+              m.ShapeGroup(shape_ids=t([2]), fill_color=None, stroke_color=t([0.0, 1.0, 0.0, 1.0])),
+              m.ShapeGroup(shape_ids=t([3]), fill_color=t([0.5, 0.5, 0.5, 1.0])),
+              m.ShapeGroup(shape_ids=t([4]), fill_color=t([0.1, 0.9, 0.3, 0.6]))]
+    return {'plain': (48, 40, shapes, groups, False), 'gamma': (48, 40, shapes[:2], groups[:2], True)}

@@ -1,7 +1,9 @@
-"""The SVG scene reader against the reference's own reader
-(tests/golden/svg_scenes.json, made by tests/golden/make_svg_golden.py):
-shape kinds and parameters, subpath closing, arcs as cubic pieces, paints,
-fill rules and group transforms, within 1e-5 for every float."""
+"""The SVG scene reader and writer against the reference's own
+(tests/golden/svg_scenes.json and svg_saved.json, made by
+tests/golden/make_svg_golden.py): the reader's shape kinds and parameters,
+subpath closing, arcs as cubic pieces, paints, fill rules and group
+transforms within 1e-5 for every float; the writer's documents byte for
+byte."""
 import json
 import os
 
@@ -38,3 +40,16 @@ def test_svg_reader_matches_the_reference(name, tmp_path):
     f.write_text(svg_cases.CASES[name])
     got = svg_cases.describe(*dvg.svg_to_scene(str(f)))
     _same(got, GOLDEN[name], name)
+
+
+with open(os.path.join(HERE, 'golden', 'svg_saved.json')) as f:
+    SAVED = json.load(f)
+
+
+@pytest.mark.parametrize('name', sorted(SAVED))
+def test_svg_writer_matches_the_reference(name, tmp_path):
+    """save_svg writes the reference's document, byte for byte."""
+    w, h, shapes, groups, gamma = svg_cases.save_scenes(dvg)[name]
+    f = tmp_path / (name + '.svg')
+    dvg.save_svg(str(f), w, h, shapes, groups, use_gamma=gamma)
+    assert f.read_text() == SAVED[name]
