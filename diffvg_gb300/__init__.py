@@ -4,8 +4,8 @@ hot path behind pydiffvg's API.
 ``import diffvg_gb300 as pydiffvg`` gives the scene classes (Circle,
 Ellipse, Path, Polygon, Rect, ShapeGroup), paints (LinearGradient,
 RadialGradient), PixelFilter, the device switches and RenderFunction with
-pydiffvg's signatures, and the SVG scene I/O (svg_to_scene, save_svg,
-from_svg_path).  Rendering runs the hand-written CUDA kernels of
+pydiffvg's signatures, the SVG scene I/O (svg_to_scene, save_svg,
+from_svg_path) and imwrite (PNG).  Rendering runs the hand-written CUDA kernels of
 libdiffvg_gb300.so through its C ABI (include/diffvg_gb300.h); there is no
 CPU fallback.
 """
@@ -17,6 +17,7 @@ from .diffvg import ShapeType, ColorType, FilterType
 from .render_pytorch import RenderFunction, OutputType, set_print_timing, clear_scene_cache
 from .parse_svg import svg_to_scene
 from .save_svg import save_svg
+from .image import imwrite
 from . import diffvg
 
 __version__ = '0.1.0'
