@@ -31,3 +31,14 @@ def test_oracle_gradients_match_finite_differences():
     assert err['color'] <= COLOR_TOL
     assert err['geometry'] <= GEOMETRY_TOL
     assert err['prefiltered_points'] <= PREFILTER_TOL
+
+
+STROKE_WIDTH_TOL = 5e-2     # 8 seeds, quarter-pixel steps
+GRADIENT_PAINT_TOL = 1e-2   # smooth at a fixed seed (observed 6.9e-4)
+
+
+def test_oracle_stroke_width_and_gradient_paint_match_finite_differences():
+    err = fd_util.run_extra_checks(_oracle_backend)
+    print(err)
+    assert err['stroke_width'] <= STROKE_WIDTH_TOL
+    assert err['linear_gradient'] <= GRADIENT_PAINT_TOL
