@@ -100,11 +100,20 @@ extern "C" int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRen
   if ((reinterpret_cast<uintptr_t>(image) & 15u) || (a->background && (reinterpret_cast<uintptr_t>(a->background) & 15u)))
     return dvg::fail(DVG_ERR_INVALID, "image and background must be 16-byte aligned");
   int G = desc->num_groups, NS = desc->num_shapes, NSEG = desc->total_segments, NGS = desc->total_group_shapes;
-  for (int g = 0, run = 0; g < G; g++) {
-    const int32_t *gi = desc->group_info + (size_t)g * DVG_GROUP_INFO_STRIDE;
-    if (gi[DVG_GROUP_SHAPES_OFF] != run)
-      return dvg::fail(DVG_ERR_INVALID, "the allocation-free render needs group shape lists stored in group order");
-    run += gi[DVG_GROUP_NUM_SHAPES];
+  if (a->flags & DVG_FLAG_NO_SYNC)
+    return dvg::fail(DVG_ERR_INVALID,
+                     "the allocation-free render has no scene handle to latch device errors in: DVG_FLAG_NO_SYNC "
+                     "is not accepted");
+  {
+    int run = 0;
+    for (int g = 0; g < G; g++) {
+      const int32_t *gi = desc->group_info + (size_t)g * DVG_GROUP_INFO_STRIDE;
+      if (gi[DVG_GROUP_SHAPES_OFF] != run)
+        return dvg::fail(DVG_ERR_INVALID, "the allocation-free render needs group shape lists stored in group order");
+      run += gi[DVG_GROUP_NUM_SHAPES];
+    }
+    if (run != NGS)
+      return dvg::fail(DVG_ERR_INVALID, "group shape lists cover %d entries of group_shapes, not all %d", run, NGS);
   }
   long long npx = (long long)a->width * a->height, n = npx * a->num_samples_x * a->num_samples_y;
   if (n > 0x7fffffffLL) return dvg::fail(DVG_ERR_INVALID, "more than 2^31-1 samples per call");
@@ -147,6 +156,8 @@ extern "C" int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRen
   for (auto &u : ups)
     if (u.bytes && e == cudaSuccess) e = cudaMemcpyAsync(base + u.off, u.src, u.bytes, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(base + o_err, 0, 4 * sizeof(unsigned), s);
+  // segments outside any path keep first point 0, as in the allocating path
+  if (e == cudaSuccess && NSEG > 0) e = cudaMemsetAsync(base + o_seg_point, 0, sizeof(int) * NSEG, s);
   if (e != cudaSuccess) return dvg::cuda_fail(e, "staging the scene in the static scratch");
 
   DevScene S;
@@ -229,7 +240,6 @@ extern "C" int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRen
     }
   }
   if (e != cudaSuccess) return dvg::cuda_fail(e, "allocation-free forward launch");
-  if (a->flags & DVG_FLAG_NO_SYNC) return DVG_OK;
   unsigned bits = 0;
   e = cudaMemcpyAsync(&bits, base + o_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

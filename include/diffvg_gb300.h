@@ -213,7 +213,10 @@ int dvg_adam_step(float *params, const float *grads, float *m, float *v, const f
  * lists, weight image, per-sample colours) lives in one static 16 MiB device
  * array inside the library, held by every GPU that loads it until exit;
  * calls needing more return DVG_ERR_CAPACITY.  Group shape lists must be
- * stored in group order (as serialize_scene produces them).  Every call
+ * stored in group order (as serialize_scene produces them) and cover all of
+ * group_shapes.  The call waits for its stream and reports device-side
+ * failures itself: with no scene handle to latch them in, DVG_FLAG_NO_SYNC
+ * is rejected with DVG_ERR_INVALID.  Every call
  * shares that array: calls that overlap on the GPU race.  The first call on
  * a device looks up the array's address; make it before any stream capture. */
 int dvg_render_forward_noalloc(const DvgSceneDesc *desc, const DvgRenderArgs *args, float *image, void *stream);

@@ -10,7 +10,12 @@ because shape.py imports it at module level for from_svg_path only.
 
 Used only to generate and check golden fixtures in this build container; the
 GPU machine has no reference checkout, so nothing on the GPU test / bench path
-imports this module.
+imports this module.  The checkout's location comes from DVG_REFERENCE_DIR,
+else from oracle/build_ref.sh (the recipe that compiles it).
+
+variant "defined" loads the module that build_ref.sh builds with the
+reference's one uninitialised read (the quintic isolator's interval slot)
+given a value; one process loads one variant.
 """
 import glob
 import importlib.util
@@ -20,17 +25,25 @@ import sys
 import types
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = os.environ.get('DVG_REFERENCE_DIR', '/root/reference')
+BUILD_SCRIPT = os.path.join(HERE, 'build_ref.sh')
+OUT_DIRS = {'stock': '_ref', 'defined': '_ref_defined'}
 
 
-def available(ref_dir=DEFAULT_REF):
-    return os.path.isfile(os.path.join(ref_dir, 'diffvg.cpp'))
+def reference_dir():
+    d = os.environ.get('DVG_REFERENCE_DIR')
+    if d:
+        return d
+    return subprocess.check_output(['bash', BUILD_SCRIPT, '--print-ref-dir'], text=True).strip()
 
 
-def build(ref_dir=DEFAULT_REF):
-    env = dict(os.environ, DVG_REFERENCE_DIR=ref_dir)
-    subprocess.check_call(['bash', os.path.join(HERE, 'build_ref.sh')], env=env)
-    libs = glob.glob(os.path.join(HERE, '_ref', 'diffvg*.so'))
+def available(ref_dir=None):
+    return os.path.isfile(os.path.join(ref_dir or reference_dir(), 'diffvg.cpp'))
+
+
+def build(ref_dir=None, variant='stock'):
+    env = dict(os.environ, DVG_REFERENCE_DIR=ref_dir or reference_dir(), DVG_REF_VARIANT=variant)
+    subprocess.check_call(['bash', BUILD_SCRIPT], env=env)
+    libs = glob.glob(os.path.join(HERE, OUT_DIRS[variant], 'diffvg*.so'))
     if not libs:
         raise RuntimeError('reference module was not built')
     return libs[0]
@@ -39,12 +52,15 @@ def build(ref_dir=DEFAULT_REF):
 _cached = None
 
 
-def load(ref_dir=DEFAULT_REF):
+def load(ref_dir=None, variant='stock'):
     """Returns (pydiffvg, diffvg) from the reference, CPU mode."""
     global _cached
     if _cached is not None:
-        return _cached
-    so = build(ref_dir)
+        if _cached[2] != variant:
+            raise RuntimeError('one reference variant per process')
+        return _cached[:2]
+    ref_dir = ref_dir or reference_dir()
+    so = build(ref_dir, variant)
     spec = importlib.util.spec_from_file_location('diffvg', so)
     native = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(native)
@@ -64,5 +80,5 @@ def load(ref_dir=DEFAULT_REF):
             if not k.startswith('__'):
                 setattr(pkg, k, v)
     pkg.set_use_gpu(False)
-    _cached = (pkg, native)
-    return _cached
+    _cached = (pkg, native, variant)
+    return pkg, native

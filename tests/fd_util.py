@@ -151,13 +151,9 @@ def run_extra_checks(make_backend):
     linear-gradient parameters (smooth at a fixed seed).
 
     A stroke's control-point gradients are not compared: the reference's
-    boundary samples lie at +-r along each segment's normal, so the round
-    caps of open paths and the round joins at corners are never sampled,
-    and its control-point gradients differ from finite differences where
-    those arcs move (measured on a closed two-cubic path with two corners:
-    the analytic values are a fraction of the finite differences; filled
-    paths agree within 1.1 %).  The renderer reproduces the reference's
-    estimator."""
+    boundary term for stroke geometry leaves out the offset curves' length
+    factor (see the notes above run_paint_checks), and the renderer
+    reproduces the reference's estimator."""
     out = {}
     wts = weight_image(48, 48)
     packed, P, fwd, bwd = make_backend(stroke_case)
@@ -172,4 +168,129 @@ def run_extra_checks(make_backend):
     g = analytic(bwd, P, wts, [3])
     fd = [central_fd(fwd, P, i, 1e-2, wts, [3]) for i in idx]
     out['linear_gradient'] = rel_err(fd, g[idx])
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Every paint kind on fills and on strokes.  The reference renders gradient
+# strokes wrongly and crashes in their backward pass (scene.cpp:866-869
+# stores the d_color buffer over the stroke colour), so for gradient-coloured
+# strokes finite differences are the only check.
+#
+# What finite differences can hold the reference's estimator to, and what
+# not (this project reproduces the estimator, so the same holds here):
+# - paint parameters (interior term): exact, except that the radial
+#   gradient's adjoint also adds d_color to its last stop for every sample
+#   (diffvg.cpp:441-499 has no return after the matching stop), so the last
+#   stop's colour is left out for radial paints;
+# - a stroke's width (boundary term): exact;
+# - a stroke's geometry (points, centre, radius, group transform) through the
+#   boundary term: biased.  The boundary samples sit at +-r along the centre
+#   line's normal with the centre line's length density, without the offset
+#   curve's length factor (1 +- r * curvature); a circle stroke's centre
+#   gradient comes out at half its finite difference, for instance, and its
+#   radius gradient adds the inner edge with the outer edge's sign
+#   (diffvg.cpp:149-156).  Not compared.
+# - path points under a non-identity group transform: the boundary term
+#   takes the points' velocity in shape space as canvas velocity
+#   (diffvg.cpp:168-270 ignore shape_to_canvas).  Not compared.
+
+def _linear(m):
+    import torch
+    return m.LinearGradient(begin=torch.tensor([8.0, 10.0]), end=torch.tensor([40.0, 36.0]),
+                            offsets=torch.tensor([0.0, 0.45, 1.0]),
+                            stop_colors=torch.tensor([[1.0, 0.0, 0.0, 1.0], [0.0, 1.0, 0.0, 0.8],
+                                                      [0.0, 0.0, 1.0, 1.0]]))
+
+
+def _radial(m):
+    import torch
+    return m.RadialGradient(center=torch.tensor([22.0, 26.0]), radius=torch.tensor([17.0, 12.0]),
+                            offsets=torch.tensor([0.0, 0.6, 1.0]),
+                            stop_colors=torch.tensor([[0.9, 0.8, 0.1, 1.0], [0.1, 0.3, 0.9, 0.7],
+                                                      [0.6, 0.1, 0.2, 1.0]]))
+
+
+def _paint(m, kind):
+    import torch
+    if kind == 'constant':
+        return torch.tensor([0.2, 0.5, 0.9, 0.9])
+    return _linear(m) if kind == 'linear' else _radial(m)
+
+
+def loop_points(cx=24.0, cy=24.0, r=14.0):
+    """A closed smooth loop of four cubic segments (a circle approximation)."""
+    k = 0.5523 * r
+    return [[cx + r, cy], [cx + r, cy + k], [cx + k, cy + r], [cx, cy + r], [cx - k, cy + r], [cx - r, cy + k],
+            [cx - r, cy], [cx - r, cy - k], [cx - k, cy - r], [cx, cy - r], [cx + k, cy - r], [cx + r, cy - k]]
+
+
+def paint_case(kind, stroke):
+    """Builder of a 48x48, 2x2-spp scene: a rect filled with `kind` paint, or
+    an open cubic path stroked with it (half width 3)."""
+    def build(m):
+        import torch
+        if stroke:
+            pts = torch.tensor([[6.0, 30.0], [14.0, 6.0], [30.0, 42.0], [42.0, 14.0]])
+            shapes = [m.Path(num_control_points=torch.tensor([2], dtype=torch.int32), points=pts, is_closed=False,
+                             stroke_width=torch.tensor(3.0))]
+            groups = [m.ShapeGroup(shape_ids=torch.tensor([0]), fill_color=None, stroke_color=_paint(m, kind))]
+        else:
+            shapes = [m.Rect(p_min=torch.tensor([4.0, 6.0]), p_max=torch.tensor([44.0, 42.0]))]
+            groups = [m.ShapeGroup(shape_ids=torch.tensor([0]), fill_color=_paint(m, kind))]
+        return 48, 48, shapes, groups, False, 2
+    build.__name__ = '%s_%s' % ('stroke' if stroke else 'fill', kind)
+    return build
+
+
+def transformed_gradient_stroke_case(m):
+    """The closed loop stroked (half width 2.5) with a radial gradient, in a
+    group with a rotated, scaled and translated shape_to_canvas; 4x4 spp."""
+    import math
+    import torch
+    c, s = math.cos(0.3), math.sin(0.3)
+    xf = torch.tensor([[1.1 * c, -0.9 * s, 2.0], [1.1 * s, 0.9 * c, -1.5], [0.0, 0.0, 1.0]])
+    shapes = [m.Path(num_control_points=torch.full((4,), 2, dtype=torch.int32),
+                     points=torch.tensor(loop_points()), is_closed=True, stroke_width=torch.tensor(2.5))]
+    groups = [m.ShapeGroup(shape_ids=torch.tensor([0]), fill_color=None, stroke_color=_radial(m),
+                           shape_to_canvas=xf)]
+    return 48, 48, shapes, groups, False, 4
+
+
+def _paint_indices(packed, kind):
+    """Arena offsets of the scene's one paint's parameters (for a radial
+    gradient without its last stop's colour, see above)."""
+    if kind == 'constant':
+        co = slot_of(packed, 'color')
+        return list(range(co, co + 4))
+    gb = slot_of(packed, 'gradient_geometry')  # begin/end or center/radius
+    so, sc = slot_of(packed, 'stop_offsets'), slot_of(packed, 'color')
+    last = 8 if kind == 'radial' else 12
+    return list(range(gb, gb + 4)) + list(range(so, so + 3)) + list(range(sc, sc + last))
+
+
+def run_paint_checks(make_backend):
+    """Paint parameters of constant / linear / radial paint on a fill and on a
+    stroke (smooth at a fixed seed: one central difference, h = 1e-2), and a
+    radial-gradient stroke in a transformed group: its paint parameters, and
+    its stroke width through the boundary term (quarter-pixel steps averaged
+    over 8 seeds).  Returns the relative errors by case name."""
+    out = {}
+    wts = weight_image(48, 48)
+    for stroke in (False, True):
+        for kind in ('constant', 'linear', 'radial'):
+            builder = paint_case(kind, stroke)
+            packed, P, fwd, bwd = make_backend(builder)
+            idx = _paint_indices(packed, kind)
+            g = analytic(bwd, P, wts, [3])
+            fd = [central_fd(fwd, P, i, 1e-2, wts, [3]) for i in idx]
+            out[builder.__name__] = rel_err(fd, g[idx])
+    packed, P, fwd, bwd = make_backend(transformed_gradient_stroke_case)
+    idx = _paint_indices(packed, 'radial')
+    g = analytic(bwd, P, wts, [3])
+    out['transformed_radial_stroke_paint'] = rel_err([central_fd(fwd, P, i, 1e-2, wts, [3]) for i in idx], g[idx])
+    seeds = list(range(1, 9))
+    sw = slot_of(packed, 'stroke_width')
+    g = analytic(bwd, P, wts, seeds)
+    out['transformed_radial_stroke_width'] = rel_err([central_fd(fwd, P, sw, 0.25, wts, seeds)], g[[sw]])
     return out

@@ -76,7 +76,7 @@ def run_case(pyd, case):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else ref_loader.DEFAULT_REF
+    ref = sys.argv[1] if len(sys.argv) > 1 else ref_loader.reference_dir()
     only = set(sys.argv[2:])
     pyd, _ = ref_loader.load(ref)
     for builder in scenes.CASES:

@@ -123,7 +123,7 @@ def load_reference_writer(ref_dir):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else ref_loader.DEFAULT_REF
+    ref = sys.argv[1] if len(sys.argv) > 1 else ref_loader.reference_dir()
     reader = load_reference_reader(ref)
     writer = load_reference_writer(ref)
     pyd = sys.modules['pydiffvg']

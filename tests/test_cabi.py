@@ -50,3 +50,37 @@ def test_create_rejects_malformed_scene_without_touching_the_device():
     st = lib.dvg_scene_create(ctypes.byref(desc), ctypes.byref(h))
     assert st == _native.DVG_ERR_INVALID
     assert b'canvas' in lib.dvg_last_error()
+
+
+def _noalloc_call(packed, extra_group_shapes=0, flags=0):
+    """Calls dvg_render_forward_noalloc with a description that fails a host
+    check, so that it returns before any CUDA call (no GPU needed)."""
+    import numpy as np
+    lib = _native.load()
+    lib.dvg_render_forward_noalloc.argtypes = [ctypes.POINTER(_native.SceneDesc), ctypes.POINTER(_native.RenderArgs),
+                                               ctypes.c_void_p, ctypes.c_void_p]
+    ip = ctypes.POINTER(ctypes.c_int32)
+    gs = np.concatenate([packed.group_shapes.reshape(-1), np.zeros(extra_group_shapes)]).astype(np.int32)
+    arrs = [np.ascontiguousarray(x.reshape(-1), dtype=np.int32) for x in
+            (packed.shape_info, packed.segment_ctrl, packed.group_info)] + [gs]
+    desc = _native.SceneDesc(packed.canvas_width, packed.canvas_height, packed.num_shapes, packed.num_groups,
+                             packed.num_params, int(packed.segment_ctrl.size), int(gs.size), int(packed.filter_type),
+                             int(packed.filter_radius_off), *[a.ctypes.data_as(ip) for a in arrs])
+    dummy = np.zeros(64, np.float32)  # never dereferenced: the call fails on the host first
+    args = _native.RenderArgs(16, 16, 1, 1, 0, 0, 0, dummy.ctypes.data, None, None, flags)
+    st = lib.dvg_render_forward_noalloc(ctypes.byref(desc), ctypes.byref(args), dummy.ctypes.data, None)
+    return st, lib.dvg_last_error()
+
+
+def test_noalloc_host_checks_without_gpu():
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import workloads
+    from diffvg_gb300.packing import pack_scene
+    w, h, shapes, groups = workloads.stroke_scene(dvg, seed=1, num_paths=8, canvas=64)
+    packed = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups))
+    # unused entries at the end of group_shapes would leave boundary pairs unset
+    st, msg = _noalloc_call(packed, extra_group_shapes=3)
+    assert st == _native.DVG_ERR_INVALID and b'group_shapes' in msg
+    # errors found on the device could not be latched anywhere
+    st, msg = _noalloc_call(packed, flags=_native.DVG_FLAG_NO_SYNC)
+    assert st == _native.DVG_ERR_INVALID and b'NO_SYNC' in msg

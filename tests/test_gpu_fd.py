@@ -34,3 +34,23 @@ def test_cuda_gradients_match_finite_differences():
     assert err['color'] <= COLOR_TOL
     assert err['geometry'] <= GEOMETRY_TOL
     assert err['prefiltered_points'] <= PREFILTER_TOL
+
+
+def test_cuda_stroke_width_and_gradient_paint_match_finite_differences():
+    from test_oracle_fd import STROKE_WIDTH_TOL, GRADIENT_PAINT_TOL
+    err = fd_util.run_extra_checks(_cuda_backend)
+    print(err)
+    assert err['stroke_width'] <= STROKE_WIDTH_TOL
+    assert err['linear_gradient'] <= GRADIENT_PAINT_TOL
+
+
+def test_cuda_every_paint_kind_on_fills_and_strokes_matches_finite_differences():
+    """Constant, linear and radial paint on a fill and on a stroke (the
+    reference cannot run gradient-coloured strokes, so finite differences are
+    their only check), and a radial-gradient stroke in a transformed group (paint parameters
+    and stroke width)."""
+    from test_oracle_fd import STROKE_WIDTH_TOL, PAINT_TOL
+    err = fd_util.run_paint_checks(_cuda_backend)
+    print(err)
+    for name, e in err.items():
+        assert e <= (STROKE_WIDTH_TOL if name.endswith('width') else PAINT_TOL), (name, e)

@@ -42,3 +42,16 @@ def test_oracle_stroke_width_and_gradient_paint_match_finite_differences():
     print(err)
     assert err['stroke_width'] <= STROKE_WIDTH_TOL
     assert err['linear_gradient'] <= GRADIENT_PAINT_TOL
+
+
+PAINT_TOL = 1e-2   # paint parameters: smooth at a fixed seed, one central difference
+
+
+def test_oracle_every_paint_kind_on_fills_and_strokes_matches_finite_differences():
+    """Constant, linear and radial paint on a fill and on a stroke, and a
+    radial-gradient stroke in a transformed group (paint parameters and stroke
+    width)."""
+    err = fd_util.run_paint_checks(_oracle_backend)
+    print(err)
+    for name, e in err.items():
+        assert e <= (STROKE_WIDTH_TOL if name.endswith('width') else PAINT_TOL), (name, e)
