@@ -365,24 +365,45 @@ def run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samp
             'api': 'RenderFunction.serialize_scene + apply + MSE + backward, scene tensors in host memory'}
 
 
-def run_configs(dev, steps=5, warmup=3, only=None):
-    """Device-resident fwd+bwd Msamples/s of the other single-scene
-    configurations, through the C ABI like the headline leg: the single
-    circle (256x256, 2x2 spp; target: the circle at (120,140), radius 48,
-    colour (0.7,0.2,0.4,1)) and the fill-heavy prefiltered scene (1024x1024,
-    1 spp, 512 closed paths, seed 3; target: the same generator with seed 4).
-    L2 flushed between steps, CUDA events per step."""
-    import torch
-    import diffvg_gb300 as dvg
-    from diffvg_gb300 import _native, workloads
-    from diffvg_gb300.packing import pack_scene
-    cases = {
+CONFIG_NAMES = ('circle_256_2x2', 'fill_prefiltered_1024_1x1', 'fill_1024_2x2', 'fill_long_1024_2x2',
+                'fill_long_prefiltered_1024_1x1')
+
+
+def config_cases(dvg):
+    """The single-scene configurations besides the headline: (scene, target
+    scene, (nsx, nsy), seed, prefiltering) by name."""
+    from diffvg_gb300 import workloads
+    long_segs = (200, 400)
+    return {
+        # the single circle (256x256, 2x2 spp; target: the circle at (120,140),
+        # radius 48, colour (0.7,0.2,0.4,1))
         'circle_256_2x2': (workloads.circle_scene(dvg),
                            workloads.circle_scene(dvg, center=(120.0, 140.0), radius=48.0,
                                                   color=(0.7, 0.2, 0.4, 1.0)), (2, 2), 0, False),
+        # the fill-heavy prefiltered scene (1024x1024, 1 spp, 512 closed paths of
+        # 8-32 cubic segments, seed 3; target: the same generator with seed 4)
         'fill_prefiltered_1024_1x1': (workloads.fill_scene(dvg, seed=3), workloads.fill_scene(dvg, seed=4), (1, 1),
                                       3, True),
+        # the same scene sampled at 2x2 without prefiltering, and scenes drawn
+        # the same way with 200-400 segments per path (15x the segments): the
+        # per-sample cost against the segment count
+        'fill_1024_2x2': (workloads.fill_scene(dvg, seed=3), workloads.fill_scene(dvg, seed=4), (2, 2), 3, False),
+        'fill_long_1024_2x2': (workloads.fill_scene(dvg, seed=3, seg_range=long_segs),
+                               workloads.fill_scene(dvg, seed=4, seg_range=long_segs), (2, 2), 3, False),
+        'fill_long_prefiltered_1024_1x1': (workloads.fill_scene(dvg, seed=3, seg_range=long_segs),
+                                           workloads.fill_scene(dvg, seed=4, seg_range=long_segs), (1, 1), 3, True),
     }
+
+
+def run_configs(dev, steps=5, warmup=3, only=None):
+    """Device-resident fwd+bwd Msamples/s of the other single-scene
+    configurations (config_cases), through the C ABI like the headline leg.
+    L2 flushed between steps, CUDA events per step."""
+    import torch
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import _native
+    from diffvg_gb300.packing import pack_scene
+    cases = config_cases(dvg)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
     flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)
@@ -427,7 +448,8 @@ def run_configs(dev, steps=5, warmup=3, only=None):
         ms = sum(a.elapsed_time(b) for a, b in ev) / steps
         n = w * h * nsx * nsy
         out[name] = {'Msamples_per_s': round(n / (ms / 1e3) / 1e6, 3), 'ms_per_step': round(ms, 4),
-                     'samples_per_step': n, 'prefiltered': pf, 'steps': steps}
+                     'samples_per_step': n, 'prefiltered': pf, 'steps': steps,
+                     'path_segments': int(packed.segment_ctrl.size)}
         scene.close()
         tscene.close()
     return out
@@ -652,7 +674,7 @@ def main():
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--profile', action='store_true',
                     help='only the device-resident steps (for ncu captures): no e2e, batched, served or CPU legs')
-    ap.add_argument('--config', choices=['circle_256_2x2', 'fill_prefiltered_1024_1x1'],
+    ap.add_argument('--config', choices=list(CONFIG_NAMES),
                     help='only this single-scene configuration (for ncu captures): target render, 3 warm-up '
                          'and 5 timed fwd+bwd steps')
     args = ap.parse_args()

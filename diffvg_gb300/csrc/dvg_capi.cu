@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -84,6 +85,10 @@ struct DvgScene {
   float4 *rec_cbox = nullptr;
   float2 *seg_tpts = nullptr;
   float *seg_th = nullptr;
+  // y-band segment lists of long paths (all null when no path has them)
+  int4 *shape_band = nullptr;  // topology
+  float2 *band_geo = nullptr;
+  int *band_n = nullptr, *band_start = nullptr, *band_seg = nullptr;
   unsigned *err = nullptr;  // [0] status bits, [1] tile-list length
   // image-sized arenas
   DevBuf weight, samples, dbg_val, dbg_flag, edge;
@@ -277,6 +282,11 @@ DevScene make_dev(DvgScene *sc, const float *params) {
   S.rec_cbox = sc->rec_cbox;
   S.seg_tpts = sc->seg_tpts;
   S.seg_th = sc->seg_th;
+  S.shape_band = sc->shape_band;
+  S.band_geo = sc->band_geo;
+  S.band_n = sc->band_n;
+  S.band_start = sc->band_start;
+  S.band_seg = sc->band_seg;
   S.seg_pmf = sc->seg_pmf;
   S.seg_cdf = sc->seg_cdf;
   S.seg_order = sc->seg_order;
@@ -481,11 +491,28 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   int NT = sc->num_total;
   sc->num_records = dvg::count_stroke_records(desc);
   int NR = sc->num_records;
+  // band lists of the paths with DVG_BAND_MIN_SEGMENTS or more segments: one
+  // band per two segments (4 to 256), room for each segment to meet four
+  // bands on average
+  std::vector<int4> shape_band(S > 0 ? S : 1, make_int4(0, 0, 0, 0));
+  long long band_starts = 0, band_entries = 0;
+  for (int i = 0; i < S; i++) {
+    const int32_t *si = desc->shape_info + (size_t)i * DVG_SHAPE_INFO_STRIDE;
+    int nseg = si[DVG_SHAPE_NUM_SEGMENTS];
+    if (si[DVG_SHAPE_KIND] != DVG_PATH || nseg < DVG_BAND_MIN_SEGMENTS) continue;
+    int nb = std::min(std::max(nseg / 2, 4), 256);
+    int cap = 4 * nseg + 2 * nb;
+    shape_band[i] = make_int4(nb, (int)band_starts, (int)band_entries, cap);
+    band_starts += nb + 1;
+    band_entries += cap;
+  }
+  if (band_starts + band_entries > 0x7fffffffLL) { delete sc; return fail(DVG_ERR_INVALID, "too many path segments"); }
+  bool banded = band_starts > 0;
   cudaError_t e;
   // topology
   std::vector<size_t> tb = {sizeof(int) * S * DVG_SHAPE_INFO_STRIDE, sizeof(int) * NSEG, sizeof(int) * NSEG,
                             sizeof(int) * G * DVG_GROUP_INFO_STRIDE, sizeof(int) * NGS, sizeof(int) * NT,
-                            sizeof(int) * NT};
+                            sizeof(int) * NT, banded ? sizeof(int4) * S : 0};
   e = sc->topo.ensure(carve_size(tb));
   if (e != cudaSuccess) { delete sc; return cuda_fail(e, "allocating the scene topology"); }
   char *p = reinterpret_cast<char *>(sc->topo.ptr);
@@ -496,7 +523,9 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   sc->group_shapes = carve<int>(p, NGS);
   sc->smp_shape = carve<int>(p, NT);
   sc->smp_group = carve<int>(p, NT);
+  if (banded) sc->shape_band = carve<int4>(p, S);
   struct Up { void *dst; const void *src; size_t n; } ups[] = {
+      {sc->shape_band, shape_band.data(), banded ? sizeof(int4) * S : 0},
       {sc->shape_info, desc->shape_info, sizeof(int) * S * DVG_SHAPE_INFO_STRIDE},
       {sc->segment_ctrl, desc->segment_ctrl, sizeof(int) * NSEG},
       {sc->seg_point, seg_point.data(), sizeof(int) * NSEG},
@@ -521,7 +550,9 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
       sizeof(unsigned) * 4,
       sizeof(float2) * DVG_TREE_PTS * (size_t)NSEG, sizeof(float) * DVG_TREE_NODES * (size_t)NSEG,  // trees
       sizeof(int2) * G, sizeof(float4) * NR, sizeof(int4) * NR, sizeof(int4) * NR, sizeof(float) * NR,  // records
-      sizeof(float4) * NR};
+      sizeof(float4) * NR,
+      banded ? sizeof(float2) * S : 0, banded ? sizeof(int) * S : 0, sizeof(int) * (size_t)band_starts,  // bands
+      sizeof(int) * (size_t)band_entries};
   e = sc->derived.ensure(carve_size(db));
   if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "allocating scene arenas"); }
   p = reinterpret_cast<char *>(sc->derived.ptr);
@@ -551,6 +582,12 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   sc->rec_b = carve<int4>(p, NR);
   sc->rec_r = carve<float>(p, NR);
   sc->rec_cbox = carve<float4>(p, NR);
+  if (banded) {
+    sc->band_geo = carve<float2>(p, S);
+    sc->band_n = carve<int>(p, S);
+    sc->band_start = carve<int>(p, (size_t)band_starts);
+    sc->band_seg = carve<int>(p, (size_t)band_entries);
+  }
   e = cudaMemset(sc->derived.ptr, 0, sc->derived.bytes);
   if (e != cudaSuccess) { dvg_scene_destroy(sc); return cuda_fail(e, "clearing scene arenas"); }
   size_t cap = (size_t)T * 32;

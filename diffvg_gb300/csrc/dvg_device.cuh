@@ -55,8 +55,8 @@ struct DevScene {
   int tiles_x, tiles_y;
   int *tile_start;          // [tiles+1]
   int *tile_list;           // candidate groups per tile, ascending
-  unsigned *tile_mask;      // per tile-list entry: bit i (< 31) set when the group's stroke record i may
-                            // reach the tile, bit 31 when any record from 31 on may
+  unsigned *tile_mask;      // per tile-list entry: bit i set when one of the group's stroke records
+                            // [i << c, (i + 1) << c) may reach the tile, c = rec_chunk_shift(records)
   int *scratch;             // [8*NSEG + 8*S] path leaf-order scratch
   int2 *g_rec;              // [G] range of each group's stroke records
   float4 *rec_box;          // [records] cull box (empty test: infinite box)
@@ -67,7 +67,19 @@ struct DevScene {
   float2 *seg_tpts = nullptr;  // [NSEG * DVG_TREE_PTS] tabulated subdivision trees (curved segments), or null
   float *seg_th = nullptr;     // [NSEG * DVG_TREE_NODES]
   unsigned *err;            // status word (DVG_EFLAG_*)
+  // y-band segment lists of long paths (null: no path has them).  A path of
+  // DVG_BAND_MIN_SEGMENTS or more segments splits its box's y-range into
+  // shape_band.x equal bands; band b lists, in visiting order, the segments
+  // whose box meets the band.  shape_band = {bands (0: none), first entry of
+  // the path's band_start (bands + 1 entries), first entry of its band_seg,
+  // band_seg capacity} is topology; the rest is derived per call.
+  const int4 *shape_band = nullptr;  // [S]
+  float2 *band_geo = nullptr;        // [S] y of the box's top, bands per unit of y
+  int *band_n = nullptr;             // [S] bands in use this call (0: lists off, e.g. over capacity)
+  int *band_start = nullptr;         // band b of path s: band_seg[shape_band.z + band_start[shape_band.y + b] ...]
+  int *band_seg = nullptr;           // segment indices within the path
 };
+#define DVG_BAND_MIN_SEGMENTS 16
 
 // Per-call render settings (image space).
 struct DevRender {
@@ -356,6 +368,15 @@ DI v2 eval_cubic(v2 p0, v2 p1, v2 p2, v2 p3, float t) {
               scl2(t * t * t, p3));
 }
 
+// log2 of the stroke records per tile-mask bit of a group with n records:
+// one record per bit up to 32 records, else the fewest records per bit (a
+// power of two) that fit the group in 32 bits
+DI int rec_chunk_shift(int n) {
+  int c = 0;
+  while ((n + (1 << c) - 1) >> c > 32) c++;
+  return c;
+}
+
 // Candidate groups for a canvas-space point: the point's tile list, or all
 // groups outside the tile grid.  Returns true when the tile list is used.
 DI bool cand_range(const DevScene &S, v2 pt, int &begin, int &end) {
@@ -485,6 +506,33 @@ DI int winding_segment(const DevScene &S, int po, int np, int nc, int i0, v2 pt)
   return w;
 }
 
+// Band of y in path s's band lists: monotone in y and clamped to the bands,
+// so a segment whose box spans [ylo, yhi] is listed in every band that
+// band_of maps a y of [ylo, yhi] to.
+DI int band_of(float2 geo, int nb, float y) {
+  float f = (y - geo.x) * geo.y;
+  f = fminf(fmaxf(f, 0.f), (float)(nb - 1));
+  return (int)f;
+}
+
+// The segment list of path s that holds every segment whose box can meet
+// the y-range [ylo, yhi]: returns false (scan all segments) unless the path
+// has band lists this call and the range falls in one band; else [b, e) are
+// entries of S.band_seg.  Lists skip only segments that the callers' own box
+// tests would skip, so results do not change.
+DI bool band_list(const DevScene &S, int s, float ylo, float yhi, int &b, int &e) {
+  if (!S.band_n) return false;
+  int nb = __ldg(&S.band_n[s]);
+  if (nb <= 0 || !(ylo == ylo) || !(yhi == yhi)) return false;
+  float2 geo = __ldg(&S.band_geo[s]);
+  int b0 = band_of(geo, nb, ylo);
+  if (b0 != band_of(geo, nb, yhi)) return false;
+  int4 sb = __ldg(&S.shape_band[s]);
+  b = sb.z + __ldg(&S.band_start[sb.y + b0]);
+  e = sb.z + __ldg(&S.band_start[sb.y + b0 + 1]);
+  return true;
+}
+
 DI int winding_shape(const DevScene &S, int s, v2 pt) {
   int kind = SI(S, s, DVG_SHAPE_KIND);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
@@ -499,7 +547,16 @@ DI int winding_shape(const DevScene &S, int s, v2 pt) {
     return (pt.x > pget(S, po) && pt.x < pget(S, po + 2) && pt.y > pget(S, po + 1) && pt.y < pget(S, po + 3)) ? 1 : 0;
   }
   int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
-  int w = 0;
+  int w = 0, b, e;
+  if (band_list(S, s, pt.y, pt.y, b, e)) {  // the segments whose box meets pt's band
+    #pragma unroll 1
+    for (int k = b; k < e; k++) {
+      int i = __ldg(&S.band_seg[k]);
+      if (!box_ray(S.seg_box[so + i], pt)) continue;
+      w += winding_segment(S, po, np, __ldg(&S.segment_ctrl[so + i]), __ldg(&S.seg_point[so + i]), pt);
+    }
+    return w;
+  }
   #pragma unroll 1
   for (int i = 0; i < nseg; i++) {
     if (nseg > 1 && !box_ray(S.seg_box[so + i], pt)) continue;
@@ -1290,9 +1347,15 @@ DN bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
   float min_dist = max_radius;
   v2 ret = V2(0, 0);
   bool found = false;
+  // with a finite search radius, the band list that covers pt.y +- radius
+  // (grown by a rounding margin) holds every segment box_in_r can pass, in
+  // visiting order
+  float slack = max_radius + 1e-5f * (fabsf(pt.y) + max_radius + 1.f);
+  int kb = 0, ke = nseg;
+  bool banded = max_radius < INFINITY && band_list(S, s, pt.y - slack, pt.y + slack, kb, ke);
   #pragma unroll 1
-  for (int k = 0; k < nseg; k++) {
-    int seg = S.seg_order[so + k];
+  for (int k = kb; k < ke; k++) {
+    int seg = banded ? __ldg(&S.band_seg[k]) : S.seg_order[so + k];
     if (nseg > 1 && !box_in_r(S.seg_box[so + seg], pt, min_dist)) continue;
     int nc = __ldg(&S.segment_ctrl[so + seg]), i0 = __ldg(&S.seg_point[so + seg]);
     float dist = 0.f, t_root = 0.f;

@@ -174,6 +174,58 @@ __global__ void k_shape_prep(DevScene S) {
   S.s_length[s] = L;
 }
 
+// y-band segment lists of the long paths (one thread per path): the path's
+// box is cut into shape_band.x bands of equal height, and every segment is
+// listed, in visiting order, in each band from band_of(its box's top) to
+// band_of(its bottom).  The reference culls a path's segments with a
+// y-sorted segment BVH (scene.cpp:602-620, walked in winding_number.h:54-172
+// and compute_distance.h:36-300); the band lists give a point's candidates as
+// one contiguous list.  A path whose lists would pass their capacity, or
+// whose box has no finite positive height, gets none this call (band_n 0):
+// its queries scan every segment, with the same results.
+__global__ void k_band_fill(DevScene S) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S.num_shapes) return;
+  int4 sb = S.shape_band[s];
+  if (sb.x <= 0) return;
+  int nb = sb.x;
+  S.band_n[s] = 0;
+  float4 box = S.s_box[s];
+  float h = box.w - box.y;
+  float inv = (float)nb / h;
+  if (!(h > 0.f) || !(inv < INFINITY)) return;
+  float2 geo = make_float2(box.y, inv);
+  S.band_geo[s] = geo;
+  int so = SI(S, s, DVG_SHAPE_SEG_OFF), nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);
+  int *st = S.band_start + sb.y;
+  int *out = S.band_seg + sb.z;
+  for (int b = 0; b <= nb; b++) st[b] = 0;
+  long long total = 0;
+  for (int k = 0; k < nseg; k++) {
+    float4 q = S.seg_box[so + S.seg_order[so + k]];
+    if (!(q.y == q.y) || !(q.w == q.w)) continue;  // a NaN box passes no box test
+    int b0 = band_of(geo, nb, q.y), b1 = band_of(geo, nb, q.w);
+    for (int b = b0; b <= b1; b++) st[b]++;
+    total += b1 - b0 + 1;
+  }
+  if (total > sb.w) return;
+  for (int b = 0, run = 0; b < nb; b++) {  // counts -> starts
+    int c = st[b];
+    st[b] = run;
+    run += c;
+  }
+  for (int k = 0; k < nseg; k++) {  // st[b] is band b's write cursor
+    int seg = S.seg_order[so + k];
+    float4 q = S.seg_box[so + seg];
+    if (!(q.y == q.y) || !(q.w == q.w)) continue;
+    int b0 = band_of(geo, nb, q.y), b1 = band_of(geo, nb, q.w);
+    for (int b = b0; b <= b1; b++) out[st[b]++] = seg;
+  }
+  for (int b = nb; b > 0; b--) st[b] = st[b - 1];  // cursors (= band ends) -> starts
+  st[0] = 0;
+  S.band_n[s] = nb;
+}
+
 __device__ __forceinline__ int clamp_tile(double f, int hi, bool lower) {
   // clamps a floored tile coordinate to the grid (first / last tile)
   if (lower) return f < 0 ? 0 : (f > hi - 1 ? hi : (int)f);
@@ -427,14 +479,15 @@ DI bool tile_keep(const DevScene &S, const int4 *g_tile_range, int g, int tx, in
   float x0 = (float)(tx * DVG_TILE), y0 = (float)(ty * DVG_TILE);
   float x1 = x0 + (float)DVG_TILE, y1 = y0 + (float)DVG_TILE;
   unsigned m = 0u;
+  int csh = rec_chunk_shift(rg.y - rg.x);
   for (int j = rg.x; j < rg.y; j++) {
-    int rel = j - rg.x;
-    if (rel >= 31) {
-      m |= 1u << 31;
-      break;
+    int bit = (j - rg.x) >> csh;
+    if (m & (1u << bit)) {  // the rest of this chunk cannot add to the mask
+      j = rg.x + ((bit + 1) << csh) - 1;
+      continue;
     }
     float4 b = S.rec_cbox[j];
-    if (b.x <= x1 && b.z >= x0 && b.y <= y1 && b.w >= y0) m |= 1u << rel;
+    if (b.x <= x1 && b.z >= x0 && b.y <= y1 && b.w >= y0) m |= 1u << bit;
   }
   *mask = m;
   return m != 0u || GI(S, g, DVG_GROUP_FILL_KIND) != DVG_PAINT_NONE;
@@ -528,6 +581,7 @@ cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4
   if (G > 0) k_group_xform<<<(G + 127) / 128, 128, 0, st>>>(S);
   if (NS > 0) k_shape_prep<<<(NS + 63) / 64, 64, 0, st>>>(S);
   if (NS > 0 && S.seg_tpts) k_seg_tree<<<(NS + 3) / 4, 128, 0, st>>>(S);
+  if (NS > 0 && S.shape_band) k_band_fill<<<(NS + 63) / 64, 64, 0, st>>>(S);
   if (G > 0) k_group_prep<<<(G + 127) / 128, 128, 0, st>>>(S, g_tile_range);
   if (G > 0) {
     k_rec_scan<<<1, 1024, 0, st>>>(S);

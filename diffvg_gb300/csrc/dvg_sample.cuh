@@ -194,18 +194,17 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
     int glo = njobs, cs = -1, slo = njobs, skip_to = rg.x;
     bool live = act, gret = false, mark = false;
     bool is_eq = act && eq && eq->group == g;
-    int jb = rg.x, j = rg.x;
+    int jb = rg.x, j = rg.x, csh = rec_chunk_shift(rg.y - rg.x);
     #pragma unroll 1
     while (j < rg.y) {
-      int rel = j - jb;
-      if (rel < 31) {  // skip the records that cannot reach the lanes' tiles
-        unsigned m = (um & 0x7fffffffu) >> rel;
-        if (m == 0u) {
-          if (!(um >> 31)) break;
-          j = jb + 31;
-          continue;
-        }
-        j += __ffs(m) - 1;
+      // skip the chunks of records that cannot reach the lanes' tiles
+      int bit = (j - jb) >> csh;
+      unsigned m = um >> bit;
+      if (m == 0u) break;
+      int ahead = __ffs(m) - 1;
+      if (ahead > 0) {
+        j = jb + ((bit + ahead) << csh);
+        continue;
       }
       float4 b = __ldg(&S.rec_box[j]);
       bool test = live && j >= skip_to && lp.x >= b.x && lp.x <= b.z && lp.y >= b.y && lp.y <= b.w;

@@ -237,6 +237,34 @@ def prefilter_transformed_strokes(m):
     return c
 
 
+def _long_fills(m):
+    # closed star paths of 200-300 cubic segments (band lists), constant /
+    # linear / radial fills, one in ten also stroked
+    from diffvg_gb300 import workloads
+    w, h, shapes, groups = workloads.fill_scene(m, seed=11, num_paths=8, canvas=96, seg_range=(200, 300),
+                                                radius_range=(14.0, 44.0), stroke_fraction=0.25)
+    return w, h, shapes, groups
+
+
+def long_path_fills(m):
+    w, h, shapes, groups = _long_fills(m)
+    return _case(w, h, shapes, groups, spp=2, seed=5)
+
+
+def long_path_fills_prefiltered(m):
+    w, h, shapes, groups = _long_fills(m)
+    return _case(w, h, shapes, groups, spp=1, seed=5, use_prefiltering=True)
+
+
+def long_path_strokes(m):
+    # open strokes of 120 cubic segments: more stroke records per group than
+    # tile-mask bits
+    from diffvg_gb300 import workloads
+    w, h, shapes, groups = workloads.stroke_scene(m, seed=12, num_paths=6, canvas=96, step=4.0, num_segments=120,
+                                                  width_range=(0.5, 2.0))
+    return _case(w, h, shapes, groups, spp=2, seed=6)
+
+
 def sdf_image(m):
     c = overlapping_groups(m)
     c['output'] = 'sdf'
@@ -263,7 +291,7 @@ CASES = [circle_fill, circle_stroke, ellipse_fill, rect_fill_stroke, polygon_fil
          _with_filter(overlapping_groups, 'parabolic', 1.0), _with_filter(overlapping_groups, 'hann', 1.5),
          background_image, render_size_differs, distance_approx_stroke, prefilter_fills, prefilter_strokes,
          prefilter_transformed_strokes,
-         sdf_image, sdf_eval_positions]
+         sdf_image, sdf_eval_positions, long_path_fills, long_path_fills_prefiltered, long_path_strokes]
 
 CASE_BY_NAME = {f.__name__: f for f in CASES}
 
