@@ -13,11 +13,17 @@ Lines printed (one JSON line, rank 0):
          HBM; each step is timed with CUDA events on the launching stream,
          the L2 is flushed (a 256 MiB write) between steps outside the timed
          events.
-  e2e    the same metric through the public API a user calls
+  e2e    the same metric through the C ABI that stands in for the
+         reference's diffvg.render (dvg_render_forward / dvg_render_backward)
+         with the parameter and gradient arenas in pinned host memory: the
+         host-to-device copy of the parameters, the render, the loss
+         gradient, the backward, the gradients and the loss copied back to
+         the host are all inside the timed region (wall clock).
+  e2e_render_function  the same through the PyTorch drop-in
          (RenderFunction.serialize_scene / apply / backward) with the scene
-         tensors in host memory: host-to-device copy of the parameters, the
-         render, the loss, the backward, the gradients copied back to host
-         tensors and the loss read back are all inside the timed region.
+         tensors in host memory; it adds PyTorch's per-tensor work for the
+         scene's 6144 leaf tensors (serialisation, autograd bookkeeping,
+         one gradient view per tensor).
   roofline  the dominant kernel's algorithmic bytes per launch over its
          CUDA-event time, against the measured HBM copy bandwidth.
   cpu_baseline  the CPU oracle port (oracle/, all host cores) on one full
@@ -305,14 +311,17 @@ def run_ours(args):
     except Exception:
         roofline['issue'] = None
 
-    # ---------------- end to end through the public API ----------------
-    e2e = None if getattr(args, 'no_e2e', False) else run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx,
-                                                              nsy, seed, n_samples, ws)
+    # ---------------- end to end with host buffers ----------------
+    e2e = e2e_rf = None
+    if not getattr(args, 'no_e2e', False):
+        e2e = run_e2e_cabi(args, packed, scene, dev, target, w, h, nsx, nsy, seed, n_samples, ws)
+        e2e_rf = run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samples, ws)
 
     out = {'metric': METRIC, 'value': round(value, 3), 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
            'warmup': max(args.warmup, 3), 'ms_per_step': round(total_ms / args.steps, 4), 'higher_is_better': True,
            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 (fp64 root solves)', 'data': 'synthetic',
-           'config': _workload_config(), 'e2e': e2e, 'roofline': roofline, 'clocks': clock_info,
+           'config': _workload_config(), 'e2e': e2e, 'e2e_render_function': e2e_rf, 'roofline': roofline,
+           'clocks': clock_info,
            'gpu_launches': gpu_launches, 'fwd_ms': round(fwd_ms, 4), 'bwd_ms': round(bwd_ms, 4),
            'kernels_ms_per_launch': {k: round(v[1] / v[0], 4) for k, v in kernels.items()},
            'loss': float(loss_buf.item())}
@@ -328,8 +337,63 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_e2e_cabi(args, packed, scene, dev, target, w, h, nsx, nsy, seed, n_samples, ws):
+    """The metric through the C ABI (the drop-in for the reference's
+    diffvg.render) with the parameters and gradients in pinned HOST memory,
+    as a native caller holds them: every step copies the parameter arena to
+    the device, renders, forms the MSE gradient and loss on the device
+    (dvg_mse_grad), runs the backward pass, and copies the gradient arena and
+    the loss back to the host; the scene handle (topology) stays resident.
+    Wall-clock time over the steps, host synchronised on both sides."""
+    import torch
+    from diffvg_gb300 import _native
+    n = packed.num_params
+    h_params = packed.param_arena(torch.device('cpu')).contiguous().pin_memory()
+    h_grads = torch.empty(n, dtype=torch.float32).pin_memory()
+    h_loss = torch.empty(1, dtype=torch.float32).pin_memory()
+    d_arena = torch.empty(n, device=dev)
+    img = torch.empty(h, w, 4, device=dev)
+    d_img = torch.empty_like(img)
+    d_params = torch.empty(n, device=dev)
+    loss = torch.empty(1, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    fa = _native.RenderArgs(w, h, nsx, nsy, seed, 0, 0, d_arena.data_ptr(), None, None, _native.DVG_FLAG_NO_SYNC)
+    ba = _native.RenderArgs(w, h, nsx, nsy, seed, 0, 0, d_arena.data_ptr(), None, None,
+                            _native.DVG_FLAG_NO_SYNC | _native.DVG_FLAG_REUSE_PREP)
+
+    def step():
+        d_arena.copy_(h_params, non_blocking=True)
+        scene.forward(fa, image_ptr=img.data_ptr(), stream=sptr)
+        loss.zero_()
+        _native.mse_grad(img, target, d_img, loss, stream=sptr)
+        d_params.zero_()
+        scene.backward(ba, d_image_ptr=d_img.data_ptr(), d_params_ptr=d_params.data_ptr(), stream=sptr)
+        h_grads.copy_(d_params, non_blocking=True)
+        h_loss.copy_(loss, non_blocking=True)
+        scene.sync(sptr)  # waits for the stream; raises on any failure the kernels latched
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    k = max(1, min(args.steps, 20))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        step()
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t0
+    return {'value': round(ws * n_samples * k / dt / 1e6, 3), 'unit': UNIT, 'h2d_bytes_per_step': 4 * n,
+            'd2h_bytes_per_step': 4 * n + 4, 'steps': k, 'ms_per_step': round(dt / k * 1e3, 3),
+            'api': 'C ABI (dvg_render_forward, dvg_mse_grad, dvg_render_backward, dvg_scene_sync) with the '
+                   'parameter and gradient arenas in pinned host memory; scene topology resident',
+            'loss': round(float(h_loss[0]) / img.numel(), 6)}
+
+
 def run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samples, ws):
-    """Same metric through RenderFunction with host-resident scene tensors."""
+    """Same metric through RenderFunction (the PyTorch drop-in) with
+    host-resident scene tensors: serialize_scene, apply, the loss in torch,
+    backward with autograd delivering a gradient to each of the scene's
+    6144 leaf tensors."""
     import torch
     params = []
     for s in shapes:
@@ -365,8 +429,8 @@ def run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samp
             'api': 'RenderFunction.serialize_scene + apply + MSE + backward, scene tensors in host memory'}
 
 
-CONFIG_NAMES = ('circle_256_2x2', 'fill_prefiltered_1024_1x1', 'fill_1024_2x2', 'fill_long_1024_2x2',
-                'fill_long_prefiltered_1024_1x1')
+CONFIG_NAMES = ('circle_256_2x2', 'fill_prefiltered_1024_1x1', 'blob_1024_2x2', 'blob_long_1024_2x2',
+                'blob_long_prefiltered_1024_1x1')
 
 
 def config_cases(dvg):
@@ -384,14 +448,14 @@ def config_cases(dvg):
         # 8-32 cubic segments, seed 3; target: the same generator with seed 4)
         'fill_prefiltered_1024_1x1': (workloads.fill_scene(dvg, seed=3), workloads.fill_scene(dvg, seed=4), (1, 1),
                                       3, True),
-        # the same scene sampled at 2x2 without prefiltering, and scenes drawn
-        # the same way with 200-400 segments per path (15x the segments): the
-        # per-sample cost against the segment count
-        'fill_1024_2x2': (workloads.fill_scene(dvg, seed=3), workloads.fill_scene(dvg, seed=4), (2, 2), 3, False),
-        'fill_long_1024_2x2': (workloads.fill_scene(dvg, seed=3, seg_range=long_segs),
-                               workloads.fill_scene(dvg, seed=4, seg_range=long_segs), (2, 2), 3, False),
-        'fill_long_prefiltered_1024_1x1': (workloads.fill_scene(dvg, seed=3, seg_range=long_segs),
-                                           workloads.fill_scene(dvg, seed=4, seg_range=long_segs), (1, 1), 3, True),
+        # 512 smooth closed paths (workloads.blob_scene) of 8-32 segments and
+        # of 200-400 segments (15x the segments, the same shapes' family):
+        # the cost per sample against the segment count
+        'blob_1024_2x2': (workloads.blob_scene(dvg, seed=5), workloads.blob_scene(dvg, seed=6), (2, 2), 3, False),
+        'blob_long_1024_2x2': (workloads.blob_scene(dvg, seed=5, seg_range=long_segs),
+                               workloads.blob_scene(dvg, seed=6, seg_range=long_segs), (2, 2), 3, False),
+        'blob_long_prefiltered_1024_1x1': (workloads.blob_scene(dvg, seed=5, seg_range=long_segs),
+                                           workloads.blob_scene(dvg, seed=6, seg_range=long_segs), (1, 1), 3, True),
     }
 
 

@@ -491,16 +491,16 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   int NT = sc->num_total;
   sc->num_records = dvg::count_stroke_records(desc);
   int NR = sc->num_records;
-  // band lists of the paths with DVG_BAND_MIN_SEGMENTS or more segments: one
-  // band per two segments (4 to 256), room for each segment to meet four
-  // bands on average
+  // band lists of the paths with DVG_BAND_MIN_SEGMENTS or more segments: up
+  // to one band per four segments (4 to 128), room for each segment to meet
+  // four bands on average
   std::vector<int4> shape_band(S > 0 ? S : 1, make_int4(0, 0, 0, 0));
   long long band_starts = 0, band_entries = 0;
   for (int i = 0; i < S; i++) {
     const int32_t *si = desc->shape_info + (size_t)i * DVG_SHAPE_INFO_STRIDE;
     int nseg = si[DVG_SHAPE_NUM_SEGMENTS];
     if (si[DVG_SHAPE_KIND] != DVG_PATH || nseg < DVG_BAND_MIN_SEGMENTS) continue;
-    int nb = std::min(std::max(nseg / 2, 4), 256);
+    int nb = std::min(std::max(nseg / 4, 4), 128);
     int cap = 4 * nseg + 2 * nb;
     shape_band[i] = make_int4(nb, (int)band_starts, (int)band_entries, cap);
     band_starts += nb + 1;

@@ -68,18 +68,23 @@ struct DevScene {
   float *seg_th = nullptr;     // [NSEG * DVG_TREE_NODES]
   unsigned *err;            // status word (DVG_EFLAG_*)
   // y-band segment lists of long paths (null: no path has them).  A path of
-  // DVG_BAND_MIN_SEGMENTS or more segments splits its box's y-range into
-  // shape_band.x equal bands; band b lists, in visiting order, the segments
-  // whose box meets the band.  shape_band = {bands (0: none), first entry of
+  // DVG_BAND_MIN_SEGMENTS or more segments splits its box's y-range into up
+  // to shape_band.x equal bands; band b lists, in visiting order, the
+  // segments whose box meets the band.  shape_band = {bands (0: none), first entry of
   // the path's band_start (bands + 1 entries), first entry of its band_seg,
   // band_seg capacity} is topology; the rest is derived per call.
   const int4 *shape_band = nullptr;  // [S]
   float2 *band_geo = nullptr;        // [S] y of the box's top, bands per unit of y
   int *band_n = nullptr;             // [S] bands in use this call (0: lists off, e.g. over capacity)
   int *band_start = nullptr;         // band b of path s: band_seg[shape_band.z + band_start[shape_band.y + b] ...]
-  int *band_seg = nullptr;           // segment indices within the path
+  int *band_seg = nullptr;           // visiting ranks k of the segments (segment seg_order[k] of the path)
 };
-#define DVG_BAND_MIN_SEGMENTS 16
+// Paths with fewer segments scan them all: a warp's lanes then walk one list
+// together, which costs less than divergent walks of short band lists.
+#define DVG_BAND_MIN_SEGMENTS 64
+// Bands are at least this tall (shape-space units), so that a warp's pixel
+// block and a prefiltering query's +-1 px range mostly fall in one band.
+#define DVG_BAND_MIN_HEIGHT 4.0f
 
 // Per-call render settings (image space).
 struct DevRender {
@@ -515,22 +520,39 @@ DI int band_of(float2 geo, int nb, float y) {
   return (int)f;
 }
 
-// The segment list of path s that holds every segment whose box can meet
-// the y-range [ylo, yhi]: returns false (scan all segments) unless the path
-// has band lists this call and the range falls in one band; else [b, e) are
-// entries of S.band_seg.  Lists skip only segments that the callers' own box
-// tests would skip, so results do not change.
-DI bool band_list(const DevScene &S, int s, float ylo, float yhi, int &b, int &e) {
+// The band lists of path s that hold every segment whose box can meet the
+// y-range [ylo, yhi]: returns false (scan all segments) unless the path has
+// band lists this call and the range falls in at most two bands; else
+// [b0, e0) and [b1, e1) are entries of S.band_seg (the second range empty
+// for one band), each in ascending visiting rank.  Lists skip only segments
+// that the callers' own box tests would skip, so results do not change.
+DI bool band_lists(const DevScene &S, int s, float ylo, float yhi, int &b0, int &e0, int &b1, int &e1) {
   if (!S.band_n) return false;
   int nb = __ldg(&S.band_n[s]);
   if (nb <= 0 || !(ylo == ylo) || !(yhi == yhi)) return false;
   float2 geo = __ldg(&S.band_geo[s]);
-  int b0 = band_of(geo, nb, ylo);
-  if (b0 != band_of(geo, nb, yhi)) return false;
+  int lo = band_of(geo, nb, ylo), hi = band_of(geo, nb, yhi);
+  if (hi > lo + 1) return false;
   int4 sb = __ldg(&S.shape_band[s]);
-  b = sb.z + __ldg(&S.band_start[sb.y + b0]);
-  e = sb.z + __ldg(&S.band_start[sb.y + b0 + 1]);
+  const int *st = S.band_start + sb.y;
+  b0 = sb.z + __ldg(&st[lo]);
+  e0 = sb.z + __ldg(&st[lo + 1]);
+  b1 = e1 = e0;
+  if (hi > lo) {
+    b1 = e0;
+    e1 = sb.z + __ldg(&st[hi + 1]);
+  }
   return true;
+}
+
+// Next visiting rank of the merge of two rank-sorted band lists (a segment
+// in both bands comes once); -1 when both are exhausted.
+DI int band_next(const DevScene &S, int &i, int e0, int &j, int e1) {
+  int a = i < e0 ? __ldg(&S.band_seg[i]) : 0x7fffffff, b = j < e1 ? __ldg(&S.band_seg[j]) : 0x7fffffff;
+  if (a == 0x7fffffff && b == 0x7fffffff) return -1;
+  if (a <= b) i++;
+  if (b <= a) j++;
+  return a < b ? a : b;
 }
 
 DI int winding_shape(const DevScene &S, int s, v2 pt) {
@@ -547,11 +569,11 @@ DI int winding_shape(const DevScene &S, int s, v2 pt) {
     return (pt.x > pget(S, po) && pt.x < pget(S, po + 2) && pt.y > pget(S, po + 1) && pt.y < pget(S, po + 3)) ? 1 : 0;
   }
   int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
-  int w = 0, b, e;
-  if (band_list(S, s, pt.y, pt.y, b, e)) {  // the segments whose box meets pt's band
+  int w = 0, b, e, b1, e1;
+  if (band_lists(S, s, pt.y, pt.y, b, e, b1, e1)) {  // the segments whose box meets pt's band
     #pragma unroll 1
     for (int k = b; k < e; k++) {
-      int i = __ldg(&S.band_seg[k]);
+      int i = __ldg(&S.seg_order[so + __ldg(&S.band_seg[k])]);
       if (!box_ray(S.seg_box[so + i], pt)) continue;
       w += winding_segment(S, po, np, __ldg(&S.segment_ctrl[so + i]), __ldg(&S.seg_point[so + i]), pt);
     }
@@ -1351,11 +1373,13 @@ DN bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
   // (grown by a rounding margin) holds every segment box_in_r can pass, in
   // visiting order
   float slack = max_radius + 1e-5f * (fabsf(pt.y) + max_radius + 1.f);
-  int kb = 0, ke = nseg;
-  bool banded = max_radius < INFINITY && band_list(S, s, pt.y - slack, pt.y + slack, kb, ke);
+  int i0 = 0, e0 = 0, i1 = 0, e1 = 0;
+  bool banded = max_radius < INFINITY && band_lists(S, s, pt.y - slack, pt.y + slack, i0, e0, i1, e1);
   #pragma unroll 1
-  for (int k = kb; k < ke; k++) {
-    int seg = banded ? __ldg(&S.band_seg[k]) : S.seg_order[so + k];
+  for (int k = 0; banded || k < nseg; k++) {
+    int rank = k;
+    if (banded && (rank = band_next(S, i0, e0, i1, e1)) < 0) break;
+    int seg = S.seg_order[so + rank];
     if (nseg > 1 && !box_in_r(S.seg_box[so + seg], pt, min_dist)) continue;
     int nc = __ldg(&S.segment_ctrl[so + seg]), i0 = __ldg(&S.seg_point[so + seg]);
     float dist = 0.f, t_root = 0.f;

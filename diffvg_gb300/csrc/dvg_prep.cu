@@ -175,9 +175,10 @@ __global__ void k_shape_prep(DevScene S) {
 }
 
 // y-band segment lists of the long paths (one thread per path): the path's
-// box is cut into shape_band.x bands of equal height, and every segment is
-// listed, in visiting order, in each band from band_of(its box's top) to
-// band_of(its bottom).  The reference culls a path's segments with a
+// box is cut into bands of equal height (as many as fit at least
+// DVG_BAND_MIN_HEIGHT, at most shape_band.x), and every segment is
+// listed, by its visiting rank in ascending order, in each band from
+// band_of(its box's top) to band_of(its bottom).  The reference culls a path's segments with a
 // y-sorted segment BVH (scene.cpp:602-620, walked in winding_number.h:54-172
 // and compute_distance.h:36-300); the band lists give a point's candidates as
 // one contiguous list.  A path whose lists would pass their capacity, or
@@ -188,12 +189,14 @@ __global__ void k_band_fill(DevScene S) {
   if (s >= S.num_shapes) return;
   int4 sb = S.shape_band[s];
   if (sb.x <= 0) return;
-  int nb = sb.x;
   S.band_n[s] = 0;
   float4 box = S.s_box[s];
   float h = box.w - box.y;
+  if (!(h > 0.f) || !(h < INFINITY)) return;
+  // bands at least DVG_BAND_MIN_HEIGHT tall (shape units), at most sb.x of them
+  int nb = (int)fminf((float)sb.x, fmaxf(1.f, floorf(h / DVG_BAND_MIN_HEIGHT)));
   float inv = (float)nb / h;
-  if (!(h > 0.f) || !(inv < INFINITY)) return;
+  if (!(inv < INFINITY)) return;
   float2 geo = make_float2(box.y, inv);
   S.band_geo[s] = geo;
   int so = SI(S, s, DVG_SHAPE_SEG_OFF), nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);
@@ -214,12 +217,11 @@ __global__ void k_band_fill(DevScene S) {
     st[b] = run;
     run += c;
   }
-  for (int k = 0; k < nseg; k++) {  // st[b] is band b's write cursor
-    int seg = S.seg_order[so + k];
-    float4 q = S.seg_box[so + seg];
+  for (int k = 0; k < nseg; k++) {  // st[b] is band b's write cursor; entries are visiting ranks
+    float4 q = S.seg_box[so + S.seg_order[so + k]];
     if (!(q.y == q.y) || !(q.w == q.w)) continue;
     int b0 = band_of(geo, nb, q.y), b1 = band_of(geo, nb, q.w);
-    for (int b = b0; b <= b1; b++) out[st[b]++] = seg;
+    for (int b = b0; b <= b1; b++) out[st[b]++] = k;
   }
   for (int b = nb; b > 0; b--) st[b] = st[b - 1];  // cursors (= band ends) -> starts
   st[0] = 0;

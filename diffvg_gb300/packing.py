@@ -16,6 +16,7 @@ module performs that unpacking once per call and splits the result in two:
 from collections import OrderedDict
 from dataclasses import dataclass, field
 import hashlib
+import operator
 import threading
 
 import numpy as np
@@ -119,6 +120,10 @@ _pack_cache = OrderedDict()
 _PACK_CACHE_SIZE = 32
 
 
+_shape_of = operator.attrgetter('shape')
+_version_of = operator.attrgetter('_version')
+
+
 def _mutable_state(args):
     """What can change inside the argument objects without changing their
     identity: the shapes of floating-point tensors (their values are
@@ -128,7 +133,11 @@ def _mutable_state(args):
     ts = [a for a in args if isinstance(a, T)]
     fl = [t for t in ts if t.is_floating_point()]
     it = [t for t in ts if not t.is_floating_point()]
-    return fl, [t.shape for t in fl], it, [t._version for t in it]
+    return fl, list(map(_shape_of, fl)), it, list(map(_version_of, it))
+
+
+def _unchanged(fl, shapes, it, versions):
+    return list(map(_shape_of, fl)) == shapes and list(map(_version_of, it)) == versions
 
 
 def _same_args(old, new):
@@ -144,15 +153,26 @@ def _same_args(old, new):
 
 def pack_scene_cached(args):
     """pack_scene with a cache for optimisation loops, which call
-    serialize_scene with the same shape objects on every step.  Entries are
-    found by a hash of the argument list (tensors hash by identity) and
-    confirmed by _same_args and by the tensors' mutable state
-    (_mutable_state); an entry keeps its argument objects alive, so tensor
-    identities cannot be reused while it is cached.  On a hit the packed
-    topology and parameter slots are reused; parameter values are read when
-    the arena is built.  Integer tensors that are converted anew on every
-    call (e.g. by a serialize_scene that copies them) simply miss the
-    cache."""
+    serialize_scene with the same shape objects on every step.
+
+    Two keys find an entry.  The identity key (the ids of the argument
+    objects) matches when every argument is the very object of the cached
+    call: the entry keeps those objects alive, so their ids cannot be reused
+    while it is cached, and only the tensors' mutable state (_mutable_state)
+    is compared.  serialize_scene interns the integers it creates, so its
+    lists hit this key.  Otherwise the value key (a hash of the argument
+    list; tensors hash by identity) is confirmed by _same_args and the
+    mutable state.  On a hit the packed topology and parameter slots are
+    reused; parameter values are read when the arena is built.  Integer
+    tensors that are converted anew on every call (e.g. by a serialize_scene
+    that copies them) simply miss the cache."""
+    ids = tuple(map(id, args))
+    with _cache_lock:
+        hit = _pack_cache.get(('id', ids))
+    if hit is not None:
+        old, packed, fl, shapes, it, versions = hit
+        if _unchanged(fl, shapes, it, versions):
+            return packed
     try:
         key = hash(tuple(args))
     except TypeError:  # an unhashable argument: no caching
@@ -161,16 +181,18 @@ def pack_scene_cached(args):
         hit = _pack_cache.get(key)
     if hit is not None:
         old, packed, fl, shapes, it, versions = hit
-        if (_same_args(old, args) and [t.shape for t in fl] == shapes and
-                [t._version for t in it] == versions):
+        if _same_args(old, args) and _unchanged(fl, shapes, it, versions):
             with _cache_lock:
                 if key in _pack_cache:
                     _pack_cache.move_to_end(key)
+                _pack_cache[('id', ids)] = hit
             return packed
     packed = pack_scene(args)
     with _cache_lock:
-        _pack_cache[key] = (list(args), packed) + tuple(_mutable_state(args))
-        while len(_pack_cache) > _PACK_CACHE_SIZE:
+        entry = (list(args), packed) + tuple(_mutable_state(args))
+        _pack_cache[key] = entry
+        _pack_cache[('id', ids)] = entry
+        while len(_pack_cache) > 2 * _PACK_CACHE_SIZE:
             _pack_cache.popitem(last=False)
     return packed
 

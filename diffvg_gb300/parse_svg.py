@@ -1,25 +1,38 @@
 """SVG file to scene: svg_to_scene(filename) -> (canvas_width, canvas_height,
-shapes, shape_groups), with pydiffvg's semantics (pydiffvg/parse_svg.py).
+shapes, shape_groups), with the semantics of pydiffvg's reader
+(pydiffvg/parse_svg.py).
 
-Supported as there: <svg> width / height / viewBox; <g> with transform and
-fill inheritance; <path>, <polygon>, <line>, <circle> and <rect>; <defs>,
-<linearGradient> and <radialGradient> (with href inheritance, stops with
-stop-color / stop-opacity, gradientTransform) and <style> class rules;
+The reader works in two steps per element.  A style resolution step folds
+the element's presentation (its class rule, then its own attributes) and its
+inline style attribute into one resolved record: transform, fill paint,
+stroke paint, half stroke width, fill rule.  An emission step turns the
+element and that record into shapes and one shape group.  Paint servers
+(<linearGradient>, <radialGradient>) and class rules (<style>) live in one
+registry filled in document order.
+
+Read as in pydiffvg: <svg> width / height / viewBox; <g> transform and fill
+(the only attributes a group passes down); <path>, <polygon>, <line>,
+<circle>, <rect>; gradients and style sheets at the top level or in <defs>;
 presentation attributes and the style attribute (fill, fill-opacity,
 opacity, fill-rule, stroke, stroke-opacity, stroke-width, transform).
 Stroke widths become half widths.  Colours: #rgb, #rrggbb, rgb(r, g, b),
 url(#id), none and the CSS 2.1 colour keywords.
 
-The reference's own behaviour is kept where it is observable from a scene:
-<ellipse> is not read; a <rect> is placed at the origin with
-p_max = (width, height) (parse_svg.py:488-500 never reads x / y);
-a radial gradient's centre and radius stay at (0, 0) (parse_svg.py:201-263
-passes its unset begin / end); fill opacity is written into the inherited
-fill colour tensor, which the shapes that inherit it share.  The reference
-depends on svgpathtools, cssutils and matplotlib for path data, style sheets
-and colour names; path data is read by diffvg_gb300.svg_path, style sheets
-by a small class-rule reader, colour names from a table.
+pydiffvg's observable behaviour is kept, including where it departs from
+SVG: <ellipse> is not read; a <rect> sits at the origin with p_max =
+(width, height) (its x / y are ignored, parse_svg.py:488-500); a radial
+gradient's centre and radius stay (0, 0) unless inherited
+(parse_svg.py:201-263); opacities are written into the paint tensor that an
+element inherits, which every element sharing it sees; the inline style's
+opacities replace the attributes' ones; an inline style moves every linear
+gradient the element uses by the element's transform, in place on the
+shared gradient.  pydiffvg reads path data, style sheets and colour names
+through svgpathtools, cssutils and matplotlib; here path data is read by
+diffvg_gb300.svg_path, style sheets by a class-rule reader and colour names
+from a table.
 """
+from dataclasses import dataclass
+import math
 import re
 import warnings
 import xml.etree.ElementTree as etree
@@ -41,381 +54,371 @@ _NAMED = {
     'teal': (0, 128, 128), 'aqua': (0, 255, 255), 'cyan': (0, 255, 255), 'orange': (255, 165, 0),
 }
 
-
-def remove_namespaces(s):
-    """'{namespace}tag' -> 'tag'."""
-    return re.sub('{.*}', '', s)
+_SHAPE_TAGS = frozenset(('path', 'polygon', 'line', 'circle', 'rect'))
 
 
-def parse_style(s, defs):
-    """'key: value; ...' -> dict; fill and stroke values become colours."""
+def _tag(element):
+    """Element name without its namespace."""
+    return element.tag.rpartition('}')[2]
+
+
+def _attr(element, local_name):
+    """Value of an attribute by local name (any namespace), or None."""
+    for key, value in element.attrib.items():
+        if key.rpartition('}')[2] == local_name:
+            return value
+    return None
+
+
+# --------------------------------------------------------------------------
+# values
+
+def _declarations(text):
+    """'name: value; ...' -> {name: value} (entries without exactly one ':'
+    are dropped)."""
     out = {}
-    for item in s.split(';'):
-        kv = item.split(':')
-        if len(kv) == 2:
-            key, value = kv[0].strip(), kv[1].strip()
-            if key in ('fill', 'stroke'):
-                value = parse_color(value, defs)
-            out[key] = value
+    for entry in text.split(';'):
+        parts = entry.split(':')
+        if len(parts) == 2:
+            out[parts[0].strip()] = parts[1].strip()
     return out
 
 
-def parse_hex(s):
-    s = s.lstrip('#')
-    if len(s) == 3:
-        s = ''.join(ch + ch for ch in s)
-    return torch.tensor([int(s[k:k + 2], 16) / 255.0 for k in (0, 2, 4)])
+def parse_style(s, defs):
+    """A style declaration list as a dict; fill and stroke values are read as
+    paints through `defs` (parse_svg.py:24-35)."""
+    out = _declarations(s)
+    for name in ('fill', 'stroke'):
+        if name in out:
+            out[name] = parse_color(out[name], defs)
+    return out
 
 
-def parse_int(s):
-    """Integer part of a length, units dropped ('512px' -> 512)."""
-    return int(float(''.join(ch for ch in s if not ch.isalpha())))
+def _rgb_hex(digits):
+    if len(digits) == 3:
+        digits = ''.join(2 * d for d in digits)
+    return [int(digits[k:k + 2], 16) / 255.0 for k in range(0, 6, 2)]
 
 
 def parse_color(s, defs):
-    """RGBA tensor, a gradient from defs, or None (parse_svg.py:54-80)."""
-    if s is None:
-        return None
-    if isinstance(s, torch.Tensor):
+    """A paint value: an RGBA tensor, a gradient registered in `defs`, or None
+    for 'none' (parse_svg.py:54-80).  An unknown value warns and gives opaque
+    black; a value that is already a tensor is returned as it is."""
+    if s is None or isinstance(s, torch.Tensor):
         return s
-    s = s.lstrip(' ')
-    color = torch.tensor([0.0, 0.0, 0.0, 1.0])
-    if s[0] == '#':
-        color[:3] = parse_hex(s)
-    elif s[:3] == 'url':
-        color = defs[s[4:-1].lstrip('#')]
-    elif s == 'none':
-        color = None
-    elif s[:4] == 'rgb(':
-        rgb = s[4:-1].split(',')
-        color = torch.tensor([int(rgb[0]) / 255.0, int(rgb[1]) / 255.0, int(rgb[2]) / 255.0, 1.0])
-    elif s.strip().lower() in _NAMED:
-        color = torch.tensor([c / 255.0 for c in _NAMED[s.strip().lower()]] + [1.0])
+    text = s.lstrip(' ')
+    if text.startswith('url'):
+        return defs[text[4:-1].lstrip('#')]
+    if text == 'none':
+        return None
+    rgba = [0.0, 0.0, 0.0, 1.0]
+    if text.startswith('#'):
+        rgba[:3] = _rgb_hex(text[1:])
+    elif text.startswith('rgb('):
+        rgba[:3] = [int(v) / 255.0 for v in text[4:-1].split(',')[:3]]
+    elif text.strip().lower() in _NAMED:
+        rgba[:3] = [v / 255.0 for v in _NAMED[text.strip().lower()]]
     else:
         warnings.warn('Unknown color command ' + s)
-    return color
+    return torch.tensor(rgba)
 
 
-def _transform_item(item):
-    kind, args = item.split('(')
-    v = [float(x) for x in args.replace(',', ' ').split()]
-    m = np.identity(3)
-    if 'matrix' in kind:
-        m[0, :] = [v[0], v[2], v[4]]
-        m[1, :] = [v[1], v[3], v[5]]
-    elif 'translate' in kind:
-        m[0, 2] = v[0]
-        if len(v) > 1:
-            m[1, 2] = v[1]
-    elif 'scale' in kind:
-        m[0, 0] = v[0]
-        m[1, 1] = v[1] if len(v) > 1 else v[0]
-    elif 'rotate' in kind:
-        a = np.radians(v[0])
-        ox, oy = (v[1], v[2]) if len(v) == 3 else (0.0, 0.0)
-        r = np.identity(3)
-        r[:2, :2] = [[np.cos(a), -np.sin(a)], [np.sin(a), np.cos(a)]]
-        to, back = np.identity(3), np.identity(3)
-        to[:2, 2] = [ox, oy]
-        back[:2, 2] = [-ox, -oy]
-        m = to @ r @ back
-    elif 'skewX' in kind:
-        m[0, 1] = np.tan(np.radians(v[0]))
-    elif 'skewY' in kind:
-        m[1, 0] = np.tan(np.radians(v[0]))
-    else:
-        warnings.warn('Unknown SVG transform type: {0}'.format(kind))
-    return m
+def _length(s):
+    """Integer part of a length with its unit letters dropped ('64px' -> 64)."""
+    return int(float(''.join(ch for ch in s if not ch.isalpha())))
+
+
+def _half_width(s):
+    """Half of a stroke-width value (pydiffvg stores half widths)."""
+    return torch.tensor(float(s[:-2] if s.endswith('px') else s) / 2.0)
+
+
+def _even_odd(value, current):
+    rules = {'evenodd': True, 'nonzero': False}
+    if value not in rules:
+        warnings.warn('Unknown fill-rule: {}'.format(value))
+        return current
+    return rules[value]
+
+
+# --------------------------------------------------------------------------
+# transforms
+
+def _affine(a, b, c, d, e, f):
+    return np.array([[a, c, e], [b, d, f], [0.0, 0.0, 1.0]])
+
+
+def _rotation(deg, cx=0.0, cy=0.0):
+    t = math.radians(deg)
+    co, si = math.cos(t), math.sin(t)
+    # about (cx, cy): translate(cx, cy) rotate(deg) translate(-cx, -cy)
+    return _affine(1, 0, 0, 1, cx, cy) @ _affine(co, si, -si, co, 0, 0) @ _affine(1, 0, 0, 1, -cx, -cy)
+
+
+_TRANSFORMS = {
+    'matrix': lambda v: _affine(*v[:6]),
+    'translate': lambda v: _affine(1, 0, 0, 1, v[0], v[1] if len(v) > 1 else 0.0),
+    'scale': lambda v: _affine(v[0], 0, 0, v[1] if len(v) > 1 else v[0], 0, 0),
+    'rotate': lambda v: _rotation(v[0], *(v[1:3] if len(v) == 3 else ())),
+    'skewX': lambda v: _affine(1, 0, math.tan(math.radians(v[0])), 1, 0, 0),
+    'skewY': lambda v: _affine(1, math.tan(math.radians(v[0])), 0, 1, 0, 0),
+}
 
 
 def parse_transform(transform_str):
-    """SVG transform list -> 3x3 float32 tensor (left to right products)."""
+    """An SVG transform list as a 3x3 float32 tensor, the product of its
+    items from left to right (parse_svg.py:82-135).  An empty string gives
+    the identity (as a float64 array, as pydiffvg returns it)."""
     if not transform_str:
         return np.identity(3)
     if not isinstance(transform_str, str):
         raise TypeError('Must provide a string to parse')
     m = np.identity(3)
     for item in transform_str.split(')')[:-1]:
-        m = m @ _transform_item(item)
+        name, _, args = item.partition('(')
+        values = [float(x) for x in args.replace(',', ' ').split()]
+        kind = next((k for k in _TRANSFORMS if k in name), None)
+        if kind is None:
+            warnings.warn('Unknown SVG transform type: {0}'.format(name))
+            continue
+        m = m @ _TRANSFORMS[kind](values)
     return torch.from_numpy(m).type(torch.float32)
 
 
-def _xform_point(m, p):
+def _apply(m, p):
+    """A 2-D point through a 3x3 (projective) transform."""
     q = m @ torch.cat((p, torch.ones([1])))
     return (q / q[2])[:2]
 
 
-def _stops(node, defs, offsets, stop_colors):
-    for child in node:
-        if remove_namespaces(child.tag) != 'stop':
-            continue
-        color = [0.0, 0.0, 0.0, 1.0]
-        if 'stop-color' in child.attrib:
-            c = parse_color(child.attrib['stop-color'], defs)
-            color[:3] = [c[0], c[1], c[2]]
-        if 'stop-opacity' in child.attrib:
-            color[3] = float(child.attrib['stop-opacity'])
-        if 'style' in child.attrib:
-            st = parse_style(child.attrib['style'], defs)
-            if 'stop-color' in st:
-                c = parse_color(st['stop-color'], defs)
-                color[:3] = [c[0], c[1], c[2]]
-            if 'stop-opacity' in st:
-                color[3] = float(st['stop-opacity'])
-        offsets.append(float(child.attrib['offset']))
-        stop_colors.append(color)
-    if isinstance(offsets, list):
-        offsets = torch.tensor(offsets)
-    if isinstance(stop_colors, list):
-        stop_colors = torch.tensor(stop_colors)
-    return offsets, stop_colors
+# --------------------------------------------------------------------------
+# paint servers and class rules
+
+def _stops(element, defs, inherited):
+    """Offsets and colours of the <stop> children.  A gradient with an href
+    keeps its parent's stop tensors; pydiffvg cannot add stops of its own to
+    those (it appends to the tensors), and neither can this reader."""
+    own = [s for s in element if _tag(s) == 'stop']
+    if inherited is not None:
+        if own:
+            raise ValueError('a gradient with an href cannot add <stop> elements to its parent\'s stops')
+        return inherited
+    offsets, colors = [], []
+    for stop in own:
+        rgba = [0.0, 0.0, 0.0, 1.0]
+        decl = {'stop-color': stop.attrib.get('stop-color'), 'stop-opacity': stop.attrib.get('stop-opacity')}
+        if 'style' in stop.attrib:
+            style = parse_style(stop.attrib['style'], defs)
+            decl.update({k: style[k] for k in ('stop-color', 'stop-opacity') if k in style})
+        if decl['stop-color'] is not None:
+            c = parse_color(decl['stop-color'], defs)
+            rgba[:3] = [c[0], c[1], c[2]]
+        if decl['stop-opacity'] is not None:
+            rgba[3] = float(decl['stop-opacity'])
+        offsets.append(float(stop.attrib['offset']))
+        colors.append(rgba)
+    return torch.tensor(offsets), torch.tensor(colors)
 
 
-def _inherited(node, defs):
-    for key in node.attrib:
-        if remove_namespaces(key) == 'href':
-            return defs[node.attrib[key].lstrip('#')]
-    return None
+def _linear_gradient(element, defs):
+    """parse_svg.py:137-199: x1 / y1 / x2 / y2 written into the (possibly
+    inherited) end-point tensors, then gradientTransform applied."""
+    parent = defs[_attr(element, 'href').lstrip('#')] if _attr(element, 'href') is not None else None
+    begin = parent.begin if parent is not None else torch.tensor([0.0, 0.0])
+    end = parent.end if parent is not None else torch.tensor([0.0, 0.0])
+    for name, (vec, k) in (('x1', (begin, 0)), ('y1', (begin, 1)), ('x2', (end, 0)), ('y2', (end, 1))):
+        value = _attr(element, name)
+        if value is not None:
+            vec[k] = float(value)
+    m = torch.eye(3)
+    if _attr(element, 'gradientTransform') is not None:
+        m = m @ parse_transform(_attr(element, 'gradientTransform'))
+    offsets, colors = _stops(element, defs, (parent.offsets, parent.stop_colors) if parent is not None else None)
+    return LinearGradient(_apply(m, begin), _apply(m, end), offsets, colors)
 
 
-def parse_linear_gradient(node, transform, defs):
-    begin, end = torch.tensor([0.0, 0.0]), torch.tensor([0.0, 0.0])
-    offsets, stop_colors = [], []
-    parent = _inherited(node, defs)
-    if parent is not None:
-        begin, end, offsets, stop_colors = parent.begin, parent.end, parent.offsets, parent.stop_colors
-    for key in node.attrib:
-        a = remove_namespaces(key)
-        if a == 'x1':
-            begin[0] = float(node.attrib['x1'])
-        elif a == 'y1':
-            begin[1] = float(node.attrib['y1'])
-        elif a == 'x2':
-            end[0] = float(node.attrib['x2'])
-        elif a == 'y2':
-            end[1] = float(node.attrib['y2'])
-        elif a == 'gradientTransform':
-            transform = transform @ parse_transform(node.attrib['gradientTransform'])
-    begin, end = _xform_point(transform, begin), _xform_point(transform, end)
-    offsets, stop_colors = _stops(node, defs, offsets, stop_colors)
-    return LinearGradient(begin, end, offsets, stop_colors)
+def _radial_gradient(element, defs):
+    """parse_svg.py:201-263 reads cx / cy / r but builds the gradient from its
+    unset begin / end: centre and radius are (0, 0), or the end points of an
+    inherited linear gradient."""
+    parent = defs[_attr(element, 'href').lstrip('#')] if _attr(element, 'href') is not None else None
+    center = getattr(parent, 'begin', torch.tensor([0.0, 0.0]))
+    radius = getattr(parent, 'end', torch.tensor([0.0, 0.0]))
+    offsets, colors = _stops(element, defs, (parent.offsets, parent.stop_colors) if parent is not None else None)
+    return RadialGradient(center, radius, offsets, colors)
 
 
-def parse_radial_gradient(node, transform, defs):
-    # the reference reads cx / cy / fx / fy / fr but builds the gradient from
-    # its unset begin / end (parse_svg.py:201-263): centre and radius (0, 0)
-    begin, end = torch.tensor([0.0, 0.0]), torch.tensor([0.0, 0.0])
-    offsets, stop_colors = [], []
-    parent = _inherited(node, defs)
-    if parent is not None:
-        begin, end = getattr(parent, 'begin', begin), getattr(parent, 'end', end)
-        offsets, stop_colors = parent.offsets, parent.stop_colors
-    offsets, stop_colors = _stops(node, defs, offsets, stop_colors)
-    return RadialGradient(begin, end, offsets, stop_colors)
+def _class_rules(element, defs):
+    """Class rules ('.name { declarations }') of a <style> element."""
+    text = re.sub(r'/\*.*?\*/', '', element.text or '', flags=re.S)
+    for selector, body in re.findall(r'([^{}]+)\{([^{}]*)\}', text):
+        selector = selector.strip()
+        if len(selector) > 1 and selector.startswith('.'):
+            defs[selector[1:]] = parse_style(body, defs)
 
 
-def parse_stylesheet(node, transform, defs):
-    """Class rules ('.name { key: value; ... }') of a <style> element."""
-    text = node.text or ''
-    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
-    for sel, body in re.findall(r'([^{}]+)\{([^{}]*)\}', text):
-        name = sel.strip()
-        if len(name) >= 2 and name[0] == '.':
-            defs[name[1:]] = parse_style(body, defs)
-    return defs
-
-
-def parse_defs(node, transform, defs):
-    for child in node:
-        tag = remove_namespaces(child.tag)
-        if tag == 'linearGradient' and 'id' in child.attrib:
-            defs[child.attrib['id']] = parse_linear_gradient(child, transform, defs)
-        elif tag == 'radialGradient' and 'id' in child.attrib:
-            defs[child.attrib['id']] = parse_radial_gradient(child, transform, defs)
-        elif tag == 'style':
-            defs = parse_stylesheet(child, transform, defs)
-    return defs
-
-
-def _half_width(v):
-    if v[-2:] == 'px':
-        v = v[:-2]
-    return torch.tensor(float(v) / 2.0)
-
-
-def _fill_rule(v, current):
-    if v == 'evenodd':
-        return True
-    if v == 'nonzero':
+def _register(element, defs):
+    """Adds a definition element (gradient with an id, or style sheet) to
+    `defs`; returns whether the element was one."""
+    tag = _tag(element)
+    if tag == 'style':
+        _class_rules(element, defs)
+    elif tag in ('linearGradient', 'radialGradient'):
+        if 'id' in element.attrib:
+            build = _linear_gradient if tag == 'linearGradient' else _radial_gradient
+            defs[element.attrib['id']] = build(element, defs)
+    else:
         return False
-    warnings.warn('Unknown fill-rule: {}'.format(v))
-    return current
+    return True
 
 
-def parse_common_attrib(node, transform, fill_color, defs):
-    """Transform, fill, stroke, half stroke width and fill rule of an element
-    (parse_svg.py:288-387)."""
-    attribs = {}
-    if 'class' in node.attrib:
-        attribs.update(defs[node.attrib['class']])
-    attribs.update(node.attrib)
-    stroke_color = None
-    stroke_width = torch.tensor(0.5)
-    even_odd = False
-    new_transform = transform
-    if 'transform' in attribs:
-        new_transform = transform @ parse_transform(attribs['transform'])
-    if 'fill' in attribs:
-        fill_color = parse_color(attribs['fill'], defs)
-    fill_opacity = 1.0
-    if 'fill-opacity' in attribs:
-        fill_opacity *= float(attribs['fill-opacity'])
-    if 'opacity' in attribs:
-        fill_opacity *= float(attribs['opacity'])
-    if isinstance(fill_color, torch.Tensor):
-        fill_color[3] = fill_opacity
-    if 'fill-rule' in attribs:
-        even_odd = _fill_rule(attribs['fill-rule'], even_odd)
-    if 'stroke' in attribs:
-        stroke_color = parse_color(attribs['stroke'], defs)
-    if 'stroke-width' in attribs:
-        stroke_width = _half_width(attribs['stroke-width'])
-    if 'stroke-opacity' in attribs:
-        stroke_color[3] = torch.tensor(float(attribs['stroke-opacity']))
-    if 'style' in attribs:
-        st = parse_style(attribs['style'], defs)
-        if 'fill' in st:
-            fill_color = parse_color(st['fill'], defs)
-        fill_opacity = 1.0
-        if 'fill-opacity' in st:
-            fill_opacity *= float(st['fill-opacity'])
-        if 'opacity' in st:
-            fill_opacity *= float(st['opacity'])
-        if 'fill-rule' in st:
-            even_odd = _fill_rule(st['fill-rule'], even_odd)
-        if isinstance(fill_color, torch.Tensor):
-            fill_color[3] = fill_opacity
-        if 'stroke' in st:
-            # parse_style already turned 'none' into None, which replaces an
-            # attribute's stroke here as in the reference
-            stroke_color = parse_color(st['stroke'], defs)
-            if isinstance(stroke_color, torch.Tensor):
-                if 'stroke-opacity' in st:
-                    stroke_color[3] = float(st['stroke-opacity'])
-                if 'opacity' in st:
-                    stroke_color[3] *= float(st['opacity'])
-            if 'stroke-width' in st:
-                stroke_width = _half_width(st['stroke-width'])
-        for paint in (fill_color, stroke_color):
-            if isinstance(paint, LinearGradient):
-                paint.begin = _xform_point(new_transform, paint.begin)
-                paint.end = _xform_point(new_transform, paint.end)
-    return new_transform, fill_color, stroke_color, stroke_width, even_odd
+# --------------------------------------------------------------------------
+# style resolution
+
+@dataclass
+class _Resolved:
+    transform: object
+    fill: object
+    stroke: object = None
+    half_width: object = None
+    even_odd: bool = False
 
 
-def is_shape(tag):
-    return tag in ('path', 'polygon', 'line', 'circle', 'rect')
+def _opacity(decl):
+    return float(decl.get('fill-opacity', 1.0)) * float(decl.get('opacity', 1.0))
 
 
-def _group(shapes, shape_groups, new_shapes, fill, stroke, even_odd, xform, name, with_xform=True):
-    first = len(shapes)
-    shapes = shapes + new_shapes
-    kw = dict(shape_ids=torch.tensor(list(range(first, len(shapes)))), fill_color=fill, stroke_color=stroke,
-              use_even_odd_rule=even_odd, id=name)
-    if with_xform:
-        kw['shape_to_canvas'] = xform
-    shape_groups.append(ShapeGroup(**kw))
-    return shapes
+def _resolve(element, transform, fill, defs):
+    """The element's resolved style (parse_svg.py:288-387): its class rule
+    overridden by its attributes (the presentation), then its style
+    attribute, each with pydiffvg's rules."""
+    presentation = dict(defs[element.attrib['class']]) if 'class' in element.attrib else {}
+    presentation.update(element.attrib)
+    r = _Resolved(transform, fill, half_width=torch.tensor(0.5))
+    if 'transform' in presentation:
+        r.transform = transform @ parse_transform(presentation['transform'])
+    # presentation: the fill's alpha becomes the product of the opacities
+    # given (1 when none is), written into the fill tensor itself
+    if 'fill' in presentation:
+        r.fill = parse_color(presentation['fill'], defs)
+    if isinstance(r.fill, torch.Tensor):
+        r.fill[3] = _opacity(presentation)
+    if 'fill-rule' in presentation:
+        r.even_odd = _even_odd(presentation['fill-rule'], r.even_odd)
+    if 'stroke' in presentation:
+        r.stroke = parse_color(presentation['stroke'], defs)
+    if 'stroke-width' in presentation:
+        r.half_width = _half_width(presentation['stroke-width'])
+    if 'stroke-opacity' in presentation:
+        r.stroke[3] = torch.tensor(float(presentation['stroke-opacity']))
+    if 'style' not in presentation:
+        return r
+    # inline style: its own opacities replace the fill's alpha again; stroke
+    # opacity and width count only together with a stroke
+    inline = parse_style(presentation['style'], defs)
+    if 'fill' in inline:
+        r.fill = parse_color(inline['fill'], defs)
+    if 'fill-rule' in inline:
+        r.even_odd = _even_odd(inline['fill-rule'], r.even_odd)
+    if isinstance(r.fill, torch.Tensor):
+        r.fill[3] = _opacity(inline)
+    if 'stroke' in inline:
+        r.stroke = parse_color(inline['stroke'], defs)
+        if isinstance(r.stroke, torch.Tensor):
+            if 'stroke-opacity' in inline:
+                r.stroke[3] = float(inline['stroke-opacity'])
+            if 'opacity' in inline:
+                r.stroke[3] *= float(inline['opacity'])
+        if 'stroke-width' in inline:
+            r.half_width = _half_width(inline['stroke-width'])
+    for paint in (r.fill, r.stroke):
+        if isinstance(paint, LinearGradient):
+            paint.begin = _apply(r.transform, paint.begin)
+            paint.end = _apply(r.transform, paint.end)
+    return r
 
 
-def parse_shape(node, transform, fill_color, shapes, shape_groups, defs):
-    """One shape element -> shapes and one group (parse_svg.py:392-516)."""
-    tag = remove_namespaces(node.tag)
-    xform, fill, stroke, width, even_odd = parse_common_attrib(node, transform, fill_color, defs)
-    name = node.attrib.get('id', '')
+# --------------------------------------------------------------------------
+# shape emission
+
+def _numbers(text):
+    return [float(v) for v in re.split(r'[\s,]+', text.strip()) if v]
+
+
+def _emit(element, style, shapes, groups):
+    """Appends the element's shapes and one group for them
+    (parse_svg.py:392-516).  Path points are mapped to the canvas and their
+    group keeps the identity transform; the other shapes keep their own
+    coordinates under the group's transform."""
+    tag = _tag(element)
+    a = element.attrib
+    name = a.get('id', '')
+    closed = style.fill is not None
+    group_id, with_transform = '', True
     if tag == 'path':
-        # the path's points are mapped to the canvas; its group keeps the identity
-        paths = from_svg_path(node.attrib['d'], xform, fill is not None)
-        for k, p in enumerate(paths):
-            p.stroke_width = width
+        new = from_svg_path(a['d'], style.transform, closed)
+        for k, p in enumerate(new):
             p.source_id = name
-            p.id = '{}-{}'.format(name, k) if len(paths) > 1 else name
-        shapes = _group(shapes, shape_groups, paths, fill, stroke, even_odd, xform, name, with_xform=False)
+            p.id = '{}-{}'.format(name, k) if len(new) > 1 else name
+        group_id, with_transform = name, False
     elif tag == 'polygon':
-        # coordinates separated by spaces and / or commas, read in pairs (the
-        # reference reads "x,y x,y ..." and "x y x y ..." the same way)
-        nums = [float(v) for v in re.split(r'[\s,]+', node.attrib['points'].strip()) if v]
-        poly = Polygon(torch.tensor(nums, dtype=torch.float32).view(-1, 2), fill is not None)
-        poly.stroke_width = width
-        shapes = _group(shapes, shape_groups, [poly], fill, stroke, even_odd, xform, name)
+        new = [Polygon(torch.tensor(_numbers(a['points']), dtype=torch.float32).view(-1, 2), closed)]
+        group_id = name
     elif tag == 'line':
-        pts = torch.tensor([[float(node.attrib['x1']), float(node.attrib['y1'])],
-                            [float(node.attrib['x2']), float(node.attrib['y2'])]])
-        line = Polygon(pts, False)
-        line.stroke_width = width
-        shapes = _group(shapes, shape_groups, [line], fill, stroke, even_odd, xform, '')
+        ends = [[float(a['x1']), float(a['y1'])], [float(a['x2']), float(a['y2'])]]
+        new = [Polygon(torch.tensor(ends), False)]
     elif tag == 'circle':
-        c = Circle(radius=torch.tensor(float(node.attrib['r'])),
-                   center=torch.tensor([float(node.attrib['cx']), float(node.attrib['cy'])]))
-        c.stroke_width = width
-        shapes = _group(shapes, shape_groups, [c], fill, stroke, even_odd, xform, '')
-    elif tag == 'rect':
-        # parse_svg.py:488-500: x / y are never read and p_max = (x + w, x + h)
-        x = y = 0.0
-        w, h = float(node.attrib['width']), float(node.attrib['height'])
-        r = Rect(p_min=torch.tensor([x, y]), p_max=torch.tensor([x + w, x + h]))
-        r.stroke_width = width
-        shapes = _group(shapes, shape_groups, [r], fill, stroke, even_odd, xform, '')
-    return shapes, shape_groups
+        new = [Circle(radius=torch.tensor(float(a['r'])), center=torch.tensor([float(a['cx']), float(a['cy'])]))]
+    else:  # rect
+        w, h = float(a['width']), float(a['height'])
+        new = [Rect(p_min=torch.tensor([0.0, 0.0]), p_max=torch.tensor([w, h]))]
+    for s in new:
+        s.stroke_width = style.half_width
+    ids = torch.tensor(list(range(len(shapes), len(shapes) + len(new))))
+    shapes.extend(new)
+    kw = dict(shape_ids=ids, fill_color=style.fill, stroke_color=style.stroke, use_even_odd_rule=style.even_odd,
+              id=group_id)
+    if with_transform:
+        kw['shape_to_canvas'] = style.transform
+    groups.append(ShapeGroup(**kw))
 
 
-def parse_group(node, transform, fill_color, shapes, shape_groups, defs):
-    if 'transform' in node.attrib:
-        transform = transform @ parse_transform(node.attrib['transform'])
-    if 'fill' in node.attrib:
-        fill_color = parse_color(node.attrib['fill'], defs)
-    for child in node:
-        tag = remove_namespaces(child.tag)
-        if is_shape(tag):
-            shapes, shape_groups = parse_shape(child, transform, fill_color, shapes, shape_groups, defs)
+def _walk(element, transform, fill, defs, shapes, groups, top_level):
+    """Shapes and groups under `element` in document order.  Definitions are
+    read at the top level and in <defs>; a <g> passes down only its
+    transform and fill attributes."""
+    for child in element:
+        tag = _tag(child)
+        if tag in _SHAPE_TAGS:
+            _emit(child, _resolve(child, transform, fill, defs), shapes, groups)
         elif tag == 'g':
-            shapes, shape_groups = parse_group(child, transform, fill_color, shapes, shape_groups, defs)
-    return shapes, shape_groups
+            t = transform @ parse_transform(child.attrib['transform']) if 'transform' in child.attrib else transform
+            f = parse_color(child.attrib['fill'], defs) if 'fill' in child.attrib else fill
+            _walk(child, t, f, defs, shapes, groups, False)
+        elif top_level and tag == 'defs':
+            for d in child:
+                _register(d, defs)
+        elif top_level:
+            _register(child, defs)
 
 
 def parse_scene(node):
-    """Root <svg> element -> (canvas_width, canvas_height, shapes, shape_groups)."""
+    """The root <svg> element as (canvas_width, canvas_height, shapes,
+    shape_groups) (parse_svg.py:533-572)."""
     width = height = -1
-    defs, shapes, shape_groups = {}, [], []
-    fill_color = torch.tensor([0.0, 0.0, 0.0, 1.0])
-    transform = torch.eye(3)
     if 'viewBox' in node.attrib:
-        vb = node.attrib['viewBox'].split()
-        width, height = parse_int(vb[2]), parse_int(vb[3])
+        box = node.attrib['viewBox'].split()
+        width, height = _length(box[2]), _length(box[3])
     else:
-        if 'width' in node.attrib:
-            width = parse_int(node.attrib['width'])
-        else:
-            warnings.warn("Can't find canvas width.")
-        if 'height' in node.attrib:
-            height = parse_int(node.attrib['height'])
-        else:
-            warnings.warn("Can't find canvas height.")
-    for child in node:
-        tag = remove_namespaces(child.tag)
-        if tag == 'defs':
-            defs = parse_defs(child, transform, defs)
-        elif tag == 'style':
-            defs = parse_stylesheet(child, transform, defs)
-        elif tag == 'linearGradient' and 'id' in child.attrib:
-            defs[child.attrib['id']] = parse_linear_gradient(child, transform, defs)
-        elif tag == 'radialGradient' and 'id' in child.attrib:
-            defs[child.attrib['id']] = parse_radial_gradient(child, transform, defs)
-        elif is_shape(tag):
-            shapes, shape_groups = parse_shape(child, transform, fill_color, shapes, shape_groups, defs)
-        elif tag == 'g':
-            shapes, shape_groups = parse_group(child, transform, fill_color, shapes, shape_groups, defs)
-    return width, height, shapes, shape_groups
+        for key in ('width', 'height'):
+            if key in node.attrib:
+                value = _length(node.attrib[key])
+                width, height = (value, height) if key == 'width' else (width, value)
+            else:
+                warnings.warn("Can't find canvas {}.".format(key))
+    shapes, groups = [], []
+    _walk(node, torch.eye(3), torch.tensor([0.0, 0.0, 0.0, 1.0]), {}, shapes, groups, True)
+    return width, height, shapes, groups
 
 
 def svg_to_scene(filename):

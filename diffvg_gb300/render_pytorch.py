@@ -55,6 +55,14 @@ _THICKNESS_PLACEHOLDER = torch.tensor(0.0)
 _cache_lock = threading.Lock()
 _scene_cache = OrderedDict()
 _token = itertools.count(1)
+_ints = {}
+
+
+def _intern(v):
+    """One object per integer value, so that repeated serialize_scene calls
+    give argument lists of identical objects (the packing cache's identity
+    key)."""
+    return _ints.setdefault(v, v) if type(v) is int and len(_ints) < 4096 else v
 
 
 def _native_scene(packed, device):
@@ -136,8 +144,8 @@ class RenderFunction:
             filter = _DEFAULT_FILTER
         if eval_positions is None:
             eval_positions = _EMPTY_EVAL
-        args = [canvas_width, canvas_height, len(shapes), len(shape_groups), output_type, use_prefiltering,
-                eval_positions]
+        args = [_intern(canvas_width), _intern(canvas_height), _intern(len(shapes)), _intern(len(shape_groups)),
+                output_type, use_prefiltering, eval_positions]
         for shp in shapes:
             use_thickness = False
             if isinstance(shp, _shape.Circle) or type(shp).__name__ == 'Circle':

@@ -86,6 +86,57 @@ def fill_scene(mod, seed=3, num_paths=512, canvas=1024, seg_range=(8, 32), radiu
     return canvas, canvas, shapes, groups
 
 
+def blob_scene(mod, seed=5, num_paths=512, canvas=1024, seg_range=(8, 32), radius_range=(10.0, 120.0),
+               lobes=(3, 7), amplitude=0.2, stroke_fraction=0.1, width_range=(0.5, 3.0)):
+    """Closed smooth cubic paths of a chosen segment count: the same shape
+    family whatever the count, for measuring how the cost per sample grows
+    with the segments per path.
+
+    Each path follows r(a) = R (1 + amplitude sin(k a + phase)) around its
+    centre, cut into n cubic segments whose control points come from the
+    curve's tangents (a C1 closed curve).  Draw order per path: n U{seg_range},
+    centre U[0,canvas)^2, R U[radius_range], k U{lobes}, phase U[0, 2 pi),
+    then the paints as in fill_scene (i%4 in {0,1}: RGBA U[0,1]^4; 2: linear,
+    3: radial, 3 stops of RGBA U[0,1]^4 at offsets 0, .5, 1), then a stroke
+    coin U[0,1) < stroke_fraction with half-width U[width_range] and RGBA
+    U[0,1]^4."""
+    gen = torch.Generator().manual_seed(seed)
+    shapes, groups = [], []
+    for i in range(num_paths):
+        n = int(torch.randint(seg_range[0], seg_range[1] + 1, (1,), generator=gen)[0])
+        c = _u(gen, 2, hi=float(canvas))
+        R = float(_u(gen, 1, lo=radius_range[0], hi=radius_range[1])[0])
+        k = int(torch.randint(lobes[0], lobes[1] + 1, (1,), generator=gen)[0])
+        phase = float(_u(gen, 1, hi=2.0 * math.pi)[0])
+        a = torch.arange(n, dtype=torch.float64) * (2.0 * math.pi / n)
+        r = R * (1.0 + amplitude * torch.sin(k * a + phase))
+        dr = R * amplitude * k * torch.cos(k * a + phase)
+        p = torch.stack([c[0] + r * torch.cos(a), c[1] + r * torch.sin(a)], 1)
+        # tangent per unit of a, scaled to one segment's span of a
+        t = torch.stack([dr * torch.cos(a) - r * torch.sin(a), dr * torch.sin(a) + r * torch.cos(a)], 1)
+        t = t * (2.0 * math.pi / n)
+        nxt = torch.roll(torch.arange(n), -1)
+        pts = torch.stack([p, p + t / 3.0, p[nxt] - t[nxt] / 3.0], 1).reshape(3 * n, 2).to(torch.float32)
+        shapes.append(mod.Path(num_control_points=torch.full((n,), 2, dtype=torch.int32), points=pts.contiguous(),
+                               is_closed=True, stroke_width=torch.tensor(1.0)))
+        kind = i % 4
+        cf = c.to(torch.float32)
+        if kind in (0, 1):
+            fill = _u(gen, 4)
+        elif kind == 2:
+            fill = mod.LinearGradient(begin=cf - R, end=cf + R, offsets=torch.tensor([0.0, 0.5, 1.0]),
+                                      stop_colors=_u(gen, 3, 4))
+        else:
+            fill = mod.RadialGradient(center=cf.clone(), radius=torch.tensor([R, R]),
+                                      offsets=torch.tensor([0.0, 0.5, 1.0]), stop_colors=_u(gen, 3, 4))
+        stroke = None
+        if float(_u(gen, 1)[0]) < stroke_fraction:
+            shapes[-1].stroke_width = _u(gen, 1, lo=width_range[0], hi=width_range[1])[0]
+            stroke = _u(gen, 4)
+        groups.append(mod.ShapeGroup(shape_ids=torch.tensor([i]), fill_color=fill, stroke_color=stroke))
+    return canvas, canvas, shapes, groups
+
+
 def batched_scenes(mod, seeds=range(100, 164), canvases=(64, 128, 256, 512), path_range=(16, 1024)):
     """Config 4: independent stroke scenes of uneven size.
 

@@ -38,6 +38,29 @@ CASES = {
     <circle cx="10" cy="10" r="4" style="fill:#ff00ff;fill-opacity:0.5;stroke:#000000;stroke-width:1"/>
   </g>
 </svg>''',
+    'inheritance_and_opacity': '''<svg xmlns="http://www.w3.org/2000/svg" xmlns:xlink="http://www.w3.org/1999/xlink"
+     width="50" height="40">
+  <radialGradient id="rg" cx="5" cy="5" r="3">
+    <stop offset="0" stop-color="red"/>
+    <stop offset="0.5" stop-color="navy" stop-opacity="0.3"/>
+    <stop offset="1" style="stop-color:#0f0"/>
+  </radialGradient>
+  <linearGradient id="base" x1="1" y1="2" x2="3" y2="4">
+    <stop offset="0" stop-color="#fff"/><stop offset="1" stop-color="#000"/>
+  </linearGradient>
+  <linearGradient id="derived" xlink:href="#base" x2="9" gradientTransform="translate(1,1)"/>
+  <style>.c1 { fill: #204060; fill-opacity: 0.5 } .c2 { stroke: #abcdef; stroke-width: 3 }</style>
+  <g fill="#808000" transform="translate(2,3)">
+    <path d="M1 1 L9 1 L9 9 Z" fill-opacity="0.25"/>
+    <path d="M11 1 L19 1 L19 9 Z"/>
+    <circle cx="30" cy="10" r="4" class="c1"/>
+    <circle cx="40" cy="10" r="4" class="c2" fill="url(#derived)" style="stroke:#123456;stroke-width:2"/>
+    <circle cx="45" cy="30" r="3" fill="url(#rg)" stroke="navy"/>
+  </g>
+  <rect width="5" height="6" style="fill:teal;opacity:0.5;stroke:black;stroke-opacity:0.4"
+        transform="translate(10 20)"/>
+  <path d="M20 20 L30 20 L30 30 Z" fill="url(#derived)" style="stroke:#ff0000"/>
+</svg>''',
 }
 
 
