@@ -395,10 +395,24 @@ bool hit_matches(const DvgScene *sc, const DvgRenderArgs *a) {
          sc->hit_seed == a->seed;
 }
 
+// Deferred fp64 walks of the paired boundary pass (scenes of 8+ groups):
+// room for one job and four candidate fragments per boundary sample; a warp
+// that finds no room solves its jobs in place.
+bool edge_defers(const DvgScene *sc, size_t n) { return sc->d.num_groups >= 8 && n < (1u << 30); }
+size_t edge_job_cap(size_t n) { return n; }
+size_t edge_frag_cap(size_t n) { return 4 * n; }
+
 size_t edge_bytes(DvgScene *sc, size_t n) {
   size_t T = (size_t)sc->tiles_x * sc->tiles_y * DVG_EDGE_CELLS;
-  return carve_size({n * sizeof(float4), n * sizeof(float4), n * sizeof(int4), n * sizeof(float2), n * sizeof(int),
-                     n * sizeof(int), n * sizeof(int), T * sizeof(int), (T + 1) * sizeof(int)});
+  std::vector<size_t> b = {n * sizeof(float4), n * sizeof(float4), n * sizeof(int4), n * sizeof(float2),
+                           n * sizeof(int), n * sizeof(int), n * sizeof(int), T * sizeof(int), (T + 1) * sizeof(int)};
+  if (edge_defers(sc, n)) {
+    size_t jc = edge_job_cap(n), fc = edge_frag_cap(n);
+    for (size_t x : {jc * sizeof(int4), jc * sizeof(float4), 2 * n * sizeof(int4), 2 * n * sizeof(unsigned),
+                     2 * n * sizeof(float4), fc * sizeof(int2), n * sizeof(int), 4 * sizeof(int)})
+      b.push_back(x);
+  }
+  return carve_size(b);
 }
 
 EdgeRecords edge_records(DvgScene *sc, size_t n) {
@@ -414,6 +428,19 @@ EdgeRecords edge_records(DvgScene *sc, size_t n) {
   E.order = carve<int>(p, n);
   E.tile_count = carve<int>(p, T);
   E.tile_start = carve<int>(p, T + 1);
+  if (edge_defers(sc, n)) {
+    size_t jc = edge_job_cap(n), fc = edge_frag_cap(n);
+    E.job_a = carve<int4>(p, jc);
+    E.job_b = carve<float4>(p, jc);
+    E.dq = carve<int4>(p, 2 * n);
+    E.dq_res = carve<unsigned>(p, 2 * n);
+    E.dq_col = carve<float4>(p, 2 * n);
+    E.frag = carve<int2>(p, fc);
+    E.ds = carve<int>(p, n);
+    E.counts = carve<int>(p, 4);
+    E.job_cap = (int)std::min(jc, (size_t)0x7fffffff);
+    E.frag_cap = (int)std::min(fc, (size_t)0x7fffffff);
+  }
   return E;
 }
 

@@ -124,6 +124,22 @@ struct EdgeRecords {
   float2 *d;        // segment t, is_stroke
   int *key, *rank, *order;
   int *tile_count, *tile_start;  // per ordering cell: [tiles * DVG_EDGE_CELLS] (+1)
+  // Deferred fp64 root walks of the paired-lane pass (null job_a: none).  A
+  // colour query q (= 2 * sorted sample position + side) whose queued
+  // segment tests the fp32 decision leaves open hands them to the job list
+  // and keeps its candidate fragments in frag; k_edge_jobs decides the jobs
+  // with full warps, k_edge_finish blends the deferred queries and
+  // accumulates their samples' gradients.
+  int4 *job_a = nullptr;     // [job_cap] {query, result bit, shape, segment}; query -1: no job
+  float4 *job_b = nullptr;   // [job_cap] {x, y, stroke radius, -} in shape space
+  int4 *dq = nullptr;        // [2n] per query of a deferred sample: {first fragment (-1: finished in the
+                             //   first pass), fragments | edge hit << 30, fp32 results, edge-query job bits}
+  unsigned *dq_res = nullptr;  // [2n] results of the query's deferred jobs
+  float4 *dq_col = nullptr;  // [2n] colour of a query finished in the first pass
+  int2 *frag = nullptr;      // [frag_cap] candidate fragments (key, meta) of deferred queries
+  int *ds = nullptr;         // [n] sorted positions of the deferred samples
+  int *counts = nullptr;     // [4] jobs, -, fragments, deferred samples reserved this call
+  int job_cap = 0, frag_cap = 0;
 };
 // Boundary samples are ordered by canvas tile and, inside a tile, by
 // 2^DVG_EDGE_CELL_SHIFT-pixel square cell in Morton order.
@@ -555,6 +571,28 @@ DI int band_next(const DevScene &S, int &i, int e0, int &j, int e1) {
   return a < b ? a : b;
 }
 
+// Winding number of a path with band lists: only the segments of pt's band
+// (band_lists; the same crossings as winding_shape's full scan).
+DN int winding_banded(const DevScene &S, int s, int po, int np, int so, v2 pt) {
+  int w = 0, b, e, b1, e1;
+  if (band_lists(S, s, pt.y, pt.y, b, e, b1, e1)) {
+    #pragma unroll 1
+    for (int k = b; k < e; k++) {
+      int i = __ldg(&S.seg_order[so + __ldg(&S.band_seg[k])]);
+      if (!box_ray(S.seg_box[so + i], pt)) continue;
+      w += winding_segment(S, po, np, __ldg(&S.segment_ctrl[so + i]), __ldg(&S.seg_point[so + i]), pt);
+    }
+    return w;
+  }
+  int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);  // NaN point: every segment, as the full scan
+  #pragma unroll 1
+  for (int i = 0; i < nseg; i++) {
+    if (!box_ray(S.seg_box[so + i], pt)) continue;
+    w += winding_segment(S, po, np, __ldg(&S.segment_ctrl[so + i]), __ldg(&S.seg_point[so + i]), pt);
+  }
+  return w;
+}
+
 DI int winding_shape(const DevScene &S, int s, v2 pt) {
   int kind = SI(S, s, DVG_SHAPE_KIND);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
@@ -569,16 +607,8 @@ DI int winding_shape(const DevScene &S, int s, v2 pt) {
     return (pt.x > pget(S, po) && pt.x < pget(S, po + 2) && pt.y > pget(S, po + 1) && pt.y < pget(S, po + 3)) ? 1 : 0;
   }
   int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
-  int w = 0, b, e, b1, e1;
-  if (band_lists(S, s, pt.y, pt.y, b, e, b1, e1)) {  // the segments whose box meets pt's band
-    #pragma unroll 1
-    for (int k = b; k < e; k++) {
-      int i = __ldg(&S.seg_order[so + __ldg(&S.band_seg[k])]);
-      if (!box_ray(S.seg_box[so + i], pt)) continue;
-      w += winding_segment(S, po, np, __ldg(&S.segment_ctrl[so + i]), __ldg(&S.seg_point[so + i]), pt);
-    }
-    return w;
-  }
+  if (S.band_n && __ldg(&S.band_n[s]) > 0) return winding_banded(S, s, po, np, so, pt);
+  int w = 0;
   #pragma unroll 1
   for (int i = 0; i < nseg; i++) {
     if (nseg > 1 && !box_ray(S.seg_box[so + i], pt)) continue;
@@ -1363,22 +1393,28 @@ DI bool group_stroke(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
 // closest point / distance (compute_distance.h:12-439)
 struct PathInfo { int base_point_id, point_id; float t_root; };
 
-DN bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
+// Closest point of path s to pt within max_radius (closest_point(Path),
+// compute_distance.h:26-311), over its segments in visiting order; with
+// BANDED, over the band lists that cover pt.y +- max_radius (grown by a
+// rounding margin: every segment box_in_r can pass), merged in visiting
+// order, so that ties resolve as in the full scan.
+template <bool BANDED>
+DN bool closest_path_t(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
   int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF), flags = SI(S, s, DVG_SHAPE_FLAGS);
   float min_dist = max_radius;
   v2 ret = V2(0, 0);
   bool found = false;
-  // with a finite search radius, the band list that covers pt.y +- radius
-  // (grown by a rounding margin) holds every segment box_in_r can pass, in
-  // visiting order
-  float slack = max_radius + 1e-5f * (fabsf(pt.y) + max_radius + 1.f);
-  int i0 = 0, e0 = 0, i1 = 0, e1 = 0;
-  bool banded = max_radius < INFINITY && band_lists(S, s, pt.y - slack, pt.y + slack, i0, e0, i1, e1);
+  int bi0 = 0, be0 = 0, bi1 = 0, be1 = 0;
+  if (BANDED) {
+    float slack = max_radius + 1e-5f * (fabsf(pt.y) + max_radius + 1.f);
+    if (!band_lists(S, s, pt.y - slack, pt.y + slack, bi0, be0, bi1, be1))
+      return closest_path_t<false>(S, s, pt, max_radius, info, result);
+  }
   #pragma unroll 1
-  for (int k = 0; banded || k < nseg; k++) {
+  for (int k = 0; BANDED || k < nseg; k++) {
     int rank = k;
-    if (banded && (rank = band_next(S, i0, e0, i1, e1)) < 0) break;
+    if (BANDED && (rank = band_next(S, bi0, be0, bi1, be1)) < 0) break;
     int seg = S.seg_order[so + rank];
     if (nseg > 1 && !box_in_r(S.seg_box[so + seg], pt, min_dist)) continue;
     int nc = __ldg(&S.segment_ctrl[so + seg]), i0 = __ldg(&S.seg_point[so + seg]);
@@ -1469,6 +1505,12 @@ DN bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo
   }
   *result = ret;
   return found;
+}
+
+DI bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
+  if (max_radius < INFINITY && S.band_n && __ldg(&S.band_n[s]) > 0)
+    return closest_path_t<true>(S, s, pt, max_radius, info, result);
+  return closest_path_t<false>(S, s, pt, max_radius, info, result);
 }
 
 DN bool closest_shape(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {

@@ -317,17 +317,43 @@ __global__ void k_edge_order(EdgeRecords E, int n) {
   if (key >= 0) E.order[E.tile_start[key] + E.rank[idx]] = idx;
 }
 
+// The end of render_edge_kernel (diffvg.cpp:1418-1474) for one boundary
+// sample whose two colours are known: orient the normal towards the hit
+// side, and accumulate the Reynolds-transport contribution.
+DI void edge_accumulate(const DevScene &S, const DevRender &R, int g, int s, v2 bpt, v2 normal, v2 lpt, float pdf,
+                        float t, const BData &bd, float4 cin, int hin, float4 cout, int hout) {
+  if (!hin && !hout) return;
+  if (!hin) {
+    normal = neg2(normal);
+    float4 tmp = cin; cin = cout; cout = tmp;
+  }
+  int bx = min(max((int)(bpt.x * R.w), 0), R.w - 1), by = min(max((int)(bpt.y * R.h), 0), R.h - 1);
+  v2 sbpt = V2(bpt.x * R.w, bpt.y * R.h);
+  float4 dc = gather_d_color(R, sbpt);
+  float norm = (float)(S.W * S.H);
+  dc = F4(dc.x / norm, dc.y / norm, dc.z / norm, dc.w / norm);
+  float contrib = dot4(sub4(cin, cout), dc) / pdf;
+  accumulate_boundary_gradient(S, g, s, contrib, t, normal, bd, lpt, R.d_params);
+  if (R.d_translation) {
+    atomicAdd(&R.d_translation[2 * (by * R.w + bx) + 0], normal.x * contrib);
+    atomicAdd(&R.d_translation[2 * (by * R.w + bx) + 1], normal.y * contrib);
+  }
+}
+
 // Boundary samples (render_edge_kernel, diffvg.cpp:1388-1475).  With PAIRS
 // set, the two colour queries of a sample (just inside and just outside the
 // boundary) run in adjacent lanes: their points are 2e-4 canvas widths apart,
 // so the two lanes walk the same candidates and tests, and a warp spreads its
 // divergence over 16 samples instead of 32 walked twice; the even lane
-// finishes the sample.  Without PAIRS one lane runs both queries: for scenes
-// of few shapes the walks are short and the gradient atomics, aggregated per
-// warp, are what costs.
+// finishes the sample.  The paired pass also hands the fp64 root walks that
+// its fp32 decision leaves open to k_edge_jobs (sample_color_edge): a sample
+// with such a query is listed in E.ds and finished by k_edge_finish.
+// Without PAIRS one lane runs both queries: for scenes of few shapes the
+// walks are short and the gradient atomics, aggregated per warp, are what
+// costs.
 template <bool PAIRS>
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
-    k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, EdgeRecords E) {
+    k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, const __grid_constant__ EdgeRecords E) {
   __shared__ WarpQueue wq[8];
   const unsigned full = 0xffffffffu;
   DevRender R = load_filter(R0, nullptr);
@@ -350,32 +376,92 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   WarpQueue *q = &wq[threadIdx.x >> 5];
   int lane = threadIdx.x & 31;
   v2 qpt = outside ? add2(bpt, scl2(1e-4f, normal)) : sub2(bpt, scl2(1e-4f, normal));
-  float4 cin = sample_color_fwd(S, bg, qpt, &qq, active, q, lane), cout;
-  int hin = qq.hit, hout;
+  float4 cin, cout;
+  int hin, hout;
   if (PAIRS) {
+    bool deferred = false;
+    if (E.job_a) {
+      cin = sample_color_edge(S, E, bg, qpt, &qq, active, q, lane, (int)gi, deferred);
+    } else {
+      cin = sample_color_fwd(S, bg, qpt, &qq, active, q, lane);
+    }
+    hin = qq.hit;
+    unsigned dm = __ballot_sync(full, deferred);
     cout = F4(__shfl_xor_sync(full, cin.x, 1), __shfl_xor_sync(full, cin.y, 1), __shfl_xor_sync(full, cin.z, 1),
               __shfl_xor_sync(full, cin.w, 1));
     hout = __shfl_xor_sync(full, hin, 1);
+    if (!active) return;
+    if ((dm >> (lane & ~1)) & 3u) {  // the sample waits for deferred jobs: k_edge_finish completes it
+      if (!deferred) {
+        E.dq[gi] = make_int4(-1, hin, 0, 0);
+        E.dq_col[gi] = cin;
+      }
+      if (!outside) E.ds[atomicAdd(&E.counts[3], 1)] = i;
+      return;
+    }
   } else {
+    cin = sample_color_fwd(S, bg, qpt, &qq, active, q, lane);
+    hin = qq.hit;
     EdgeQ qo = {g, s, 0};
     cout = sample_color_fwd(S, bg, add2(bpt, scl2(1e-4f, normal)), &qo, active, q, lane);
     hout = qo.hit;
   }
   if (outside || !active) return;
-  if (!hin && !hout) return;
-  if (!hin) {
-    normal = neg2(normal);
-    float4 tmp = cin; cin = cout; cout = tmp;
+  edge_accumulate(S, R, g, s, bpt, normal, lpt, pdf, t, bd, cin, hin, cout, hout);
+}
+
+// The deferred fp64 root walks of the paired boundary pass, one per thread
+// (full warps): each sets its result bit in its query's dq_res.
+__global__ void __launch_bounds__(256) k_edge_jobs(const __grid_constant__ DevScene S, const __grid_constant__ EdgeRecords E) {
+  int n = min(*(volatile const int *)&E.counts[0], E.job_cap);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    int4 ja = E.job_a[k];
+    if (ja.x < 0) continue;
+    float4 jb = E.job_b[k];
+    int s = ja.z;
+    int hit = segment_root_test(S, SI(S, s, DVG_SHAPE_PARAM_OFF), SI(S, s, DVG_SHAPE_NUM_POINTS),
+                                SI(S, s, DVG_SHAPE_THICKNESS_OFF), __ldg(&S.segment_ctrl[ja.w]),
+                                __ldg(&S.seg_point[ja.w]), V2(jb.x, jb.y), jb.z);
+    if (hit) atomicOr(&E.dq_res[ja.x], 1u << ja.y);
   }
-  v2 sbpt = V2(bpt.x * R.w, bpt.y * R.h);
-  float4 dc = gather_d_color(R, sbpt);
-  float norm = (float)(S.W * S.H);
-  dc = F4(dc.x / norm, dc.y / norm, dc.z / norm, dc.w / norm);
-  float contrib = dot4(sub4(cin, cout), dc) / pdf;
-  accumulate_boundary_gradient(S, g, s, contrib, t, normal, bd, lpt, R.d_params);
-  if (R.d_translation) {
-    atomicAdd(&R.d_translation[2 * (by * R.w + bx) + 0], normal.x * contrib);
-    atomicAdd(&R.d_translation[2 * (by * R.w + bx) + 1], normal.y * contrib);
+}
+
+// The boundary samples whose colour queries were deferred: blend each
+// deferred query's fragments with its fp32 and fp64 results, take the other
+// query's colour from the first pass, and accumulate the sample.
+__global__ void __launch_bounds__(256) k_edge_finish(const __grid_constant__ DevScene S, DevRender R0, const __grid_constant__ EdgeRecords E) {
+  DevRender R = load_filter(R0, nullptr);
+  int n = *(volatile const int *)&E.counts[3];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    int i = E.ds[k];
+    int idx = E.order[i];
+    float4 a = E.a[idx], b = E.b[idx];
+    int4 c = E.c[idx];
+    float2 d = E.d[idx];
+    v2 bpt = V2(a.x, a.y), normal = V2(a.z, a.w), lpt = V2(b.x, b.y);
+    int g = c.x, s = c.y;
+    BData bd = {c.z, c.w, d.x, d.y != 0.f ? 1 : 0};
+    int bx = min(max((int)(bpt.x * R.w), 0), R.w - 1), by = min(max((int)(bpt.y * R.h), 0), R.h - 1);
+    const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (by * R.w + bx) : nullptr;
+    float4 col[2];
+    int hit[2];
+    for (int side = 0; side < 2; side++) {
+      int qid = 2 * i + side;
+      int4 rec = E.dq[qid];
+      if (rec.x < 0) {
+        col[side] = E.dq_col[qid];
+        hit[side] = rec.y;
+        continue;
+      }
+      v2 qpt = side ? add2(bpt, scl2(1e-4f, normal)) : sub2(bpt, scl2(1e-4f, normal));
+      EdgeQ eq = {g, s, (rec.y >> 30) & 1};
+      unsigned res = (unsigned)rec.z | E.dq_res[qid];
+      col[side] = blend_fragments(S, bg, V2(qpt.x * S.W, qpt.y * S.H), &eq,
+                                  reinterpret_cast<const FragRef *>(E.frag + rec.x), rec.y & 0x3fffffff, res,
+                                  (unsigned)rec.w);
+      hit[side] = eq.hit;
+    }
+    edge_accumulate(S, R, g, s, bpt, normal, lpt, b.z, b.w, bd, col[0], hit[0], col[1], hit[1]);
   }
 }
 
@@ -451,8 +537,20 @@ void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cu
   k_edge_sample<<<blocks_of(n), 256, 0, st>>>(S, R, E);
   k_edge_scan<<<1, 1024, 0, st>>>(S, E);
   k_edge_order<<<blocks_of(n), 256, 0, st>>>(E, (int)n);
-  if (S.num_groups >= 8) k_edge_eval<true><<<blocks_of(2 * (long long)n), 256, 0, st>>>(S, R, E);  // two lanes per sample
-  else k_edge_eval<false><<<blocks_of(n), 256, 0, st>>>(S, R, E);
+  if (S.num_groups >= 8) {  // two lanes per sample
+    if (E.job_a) cudaMemsetAsync(E.counts, 0, 4 * sizeof(int), st);
+    k_edge_eval<true><<<blocks_of(2 * (long long)n), 256, 0, st>>>(S, R, E);
+    if (E.job_a) {
+      int dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      unsigned grid = (unsigned)(sms > 0 ? 8 * sms : 1024);
+      k_edge_jobs<<<grid, 256, 0, st>>>(S, E);
+      k_edge_finish<<<grid, 256, 0, st>>>(S, R, E);
+    }
+  } else {
+    k_edge_eval<false><<<blocks_of(n), 256, 0, st>>>(S, R, E);
+  }
 }
 void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
                 const float *d_sdf, cudaStream_t st) {

@@ -75,6 +75,7 @@ struct WarpQueue {
   unsigned result[32];
   int offs[33];
   unsigned char pend[32 * DVG_LANE_JOBS];  // jobs the fp32 decision left open
+  unsigned pend_lanes;                     // lanes that own one of them
 };
 static_assert(32 * DVG_LANE_JOBS <= 256, "job numbers are stored in bytes");
 
@@ -96,10 +97,10 @@ DI const SegJob &warp_job(const WarpQueue *q, int j, int &owner, int &idx) {
   return q->job[lo][idx];
 }
 
-// Decide every queued job of the warp, spread over its lanes: the fp32
-// decision first, then the fp64 solve of the jobs it left open, compacted so
-// that the lanes run those together.
-DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
+// Decide every queued job of the warp, spread over its lanes, with the fp32
+// decision; the jobs it leaves open are listed in q->pend (their owners in
+// q->pend_lanes).  Returns how many (the same in every lane).
+DI int warp_decide(const DevScene &S, WarpQueue *q, int lane, int njobs) {
   const unsigned full = 0xffffffffu;
   int incl = njobs;
 #pragma unroll
@@ -111,6 +112,7 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
   q->offs[lane] = incl - njobs;
   if (lane == 31) q->offs[32] = total;
   q->result[lane] = 0u;
+  if (lane == 0) q->pend_lanes = 0u;
   __syncwarp();
   int npend = 0;
   #pragma unroll 1
@@ -127,10 +129,19 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
     if (valid && f == 1) atomicOr(&q->result[owner], 1u << idx);
     bool pending = valid && f == 2;
     unsigned bal = __ballot_sync(full, pending);
-    if (pending) q->pend[npend + __popc(bal & ((1u << lane) - 1u))] = (unsigned char)j;
+    if (pending) {
+      q->pend[npend + __popc(bal & ((1u << lane) - 1u))] = (unsigned char)j;
+      atomicOr(&q->pend_lanes, 1u << owner);
+    }
     npend += __popc(bal);
   }
   __syncwarp();
+  return npend;
+}
+
+// The fp64 solves of the warp's open jobs, compacted so that as many lanes
+// as there are jobs run them together.
+DI void warp_fp64(const DevScene &S, WarpQueue *q, int lane, int npend) {
   #pragma unroll 1
   for (int k = lane; k < npend; k += 32) {
     int owner, idx;
@@ -142,6 +153,12 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
     if (hit) atomicOr(&q->result[owner], 1u << idx);
   }
   __syncwarp();
+}
+
+// Decide every queued job of the warp: the fp32 decision first, then the
+// fp64 solve of the jobs it left open.
+DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
+  warp_fp64(S, q, lane, warp_decide(S, q, lane, njobs));
 }
 
 // Pass 1 of a sample: candidate fragments in group order, undecided stroke
@@ -267,14 +284,46 @@ DI bool frag_hit(int meta, unsigned res) {
   return ((res >> lo) & mask) != 0u;
 }
 
-// Forward colour of one sample (sample_color, diffvg.cpp:525-655).  With an
-// EdgeQuery the hit flag follows the reference's rule: the last fragment
-// that is either of the queried group (sets it) or opaque (clears it)
-// decides; without such a fragment the flag keeps what the coverage tests
-// of the queried shape set (diffvg.cpp:624-633).
+// Blend of a sample's decided candidate fragments (the end of sample_color,
+// diffvg.cpp:586-655): the fragments of frags[0..nf) that hit (res holds the
+// results of the sample's queued segment tests) in group order over the
+// background.  With an EdgeQuery the hit flag follows the reference's rule:
+// the last fragment that is either of the queried group (sets it) or opaque
+// (clears it) decides; without such a fragment the flag keeps what the
+// coverage tests of the queried shape set (diffvg.cpp:624-633); eq->hit holds
+// that on entry, and eq_jobs marks the queried shape's jobs.  With hit_keys
+// set, the hit fragment keys (blend order) and their count are stored for
+// the backward pass (sample idx of n).
+DI float4 blend_fragments(const DevScene &S, const float4 *bg, v2 pt, EdgeQ *eq, const FragRef *frags, int nf,
+                          unsigned res, unsigned eq_jobs, int *hit_keys = nullptr, unsigned char *hit_cnt = nullptr,
+                          int n = 0, int idx = 0) {
+  if (eq && (res & eq_jobs)) eq->hit = 1;
+  float4 acc = bg ? *bg : F4(0, 0, 0, 0);
+  int nhit = 0, ev = -1;
+  #pragma unroll 1
+  for (int i = 0; i < nf; i++) {
+    FragRef fr = frags[i];
+    if (!frag_hit(fr.meta, res)) continue;
+    int g = fr.key >> 1;
+    float4 c = (fr.key & 1)
+                   ? paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
+                                 GI(S, g, DVG_GROUP_STROKE_STOPS), pt)
+                   : paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF),
+                                 GI(S, g, DVG_GROUP_FILL_STOPS), pt);
+    if (eq) ev = (eq->group == g) ? 1 : (c.w >= 1.f ? 0 : ev);
+    blend(acc, c);
+    if (hit_keys && nhit < DVG_HIT_SLOTS) hit_keys[(size_t)nhit * n + idx] = fr.key;
+    nhit++;
+  }
+  if (hit_cnt) hit_cnt[idx] = nhit > DVG_HIT_SLOTS ? DVG_HIT_NONE : (unsigned char)nhit;
+  if (eq && ev >= 0) eq->hit = ev;
+  if (nhit <= 0) return bg ? *bg : F4(0, 0, 0, 0);
+  return finish_color(acc);
+}
+
+// Forward colour of one sample (sample_color, diffvg.cpp:525-655); see
+// blend_fragments for the EdgeQuery rule and the fragment cache.
 // Out of line: the boundary pass calls it twice per sample.
-// With hit_keys set, the sample's hit fragment keys (blend order) and their
-// count are stored for the backward pass (sample idx of n).
 static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq,
                                                       bool active, WarpQueue *q, int lane, int *hit_keys = nullptr,
                                                       unsigned char *hit_cnt = nullptr, int n = 0, int idx = 0) {
@@ -287,29 +336,78 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
   nf = collect_fragments(S, pt, frags, q, lane, njobs, eq, eq_jobs, overflow, active);
   warp_solve(S, q, lane, njobs);
   if (!active) return F4(0, 0, 0, 0);
-  unsigned res = q->result[lane];
-  if (eq && (res & eq_jobs)) eq->hit = 1;
-  float4 acc = bg ? *bg : F4(0, 0, 0, 0);
-  int nhit = 0, ev = -1;
-  #pragma unroll 1
-  for (int i = 0; i < nf; i++) {
-    if (!frag_hit(frags[i].meta, res)) continue;
-    int g = frags[i].key >> 1;
-    float4 c = (frags[i].key & 1)
-                   ? paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
-                                 GI(S, g, DVG_GROUP_STROKE_STOPS), pt)
-                   : paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF),
-                                 GI(S, g, DVG_GROUP_FILL_STOPS), pt);
-    if (eq) ev = (eq->group == g) ? 1 : (c.w >= 1.f ? 0 : ev);
-    blend(acc, c);
-    if (hit_keys && nhit < DVG_HIT_SLOTS) hit_keys[(size_t)nhit * n + idx] = frags[i].key;
-    nhit++;
+  if (overflow) flag_error(S, DVG_EFLAG_CAPACITY);
+  float4 c = blend_fragments(S, bg, pt, eq, frags, nf, q->result[lane], eq_jobs, hit_keys, hit_cnt, n, idx);
+  if (hit_cnt && overflow) hit_cnt[idx] = DVG_HIT_NONE;
+  return c;
+}
+
+// One colour query of the paired-lane boundary pass (query qid).  As
+// sample_color_fwd, except that the fp64 solves the fp32 decision leaves
+// open are handed to E's job list instead of run here, when the lists have
+// room: the lanes that own such jobs keep their candidate fragments in
+// E.frag and their query state in E.dq[qid], and report deferred = true
+// (their colour comes from k_edge_finish).  Without room the warp solves
+// its jobs in place, as sample_color_fwd does.
+static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const EdgeRecords &E, const float4 *bg,
+                                                       v2 screen_pt, EdgeQ *eq, bool active, WarpQueue *q, int lane,
+                                                       int qid, bool &deferred) {
+  const unsigned full = 0xffffffffu;
+  FragRef frags[DVG_MAX_FRAGMENTS];
+  int nf = 0, njobs = 0;
+  unsigned eq_jobs = 0;
+  bool overflow = false;
+  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+  eq->hit = 0;
+  nf = collect_fragments(S, pt, frags, q, lane, njobs, eq, eq_jobs, overflow, active);
+  int npend = warp_decide(S, q, lane, njobs);
+  deferred = false;
+  if (npend > 0) {
+    bool mine = active && ((q->pend_lanes >> lane) & 1u);
+    // room for the deferring lanes' fragments, then for the warp's jobs
+    int nfr = mine ? nf : 0, incl = nfr;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int v = __shfl_up_sync(full, incl, o);
+      if (lane >= o) incl += v;
+    }
+    int fbase = 0, jbase = 0;
+    if (lane == 31) fbase = atomicAdd(&E.counts[2], incl);
+    fbase = __shfl_sync(full, fbase, 31);
+    bool room = (long long)fbase + __shfl_sync(full, incl, 31) <= E.frag_cap;
+    if (room) {
+      if (lane == 0) jbase = atomicAdd(&E.counts[0], npend);
+      jbase = __shfl_sync(full, jbase, 0);
+      if ((long long)jbase + npend > E.job_cap) {
+        room = false;
+        for (int k = jbase + lane; k < E.job_cap && k < jbase + npend; k += 32) E.job_a[k].x = -1;
+      }
+    }
+    if (room) {
+      int qbase = qid - lane;  // the warp's queries are consecutive
+      #pragma unroll 1
+      for (int k = lane; k < npend; k += 32) {
+        int owner, idx;
+        SegJob jb = warp_job(q, q->pend[k], owner, idx);
+        E.job_a[jbase + k] = make_int4(qbase + owner, idx, jb.shape, jb.seg);
+        E.job_b[jbase + k] = F4(jb.x, jb.y, jb.r, 0.f);
+      }
+      if (mine) {
+        int f0 = fbase + incl - nfr;
+        for (int i = 0; i < nf; i++) E.frag[f0 + i] = make_int2(frags[i].key, frags[i].meta);
+        E.dq[qid] = make_int4(f0, nf | (eq->hit << 30), (int)q->result[lane], (int)eq_jobs);
+        E.dq_res[qid] = 0u;
+        deferred = true;
+      }
+      __syncwarp();
+    } else {
+      warp_fp64(S, q, lane, npend);
+    }
   }
-  if (hit_cnt) hit_cnt[idx] = (overflow || nhit > DVG_HIT_SLOTS) ? DVG_HIT_NONE : (unsigned char)nhit;
-  if (overflow || nhit > DVG_MAX_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
-  if (eq && ev >= 0) eq->hit = ev;
-  if (nhit <= 0) return bg ? *bg : F4(0, 0, 0, 0);
-  return finish_color(acc);
+  if (!active) return F4(0, 0, 0, 0);
+  if (overflow) flag_error(S, DVG_EFLAG_CAPACITY);
+  if (deferred) return F4(0, 0, 0, 0);
+  return blend_fragments(S, bg, pt, eq, frags, nf, q->result[lane], eq_jobs);
 }
 
 // Adjoint of sample_color (diffvg.cpp:525-707 with d_color != nullptr).

@@ -44,6 +44,8 @@ def estimate_device_bytes(packed, width, height, spp):
     # prefiltering 16 fragments of 64 B, and a count
     samples = 16 * n + ((16 * 64 if packed.use_prefiltering else 16 * 4) + 1) * n
     edges = 68 * n                                  # boundary-sample records and ordering
+    if ng >= 8:  # deferred fp64 walks: jobs, per-query state and colours, fragments, deferred samples
+        edges += 32 * n + 2 * (16 + 4 + 16) * n + 4 * 8 * n + 4 * n
     scene = 4 * (8 * ns + 12 * ng + 2 * nseg + 2 * ng) + 64 * ng + 40 * ns + 48 * nseg + 4 * (10 * nseg + 8 * ns)
     scene += (8 * 33 + 4 * 64) * nseg                # tabulated subdivision trees of the segments
     tile_lists = 4 * max(65536, 32 * tiles) * 5 // 4 + 8 * tiles
