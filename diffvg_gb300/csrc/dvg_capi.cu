@@ -168,7 +168,7 @@ int validate_desc(const DvgSceneDesc *d, int *seg_point) {
   if ((d->num_shapes > 0 && !d->shape_info) || (d->num_groups > 0 && !d->group_info) ||
       (d->total_segments > 0 && !d->segment_ctrl) || (d->total_group_shapes > 0 && !d->group_shapes))
     return fail(DVG_ERR_INVALID, "missing topology array");
-  if (d->filter_type < DVG_BOX || d->filter_type > DVG_HANN) return fail(DVG_ERR_INVALID, "unknown filter type");
+  if (d->filter_type < DVG_BOX || d->filter_type > DVG_GAUSSIAN) return fail(DVG_ERR_INVALID, "unknown filter type");
   auto in_params = [&](long long off, long long n) { return off >= 0 && n >= 0 && off + n <= d->num_params; };
   if (!in_params(d->filter_radius_off, 1)) return fail(DVG_ERR_INVALID, "filter radius offset out of range");
   for (int s = 0; s < d->num_shapes; s++) {

@@ -335,9 +335,16 @@ DN int solve_cubic_f(float a, float b, float c, float d, float t[3]) {
 }
 
 // ---------------------------------------------------------------------------
-// pixel filters (filter.h:22-106)
+// pixel filters (filter.h:22-106).  DVG_GAUSSIAN has no counterpart in the
+// reference: a separable Gaussian of standard deviation r / 2 shifted down
+// to reach 0 at the edge of the support |dx|, |dy| <= r (continuous there,
+// so its radius gradient needs no boundary term):
+//   w = g(dx) g(dy),  g(x) = exp(-2 x^2 / r^2) - exp(-2).
+// Weights need no normalisation: pixels divide by their weight sums.
+DI float gauss_1d(float x, float r) { return expf(-2.f * sq(x) / sq(r)) - expf(-2.f); }
 DI float filter_weight(int type, float r, float dx, float dy) {
   if (fabsf(dx) > r || fabsf(dy) > r) return 0;
+  if (type == DVG_GAUSSIAN) return r > 0.f ? gauss_1d(dx, r) * gauss_1d(dy, r) : 0.f;
   if (type == DVG_BOX) return 1.f / sq(2 * r);
   if (type == DVG_TENT) return (r - fabsf(dx)) * (r - fabsf(dy)) / sq(sq(r));
   if (type == DVG_PARABOLIC) return (4.f / 3.f) * (1 - sq(dx / r)) * (4.f / 3.f) * (1 - sq(dy / r));
@@ -345,6 +352,12 @@ DI float filter_weight(int type, float r, float dx, float dy) {
   return 0.5f * (1.f - cosf((float)(2 * DVG_PI) * ndx)) * 0.5f * (1.f - cosf((float)(2 * DVG_PI) * ndy)) / sq(r);
 }
 DI float d_filter_weight(int type, float r, float dx, float dy, float d_ret) {
+  if (type == DVG_GAUSSIAN) {
+    if (!(r > 0.f) || fabsf(dx) > r || fabsf(dy) > r) return 0.f;
+    float r3 = r * r * r;  // dg/dr = exp(-2 x^2 / r^2) 4 x^2 / r^3
+    float dgx = expf(-2.f * sq(dx) / sq(r)) * 4.f * sq(dx) / r3, dgy = expf(-2.f * sq(dy) / sq(r)) * 4.f * sq(dy) / r3;
+    return d_ret * (dgx * gauss_1d(dy, r) + gauss_1d(dx, r) * dgy);
+  }
   if (type == DVG_BOX) {
     return d_ret * (-2) * 2 * r / ((2 * r) * (2 * r) * (2 * r));
   } else if (type == DVG_TENT) {

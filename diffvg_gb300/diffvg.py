@@ -26,3 +26,4 @@ class FilterType(IntEnum):
     tent = 1
     parabolic = 2
     hann = 3
+    gaussian = 4  # not in the reference: separable Gaussian, sigma = radius / 2, zero at the support's edge

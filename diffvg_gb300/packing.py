@@ -360,7 +360,7 @@ def pack_scene(args):
         key.append(('g', ids.tobytes(), kf, ks, int(gi[8])))
 
     ftype = _enum_value(args[i]); i += 1
-    if ftype not in (FilterType.box, FilterType.tent, FilterType.parabolic, FilterType.hann):
+    if ftype not in tuple(FilterType):
         raise SceneError('unknown filter type %r' % (ftype,))
     fr = _as_tensor(args[i])
     if fr.numel() != 1:

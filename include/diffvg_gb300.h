@@ -53,8 +53,11 @@ extern "C" {
 enum DvgShapeKind { DVG_CIRCLE = 0, DVG_ELLIPSE = 1, DVG_PATH = 2, DVG_RECT = 3 };
 /* Paint kinds: values of diffvg.ColorType (color.h:7-11); -1 = no paint. */
 enum DvgPaintKind { DVG_PAINT_NONE = -1, DVG_CONSTANT = 0, DVG_LINEAR = 1, DVG_RADIAL = 2 };
-/* Pixel filters: values of diffvg.FilterType (filter.h:6-11). */
-enum DvgFilterKind { DVG_BOX = 0, DVG_TENT = 1, DVG_PARABOLIC = 2, DVG_HANN = 3 };
+/* Pixel filters: values of diffvg.FilterType (filter.h:6-11).  DVG_GAUSSIAN
+ * has no counterpart in the reference: a separable Gaussian of standard
+ * deviation radius / 2, shifted to reach 0 at the edge of its support
+ * |dx|, |dy| <= radius. */
+enum DvgFilterKind { DVG_BOX = 0, DVG_TENT = 1, DVG_PARABOLIC = 2, DVG_HANN = 3, DVG_GAUSSIAN = 4 };
 
 enum DvgStatus {
   DVG_OK = 0,

@@ -253,8 +253,13 @@ static int solve_cubic_f(float a, float b, float c, float d, float t[3]) {
 /* ------------------------------------------------------------------------ */
 /* pixel filters (filter.h:22-106)                                           */
 /* ------------------------------------------------------------------------ */
+/* DVG_GAUSSIAN is not in the reference: the definition of this project's
+ * kernels (separable Gaussian, standard deviation r / 2, shifted to 0 at the
+ * edge of the support), checked by finite differences only. */
+static float gauss_1d(float x, float r) { return expf(-2.f * sq(x) / sq(r)) - expf(-2.f); }
 static float filter_weight(int type, float r, float dx, float dy) {
   if (fabsf(dx) > r || fabsf(dy) > r) return 0;
+  if (type == DVG_GAUSSIAN) return r > 0.f ? gauss_1d(dx, r) * gauss_1d(dy, r) : 0.f;
   if (type == DVG_BOX) return 1.f / sq(2 * r);
   if (type == DVG_TENT) return (r - fabsf(dx)) * (r - fabsf(dy)) / sq(sq(r));
   if (type == DVG_PARABOLIC)
@@ -265,6 +270,12 @@ static float filter_weight(int type, float r, float dx, float dy) {
   }
 }
 static float d_filter_weight(int type, float r, float dx, float dy, float d_ret) {
+  if (type == DVG_GAUSSIAN) {
+    if (!(r > 0.f) || fabsf(dx) > r || fabsf(dy) > r) return 0.f;
+    float r3 = r * r * r;
+    float dgx = expf(-2.f * sq(dx) / sq(r)) * 4.f * sq(dx) / r3, dgy = expf(-2.f * sq(dy) / sq(r)) * 4.f * sq(dy) / r3;
+    return d_ret * (dgx * gauss_1d(dy, r) + gauss_1d(dx, r) * dgy);
+  }
   if (type == DVG_BOX) {
     return d_ret * (-2) * 2 * r / ((2 * r) * (2 * r) * (2 * r));
   } else if (type == DVG_TENT) {

@@ -294,3 +294,42 @@ def run_paint_checks(make_backend):
     g = analytic(bwd, P, wts, seeds)
     out['transformed_radial_stroke_width'] = rel_err([central_fd(fwd, P, sw, 0.25, wts, seeds)], g[[sw]])
     return out
+
+
+# ---------------------------------------------------------------------------
+# Pixel filters.  The filter enters the gradients through gather_d_color
+# (diffvg.cpp:777-815), for the interior and the boundary term alike, so the
+# colour and geometry checks of run_checks are repeated under the tent, Hann
+# and Gaussian filters (the Gaussian is not in the reference: these and the
+# oracle parity test are its checks).  The filter radius's own gradient is
+# not compared: the reference differentiates the normalised filter with
+# (d.c ws - w d.c (ws - w)) / ws^2 (diffvg.cpp:1259-1262), which is not the
+# derivative of sum(w c) / sum(w), and this project keeps that estimator.
+
+def filter_case(ftype, radius):
+    """Builder of the circle scene of circle_case rendered with pixel filter
+    `ftype` of `radius` (attached as builder.filter), 48x48, 4x4 spp."""
+    def build(m):
+        return circle_case(m)
+    build.filter = (ftype, radius)
+    build.__name__ = 'filter_%s' % ftype
+    return build
+
+
+def run_filter_checks(make_backend):
+    """Per filter (tent, Hann, Gaussian): the circle's colour gradient (one
+    central difference, h = 1e-2) and its radius and centre through the
+    boundary term (quarter-pixel steps averaged over 8 seeds)."""
+    out = {}
+    wts = weight_image(48, 48)
+    seeds = list(range(1, 9))
+    for ftype, radius in (('tent', 1.0), ('hann', 1.5), ('gaussian', 1.25)):
+        packed, P, fwd, bwd = make_backend(filter_case(ftype, radius))
+        co = slot_of(packed, 'color')
+        g = analytic(bwd, P, wts, [1])
+        out[ftype + '_color'] = rel_err([central_fd(fwd, P, co + k, 1e-2, wts, [1]) for k in range(4)], g[co:co + 4])
+        ro, ce = slot_of(packed, 'radius'), slot_of(packed, 'center')
+        idx = [ro, ce, ce + 1]
+        g = analytic(bwd, P, wts, seeds)
+        out[ftype + '_geometry'] = rel_err([central_fd(fwd, P, i, 0.25, wts, seeds) for i in idx], g[idx])
+    return out

@@ -17,13 +17,15 @@ FWD_TOL = 1e-4
 GRAD_TOL = 1e-3
 
 
-def _run(builder, spp, seed, prefilter=False):
+def _run(builder, spp, seed, prefilter=False, filt=None):
+    import torch
     import diffvg_gb300 as dvg
     from diffvg_gb300.packing import pack_scene
     import oracle
     import native_util as nu
     w, h, shapes, groups = builder(dvg)
-    args = dvg.RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=prefilter)
+    pf = None if filt is None else dvg.PixelFilter(type=filt[0], radius=torch.tensor(filt[1]))
+    args = dvg.RenderFunction.serialize_scene(w, h, shapes, groups, filter=pf, use_prefiltering=prefilter)
     packed = pack_scene(args)
     P = oracle.params_of(packed)
     ref = oracle.render(packed, P, w, h, spp, spp, seed, num_threads=8)
@@ -82,3 +84,13 @@ def test_fill_scene_full_size_prefiltered():
     constant / linear / radial fills, 10% stroked, prefiltered, 1 spp)."""
     from diffvg_gb300 import workloads
     _run(lambda m: workloads.fill_scene(m, seed=3), 1, 3, prefilter=True)
+
+
+def test_gaussian_filter_scene():
+    """The Gaussian pixel filter (not in the reference; the oracle implements
+    the same definition) on a stroke scene and a prefiltered fill scene."""
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import workloads
+    g = (dvg.FilterType.gaussian, 1.25)
+    _run(lambda m: workloads.stroke_scene(m, seed=7, num_paths=128, canvas=128), 2, 4, filt=g)
+    _run(lambda m: workloads.fill_scene(m, seed=8, num_paths=24, canvas=128), 1, 5, prefilter=True, filt=g)

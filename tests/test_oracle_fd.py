@@ -14,7 +14,12 @@ def _oracle_backend(builder):
     from diffvg_gb300.packing import pack_scene
     import oracle
     w, h, shapes, groups, pf, spp = builder(dvg)
-    packed = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=pf))
+    filt = None
+    if getattr(builder, 'filter', None):
+        import torch
+        filt = dvg.PixelFilter(type=getattr(dvg.diffvg.FilterType, builder.filter[0]),
+                               radius=torch.tensor(builder.filter[1]))
+    packed = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups, filter=filt, use_prefiltering=pf))
     P = oracle.params_of(packed)
 
     def fwd(Pv, seed):
@@ -55,3 +60,12 @@ def test_oracle_every_paint_kind_on_fills_and_strokes_matches_finite_differences
     print(err)
     for name, e in err.items():
         assert e <= (STROKE_WIDTH_TOL if name.endswith('width') else PAINT_TOL), (name, e)
+
+
+def test_oracle_gradients_under_each_filter_match_finite_differences():
+    """Colour and circle geometry gradients under the tent, Hann and
+    Gaussian pixel filters (the Gaussian is not in the reference)."""
+    err = fd_util.run_filter_checks(_oracle_backend)
+    print(err)
+    for name, e in err.items():
+        assert e <= (COLOR_TOL if name.endswith('color') else GEOMETRY_TOL), (name, e)
