@@ -523,10 +523,16 @@ def run_batched(dev, steps=10, warmup=3, plain_steps=2):
     """The batched workload: 64 stroke scenes (seeds 100-163), canvas sizes
     drawn from {64,128,256,512}^2, path counts log-uniform in [16, 1024],
     2x2 spp, each optimised with Adam (lr 1e-2) towards a perturbed render
-    of itself (points N(0, 2 px), colours N(0, 0.05)).  Reports the batched
-    path (one CUDA graph per step) and the plain per-call path
-    (RenderFunction.apply + backward + torch Adam per scene) on the same
-    scenes."""
+    of itself (points N(0, 2 px), colours N(0, 0.05)).
+
+    The batch's step (forward, MSE gradient, backward and Adam for every
+    scene, one CUDA graph) is autotuned over its candidates: per-scene
+    launches on 8 streams, or persistent launches over a (scene, tile) work
+    queue with 1 or 2 resident blocks per SM and 1, 2 or 4 samples per
+    thread.  Reports the chosen candidate's steps/s, every candidate's time,
+    and the plain per-call path (RenderFunction.apply + backward + torch Adam
+    per scene) on the same scenes; equal error: every scene's loss at step
+    plain_steps + 1 from the same start, batched against plain."""
     import torch
     import diffvg_gb300 as dvg
     from diffvg_gb300 import workloads
@@ -538,6 +544,16 @@ def run_batched(dev, steps=10, warmup=3, plain_steps=2):
     targets = [b.render(i, workloads.perturbed_target_params(p, b.scene_params(i), seeds[i]))
                for i, p in enumerate(b.packed)]
     b.set_targets(targets)
+    candidates = [('streams', (2, 1))] + [('persistent', (c, t)) for c in (1, 2) for t in (1, 2, 4)]
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:  # a fresh cache: every candidate is timed in this run
+        timings = b.autotune(candidates=candidates, steps=3, cache_path=os.path.join(td, 'autotune.json'))
+    # equal error: the batch's per-scene losses at step plain_steps + 1
+    k_eq = plain_steps + 1
+    for _ in range(k_eq):
+        b.step()
+    torch.cuda.synchronize(dev)
+    batched_losses = b.loss()
     for _ in range(warmup):
         b.step()
     torch.cuda.synchronize(dev)
@@ -550,11 +566,18 @@ def run_batched(dev, steps=10, warmup=3, plain_steps=2):
     b.check()
     ms = e0.elapsed_time(e1) / steps
     n = b.samples_per_step()
+    streams_ms = timings.get('streams 2 1')
+    pers = {k: v for k, v in timings.items() if k.startswith('persistent')}
+    best_p = min(pers, key=pers.get) if pers else None
     out = {'workload': '64 stroke scenes, canvases {64,128,256,512}^2, 16-1024 paths (log-uniform), 2x2 spp, '
                        'Adam lr 1e-2 towards perturbed self-renders', 'samples_per_step': n,
            'steps_per_s': round(1e3 / ms, 3), 'ms_per_step': round(ms, 3), 'Msamples_per_s': round(n / ms / 1e3, 3),
-           'graph': 'one CUDA graph per step (forward, MSE gradient, backward per scene on 8 streams; one Adam)'}
-    # plain per-call path on the same scenes and targets
+           'mode': b.mode, 'tuning': {'ctas_per_sm': b.tuning.ctas_per_sm,
+                                      'samples_per_thread': b.tuning.samples_per_thread},
+           'graph': 'one CUDA graph per step (forward, MSE gradient, backward of every scene; one Adam)',
+           'autotune_ms_per_step': {k: round(v, 3) for k, v in timings.items()},
+           'persistent_vs_streams': (round(streams_ms / pers[best_p], 3) if best_p and streams_ms else None)}
+    # plain per-call path on the same scenes and targets, from the same start
     params, opts = [], []
     for (w, h, shapes, groups) in scenes:
         ps = []
@@ -569,6 +592,7 @@ def run_batched(dev, steps=10, warmup=3, plain_steps=2):
         opts.append(torch.optim.Adam(ps, lr=1e-2))
 
     def plain_step():
+        losses = []
         for i, (w, h, shapes, groups) in enumerate(scenes):
             opts[i].zero_grad()
             a = dvg.RenderFunction.serialize_scene(w, h, shapes, groups)
@@ -576,16 +600,23 @@ def run_batched(dev, steps=10, warmup=3, plain_steps=2):
             loss = ((img - targets[i]) ** 2).mean()
             loss.backward()
             opts[i].step()
-    plain_step()
+            losses.append(loss.detach())
+        return losses
+    plain_step()  # warm-up: packing and scene handles of every scene
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for _ in range(plain_steps):
-        plain_step()
+        plain_losses = plain_step()
     torch.cuda.synchronize(dev)
     pms = (time.perf_counter() - t0) / plain_steps * 1e3
+    plain_losses = [float(l) for l in plain_losses]
+    rel = [abs(a - p) / max(abs(p), 1e-12) for a, p in zip(batched_losses, plain_losses)]
     out['plain_steps_per_s'] = round(1e3 / pms, 3)
     out['plain_ms_per_step'] = round(pms, 2)
     out['speedup_vs_plain'] = round(pms / ms, 2)
+    out['equal_error_check'] = {'step': k_eq, 'scenes': len(rel), 'max_rel_loss_diff': float('%.3g' % max(rel)),
+                                'mean_loss_batched': round(sum(batched_losses) / len(rel), 6),
+                                'mean_loss_plain': round(sum(plain_losses) / len(rel), 6)}
     return out
 
 

@@ -27,6 +27,7 @@ DVG_FLAG_REUSE_PREP = 2
 
 EXPORTS = ('dvg_scene_create', 'dvg_scene_destroy', 'dvg_render_forward', 'dvg_render_backward',
            'dvg_scene_sync', 'dvg_scene_profile', 'dvg_scene_profile_read', 'dvg_mse_grad', 'dvg_adam_step',
+           'dvg_batch_create', 'dvg_batch_destroy', 'dvg_batch_forward', 'dvg_batch_backward',
            'dvg_last_error', 'dvg_version')
 
 
@@ -54,6 +55,10 @@ class RenderArgs(ctypes.Structure):
         ('params', ctypes.c_void_p), ('background', ctypes.c_void_p), ('eval_positions', ctypes.c_void_p),
         ('flags', ctypes.c_int32),
     ]
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [('ctas_per_sm', ctypes.c_int32), ('samples_per_thread', ctypes.c_int32)]
 
 
 class RenderError(RuntimeError):
@@ -118,6 +123,17 @@ def load(build_if_missing=True):
                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]
         lib.dvg_adam_step.restype = ctypes.c_int
+        lib.dvg_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        lib.dvg_batch_create.restype = ctypes.c_int
+        lib.dvg_batch_destroy.argtypes = [ctypes.c_void_p]
+        lib.dvg_batch_destroy.restype = ctypes.c_int
+        lib.dvg_batch_forward.argtypes = [ctypes.c_void_p, ctypes.POINTER(RenderArgs), ctypes.POINTER(ctypes.c_void_p),
+                                          ctypes.POINTER(BatchTuning), ctypes.c_void_p]
+        lib.dvg_batch_forward.restype = ctypes.c_int
+        lib.dvg_batch_backward.argtypes = [ctypes.c_void_p, ctypes.POINTER(RenderArgs), ctypes.POINTER(ctypes.c_void_p),
+                                           ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(BatchTuning),
+                                           ctypes.c_void_p]
+        lib.dvg_batch_backward.restype = ctypes.c_int
         lib.dvg_last_error.argtypes = []
         lib.dvg_last_error.restype = ctypes.c_char_p
         lib.dvg_version.argtypes = []
@@ -192,6 +208,45 @@ class NativeScene:
         n = ctypes.c_int()
         check(self._lib.dvg_scene_profile_read(self.handle, arr, 16, ctypes.byref(n)))
         return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(min(n.value, 16))}
+
+
+class NativeBatch:
+    """Owns a DvgBatch handle over NativeScene objects (kept alive here):
+    persistent batched launches of their sample passes."""
+
+    def __init__(self, scenes):
+        lib = load()
+        self._lib = lib
+        self.scenes = list(scenes)
+        arr = (ctypes.c_void_p * len(self.scenes))(*[sc.handle.value for sc in self.scenes])
+        h = ctypes.c_void_p()
+        check(lib.dvg_batch_create(arr, len(self.scenes), ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, 'handle', None):
+            self._lib.dvg_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _ptrs(ptrs):
+        return (ctypes.c_void_p * len(ptrs))(*ptrs)
+
+    def forward(self, args, image_ptrs, tuning=None, stream=0):
+        a = (RenderArgs * len(args))(*args)
+        check(self._lib.dvg_batch_forward(self.handle, a, self._ptrs(image_ptrs),
+                                          None if tuning is None else ctypes.byref(tuning), stream))
+
+    def backward(self, args, d_image_ptrs, d_params_ptrs, tuning=None, stream=0):
+        a = (RenderArgs * len(args))(*args)
+        check(self._lib.dvg_batch_backward(self.handle, a, self._ptrs(d_image_ptrs), self._ptrs(d_params_ptrs),
+                                           None if tuning is None else ctypes.byref(tuning), stream))
 
 
 def mse_grad(image, target, d_image, loss=None, scale=None, stream=0):

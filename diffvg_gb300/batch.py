@@ -19,7 +19,21 @@ A step is one graph replay; there is no host work per scene.  Failures the
 kernels latch while the graph runs (a tile list outgrowing its capacity as
 shapes move) are checked every `check_every` steps; a grown tile list makes
 the graph be captured again.
+
+Two ways to run the scenes' render passes inside the step:
+  * mode 'streams': per-scene launches spread over several streams;
+  * mode 'persistent': the forward sample pass, the interior adjoint and the
+    boundary pass of all scenes each run as one persistent launch over a
+    (scene, tile) work queue, largest scenes first (dvg_batch_forward /
+    dvg_batch_backward), tuned by resident blocks per SM and samples per
+    thread.
+autotune() times the candidates on the batch itself and keeps the fastest;
+its choice is cached in a JSON file by GPU and workload.
 """
+import hashlib
+import json
+import os
+
 import torch
 
 from . import _native
@@ -45,7 +59,7 @@ class BatchedScenes:
 
     def __init__(self, scene_args, num_samples=(2, 2), seeds=None, sizes=None, targets=None, lr=1e-2,
                  betas=(0.9, 0.999), eps=1e-8, trainable=DEFAULT_TRAINABLE, streams=8, check_every=16,
-                 device=None):
+                 device=None, mode='streams', tuning=(2, 1)):
         self.device = device or torch.device('cuda', torch.cuda.current_device())
         self.nsx, self.nsy = num_samples
         self.packed = [pack_scene(a) for a in scene_args]
@@ -81,8 +95,21 @@ class BatchedScenes:
         self.streams = [torch.cuda.Stream(device=dev) for _ in range(max(1, min(streams, n)))]
         self.graph = None
         self.steps_taken = 0
+        self.native_batch = None
+        self.set_mode(mode, tuning)
         if targets is not None:
             self.set_targets(targets)
+
+    def set_mode(self, mode, tuning=(2, 1)):
+        """'streams' or 'persistent' (with tuning = (blocks per SM, samples
+        per thread)); the next step captures its graph again."""
+        if mode not in ('streams', 'persistent'):
+            raise ValueError('mode must be streams or persistent')
+        if mode == 'persistent' and self.native_batch is None:
+            self.native_batch = _native.NativeBatch(self.scenes)
+        self.mode = mode
+        self.tuning = _native.BatchTuning(int(tuning[0]), int(tuning[1]))
+        self.graph = None
 
     @property
     def num_scenes(self):
@@ -124,6 +151,8 @@ class BatchedScenes:
                     d_image_ptr=self.d_images[i].data_ptr(), d_params_ptr=self.grads[o:o + n].data_ptr(), stream=sp)
 
     def _step_body(self):
+        if self.mode == 'persistent':
+            return self._step_body_persistent()
         main = torch.cuda.current_stream(self.device)
         self.losses.zero_()
         for st in self.streams:
@@ -136,6 +165,81 @@ class BatchedScenes:
             main.wait_stream(st)
         _native.adam_step(self.params, self.grads, self.m, self.v, self.step_count, self.lr, self.betas, self.eps,
                           lr_scale=self.lr_scale, stream=main.cuda_stream)
+
+    def _step_body_persistent(self):
+        main = torch.cuda.current_stream(self.device)
+        sp = main.cuda_stream
+        n = self.num_scenes
+        self.losses.zero_()
+        self.native_batch.forward([self._args(i, _native.DVG_FLAG_NO_SYNC) for i in range(n)],
+                                  [im.data_ptr() for im in self.images], self.tuning, stream=sp)
+        for i in range(n):
+            _native.mse_grad(self.images[i], self.targets[i], self.d_images[i], self.losses[i:i + 1], stream=sp)
+        self.grads.zero_()
+        flags = _native.DVG_FLAG_NO_SYNC | _native.DVG_FLAG_REUSE_PREP
+        self.native_batch.backward([self._args(i, flags) for i in range(n)], [d.data_ptr() for d in self.d_images],
+                                   [self.grads[o:o + 1].data_ptr() for o in self.offsets], self.tuning, stream=sp)
+        _native.adam_step(self.params, self.grads, self.m, self.v, self.step_count, self.lr, self.betas, self.eps,
+                          lr_scale=self.lr_scale, stream=sp)
+
+    def workload_key(self):
+        """GPU name and a hash of the batch's scene and image sizes: the key of
+        the autotuner's cache."""
+        h = hashlib.blake2b(digest_size=8)
+        h.update(repr(sorted((w, h_, self.nsx, self.nsy, p.num_shapes, int(p.segment_ctrl.size))
+                             for (w, h_), p in zip(self.sizes, self.packed))).encode())
+        return '%s|%s' % (torch.cuda.get_device_name(self.device), h.hexdigest())
+
+    def autotune(self, candidates=None, steps=3, cache_path=None):
+        """Times each candidate (mode, tuning) for `steps` graph replays on this
+        batch, keeps the fastest, and returns {candidate: ms per step}.  The
+        optimiser state is restored afterwards.  Choices are cached in
+        cache_path (default: $DVG_AUTOTUNE_CACHE, else autotune.json beside the
+        library) by workload_key(); a cached choice is used without timing."""
+        if cache_path is None:
+            cache_path = os.environ.get('DVG_AUTOTUNE_CACHE') or os.path.join(
+                os.path.dirname(_native.library_path()), 'autotune.json')
+        if candidates is None:
+            candidates = [('streams', (2, 1))] + [('persistent', (c, t)) for c in (1, 2) for t in (1, 2, 4)]
+        key = self.workload_key()
+        cache = {}
+        if os.path.exists(cache_path):
+            try:
+                with open(cache_path) as f:
+                    cache = json.load(f)
+            except (OSError, ValueError):
+                cache = {}
+        if key in cache:
+            mode, tuning = cache[key]['mode'], tuple(cache[key]['tuning'])
+            self.set_mode(mode, tuning)
+            return dict(cache[key].get('timings_ms', {}))
+        saved = (self.params.clone(), self.m.clone(), self.v.clone(), self.step_count.clone(), self.steps_taken)
+        timings = {}
+        for mode, tuning in candidates:
+            self.set_mode(mode, tuning)
+            self.step()  # capture and warm up
+            torch.cuda.synchronize(self.device)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(steps):
+                self.graph.replay()
+            e1.record()
+            torch.cuda.synchronize(self.device)
+            timings['%s %d %d' % (mode, tuning[0], tuning[1])] = e0.elapsed_time(e1) / steps
+        self.params.copy_(saved[0]); self.m.copy_(saved[1]); self.v.copy_(saved[2])
+        self.step_count.copy_(saved[3])
+        self.steps_taken = saved[4]
+        best = min(timings, key=timings.get)
+        mode, c, t = best.split()
+        self.set_mode(mode, (int(c), int(t)))
+        cache[key] = {'mode': mode, 'tuning': [int(c), int(t)], 'timings_ms': timings}
+        try:
+            os.makedirs(os.path.dirname(os.path.abspath(cache_path)), exist_ok=True)
+            with open(cache_path, 'w') as f:
+                json.dump(cache, f, indent=1, sort_keys=True)
+        except OSError:
+            pass
+        return timings
 
     def check(self):
         """Waits for the device and raises a latched failure; returns True if

@@ -839,3 +839,266 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched launches: the forward samples, the interior adjoint and the
+// boundary pass of many scenes, each as one persistent launch over a work
+// queue of (scene, tile) items (dvg_batch_forward / dvg_batch_backward).
+// The per-scene steps around them (scene preparation, weights, resolve,
+// drawing and ordering the boundary samples) are launched per scene.
+
+struct DvgBatch {
+  int device = 0;
+  std::vector<DvgScene *> scenes;
+  DevBuf dev;                   // BatchScene[2n], int orders and item starts, counters
+  BatchScene *h_bs = nullptr;   // pinned staging of the BatchScene arrays (forward, backward)
+  int *h_ints = nullptr;        // pinned staging of the orders and item starts
+  BatchScene *d_fwd = nullptr, *d_bwd = nullptr;
+  int *d_ints = nullptr, *d_counters = nullptr;
+  size_t nints = 0;
+};
+
+namespace {
+
+size_t batch_ints(int n) { return (size_t)5 * n + 4; }  // order, item starts (n + 1), edge order, pad
+
+int batch_check(DvgBatch *b, const DvgRenderArgs *args) {
+  if (!b) return fail(DVG_ERR_INVALID, "batch is NULL");
+  if (!args) return fail(DVG_ERR_INVALID, "render arguments are NULL");
+  for (size_t i = 0; i < b->scenes.size(); i++) {
+    int st = check_args(b->scenes[i], &args[i]);
+    if (st != DVG_OK) return st;
+    if (args[i].use_prefiltering || args[i].background || args[i].num_eval_positions > 0)
+      return fail(DVG_ERR_INVALID, "batched launches render sampled colour images without a background (scene %zu)",
+                  i);
+  }
+  return DVG_OK;
+}
+
+// Scenes in descending order of work, and the first work item of each in
+// that order (items of `spt` 32-sample chunks; 8 chunks per tile and sample
+// plane).
+void batch_items(const DvgRenderArgs *args, int n, int spt, int *order, int *item_start) {
+  std::vector<std::pair<long long, int>> work;
+  for (int i = 0; i < n; i++)
+    work.push_back({(long long)args[i].width * args[i].height * args[i].num_samples_x * args[i].num_samples_y, i});
+  std::stable_sort(work.begin(), work.end(), [](const std::pair<long long, int> &a, const std::pair<long long, int> &b) {
+    return a.first > b.first;
+  });
+  int run = 0;
+  for (int r = 0; r < n; r++) {
+    const DvgRenderArgs &a = args[work[r].second];
+    long long chunks = (long long)((a.width + DVG_TILE - 1) / DVG_TILE) * ((a.height + DVG_TILE - 1) / DVG_TILE) *
+                       a.num_samples_x * a.num_samples_y * 8;
+    order[r] = work[r].second;
+    item_start[r] = run;
+    run += (int)((chunks + spt - 1) / spt);
+  }
+  item_start[n] = run;
+}
+
+int batch_tuning(const DvgBatchTuning *t, int *ctas, int *spt) {
+  *ctas = t && t->ctas_per_sm > 0 ? t->ctas_per_sm : 2;
+  *spt = t && t->samples_per_thread > 0 ? t->samples_per_thread : 1;
+  if (*ctas > 2 || *spt > 64) return fail(DVG_ERR_INVALID, "tuning: ctas_per_sm must be 1 or 2, samples_per_thread <= 64");
+  return DVG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dvg_batch_create(DvgScene *const *scenes, int num_scenes, DvgBatch **out) {
+  dvg::clear_error();
+  if (!out) return fail(DVG_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!scenes || num_scenes < 1 || num_scenes > DVG_BATCH_MAX)
+    return fail(DVG_ERR_INVALID, "a batch holds 1 to %d scenes", DVG_BATCH_MAX);
+  for (int i = 0; i < num_scenes; i++) {
+    if (!scenes[i]) return fail(DVG_ERR_INVALID, "scene %d is NULL", i);
+    if (scenes[i]->device != scenes[0]->device) return fail(DVG_ERR_INVALID, "the scenes of a batch share one device");
+  }
+  DvgBatch *b = new DvgBatch();
+  b->device = scenes[0]->device;
+  b->scenes.assign(scenes, scenes + num_scenes);
+  DeviceGuard guard(b->device);
+  int n = num_scenes;
+  b->nints = batch_ints(n);
+  cudaError_t e = cudaMallocHost(&b->h_bs, 2 * n * sizeof(BatchScene));
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_ints, 2 * b->nints * sizeof(int));
+  if (e == cudaSuccess) e = b->dev.ensure(carve_size({2 * n * sizeof(BatchScene), 2 * b->nints * sizeof(int), 16}));
+  if (e != cudaSuccess) {
+    dvg_batch_destroy(b);
+    return cuda_fail(e, "allocating a batch");
+  }
+  char *p = reinterpret_cast<char *>(b->dev.ptr);
+  b->d_fwd = carve<BatchScene>(p, n);
+  b->d_bwd = carve<BatchScene>(p, n);
+  b->d_ints = carve<int>(p, 2 * b->nints);
+  b->d_counters = carve<int>(p, 4);
+  *out = b;
+  return DVG_OK;
+}
+
+int dvg_batch_destroy(DvgBatch *b) {
+  dvg::clear_error();
+  if (!b) return DVG_OK;
+  DeviceGuard guard(b->device);
+  if (b->h_bs) cudaFreeHost(b->h_bs);
+  if (b->h_ints) cudaFreeHost(b->h_ints);
+  b->dev.release();
+  delete b;
+  return DVG_OK;
+}
+
+int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *images, const DvgBatchTuning *tuning,
+                      void *stream) {
+  dvg::clear_error();
+  int st = batch_check(b, args);
+  if (st != DVG_OK) return st;
+  if (!images) return fail(DVG_ERR_INVALID, "images is NULL");
+  int ctas, spt;
+  if ((st = batch_tuning(tuning, &ctas, &spt)) != DVG_OK) return st;
+  DeviceGuard guard(b->device);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int n = (int)b->scenes.size();
+  cudaError_t e = cudaSuccess;
+  BatchScene *hb = b->h_bs;
+  std::vector<int> live;
+  std::vector<DvgRenderArgs> live_args;
+  for (int i = 0; i < n; i++) {
+    DvgScene *sc = b->scenes[i];
+    const DvgRenderArgs *a = &args[i];
+    if (!images[i] || (reinterpret_cast<uintptr_t>(images[i]) & 15u))
+      return fail(DVG_ERR_INVALID, "image %d must be set and 16-byte aligned", i);
+    size_t npx = (size_t)a->width * a->height, ns = npx * a->num_samples_x * a->num_samples_y;
+    sc->hit_live = false;
+    if (sc->d.num_groups == 0) {  // empty scene: transparent black
+      e = cudaMemsetAsync(images[i], 0, npx * 4 * sizeof(float), s);
+      if (e != cudaSuccess) return cuda_fail(e, "batched forward");
+      continue;
+    }
+    e = sc->weight.ensure(npx * sizeof(float));
+    if (e == cudaSuccess) e = sc->samples.ensure(ns * sizeof(float4));
+    if (e == cudaSuccess) e = sc->hits.ensure(hit_bytes(sc, ns, false));
+    if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
+    BatchScene &bs = hb[live.size()];
+    bs.S = make_dev(sc, a->params);
+    DvgRenderArgs ai = *a;
+    ai.flags |= DVG_FLAG_NO_SYNC;  // failures stay latched in the scene (dvg_scene_sync)
+    if ((st = prepare(sc, bs.S, &ai, s)) != DVG_OK) return st;
+    bs.R = make_render(sc, a);
+    HitArena h = hit_arena(sc, ns, false);
+    bs.R.hit_keys = h.keys;
+    bs.R.hit_cnt = h.cnt;
+    bs.E = EdgeRecords{};
+    bs.samples = reinterpret_cast<float4 *>(sc->samples.ptr);
+    dvg::launch_weight(bs.S, bs.R, s);
+    live.push_back(i);
+    live_args.push_back(*a);
+  }
+  int nl = (int)live.size();
+  if (nl == 0) return DVG_OK;
+  int *order = b->h_ints, *item_start = b->h_ints + nl;
+  batch_items(live_args.data(), nl, spt, order, item_start);
+  e = cudaMemcpyAsync(b->d_fwd, hb, nl * sizeof(BatchScene), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_ints, b->h_ints, (2 * nl + 1) * sizeof(int), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "staging a batch");
+  dvg::launch_batch_sample_fwd(b->d_fwd, nl, b->d_ints, b->d_ints + nl, spt, ctas, b->d_counters, s);
+  for (int k = 0; k < nl; k++) {
+    int i = live[k];
+    DvgScene *sc = b->scenes[i];
+    const DvgRenderArgs *a = &args[i];
+    size_t ns = (size_t)a->width * a->height * a->num_samples_x * a->num_samples_y;
+    dvg::launch_resolve(hb[k].R, hb[k].samples, images[i], s);
+    HitArena h = hit_arena(sc, ns, false);
+    if (sc->d.num_params > 0)
+      e = cudaMemcpyAsync(h.params, a->params, (size_t)sc->d.num_params * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "batched forward");
+    sc->hit_live = true;
+    sc->hit_pf = false;
+    sc->hit_w = a->width;
+    sc->hit_h = a->height;
+    sc->hit_nsx = a->num_samples_x;
+    sc->hit_nsy = a->num_samples_y;
+    sc->hit_seed = a->seed;
+  }
+  e = cudaGetLastError();
+  return e == cudaSuccess ? DVG_OK : cuda_fail(e, "batched forward launch");
+}
+
+int dvg_batch_backward(DvgBatch *b, const DvgRenderArgs *args, const float *const *d_images, float *const *d_params,
+                       const DvgBatchTuning *tuning, void *stream) {
+  dvg::clear_error();
+  int st = batch_check(b, args);
+  if (st != DVG_OK) return st;
+  if (!d_images || !d_params) return fail(DVG_ERR_INVALID, "d_images / d_params is NULL");
+  int ctas, spt;
+  if ((st = batch_tuning(tuning, &ctas, &spt)) != DVG_OK) return st;
+  DeviceGuard guard(b->device);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int n = (int)b->scenes.size();
+  cudaError_t e = cudaSuccess;
+  BatchScene *hb = b->h_bs + n;
+  std::vector<int> live;
+  std::vector<DvgRenderArgs> live_args;
+  for (int i = 0; i < n; i++) {
+    DvgScene *sc = b->scenes[i];
+    const DvgRenderArgs *a = &args[i];
+    if (!d_images[i] || !d_params[i] || (reinterpret_cast<uintptr_t>(d_images[i]) & 15u))
+      return fail(DVG_ERR_INVALID, "d_image %d / d_params %d must be set, d_image 16-byte aligned", i, i);
+    if (sc->d.num_groups == 0) continue;  // empty scene: nothing to differentiate
+    size_t npx = (size_t)a->width * a->height, ns = npx * a->num_samples_x * a->num_samples_y;
+    e = sc->weight.ensure(npx * sizeof(float));
+    if (e == cudaSuccess) e = sc->edge.ensure(edge_bytes(sc, ns));
+    if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
+    BatchScene &bs = hb[live.size()];
+    bs.S = make_dev(sc, a->params);
+    DvgRenderArgs ai = *a;
+    ai.flags |= DVG_FLAG_NO_SYNC;
+    if ((st = prepare(sc, bs.S, &ai, s)) != DVG_OK) return st;
+    bs.R = make_render(sc, a);
+    bs.R.d_params = d_params[i];
+    bs.R.d_image = d_images[i];
+    if (hit_matches(sc, a)) {
+      HitArena h = hit_arena(sc, ns, false);
+      e = cudaMemsetAsync(h.stale, 0, sizeof(unsigned), s);
+      if (e != cudaSuccess) return cuda_fail(e, "batched backward");
+      if (sc->d.num_params > 0) dvg::launch_hit_check(a->params, h.params, sc->d.num_params, h.stale, s);
+      bs.R.hit_keys = h.keys;
+      bs.R.hit_cnt = h.cnt;
+      bs.R.hit_stale = h.stale;
+    }
+    bs.E = edge_records(sc, ns);
+    bs.samples = nullptr;
+    dvg::launch_weight(bs.S, bs.R, s);
+    live.push_back(i);
+    live_args.push_back(*a);
+  }
+  int nl = (int)live.size();
+  if (nl == 0) return DVG_OK;
+  // staged ints: scene order, item starts (nl + 1), the paired-lane scenes' order
+  int *ints = b->h_ints + b->nints, *d_ints = b->d_ints + b->nints;
+  int *order = ints, *item_start = ints + nl, *edge_order = ints + 2 * nl + 1;
+  batch_items(live_args.data(), nl, spt, order, item_start);
+  // the boundary samples: drawn and ordered per scene, evaluated together
+  // (scenes of fewer than 8 groups evaluate theirs per scene)
+  int n_edge = 0;
+  for (int r = 0; r < nl; r++) {
+    int k = order[r];
+    dvg::launch_edge_setup(hb[k].S, hb[k].R, hb[k].E, s);
+    if (b->scenes[live[k]]->d.num_groups >= 8 && hb[k].E.job_a) edge_order[n_edge++] = k;
+  }
+  e = cudaMemcpyAsync(b->d_bwd, hb, nl * sizeof(BatchScene), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_ints, ints, (2 * nl + 1 + n_edge) * sizeof(int), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "staging a batch");
+  dvg::launch_batch_sample_bwd(b->d_bwd, nl, d_ints, d_ints + nl, spt, ctas, b->d_counters + 1, s);
+  if (n_edge > 0) dvg::launch_batch_edge(b->d_bwd, n_edge, d_ints + 2 * nl + 1, spt, ctas, b->d_counters + 2, s);
+  for (int k = 0; k < nl; k++)
+    if (!(b->scenes[live[k]]->d.num_groups >= 8 && hb[k].E.job_a)) dvg::launch_edge_eval(hb[k].S, hb[k].R, hb[k].E, s);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? DVG_OK : cuda_fail(e, "batched backward launch");
+}
+
+}  // extern "C"

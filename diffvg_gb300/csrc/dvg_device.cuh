@@ -146,6 +146,17 @@ struct EdgeRecords {
 #define DVG_EDGE_CELL_SHIFT 2
 #define DVG_EDGE_CELLS ((DVG_TILE >> DVG_EDGE_CELL_SHIFT) * (DVG_TILE >> DVG_EDGE_CELL_SHIFT))
 
+// One scene of a batched launch (dvg_batch_forward / dvg_batch_backward):
+// the persistent batched kernels take an array of these in device memory
+// and a work queue over the scenes' tiles or boundary samples.
+struct BatchScene {
+  DevScene S;
+  DevRender R;
+  EdgeRecords E;
+  float4 *samples;  // forward sample colours
+};
+#define DVG_BATCH_MAX 256  // scenes per batched launch
+
 typedef float2 v2;
 
 #define DI __device__ __forceinline__
@@ -606,6 +617,9 @@ DN int winding_banded(const DevScene &S, int s, int po, int np, int so, v2 pt) {
   return w;
 }
 
+// Winding number of shape s at pt; with BANDED (the scene has band lists),
+// paths that have band lists scan only pt's band.
+template <bool BANDED>
 DI int winding_shape(const DevScene &S, int s, v2 pt) {
   int kind = SI(S, s, DVG_SHAPE_KIND);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
@@ -620,7 +634,7 @@ DI int winding_shape(const DevScene &S, int s, v2 pt) {
     return (pt.x > pget(S, po) && pt.x < pget(S, po + 2) && pt.y > pget(S, po + 1) && pt.y < pget(S, po + 3)) ? 1 : 0;
   }
   int nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS), so = SI(S, s, DVG_SHAPE_SEG_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
-  if (S.band_n && __ldg(&S.band_n[s]) > 0) return winding_banded(S, s, po, np, so, pt);
+  if (BANDED && __ldg(&S.band_n[s]) > 0) return winding_banded(S, s, po, np, so, pt);
   int w = 0;
   #pragma unroll 1
   for (int i = 0; i < nseg; i++) {
@@ -632,8 +646,10 @@ DI int winding_shape(const DevScene &S, int s, v2 pt) {
 
 struct EdgeQ { int group, shape, hit; };
 
-// is_inside (diffvg.cpp:33-87)
-DN bool group_inside(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
+// is_inside (diffvg.cpp:33-87).  Scenes with band lists take the
+// BANDED instance (one test at entry, so the common instance is unchanged).
+template <bool BANDED>
+DI bool group_inside_body(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
   v2 lp = xform_pt(S.c2s + 9 * g, pt);
   if (!box_in(S.g_local_box[g], lp)) return false;
   int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
@@ -643,13 +659,18 @@ DN bool group_inside(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
   for (int k = 0; k < nsh; k++) {
     int s = __ldg(&S.group_shapes[off + k]);
     if (nsh > 1 && !box_in(S.s_box[s], lp)) continue;
-    int ws = winding_shape(S, s, lp);
+    int ws = winding_shape<BANDED>(S, s, lp);
     w += ws;
     if (eq && eq->group == g && eq->shape == s) {
       if ((eo && abs(ws) % 2 == 1) || (!eo && ws != 0)) eq->hit = 1;
     }
   }
   return eo ? (abs(w) % 2 == 1) : (w != 0);
+}
+DN bool group_inside_banded(const DevScene &S, int g, v2 pt, EdgeQ *eq) { return group_inside_body<true>(S, g, pt, eq); }
+DN bool group_inside(const DevScene &S, int g, v2 pt, EdgeQ *eq) {
+  if (S.band_n) return group_inside_banded(S, g, pt, eq);
+  return group_inside_body<false>(S, g, pt, eq);
 }
 
 // ---------------------------------------------------------------------------
@@ -1520,13 +1541,9 @@ DN bool closest_path_t(const DevScene &S, int s, v2 pt, float max_radius, PathIn
   return found;
 }
 
-DI bool closest_path(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
-  if (max_radius < INFINITY && S.band_n && __ldg(&S.band_n[s]) > 0)
-    return closest_path_t<true>(S, s, pt, max_radius, info, result);
-  return closest_path_t<false>(S, s, pt, max_radius, info, result);
-}
-
-DN bool closest_shape(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
+// closest_point(shape) (compute_distance.h:313-371)
+template <bool BANDED>
+DI bool closest_shape_body(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
   int kind = SI(S, s, DVG_SHAPE_KIND);
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
   if (kind == DVG_CIRCLE) {
@@ -1559,7 +1576,18 @@ DN bool closest_shape(const DevScene &S, int s, v2 pt, float max_radius, PathInf
     *result = cp;
     return true;
   }
-  return closest_path(S, s, pt, max_radius, info, result);
+  if (BANDED && max_radius < INFINITY && __ldg(&S.band_n[s]) > 0)
+    return closest_path_t<true>(S, s, pt, max_radius, info, result);
+  return closest_path_t<false>(S, s, pt, max_radius, info, result);
+}
+// scenes with band lists take the BANDED instance (one test at entry, so the
+// common instance is unchanged)
+DN bool closest_shape_banded(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
+  return closest_shape_body<true>(S, s, pt, max_radius, info, result);
+}
+DN bool closest_shape(const DevScene &S, int s, v2 pt, float max_radius, PathInfo *info, v2 *result) {
+  if (S.band_n) return closest_shape_banded(S, s, pt, max_radius, info, result);
+  return closest_shape_body<false>(S, s, pt, max_radius, info, result);
 }
 
 // compute_distance (compute_distance.h:373-439)

@@ -37,6 +37,20 @@ void launch_sample_bwd(const DevScene &S, const DevRender &R, float4 *dbg_val, i
 void launch_bg_combine(const DevScene &S, const DevRender &R, const float4 *dbg_val, const int *dbg_flag,
                        cudaStream_t st);
 void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st);
+// launch_edge in two halves: drawing and ordering the boundary samples, then
+// evaluating them (the batched path evaluates every scene's in one launch)
+void launch_edge_setup(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st);
+void launch_edge_eval(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st);
+// Persistent batched passes over nb scenes B[order[r]] (device arrays);
+// item_start[r] is the first work item of the r-th scene (nb + 1 entries),
+// spt the 32-sample chunks per item, counter a device int (zeroed here).
+// The boundary pass takes the scenes with paired lanes (8+ groups) only.
+void launch_batch_sample_fwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
+                             int ctas_per_sm, int *counter, cudaStream_t st);
+void launch_batch_sample_bwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
+                             int ctas_per_sm, int *counter, cudaStream_t st);
+void launch_batch_edge(const BatchScene *B, int nb, const int *order, int spt, int ctas_per_sm, int *counter,
+                       cudaStream_t st);
 // Signed distance output (forward: sdf, backward: d_sdf).
 void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
                 const float *d_sdf, cudaStream_t st);

@@ -68,22 +68,23 @@ __global__ void __launch_bounds__(256) k_weight(DevRender R0, const __grid_const
 // lanes of a warp hold neighbouring samples and meet the same segments.
 __device__ __forceinline__ int morton_x(int k) { return (k & 1) | ((k >> 1) & 2) | ((k >> 2) & 4) | ((k >> 3) & 8); }
 __device__ __forceinline__ int morton_y(int k) { return ((k >> 1) & 1) | ((k >> 2) & 2) | ((k >> 3) & 4) | ((k >> 4) & 8); }
-__device__ __forceinline__ void tile_sample(int spp, int &dx, int &dy, int &sub) {
-  int j = blockIdx.y * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void tile_sample(int spp, int cta_y, int tid, int &dx, int &dy, int &sub) {
+  int j = cta_y * 256 + tid;
   int k = j / spp;
   sub = j - k * spp;
   dx = morton_x(k);
   dy = morton_y(k);
 }
 
+// One sample of the forward sample pass: thread tid of the 256-thread group
+// cta_y of image tile `tile` (a warp's lanes call it together).
 template <bool PREFILTER>
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
-    k_sample_fwd(const __grid_constant__ DevScene S, DevRender R, float4 *samples) {
-  __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
+__device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRender &R, int tile, int cta_y, int tid,
+                                               float4 *samples, WarpQueue *q, int lane) {
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
-  int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  int tx = tile % tiles_x, ty = tile / tiles_x;
   int dx, dy, sub;
-  tile_sample(R.spp, dx, dy, sub);
+  tile_sample(R.spp, cta_y, tid, dx, dy, sub);
   int px = tx * DVG_TILE + dx, py = ty * DVG_TILE + dy;
   bool active = px < R.w && py < R.h;
   if (PREFILTER && !active) return;
@@ -104,10 +105,18 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
     int n = R.w * R.h * R.spp;
     bool cache = R.hit_keys && !bins_overflowed(S);
     if (active && R.hit_cnt && !cache) R.hit_cnt[idx] = DVG_HIT_NONE;
-    c = sample_color_fwd(S, bg, npt, nullptr, active, &wq[threadIdx.x >> 5], threadIdx.x & 31,
-                         cache ? R.hit_keys : nullptr, cache ? R.hit_cnt : nullptr, n, idx);
+    c = sample_color_fwd(S, bg, npt, nullptr, active, q, lane, cache ? R.hit_keys : nullptr,
+                         cache ? R.hit_cnt : nullptr, n, idx);
   }
   if (active) samples[idx] = c;
+}
+
+template <bool PREFILTER>
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+    k_sample_fwd(const __grid_constant__ DevScene S, const __grid_constant__ DevRender R, float4 *samples) {
+  __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
+  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, samples, &wq[PREFILTER ? 0 : threadIdx.x >> 5],
+                            threadIdx.x & 31);
 }
 
 // filtered pixel colour from the sample colours around it
@@ -144,16 +153,17 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-// interior adjoint (render_kernel with d_render_image, diffvg.cpp:1160-1268)
+// One sample of the interior adjoint (render_kernel with d_render_image,
+// diffvg.cpp:1160-1268): thread tid of the 256-thread group cta_y of image
+// tile `tile`; R carries the filter loaded by load_filter.  A warp's lanes
+// call it together (the filter-radius adjoint is summed per warp).
 template <bool PREFILTER>
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
-    k_sample_bwd(const __grid_constant__ DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
-  __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
-  DevRender R = load_filter(R0, nullptr);
+__device__ __forceinline__ void sample_bwd_one(const DevScene &S, const DevRender &R, int tile, int cta_y, int tid,
+                                               float4 *dbg_val, int *dbg_flag, WarpQueue *q, int lane) {
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
-  int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  int tx = tile % tiles_x, ty = tile / tiles_x;
   int dx, dy, sub;
-  tile_sample(R.spp, dx, dy, sub);
+  tile_sample(R.spp, cta_y, tid, dx, dy, sub);
   int px = tx * DVG_TILE + dx, py = ty * DVG_TILE + dy;
   bool active = px < R.w && py < R.h && !bins_overflowed(S);
   float dfr = 0.f;
@@ -184,8 +194,8 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
       int c = R.hit_cnt[idx];
       if (c != DVG_HIT_NONE) cached = c;
     }
-    color = sample_color_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params, active, &wq[threadIdx.x >> 5],
-                             threadIdx.x & 31, R.hit_keys, R.w * R.h * R.spp, idx, cached);
+    color = sample_color_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params, active, q, lane, R.hit_keys,
+                             R.w * R.h * R.spp, idx, cached);
   }
   if (active) {
     if (R.d_background) { dbg_val[idx] = dbg; dbg_flag[idx] = assign; }
@@ -205,7 +215,16 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
       }
   }
   float tot = warp_sum(dfr);
-  if ((threadIdx.x & 31) == 0 && tot != 0.f) atomicAdd(R.d_params + R.filter_radius_off, tot);
+  if (lane == 0 && tot != 0.f) atomicAdd(R.d_params + R.filter_radius_off, tot);
+}
+
+template <bool PREFILTER>
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+    k_sample_bwd(const __grid_constant__ DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
+  __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
+  DevRender R = load_filter(R0, nullptr);
+  sample_bwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, dbg_val, dbg_flag,
+                            &wq[PREFILTER ? 0 : threadIdx.x >> 5], threadIdx.x & 31);
 }
 
 // Background adjoint in sample order per pixel: a sample without fragments
@@ -351,13 +370,12 @@ DI void edge_accumulate(const DevScene &S, const DevRender &R, int g, int s, v2 
 // Without PAIRS one lane runs both queries: for scenes of few shapes the
 // walks are short and the gradient atomics, aggregated per warp, are what
 // costs.
+// One lane (gi: index of the lane over the pass) of the boundary pass; R
+// carries the filter loaded by load_filter; a warp's lanes call it together.
 template <bool PAIRS>
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
-    k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, const __grid_constant__ EdgeRecords E) {
-  __shared__ WarpQueue wq[8];
+__device__ __forceinline__ void edge_eval_one(const DevScene &S, const DevRender &R, const EdgeRecords &E, long long gi,
+                                              WarpQueue *q, int lane) {
   const unsigned full = 0xffffffffu;
-  DevRender R = load_filter(R0, nullptr);
-  long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int i = (int)(PAIRS ? gi >> 1 : gi);
   bool outside = PAIRS && (gi & 1);
   int T = S.tiles_x * S.tiles_y * DVG_EDGE_CELLS;
@@ -373,8 +391,6 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   int bx = min(max((int)(bpt.x * R.w), 0), R.w - 1), by = min(max((int)(bpt.y * R.h), 0), R.h - 1);
   EdgeQ qq = {g, s, 0};
   const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (by * R.w + bx) : nullptr;
-  WarpQueue *q = &wq[threadIdx.x >> 5];
-  int lane = threadIdx.x & 31;
   v2 qpt = outside ? add2(bpt, scl2(1e-4f, normal)) : sub2(bpt, scl2(1e-4f, normal));
   float4 cin, cout;
   int hin, hout;
@@ -410,6 +426,15 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   edge_accumulate(S, R, g, s, bpt, normal, lpt, pdf, t, bd, cin, hin, cout, hout);
 }
 
+template <bool PAIRS>
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+    k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, const __grid_constant__ EdgeRecords E) {
+  __shared__ WarpQueue wq[8];
+  DevRender R = load_filter(R0, nullptr);
+  edge_eval_one<PAIRS>(S, R, E, (long long)blockIdx.x * blockDim.x + threadIdx.x, &wq[threadIdx.x >> 5],
+                       threadIdx.x & 31);
+}
+
 // The deferred fp64 root walks of the paired boundary pass, one per thread
 // (full warps): each sets its result bit in its query's dq_res.
 __global__ void __launch_bounds__(256) k_edge_jobs(const __grid_constant__ DevScene S, const __grid_constant__ EdgeRecords E) {
@@ -426,42 +451,55 @@ __global__ void __launch_bounds__(256) k_edge_jobs(const __grid_constant__ DevSc
   }
 }
 
-// The boundary samples whose colour queries were deferred: blend each
-// deferred query's fragments with its fp32 and fp64 results, take the other
-// query's colour from the first pass, and accumulate the sample.
-__global__ void __launch_bounds__(256) k_edge_finish(const __grid_constant__ DevScene S, DevRender R0, const __grid_constant__ EdgeRecords E) {
+// Deferred boundary sample k of E.ds: blend each deferred query's fragments
+// with its fp32 and fp64 results, take the other query's colour from the
+// first pass, and accumulate the sample.
+__device__ __forceinline__ void edge_finish_one(const DevScene &S, const DevRender &R, const EdgeRecords &E, int k) {
+  int i = E.ds[k];
+  int idx = E.order[i];
+  float4 a = E.a[idx], b = E.b[idx];
+  int4 c = E.c[idx];
+  float2 d = E.d[idx];
+  v2 bpt = V2(a.x, a.y), normal = V2(a.z, a.w), lpt = V2(b.x, b.y);
+  int g = c.x, s = c.y;
+  BData bd = {c.z, c.w, d.x, d.y != 0.f ? 1 : 0};
+  int bx = min(max((int)(bpt.x * R.w), 0), R.w - 1), by = min(max((int)(bpt.y * R.h), 0), R.h - 1);
+  const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (by * R.w + bx) : nullptr;
+  float4 col[2];
+  int hit[2];
+  for (int side = 0; side < 2; side++) {
+    int qid = 2 * i + side;
+    int4 rec = E.dq[qid];
+    if (rec.x < 0) {
+      col[side] = E.dq_col[qid];
+      hit[side] = rec.y;
+      continue;
+    }
+    v2 qpt = side ? add2(bpt, scl2(1e-4f, normal)) : sub2(bpt, scl2(1e-4f, normal));
+    EdgeQ eq = {g, s, (rec.y >> 30) & 1};
+    unsigned res = (unsigned)rec.z | E.dq_res[qid];
+    col[side] = blend_fragments(S, bg, V2(qpt.x * S.W, qpt.y * S.H), &eq,
+                                reinterpret_cast<const FragRef *>(E.frag + rec.x), rec.y & 0x3fffffff, res,
+                                (unsigned)rec.w);
+    hit[side] = eq.hit;
+  }
+  edge_accumulate(S, R, g, s, bpt, normal, lpt, b.z, b.w, bd, col[0], hit[0], col[1], hit[1]);
+}
+
+__global__ void __launch_bounds__(256) k_edge_finish(const __grid_constant__ DevScene S, DevRender R0,
+                                                     const __grid_constant__ EdgeRecords E) {
   DevRender R = load_filter(R0, nullptr);
   int n = *(volatile const int *)&E.counts[3];
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    int i = E.ds[k];
-    int idx = E.order[i];
-    float4 a = E.a[idx], b = E.b[idx];
-    int4 c = E.c[idx];
-    float2 d = E.d[idx];
-    v2 bpt = V2(a.x, a.y), normal = V2(a.z, a.w), lpt = V2(b.x, b.y);
-    int g = c.x, s = c.y;
-    BData bd = {c.z, c.w, d.x, d.y != 0.f ? 1 : 0};
-    int bx = min(max((int)(bpt.x * R.w), 0), R.w - 1), by = min(max((int)(bpt.y * R.h), 0), R.h - 1);
-    const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (by * R.w + bx) : nullptr;
-    float4 col[2];
-    int hit[2];
-    for (int side = 0; side < 2; side++) {
-      int qid = 2 * i + side;
-      int4 rec = E.dq[qid];
-      if (rec.x < 0) {
-        col[side] = E.dq_col[qid];
-        hit[side] = rec.y;
-        continue;
-      }
-      v2 qpt = side ? add2(bpt, scl2(1e-4f, normal)) : sub2(bpt, scl2(1e-4f, normal));
-      EdgeQ eq = {g, s, (rec.y >> 30) & 1};
-      unsigned res = (unsigned)rec.z | E.dq_res[qid];
-      col[side] = blend_fragments(S, bg, V2(qpt.x * S.W, qpt.y * S.H), &eq,
-                                  reinterpret_cast<const FragRef *>(E.frag + rec.x), rec.y & 0x3fffffff, res,
-                                  (unsigned)rec.w);
-      hit[side] = eq.hit;
-    }
-    edge_accumulate(S, R, g, s, bpt, normal, lpt, b.z, b.w, bd, col[0], hit[0], col[1], hit[1]);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) edge_finish_one(S, R, E, k);
+}
+
+__global__ void __launch_bounds__(256) k_edge_finish_batch(const BatchScene *B, int nb, const int *order) {
+  for (int r = 0; r < nb; r++) {
+    const BatchScene &b = B[__ldg(&order[r])];
+    if (!b.E.job_a) continue;
+    DevRender R = load_filter(b.R, nullptr);
+    int n = *(volatile const int *)&b.E.counts[3];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) edge_finish_one(b.S, R, b.E, k);
   }
 }
 
@@ -502,6 +540,128 @@ __global__ void k_hit_check(const float *params, const float *fwd_params, int n,
   if (__syncthreads_or(diff) && threadIdx.x == 0) atomicOr(stale, 1u);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent batched passes.  One launch serves every scene of a batch: warps
+// take work items from a global counter until the batch's items run out, so
+// small scenes do not leave the GPU idle between launches and large ones are
+// spread over every SM.  An item is `spt` consecutive 32-sample chunks of one
+// scene (spt: samples per thread).  Scenes are taken in `order` (largest
+// first); item_start[r] is the first item of the r-th scene of that order.
+
+// range r with item_start[r] <= item < item_start[r + 1]
+__device__ __forceinline__ int batch_range_of(const int *item_start, int nb, int item) {
+  int lo = 0, hi = nb - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&item_start[mid]) <= item) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// The next item of the warp (lane 0 takes it, every lane gets it).
+__device__ __forceinline__ int batch_next(int *counter, int lane) {
+  int item = 0;
+  if (lane == 0) item = atomicAdd(counter, 1);
+  return __shfl_sync(0xffffffffu, item, 0);
+}
+
+// forward sample pass: a scene has tiles * spp * 8 chunks (the 8 warps of a
+// tile's 256-sample group)
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+    k_sample_fwd_batch(const BatchScene *B, int nb, const int *order, const int *item_start, int spt, int *counter) {
+  __shared__ WarpQueue wq[8];
+  int lane = threadIdx.x & 31;
+  WarpQueue *q = &wq[threadIdx.x >> 5];
+  int total = __ldg(&item_start[nb]);
+  #pragma unroll 1
+  for (int item = batch_next(counter, lane); item < total; item = batch_next(counter, lane)) {
+    int r = batch_range_of(item_start, nb, item);
+    const BatchScene &b = B[__ldg(&order[r])];
+    int spp = b.R.spp, nchunk = ((b.R.w + DVG_TILE - 1) / DVG_TILE) * ((b.R.h + DVG_TILE - 1) / DVG_TILE) * spp * 8;
+    int c0 = (item - __ldg(&item_start[r])) * spt;
+    #pragma unroll 1
+    for (int c = c0; c < c0 + spt && c < nchunk; c++) {
+      int rest = c >> 3;
+      sample_fwd_one<false>(b.S, b.R, rest / spp, rest % spp, (c & 7) * 32 + lane, b.samples, q, lane);
+    }
+  }
+}
+
+// interior adjoint
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+    k_sample_bwd_batch(const BatchScene *B, int nb, const int *order, const int *item_start, int spt, int *counter) {
+  __shared__ WarpQueue wq[8];
+  int lane = threadIdx.x & 31;
+  WarpQueue *q = &wq[threadIdx.x >> 5];
+  int total = __ldg(&item_start[nb]);
+  #pragma unroll 1
+  for (int item = batch_next(counter, lane); item < total; item = batch_next(counter, lane)) {
+    int r = batch_range_of(item_start, nb, item);
+    const BatchScene &b = B[__ldg(&order[r])];
+    DevRender R = load_filter(b.R, nullptr);
+    int spp = R.spp, nchunk = ((R.w + DVG_TILE - 1) / DVG_TILE) * ((R.h + DVG_TILE - 1) / DVG_TILE) * spp * 8;
+    int c0 = (item - __ldg(&item_start[r])) * spt;
+    #pragma unroll 1
+    for (int c = c0; c < c0 + spt && c < nchunk; c++) {
+      int rest = c >> 3;
+      sample_bwd_one<false>(b.S, R, rest / spp, rest % spp, (c & 7) * 32 + lane, nullptr, nullptr, q, lane);
+    }
+  }
+}
+
+// paired-lane boundary pass: a scene has ceil(2 * boundary samples / 32)
+// chunks; the sample counts are known on the device only, so every block
+// forms the item list itself
+__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+    k_edge_eval_batch(const BatchScene *B, int nb, const int *order, int spt, int *counter) {
+  __shared__ WarpQueue wq[8];
+  __shared__ int start[DVG_BATCH_MAX + 1];
+  int lane = threadIdx.x & 31;
+  WarpQueue *q = &wq[threadIdx.x >> 5];
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int r = 0; r < nb; r++) {
+      start[r] = run;
+      const BatchScene &b = B[__ldg(&order[r])];
+      int T = b.S.tiles_x * b.S.tiles_y * DVG_EDGE_CELLS;
+      int chunks = (2 * __ldg(&b.E.tile_start[T]) + 31) / 32;
+      run += (chunks + spt - 1) / spt;
+    }
+    start[nb] = run;
+  }
+  __syncthreads();
+  int total = start[nb];
+  #pragma unroll 1
+  for (int item = batch_next(counter, lane); item < total; item = batch_next(counter, lane)) {
+    int r = batch_range_of(start, nb, item);
+    const BatchScene &b = B[__ldg(&order[r])];
+    DevRender R = load_filter(b.R, nullptr);
+    long long c0 = (long long)(item - start[r]) * spt;
+    #pragma unroll 1
+    for (int k = 0; k < spt; k++) edge_eval_one<true>(b.S, R, b.E, (c0 + k) * 32 + lane, q, lane);
+  }
+}
+
+// deferred fp64 walks and deferred samples of every scene of the batch
+__global__ void __launch_bounds__(256) k_edge_jobs_batch(const BatchScene *B, int nb, const int *order) {
+  for (int r = 0; r < nb; r++) {
+    const BatchScene &b = B[__ldg(&order[r])];
+    if (!b.E.job_a) continue;
+    int n = min(*(volatile const int *)&b.E.counts[0], b.E.job_cap);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+      int4 ja = b.E.job_a[k];
+      if (ja.x < 0) continue;
+      float4 jb = b.E.job_b[k];
+      const DevScene &S = b.S;
+      int s = ja.z;
+      int hit = segment_root_test(S, SI(S, s, DVG_SHAPE_PARAM_OFF), SI(S, s, DVG_SHAPE_NUM_POINTS),
+                                  SI(S, s, DVG_SHAPE_THICKNESS_OFF), __ldg(&S.segment_ctrl[ja.w]),
+                                  __ldg(&S.seg_point[ja.w]), V2(jb.x, jb.y), jb.z);
+      if (hit) atomicOr(&b.E.dq_res[ja.x], 1u << ja.y);
+    }
+  }
+}
+
 static inline int tiles_of(const DevRender &R) {
   return ((R.w + DVG_TILE - 1) / DVG_TILE) * ((R.h + DVG_TILE - 1) / DVG_TILE);
 }
@@ -531,26 +691,58 @@ void launch_bg_combine(const DevScene &S, const DevRender &R, const float4 *dbg_
                        cudaStream_t st) {
   k_bg_combine<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(S, R, dbg_val, dbg_flag);
 }
-void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
+static unsigned persistent_grid(int ctas_per_sm) {
+  static int sms = 0;
+  if (sms <= 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 128;
+  }
+  return (unsigned)(sms * (ctas_per_sm > 0 ? ctas_per_sm : 1));
+}
+
+void launch_edge_setup(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
   long long n = (long long)R.w * R.h * R.spp;
   cudaMemsetAsync(E.tile_count, 0, sizeof(int) * S.tiles_x * S.tiles_y * DVG_EDGE_CELLS, st);
   k_edge_sample<<<blocks_of(n), 256, 0, st>>>(S, R, E);
   k_edge_scan<<<1, 1024, 0, st>>>(S, E);
   k_edge_order<<<blocks_of(n), 256, 0, st>>>(E, (int)n);
+  if (S.num_groups >= 8 && E.job_a) cudaMemsetAsync(E.counts, 0, 4 * sizeof(int), st);
+}
+void launch_edge_eval(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
+  long long n = (long long)R.w * R.h * R.spp;
   if (S.num_groups >= 8) {  // two lanes per sample
-    if (E.job_a) cudaMemsetAsync(E.counts, 0, 4 * sizeof(int), st);
-    k_edge_eval<true><<<blocks_of(2 * (long long)n), 256, 0, st>>>(S, R, E);
+    k_edge_eval<true><<<blocks_of(2 * n), 256, 0, st>>>(S, R, E);
     if (E.job_a) {
-      int dev = 0, sms = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      unsigned grid = (unsigned)(sms > 0 ? 8 * sms : 1024);
-      k_edge_jobs<<<grid, 256, 0, st>>>(S, E);
-      k_edge_finish<<<grid, 256, 0, st>>>(S, R, E);
+      k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, E);
+      k_edge_finish<<<persistent_grid(8), 256, 0, st>>>(S, R, E);
     }
   } else {
     k_edge_eval<false><<<blocks_of(n), 256, 0, st>>>(S, R, E);
   }
+}
+void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
+  launch_edge_setup(S, R, E, st);
+  launch_edge_eval(S, R, E, st);
+}
+
+void launch_batch_sample_fwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
+                             int ctas_per_sm, int *counter, cudaStream_t st) {
+  cudaMemsetAsync(counter, 0, sizeof(int), st);
+  k_sample_fwd_batch<<<persistent_grid(ctas_per_sm), 256, 0, st>>>(B, nb, order, item_start, spt, counter);
+}
+void launch_batch_sample_bwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
+                             int ctas_per_sm, int *counter, cudaStream_t st) {
+  cudaMemsetAsync(counter, 0, sizeof(int), st);
+  k_sample_bwd_batch<<<persistent_grid(ctas_per_sm), 256, 0, st>>>(B, nb, order, item_start, spt, counter);
+}
+void launch_batch_edge(const BatchScene *B, int nb, const int *order, int spt, int ctas_per_sm, int *counter,
+                       cudaStream_t st) {
+  cudaMemsetAsync(counter, 0, sizeof(int), st);
+  k_edge_eval_batch<<<persistent_grid(ctas_per_sm), 256, 0, st>>>(B, nb, order, spt, counter);
+  k_edge_jobs_batch<<<persistent_grid(8), 256, 0, st>>>(B, nb, order);
+  k_edge_finish_batch<<<persistent_grid(8), 256, 0, st>>>(B, nb, order);
 }
 void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
                 const float *d_sdf, cudaStream_t st) {

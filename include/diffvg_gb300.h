@@ -205,6 +205,35 @@ int dvg_mse_grad(const float *image, const float *target, int64_t num_pixels, fl
 int dvg_adam_step(float *params, const float *grads, float *m, float *v, const float *lr_scale, int64_t n,
                   float lr, float beta1, float beta2, float eps, int *step, void *stream);
 
+/* Batched launches over many scenes (no reference counterpart: the reference
+ * renders one scene per call, and its batch workloads loop over scenes in
+ * Python, apps/generative_models/rendering.py:46-95).  A DvgBatch groups
+ * existing scene handles (1 to 256, one device).  dvg_batch_forward renders
+ * every scene's colour image like dvg_render_forward, and
+ * dvg_batch_backward accumulates every scene's gradient like
+ * dvg_render_backward, except that the sample passes of all scenes (the
+ * forward samples, the interior adjoint, the boundary pass) each run as one
+ * persistent launch whose warps take (scene, tile) work items from a queue,
+ * largest scenes first.  args, images, d_images and d_params hold one entry
+ * per scene in batch order (device pointers in host arrays); images must be
+ * 16-byte aligned; sampled colour renders only (no prefiltering, background
+ * or eval positions).  Calls are stream-ordered and do not wait: failures
+ * latch in each scene, read them with dvg_scene_sync().  The first call on a
+ * batch sizes the scenes' arenas (it may allocate); later calls with the
+ * same image sizes allocate nothing, so they can be captured in a CUDA graph.
+ * tuning may be NULL (2 CTAs per SM, 1 sample per thread per item). */
+typedef struct DvgBatch DvgBatch;
+typedef struct DvgBatchTuning {
+  int32_t ctas_per_sm;         /* resident blocks per SM of the persistent launches: 1 or 2 */
+  int32_t samples_per_thread;  /* samples each thread takes per work item: 1 to 64 */
+} DvgBatchTuning;
+int dvg_batch_create(DvgScene *const *scenes, int num_scenes, DvgBatch **out_batch);
+int dvg_batch_destroy(DvgBatch *batch);
+int dvg_batch_forward(DvgBatch *batch, const DvgRenderArgs *args, float *const *images,
+                      const DvgBatchTuning *tuning, void *stream);
+int dvg_batch_backward(DvgBatch *batch, const DvgRenderArgs *args, const float *const *d_images,
+                       float *const *d_params, const DvgBatchTuning *tuning, void *stream);
+
 /* Forward colour render that allocates nothing (no counterpart in the
  * reference).  For callers that must not allocate device memory: a host
  * process that owns all GPU memory through its own pool and bars plugins

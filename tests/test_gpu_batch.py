@@ -77,3 +77,66 @@ def test_native_adam_matches_reference_update():
     torch.cuda.synchronize()
     assert int(step.item()) == 4
     assert torch.allclose(p.cpu().double(), ref, rtol=1e-5, atol=1e-6)
+
+
+def _batch_mixed(n=6, seed0=200):
+    """Scenes of uneven size, one of them with fewer than 8 groups (its
+    boundary pass runs per scene inside the batched call)."""
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import workloads
+    from diffvg_gb300.batch import BatchedScenes
+    scenes = workloads.batched_scenes(dvg, seeds=range(seed0, seed0 + n - 1), canvases=(64, 96, 160), path_range=(8, 96))
+    scenes.append(workloads.stroke_scene(dvg, seed=seed0 + 99, num_paths=5, canvas=80))
+    args = [dvg.RenderFunction.serialize_scene(w, h, s, g) for (w, h, s, g) in scenes]
+    seeds = list(range(seed0, seed0 + n))
+    b = BatchedScenes(args, seeds=seeds, lr=1e-2, streams=3)
+    targets = []
+    for i, p in enumerate(b.packed):
+        tp = workloads.perturbed_target_params(p, b.scene_params(i), seed0 + i)
+        targets.append(b.render(i, tp))
+    b.set_targets(targets)
+    return b
+
+
+@pytest.mark.parametrize('tuning', [(1, 1), (2, 2), (2, 5)])
+def test_persistent_batch_matches_per_scene_launches(tuning):
+    """One persistent launch per pass over all scenes (dvg_batch_forward /
+    dvg_batch_backward) gives every scene the images of its own launches and
+    its gradients within 1e-3 relative L2 (atomic order), also after graph
+    replays of full steps."""
+    import torch
+    b1, b2 = _batch_mixed(), _batch_mixed()
+    b2.set_mode('persistent', tuning)
+    b1.step_eager()
+    b2.step_eager()
+    torch.cuda.synchronize()
+    for i in range(b1.num_scenes):
+        assert torch.equal(b1.images[i], b2.images[i]), i
+        o, n = b1.offsets[i], b1.packed[i].num_params
+        g1, g2 = b1.grads[o:o + n], b2.grads[o:o + n]
+        assert float((g1 - g2).norm()) <= 1e-3 * max(float(g1.norm()), 1e-12), i
+    for _ in range(3):
+        b1.step()
+        b2.step()
+    torch.cuda.synchronize()
+    assert b2.check() is False
+    assert torch.allclose(b1.params, b2.params, rtol=1e-4, atol=1e-4)
+    assert b1.loss() == pytest.approx(b2.loss(), rel=1e-4)
+
+
+def test_autotuner_picks_and_caches_a_candidate(tmp_path):
+    import json
+    import torch
+    b = _batch_mixed(n=4, seed0=300)
+    before = b.params.clone()
+    path = tmp_path / 'tune.json'
+    t = b.autotune(candidates=[('streams', (2, 1)), ('persistent', (2, 1)), ('persistent', (1, 2))], steps=2,
+                   cache_path=str(path))
+    assert set(t) == {'streams 2 1', 'persistent 2 1', 'persistent 1 2'} and all(v > 0 for v in t.values())
+    assert torch.equal(b.params, before)  # the timing steps leave no trace
+    cached = json.loads(path.read_text())[b.workload_key()]
+    assert '%s %d %d' % (cached['mode'], *cached['tuning']) == min(t, key=t.get)
+    b2 = _batch_mixed(n=4, seed0=300)
+    assert b2.autotune(cache_path=str(path)) == t  # taken from the cache, not timed again
+    assert (b2.mode, (b2.tuning.ctas_per_sm, b2.tuning.samples_per_thread)) == (cached['mode'],
+                                                                                  tuple(cached['tuning']))
