@@ -548,12 +548,13 @@ __global__ void k_hit_check(const float *params, const float *fwd_params, int n,
 // scene (spt: samples per thread).  Scenes are taken in `order` (largest
 // first); item_start[r] is the first item of the r-th scene of that order.
 
-// range r with item_start[r] <= item < item_start[r + 1]
+// range r with item_start[r] <= item < item_start[r + 1] (item_start in
+// global or shared memory: plain loads)
 __device__ __forceinline__ int batch_range_of(const int *item_start, int nb, int item) {
   int lo = 0, hi = nb - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    if (__ldg(&item_start[mid]) <= item) lo = mid; else hi = mid - 1;
+    if (item_start[mid] <= item) lo = mid; else hi = mid - 1;
   }
   return lo;
 }
