@@ -51,6 +51,7 @@ WORKLOAD = dict(canvas=512, num_paths=2048, spp=(2, 2), seed=1, target_seed=2, f
 METRIC = 'fwd+bwd Msamples/s'
 UNIT = 'Msamples/s'
 PREP_KERNELS = 7  # kernels launched by one scene preparation
+HEADLINE = 'stroke_512_2x2'  # the headline workload's name among the counted configurations
 
 
 def _dist():
@@ -157,6 +158,46 @@ def issue_roofline(warp_instructions, avg_launch_s, num_sms, sm_mhz):
     return {'achieved': round(achieved, 2), 'peak': round(peak, 2), 'unit': 'G warp instructions/s',
             'frac': round(achieved / peak, 4), 'warp_instructions': int(warp_instructions),
             'source': 'profiles/ncu_traffic.json (ncu smsp__inst_executed.sum per launch)'}
+
+
+FP64_PEAK_OPS = 1.25e12   # GB300 nominal dense fp64 rate, ops/s (no per-pool measurement exists)
+
+
+def _work_counts():
+    """Counted algorithmic ops per kernel and configuration (oracle/count_work.py)."""
+    try:
+        with open(os.path.join(ROOT, 'baseline', 'work_counts.json')) as f:
+            return json.load(f).get('configs', {})
+    except Exception:
+        return {}
+
+
+def op_roofline(config, kernel, avg_launch_s, num_sms, sm_mhz):
+    """Counted-op roofline of one kernel: the reference algorithm's fp32 ops,
+    fp64 ops and sqrt / transcendental calls per launch (counted once per
+    configuration by the oracle's counting build) over the live launch time.
+    Peaks at the sampled SM clock: fp32 128 ops per SM per clock (one add,
+    sub or mul per lane; the kernels are compiled with --fmad=false, so no
+    pair fuses), transcendental 16 per SM per clock (the special-function
+    units), fp64 the GB300 nominal 1.25e12 ops/s.  'fp32_fp64_as_fp32'
+    counts every fp32 and fp64 op against the fp32 peak: the kernels run the
+    reference's fp64 root solves as certified fp32 with rare fp64 fallbacks,
+    so the fp64 fraction on its own can exceed 1.  None when a count or a
+    time is missing."""
+    counts = _work_counts().get(config, {}).get('kernels', {}).get(kernel)
+    if not counts or not avg_launch_s or not num_sms or not sm_mhz:
+        return None
+    clk = sm_mhz * 1e6
+    p32, ptr = 128.0 * num_sms * clk, 16.0 * num_sms * clk
+    f32, f64, tr = counts['fp32'], counts['fp64'], counts['transcendental']
+    return {'unit': 'Gop/s', 'source': 'baseline/work_counts.json',
+            'fp32': {'achieved': round(f32 / avg_launch_s / 1e9, 2), 'peak': round(p32 / 1e9, 1),
+                     'frac': round(f32 / avg_launch_s / p32, 5), 'ops': f32},
+            'fp64': {'achieved': round(f64 / avg_launch_s / 1e9, 2), 'peak': FP64_PEAK_OPS / 1e9,
+                     'frac': round(f64 / avg_launch_s / FP64_PEAK_OPS, 5), 'ops': f64},
+            'transcendental': {'achieved': round(tr / avg_launch_s / 1e9, 3), 'peak': round(ptr / 1e9, 1),
+                               'frac': round(tr / avg_launch_s / ptr, 5), 'ops': tr},
+            'fp32_fp64_as_fp32': {'frac': round((f32 + f64) / avg_launch_s / p32, 5)}}
 
 
 def _ncu_traffic():
@@ -304,12 +345,13 @@ def run_ours(args):
                 'traffic': traffic, 'algorithmic_bytes': alg, 'avg_launch_ms': round(avg_s * 1e3, 4),
                 'note': 'the path is FP32/FP64-issue bound (no dense contraction); the HBM fraction is small by '
                         'construction, the issue-slot fraction is the binding one'}
-    try:
-        sm_mhz = clock_info.get('sm_mhz') or clock_info.get('sm_max_mhz') or 2070.0
-        roofline['issue'] = issue_roofline(_ncu_traffic().get(dom + '_warp_instructions'), avg_s,
-                                           torch.cuda.get_device_properties(dev).multi_processor_count, sm_mhz)
-    except Exception:
-        roofline['issue'] = None
+    sm_mhz = clock_info.get('sm_mhz') or clock_info.get('sm_max_mhz') or 2070.0
+    num_sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    roofline['issue'] = issue_roofline(_ncu_traffic().get(dom + '_warp_instructions'), avg_s, num_sms, sm_mhz)
+    # counted-op rooflines: the dominant kernel first, then every kernel with counts
+    roofline['fp32'] = op_roofline(HEADLINE, dom, avg_s, num_sms, sm_mhz)
+    roofline['by_kernel'] = {k: op_roofline(HEADLINE, k, ms / cnt / 1e3, num_sms, sm_mhz)
+                             for k, (cnt, ms) in kernels.items() if k != 'prepare'}
 
     # ---------------- end to end with host buffers ----------------
     e2e = e2e_rf = None
@@ -326,7 +368,7 @@ def run_ours(args):
            'kernels_ms_per_launch': {k: round(v[1] / v[0], 4) for k, v in kernels.items()},
            'loss': float(loss_buf.item())}
     if rank == 0 and not args.no_batched:
-        out['configs'] = run_configs(dev)
+        out['configs'] = run_configs(dev, sm_mhz=sm_mhz, cpu=not args.no_cpu_baseline)
         out['batched'] = run_batched(dev)
         out['served'] = run_served(dev)
     if rank == 0 and not args.no_cpu_baseline:
@@ -459,10 +501,16 @@ def config_cases(dvg):
     }
 
 
-def run_configs(dev, steps=5, warmup=3, only=None):
+CPU_BASELINE_CONFIGS = ('circle_256_2x2', 'fill_prefiltered_1024_1x1')
+
+
+def run_configs(dev, steps=5, warmup=3, only=None, sm_mhz=None, cpu=True):
     """Device-resident fwd+bwd Msamples/s of the other single-scene
     configurations (config_cases), through the C ABI like the headline leg.
-    L2 flushed between steps, CUDA events per step."""
+    L2 flushed between steps, CUDA events per step; per-kernel launch times
+    over the timed steps with the counted-op roofline of each kernel; for
+    the circle and the fill-heavy prefiltered scene, the CPU oracle port on
+    the same step (cpu_baseline)."""
     import torch
     import diffvg_gb300 as dvg
     from diffvg_gb300 import _native
@@ -501,6 +549,7 @@ def run_configs(dev, steps=5, warmup=3, only=None):
             step()
         scene.sync(sptr)
         torch.cuda.synchronize(dev)
+        scene.profile(True)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         for i, (a, b) in enumerate(ev):
             flush.fill_(float(i))
@@ -509,11 +558,24 @@ def run_configs(dev, steps=5, warmup=3, only=None):
             b.record(stream)
         torch.cuda.synchronize(dev)
         scene.sync(sptr)
+        kernels = scene.profile_read()
+        scene.profile(False)
         ms = sum(a.elapsed_time(b) for a, b in ev) / steps
         n = w * h * nsx * nsy
+        num_sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        per_launch = {k: v[1] / v[0] / 1e3 for k, v in kernels.items() if v[0]}
+        dom = max((k for k in kernels if k != 'prepare'), key=lambda k: kernels[k][1])
         out[name] = {'Msamples_per_s': round(n / (ms / 1e3) / 1e6, 3), 'ms_per_step': round(ms, 4),
                      'samples_per_step': n, 'prefiltered': pf, 'steps': steps,
-                     'path_segments': int(packed.segment_ctrl.size)}
+                     'path_segments': int(packed.segment_ctrl.size),
+                     'kernels_ms_per_launch': {k: round(v * 1e3, 4) for k, v in per_launch.items()},
+                     'roofline': {'kernel': dom,
+                                  'fp32': op_roofline(name, dom, per_launch[dom], num_sms, sm_mhz or 2070.0),
+                                  'by_kernel': {k: op_roofline(name, k, t, num_sms, sm_mhz or 2070.0)
+                                                for k, t in per_launch.items() if k != 'prepare'}}}
+        if cpu and name in CPU_BASELINE_CONFIGS:
+            out[name]['cpu_baseline'] = cpu_baseline(packed, oracle_params(packed), w, h, nsx, nsy, seed,
+                                                     target.cpu().numpy(), min_seconds=2.0)
         scene.close()
         tscene.close()
     return out
@@ -726,19 +788,26 @@ def oracle_params(packed):
     return oracle.params_of(packed)
 
 
-def cpu_baseline(packed, P, w, h, nsx, nsy, seed, target, threads=None):
-    """One full step of the workload on the host cores with the oracle port."""
+def cpu_baseline(packed, P, w, h, nsx, nsy, seed, target, threads=None, min_seconds=0.0):
+    """Full fwd+bwd steps of the workload on the host cores with the oracle
+    port: one step, or as many as fill min_seconds."""
     import numpy as np
     import oracle
     threads = threads or os.cpu_count() or 1
+    steps = 0
     t0 = time.perf_counter()
-    fwd = oracle.render(packed, P, w, h, nsx, nsy, seed, num_threads=threads)
-    d_img = (2.0 / fwd['image'].size) * (fwd['image'] - target)
-    oracle.render(packed, P, w, h, nsx, nsy, seed, forward=False, d_image=d_img.astype(np.float32),
-                  num_threads=threads)
-    dt = time.perf_counter() - t0
-    return {'value': round(w * h * nsx * nsy / dt / 1e6, 4), 'unit': UNIT, 'cores': threads, 'kind': 'port',
-            'sample': 'one full fwd+bwd step of the workload (1,048,576 samples), %.2f s' % dt}
+    while True:
+        fwd = oracle.render(packed, P, w, h, nsx, nsy, seed, num_threads=threads)
+        d_img = (2.0 / fwd['image'].size) * (fwd['image'] - target)
+        oracle.render(packed, P, w, h, nsx, nsy, seed, forward=False, d_image=d_img.astype(np.float32),
+                      num_threads=threads)
+        steps += 1
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            break
+    n = w * h * nsx * nsy
+    return {'value': round(n * steps / dt / 1e6, 4), 'unit': UNIT, 'cores': threads, 'kind': 'port',
+            'sample': '%d full fwd+bwd step(s) of the workload (%d samples each), %.2f s' % (steps, n, dt)}
 
 
 def run_reference(args):
@@ -800,7 +869,7 @@ def main():
     args = ap.parse_args()
     if args.config:
         import torch
-        print(json.dumps({'configs': run_configs(torch.device('cuda', 0), only=args.config)}))
+        print(json.dumps({'configs': run_configs(torch.device('cuda', 0), only=args.config, cpu=False)}))
         return
     if args.profile:
         args.no_batched = args.no_cpu_baseline = True

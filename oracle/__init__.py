@@ -16,26 +16,30 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, '_build')
 LIB_PATH = os.path.join(BUILD_DIR, 'libdvg_oracle.so')
+# the same source with the work counters compiled in (-DDVG_COUNT_OPS)
+COUNT_LIB_PATH = os.path.join(BUILD_DIR, 'libdvg_oracle_count.so')
 SOURCES = [os.path.join(HERE, 'dvg_oracle.c')]
 HEADERS = [os.path.join(HERE, 'dvg_oracle.h'), os.path.join(HERE, '..', 'include', 'diffvg_gb300.h')]
 
 _lock = threading.Lock()
-_lib = None
+_libs = {}
 
 
-def build(force=False):
-    """Compiles the oracle into oracle/_build/libdvg_oracle.so (gcc, no GPU)."""
+def build(force=False, count_ops=False):
+    """Compiles the oracle into oracle/_build/libdvg_oracle.so (gcc, no GPU);
+    with count_ops, the work-counting variant libdvg_oracle_count.so."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if not force and os.path.exists(LIB_PATH):
+    path = COUNT_LIB_PATH if count_ops else LIB_PATH
+    if not force and os.path.exists(path):
         newest = max(os.path.getmtime(p) for p in SOURCES + HEADERS)
-        if os.path.getmtime(LIB_PATH) >= newest:
-            return LIB_PATH
-    tmp = LIB_PATH + '.%d.tmp' % os.getpid()
+        if os.path.getmtime(path) >= newest:
+            return path
+    tmp = path + '.%d.tmp' % os.getpid()
     cmd = ['gcc', '-O2', '-std=c11', '-ffp-contract=off', '-fno-fast-math', '-fPIC', '-shared',
-           '-o', tmp] + SOURCES + ['-lm', '-lpthread']
+           '-o', tmp] + SOURCES + ['-lm', '-lpthread'] + (['-DDVG_COUNT_OPS'] if count_ops else [])
     subprocess.check_call(cmd)
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, path)
+    return path
 
 
 class _SceneDesc(ctypes.Structure):
@@ -70,16 +74,22 @@ class _OracleArgs(ctypes.Structure):
     ]
 
 
-def _load():
-    global _lib
+def _load(count_ops=False):
     with _lock:
-        if _lib is None:
-            lib = ctypes.CDLL(build())
+        if count_ops not in _libs:
+            lib = ctypes.CDLL(build(count_ops=count_ops))
             lib.dvg_oracle_render.argtypes = [ctypes.POINTER(_SceneDesc), ctypes.POINTER(_OracleArgs),
                                               ctypes.c_char_p, ctypes.c_int]
             lib.dvg_oracle_render.restype = ctypes.c_int
-            _lib = lib
-    return _lib
+            if count_ops:
+                lib.dvg_oracle_ops.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]
+                lib.dvg_oracle_ops.restype = None
+            _libs[count_ops] = lib
+    return _libs[count_ops]
+
+
+PHASES = ('weight', 'render', 'resolve', 'edge')
+OP_KINDS = ('fp32', 'fp64', 'transcendental')
 
 
 class OracleError(RuntimeError):
@@ -101,11 +111,16 @@ def _f32(a):
 def render(packed, params, width, height, num_samples_x, num_samples_y, seed,
            background=None, forward=True, d_image=None, d_sdf=None,
            want_translation=False, want_background_grad=False, eval_positions=None,
-           output_sdf=False, num_threads=1):
+           output_sdf=False, num_threads=1, count_ops=False):
     """Runs the oracle on a PackedScene with host parameters `params`
     (numpy fp32, the parameter arena).  Returns a dict with 'image' or 'sdf'
-    (forward) and 'd_params', 'd_background', 'd_translation' (backward)."""
-    lib = _load()
+    (forward) and 'd_params', 'd_background', 'd_translation' (backward).
+    With count_ops the call runs the counting build and the dict also holds
+    'ops': {phase: {'fp32', 'fp64', 'transcendental'}} of this call."""
+    lib = _load(count_ops)
+    if count_ops:
+        ops = (ctypes.c_uint64 * 12)()
+        lib.dvg_oracle_ops(ops, 1)
     params = _f32(params)
     si = np.ascontiguousarray(packed.shape_info.reshape(-1), dtype=np.int32)
     sc = np.ascontiguousarray(packed.segment_ctrl, dtype=np.int32)
@@ -156,6 +171,9 @@ def render(packed, params, width, height, num_samples_x, num_samples_y, seed,
         out['d_background'] = dbg
         out['d_translation'] = dtr
     out['overflow'] = int(counters[0])
+    if count_ops:
+        lib.dvg_oracle_ops(ops, 1)
+        out['ops'] = {ph: {k: int(ops[3 * i + j]) for j, k in enumerate(OP_KINDS)} for i, ph in enumerate(PHASES)}
     return out
 
 

@@ -44,6 +44,48 @@
 #include <string.h>
 
 /* ------------------------------------------------------------------------ */
+/* Work counts (compiled in with -DDVG_COUNT_OPS only; oracle/count_work.py)  */
+/* ------------------------------------------------------------------------ */
+/* The arithmetic of the reference algorithm as restated here, per phase of
+ * a call (weight image, sample colours or interior adjoint, filtered
+ * resolve, boundary pass): fp32 add / sub / mul / div, fp64 add / sub / mul
+ * / div, and calls of sqrt and the transcendental functions (the reference's
+ * own precision decides fp32 or fp64).  Comparisons, bounding-box culls,
+ * index arithmetic and the traversal are not counted: the count is that of
+ * the formulas a sample evaluates once culling is exact.  Root iterations
+ * are counted as executed.  The counts are made by hand per formula in the
+ * OPS(...) annotations below. */
+#ifdef DVG_COUNT_OPS
+#include <stdatomic.h>
+enum { PH_WEIGHT, PH_RENDER, PH_RESOLVE, PH_EDGE, PH_COUNT };
+static __thread int g_phase;
+static __thread uint64_t g_ops[PH_COUNT][3];
+static _Atomic uint64_t g_ops_total[PH_COUNT][3];
+#define OPS(f32, f64, tr) (g_ops[g_phase][0] += (f32), g_ops[g_phase][1] += (f64), g_ops[g_phase][2] += (tr))
+/* a task chunk starts from zero: what the scene set-up counted is dropped */
+#define PHASE(p) (g_phase = (p), memset(g_ops, 0, sizeof g_ops))
+static void ops_flush(void) {
+  for (int p = 0; p < PH_COUNT; p++)
+    for (int k = 0; k < 3; k++) {
+      atomic_fetch_add(&g_ops_total[p][k], g_ops[p][k]);
+      g_ops[p][k] = 0;
+    }
+}
+/* phase-major [weight, render, resolve, edge] x [fp32, fp64, transcendental] */
+void dvg_oracle_ops(uint64_t out[12], int reset) {
+  for (int p = 0; p < PH_COUNT; p++)
+    for (int k = 0; k < 3; k++) {
+      out[3 * p + k] = atomic_load(&g_ops_total[p][k]);
+      if (reset) atomic_store(&g_ops_total[p][k], 0);
+    }
+}
+#else
+#define OPS(f32, f64, tr) ((void)0)
+#define PHASE(p) ((void)0)
+#define ops_flush() ((void)0)
+#endif
+
+/* ------------------------------------------------------------------------ */
 /* small vector / box / matrix helpers (vector.h, aabb.h, matrix.h)          */
 /* ------------------------------------------------------------------------ */
 typedef struct { float x, y; } v2;
@@ -183,7 +225,9 @@ static inline pcg32 pcg_init(int32_t idx, uint64_t seed) {
 /* ------------------------------------------------------------------------ */
 static int solve_quadratic_f(float a, float b, float c, float *t0, float *t1) {
   float discrim = b * b - 4 * a * c;
+  OPS(4, 0, 0);
   if (discrim < 0) return 0;
+  OPS(4, 0, 1);
   float root = sqrtf(discrim);
   float q = (b < 0) ? -0.5f * (b - root) : -0.5f * (b + root);
   *t0 = q / a;
@@ -193,7 +237,9 @@ static int solve_quadratic_f(float a, float b, float c, float *t0, float *t1) {
 }
 static int solve_quadratic_d(double a, double b, double c, double *t0, double *t1) {
   double discrim = b * b - 4 * a * c;
+  OPS(0, 4, 0);
   if (discrim < 0) return 0;
+  OPS(0, 4, 1);
   double root = sqrt(discrim);
   double q = (b < 0) ? -0.5f * (b - root) : -0.5f * (b + root);
   *t0 = q / a;
@@ -208,13 +254,16 @@ static int solve_cubic_d(double a, double b, double c, double d, double t[3]) {
   b /= a; c /= a; d /= a;
   double Q = (b * b - 3 * c) / 9.f;
   double R = (2 * b * b * b - 9 * b * c + 27 * d) / 54.f;
+  OPS(0, 19, 0);
   if (R * R < Q * Q * Q) {
+    OPS(0, 21, 8);
     double theta = acos(R / sqrt(Q * Q * Q));
     t[0] = -2.f * sqrt(Q) * cos(theta / 3.f) - b / 3.f;
     t[1] = -2.f * sqrt(Q) * cos((theta + 2.f * (double)M_PI) / 3.f) - b / 3.f;
     t[2] = -2.f * sqrt(Q) * cos((theta - 2.f * (double)M_PI) / 3.f) - b / 3.f;
     return 3;
   } else {
+    OPS(0, 10, 2);
     double A = R > 0 ? -pow(R + sqrt(R * R - Q * Q * Q), (double)(1. / 3.))
                      : pow(-R + sqrt(R * R - Q * Q * Q), (double)(1. / 3.));
     double B = fabs(A) > 1e-6f ? Q / A : 0.0;
@@ -234,13 +283,16 @@ static int solve_cubic_f(float a, float b, float c, float d, float t[3]) {
   b /= a; c /= a; d /= a;
   float Q = (b * b - 3 * c) / 9.f;
   float R = (2 * b * b * b - 9 * b * c + 27 * d) / 54.f;
+  OPS(19, 0, 0);
   if (R * R < Q * Q * Q) {
+    OPS(6, 15, 8);
     float theta = (float)acos((double)R / sqrt((double)(Q * Q * Q)));
     t[0] = (float)(-2.f * sqrt((double)Q) * cos((double)(theta / 3.f)) - (double)(b / 3.f));
     t[1] = (float)(-2.f * sqrt((double)Q) * cos((double)((theta + 2.f * (float)M_PI) / 3.f)) - (double)(b / 3.f));
     t[2] = (float)(-2.f * sqrt((double)Q) * cos((double)((theta - 2.f * (float)M_PI) / 3.f)) - (double)(b / 3.f));
     return 3;
   } else {
+    OPS(4, 6, 2);
     double third = (double)(float)(1. / 3.);
     float A = R > 0 ? (float)(-pow((double)R + sqrt((double)(R * R - Q * Q * Q)), third))
                     : (float)pow((double)(-R) + sqrt((double)(R * R - Q * Q * Q)), third);
@@ -259,6 +311,8 @@ static int solve_cubic_f(float a, float b, float c, float d, float t[3]) {
 static float gauss_1d(float x, float r) { return expf(-2.f * sq(x) / sq(r)) - expf(-2.f); }
 static float filter_weight(int type, float r, float dx, float dy) {
   if (fabsf(dx) > r || fabsf(dy) > r) return 0;
+  OPS(type == DVG_BOX ? 3 : type == DVG_TENT ? 6 : type == DVG_PARABOLIC ? 10 : type == DVG_HANN ? 16 : 12, 0,
+      type == DVG_HANN || type == DVG_GAUSSIAN ? 2 : 0);
   if (type == DVG_GAUSSIAN) return r > 0.f ? gauss_1d(dx, r) * gauss_1d(dy, r) : 0.f;
   if (type == DVG_BOX) return 1.f / sq(2 * r);
   if (type == DVG_TENT) return (r - fabsf(dx)) * (r - fabsf(dy)) / sq(sq(r));
@@ -270,6 +324,8 @@ static float filter_weight(int type, float r, float dx, float dy) {
   }
 }
 static float d_filter_weight(int type, float r, float dx, float dy, float d_ret) {
+  OPS(type == DVG_BOX ? 7 : type == DVG_TENT ? 14 : type == DVG_PARABOLIC ? 9 : 40, 0,
+      type == DVG_HANN || type == DVG_GAUSSIAN ? 4 : (type == DVG_TENT ? 1 : 0));
   if (type == DVG_GAUSSIAN) {
     if (!(r > 0.f) || fabsf(dx) > r || fabsf(dy) > r) return 0.f;
     float r3 = r * r * r;
@@ -364,10 +420,12 @@ static inline float stroke_width(const Scene *S, int s) { return S->P[SI(S, s, D
 
 /* eval of a Bezier segment (within_distance.h:63-66, 128-131) */
 static inline v2 eval_quad(v2 p0, v2 p1, v2 p2, float t) {
+  OPS(15, 0, 0);
   float tt = 1 - t;
   return add2(add2(scl2(tt * tt, p0), scl2(2 * tt * t, p1)), scl2(t * t, p2));
 }
 static inline v2 eval_cubic(v2 p0, v2 p1, v2 p2, v2 p3, float t) {
+  OPS(25, 0, 0);
   float tt = 1 - t;
   return add2(add2(add2(scl2(tt * tt * tt, p0), scl2(3 * tt * tt * t, p1)), scl2(3 * tt * t * t, p2)),
               scl2(t * t * t, p3));
@@ -670,7 +728,9 @@ static int winding_segment(const Scene *S, int s, int seg, v2 pt) {
     v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, (i0 + 1) % np);
     if (p1.y != p0.y) {
       float t = (pt.y - p0.y) / (p1.y - p0.y);
+      OPS(3, 0, 0);
       if (t >= 0 && t <= 1) {
+        OPS(5, 0, 0);
         float tp = p0.x - pt.x + t * (p1.x - p0.x);
         if (tp >= 0) w += (p1.y - p0.y > 0) ? 1 : -1;
       }
@@ -678,9 +738,11 @@ static int winding_segment(const Scene *S, int s, int seg, v2 pt) {
   } else if (nc == 1) {
     v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, i0 + 1), p2 = path_pt(S, s, (i0 + 2) % np);
     float t[2];
+    OPS(7, 0, 0);
     if (solve_quadratic_f(p0.y - 2 * p1.y + p2.y, -2 * p0.y + 2 * p1.y, p0.y - pt.y, &t[0], &t[1])) {
       for (int j = 0; j < 2; j++) {
         if (t[j] >= 0 && t[j] <= 1) {
+          OPS(19, 0, 0);
           float tp = (p0.x - 2 * p1.x + p2.x) * t[j] * t[j] + (-2 * p0.x + 2 * p1.x) * t[j] + p0.x - pt.x;
           if (tp >= 0) w += (2 * (p0.y - 2 * p1.y + p2.y) * t[j] + (-2 * p0.y + 2 * p1.y) > 0) ? 1 : -1;
         }
@@ -689,10 +751,12 @@ static int winding_segment(const Scene *S, int s, int seg, v2 pt) {
   } else {
     v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, i0 + 1), p2 = path_pt(S, s, i0 + 2), p3 = path_pt(S, s, (i0 + 3) % np);
     double t[3];
+    OPS(14, 0, 0);
     int n = solve_cubic_d((double)(-p0.y + 3 * p1.y - 3 * p2.y + p3.y), (double)(3 * p0.y - 6 * p1.y + 3 * p2.y),
                           (double)(-3 * p0.y + 3 * p1.y), (double)(p0.y - pt.y), t);
     for (int j = 0; j < n; j++) {
       if (t[j] >= 0 && t[j] <= 1) {
+        OPS(27, 18, 0);
         double tp = (-p0.x + 3 * p1.x - 3 * p2.x + p3.x) * t[j] * t[j] * t[j] +
                     (3 * p0.x - 6 * p1.x + 3 * p2.x) * t[j] * t[j] + (-3 * p0.x + 3 * p1.x) * t[j] + p0.x - pt.x;
         if (tp > 0) {
@@ -732,6 +796,7 @@ typedef struct { int group, shape, hit; } EdgeQ;
 /* is_inside (diffvg.cpp:33-87) */
 static int group_inside(const Scene *S, int g, v2 pt, EdgeQ *eq) {
   v2 lp = xform_pt(S->c2s + 9 * g, pt);
+  OPS(14, 0, 0);
   if (!box_in(S->g_local_box[g], lp)) return 0;
   int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
   int eo = GI(S, g, DVG_GROUP_EVEN_ODD);
@@ -778,6 +843,7 @@ static Quintic cubic_quintic(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
   v2 c = add2(scl2(-3, p0), scl2(3, p1));
   v2 e = sub2(p0, pt);
   Quintic q;
+  OPS(66, 5, 0);
   q.A = (double)(3 * sum2(mul2(a, a)));
   q.B = (double)(5 * sum2(mul2(a, b)));
   q.C = (double)(4 * sum2(mul2(a, c)) + 2 * sum2(mul2(b, b)));
@@ -788,9 +854,11 @@ static Quintic cubic_quintic(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
   return q;
 }
 static inline double quintic_eval(const Quintic *q, double t) {
+  OPS(0, 19, 0);
   return t * t * t * t * t + q->B * t * t * t * t + q->C * t * t * t + q->D * t * t + q->E * t + q->F;
 }
 static inline double quintic_deriv(const Quintic *q, double t) {
+  OPS(0, 17, 0);
   return 5 * t * t * t * t + 4 * q->B * t * t * t + 3 * q->C * t * t + 2 * q->D * t + q->E;
 }
 /* isolator intervals of the normalised quintic (within_distance.h:181-236);
@@ -802,6 +870,7 @@ static int quintic_intervals(const Quintic *q, float iv[4]) {
   double p1D = q->F - q->B * q->E / 25.f;
   double q_root = -q->B / 5.f;
   double pr[3];
+  OPS(0, 17, 0);
   int ns = solve_cubic_d(p1A, p1B, p1C, p1D, pr);
   iv[0] = (q_root >= 0 && q_root <= 1) ? (float)q_root : -1.0f;
   for (int j = 0; j < ns; j++) iv[j + 1] = (float)pr[j];
@@ -820,6 +889,7 @@ static float quintic_root(const Quintic *q, float lb, float ub) {
     if (value > 0.f) ub = t; else lb = t;
     double derivative = quintic_deriv(q, t);
     t = (float)(t - value / derivative);
+    OPS(0, 2, 0);
   }
   return t;
 }
@@ -834,8 +904,10 @@ static int within_segment(const Scene *S, int s, int seg, v2 pt, float r) {
     float t = dot2(sub2(pt, p0), sub2(p1, p0)) / dot2(sub2(p1, p0), sub2(p1, p0));
     float r0 = r, r1 = r;
     if (th >= 0) { r0 = P[th + i0]; r1 = P[th + i1]; }
+    OPS(17, 0, 0);
     if (t < 0) return distsq2(p0, pt) < r0 * r0 ? 1 : 0;
     if (t > 1) return distsq2(p1, pt) < r1 * r1 ? 1 : 0;
+    OPS(9, 0, 0);
     float rr = r0 + t * (r1 - r0);
     return distsq2(add2(p0, scl2(t, sub2(p1, p0))), pt) < rr * rr ? 1 : 0;
   } else if (nc == 1) {
@@ -843,12 +915,16 @@ static int within_segment(const Scene *S, int s, int seg, v2 pt, float r) {
     v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, i1), p2 = path_pt(S, s, i2);
     if (SI(S, s, DVG_SHAPE_FLAGS) & 2) {
       v2 cp = quad_closest_approx(p0, p1, p2, pt, NULL);
+      OPS(46, 0, 0);
       return distsq2(cp, pt) < r * r ? 1 : -1; /* -1: the reference returns false for the whole path */
     }
     float r0 = r, r1 = r, r2 = r;
     if (th >= 0) { r0 = P[th + i0]; r1 = P[th + i1]; r2 = P[th + i2]; }
+    OPS(6, 0, 0);
     if (distsq2(eval_quad(p0, p1, p2, 0), pt) < r0 * r0) return 1;
+    OPS(6, 0, 0);
     if (distsq2(eval_quad(p0, p1, p2, 1), pt) < r2 * r2) return 1;
+    OPS(34, 0, 0);
     v2 v = add2(sub2(p0, scl2(2, p1)), p2), w = add2(neg2(p0), p1);
     float A = sum2(mul2(v, v));
     float B = sum2(mul2(scl2(3, v), w));
@@ -858,6 +934,7 @@ static int within_segment(const Scene *S, int s, int seg, v2 pt, float r) {
     int n = solve_cubic_f(A, B, C, D, t);
     for (int j = 0; j < n; j++) {
       if (t[j] >= 0 && t[j] <= 1) {
+        OPS(16, 0, 0);
         float tt = 1 - t[j];
         float rr = (tt * tt) * r0 + (2 * tt * t[j]) * r1 + (t[j] * t[j]) * r2;
         if (distsq2(eval_quad(p0, p1, p2, t[j]), pt) < rr * rr) return 1;
@@ -869,7 +946,9 @@ static int within_segment(const Scene *S, int s, int seg, v2 pt, float r) {
     v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, i1), p2 = path_pt(S, s, i2), p3 = path_pt(S, s, i3);
     float r0 = r, r1 = r, r2 = r, r3 = r;
     if (th >= 0) { r0 = P[th + i0]; r1 = P[th + i1]; r2 = P[th + i2]; r3 = P[th + i3]; }
+    OPS(6, 0, 0);
     if (distsq2(eval_cubic(p0, p1, p2, p3, 0), pt) < r0 * r0) return 1;
+    OPS(6, 0, 0);
     if (distsq2(eval_cubic(p0, p1, p2, p3, 1), pt) < r3 * r3) return 1;
     Quintic q = cubic_quintic(p0, p1, p2, p3, pt);
     float iv[4];
@@ -880,9 +959,11 @@ static int within_segment(const Scene *S, int s, int seg, v2 pt, float r) {
       float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
       float lb = lower, ub = upper;
       double lbe = quintic_eval(&q, lb), ube = quintic_eval(&q, ub);
+      OPS(0, 1, 0);
       if (lbe * ube > 0) continue;
       if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
       float t = quintic_root(&q, lb, ub);
+      OPS(21, 0, 0);
       float tt = 1 - t;
       float rr = (tt * tt * tt) * r0 + (3 * tt * tt * t) * r1 + (3 * tt * t * t) * r2 + (t * t * t) * r3;
       if (distsq2(eval_cubic(p0, p1, p2, p3, t), pt) < rr * rr) return 1;
@@ -929,6 +1010,7 @@ static int within_shape(const Scene *S, int s, v2 pt, float r) {
 /* within_distance(scene, group, pt, edge_query) (within_distance.h:355-446) */
 static int group_stroke(const Scene *S, int g, v2 pt, EdgeQ *eq) {
   v2 lp = xform_pt(S->c2s + 9 * g, pt);
+  OPS(14, 0, 0);
   int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
   int ret = 0;
   for (int k = 0; k < nsh; k++) {
@@ -963,6 +1045,8 @@ static int closest_path(const Scene *S, int s, v2 pt, float max_radius, PathInfo
     if (nc == 0) {
       v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, (i0 + 1) % np);
       float t = dot2(sub2(pt, p0), sub2(p1, p0)) / dot2(sub2(p1, p0), sub2(p1, p0));
+      OPS(16, 0, 1);
+      if (t >= 0 && t <= 1) OPS(12, 0, 0);
       if (t < 0) { dist = dist2(p0, pt); cp = p0; t_root = 0; }
       else if (t > 1) { dist = dist2(p1, pt); cp = p1; t_root = 1; }
       else { dist = dist2(add2(p0, scl2(t, sub2(p1, p0))), pt); cp = add2(p0, scl2(t, sub2(p1, p0))); t_root = t; }
@@ -971,9 +1055,11 @@ static int closest_path(const Scene *S, int s, v2 pt, float max_radius, PathInfo
       if (SI(S, s, DVG_SHAPE_FLAGS) & 2) {
         cp = quad_closest_approx(p0, p1, p2, pt, &t_root);
         dist = dist2(cp, pt);
+        OPS(45, 0, 1);
       } else {
         v2 pt0 = eval_quad(p0, p1, p2, 0), pt1 = eval_quad(p0, p1, p2, 1);
         float d0 = dist2(pt0, pt), d1 = dist2(pt1, pt);
+        OPS(44, 0, 2);
         dist = d0; cp = pt0; t_root = 0;
         if (d1 < dist) { dist = d1; cp = pt1; t_root = 1; }
         v2 v = add2(sub2(p0, scl2(2, p1)), p2), w = add2(neg2(p0), p1);
@@ -987,6 +1073,7 @@ static int closest_path(const Scene *S, int s, v2 pt, float max_radius, PathInfo
           if (t[j] >= 0 && t[j] <= 1) {
             v2 p = eval_quad(p0, p1, p2, t[j]);
             float dp = dist2(p, pt);
+            OPS(5, 0, 1);
             if (dp < dist) { dist = dp; cp = p; t_root = t[j]; }
           }
         }
@@ -995,6 +1082,7 @@ static int closest_path(const Scene *S, int s, v2 pt, float max_radius, PathInfo
       v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, i0 + 1), p2 = path_pt(S, s, i0 + 2), p3 = path_pt(S, s, (i0 + 3) % np);
       v2 pt0 = eval_cubic(p0, p1, p2, p3, 0), pt1 = eval_cubic(p0, p1, p2, p3, 1);
       float d0 = dist2(pt0, pt), d1 = dist2(pt1, pt);
+      OPS(10, 0, 2);
       dist = d0; cp = pt0; t_root = 0;
       if (d1 < dist) { dist = d1; cp = pt1; t_root = 1; }
       Quintic q = cubic_quintic(p0, p1, p2, p3, pt);
@@ -1006,11 +1094,13 @@ static int closest_path(const Scene *S, int s, v2 pt, float max_radius, PathInfo
         float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
         float lb = lower, ub = upper;
         double lbe = quintic_eval(&q, lb), ube = quintic_eval(&q, ub);
+        OPS(0, 1, 0);
         if (lbe * ube > 0) continue;
         if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
         float t = quintic_root(&q, lb, ub);
         v2 p = eval_cubic(p0, p1, p2, p3, t);
         float dp = dist2(p, pt);
+        OPS(5, 0, 1);
         if (dp < dist) { dist = dp; cp = p; t_root = t; }
         if (upper >= 1.f) break;
         lower = upper;
@@ -1063,6 +1153,7 @@ static int closest_shape(const Scene *S, int s, v2 pt, float max_radius, PathInf
 static int group_distance(const Scene *S, int g, v2 pt, float max_radius, int *min_shape, v2 *closest,
                           PathInfo *info, float *result) {
   v2 lp = xform_pt(S->c2s + 9 * g, pt);
+  OPS(14, 0, 0);
   const float *s2c = S->P + GI(S, g, DVG_GROUP_XFORM_OFF);
   int nsh = GI(S, g, DVG_GROUP_NUM_SHAPES), off = GI(S, g, DVG_GROUP_SHAPES_OFF);
   float min_dist = max_radius;
@@ -1075,6 +1166,7 @@ static int group_distance(const Scene *S, int g, v2 pt, float max_radius, int *m
     if (closest_shape(S, s, lp, max_radius, &li, &lcp)) {
       v2 cp = xform_pt(s2c, lcp);
       float dist = dist2(cp, pt);
+      OPS(19, 0, 1);
       if (!found || dist < min_dist) {
         found = 1; min_dist = dist;
         if (min_shape) *min_shape = s;
@@ -1132,7 +1224,9 @@ static v4 paint_color(const Scene *S, int kind, int off, int nstops, v2 pt) {
   if (kind == DVG_LINEAR) {
     v2 beg = V2(c[0], c[1]), end = V2(c[2], c[3]);
     t = dot2(sub2(pt, beg), sub2(end, beg)) / rmax(dot2(sub2(end, beg), sub2(end, beg)), 1e-3f);
+    OPS(11, 0, 0);
   } else {
+    OPS(7, 0, 1);
     v2 cen = V2(c[0], c[1]), rad = V2(c[2], c[3]);
     v2 off2 = sub2(pt, cen);
     v2 no = V2(off2.x / rad.x, off2.y / rad.y);
@@ -1145,6 +1239,7 @@ static v4 paint_color(const Scene *S, int kind, int off, int nstops, v2 pt) {
     if (t >= oc && t < on) {
       v4 cc = stop_color(cols, i), cn = stop_color(cols, i + 1);
       float tt = (t - oc) / (on - oc);
+      OPS(16, 0, 0);
       return add4(scl4(1 - tt, cc), scl4(tt, cn));
     }
   }
@@ -1164,7 +1259,9 @@ static void d_paint_color(const Scene *S, int kind, int off, int nstops, v2 pt, 
   if (kind == DVG_LINEAR) {
     beg = V2(c[0], c[1]); end = V2(c[2], c[3]);
     t = dot2(sub2(pt, beg), sub2(end, beg)) / rmax(dot2(sub2(end, beg), sub2(end, beg)), 1e-3f);
+    OPS(11, 0, 0);
   } else {
+    OPS(7, 0, 1);
     cen = V2(c[0], c[1]); rad = V2(c[2], c[3]);
     off2 = sub2(pt, cen);
     no = V2(off2.x / rad.x, off2.y / rad.y);
@@ -1179,6 +1276,7 @@ static void d_paint_color(const Scene *S, int kind, int off, int nstops, v2 pt, 
     if (t >= oc && t < on) {
       v4 cc = stop_color(cols, i), cn = stop_color(cols, i + 1);
       float tt = (t - oc) / (on - oc);
+      OPS(28, 0, 0);
       v4 dcc = scl4(1 - tt, d_color), dcn = scl4(tt, d_color);
       v4 diff = sub4(cn, cc);
       float d_tt = d_color.x * diff.x + d_color.y * diff.y + d_color.z * diff.z + d_color.w * diff.w;
@@ -1190,6 +1288,7 @@ static void d_paint_color(const Scene *S, int kind, int off, int nstops, v2 pt, 
       gadd(G, co + 4 * (i + 1) + 2, dcn.z); gadd(G, co + 4 * (i + 1) + 3, dcn.w);
       gadd(G, oo + i, d_oc); gadd(G, oo + i + 1, d_on);
       if (kind == DVG_LINEAR) {
+        OPS(34, 0, 0);
         float l = rmax(dot2(sub2(end, beg), sub2(end, beg)), 1e-3f);
         v2 d_beg = div2s(scl2(d_t, sub2(neg2(sub2(pt, beg)), sub2(end, beg))), l);
         v2 d_end = div2s(scl2(d_t, sub2(pt, beg)), l);
@@ -1202,6 +1301,7 @@ static void d_paint_color(const Scene *S, int kind, int off, int nstops, v2 pt, 
         if (d_translation) { d_translation[0] += d_beg.x + d_end.x; d_translation[1] += d_beg.y + d_end.y; }
         return;
       } else {
+        OPS(20, 0, 1);
         v2 d_no = d_length2(no, d_t);
         v2 d_off = V2(d_no.x / rad.x, d_no.y / rad.y);
         v2 d_rad = V2(-d_no.x * off2.x / (rad.x * rad.x), -d_no.y * off2.y / (rad.y * rad.y));
@@ -1230,6 +1330,7 @@ static void d_closest_path(const Scene *S, int s, v2 pt, v2 d_cp, const PathInfo
     int i1 = (i0 + 1) % np;
     v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, i1);
     float tl = dot2(sub2(pt, p0), sub2(p1, p0)) / dot2(sub2(p1, p0), sub2(p1, p0));
+    OPS(20, 0, 0);
     v2 d0 = V2(0, 0), d1 = V2(0, 0);
     if (tl < 0) d0 = add2(d0, d_cp);
     else if (tl > 1) d1 = add2(d1, d_cp);
@@ -1250,6 +1351,7 @@ static void d_closest_path(const Scene *S, int s, v2 pt, v2 d_cp, const PathInfo
       float B = sum2(mul2(scl2(3, v), w));
       float C = sum2(add2(mul2(scl2(2, w), w), mul2(v, sub2(p0, pt))));
       v2 d_p = d_cp;
+      OPS(45, 0, 0);
       float tt = 1 - t;
       float d_tt = 2 * tt * dot2(d_p, p0) + 2 * t * dot2(d_p, p1);
       float d_t = -d_tt + 2 * tt * dot2(d_p, p1) + 2 * t * dot2(d_p, p2);
@@ -1275,6 +1377,7 @@ static void d_closest_path(const Scene *S, int s, v2 pt, v2 d_cp, const PathInfo
       double A = (double)(3 * sum2(mul2(add2(sub2(add2(neg2(p0), scl2(3, p1)), scl2(3, p2)), p3),
                                          add2(sub2(add2(neg2(p0), scl2(3, p1)), scl2(3, p2)), p3))));
       v2 d_p = d_cp;
+      OPS(84, 0, 0);
       float tt = 1 - t;
       float d_tt = 3 * tt * tt * dot2(d_p, p0) + 6 * tt * t * dot2(d_p, p1) + 3 * t * t * dot2(d_p, p2);
       float d_t = -d_tt + 3 * tt * tt * dot2(d_p, p1) + 6 * tt * t * dot2(d_p, p2) + 3 * t * t * dot2(d_p, p3);
@@ -1284,6 +1387,7 @@ static void d_closest_path(const Scene *S, int s, v2 pt, v2 d_cp, const PathInfo
       d3 = add2(d3, scl2(t * t * t, d_p));
       double pd = quintic_deriv(&q, t);
       if (fabs(pd) > 1e-10f) {
+        OPS(70, 115, 0);
         double dB = -(d_t / pd) * t * t * t * t;
         double dC = -(d_t / pd) * t * t * t;
         double dD = -(d_t / pd) * t * t;
@@ -1432,7 +1536,9 @@ static void mat_mul3(const float *a, const float *b, float *r) {
 
 static void d_group_distance(const Scene *S, int g, int s, v2 pt, v2 closest, const PathInfo *info, float d_dist,
                              Grad *G, float *d_translation) {
+  OPS(5, 0, 0);
   if (distsq2(pt, closest) < 1e-10f) return;
+  OPS(221, 0, 1);
   const float *c2s = S->c2s + 9 * g;
   int xo = GI(S, g, DVG_GROUP_XFORM_OFF);
   const float *s2c = S->P + xo;
@@ -1510,13 +1616,14 @@ static v4 sample_color(const Scene *S, const v4 *bg, v2 screen_pt, const v4 *d_c
       if (na >= 1.f && eq->hit) eq->hit = 0;
       if (eq->group == f->group) eq->hit = 1;
     }
+    OPS(12, 0, 0);
     acc_r[i] = pr * (1 - na) + na * f->r;
     acc_g[i] = pg * (1 - na) + na * f->g;
     acc_b[i] = pb * (1 - na) + na * f->b;
     acc_a[i] = pa * (1 - na) + na;
   }
   float fr = acc_r[nf - 1], fg = acc_g[nf - 1], fb = acc_b[nf - 1], fa = acc_a[nf - 1];
-  if (fa > 1e-6f) { fr /= fa; fg /= fa; fb /= fa; }
+  if (fa > 1e-6f) { fr /= fa; fg /= fa; fb /= fa; OPS(3, 0, 0); }
   if (d_color) {
     float dcr = d_color->x, dcg = d_color->y, dcb = d_color->z, dca = d_color->w;
     if (fa > 1e-6f) {
@@ -1528,6 +1635,7 @@ static v4 sample_color(const Scene *S, const v4 *bg, v2 screen_pt, const v4 *d_c
       const Frag *f = &frags[i];
       float pa = i > 0 ? acc_a[i - 1] : first_a;
       float pr = i > 0 ? acc_r[i - 1] : first_r, pg = i > 0 ? acc_g[i - 1] : first_g, pb = i > 0 ? acc_b[i - 1] : first_b;
+      OPS(21, 0, 0);
       float d_pa = dca * (1.f - f->a);
       float d_ai = dca * (1.f - pa);
       d_ai += dcr * (f->r - pr) + dcg * (f->g - pg) + dcb * (f->b - pb);
@@ -1547,11 +1655,13 @@ static v4 sample_color(const Scene *S, const v4 *bg, v2 screen_pt, const v4 *d_c
 
 /* smoothstep / d_smoothstep (diffvg.cpp:817-833) */
 static inline float smoothstep(float d) {
+  OPS(6, 0, 0);
   float t = clampf_((d + 1.f) / 2.f, 0.f, 1.f);
   return t * t * (3 - 2 * t);
 }
 static inline float d_smoothstep(float d, float d_ret) {
   if (d < -1.f || d > 1.f) return 0.f;
+  OPS(7, 0, 0);
   float t = (d + 1.f) / 2.f;
   float d_t = d_ret * (6 * t - 6 * t * t);
   return d_t / 2.f;
@@ -1622,13 +1732,14 @@ static v4 sample_color_prefiltered(const Scene *S, const v4 *bg, v2 screen_pt, c
     float na = f->a;
     float pa = i > 0 ? acc_a[i - 1] : first_a;
     float pr = i > 0 ? acc_r[i - 1] : first_r, pg = i > 0 ? acc_g[i - 1] : first_g, pb = i > 0 ? acc_b[i - 1] : first_b;
+    OPS(12, 0, 0);
     acc_r[i] = pr * (1 - na) + na * f->r;
     acc_g[i] = pg * (1 - na) + na * f->g;
     acc_b[i] = pb * (1 - na) + na * f->b;
     acc_a[i] = pa * (1 - na) + na;
   }
   float fr = acc_r[nf - 1], fg = acc_g[nf - 1], fb = acc_b[nf - 1], fa = acc_a[nf - 1];
-  if (fa > 1e-6f) { fr /= fa; fg /= fa; fb /= fa; }
+  if (fa > 1e-6f) { fr /= fa; fg /= fa; fb /= fa; OPS(3, 0, 0); }
   if (d_color) {
     float dcr = d_color->x, dcg = d_color->y, dcb = d_color->z, dca = d_color->w;
     if (fa > 1e-6f) {
@@ -1640,6 +1751,7 @@ static v4 sample_color_prefiltered(const Scene *S, const v4 *bg, v2 screen_pt, c
       const PFrag *f = &frags[i];
       float pa = i > 0 ? acc_a[i - 1] : first_a;
       float pr = i > 0 ? acc_r[i - 1] : first_r, pg = i > 0 ? acc_g[i - 1] : first_g, pb = i > 0 ? acc_b[i - 1] : first_b;
+      OPS(21, 0, 0);
       float d_pa = dca * (1.f - f->a);
       float d_ai = dca * (1.f - pa);
       d_ai += dcr * (f->r - pr) + dcg * (f->g - pg) + dcb * (f->b - pb);
@@ -1748,12 +1860,14 @@ static v2 sample_shape_boundary(const Scene *S, int s, float t, v2 *normal, floa
   float sr = stroke_width(S, s);
   if (kind == DVG_CIRCLE) {
     float r = p[0]; v2 c = V2(p[1], p[2]);
+    OPS(19, 0, 3);
     v2 off = V2((float)(r * dcos(2 * (float)M_PI * t)), (float)(r * dsin(2 * (float)M_PI * t)));
     *normal = normalize2(off);
     *pdf /= (2 * (float)M_PI * r);
     return perturb(add2(c, off), normal, dir, sr);
   } else if (kind == DVG_ELLIPSE) {
     v2 r = V2(p[0], p[1]), c = V2(p[2], p[3]);
+    OPS(30, 0, 5);
     v2 off = V2((float)(r.x * dcos(2 * (float)M_PI * t)), (float)(r.y * dsin(2 * (float)M_PI * t)));
     float dxdt = (float)(-r.x * dsin(2 * (float)M_PI * t) * 2 * (float)M_PI);
     float dydt = (float)(r.y * dcos(2 * (float)M_PI * t) * 2 * (float)M_PI);
@@ -1762,6 +1876,7 @@ static v2 sample_shape_boundary(const Scene *S, int s, float t, v2 *normal, floa
     return perturb(add2(c, off), normal, dir, sr);
   } else if (kind == DVG_RECT) {
     v2 pmin = V2(p[0], p[1]), pmax = V2(p[2], p[3]);
+    OPS(12, 0, 0);
     float w = pmax.x - pmin.x, h = pmax.y - pmin.y;
     *pdf /= (2 * (w + h));
     if (t <= w / (w + h)) {
@@ -1794,7 +1909,9 @@ static v2 sample_shape_boundary(const Scene *S, int s, float t, v2 *normal, floa
     if (th >= 0) cap_length = (float)M_PI * (P[th] + P[th + np - 1]);
     else cap_length = 2 * (float)M_PI * sr;
     float cap_prob = cap_length / (cap_length + S->s_length[s]);
+    OPS(5, 0, 0);
     if (t < cap_prob) {
+      OPS(14, 0, 3);
       t = t / cap_prob;
       *pdf *= cap_prob;
       float r0 = sr, r1 = sr;
@@ -1829,6 +1946,7 @@ static v2 sample_shape_boundary(const Scene *S, int s, float t, v2 *normal, floa
   if (nc == 0) {
     int i1 = (i0 + 1) % np;
     v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, i1);
+    OPS(19, 0, 1);
     v2 tan = sub2(p1, p0);
     float tl = len2(tan);
     if (tl == 0) { *pdf = 0; return V2(0, 0); }
@@ -1846,6 +1964,7 @@ static v2 sample_shape_boundary(const Scene *S, int s, float t, v2 *normal, floa
     int i1 = i0 + 1, i2 = (i0 + 2) % np;
     v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, i1), p2 = path_pt(S, s, i2);
     v2 tan = add2(scl2(2 * (1 - t), sub2(p1, p0)), scl2(2 * t, sub2(p2, p1)));
+    OPS(32, 0, 1);
     float tl = len2(tan);
     if (tl == 0) { *pdf = 0; return V2(0, 0); }
     *normal = div2s(V2(-tan.y, tan.x), tl);
@@ -1863,6 +1982,7 @@ static v2 sample_shape_boundary(const Scene *S, int s, float t, v2 *normal, floa
     int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
     v2 p0 = path_pt(S, s, i0), p1 = path_pt(S, s, i1), p2 = path_pt(S, s, i2), p3 = path_pt(S, s, i3);
     v2 tan = add2(add2(scl2(3 * sq(1 - t), sub2(p1, p0)), scl2(6 * (1 - t) * t, sub2(p2, p1))), scl2(3 * t * t, sub2(p3, p2)));
+    OPS(44, 0, 1);
     float tl = len2(tan);
     if (tl == 0) { *pdf = 0; return V2(0, 0); }
     *normal = div2s(V2(-tan.y, tan.x), tl);
@@ -1904,6 +2024,8 @@ static v2 sample_boundary(const Scene *S, int g, int s, float t, v2 *normal, flo
 static void accumulate_boundary_gradient(const Scene *S, int g, int s, float contrib, float t, v2 normal,
                                          const BData *bd, v2 local_pt, Grad *G) {
   int kind = SI(S, s, DVG_SHAPE_KIND), po = SI(S, s, DVG_SHAPE_PARAM_OFF);
+  /* the shape_to_canvas adjoint (d_xform_pt) and the control-point weights */
+  OPS(40 + (kind == DVG_PATH ? 30 : kind == DVG_ELLIPSE ? 10 : 3), 0, kind == DVG_ELLIPSE ? 2 : 0);
   int th = kind == DVG_PATH ? SI(S, s, DVG_SHAPE_THICKNESS_OFF) : -1;
   int np = kind == DVG_PATH ? SI(S, s, DVG_SHAPE_NUM_POINTS) : 0;
   int so = kind == DVG_PATH ? SI(S, s, DVG_SHAPE_SEG_OFF) : 0;
@@ -1994,6 +2116,7 @@ static inline v2 sample_pos(const Ctx *C, int idx, int prefilter, int *x, int *y
   *x = (idx / (C->nsx * C->nsy)) % C->w;
   *y = (idx / (C->nsx * C->nsy * C->w));
   float rx = pcg_float(&rng), ry = pcg_float(&rng);
+  OPS(8, 0, 0);
   if (prefilter) { rx = 0.5f; ry = 0.5f; }
   return V2(*x + ((float)sx + rx) / C->nsx, *y + ((float)sy + ry) / C->nsy);
 }
@@ -2027,6 +2150,7 @@ static void run_parallel(Ctx *C, task_fn fn, int64_t n, int64_t chunk) {
  * use_prefiltering, diffvg.cpp:1525-1533) */
 static void task_weight(Ctx *C, int tid, int64_t b, int64_t e) {
   (void)tid;
+  PHASE(PH_WEIGHT);
   int spp = C->nsx * C->nsy;
   for (int64_t p = b; p < e; p++) {
     int px = (int)(p % C->w), py = (int)(p / C->w);
@@ -2044,6 +2168,7 @@ static void task_weight(Ctx *C, int tid, int64_t b, int64_t e) {
     }
     C->weight[p] = ws;
   }
+  ops_flush();
 }
 
 static v4 gather_d_color(const Ctx *C, v2 pt) {
@@ -2058,6 +2183,7 @@ static v4 gather_d_color(const Ctx *C, v2 pt) {
         float ws = C->weight[yy * C->w + xx];
         if (ws > 0) {
           const float *di = C->A->d_image + 4 * (yy * C->w + xx);
+          OPS(11, 0, 0);
           d = add4(d, scl4(fw / ws, V4(di[0], di[1], di[2], di[3])));
         }
       }
@@ -2071,6 +2197,7 @@ static void task_render(Ctx *C, int tid, int64_t b, int64_t e) {
   const Scene *S = C->S;
   Grad *G = &C->grads[tid];
   int spp = C->nsx * C->nsy;
+  PHASE(PH_RENDER);
   for (int64_t i = b; i < e; i++) {
     int idx = (int)i, x = 0, y = 0;
     v2 pt;
@@ -2106,6 +2233,7 @@ static void task_render(Ctx *C, int tid, int64_t b, int64_t e) {
               const float *di = A->d_image + 4 * (yy * C->w + xx);
               v4 dp = V4(di[0], di[1], di[2], di[3]);
               float dd = dot4(dp, color);
+              OPS(15, 0, 0);
               float d_weight = (dd * ws - fw * dd * (ws - fw)) / (ws * ws);
               G->d_filter += d_filter_weight(C->ftype, C->fr, xc - pt.x, yc - pt.y, d_weight);
             }
@@ -2124,12 +2252,14 @@ static void task_render(Ctx *C, int tid, int64_t b, int64_t e) {
       }
     }
   }
+  ops_flush();
 }
 
 /* filtered colour of each pixel from the stored sample colours (the splat
  * of render_kernel, diffvg.cpp:1218-1249, gathered per pixel) */
 static void task_resolve(Ctx *C, int tid, int64_t b, int64_t e) {
   (void)tid;
+  PHASE(PH_RESOLVE);
   int spp = C->nsx * C->nsy;
   for (int64_t p = b; p < e; p++) {
     int px = (int)(p % C->w), py = (int)(p / C->w);
@@ -2145,6 +2275,7 @@ static void task_resolve(Ctx *C, int tid, int64_t b, int64_t e) {
           v2 pt = sample_pos(C, idx, C->A->use_prefiltering, &x, &y);
           float fw = filter_weight(C->ftype, C->fr, (px + 0.5f) - pt.x, (py + 0.5f) - pt.y);
           v4 c = C->samples[idx];
+          OPS(12, 0, 0);
           acc = add4(acc, V4(fw * c.x / ws, fw * c.y / ws, fw * c.z / ws, fw * c.w / ws));
         }
       }
@@ -2152,6 +2283,7 @@ static void task_resolve(Ctx *C, int tid, int64_t b, int64_t e) {
     float *o = C->A->image + 4 * p;
     o[0] += acc.x; o[1] += acc.y; o[2] += acc.z; o[3] += acc.w;
   }
+  ops_flush();
 }
 
 /* sample_boundary_kernel + render_edge_kernel (diffvg.cpp:1325-1475) */
@@ -2159,6 +2291,7 @@ static void task_edge(Ctx *C, int tid, int64_t b, int64_t e) {
   const DvgOracleArgs *A = C->A;
   const Scene *S = C->S;
   Grad *G = &C->grads[tid];
+  PHASE(PH_EDGE);
   for (int64_t i = b; i < e; i++) {
     int idx = (int)i;
     pcg32 rng = pcg_init(idx, A->seed);
@@ -2175,6 +2308,7 @@ static void task_edge(Ctx *C, int tid, int64_t b, int64_t e) {
     v2 lpt = sample_boundary(S, g, s, t, &normal, &pdf, &bd);
     if (pdf <= 0) continue;
     const float *s2c = S->P + GI(S, g, DVG_GROUP_XFORM_OFF);
+    OPS(40, 0, 1);  /* the boundary point and normal to the canvas, the query points */
     v2 bpt = xform_pt(s2c, lpt);
     normal = xform_normal(S->c2s + 9 * g, normal);
     bpt.x /= S->W; bpt.y /= S->H;
@@ -2195,6 +2329,7 @@ static void task_edge(Ctx *C, int tid, int64_t b, int64_t e) {
     v2 sbpt = V2(bpt.x * C->w, bpt.y * C->h);
     v4 dc = gather_d_color(C, sbpt);
     float norm = (float)(S->W * S->H);
+    OPS(16, 0, 0);
     dc = V4(dc.x / norm, dc.y / norm, dc.z / norm, dc.w / norm);
     float contrib = dot4(sub4(cin, cout), dc) / pdf;
     accumulate_boundary_gradient(S, g, s, contrib, t, normal, &bd, lpt, G);
@@ -2203,6 +2338,7 @@ static void task_edge(Ctx *C, int tid, int64_t b, int64_t e) {
       atomic_addf(&A->d_translation[2 * (by * C->w + bx) + 1], normal.y * contrib);
     }
   }
+  ops_flush();
 }
 
 int dvg_oracle_render(const DvgSceneDesc *desc, const DvgOracleArgs *A, char *err, int err_len) {
