@@ -383,29 +383,30 @@ def run_e2e_cabi(args, packed, scene, dev, target, w, h, nsx, nsy, seed, n_sampl
     """The metric through the C ABI (the drop-in for the reference's
     diffvg.render) with the parameters and gradients in pinned HOST memory,
     as a native caller holds them: every step copies the parameter arena to
-    the device, renders, forms the MSE gradient and loss on the device
-    (dvg_mse_grad), runs the backward pass, and copies the gradient arena and
-    the loss back to the host; the scene handle (topology) stays resident.
-    Wall-clock time over the steps, host synchronised on both sides."""
+    the scene (dvg_scene_update_params), renders, forms the MSE gradient and
+    loss on the device (dvg_mse_grad), runs the backward pass, and copies the
+    gradient arena and the loss back to the host; the scene handle
+    (topology) stays resident.  Wall-clock time over the steps, host
+    synchronised on both sides."""
     import torch
     from diffvg_gb300 import _native
     n = packed.num_params
     h_params = packed.param_arena(torch.device('cpu')).contiguous().pin_memory()
     h_grads = torch.empty(n, dtype=torch.float32).pin_memory()
     h_loss = torch.empty(1, dtype=torch.float32).pin_memory()
-    d_arena = torch.empty(n, device=dev)
     img = torch.empty(h, w, 4, device=dev)
     d_img = torch.empty_like(img)
     d_params = torch.empty(n, device=dev)
     loss = torch.empty(1, device=dev)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
-    fa = _native.RenderArgs(w, h, nsx, nsy, seed, 0, 0, d_arena.data_ptr(), None, None, _native.DVG_FLAG_NO_SYNC)
-    ba = _native.RenderArgs(w, h, nsx, nsy, seed, 0, 0, d_arena.data_ptr(), None, None,
+    # params None: the scene's own arena, filled by update_params
+    fa = _native.RenderArgs(w, h, nsx, nsy, seed, 0, 0, None, None, None, _native.DVG_FLAG_NO_SYNC)
+    ba = _native.RenderArgs(w, h, nsx, nsy, seed, 0, 0, None, None, None,
                             _native.DVG_FLAG_NO_SYNC | _native.DVG_FLAG_REUSE_PREP)
 
     def step():
-        d_arena.copy_(h_params, non_blocking=True)
+        scene.update_params(h_params.data_ptr(), stream=sptr)
         scene.forward(fa, image_ptr=img.data_ptr(), stream=sptr)
         loss.zero_()
         _native.mse_grad(img, target, d_img, loss, stream=sptr)
@@ -426,8 +427,9 @@ def run_e2e_cabi(args, packed, scene, dev, target, w, h, nsx, nsy, seed, n_sampl
     dt = time.perf_counter() - t0
     return {'value': round(ws * n_samples * k / dt / 1e6, 3), 'unit': UNIT, 'h2d_bytes_per_step': 4 * n,
             'd2h_bytes_per_step': 4 * n + 4, 'steps': k, 'ms_per_step': round(dt / k * 1e3, 3),
-            'api': 'C ABI (dvg_render_forward, dvg_mse_grad, dvg_render_backward, dvg_scene_sync) with the '
-                   'parameter and gradient arenas in pinned host memory; scene topology resident',
+            'api': 'C ABI (dvg_scene_update_params, dvg_render_forward, dvg_mse_grad, dvg_render_backward, '
+                   'dvg_scene_sync) with the parameter and gradient arenas in pinned host memory; scene topology '
+                   'resident',
             'loss': round(float(h_loss[0]) / img.numel(), 6)}
 
 

@@ -25,7 +25,8 @@ DVG_ERR_SCENE = -5
 DVG_FLAG_NO_SYNC = 1
 DVG_FLAG_REUSE_PREP = 2
 
-EXPORTS = ('dvg_scene_create', 'dvg_scene_destroy', 'dvg_render_forward', 'dvg_render_backward',
+EXPORTS = ('dvg_scene_create', 'dvg_scene_destroy', 'dvg_scene_update_params', 'dvg_render_forward',
+           'dvg_render_backward',
            'dvg_scene_sync', 'dvg_scene_profile', 'dvg_scene_profile_read', 'dvg_mse_grad', 'dvg_adam_step',
            'dvg_batch_create', 'dvg_batch_destroy', 'dvg_batch_forward', 'dvg_batch_backward',
            'dvg_last_error', 'dvg_version')
@@ -111,6 +112,8 @@ def load(build_if_missing=True):
         lib.dvg_render_backward.restype = ctypes.c_int
         lib.dvg_scene_sync.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         lib.dvg_scene_sync.restype = ctypes.c_int
+        lib.dvg_scene_update_params.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
+        lib.dvg_scene_update_params.restype = ctypes.c_int
         lib.dvg_scene_profile.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.dvg_scene_profile.restype = ctypes.c_int
         lib.dvg_scene_profile_read.argtypes = [ctypes.c_void_p, ctypes.POINTER(KernelTime), ctypes.c_int,
@@ -186,6 +189,12 @@ class NativeScene:
             self.close()
         except Exception:
             pass
+
+    def update_params(self, params_ptr, stream=0):
+        """Copies the parameter arena (num_params floats at params_ptr, host
+        or device memory) into the scene's own arena; calls whose
+        RenderArgs.params is None then read it."""
+        check(self._lib.dvg_scene_update_params(self.handle, params_ptr, self.num_params, stream))
 
     def forward(self, args, image_ptr=None, sdf_ptr=None, stream=0):
         check(self._lib.dvg_render_forward(self.handle, ctypes.byref(args), image_ptr, sdf_ptr, stream))

@@ -92,11 +92,18 @@ struct DvgScene {
   unsigned *err = nullptr;  // [0] status bits, [1] tile-list length
   // image-sized arenas
   DevBuf weight, samples, dbg_val, dbg_flag, edge;
+  // backward: the count and list of the samples left to the deep pass
+  DevBuf deep;
+  // the scene's own parameter arena (dvg_scene_update_params), read by calls
+  // whose DvgRenderArgs.params is NULL
+  DevBuf own_params;
+  bool has_params = false;
   // fragment cache of the last image forward (no prefiltering): per-sample
   // hit keys and counts, a copy of its parameters and the stale flag the
   // backward sets when its parameters differ
   DevBuf hits;
   bool hit_live = false, hit_pf = false;
+  size_t hit_chunks_seen = 0;  // chunks the last synchronous forward asked for
   int hit_w = 0, hit_h = 0, hit_nsx = 0, hit_nsy = 0;
   uint64_t hit_seed = 0;
   unsigned *h_status = nullptr;  // pinned mirror of err[0..1]
@@ -302,6 +309,14 @@ DevScene make_dev(DvgScene *sc, const float *params) {
   return S;
 }
 
+// a's parameters: a->params, or the scene's own arena when that is NULL
+const DvgRenderArgs *with_params(DvgScene *sc, const DvgRenderArgs *a, DvgRenderArgs &tmp) {
+  if (!sc || !a || a->params || !sc->has_params) return a;
+  tmp = *a;
+  tmp.params = reinterpret_cast<const float *>(sc->own_params.ptr);
+  return &tmp;
+}
+
 int check_args(DvgScene *sc, const DvgRenderArgs *a) {
   if (!sc) return fail(DVG_ERR_INVALID, "scene is NULL");
   if (!a) return fail(DVG_ERR_INVALID, "render arguments are NULL");
@@ -309,7 +324,7 @@ int check_args(DvgScene *sc, const DvgRenderArgs *a) {
     return fail(DVG_ERR_INVALID, "image size and sample counts must be positive");
   if ((long long)a->width * a->height * a->num_samples_x * a->num_samples_y > 0x7fffffffLL)
     return fail(DVG_ERR_INVALID, "more than 2^31-1 samples per call (the reference indexes samples with int)");
-  if (!a->params) return fail(DVG_ERR_INVALID, "params is NULL");
+  if (!a->params) return fail(DVG_ERR_INVALID, "params is NULL and the scene has no arena of its own");
   if (a->background && (reinterpret_cast<uintptr_t>(a->background) & 15u))
     return fail(DVG_ERR_INVALID, "background must be 16-byte aligned");
   return DVG_OK;
@@ -370,23 +385,77 @@ int prepare(DvgScene *sc, const DevScene &S, const DvgRenderArgs *a, cudaStream_
   return DVG_OK;
 }
 
-struct HitArena { int *keys; unsigned char *cnt; float *params; unsigned *stale; };
+struct HitArena {
+  int *keys;
+  unsigned short *cnt;
+  float *params;
+  unsigned *stale;
+  int *chunks, *first, *chunk_count;
+  int chunk_cap;
+};
 
 // per sample: DVG_HIT_SLOTS fragment keys, or with prefiltering DVG_PF_SLOTS whole fragments
 size_t hit_slot_bytes(bool prefilter) { return prefilter ? DVG_PF_SLOTS * DVG_PF_BYTES : DVG_HIT_SLOTS * sizeof(int); }
 
+// chunks for the keys past the slots (no prefiltering): one per two
+// samples (8 more keys per sample on average), or what the last synchronous
+// forward asked for with a quarter to spare, up to the 15 a sample of
+// DVG_MAX_FRAGMENTS hits needs.  Samples that find none left are
+// recomputed by the backward pass.
+size_t hit_chunk_cap(DvgScene *sc, size_t n, bool prefilter) {
+  if (prefilter) return 0;
+  size_t want = std::max(n / 2 + 64, sc->hit_chunks_seen + sc->hit_chunks_seen / 4);
+  return std::min(want, (size_t)(DVG_MAX_FRAGMENTS - DVG_HIT_SLOTS) / DVG_HIT_CHUNK * n + 64);
+}
+
 size_t hit_bytes(DvgScene *sc, size_t n, bool prefilter) {
-  return carve_size({hit_slot_bytes(prefilter) * n, n, (size_t)sc->d.num_params * sizeof(float), sizeof(unsigned)});
+  size_t cap = hit_chunk_cap(sc, n, prefilter);
+  return carve_size({hit_slot_bytes(prefilter) * n, n * sizeof(unsigned short), (size_t)sc->d.num_params * sizeof(float),
+                     sizeof(unsigned), cap * (DVG_HIT_CHUNK + 1) * sizeof(int), (prefilter ? 0 : n) * sizeof(int),
+                     sizeof(int)});
 }
 
 HitArena hit_arena(DvgScene *sc, size_t n, bool prefilter) {
   char *p = reinterpret_cast<char *>(sc->hits.ptr);
+  size_t cap = hit_chunk_cap(sc, n, prefilter);
   HitArena h;
   h.keys = carve<int>(p, hit_slot_bytes(prefilter) * n / sizeof(int));
-  h.cnt = carve<unsigned char>(p, n);
+  h.cnt = carve<unsigned short>(p, n);
   h.params = carve<float>(p, sc->d.num_params);
   h.stale = carve<unsigned>(p, 1);
+  h.chunks = carve<int>(p, cap * (DVG_HIT_CHUNK + 1));
+  h.first = carve<int>(p, prefilter ? 0 : n);
+  h.chunk_count = carve<int>(p, 1);
+  h.chunk_cap = (int)cap;
+  if (prefilter) h.chunks = h.first = h.chunk_count = nullptr;
   return h;
+}
+
+// R's view of the non-prefiltered cache
+void set_hit_cache(DevRender &R, const HitArena &h) {
+  R.hit_keys = h.keys;
+  R.hit_cnt = h.cnt;
+  R.hit_chunks = h.chunks;
+  R.hit_first = h.first;
+  R.hit_chunk_count = h.chunk_count;
+  R.hit_chunk_cap = h.chunk_cap;
+}
+
+// After a synchronous forward: when its samples asked for more chunks than
+// the cache holds, the cache is enlarged now (between calls, never while a
+// graph may be capturing one) and the keys just written are dropped.
+void grow_hit_chunks(DvgScene *sc, size_t n) {
+  HitArena h = hit_arena(sc, n, false);
+  int asked = 0;
+  if (cudaMemcpy(&asked, h.chunk_count, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return;
+  if (asked <= h.chunk_cap) return;
+  sc->hit_chunks_seen = (size_t)asked;
+  sc->hit_live = false;
+  if (sc->hits.ensure(hit_bytes(sc, n, false)) != cudaSuccess) {
+    cudaGetLastError();
+    sc->hit_chunks_seen = 0;  // keep the smaller cache
+    sc->hits.ensure(hit_bytes(sc, n, false));
+  }
 }
 
 bool hit_matches(const DvgScene *sc, const DvgRenderArgs *a) {
@@ -628,6 +697,24 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   return DVG_OK;
 }
 
+int dvg_scene_update_params(DvgScene *sc, const float *params, int num_params, void *stream) {
+  dvg::clear_error();
+  if (!sc) return fail(DVG_ERR_INVALID, "scene is NULL");
+  if (!params) return fail(DVG_ERR_INVALID, "params is NULL");
+  if (num_params != sc->d.num_params)
+    return fail(DVG_ERR_INVALID, "num_params %d differs from the scene's %d", num_params, sc->d.num_params);
+  DeviceGuard guard(sc->device);
+  size_t bytes = (size_t)(num_params > 0 ? num_params : 1) * sizeof(float);
+  cudaError_t e = sc->own_params.ensure(bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "allocating the parameter arena");
+  if (num_params > 0)
+    e = cudaMemcpyAsync(sc->own_params.ptr, params, (size_t)num_params * sizeof(float), cudaMemcpyDefault,
+                        reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "copying the parameters");
+  sc->has_params = true;
+  return DVG_OK;
+}
+
 int dvg_scene_destroy(DvgScene *sc) {
   if (!sc) return DVG_OK;
   DeviceGuard guard(sc->device);
@@ -638,6 +725,8 @@ int dvg_scene_destroy(DvgScene *sc) {
   sc->samples.release();
   sc->dbg_val.release();
   sc->dbg_flag.release();
+  sc->deep.release();
+  sc->own_params.release();
   sc->edge.release();
   sc->hits.release();
   if (sc->h_status) cudaFreeHost(sc->h_status);
@@ -702,6 +791,8 @@ int dvg_scene_sync(DvgScene *sc, void *stream) {
 
 int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float *sdf, void *stream) {
   dvg::clear_error();
+  DvgRenderArgs tmp;
+  a = with_params(sc, a, tmp);
   int st = check_args(sc, a);
   if (st != DVG_OK) return st;
   if ((image == nullptr) == (sdf == nullptr)) return fail(DVG_ERR_INVALID, "exactly one of image / sdf must be set");
@@ -733,9 +824,12 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
       HitArena h{};
       if (cache) {
         h = hit_arena(sc, n, pf);
-        if (pf) R.pf_frags = h.keys;
-        else R.hit_keys = h.keys;
-        R.hit_cnt = h.cnt;
+        if (pf) {
+          R.pf_frags = h.keys;
+          R.hit_cnt = h.cnt;
+        } else {
+          set_hit_cache(R, h);
+        }
       }
       timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
       timed(sc, K_SAMPLE_FWD, s, [&] { dvg::launch_sample_fwd(S, R, samples, s); });
@@ -767,7 +861,10 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
     if (a->flags & DVG_FLAG_NO_SYNC) return DVG_OK;
     bool retry = false;
     if ((st = finish(sc, s, &retry)) != DVG_OK) return st;
-    if (!retry) return DVG_OK;
+    if (!retry) {
+      if (cache && !pf) grow_hit_chunks(sc, n);
+      return DVG_OK;
+    }
   }
   return fail(DVG_ERR_CAPACITY, "tile candidate lists kept overflowing");
 }
@@ -775,6 +872,8 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
 int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_image, const float *d_sdf,
                         float *d_params, float *d_background, float *d_translation, void *stream) {
   dvg::clear_error();
+  DvgRenderArgs tmp;
+  a = with_params(sc, a, tmp);
   int st = check_args(sc, a);
   if (st != DVG_OK) return st;
   if ((d_image == nullptr) == (d_sdf == nullptr)) return fail(DVG_ERR_INVALID, "exactly one of d_image / d_sdf must be set");
@@ -792,6 +891,7 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
   if (e == cudaSuccess && d_background) e = sc->dbg_val.ensure(n * sizeof(float4));
   if (e == cudaSuccess && d_background) e = sc->dbg_flag.ensure(n * sizeof(int));
   if (e == cudaSuccess && d_image && !a->use_prefiltering) e = sc->edge.ensure(edge_bytes(sc, n));
+  if (e == cudaSuccess && d_image) e = sc->deep.ensure((n + 1) * sizeof(int));
   if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
   for (int attempt = 0; attempt < 3; attempt++) {
     DevScene S = make_dev(sc, a->params);
@@ -802,6 +902,8 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
     if (d_image) {
       R.d_image = d_image;
       R.d_background = d_background;
+      R.deep_count = reinterpret_cast<int *>(sc->deep.ptr);
+      R.deep_list = R.deep_count + 1;
       float4 *dbg_val = reinterpret_cast<float4 *>(sc->dbg_val.ptr);
       int *dbg_flag = reinterpret_cast<int *>(sc->dbg_flag.ptr);
       if (hit_matches(sc, a)) {
@@ -810,9 +912,13 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
         e = cudaMemsetAsync(h.stale, 0, sizeof(unsigned), s);
         if (e != cudaSuccess) return cuda_fail(e, "backward launch");
         if (sc->d.num_params > 0) dvg::launch_hit_check(a->params, h.params, sc->d.num_params, h.stale, s);
-        if (pf) R.pf_frags = h.keys;
-        else R.hit_keys = h.keys;
-        R.hit_cnt = h.cnt;
+        if (pf) {
+          R.pf_frags = h.keys;
+          R.hit_cnt = h.cnt;
+        } else {
+          set_hit_cache(R, h);
+          R.hit_chunk_count = nullptr;  // read only: the backward hands out no chunks
+        }
         R.hit_stale = h.stale;
       }
       timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
@@ -861,6 +967,17 @@ struct DvgBatch {
 namespace {
 
 size_t batch_ints(int n) { return (size_t)5 * n + 4; }  // order, item starts (n + 1), edge order, pad
+
+// the batch's arguments with NULL params replaced by the scenes' own arenas
+const DvgRenderArgs *batch_args(DvgBatch *b, const DvgRenderArgs *args, std::vector<DvgRenderArgs> &own) {
+  if (!b || !args) return args;
+  own.assign(args, args + b->scenes.size());
+  for (size_t i = 0; i < own.size(); i++) {
+    DvgRenderArgs tmp;
+    own[i] = *with_params(b->scenes[i], &own[i], tmp);
+  }
+  return own.data();
+}
 
 int batch_check(DvgBatch *b, const DvgRenderArgs *args) {
   if (!b) return fail(DVG_ERR_INVALID, "batch is NULL");
@@ -954,6 +1071,8 @@ int dvg_batch_destroy(DvgBatch *b) {
 int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *images, const DvgBatchTuning *tuning,
                       void *stream) {
   dvg::clear_error();
+  std::vector<DvgRenderArgs> own;
+  args = batch_args(b, args, own);
   int st = batch_check(b, args);
   if (st != DVG_OK) return st;
   if (!images) return fail(DVG_ERR_INVALID, "images is NULL");
@@ -989,8 +1108,9 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
     if ((st = prepare(sc, bs.S, &ai, s)) != DVG_OK) return st;
     bs.R = make_render(sc, a);
     HitArena h = hit_arena(sc, ns, false);
-    bs.R.hit_keys = h.keys;
-    bs.R.hit_cnt = h.cnt;
+    set_hit_cache(bs.R, h);
+    e = cudaMemsetAsync(h.chunk_count, 0, sizeof(int), s);
+    if (e != cudaSuccess) return cuda_fail(e, "batched forward");
     bs.E = EdgeRecords{};
     bs.samples = reinterpret_cast<float4 *>(sc->samples.ptr);
     dvg::launch_weight(bs.S, bs.R, s);
@@ -1030,6 +1150,8 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
 int dvg_batch_backward(DvgBatch *b, const DvgRenderArgs *args, const float *const *d_images, float *const *d_params,
                        const DvgBatchTuning *tuning, void *stream) {
   dvg::clear_error();
+  std::vector<DvgRenderArgs> own;
+  args = batch_args(b, args, own);
   int st = batch_check(b, args);
   if (st != DVG_OK) return st;
   if (!d_images || !d_params) return fail(DVG_ERR_INVALID, "d_images / d_params is NULL");
@@ -1051,6 +1173,7 @@ int dvg_batch_backward(DvgBatch *b, const DvgRenderArgs *args, const float *cons
     size_t npx = (size_t)a->width * a->height, ns = npx * a->num_samples_x * a->num_samples_y;
     e = sc->weight.ensure(npx * sizeof(float));
     if (e == cudaSuccess) e = sc->edge.ensure(edge_bytes(sc, ns));
+    if (e == cudaSuccess) e = sc->deep.ensure((ns + 1) * sizeof(int));
     if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
     BatchScene &bs = hb[live.size()];
     bs.S = make_dev(sc, a->params);
@@ -1060,13 +1183,17 @@ int dvg_batch_backward(DvgBatch *b, const DvgRenderArgs *args, const float *cons
     bs.R = make_render(sc, a);
     bs.R.d_params = d_params[i];
     bs.R.d_image = d_images[i];
+    bs.R.deep_count = reinterpret_cast<int *>(sc->deep.ptr);
+    bs.R.deep_list = bs.R.deep_count + 1;
+    e = cudaMemsetAsync(bs.R.deep_count, 0, sizeof(int), s);
+    if (e != cudaSuccess) return cuda_fail(e, "batched backward");
     if (hit_matches(sc, a)) {
       HitArena h = hit_arena(sc, ns, false);
       e = cudaMemsetAsync(h.stale, 0, sizeof(unsigned), s);
       if (e != cudaSuccess) return cuda_fail(e, "batched backward");
       if (sc->d.num_params > 0) dvg::launch_hit_check(a->params, h.params, sc->d.num_params, h.stale, s);
-      bs.R.hit_keys = h.keys;
-      bs.R.hit_cnt = h.cnt;
+      set_hit_cache(bs.R, h);
+      bs.R.hit_chunk_count = nullptr;
       bs.R.hit_stale = h.stale;
     }
     bs.E = edge_records(sc, ns);

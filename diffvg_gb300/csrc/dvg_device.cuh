@@ -107,11 +107,22 @@ struct DevRender {
   // ([DVG_HIT_SLOTS][samples]) and their count (DVG_HIT_NONE: not cached)
   int *hit_keys = nullptr;
   void *pf_frags = nullptr;  // prefiltered: [DVG_PF_SLOTS][samples] fragments instead of keys
-  unsigned char *hit_cnt = nullptr;
+  unsigned short *hit_cnt = nullptr;
   const unsigned *hit_stale = nullptr;  // backward: nonzero when the parameters differ from the forward's
+  // keys past the slots (no prefiltering): chunks of DVG_HIT_CHUNK keys and
+  // the next chunk's index ([hit_chunk_cap][DVG_HIT_CHUNK + 1]), each
+  // sample's first chunk ([samples]) and the count of chunks handed out
+  int *hit_chunks = nullptr;
+  int *hit_first = nullptr;
+  int *hit_chunk_count = nullptr;
+  int hit_chunk_cap = 0;
+  // backward: the samples left to the deep pass ([samples]) and their count
+  int *deep_list = nullptr;
+  int *deep_count = nullptr;
 };
 #define DVG_HIT_SLOTS 16
-#define DVG_HIT_NONE 255
+#define DVG_HIT_NONE 0xffff
+#define DVG_HIT_CHUNK 16
 #define DVG_PF_SLOTS 16   // prefiltered fragments cached per sample
 #define DVG_PF_BYTES 64   // bytes per cached prefiltered fragment
 
@@ -133,9 +144,10 @@ struct EdgeRecords {
   int4 *job_a = nullptr;     // [job_cap] {query, result bit, shape, segment}; query -1: no job
   float4 *job_b = nullptr;   // [job_cap] {x, y, stroke radius, -} in shape space
   int4 *dq = nullptr;        // [2n] per query of a deferred sample: {first fragment (-1: finished in the
-                             //   first pass), fragments | edge hit << 30, fp32 results, edge-query job bits}
+                             //   first pass), state word (dq_state), fp32 results, edge-query job bits}
   unsigned *dq_res = nullptr;  // [2n] results of the query's deferred jobs
-  float4 *dq_col = nullptr;  // [2n] colour of a query finished in the first pass
+  float4 *dq_col = nullptr;  // [2n] colour of a query finished in the first pass; of a deferred
+                             //   query, the blend of the fragments its walk flushed
   int2 *frag = nullptr;      // [frag_cap] candidate fragments (key, meta) of deferred queries
   int *ds = nullptr;         // [n] sorted positions of the deferred samples
   int *counts = nullptr;     // [4] jobs, -, fragments, deferred samples reserved this call

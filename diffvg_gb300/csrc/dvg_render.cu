@@ -13,6 +13,9 @@
 #include "dvg_internal.h"
 #include "dvg_sample.cuh"
 
+#include <atomic>
+#include <mutex>
+
 // resident blocks per SM the sample kernels are compiled for (sets their
 // register budget: 65536 / (256 * blocks))
 #ifndef DVG_SAMPLE_MIN_BLOCKS
@@ -20,6 +23,13 @@
 #endif
 
 namespace dvg {
+
+// The warp queues of the 256-thread sample kernels (8 x sizeof(WarpQueue),
+// about 76 KB) are dynamic shared memory: a block may declare at most 48 KB
+// statically.
+extern __shared__ __align__(16) unsigned char dvg_smem[];
+constexpr int kQueueBytes = 8 * (int)sizeof(WarpQueue);
+__device__ __forceinline__ WarpQueue *warp_queue() { return reinterpret_cast<WarpQueue *>(dvg_smem) + (threadIdx.x >> 5); }
 
 // Kernels that accumulate into caller-visible outputs do nothing when the
 // tile lists overflowed their capacity; the host then grows the lists and
@@ -63,6 +73,12 @@ __global__ void __launch_bounds__(256) k_weight(DevRender R0, const __grid_const
   R.weight[p] = ws;
 }
 
+// sample idx's entry of R's fragment cache
+__device__ __forceinline__ HitCache hit_cache(const DevRender &R, int idx) {
+  return HitCache{R.hit_keys, R.hit_chunks, R.hit_first, R.hit_chunk_count, R.hit_cnt, R.hit_chunk_cap,
+                  R.w * R.h * R.spp, idx};
+}
+
 // Sample of thread threadIdx.x in CTA blockIdx.y of its tile: the tile's
 // 256 * spp samples are numbered pixel-major, pixels in Morton order, so the
 // lanes of a warp hold neighbouring samples and meet the same segments.
@@ -102,11 +118,10 @@ __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRende
                                      cache ? R.hit_cnt : nullptr, n, idx);
   }
   else {
-    int n = R.w * R.h * R.spp;
-    bool cache = R.hit_keys && !bins_overflowed(S);
+    bool cache = active && R.hit_keys && !bins_overflowed(S);
     if (active && R.hit_cnt && !cache) R.hit_cnt[idx] = DVG_HIT_NONE;
-    c = sample_color_fwd(S, bg, npt, nullptr, active, q, lane, cache ? R.hit_keys : nullptr,
-                         cache ? R.hit_cnt : nullptr, n, idx);
+    HitCache hc = hit_cache(R, idx);
+    c = sample_color_fwd(S, bg, npt, nullptr, active, q, lane, cache ? &hc : nullptr);
   }
   if (active) samples[idx] = c;
 }
@@ -114,9 +129,7 @@ __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRende
 template <bool PREFILTER>
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
     k_sample_fwd(const __grid_constant__ DevScene S, const __grid_constant__ DevRender R, float4 *samples) {
-  __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
-  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, samples, &wq[PREFILTER ? 0 : threadIdx.x >> 5],
-                            threadIdx.x & 31);
+  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, samples, warp_queue(), threadIdx.x & 31);
 }
 
 // filtered pixel colour from the sample colours around it
@@ -153,10 +166,43 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// The end of one sample's interior adjoint: its background adjoint and its
+// share of the filter-radius adjoint (diffvg.cpp:1250-1268).
+__device__ __forceinline__ float sample_bwd_tail(const DevRender &R, int idx, int x, int y, v2 pt, float4 color,
+                                                 float4 dbg, int assign, float4 *dbg_val, int *dbg_flag) {
+  if (R.d_background) { dbg_val[idx] = dbg; dbg_flag[idx] = assign; }
+  float dfr = 0.f;
+  for (int dy = -R.ri; dy <= R.ri; dy++)
+    for (int dx = -R.ri; dx <= R.ri; dx++) {
+      int xx = x + dx, yy = y + dy;
+      if (xx >= 0 && xx < R.w && yy >= 0 && yy < R.h && R.weight[yy * R.w + xx] > 0) {
+        float ws = R.weight[yy * R.w + xx];
+        float xc = xx + 0.5f, yc = yy + 0.5f;
+        float fw = filter_weight(R.ftype, R.fr, xc - pt.x, yc - pt.y);
+        float4 di = __ldg(reinterpret_cast<const float4 *>(R.d_image) + (yy * R.w + xx));
+        float dd = dot4(di, color);
+        float d_weight = (dd * ws - fw * dd * (ws - fw)) / (ws * ws);
+        dfr += d_filter_weight(R.ftype, R.fr, xc - pt.x, yc - pt.y, d_weight);
+      }
+    }
+  return dfr;
+}
+
+// fragment-cache count of sample idx for the backward pass (-1: none valid)
+__device__ __forceinline__ int cached_count(const DevRender &R, int idx, bool prefilter) {
+  if ((prefilter ? R.pf_frags : (void *)R.hit_keys) && R.hit_cnt && *R.hit_stale == 0u) {
+    int c = R.hit_cnt[idx];
+    if (c != DVG_HIT_NONE) return c;
+  }
+  return -1;
+}
+
 // One sample of the interior adjoint (render_kernel with d_render_image,
 // diffvg.cpp:1160-1268): thread tid of the 256-thread group cta_y of image
 // tile `tile`; R carries the filter loaded by load_filter.  A warp's lanes
-// call it together (the filter-radius adjoint is summed per warp).
+// call it together (the filter-radius adjoint is summed per warp).  A
+// sample deeper than the per-thread lists hold is appended to R.deep_list
+// and left to the deep pass (k_sample_bwd_deep).
 template <bool PREFILTER>
 __device__ __forceinline__ void sample_bwd_one(const DevScene &S, const DevRender &R, int tile, int cta_y, int tid,
                                                float4 *dbg_val, int *dbg_flag, WarpQueue *q, int lane) {
@@ -177,43 +223,20 @@ __device__ __forceinline__ void sample_bwd_one(const DevScene &S, const DevRende
   int assign = 0;
   float *d_tr = R.d_translation ? R.d_translation + 2 * (y * R.w + x) : nullptr;
   float4 *dbgp = R.d_background ? &dbg : nullptr;
+  int n = R.w * R.h * R.spp;
   float4 color;
+  bool deep = false;
   if (PREFILTER) {
-    int cached = -1;
-    if (active && R.pf_frags && R.hit_cnt && *R.hit_stale == 0u) {
-      int c = R.hit_cnt[idx];
-      if (c != DVG_HIT_NONE) cached = c;
-    }
     color = active ? sample_color_prefiltered_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params,
-                                                  static_cast<const PFrag *>(R.pf_frags), R.w * R.h * R.spp, idx,
-                                                  cached)
+                                                  static_cast<const PFrag *>(R.pf_frags), n, idx,
+                                                  cached_count(R, idx, true), deep)
                    : F4(0, 0, 0, 0);
   } else {
-    int cached = -1;
-    if (active && R.hit_cnt && *R.hit_stale == 0u) {
-      int c = R.hit_cnt[idx];
-      if (c != DVG_HIT_NONE) cached = c;
-    }
-    color = sample_color_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params, active, q, lane, R.hit_keys,
-                             R.w * R.h * R.spp, idx, cached);
+    color = sample_color_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params, active, q, lane, hit_cache(R, idx),
+                             active ? cached_count(R, idx, false) : -1, deep);
   }
-  if (active) {
-    if (R.d_background) { dbg_val[idx] = dbg; dbg_flag[idx] = assign; }
-    // d filter radius (diffvg.cpp:1250-1268)
-    for (int dy = -R.ri; dy <= R.ri; dy++)
-      for (int dx = -R.ri; dx <= R.ri; dx++) {
-        int xx = x + dx, yy = y + dy;
-        if (xx >= 0 && xx < R.w && yy >= 0 && yy < R.h && R.weight[yy * R.w + xx] > 0) {
-          float ws = R.weight[yy * R.w + xx];
-          float xc = xx + 0.5f, yc = yy + 0.5f;
-          float fw = filter_weight(R.ftype, R.fr, xc - pt.x, yc - pt.y);
-          float4 di = __ldg(reinterpret_cast<const float4 *>(R.d_image) + (yy * R.w + xx));
-          float dd = dot4(di, color);
-          float d_weight = (dd * ws - fw * dd * (ws - fw)) / (ws * ws);
-          dfr += d_filter_weight(R.ftype, R.fr, xc - pt.x, yc - pt.y, d_weight);
-        }
-      }
-  }
+  if (active && deep) R.deep_list[atomicAdd(R.deep_count, 1)] = idx;
+  else if (active) dfr = sample_bwd_tail(R, idx, x, y, pt, color, dbg, assign, dbg_val, dbg_flag);
   float tot = warp_sum(dfr);
   if (lane == 0 && tot != 0.f) atomicAdd(R.d_params + R.filter_radius_off, tot);
 }
@@ -221,10 +244,70 @@ __device__ __forceinline__ void sample_bwd_one(const DevScene &S, const DevRende
 template <bool PREFILTER>
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
     k_sample_bwd(const __grid_constant__ DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
-  __shared__ WarpQueue wq[PREFILTER ? 1 : 8];
   DevRender R = load_filter(R0, nullptr);
-  sample_bwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, dbg_val, dbg_flag,
-                            &wq[PREFILTER ? 0 : threadIdx.x >> 5], threadIdx.x & 31);
+  sample_bwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, dbg_val, dbg_flag, warp_queue(),
+                            threadIdx.x & 31);
+}
+
+// The deep pass: the interior adjoint of the samples that sample_bwd_one
+// listed in R.deep_list, 32 listed samples per warp and step.  Without
+// prefiltering the blocks are single warps, each with its per-lane hit lists
+// (DeepKeys) in shared memory; the prefiltered samples keep their runs in
+// registers and run 8 warps per block.
+template <bool PREFILTER>
+__device__ __forceinline__ void sample_bwd_deep_one(const DevScene &S, const DevRender &R, int idx, bool active,
+                                                    float4 *dbg_val, int *dbg_flag, WarpQueue *q, DeepKeys *dk,
+                                                    int lane) {
+  int x, y;
+  v2 pt = sample_pos(R, idx, PREFILTER, x, y);
+  v2 npt = V2(pt.x / R.w, pt.y / R.h);
+  float4 d_color = active ? gather_d_color(R, pt) : F4(0, 0, 0, 0);
+  const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
+  float4 dbg = F4(0, 0, 0, 0);
+  int assign = 0;
+  float *d_tr = R.d_translation ? R.d_translation + 2 * (y * R.w + x) : nullptr;
+  float4 *dbgp = R.d_background ? &dbg : nullptr;
+  float4 color;
+  if (PREFILTER) {
+    color = active ? sample_color_prefiltered_bwd_deep(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params,
+                                                       static_cast<const PFrag *>(R.pf_frags), R.w * R.h * R.spp, idx,
+                                                       cached_count(R, idx, true))
+                   : F4(0, 0, 0, 0);
+  } else {
+    color = sample_color_bwd_deep(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params, active, q, dk, lane);
+  }
+  float dfr = active ? sample_bwd_tail(R, idx, x, y, pt, color, dbg, assign, dbg_val, dbg_flag) : 0.f;
+  float tot = warp_sum(dfr);
+  if (lane == 0 && tot != 0.f) atomicAdd(R.d_params + R.filter_radius_off, tot);
+}
+
+// the listed samples of one scene, from warp `warp` of `nwarps` on
+template <bool PREFILTER>
+__device__ __forceinline__ void deep_samples(const DevScene &S, const DevRender &R, float4 *dbg_val, int *dbg_flag,
+                                             WarpQueue *q, DeepKeys *dk, int warp, int nwarps, int lane) {
+  if (bins_overflowed(S)) return;
+  int count = *(volatile const int *)R.deep_count;
+  #pragma unroll 1
+  for (int base = warp * 32; base < count; base += nwarps * 32) {
+    int j = base + lane;
+    bool act = j < count;
+    sample_bwd_deep_one<PREFILTER>(S, R, act ? R.deep_list[j] : 0, act, dbg_val, dbg_flag, q, dk, lane);
+  }
+}
+
+__global__ void __launch_bounds__(32) k_sample_bwd_deep(const __grid_constant__ DevScene S, DevRender R0,
+                                                        float4 *dbg_val, int *dbg_flag) {
+  __shared__ WarpQueue wq;
+  __shared__ DeepKeys dk;
+  DevRender R = load_filter(R0, nullptr);
+  deep_samples<false>(S, R, dbg_val, dbg_flag, &wq, &dk, blockIdx.x, gridDim.x, threadIdx.x);
+}
+
+__global__ void __launch_bounds__(256) k_sample_bwd_deep_pf(const __grid_constant__ DevScene S, DevRender R0,
+                                                            float4 *dbg_val, int *dbg_flag) {
+  DevRender R = load_filter(R0, nullptr);
+  deep_samples<true>(S, R, dbg_val, dbg_flag, nullptr, nullptr, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                     (gridDim.x * blockDim.x) >> 5, threadIdx.x & 31);
 }
 
 // Background adjoint in sample order per pixel: a sample without fragments
@@ -429,10 +512,8 @@ __device__ __forceinline__ void edge_eval_one(const DevScene &S, const DevRender
 template <bool PAIRS>
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
     k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, const __grid_constant__ EdgeRecords E) {
-  __shared__ WarpQueue wq[8];
   DevRender R = load_filter(R0, nullptr);
-  edge_eval_one<PAIRS>(S, R, E, (long long)blockIdx.x * blockDim.x + threadIdx.x, &wq[threadIdx.x >> 5],
-                       threadIdx.x & 31);
+  edge_eval_one<PAIRS>(S, R, E, (long long)blockIdx.x * blockDim.x + threadIdx.x, warp_queue(), threadIdx.x & 31);
 }
 
 // The deferred fp64 root walks of the paired boundary pass, one per thread
@@ -478,9 +559,9 @@ __device__ __forceinline__ void edge_finish_one(const DevScene &S, const DevRend
     v2 qpt = side ? add2(bpt, scl2(1e-4f, normal)) : sub2(bpt, scl2(1e-4f, normal));
     EdgeQ eq = {g, s, (rec.y >> 30) & 1};
     unsigned res = (unsigned)rec.z | E.dq_res[qid];
-    col[side] = blend_fragments(S, bg, V2(qpt.x * S.W, qpt.y * S.H), &eq,
-                                reinterpret_cast<const FragRef *>(E.frag + rec.x), rec.y & 0x3fffffff, res,
-                                (unsigned)rec.w);
+    col[side] = blend_deferred(S, bg, V2(qpt.x * S.W, qpt.y * S.H), &eq,
+                               reinterpret_cast<const FragRef *>(E.frag + rec.x), rec.y, E.dq_col[qid], res,
+                               (unsigned)rec.w);
     hit[side] = eq.hit;
   }
   edge_accumulate(S, R, g, s, bpt, normal, lpt, b.z, b.w, bd, col[0], hit[0], col[1], hit[1]);
@@ -570,9 +651,8 @@ __device__ __forceinline__ int batch_next(int *counter, int lane) {
 // tile's 256-sample group)
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
     k_sample_fwd_batch(const BatchScene *B, int nb, const int *order, const int *item_start, int spt, int *counter) {
-  __shared__ WarpQueue wq[8];
   int lane = threadIdx.x & 31;
-  WarpQueue *q = &wq[threadIdx.x >> 5];
+  WarpQueue *q = warp_queue();
   int total = __ldg(&item_start[nb]);
   #pragma unroll 1
   for (int item = batch_next(counter, lane); item < total; item = batch_next(counter, lane)) {
@@ -591,9 +671,8 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
 // interior adjoint
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
     k_sample_bwd_batch(const BatchScene *B, int nb, const int *order, const int *item_start, int spt, int *counter) {
-  __shared__ WarpQueue wq[8];
   int lane = threadIdx.x & 31;
-  WarpQueue *q = &wq[threadIdx.x >> 5];
+  WarpQueue *q = warp_queue();
   int total = __ldg(&item_start[nb]);
   #pragma unroll 1
   for (int item = batch_next(counter, lane); item < total; item = batch_next(counter, lane)) {
@@ -610,15 +689,25 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   }
 }
 
+// the deep pass of every scene of the batch (no prefiltering in batches)
+__global__ void __launch_bounds__(32) k_sample_bwd_deep_batch(const BatchScene *B, int nb, const int *order) {
+  __shared__ WarpQueue wq;
+  __shared__ DeepKeys dk;
+  for (int r = 0; r < nb; r++) {
+    const BatchScene &b = B[__ldg(&order[r])];
+    DevRender R = load_filter(b.R, nullptr);
+    deep_samples<false>(b.S, R, nullptr, nullptr, &wq, &dk, blockIdx.x, gridDim.x, threadIdx.x);
+  }
+}
+
 // paired-lane boundary pass: a scene has ceil(2 * boundary samples / 32)
 // chunks; the sample counts are known on the device only, so every block
 // forms the item list itself
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
     k_edge_eval_batch(const BatchScene *B, int nb, const int *order, int spt, int *counter) {
-  __shared__ WarpQueue wq[8];
   __shared__ int start[DVG_BATCH_MAX + 1];
   int lane = threadIdx.x & 31;
-  WarpQueue *q = &wq[threadIdx.x >> 5];
+  WarpQueue *q = warp_queue();
   if (threadIdx.x == 0) {
     int run = 0;
     for (int r = 0; r < nb; r++) {
@@ -668,13 +757,48 @@ static inline int tiles_of(const DevRender &R) {
 }
 static inline unsigned blocks_of(long long n) { return (unsigned)((n + 255) / 256); }
 
+// Opts kernel `id` (one of QueueKernel) into kQueueBytes of dynamic shared
+// memory, once per device (devices 0-63; the others every call).
+enum QueueKernel { QK_FWD, QK_BWD, QK_EDGE_PAIRS, QK_EDGE, QK_FWD_BATCH, QK_BWD_BATCH, QK_EDGE_BATCH, QK_COUNT };
+template <class K>
+static void allow_queues(K *kernel, int id) {
+  static std::atomic<unsigned long long> done[QK_COUNT];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done[id].load() & bit)) return;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kQueueBytes);
+  done[id].fetch_or(bit);
+}
+
+// SM count of the current device
+static int sm_count() {
+  static std::mutex mu;
+  static int sms[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (sms[dev] <= 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    sms[dev] = v > 0 ? v : 128;
+  }
+  return sms[dev];
+}
+
 void launch_weight(const DevScene &S, const DevRender &R, cudaStream_t st) {
   k_weight<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(R, S);
 }
 void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, cudaStream_t st) {
   dim3 grid(tiles_of(R), R.spp);
-  if (R.prefilter) k_sample_fwd<true><<<grid, 256, 0, st>>>(S, R, samples);
-  else k_sample_fwd<false><<<grid, 256, 0, st>>>(S, R, samples);
+  if (R.hit_chunk_count) cudaMemsetAsync(R.hit_chunk_count, 0, sizeof(int), st);
+  if (R.prefilter) {
+    k_sample_fwd<true><<<grid, 256, 0, st>>>(S, R, samples);
+  } else {
+    allow_queues(k_sample_fwd<false>, QK_FWD);
+    k_sample_fwd<false><<<grid, 256, kQueueBytes, st>>>(S, R, samples);
+  }
 }
 void launch_hit_check(const float *params, const float *fwd_params, int n, unsigned *stale, cudaStream_t st) {
   int blocks = (n + 255) / 256;
@@ -685,22 +809,22 @@ void launch_resolve(const DevRender &R, const float4 *samples, float *image, cud
 }
 void launch_sample_bwd(const DevScene &S, const DevRender &R, float4 *dbg_val, int *dbg_flag, cudaStream_t st) {
   dim3 grid(tiles_of(R), R.spp);
-  if (R.prefilter) k_sample_bwd<true><<<grid, 256, 0, st>>>(S, R, dbg_val, dbg_flag);
-  else k_sample_bwd<false><<<grid, 256, 0, st>>>(S, R, dbg_val, dbg_flag);
+  cudaMemsetAsync(R.deep_count, 0, sizeof(int), st);
+  if (R.prefilter) {
+    k_sample_bwd<true><<<grid, 256, 0, st>>>(S, R, dbg_val, dbg_flag);
+    k_sample_bwd_deep_pf<<<sm_count() * 2, 256, 0, st>>>(S, R, dbg_val, dbg_flag);
+  } else {
+    allow_queues(k_sample_bwd<false>, QK_BWD);
+    k_sample_bwd<false><<<grid, 256, kQueueBytes, st>>>(S, R, dbg_val, dbg_flag);
+    k_sample_bwd_deep<<<sm_count() * 4, 32, 0, st>>>(S, R, dbg_val, dbg_flag);
+  }
 }
 void launch_bg_combine(const DevScene &S, const DevRender &R, const float4 *dbg_val, const int *dbg_flag,
                        cudaStream_t st) {
   k_bg_combine<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(S, R, dbg_val, dbg_flag);
 }
 static unsigned persistent_grid(int ctas_per_sm) {
-  static int sms = 0;
-  if (sms <= 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 128;
-  }
-  return (unsigned)(sms * (ctas_per_sm > 0 ? ctas_per_sm : 1));
+  return (unsigned)(sm_count() * (ctas_per_sm > 0 ? ctas_per_sm : 1));
 }
 
 void launch_edge_setup(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
@@ -714,13 +838,15 @@ void launch_edge_setup(const DevScene &S, const DevRender &R, const EdgeRecords 
 void launch_edge_eval(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
   long long n = (long long)R.w * R.h * R.spp;
   if (S.num_groups >= 8) {  // two lanes per sample
-    k_edge_eval<true><<<blocks_of(2 * n), 256, 0, st>>>(S, R, E);
+    allow_queues(k_edge_eval<true>, QK_EDGE_PAIRS);
+    k_edge_eval<true><<<blocks_of(2 * n), 256, kQueueBytes, st>>>(S, R, E);
     if (E.job_a) {
       k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, E);
       k_edge_finish<<<persistent_grid(8), 256, 0, st>>>(S, R, E);
     }
   } else {
-    k_edge_eval<false><<<blocks_of(n), 256, 0, st>>>(S, R, E);
+    allow_queues(k_edge_eval<false>, QK_EDGE);
+    k_edge_eval<false><<<blocks_of(n), 256, kQueueBytes, st>>>(S, R, E);
   }
 }
 void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
@@ -731,17 +857,21 @@ void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cu
 void launch_batch_sample_fwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
                              int ctas_per_sm, int *counter, cudaStream_t st) {
   cudaMemsetAsync(counter, 0, sizeof(int), st);
-  k_sample_fwd_batch<<<persistent_grid(ctas_per_sm), 256, 0, st>>>(B, nb, order, item_start, spt, counter);
+  allow_queues(k_sample_fwd_batch, QK_FWD_BATCH);
+  k_sample_fwd_batch<<<persistent_grid(ctas_per_sm), 256, kQueueBytes, st>>>(B, nb, order, item_start, spt, counter);
 }
 void launch_batch_sample_bwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
                              int ctas_per_sm, int *counter, cudaStream_t st) {
   cudaMemsetAsync(counter, 0, sizeof(int), st);
-  k_sample_bwd_batch<<<persistent_grid(ctas_per_sm), 256, 0, st>>>(B, nb, order, item_start, spt, counter);
+  allow_queues(k_sample_bwd_batch, QK_BWD_BATCH);
+  k_sample_bwd_batch<<<persistent_grid(ctas_per_sm), 256, kQueueBytes, st>>>(B, nb, order, item_start, spt, counter);
+  k_sample_bwd_deep_batch<<<persistent_grid(4), 32, 0, st>>>(B, nb, order);
 }
 void launch_batch_edge(const BatchScene *B, int nb, const int *order, int spt, int ctas_per_sm, int *counter,
                        cudaStream_t st) {
   cudaMemsetAsync(counter, 0, sizeof(int), st);
-  k_edge_eval_batch<<<persistent_grid(ctas_per_sm), 256, 0, st>>>(B, nb, order, spt, counter);
+  allow_queues(k_edge_eval_batch, QK_EDGE_BATCH);
+  k_edge_eval_batch<<<persistent_grid(ctas_per_sm), 256, kQueueBytes, st>>>(B, nb, order, spt, counter);
   k_edge_jobs_batch<<<persistent_grid(8), 256, 0, st>>>(B, nb, order);
   k_edge_finish_batch<<<persistent_grid(8), 256, 0, st>>>(B, nb, order);
 }

@@ -69,21 +69,29 @@ DI float4 finish_color(float4 acc) {
 // fragments in group order with the solved results.  Every lane of the warp
 // must call the batched functions (inactive lanes pass active = false).
 #define DVG_LANE_JOBS 8
+// Candidate fragments a lane holds before the warp decides and blends them
+// (its column of the warp's fragment front, in shared memory).  A group adds
+// at most two (its stroke and its fill).
+#ifndef DVG_FRONT
+#define DVG_FRONT 16
+#endif
 struct SegJob { int shape, seg; float x, y, r; };
-struct WarpQueue {
-  SegJob job[32][DVG_LANE_JOBS];
-  unsigned result[32];
-  int offs[33];
-  unsigned char pend[32 * DVG_LANE_JOBS];  // jobs the fp32 decision left open
-  unsigned pend_lanes;                     // lanes that own one of them
-};
-static_assert(32 * DVG_LANE_JOBS <= 256, "job numbers are stored in bytes");
 
 // candidate fragment of a sample: key = 2 * group + is_stroke; meta bit 31
 // = decided hit, else bits 0-7 / 8-15 = the lane's job range whose results
 // decide it
 struct FragRef { int key, meta; };
 #define DVG_META_HIT (1 << 31)
+
+struct WarpQueue {
+  SegJob job[32][DVG_LANE_JOBS];
+  FragRef front[DVG_FRONT][32];            // lane l's candidate fragments in front[0..nf)[l]
+  unsigned result[32];
+  int offs[33];
+  unsigned char pend[32 * DVG_LANE_JOBS];  // jobs the fp32 decision left open
+  unsigned pend_lanes;                     // lanes that own one of them
+};
+static_assert(32 * DVG_LANE_JOBS <= 256, "job numbers are stored in bytes");
 
 // owner lane and slot of the warp's j-th queued job
 DI const SegJob &warp_job(const WarpQueue *q, int j, int &owner, int &idx) {
@@ -162,7 +170,7 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
 }
 
 // Pass 1 of a sample: candidate fragments in group order, undecided stroke
-// segments queued.  Returns the number of candidate fragments (capped).
+// segments queued.
 //
 // All 32 lanes of the warp call it (lanes without a sample pass active =
 // false) and walk the candidates together: the groups of the lanes' tile
@@ -175,17 +183,30 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
 // culls pass run together.  A shape that hits ends the lane's walk of that
 // shape (and of its group, outside the group of an edge query) as the
 // reference's early returns do.
-DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q, int lane, int &njobs, EdgeQ *eq,
-                         unsigned &eq_jobs, bool &overflow, bool active) {
+//
+// The lane's candidate fragments go to its column of the warp's fragment
+// front.  Before a group that could overfill a lane's front, the warp
+// decides the queued jobs, every active lane hands its front in order to
+// flush(nf, results, eq_jobs) and starts an empty one, and flushed is set
+// (the same in every lane).  Returns the
+// number of fragments left in the lane's front; overflow is set when the
+// sample has more than DVG_MAX_FRAGMENTS candidates (diffvg.cpp:542).
+template <class Flush>
+DI int collect_fragments(const DevScene &S, v2 pt, WarpQueue *q, int lane, int &njobs, EdgeQ *eq, unsigned &eq_jobs,
+                         bool &overflow, bool &flushed, bool active, Flush &flush) {
   const unsigned full = 0xffffffffu;
   int k = 0, e = 0;
   bool list = true;
   if (active) list = cand_range(S, pt, k, e);
   const int G = S.num_groups;
-  int nf = 0;
+  int nf = 0, total = 0;
   auto emit = [&](int key, int meta) {
-    if (nf < DVG_MAX_FRAGMENTS) frags[nf++] = FragRef{key, meta};
-    else overflow = true;
+    if (total < DVG_MAX_FRAGMENTS) {
+      q->front[nf++][lane] = FragRef{key, meta};
+      total++;
+    } else {
+      overflow = true;
+    }
   };
   auto fill = [&](int gg) {
     if (GI(S, gg, DVG_GROUP_FILL_KIND) != DVG_PAINT_NONE && group_inside(S, gg, pt, eq)) emit(2 * gg, DVG_META_HIT);
@@ -195,6 +216,14 @@ DI int collect_fragments(const DevScene &S, v2 pt, FragRef *frags, WarpQueue *q,
     int myg = k < e ? (list ? __ldg(&S.tile_list[k]) : k) : 0x7fffffff;
     int g = __reduce_min_sync(full, myg);
     if (g == 0x7fffffff) break;
+    if (__any_sync(full, nf > DVG_FRONT - 2)) {
+      warp_solve(S, q, lane, njobs);
+      if (active) flush(nf, q->result[lane], eq_jobs);
+      nf = 0;
+      njobs = 0;
+      eq_jobs = 0u;
+      flushed = true;
+    }
     bool act = myg == g;
     unsigned tmask = act ? (list ? __ldg(&S.tile_mask[k]) : full) : 0u;
     if (act) k++;
@@ -284,61 +313,151 @@ DI bool frag_hit(int meta, unsigned res) {
   return ((res >> lo) & mask) != 0u;
 }
 
-// Blend of a sample's decided candidate fragments (the end of sample_color,
-// diffvg.cpp:586-655): the fragments of frags[0..nf) that hit (res holds the
-// results of the sample's queued segment tests) in group order over the
-// background.  With an EdgeQuery the hit flag follows the reference's rule:
-// the last fragment that is either of the queried group (sets it) or opaque
-// (clears it) decides; without such a fragment the flag keeps what the
-// coverage tests of the queried shape set (diffvg.cpp:624-633); eq->hit holds
-// that on entry, and eq_jobs marks the queried shape's jobs.  With hit_keys
-// set, the hit fragment keys (blend order) and their count are stored for
-// the backward pass (sample idx of n).
-DI float4 blend_fragments(const DevScene &S, const float4 *bg, v2 pt, EdgeQ *eq, const FragRef *frags, int nf,
-                          unsigned res, unsigned eq_jobs, int *hit_keys = nullptr, unsigned char *hit_cnt = nullptr,
-                          int n = 0, int idx = 0) {
-  if (eq && (res & eq_jobs)) eq->hit = 1;
-  float4 acc = bg ? *bg : F4(0, 0, 0, 0);
-  int nhit = 0, ev = -1;
-  #pragma unroll 1
-  for (int i = 0; i < nf; i++) {
-    FragRef fr = frags[i];
-    if (!frag_hit(fr.meta, res)) continue;
-    int g = fr.key >> 1;
-    float4 c = (fr.key & 1)
-                   ? paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
+// paint of fragment key (2 * group + is_stroke) at pt
+DI float4 frag_color(const DevScene &S, int key, v2 pt) {
+  int g = key >> 1;
+  return (key & 1) ? paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
                                  GI(S, g, DVG_GROUP_STROKE_STOPS), pt)
                    : paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF),
                                  GI(S, g, DVG_GROUP_FILL_STOPS), pt);
-    if (eq) ev = (eq->group == g) ? 1 : (c.w >= 1.f ? 0 : ev);
-    blend(acc, c);
-    if (hit_keys && nhit < DVG_HIT_SLOTS) hit_keys[(size_t)nhit * n + idx] = fr.key;
-    nhit++;
+}
+
+// Blend of a sample's decided candidate fragments (the end of sample_color,
+// diffvg.cpp:586-655), fed in group order in one or more runs: the
+// fragments that hit (res holds the results of the run's queued segment
+// tests) over the background.  With an EdgeQuery the hit flag follows the
+// reference's rule: the last fragment that is either of the queried group
+// (sets it) or opaque (clears it) decides; without such a fragment the flag
+// keeps what the coverage tests of the queried shape set
+// (diffvg.cpp:624-633); eq->hit collects those, and eq_jobs marks the
+// queried shape's jobs of the run.  With a HitCache, the hit fragment keys
+// (blend order) are stored for the backward pass.
+struct BlendRun {
+  float4 acc;
+  int nhit;
+  int ev;     // edge-query decision of the last deciding fragment (-1: none)
+  int chunk;  // cache chunk taking the keys past the slots (-1: none yet; <= -2: none was left for
+              // the key of hit -2 - chunk)
+};
+DI BlendRun blend_start(const float4 *bg) { return BlendRun{bg ? *bg : F4(0, 0, 0, 0), 0, -1, -1}; }
+
+// Sample idx's entry of the forward pass's fragment cache: its hit keys in
+// DVG_HIT_SLOTS slots ([slot][n]), the rest in chunks of DVG_HIT_CHUNK keys
+// linked from first[idx], and its key count in cnt[idx] (DVG_HIT_NONE: not
+// cached, when the chunks ran out).
+struct HitCache {
+  int *keys;
+  int *chunks;  // [cap][DVG_HIT_CHUNK + 1]: keys, next chunk
+  int *first;
+  int *count;   // chunks handed out in this pass
+  unsigned short *cnt;
+  int cap, n, idx;
+  DI int key(int i, const int *cid) const {
+    return i < DVG_HIT_SLOTS ? __ldg(&keys[(size_t)i * n + idx])
+                             : __ldg(&chunks[(size_t)cid[(i - DVG_HIT_SLOTS) / DVG_HIT_CHUNK] * (DVG_HIT_CHUNK + 1) +
+                                             (i - DVG_HIT_SLOTS) % DVG_HIT_CHUNK]);
   }
-  if (hit_cnt) hit_cnt[idx] = nhit > DVG_HIT_SLOTS ? DVG_HIT_NONE : (unsigned char)nhit;
-  if (eq && ev >= 0) eq->hit = ev;
-  if (nhit <= 0) return bg ? *bg : F4(0, 0, 0, 0);
-  return finish_color(acc);
+};
+
+DI void cache_key(const HitCache &hc, BlendRun &st, int key) {
+  int k = st.nhit;
+  if (k < DVG_HIT_SLOTS) {
+    hc.keys[(size_t)k * hc.n + hc.idx] = key;
+    return;
+  }
+  if (st.chunk <= -2) return;
+  int j = (k - DVG_HIT_SLOTS) % DVG_HIT_CHUNK;
+  if (j == 0) {
+    int c = hc.chunks ? atomicAdd(hc.count, 1) : hc.cap;
+    if (c >= hc.cap) {
+      st.chunk = -2 - k;
+      return;
+    }
+    if (k == DVG_HIT_SLOTS) hc.first[hc.idx] = c;
+    else hc.chunks[(size_t)st.chunk * (DVG_HIT_CHUNK + 1) + DVG_HIT_CHUNK] = c;
+    st.chunk = c;
+  }
+  hc.chunks[(size_t)st.chunk * (DVG_HIT_CHUNK + 1) + j] = key;
+}
+
+template <class Get>
+DI void blend_run(const DevScene &S, BlendRun &st, v2 pt, EdgeQ *eq, const Get &get, int nf, unsigned res,
+                  unsigned eq_jobs, const HitCache *hc = nullptr) {
+  if (eq && (res & eq_jobs)) eq->hit = 1;
+  #pragma unroll 1
+  for (int i = 0; i < nf; i++) {
+    FragRef fr = get(i);
+    if (!frag_hit(fr.meta, res)) continue;
+    float4 c = frag_color(S, fr.key, pt);
+    if (eq) st.ev = (eq->group == (fr.key >> 1)) ? 1 : (c.w >= 1.f ? 0 : st.ev);
+    blend(st.acc, c);
+    if (hc) cache_key(*hc, st, fr.key);
+    st.nhit++;
+  }
+}
+
+// colour of a finished run; the cache (if set) receives the key count.  A
+// sample that found no chunk left adds the further chunks it would have
+// taken to the count, so that the count is what the pass needed.
+DI float4 blend_finish(const BlendRun &st, const float4 *bg, EdgeQ *eq, const HitCache *hc = nullptr) {
+  if (hc) {
+    if (st.chunk <= -2) {
+      int need = (st.nhit - DVG_HIT_SLOTS + DVG_HIT_CHUNK - 1) / DVG_HIT_CHUNK;
+      int asked = (-2 - st.chunk - DVG_HIT_SLOTS) / DVG_HIT_CHUNK + 1;
+      if (hc->chunks && need > asked) atomicAdd(hc->count, need - asked);
+    }
+    hc->cnt[hc->idx] = st.chunk <= -2 ? (unsigned short)DVG_HIT_NONE : (unsigned short)st.nhit;
+  }
+  if (eq && st.ev >= 0) eq->hit = st.ev;
+  if (st.nhit <= 0) return bg ? *bg : F4(0, 0, 0, 0);
+  return finish_color(st.acc);
+}
+
+// The lane's fragment front blended into st: one out-of-line copy shared by
+// the walk's flushes and the final blend, so that the paint and blend code
+// is not repeated inside every walk loop.
+static __device__ __noinline__ void blend_front(const DevScene &S, BlendRun &st, v2 pt, EdgeQ *eq, const WarpQueue *q,
+                                               int lane, int nf, unsigned res, unsigned eq_jobs,
+                                               const HitCache *hc) {
+  blend_run(S, st, pt, eq, [&](int i) { return q->front[i][lane]; }, nf, res, eq_jobs, hc);
+}
+
+// State word of a deferred boundary query: its stored fragment count (bits
+// 0-7), the blend state of its flushed fragments (bit 28: some hit; bits
+// 26-27: edge decision + 1) and its edge hit flag (bit 30).
+DI int dq_state(int nf, const BlendRun &st, int hit) {
+  return nf | ((st.ev + 1) << 26) | ((st.nhit > 0 ? 1 : 0) << 28) | (hit << 30);
+}
+
+// A deferred query's stored candidates, blended over the state its walk
+// left (acc: the blend of the fragments it flushed, state: dq_state).
+DI float4 blend_deferred(const DevScene &S, const float4 *bg, v2 pt, EdgeQ *eq, const FragRef *frags, int state,
+                         float4 acc, unsigned res, unsigned eq_jobs) {
+  BlendRun st{acc, (state >> 28) & 1, ((state >> 26) & 3) - 1, -1};
+  blend_run(S, st, pt, eq, [&](int i) { return frags[i]; }, state & 0xff, res, eq_jobs);
+  return blend_finish(st, bg, eq);
 }
 
 // Forward colour of one sample (sample_color, diffvg.cpp:525-655); see
-// blend_fragments for the EdgeQuery rule and the fragment cache.
+// blend_run for the EdgeQuery rule and the fragment cache.
 // Out of line: the boundary pass calls it twice per sample.
 static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq,
-                                                      bool active, WarpQueue *q, int lane, int *hit_keys = nullptr,
-                                                      unsigned char *hit_cnt = nullptr, int n = 0, int idx = 0) {
-  FragRef frags[DVG_MAX_FRAGMENTS];
-  int nf = 0, njobs = 0;
+                                                      bool active, WarpQueue *q, int lane,
+                                                      const HitCache *hc = nullptr) {
+  int njobs = 0;
   unsigned eq_jobs = 0;
-  bool overflow = false;
+  bool overflow = false, flushed = false;
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   if (eq) eq->hit = 0;
-  nf = collect_fragments(S, pt, frags, q, lane, njobs, eq, eq_jobs, overflow, active);
+  BlendRun st = blend_start(bg);
+  auto flush = [&](int nf, unsigned res, unsigned eqj) { blend_front(S, st, pt, eq, q, lane, nf, res, eqj, hc); };
+  int nf = collect_fragments(S, pt, q, lane, njobs, eq, eq_jobs, overflow, flushed, active, flush);
   warp_solve(S, q, lane, njobs);
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) flag_error(S, DVG_EFLAG_CAPACITY);
-  float4 c = blend_fragments(S, bg, pt, eq, frags, nf, q->result[lane], eq_jobs, hit_keys, hit_cnt, n, idx);
-  if (hit_cnt && overflow) hit_cnt[idx] = DVG_HIT_NONE;
+  flush(nf, q->result[lane], eq_jobs);
+  float4 c = blend_finish(st, bg, eq, hc);
+  if (hc && overflow) hc->cnt[hc->idx] = DVG_HIT_NONE;
   return c;
 }
 
@@ -346,20 +465,24 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
 // sample_color_fwd, except that the fp64 solves the fp32 decision leaves
 // open are handed to E's job list instead of run here, when the lists have
 // room: the lanes that own such jobs keep their candidate fragments in
-// E.frag and their query state in E.dq[qid], and report deferred = true
-// (their colour comes from k_edge_finish).  Without room the warp solves
-// its jobs in place, as sample_color_fwd does.
+// E.frag, their query state in E.dq[qid] and the blend of the fragments
+// their walk already flushed in E.dq_col[qid], and report deferred = true
+// (their colour comes from k_edge_finish).  Without room the warp solves its
+// jobs in place, as sample_color_fwd does.
 static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const EdgeRecords &E, const float4 *bg,
                                                        v2 screen_pt, EdgeQ *eq, bool active, WarpQueue *q, int lane,
                                                        int qid, bool &deferred) {
   const unsigned full = 0xffffffffu;
-  FragRef frags[DVG_MAX_FRAGMENTS];
-  int nf = 0, njobs = 0;
+  int njobs = 0;
   unsigned eq_jobs = 0;
-  bool overflow = false;
+  bool overflow = false, flushed = false;
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   eq->hit = 0;
-  nf = collect_fragments(S, pt, frags, q, lane, njobs, eq, eq_jobs, overflow, active);
+  BlendRun st = blend_start(bg);
+  auto flush = [&](int nf, unsigned res, unsigned eqj) {
+    blend_front(S, st, pt, eq, q, lane, nf, res, eqj, nullptr);
+  };
+  int nf = collect_fragments(S, pt, q, lane, njobs, eq, eq_jobs, overflow, flushed, active, flush);
   int npend = warp_decide(S, q, lane, njobs);
   deferred = false;
   if (npend > 0) {
@@ -394,9 +517,13 @@ static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const
       }
       if (mine) {
         int f0 = fbase + incl - nfr;
-        for (int i = 0; i < nf; i++) E.frag[f0 + i] = make_int2(frags[i].key, frags[i].meta);
-        E.dq[qid] = make_int4(f0, nf | (eq->hit << 30), (int)q->result[lane], (int)eq_jobs);
+        for (int i = 0; i < nf; i++) {
+          FragRef fr = q->front[i][lane];
+          E.frag[f0 + i] = make_int2(fr.key, fr.meta);
+        }
+        E.dq[qid] = make_int4(f0, dq_state(nf, st, eq->hit), (int)q->result[lane], (int)eq_jobs);
         E.dq_res[qid] = 0u;
+        E.dq_col[qid] = st.acc;
         deferred = true;
       }
       __syncwarp();
@@ -407,7 +534,106 @@ static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) flag_error(S, DVG_EFLAG_CAPACITY);
   if (deferred) return F4(0, 0, 0, 0);
-  return blend_fragments(S, bg, pt, eq, frags, nf, q->result[lane], eq_jobs);
+  flush(nf, q->result[lane], eq_jobs);
+  return blend_finish(st, bg, eq);
+}
+
+// Adjoint of the blend's output (diffvg.cpp:656-676): d_color of the
+// finished colour -> the adjoint at the last fragment; fin receives the
+// finished colour of acc.
+DI float4 blend_out_adjoint(float4 acc, float4 d_color, float4 &fin) {
+  fin = finish_color(acc);
+  float4 dc = d_color;
+  if (acc.w > 1e-6f) {
+    float fa = acc.w;
+    float nr = d_color.x / fa, ng = d_color.y / fa, nb = d_color.z / fa;
+    dc.w -= (d_color.x * fin.x + d_color.y * fin.y + d_color.z * fin.z) / fa;
+    dc.x = nr; dc.y = ng; dc.z = nb;
+  }
+  return dc;
+}
+
+// Reverse step over one fragment (diffvg.cpp:677-698): colour f blended
+// onto p; dc is the adjoint after the fragment on entry, before it on exit.
+DI void blend_step_adjoint(const DevScene &S, int key, float4 f, float4 p, float4 &dc, v2 pt, float *dp,
+                           float *d_tr) {
+  float d_pa = dc.w * (1.f - f.w);
+  float d_ai = dc.w * (1.f - p.w);
+  d_ai += dc.x * (f.x - p.x) + dc.y * (f.y - p.y) + dc.z * (f.z - p.z);
+  float d_pr = dc.x * (1 - f.w), d_pg = dc.y * (1 - f.w), d_pb = dc.z * (1 - f.w);
+  float4 dci = F4(dc.x * f.w, dc.y * f.w, dc.z * f.w, d_ai);
+  int g = key >> 1;
+  if (key & 1)
+    d_paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
+                  GI(S, g, DVG_GROUP_STROKE_STOPS), pt, dci, dp, d_tr, true);
+  else
+    d_paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS), pt,
+                  dci, dp, d_tr, true);
+  dc = F4(d_pr, d_pg, d_pb, d_pa);
+}
+
+// Reverse walk over nh hits in blend order (diffvg.cpp:656-698): key_at(i)
+// gives hit i's key, ck[r] the blend state before hit 16 r, and accs[j] the
+// state after hit 16 R + j of the last run R (the forward walk leaves them
+// there).  Each earlier run's states are rebuilt from its checkpoint with
+// the same operations in the same order, so they are the forward walk's
+// values.  dc enters as the adjoint of the final blend state and leaves as
+// that of the background.
+template <class KeyAt>
+DI void reverse_hits(const DevScene &S, v2 pt, const KeyAt &key_at, int nh, const float4 *ck, float4 *accs,
+                     float4 &dc, float *dp, float *d_tr) {
+  int last = (nh - 1) >> 4;
+  #pragma unroll 1
+  for (int r = last; r >= 0; r--) {
+    int lo = r << 4, m = min(nh - lo, 16);
+    if (r != last) {
+      float4 a = ck[r];
+      for (int j = 0; j < m; j++) {
+        blend(a, frag_color(S, key_at(lo + j), pt));
+        accs[j] = a;
+      }
+    }
+    for (int j = m - 1; j >= 0; j--) {
+      int key = key_at(lo + j);
+      blend_step_adjoint(S, key, frag_color(S, key, pt), j > 0 ? accs[j - 1] : ck[r], dc, pt, dp, d_tr);
+    }
+  }
+}
+
+// Forward walk over the hits, as reverse_hits expects it: the checkpoint
+// before every 16th hit and the states of the current run.
+struct HitWalk {
+  float4 acc;
+  int nh;
+  DI void add(const DevScene &S, int key, v2 pt, float4 *ck, float4 *accs) {
+    if ((nh & 15) == 0) ck[nh >> 4] = acc;
+    blend(acc, frag_color(S, key, pt));
+    accs[nh & 15] = acc;
+    nh++;
+  }
+};
+
+// Hits the interior adjoint takes per sample when it collects them itself
+// (keys in a small stack array).  A sample with more, and no complete cache
+// entry, goes to the deep pass (sample_color_bwd_deep).
+#define DVG_BWD_HITS 16
+
+// The hits of the lane's fragment front appended to the walk and to keys
+// (deep set past DVG_BWD_HITS); out of line, shared by the walk's flushes
+// and the final step.
+static __device__ __noinline__ void take_front(const DevScene &S, HitWalk &hw, v2 pt, const WarpQueue *q, int lane,
+                                              int nf, unsigned res, int *keys, float4 *ck, float4 *accs,
+                                              bool &deep) {
+  for (int i = 0; i < nf; i++) {
+    FragRef fr = q->front[i][lane];
+    if (!frag_hit(fr.meta, res)) continue;
+    if (hw.nh >= DVG_BWD_HITS) {
+      deep = true;
+      continue;
+    }
+    keys[hw.nh] = fr.key;
+    hw.add(S, fr.key, pt, ck, accs);
+  }
 }
 
 // Adjoint of sample_color (diffvg.cpp:525-707 with d_color != nullptr).
@@ -415,79 +641,103 @@ static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const
 // *assign = 1 when the sample has no fragment (the reference then
 // overwrites the pixel's background gradient with d_color).
 // cached >= 0: the forward pass's hit fragments of this sample (cached of
-// them, keys in hit_keys) stand in for collecting and deciding them again.
+// them, keys in hc) stand in for collecting and deciding them again.
+// deep is set (and nothing accumulated) when the sample has no cache entry
+// and more than DVG_BWD_HITS hits.
 DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color, float4 *d_bg,
                            int *assign, float *d_tr, float *dp, bool active, WarpQueue *q, int lane,
-                           const int *hit_keys, int n, int idx, int cached) {
-  FragRef frags[DVG_MAX_FRAGMENTS];
-  int nf = 0, njobs = 0;
+                           const HitCache &hc, int cached, bool &deep) {
+  int njobs = 0;
   unsigned eq_jobs = 0;
-  bool overflow = false;
+  bool overflow = false, flushed = false;
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
-  nf = collect_fragments(S, pt, frags, q, lane, njobs, nullptr, eq_jobs, overflow, active && cached < 0);
-  if (active && cached >= 0) {
-    nf = cached;
-    for (int i = 0; i < nf; i++) frags[i] = FragRef{__ldg(&hit_keys[(size_t)i * n + idx]), DVG_META_HIT};
-  }
+  float4 ck[DVG_MAX_FRAGMENTS / 16], accs[16];
+  int keys[DVG_BWD_HITS];
+  float4 first = bg ? *bg : F4(0, 0, 0, 0);
+  HitWalk hw{first, 0};
+  deep = false;
+  auto flush = [&](int nf, unsigned res, unsigned) { take_front(S, hw, pt, q, lane, nf, res, keys, ck, accs, deep); };
+  int nf = collect_fragments(S, pt, q, lane, njobs, nullptr, eq_jobs, overflow, flushed, active && cached < 0, flush);
   warp_solve(S, q, lane, njobs);
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) {
     flag_error(S, DVG_EFLAG_CAPACITY);
     return F4(0, 0, 0, 0);
   }
-  unsigned res = q->result[lane];
-  float4 cols[DVG_MAX_FRAGMENTS];
-  float4 accs[DVG_MAX_FRAGMENTS];
-  int keys[DVG_MAX_FRAGMENTS];
-  float4 first = bg ? *bg : F4(0, 0, 0, 0);
-  float4 acc = first;
-  int nh = 0;
-  #pragma unroll 1
-  for (int i = 0; i < nf; i++) {
-    if (!frag_hit(frags[i].meta, res)) continue;
-    int g = frags[i].key >> 1;
-    float4 c = (frags[i].key & 1)
-                   ? paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
-                                 GI(S, g, DVG_GROUP_STROKE_STOPS), pt)
-                   : paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF),
-                                 GI(S, g, DVG_GROUP_FILL_STOPS), pt);
-    blend(acc, c);
-    cols[nh] = c; accs[nh] = acc; keys[nh] = frags[i].key;
-    nh++;
+  int cid[(DVG_MAX_FRAGMENTS - DVG_HIT_SLOTS) / DVG_HIT_CHUNK];
+  if (cached >= 0) {
+    for (int i = 0; i < cached; i++) {
+      if (i >= DVG_HIT_SLOTS && (i - DVG_HIT_SLOTS) % DVG_HIT_CHUNK == 0) {
+        int r = (i - DVG_HIT_SLOTS) / DVG_HIT_CHUNK;
+        cid[r] = r == 0 ? __ldg(&hc.first[hc.idx])
+                        : __ldg(&hc.chunks[(size_t)cid[r - 1] * (DVG_HIT_CHUNK + 1) + DVG_HIT_CHUNK]);
+      }
+      hw.add(S, hc.key(i, cid), pt, ck, accs);
+    }
+  } else {
+    flush(nf, q->result[lane], eq_jobs);
   }
-  if (nh <= 0) {
+  if (deep) return F4(0, 0, 0, 0);
+  if (hw.nh <= 0) {
     if (bg) {
       if (d_bg) { *d_bg = d_color; *assign = 1; }
       return *bg;
     }
     return F4(0, 0, 0, 0);
   }
-  float4 fin = finish_color(acc);
-  float dcr = d_color.x, dcg = d_color.y, dcb = d_color.z, dca = d_color.w;
-  if (acc.w > 1e-6f) {
-    float fa = acc.w;
-    float nr = d_color.x / fa, ng = d_color.y / fa, nb = d_color.z / fa;
-    dca -= (d_color.x * fin.x + d_color.y * fin.y + d_color.z * fin.z) / fa;
-    dcr = nr; dcg = ng; dcb = nb;
+  float4 fin;
+  float4 dc = blend_out_adjoint(hw.acc, d_color, fin);
+  reverse_hits(S, pt, [&](int i) { return cached >= 0 ? hc.key(i, cid) : keys[i]; }, hw.nh, ck, accs, dc, dp, d_tr);
+  if (d_bg) { d_bg->x += dc.x; d_bg->y += dc.y; d_bg->z += dc.z; d_bg->w += dc.w; }
+  return fin;
+}
+
+// The deep pass's per-warp hit lists: up to DVG_MAX_FRAGMENTS keys per lane
+// (key i of lane l in key[i][l]).
+struct DeepKeys {
+  int key[DVG_MAX_FRAGMENTS][32];
+};
+
+// sample_color_bwd for a sample of any depth without a cache entry (the
+// deep pass, one warp per block): the hit keys go to the lane's column of
+// the warp's DeepKeys.
+DI float4 sample_color_bwd_deep(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color, float4 *d_bg,
+                                int *assign, float *d_tr, float *dp, bool active, WarpQueue *q, DeepKeys *dk,
+                                int lane) {
+  int njobs = 0;
+  unsigned eq_jobs = 0;
+  bool overflow = false, flushed = false;
+  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+  float4 ck[DVG_MAX_FRAGMENTS / 16], accs[16];
+  float4 first = bg ? *bg : F4(0, 0, 0, 0);
+  HitWalk hw{first, 0};
+  auto flush = [&](int nf, unsigned res, unsigned) {
+    for (int i = 0; i < nf; i++) {
+      FragRef fr = q->front[i][lane];
+      if (!frag_hit(fr.meta, res)) continue;
+      dk->key[hw.nh][lane] = fr.key;
+      hw.add(S, fr.key, pt, ck, accs);
+    }
+  };
+  int nf = collect_fragments(S, pt, q, lane, njobs, nullptr, eq_jobs, overflow, flushed, active, flush);
+  warp_solve(S, q, lane, njobs);
+  if (!active) return F4(0, 0, 0, 0);
+  if (overflow) {
+    flag_error(S, DVG_EFLAG_CAPACITY);
+    return F4(0, 0, 0, 0);
   }
-  for (int i = nh - 1; i >= 0; i--) {
-    float4 f = cols[i];
-    float4 p = i > 0 ? accs[i - 1] : first;
-    float d_pa = dca * (1.f - f.w);
-    float d_ai = dca * (1.f - p.w);
-    d_ai += dcr * (f.x - p.x) + dcg * (f.y - p.y) + dcb * (f.z - p.z);
-    float d_pr = dcr * (1 - f.w), d_pg = dcg * (1 - f.w), d_pb = dcb * (1 - f.w);
-    float4 dci = F4(dcr * f.w, dcg * f.w, dcb * f.w, d_ai);
-    int g = keys[i] >> 1;
-    if (keys[i] & 1)
-      d_paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
-                    GI(S, g, DVG_GROUP_STROKE_STOPS), pt, dci, dp, d_tr, true);
-    else
-      d_paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS),
-                    pt, dci, dp, d_tr, true);
-    dcr = d_pr; dcg = d_pg; dcb = d_pb; dca = d_pa;
+  flush(nf, q->result[lane], eq_jobs);
+  if (hw.nh <= 0) {
+    if (bg) {
+      if (d_bg) { *d_bg = d_color; *assign = 1; }
+      return *bg;
+    }
+    return F4(0, 0, 0, 0);
   }
-  if (d_bg) { d_bg->x += dcr; d_bg->y += dcg; d_bg->z += dcb; d_bg->w += dca; }
+  float4 fin;
+  float4 dc = blend_out_adjoint(hw.acc, d_color, fin);
+  reverse_hits(S, pt, [&](int i) { return dk->key[i][lane]; }, hw.nh, ck, accs, dc, dp, d_tr);
+  if (d_bg) { d_bg->x += dc.x; d_bg->y += dc.y; d_bg->z += dc.z; d_bg->w += dc.w; }
   return fin;
 }
 
@@ -606,7 +856,7 @@ DI int prefilter_group(const DevScene &S, int g, v2 pt, PFrag *out) {
 // count; the backward pass then resumes the walk after the last stored group.
 #define DVG_PF_PARTIAL 0x80
 DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, PFrag *cache = nullptr,
-                                       unsigned char *cache_cnt = nullptr, int n = 0, int idx = 0) {
+                                       unsigned short *cache_cnt = nullptr, int n = 0, int idx = 0) {
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   int b, e;
   bool list = cand_range(S, pt, b, e);
@@ -630,56 +880,147 @@ DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 s
     for (int j = 0; j < m; j++) blend(acc, fr[j].c);
     nf += m;
   }
-  if (cache_cnt) cache_cnt[idx] = (unsigned char)(caching ? nc : (nc | DVG_PF_PARTIAL));
+  if (cache_cnt) cache_cnt[idx] = (unsigned short)(caching ? nc : (nc | DVG_PF_PARTIAL));
   if (nf > DVG_MAX_PREFILTER_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
   if (nf <= 0) return bg ? *bg : F4(0, 0, 0, 0);
   return finish_color(acc);
 }
 
-// Adjoint of sample_color_prefiltered (diffvg.cpp:960-1113)
-// cached >= 0: the forward pass's cache entry of this sample (a count, with
-// DVG_PF_PARTIAL when only the leading groups' fragments were stored); the
-// stored fragments stand in for computing them again.
+// Reverse step over one prefiltered fragment f blended onto p
+// (diffvg.cpp:1040-1105); dc is the adjoint after the fragment on entry,
+// before it on exit.
+DI void pf_step_adjoint(const DevScene &S, const PFrag &f, float4 p, float4 &dc, v2 pt, float *dp, float *d_tr) {
+  float d_pa = dc.w * (1.f - f.c.w);
+  float d_ai = dc.w * (1.f - p.w);
+  d_ai += dc.x * (f.c.x - p.x) + dc.y * (f.c.y - p.y) + dc.z * (f.c.z - p.z);
+  float d_pr = dc.x * (1 - f.c.w), d_pg = dc.y * (1 - f.c.w), d_pb = dc.z * (1 - f.c.w);
+  float dcir = dc.x * f.c.w, dcig = dc.y * f.c.w, dcib = dc.z * f.c.w;
+  int g = f.group_stroke >> 1;
+  if (f.group_stroke & 1) {
+    float d = f.distance;
+    float sw = stroke_width(S, f.shape);
+    float apw = fabsf(d) + sw, amw = fabsf(d) - sw;
+    float w = smoothstep(apw) - smoothstep(amw);
+    if (w != 0) {
+      float d_w = w > 0 ? (f.c.w / w) * d_ai : 0.f;
+      d_ai *= w;
+      d_paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
+                    GI(S, g, DVG_GROUP_STROKE_STOPS), pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr, true);
+      float d_apw = d_smoothstep(apw, d_w);
+      float d_amw = -d_smoothstep(amw, d_w);
+      float d_d = d_apw + d_amw;
+      if (d < 0) d_d = -d_d;
+      float d_sw = d_apw - d_amw;
+      if (fabsf(d_d) > 1e-10f) d_group_distance(S, g, f.shape, pt, f.closest, f.info, d_d, dp, d_tr);
+      gadd(dp, SI(S, f.shape, DVG_SHAPE_STROKE_WIDTH_OFF), d_sw);
+    }
+  } else {
+    float d = f.distance;
+    float w = smoothstep(d);
+    if (w != 0) {
+      float d_w = w > 0 ? (f.c.w / w) * d_ai : 0.f;
+      d_ai *= w;
+      d_paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS),
+                    pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr, true);
+      float d_d = d_smoothstep(d, d_w);
+      if (d < 0) d_d = -d_d;
+      if (fabsf(d_d) > 1e-10f && f.within) d_group_distance(S, g, f.shape, pt, f.closest, f.info, d_d, dp, d_tr);
+    }
+  }
+  dc = F4(d_pr, d_pg, d_pb, d_pa);
+}
+
+// Adjoint of sample_color_prefiltered (diffvg.cpp:960-1113) for a sample
+// whose fragments are all in the forward pass's cache (cached = their
+// count, at most DVG_PF_SLOTS): the reverse walk reads them in place.  Any
+// other sample (no valid cache entry, or only its leading groups cached)
+// sets deep and is left to sample_color_prefiltered_bwd_deep.
 DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color,
-                                       float4 *d_bg, int *assign, float *d_tr, float *dp,
-                                       const PFrag *cache = nullptr, int n = 0, int idx = 0, int cached = -1) {
+                                       float4 *d_bg, int *assign, float *d_tr, float *dp, const PFrag *cache, int n,
+                                       int idx, int cached, bool &deep) {
+  deep = cached < 0 || (cached & DVG_PF_PARTIAL) != 0;
+  if (deep) return F4(0, 0, 0, 0);
+  v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
+  int nc = min(cached, DVG_PF_SLOTS);
+  float4 accs[DVG_PF_SLOTS];
+  float4 first = bg ? *bg : F4(0, 0, 0, 0);
+  float4 acc = first;
+  for (int j = 0; j < nc; j++) {
+    blend(acc, cache[(size_t)j * n + idx].c);
+    accs[j] = acc;
+  }
+  if (nc <= 0) {
+    if (bg) {
+      if (d_bg) { *d_bg = d_color; *assign = 1; }
+      return *bg;
+    }
+    return F4(0, 0, 0, 0);
+  }
+  float4 fin;
+  float4 dc = blend_out_adjoint(acc, d_color, fin);
+  for (int i = nc - 1; i >= 0; i--)
+    pf_step_adjoint(S, cache[(size_t)i * n + idx], i > 0 ? accs[i - 1] : first, dc, pt, dp, d_tr);
+  if (d_bg) { d_bg->x += dc.x; d_bg->y += dc.y; d_bg->z += dc.z; d_bg->w += dc.w; }
+  return fin;
+}
+
+// The prefiltered adjoint for any sample (the deep pass).  The sample's
+// fragments come in units: the cached fragments one by one, then the
+// candidate groups after the last cached group (0 to 2 fragments each,
+// from prefilter_group).  The forward walk keeps, at the start of every run
+// of at least DVG_PF_RUN fragments, the blend state and the unit; the
+// reverse walk regenerates each run from its checkpoint (prefilter_group is
+// deterministic, so the fragments and blend states are the ones of the
+// forward walk) and steps back through it.
+#define DVG_PF_RUN 4
+#define DVG_PF_RUNS (DVG_MAX_PREFILTER_FRAGMENTS / DVG_PF_RUN)
+DI float4 sample_color_prefiltered_bwd_deep(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color,
+                                            float4 *d_bg, int *assign, float *d_tr, float *dp, const PFrag *cache,
+                                            int n, int idx, int cached) {
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   int b, e;
   bool list = cand_range(S, pt, b, e);
-  PFrag frags[DVG_MAX_PREFILTER_FRAGMENTS];
-  float4 accs[DVG_MAX_PREFILTER_FRAGMENTS];
+  const int G = S.num_groups;
+  int nc = 0, g_done = -1;
+  if (cached >= 0) {
+    nc = min(cached & ~DVG_PF_PARTIAL, DVG_PF_SLOTS);
+    if (cached & DVG_PF_PARTIAL) g_done = nc > 0 ? cache[(size_t)(nc - 1) * n + idx].group_stroke >> 1 : -1;
+    else e = b;  // every fragment is cached: no group is walked
+  }
+  const int nunits = nc + (e - b);
+  // the fragments of unit u (cached entry u, or candidate b + u - nc)
+  auto unit = [&](int u, PFrag *out) -> int {
+    if (u < nc) {
+      out[0] = cache[(size_t)u * n + idx];
+      return 1;
+    }
+    int k = b + (u - nc);
+    int g = list ? __ldg(&S.tile_list[k]) : k;
+    if (g <= g_done) return 0;  // candidates run in ascending group id
+    if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) return 0;
+    return prefilter_group(S, g, pt, out);
+  };
+  float4 ck_acc[DVG_PF_RUNS];
+  int ck_unit[DVG_PF_RUNS];
+  int nruns = 0, in_run = DVG_PF_RUN, nf = 0;
   float4 first = bg ? *bg : F4(0, 0, 0, 0);
   float4 acc = first;
-  int nf = 0;
   bool overflow = false;
-  int G = S.num_groups;
-  // cached fragments stay in the cache (read again by the reverse walk);
-  // only the recomputed ones go to the per-thread list
-  int g_done = -1;  // groups up to this id are in the cache
-  int nc = 0;
-  if (cached >= 0) {
-    nc = cached & ~DVG_PF_PARTIAL;
-    for (int j = 0; j < nc; j++) {
-      blend(acc, cache[(size_t)j * n + idx].c);
-      accs[j] = acc;
+  PFrag fr[2];
+  #pragma unroll 1
+  for (int u = 0; u < nunits; u++) {
+    int m = unit(u, fr);
+    if (m == 0) continue;
+    if (nf + m > DVG_MAX_PREFILTER_FRAGMENTS) { overflow = true; break; }
+    if (in_run >= DVG_PF_RUN) {  // a run holds DVG_PF_RUN or DVG_PF_RUN + 1 fragments
+      ck_acc[nruns] = acc;
+      ck_unit[nruns] = u;
+      nruns++;
+      in_run = 0;
     }
-    nf = nc;
-    if (cached & DVG_PF_PARTIAL) g_done = nc > 0 ? cache[(size_t)(nc - 1) * n + idx].group_stroke >> 1 : -1;
-    else e = b;  // the walk below has nothing left to do
-  }
-  for (int k = b; k < e; k++) {
-    int g = list ? __ldg(&S.tile_list[k]) : k;
-    if (g <= g_done) continue;  // candidates run in ascending group id
-    if (G > 1 && !box_in_r(S.g_canvas_box[g], pt, S.g_max_radius[g])) continue;
-    PFrag fr[2];
-    int n = prefilter_group(S, g, pt, fr);
-    if (nf + n > DVG_MAX_PREFILTER_FRAGMENTS) { overflow = true; break; }
-    for (int j = 0; j < n; j++) {
-      blend(acc, fr[j].c);
-      frags[nf] = fr[j];
-      accs[nf] = acc;
-      nf++;
-    }
+    for (int j = 0; j < m; j++) blend(acc, fr[j].c);
+    nf += m;
+    in_run += m;
   }
   if (overflow) {
     flag_error(S, DVG_EFLAG_CAPACITY);
@@ -692,57 +1033,28 @@ DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 s
     }
     return F4(0, 0, 0, 0);
   }
-  float4 fin = finish_color(acc);
-  float dcr = d_color.x, dcg = d_color.y, dcb = d_color.z, dca = d_color.w;
-  if (acc.w > 1e-6f) {
-    float fa = acc.w;
-    float nr = d_color.x / fa, ng = d_color.y / fa, nb = d_color.z / fa;
-    dca -= (d_color.x * fin.x + d_color.y * fin.y + d_color.z * fin.z) / fa;
-    dcr = nr; dcg = ng; dcb = nb;
-  }
-  for (int i = nf - 1; i >= 0; i--) {
-    const PFrag f = i < nc ? cache[(size_t)i * n + idx] : frags[i];
-    float4 p = i > 0 ? accs[i - 1] : first;
-    float d_pa = dca * (1.f - f.c.w);
-    float d_ai = dca * (1.f - p.w);
-    d_ai += dcr * (f.c.x - p.x) + dcg * (f.c.y - p.y) + dcb * (f.c.z - p.z);
-    float d_pr = dcr * (1 - f.c.w), d_pg = dcg * (1 - f.c.w), d_pb = dcb * (1 - f.c.w);
-    float dcir = dcr * f.c.w, dcig = dcg * f.c.w, dcib = dcb * f.c.w;
-    int g = f.group_stroke >> 1;
-    if (f.group_stroke & 1) {
-      float d = f.distance;
-      float sw = stroke_width(S, f.shape);
-      float apw = fabsf(d) + sw, amw = fabsf(d) - sw;
-      float w = smoothstep(apw) - smoothstep(amw);
-      if (w != 0) {
-        float d_w = w > 0 ? (f.c.w / w) * d_ai : 0.f;
-        d_ai *= w;
-        d_paint_color(S, GI(S, g, DVG_GROUP_STROKE_KIND), GI(S, g, DVG_GROUP_STROKE_OFF),
-                      GI(S, g, DVG_GROUP_STROKE_STOPS), pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr, true);
-        float d_apw = d_smoothstep(apw, d_w);
-        float d_amw = -d_smoothstep(amw, d_w);
-        float d_d = d_apw + d_amw;
-        if (d < 0) d_d = -d_d;
-        float d_sw = d_apw - d_amw;
-        if (fabsf(d_d) > 1e-10f) d_group_distance(S, g, f.shape, pt, f.closest, f.info, d_d, dp, d_tr);
-        gadd(dp, SI(S, f.shape, DVG_SHAPE_STROKE_WIDTH_OFF), d_sw);
-      }
-    } else {
-      float d = f.distance;
-      float w = smoothstep(d);
-      if (w != 0) {
-        float d_w = w > 0 ? (f.c.w / w) * d_ai : 0.f;
-        d_ai *= w;
-        d_paint_color(S, GI(S, g, DVG_GROUP_FILL_KIND), GI(S, g, DVG_GROUP_FILL_OFF), GI(S, g, DVG_GROUP_FILL_STOPS),
-                      pt, F4(dcir, dcig, dcib, d_ai), dp, d_tr, true);
-        float d_d = d_smoothstep(d, d_w);
-        if (d < 0) d_d = -d_d;
-        if (fabsf(d_d) > 1e-10f && f.within) d_group_distance(S, g, f.shape, pt, f.closest, f.info, d_d, dp, d_tr);
+  float4 fin;
+  float4 dc = blend_out_adjoint(acc, d_color, fin);
+  PFrag run[DVG_PF_RUN + 1];
+  float4 run_acc[DVG_PF_RUN + 1];
+  #pragma unroll 1
+  for (int r = nruns - 1; r >= 0; r--) {
+    int u1 = r + 1 < nruns ? ck_unit[r + 1] : nunits;
+    float4 a = ck_acc[r];
+    int m = 0;
+    #pragma unroll 1
+    for (int u = ck_unit[r]; u < u1 && m < DVG_PF_RUN + 1; u++) {
+      int k = unit(u, fr);
+      for (int j = 0; j < k && m < DVG_PF_RUN + 1; j++) {
+        run[m] = fr[j];
+        blend(a, fr[j].c);
+        run_acc[m] = a;
+        m++;
       }
     }
-    dcr = d_pr; dcg = d_pg; dcb = d_pb; dca = d_pa;
+    for (int i = m - 1; i >= 0; i--) pf_step_adjoint(S, run[i], i > 0 ? run_acc[i - 1] : ck_acc[r], dc, pt, dp, d_tr);
   }
-  if (d_bg) { d_bg->x += dcr; d_bg->y += dcg; d_bg->z += dcb; d_bg->w += dca; }
+  if (d_bg) { d_bg->x += dc.x; d_bg->y += dc.y; d_bg->z += dc.z; d_bg->w += dc.w; }
   return fin;
 }
 

@@ -131,8 +131,16 @@ def _eval_positions(packed, device):
     return ev.to(device=device, dtype=torch.float32).reshape(-1, 2).contiguous()
 
 
-class RenderFunction:
-    """The PyTorch interface of the renderer (render_pytorch.py:18-868)."""
+class RenderFunction(torch.autograd.Function):
+    """The PyTorch interface of the renderer (render_pytorch.py:18-868): a
+    torch.autograd.Function with the reference's static forward(ctx, width,
+    height, num_samples_x, num_samples_y, seed, background_image, *args) and
+    backward(ctx, grad_img) (one gradient or None per input, in input
+    order), so code that calls them directly works.  ``apply`` does not go
+    through them: it hands autograd only the argument tensors that require
+    grad (_RenderCore), so a step over thousands of shapes pays no
+    per-argument bookkeeping for the others; the values are the same.
+    """
 
     @staticmethod
     def serialize_scene(canvas_width, canvas_height, shapes, shape_groups,
@@ -210,6 +218,28 @@ class RenderFunction:
         return _RenderCore.apply(call, background_image, *[packed.tensors[k] for k in grad_slots])
 
     @staticmethod
+    def forward(ctx, width, height, num_samples_x, num_samples_y, seed, background_image, *args):
+        """The render (render_pytorch.py:174-428); keeps on ctx what
+        backward needs, for every differentiable argument."""
+        packed = pack_scene_cached(args)
+        slots = [k for k, sl in enumerate(packed.slots) if sl.differentiable]
+        call = _RenderCall((width, height, num_samples_x, num_samples_y, seed), packed, slots)
+        ctx.num_args = len(args)
+        return _render_forward(ctx, call, background_image)
+
+    @staticmethod
+    def backward(ctx, grad_img):
+        """Gradients of <grad_img, render> for every input of forward, in
+        input order (render_pytorch.py:668-868): None for the image size,
+        sample counts, seed and the non-differentiable arguments; the
+        background gradient when a background was given."""
+        d_bg, grads = _render_backward(ctx, grad_img)
+        out = [None] * ctx.num_args
+        for k, g in zip(ctx.grad_slots, grads):
+            out[ctx.packed.slots[k].arg_index] = g
+        return (None, None, None, None, None, d_bg) + tuple(out)
+
+    @staticmethod
     def render_grad(grad_img, width, height, num_samples_x, num_samples_y, seed, background_image, *args):
         """Gradient of <grad_img, render> with respect to a screen-space
         translation of every pixel's content: a [H, W, 2] image
@@ -250,104 +280,118 @@ class _RenderCall:
         self.dims, self.packed, self.grad_slots = dims, packed, grad_slots
 
 
+def _render_forward(ctx, call, background_image):
+    """Forward render of `call` into a new output tensor; keeps on ctx what
+    _render_backward needs (render_pytorch.py:186-428)."""
+    width, height, num_samples_x, num_samples_y, seed = call.dims
+    packed = call.packed
+    device = _render_device()
+    scene = _native_scene(packed, device)
+    arena = packed.param_arena(device).contiguous()
+    ev = _eval_positions(packed, device)
+    if packed.output_type == OutputType.color:
+        assert ev is None, 'eval_positions apply to the sdf output only'
+        out = torch.empty(height, width, 4, device=device)
+    else:
+        out = torch.empty((height, width, 1) if ev is None else (ev.shape[0], 1), device=device)
+    bg = _background(background_image, out.shape[0], out.shape[1], device)
+    if not bool(torch.isfinite(arena).all()):
+        raise ValueError('scene parameters contain a non-finite value')
+    token = next(_token)
+    rargs = _render_args(packed, width, height, num_samples_x, num_samples_y, seed, arena, bg, ev)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    with torch.cuda.device(device):
+        if packed.output_type == OutputType.color:
+            scene.forward(rargs, image_ptr=out.data_ptr(), stream=stream)
+        else:
+            scene.forward(rargs, sdf_ptr=out.data_ptr(), stream=stream)
+    scene.last_token = token
+    ctx.packed = packed
+    ctx.scene = scene
+    ctx.arena = arena
+    ctx.token = token
+    ctx.background_image = bg
+    ctx.bg_requested = background_image is not None
+    ctx.eval_positions = ev
+    ctx.dims = call.dims
+    ctx.device = device
+    ctx.grad_slots = call.grad_slots
+    return out
+
+
+def _render_backward(ctx, grad_img):
+    """The backward render of a _render_forward (render_pytorch.py:668-868):
+    (background gradient or None, gradients of the call's slots in
+    ctx.grad_slots order, each on its input's device)."""
+    packed, scene, device = ctx.packed, ctx.scene, ctx.device
+    width, height, nsx, nsy, seed = ctx.dims
+    grad = grad_img.to(device=device, dtype=torch.float32).contiguous()
+    d_arena = torch.zeros(max(packed.num_params, 1), device=device)
+    bg = ctx.background_image
+    d_bg = torch.zeros_like(bg) if bg is not None else None
+    reuse = _native.DVG_FLAG_REUSE_PREP if scene.last_token == ctx.token else 0
+    stream = torch.cuda.current_stream(device).cuda_stream
+
+    def launch(flags):
+        rargs = _render_args(packed, width, height, nsx, nsy, seed, ctx.arena, bg, ctx.eval_positions, flags)
+        with torch.cuda.device(device):
+            if packed.output_type == OutputType.color:
+                scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
+                               d_background_ptr=None if d_bg is None else d_bg.data_ptr(), stream=stream)
+            else:
+                scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(), stream=stream)
+
+    # the kernels run while the host lays out the gradient views; the
+    # status is checked once the gradient has been read back
+    launch(reuse | _native.DVG_FLAG_NO_SYNC)
+    scene.last_token = ctx.token
+    slots, tensors = packed.slots, packed.tensors
+    ks = ctx.grad_slots
+    dst_of = [tensors[k].device for k in ks]
+    bufs = {device: d_arena}
+    for dst in set(dst_of):
+        if dst != device:
+            bufs[dst] = torch.empty(d_arena.shape, dtype=torch.float32, device=dst)
+    sizes = [sl.numel for sl in slots]
+    parts = {dst: torch.split(bufs[dst][:sum(sizes)], sizes) for dst in set(dst_of)}
+    grads = []
+    for k, dst in zip(ks, dst_of):
+        slot, t = slots[k], tensors[k]
+        g = parts[dst][k]
+        if len(slot.shape) != 1:
+            g = g.view(slot.shape)
+        if t.dtype != g.dtype:
+            g = g.to(t.dtype)
+        grads.append(g)
+    for dst, b in bufs.items():
+        if dst != device:
+            b.copy_(d_arena)  # waits for the kernels
+    try:
+        scene.sync(stream)
+    except _native.SceneCapacityError as e:
+        if 'grown' not in str(e):
+            raise
+        # the tile lists outgrew their capacity and were grown: the
+        # gradient is computed again, synchronously
+        d_arena.zero_()
+        if d_bg is not None:
+            d_bg.zero_()
+        launch(0)
+        for dst, b in bufs.items():
+            if dst != device:
+                b.copy_(d_arena)
+    return (d_bg if ctx.bg_requested else None), grads
+
+
 class _RenderCore(torch.autograd.Function):
-    """Forward and backward of one render (render_pytorch.py:186-428 and
-    668-868): inputs are the tensors that require grad, in slot order."""
+    """Forward and backward of one render: inputs are the tensors that
+    require grad, in slot order."""
 
     @staticmethod
     def forward(ctx, call, background_image, *grad_tensors):
-        width, height, num_samples_x, num_samples_y, seed = call.dims
-        packed = call.packed
-        device = _render_device()
-        scene = _native_scene(packed, device)
-        arena = packed.param_arena(device).contiguous()
-        ev = _eval_positions(packed, device)
-        if packed.output_type == OutputType.color:
-            assert ev is None, 'eval_positions apply to the sdf output only'
-            out = torch.empty(height, width, 4, device=device)
-        else:
-            out = torch.empty((height, width, 1) if ev is None else (ev.shape[0], 1), device=device)
-        bg = _background(background_image, out.shape[0], out.shape[1], device)
-        if not bool(torch.isfinite(arena).all()):
-            raise ValueError('scene parameters contain a non-finite value')
-        token = next(_token)
-        rargs = _render_args(packed, width, height, num_samples_x, num_samples_y, seed, arena, bg, ev)
-        stream = torch.cuda.current_stream(device).cuda_stream
-        with torch.cuda.device(device):
-            if packed.output_type == OutputType.color:
-                scene.forward(rargs, image_ptr=out.data_ptr(), stream=stream)
-            else:
-                scene.forward(rargs, sdf_ptr=out.data_ptr(), stream=stream)
-        scene.last_token = token
-        ctx.packed = packed
-        ctx.scene = scene
-        ctx.arena = arena
-        ctx.token = token
-        ctx.background_image = bg
-        ctx.bg_requested = background_image is not None
-        ctx.eval_positions = ev
-        ctx.dims = call.dims
-        ctx.device = device
-        ctx.grad_slots = call.grad_slots
-        return out
+        return _render_forward(ctx, call, background_image)
 
     @staticmethod
     def backward(ctx, grad_img):
-        packed, scene, device = ctx.packed, ctx.scene, ctx.device
-        width, height, nsx, nsy, seed = ctx.dims
-        grad = grad_img.to(device=device, dtype=torch.float32).contiguous()
-        d_arena = torch.zeros(max(packed.num_params, 1), device=device)
-        bg = ctx.background_image
-        d_bg = torch.zeros_like(bg) if bg is not None else None
-        reuse = _native.DVG_FLAG_REUSE_PREP if scene.last_token == ctx.token else 0
-        stream = torch.cuda.current_stream(device).cuda_stream
-
-        def launch(flags):
-            rargs = _render_args(packed, width, height, nsx, nsy, seed, ctx.arena, bg, ctx.eval_positions, flags)
-            with torch.cuda.device(device):
-                if packed.output_type == OutputType.color:
-                    scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
-                                   d_background_ptr=None if d_bg is None else d_bg.data_ptr(), stream=stream)
-                else:
-                    scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(), stream=stream)
-
-        # the kernels run while the host lays out the gradient views; the
-        # status is checked once the gradient has been read back
-        launch(reuse | _native.DVG_FLAG_NO_SYNC)
-        scene.last_token = ctx.token
-        slots, tensors = packed.slots, packed.tensors
-        ks = ctx.grad_slots
-        dst_of = [tensors[k].device for k in ks]
-        bufs = {device: d_arena}
-        for dst in set(dst_of):
-            if dst != device:
-                bufs[dst] = torch.empty(d_arena.shape, dtype=torch.float32, device=dst)
-        sizes = [sl.numel for sl in slots]
-        parts = {dst: torch.split(bufs[dst][:sum(sizes)], sizes) for dst in set(dst_of)}
-        grads = []
-        for k, dst in zip(ks, dst_of):
-            slot, t = slots[k], tensors[k]
-            g = parts[dst][k]
-            if len(slot.shape) != 1:
-                g = g.view(slot.shape)
-            if t.dtype != g.dtype:
-                g = g.to(t.dtype)
-            grads.append(g)
-        for dst, b in bufs.items():
-            if dst != device:
-                b.copy_(d_arena)  # waits for the kernels
-        try:
-            scene.sync(stream)
-        except _native.SceneCapacityError as e:
-            if 'grown' not in str(e):
-                raise
-            # the tile lists outgrew their capacity and were grown: the
-            # gradient is computed again, synchronously
-            d_arena.zero_()
-            if d_bg is not None:
-                d_bg.zero_()
-            launch(0)
-            for dst, b in bufs.items():
-                if dst != device:
-                    b.copy_(d_arena)
-        return (None, d_bg if ctx.bg_requested else None) + tuple(grads)
+        d_bg, grads = _render_backward(ctx, grad_img)
+        return (None, d_bg) + tuple(grads)

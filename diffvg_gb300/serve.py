@@ -29,7 +29,57 @@ import torch
 
 from . import _native
 from .batch import DEFAULT_TRAINABLE
+from .diffvg import ShapeType
 from .packing import pack_scene
+
+
+def mean_depth(packed):
+    """Mean number of groups whose canvas bounding box (shapes' boxes
+    grown by their stroke widths, through the group transform) covers a
+    canvas point: an upper-leaning estimate of the hits per sample."""
+    import numpy as np
+    W, H = float(packed.canvas_width), float(packed.canvas_height)
+    if packed.num_groups == 0 or W <= 0 or H <= 0:
+        return 0.0
+    P = np.concatenate([t.detach().reshape(-1).float().cpu().numpy() for t in packed.tensors]) \
+        if packed.tensors else np.zeros(1, np.float32)
+    si, gi, gs = packed.shape_info, packed.group_info, packed.group_shapes
+    boxes = np.zeros((packed.num_shapes, 4))
+    for s in range(packed.num_shapes):
+        kind, po, npts = int(si[s, 0]), int(si[s, 1]), int(si[s, 2])
+        if kind == ShapeType.circle:
+            r, c = abs(P[po]), P[po + 1:po + 3]
+            b = [c[0] - r, c[1] - r, c[0] + r, c[1] + r]
+        elif kind == ShapeType.ellipse:
+            r, c = np.abs(P[po:po + 2]), P[po + 2:po + 4]
+            b = [c[0] - r[0], c[1] - r[1], c[0] + r[0], c[1] + r[1]]
+        elif kind == ShapeType.path and npts > 0:
+            pts = P[po:po + 2 * npts].reshape(-1, 2)
+            b = [*pts.min(0), *pts.max(0)]
+        elif kind == ShapeType.rect:
+            b = [*np.minimum(P[po:po + 2], P[po + 2:po + 4]), *np.maximum(P[po:po + 2], P[po + 2:po + 4])]
+        else:
+            b = [0.0, 0.0, 0.0, 0.0]
+        sw = abs(P[int(si[s, 7])]) if int(si[s, 7]) >= 0 else 0.0
+        boxes[s] = [b[0] - sw, b[1] - sw, b[2] + sw, b[3] + sw]
+    area = 0.0
+    for g in range(packed.num_groups):
+        n, off = int(gi[g, 0]), int(gi[g, 1])
+        if n == 0:
+            continue
+        bb = boxes[gs[off:off + n]]
+        lo, hi = bb[:, :2].min(0), bb[:, 2:].max(0)
+        m = P[int(gi[g, 9]):int(gi[g, 9]) + 9].reshape(3, 3)
+        corners = np.array([[lo[0], lo[1], 1], [hi[0], lo[1], 1], [lo[0], hi[1], 1], [hi[0], hi[1], 1]]) @ m.T
+        w = corners[:, 2:3]
+        if np.any(np.abs(w) < 1e-12):
+            area += W * H
+            continue
+        c = corners[:, :2] / w
+        x0, y0 = max(c[:, 0].min(), 0.0), max(c[:, 1].min(), 0.0)
+        x1, y1 = min(c[:, 0].max(), W), min(c[:, 1].max(), H)
+        area += max(x1 - x0, 0.0) * max(y1 - y0, 0.0)
+    return area / (W * H)
 
 
 def estimate_device_bytes(packed, width, height, spp):
@@ -41,8 +91,16 @@ def estimate_device_bytes(packed, width, height, spp):
     params = 4 * P * 6                              # params, grads, m, v, lr scale, spare
     images = 16 * npx * 3 + 4 * npx                 # image, adjoint, target; weight image
     # forward sample colours; fragment cache per sample: 16 hit keys, or with
-    # prefiltering 16 fragments of 64 B, and a count
-    samples = 16 * n + ((16 * 64 if packed.use_prefiltering else 16 * 4) + 1) * n
+    # prefiltering 16 fragments of 64 B, and a count; without prefiltering
+    # also each sample's first chunk for keys past 16, and the chunks (68 B
+    # each): one per two samples, or as many as twice the mean box depth
+    # asks for (up to 15 per sample); the backward's deep-pass list
+    if packed.use_prefiltering:
+        cache = 16 * 64
+    else:
+        chunks = min(15.0, max(0.5, (2.0 * mean_depth(packed) - 16.0) / 16.0))
+        cache = 16 * 4 + 4 + int(68 * chunks + 0.5)
+    samples = 16 * n + (cache + 2 + 4) * n
     edges = 68 * n                                  # boundary-sample records and ordering
     if ng >= 8:  # deferred fp64 walks: jobs, per-query state and colours, fragments, deferred samples
         edges += 32 * n + 2 * (16 + 4 + 16) * n + 4 * 8 * n + 4 * n

@@ -121,7 +121,8 @@ typedef struct DvgRenderArgs {
   uint64_t seed;
   int32_t use_prefiltering;
   int32_t num_eval_positions;    /* >0: SDF at eval_positions instead of an image */
-  const float *params;           /* [num_params] parameter arena             */
+  const float *params;           /* [num_params] parameter arena; NULL: the
+                                    scene's own (dvg_scene_update_params)     */
   const float *background;       /* [height*width*4] or NULL                 */
   const float *eval_positions;   /* [num_eval_positions*2] or NULL           */
   int32_t flags;                 /* DVG_FLAG_* bits                          */
@@ -148,6 +149,17 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene);
 
 /* Frees a scene and its arenas.  Replaces Scene::~Scene (scene.cpp:1000-1023). */
 int dvg_scene_destroy(DvgScene *scene);
+
+/* Copies num_params floats (the parameter arena layout; host or device
+ * memory) into the scene's own parameter arena, ordered on `stream`.  A
+ * render call (single or batched) whose DvgRenderArgs.params is NULL reads
+ * that arena.  num_params must equal the scene's.  The first call allocates
+ * the arena (make it before capturing a graph); later calls only copy.
+ * Replaces the reference's parameter upload: Scene's constructor copies the
+ * shapes' and groups' parameters into the one buffer it owns
+ * (scene.cpp:919-998), rebuilt on every RenderFunction call
+ * (render_pytorch.py:366-368). */
+int dvg_scene_update_params(DvgScene *scene, const float *params, int32_t num_params, void *stream);
 
 /* Forward render.  Exactly one of image / sdf is non-NULL:
  *   image: [height*width*4] colour output (OutputType.color)

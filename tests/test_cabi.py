@@ -84,3 +84,41 @@ def test_noalloc_host_checks_without_gpu():
     # errors found on the device could not be latched anywhere
     st, msg = _noalloc_call(packed, flags=_native.DVG_FLAG_NO_SYNC)
     assert st == _native.DVG_ERR_INVALID and b'NO_SYNC' in msg
+
+
+def test_update_params_host_checks_without_gpu():
+    lib = _native.load()
+    x = (ctypes.c_float * 4)()
+    assert lib.dvg_scene_update_params(None, x, 4, None) == _native.DVG_ERR_INVALID
+    assert b'scene' in lib.dvg_last_error()
+
+
+@pytest.mark.gpu
+def test_scene_owned_parameters_render_like_passed_ones():
+    """dvg_scene_update_params from host memory, then calls with params NULL:
+    the image and the gradient equal those of calls that pass the arena."""
+    import torch
+    import diffvg_gb300 as dvg
+    from diffvg_gb300 import workloads
+    from diffvg_gb300.packing import pack_scene
+    dev = torch.device('cuda', 0)
+    w, h, shapes, groups = workloads.stroke_scene(dvg, seed=4, num_paths=48, canvas=96)
+    packed = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups))
+    scene = _native.NativeScene(packed)
+    arena = packed.param_arena(dev).contiguous()
+    host = arena.cpu().contiguous()
+    s = torch.cuda.current_stream(dev).cuda_stream
+    img_a, img_b = torch.empty(h, w, 4, device=dev), torch.empty(h, w, 4, device=dev)
+    scene.forward(_native.RenderArgs(w, h, 2, 2, 3, 0, 0, arena.data_ptr(), None, None, 0), image_ptr=img_a.data_ptr(),
+                  stream=s)
+    scene.update_params(host.data_ptr(), stream=s)
+    scene.forward(_native.RenderArgs(w, h, 2, 2, 3, 0, 0, None, None, None, 0), image_ptr=img_b.data_ptr(), stream=s)
+    assert torch.equal(img_a, img_b)
+    d_img = torch.rand(h, w, 4, device=dev)
+    ga, gb = torch.zeros(scene.num_params, device=dev), torch.zeros(scene.num_params, device=dev)
+    scene.backward(_native.RenderArgs(w, h, 2, 2, 3, 0, 0, arena.data_ptr(), None, None, 0),
+                   d_image_ptr=d_img.data_ptr(), d_params_ptr=ga.data_ptr(), stream=s)
+    scene.backward(_native.RenderArgs(w, h, 2, 2, 3, 0, 0, None, None, None, 0), d_image_ptr=d_img.data_ptr(),
+                   d_params_ptr=gb.data_ptr(), stream=s)
+    assert float((ga - gb).norm()) <= 1e-5 * max(float(ga.norm()), 1e-12)
+    scene.close()

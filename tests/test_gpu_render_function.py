@@ -43,3 +43,36 @@ def test_no_grad_render_needs_no_autograd():
     with torch.no_grad():
         img = dvg.RenderFunction.apply(w, h, 2, 2, 3, None, *dvg.RenderFunction.serialize_scene(w, h, shapes, groups))
     assert img.shape == (h, w, 4) and not img.requires_grad
+
+
+def test_direct_forward_backward_like_the_reference():
+    """RenderFunction is a torch.autograd.Function whose static forward /
+    backward can be called directly (render_pytorch.py:174, 668): backward
+    returns one entry per forward input, the gradients at the differentiable
+    arguments' positions equal what autograd delivers through apply, None
+    elsewhere."""
+    import diffvg_gb300 as dvg
+    assert issubclass(dvg.RenderFunction, torch.autograd.Function)
+    shapes, groups = _grads({'points', 'width', 'color'})
+    w, h, shapes2, groups2 = _scene(dvg)
+    args = dvg.RenderFunction.serialize_scene(w, h, shapes2, groups2)
+
+    class Ctx:
+        pass
+    ctx = Ctx()
+    img = dvg.RenderFunction.forward(ctx, w, h, 2, 2, 3, None, *args)
+    grad = torch.linspace(0, 1, img.numel(), device=img.device).reshape(img.shape)
+    out = dvg.RenderFunction.backward(ctx, grad)
+    assert len(out) == 6 + len(args)
+    assert all(x is None for x in out[:6])
+    for pos, a in enumerate(args):
+        g = out[6 + pos]
+        if g is not None:
+            assert isinstance(a, torch.Tensor) and g.shape == a.shape
+    idx = {id(a): 6 + k for k, a in enumerate(args)}
+    for a, b in zip(shapes, shapes2):
+        torch.testing.assert_close(out[idx[id(b.points)]], a.points.grad, rtol=1e-4, atol=1e-5)
+        torch.testing.assert_close(out[idx[id(b.stroke_width)]], a.stroke_width.grad, rtol=1e-4, atol=1e-5)
+    for a, b in zip(groups, groups2):
+        torch.testing.assert_close(out[idx[id(b.stroke_color)]], a.stroke_color.grad, rtol=1e-4, atol=1e-5)
+        assert out[idx[id(b.shape_ids)]] is None
