@@ -24,6 +24,9 @@ Lines printed (one JSON line, rank 0):
          tensors in host memory; it adds PyTorch's per-tensor work for the
          scene's 6144 leaf tensors (serialisation, autograd bookkeeping,
          one gradient view per tensor).
+  e2e_render_function_fused  the drop-in with the scene's parameters
+         fused into one device tensor (fuse_parameters): autograd tracks
+         one tensor; the loss is read back every step.
   roofline  the dominant kernel's algorithmic bytes per launch over its
          CUDA-event time, against the measured HBM copy bandwidth.
   cpu_baseline  the CPU oracle port (oracle/, all host cores) on one full
@@ -354,15 +357,17 @@ def run_ours(args):
                              for k, (cnt, ms) in kernels.items() if k != 'prepare'}
 
     # ---------------- end to end with host buffers ----------------
-    e2e = e2e_rf = None
+    e2e = e2e_rf = e2e_fused = None
     if not getattr(args, 'no_e2e', False):
         e2e = run_e2e_cabi(args, packed, scene, dev, target, w, h, nsx, nsy, seed, n_samples, ws)
         e2e_rf = run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samples, ws)
+        e2e_fused = run_e2e_fused(args, dvg, dev, target, n_samples, ws)
 
     out = {'metric': METRIC, 'value': round(value, 3), 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
            'warmup': max(args.warmup, 3), 'ms_per_step': round(total_ms / args.steps, 4), 'higher_is_better': True,
            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 (fp64 root solves)', 'data': 'synthetic',
-           'config': _workload_config(), 'e2e': e2e, 'e2e_render_function': e2e_rf, 'roofline': roofline,
+           'config': _workload_config(), 'e2e': e2e, 'e2e_render_function': e2e_rf,
+           'e2e_render_function_fused': e2e_fused, 'roofline': roofline,
            'clocks': clock_info,
            'gpu_launches': gpu_launches, 'fwd_ms': round(fwd_ms, 4), 'bwd_ms': round(bwd_ms, 4),
            'kernels_ms_per_launch': {k: round(v[1] / v[0], 4) for k, v in kernels.items()},
@@ -471,6 +476,41 @@ def run_e2e(args, dvg, dev, shapes, groups, target, w, h, nsx, nsy, seed, n_samp
     return {'value': round(ws * n_samples * k / dt / 1e6, 3), 'unit': UNIT, 'h2d_bytes_per_step': h2d,
             'd2h_bytes_per_step': d2h, 'steps': k, 'ms_per_step': round(dt / k * 1e3, 3),
             'api': 'RenderFunction.serialize_scene + apply + MSE + backward, scene tensors in host memory'}
+
+
+def run_e2e_fused(args, dvg, dev, target, n_samples, ws):
+    """Same metric through RenderFunction with the scene's parameters fused
+    into one device tensor (fuse_parameters): serialize_scene, apply, the
+    loss in torch, backward (autograd tracks the one tensor) and the loss
+    read back to the host each step.  A fresh copy of the workload's scene,
+    so the other legs' objects are untouched."""
+    import torch
+    (w, h, shapes, groups), _ = build_workload(dvg, dev)
+    nsx, nsy = WORKLOAD['spp']
+    seed = WORKLOAD['seed']
+    arena, filt = dvg.fuse_parameters(w, h, shapes, groups)
+
+    def step():
+        arena.grad = None
+        sargs = dvg.RenderFunction.serialize_scene(w, h, shapes, groups, filter=filt)
+        img = dvg.RenderFunction.apply(w, h, nsx, nsy, seed, None, *sargs)
+        loss = ((img - target) ** 2).mean()
+        loss.backward()
+        return float(loss.item())
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(dev)
+    k = max(1, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        step()
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t0
+    return {'value': round(ws * n_samples * k / dt / 1e6, 3), 'unit': UNIT, 'h2d_bytes_per_step': 0,
+            'd2h_bytes_per_step': 4, 'steps': k, 'ms_per_step': round(dt / k * 1e3, 3),
+            'api': 'fuse_parameters + RenderFunction.serialize_scene + apply + MSE + backward, parameters in '
+                   'one device tensor (one autograd leaf), loss read back each step'}
 
 
 CONFIG_NAMES = ('circle_256_2x2', 'fill_prefiltered_1024_1x1', 'blob_1024_2x2', 'blob_long_1024_2x2',

@@ -104,6 +104,7 @@ struct DvgScene {
   DevBuf hits;
   bool hit_live = false, hit_pf = false;
   size_t hit_chunks_seen = 0;  // chunks the last synchronous forward asked for
+  bool hit_pf_seen = false;    // ... with prefiltering
   int hit_w = 0, hit_h = 0, hit_nsx = 0, hit_nsy = 0;
   uint64_t hit_seed = 0;
   unsigned *h_status = nullptr;  // pinned mirror of err[0..1]
@@ -386,33 +387,38 @@ int prepare(DvgScene *sc, const DevScene &S, const DvgRenderArgs *a, cudaStream_
 }
 
 struct HitArena {
-  int *keys;
+  int *keys;  // [DVG_HIT_SLOTS][n] keys, or with prefiltering [DVG_PF_SLOTS][n] fragments
   unsigned short *cnt;
   float *params;
   unsigned *stale;
-  int *chunks, *first, *chunk_count;
+  int *chunks;       // keys and next chunk, or with prefiltering the next chunk only
+  void *pf_chunks;   // prefiltering: [chunk_cap][DVG_PF_CHUNK] fragments
+  int *first, *chunk_count;
   int chunk_cap;
 };
 
 // per sample: DVG_HIT_SLOTS fragment keys, or with prefiltering DVG_PF_SLOTS whole fragments
 size_t hit_slot_bytes(bool prefilter) { return prefilter ? DVG_PF_SLOTS * DVG_PF_BYTES : DVG_HIT_SLOTS * sizeof(int); }
 
-// chunks for the keys past the slots (no prefiltering): one per two
-// samples (8 more keys per sample on average), or what the last synchronous
-// forward asked for with a quarter to spare, up to the 15 a sample of
-// DVG_MAX_FRAGMENTS hits needs.  Samples that find none left are
-// recomputed by the backward pass.
+// Chunks for the entries past the slots: without prefiltering one per two
+// samples (8 more keys per sample on average), with prefiltering one per
+// sixteen samples, or what the last synchronous forward asked for with a
+// quarter to spare, up to what a sample of the reference's maximum
+// fragment count needs.  Samples that find none left are recomputed by the
+// backward pass.
 size_t hit_chunk_cap(DvgScene *sc, size_t n, bool prefilter) {
-  if (prefilter) return 0;
-  size_t want = std::max(n / 2 + 64, sc->hit_chunks_seen + sc->hit_chunks_seen / 4);
-  return std::min(want, (size_t)(DVG_MAX_FRAGMENTS - DVG_HIT_SLOTS) / DVG_HIT_CHUNK * n + 64);
+  size_t base = prefilter ? n / 16 + 64 : n / 2 + 64;
+  size_t most = prefilter ? (size_t)(DVG_MAX_PREFILTER_FRAGMENTS - DVG_PF_SLOTS) / DVG_PF_CHUNK * n + 64
+                          : (size_t)(DVG_MAX_FRAGMENTS - DVG_HIT_SLOTS) / DVG_HIT_CHUNK * n + 64;
+  size_t seen = sc->hit_pf_seen == prefilter ? sc->hit_chunks_seen : 0;
+  return std::min(std::max(base, seen + seen / 4), most);
 }
 
 size_t hit_bytes(DvgScene *sc, size_t n, bool prefilter) {
   size_t cap = hit_chunk_cap(sc, n, prefilter);
   return carve_size({hit_slot_bytes(prefilter) * n, n * sizeof(unsigned short), (size_t)sc->d.num_params * sizeof(float),
-                     sizeof(unsigned), cap * (DVG_HIT_CHUNK + 1) * sizeof(int), (prefilter ? 0 : n) * sizeof(int),
-                     sizeof(int)});
+                     sizeof(unsigned), cap * (prefilter ? sizeof(int) : (DVG_HIT_CHUNK + 1) * sizeof(int)),
+                     prefilter ? cap * DVG_PF_CHUNK * DVG_PF_BYTES : 0, n * sizeof(int), sizeof(int)});
 }
 
 HitArena hit_arena(DvgScene *sc, size_t n, bool prefilter) {
@@ -423,17 +429,23 @@ HitArena hit_arena(DvgScene *sc, size_t n, bool prefilter) {
   h.cnt = carve<unsigned short>(p, n);
   h.params = carve<float>(p, sc->d.num_params);
   h.stale = carve<unsigned>(p, 1);
-  h.chunks = carve<int>(p, cap * (DVG_HIT_CHUNK + 1));
-  h.first = carve<int>(p, prefilter ? 0 : n);
+  h.chunks = carve<int>(p, cap * (prefilter ? 1 : DVG_HIT_CHUNK + 1));
+  h.pf_chunks = carve<char>(p, prefilter ? cap * DVG_PF_CHUNK * DVG_PF_BYTES : 0);
+  if (!prefilter) h.pf_chunks = nullptr;
+  h.first = carve<int>(p, n);
   h.chunk_count = carve<int>(p, 1);
   h.chunk_cap = (int)cap;
-  if (prefilter) h.chunks = h.first = h.chunk_count = nullptr;
   return h;
 }
 
-// R's view of the non-prefiltered cache
-void set_hit_cache(DevRender &R, const HitArena &h) {
-  R.hit_keys = h.keys;
+// R's view of the cache
+void set_hit_cache(DevRender &R, const HitArena &h, bool prefilter) {
+  if (prefilter) {
+    R.pf_frags = h.keys;
+    R.pf_chunk_frags = h.pf_chunks;
+  } else {
+    R.hit_keys = h.keys;
+  }
   R.hit_cnt = h.cnt;
   R.hit_chunks = h.chunks;
   R.hit_first = h.first;
@@ -444,17 +456,18 @@ void set_hit_cache(DevRender &R, const HitArena &h) {
 // After a synchronous forward: when its samples asked for more chunks than
 // the cache holds, the cache is enlarged now (between calls, never while a
 // graph may be capturing one) and the keys just written are dropped.
-void grow_hit_chunks(DvgScene *sc, size_t n) {
-  HitArena h = hit_arena(sc, n, false);
+void grow_hit_chunks(DvgScene *sc, size_t n, bool pf) {
+  HitArena h = hit_arena(sc, n, pf);
   int asked = 0;
   if (cudaMemcpy(&asked, h.chunk_count, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return;
   if (asked <= h.chunk_cap) return;
   sc->hit_chunks_seen = (size_t)asked;
+  sc->hit_pf_seen = pf;
   sc->hit_live = false;
-  if (sc->hits.ensure(hit_bytes(sc, n, false)) != cudaSuccess) {
+  if (sc->hits.ensure(hit_bytes(sc, n, pf)) != cudaSuccess) {
     cudaGetLastError();
     sc->hit_chunks_seen = 0;  // keep the smaller cache
-    sc->hits.ensure(hit_bytes(sc, n, false));
+    sc->hits.ensure(hit_bytes(sc, n, pf));
   }
 }
 
@@ -824,12 +837,7 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
       HitArena h{};
       if (cache) {
         h = hit_arena(sc, n, pf);
-        if (pf) {
-          R.pf_frags = h.keys;
-          R.hit_cnt = h.cnt;
-        } else {
-          set_hit_cache(R, h);
-        }
+        set_hit_cache(R, h, pf);
       }
       timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
       timed(sc, K_SAMPLE_FWD, s, [&] { dvg::launch_sample_fwd(S, R, samples, s); });
@@ -862,7 +870,7 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
     bool retry = false;
     if ((st = finish(sc, s, &retry)) != DVG_OK) return st;
     if (!retry) {
-      if (cache && !pf) grow_hit_chunks(sc, n);
+      if (cache) grow_hit_chunks(sc, n, pf);
       return DVG_OK;
     }
   }
@@ -912,13 +920,8 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
         e = cudaMemsetAsync(h.stale, 0, sizeof(unsigned), s);
         if (e != cudaSuccess) return cuda_fail(e, "backward launch");
         if (sc->d.num_params > 0) dvg::launch_hit_check(a->params, h.params, sc->d.num_params, h.stale, s);
-        if (pf) {
-          R.pf_frags = h.keys;
-          R.hit_cnt = h.cnt;
-        } else {
-          set_hit_cache(R, h);
-          R.hit_chunk_count = nullptr;  // read only: the backward hands out no chunks
-        }
+        set_hit_cache(R, h, pf);
+        R.hit_chunk_count = nullptr;  // read only: the backward hands out no chunks
         R.hit_stale = h.stale;
       }
       timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
@@ -1108,7 +1111,7 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
     if ((st = prepare(sc, bs.S, &ai, s)) != DVG_OK) return st;
     bs.R = make_render(sc, a);
     HitArena h = hit_arena(sc, ns, false);
-    set_hit_cache(bs.R, h);
+    set_hit_cache(bs.R, h, false);
     e = cudaMemsetAsync(h.chunk_count, 0, sizeof(int), s);
     if (e != cudaSuccess) return cuda_fail(e, "batched forward");
     bs.E = EdgeRecords{};
@@ -1192,7 +1195,7 @@ int dvg_batch_backward(DvgBatch *b, const DvgRenderArgs *args, const float *cons
       e = cudaMemsetAsync(h.stale, 0, sizeof(unsigned), s);
       if (e != cudaSuccess) return cuda_fail(e, "batched backward");
       if (sc->d.num_params > 0) dvg::launch_hit_check(a->params, h.params, sc->d.num_params, h.stale, s);
-      set_hit_cache(bs.R, h);
+      set_hit_cache(bs.R, h, false);
       bs.R.hit_chunk_count = nullptr;
       bs.R.hit_stale = h.stale;
     }

@@ -109,10 +109,13 @@ struct DevRender {
   void *pf_frags = nullptr;  // prefiltered: [DVG_PF_SLOTS][samples] fragments instead of keys
   unsigned short *hit_cnt = nullptr;
   const unsigned *hit_stale = nullptr;  // backward: nonzero when the parameters differ from the forward's
-  // keys past the slots (no prefiltering): chunks of DVG_HIT_CHUNK keys and
-  // the next chunk's index ([hit_chunk_cap][DVG_HIT_CHUNK + 1]), each
-  // sample's first chunk ([samples]) and the count of chunks handed out
+  // entries past the slots: without prefiltering, chunks of DVG_HIT_CHUNK
+  // keys and the next chunk's index ([hit_chunk_cap][DVG_HIT_CHUNK + 1]);
+  // with prefiltering, chunks of DVG_PF_CHUNK fragments (pf_chunk_frags)
+  // and the next chunk's index ([hit_chunk_cap]); each sample's first chunk
+  // ([samples]) and the count of chunks handed out
   int *hit_chunks = nullptr;
+  void *pf_chunk_frags = nullptr;
   int *hit_first = nullptr;
   int *hit_chunk_count = nullptr;
   int hit_chunk_cap = 0;
@@ -125,6 +128,7 @@ struct DevRender {
 #define DVG_HIT_CHUNK 16
 #define DVG_PF_SLOTS 16   // prefiltered fragments cached per sample
 #define DVG_PF_BYTES 64   // bytes per cached prefiltered fragment
+#define DVG_PF_CHUNK 16   // prefiltered fragments per cache chunk past the slots
 
 // Boundary samples filed by canvas tile (edge-sampling pass), n entries
 // each; tile_count / tile_start have one entry per canvas tile (+1).

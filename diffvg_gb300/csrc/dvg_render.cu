@@ -78,6 +78,10 @@ __device__ __forceinline__ HitCache hit_cache(const DevRender &R, int idx) {
   return HitCache{R.hit_keys, R.hit_chunks, R.hit_first, R.hit_chunk_count, R.hit_cnt, R.hit_chunk_cap,
                   R.w * R.h * R.spp, idx};
 }
+__device__ __forceinline__ PfCache pf_cache(const DevRender &R, int idx) {
+  return PfCache{static_cast<PFrag *>(R.pf_frags), static_cast<PFrag *>(R.pf_chunk_frags), R.hit_chunks, R.hit_first,
+                 R.hit_chunk_count, R.hit_cnt, R.hit_chunk_cap, R.w * R.h * R.spp, idx};
+}
 
 // Sample of thread threadIdx.x in CTA blockIdx.y of its tile: the tile's
 // 256 * spp samples are numbered pixel-major, pixels in Morton order, so the
@@ -111,11 +115,10 @@ __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRende
   const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
   float4 c;
   if (PREFILTER) {
-    int n = R.w * R.h * R.spp;
     bool cache = R.pf_frags && !bins_overflowed(S);
     if (R.hit_cnt && !cache) R.hit_cnt[idx] = DVG_HIT_NONE;
-    c = sample_color_prefiltered_fwd(S, bg, npt, cache ? static_cast<PFrag *>(R.pf_frags) : nullptr,
-                                     cache ? R.hit_cnt : nullptr, n, idx);
+    PfCache pc = pf_cache(R, idx);
+    c = sample_color_prefiltered_fwd(S, bg, npt, cache ? &pc : nullptr);
   }
   else {
     bool cache = active && R.hit_keys && !bins_overflowed(S);
@@ -223,13 +226,11 @@ __device__ __forceinline__ void sample_bwd_one(const DevScene &S, const DevRende
   int assign = 0;
   float *d_tr = R.d_translation ? R.d_translation + 2 * (y * R.w + x) : nullptr;
   float4 *dbgp = R.d_background ? &dbg : nullptr;
-  int n = R.w * R.h * R.spp;
   float4 color;
   bool deep = false;
   if (PREFILTER) {
     color = active ? sample_color_prefiltered_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params,
-                                                  static_cast<const PFrag *>(R.pf_frags), n, idx,
-                                                  cached_count(R, idx, true), deep)
+                                                  pf_cache(R, idx), cached_count(R, idx, true), deep)
                    : F4(0, 0, 0, 0);
   } else {
     color = sample_color_bwd(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params, active, q, lane, hit_cache(R, idx),
@@ -270,8 +271,7 @@ __device__ __forceinline__ void sample_bwd_deep_one(const DevScene &S, const Dev
   float4 color;
   if (PREFILTER) {
     color = active ? sample_color_prefiltered_bwd_deep(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params,
-                                                       static_cast<const PFrag *>(R.pf_frags), R.w * R.h * R.spp, idx,
-                                                       cached_count(R, idx, true))
+                                                       pf_cache(R, idx), cached_count(R, idx, true))
                    : F4(0, 0, 0, 0);
   } else {
     color = sample_color_bwd_deep(S, bg, npt, d_color, dbgp, &assign, d_tr, R.d_params, active, q, dk, lane);

@@ -83,15 +83,38 @@ struct SegJob { int shape, seg; float x, y, r; };
 struct FragRef { int key, meta; };
 #define DVG_META_HIT (1 << 31)
 
+#ifndef DVG_FRONT_SMEM
+#define DVG_FRONT_SMEM 1
+#endif
 struct WarpQueue {
   SegJob job[32][DVG_LANE_JOBS];
+#if DVG_FRONT_SMEM
   FragRef front[DVG_FRONT][32];            // lane l's candidate fragments in front[0..nf)[l]
+#endif
   unsigned result[32];
   int offs[33];
   unsigned char pend[32 * DVG_LANE_JOBS];  // jobs the fp32 decision left open
   unsigned pend_lanes;                     // lanes that own one of them
 };
 static_assert(32 * DVG_LANE_JOBS <= 256, "job numbers are stored in bytes");
+
+// A lane's fragment front: its column of the warp queue's front in shared
+// memory, or (DVG_FRONT_SMEM 0) a small array of its own.
+#if DVG_FRONT_SMEM
+struct Front {
+  WarpQueue *q;
+  int lane;
+  DI Front(WarpQueue *q_, int lane_) : q(q_), lane(lane_) {}
+  DI FragRef &operator[](int i) const { return q->front[i][lane]; }
+};
+#else
+struct Front {
+  FragRef f[DVG_FRONT];
+  DI Front(WarpQueue *, int) {}
+  DI FragRef &operator[](int i) { return f[i]; }
+  DI const FragRef &operator[](int i) const { return f[i]; }
+};
+#endif
 
 // owner lane and slot of the warp's j-th queued job
 DI const SegJob &warp_job(const WarpQueue *q, int j, int &owner, int &idx) {
@@ -192,8 +215,8 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
 // number of fragments left in the lane's front; overflow is set when the
 // sample has more than DVG_MAX_FRAGMENTS candidates (diffvg.cpp:542).
 template <class Flush>
-DI int collect_fragments(const DevScene &S, v2 pt, WarpQueue *q, int lane, int &njobs, EdgeQ *eq, unsigned &eq_jobs,
-                         bool &overflow, bool &flushed, bool active, Flush &flush) {
+DI int collect_fragments(const DevScene &S, v2 pt, WarpQueue *q, Front &front, int lane, int &njobs, EdgeQ *eq,
+                         unsigned &eq_jobs, bool &overflow, bool &flushed, bool active, Flush &flush) {
   const unsigned full = 0xffffffffu;
   int k = 0, e = 0;
   bool list = true;
@@ -202,7 +225,7 @@ DI int collect_fragments(const DevScene &S, v2 pt, WarpQueue *q, int lane, int &
   int nf = 0, total = 0;
   auto emit = [&](int key, int meta) {
     if (total < DVG_MAX_FRAGMENTS) {
-      q->front[nf++][lane] = FragRef{key, meta};
+      front[nf++] = FragRef{key, meta};
       total++;
     } else {
       overflow = true;
@@ -416,10 +439,9 @@ DI float4 blend_finish(const BlendRun &st, const float4 *bg, EdgeQ *eq, const Hi
 // The lane's fragment front blended into st: one out-of-line copy shared by
 // the walk's flushes and the final blend, so that the paint and blend code
 // is not repeated inside every walk loop.
-static __device__ __noinline__ void blend_front(const DevScene &S, BlendRun &st, v2 pt, EdgeQ *eq, const WarpQueue *q,
-                                               int lane, int nf, unsigned res, unsigned eq_jobs,
-                                               const HitCache *hc) {
-  blend_run(S, st, pt, eq, [&](int i) { return q->front[i][lane]; }, nf, res, eq_jobs, hc);
+static __device__ __noinline__ void blend_front(const DevScene &S, BlendRun &st, v2 pt, EdgeQ *eq, const Front &front,
+                                               int nf, unsigned res, unsigned eq_jobs, const HitCache *hc) {
+  blend_run(S, st, pt, eq, [&](int i) { return front[i]; }, nf, res, eq_jobs, hc);
 }
 
 // State word of a deferred boundary query: its stored fragment count (bits
@@ -450,12 +472,14 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   if (eq) eq->hit = 0;
   BlendRun st = blend_start(bg);
-  auto flush = [&](int nf, unsigned res, unsigned eqj) { blend_front(S, st, pt, eq, q, lane, nf, res, eqj, hc); };
-  int nf = collect_fragments(S, pt, q, lane, njobs, eq, eq_jobs, overflow, flushed, active, flush);
+  Front front(q, lane);
+  auto flush = [&](int nf, unsigned res, unsigned eqj) { blend_front(S, st, pt, eq, front, nf, res, eqj, hc); };
+  int nf = collect_fragments(S, pt, q, front, lane, njobs, eq, eq_jobs, overflow, flushed, active, flush);
   warp_solve(S, q, lane, njobs);
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) flag_error(S, DVG_EFLAG_CAPACITY);
-  flush(nf, q->result[lane], eq_jobs);
+  // the final blend in line (the flushes call blend_front)
+  blend_run(S, st, pt, eq, [&](int i) { return front[i]; }, nf, q->result[lane], eq_jobs, hc);
   float4 c = blend_finish(st, bg, eq, hc);
   if (hc && overflow) hc->cnt[hc->idx] = DVG_HIT_NONE;
   return c;
@@ -479,10 +503,11 @@ static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   eq->hit = 0;
   BlendRun st = blend_start(bg);
+  Front front(q, lane);
   auto flush = [&](int nf, unsigned res, unsigned eqj) {
-    blend_front(S, st, pt, eq, q, lane, nf, res, eqj, nullptr);
+    blend_front(S, st, pt, eq, front, nf, res, eqj, nullptr);
   };
-  int nf = collect_fragments(S, pt, q, lane, njobs, eq, eq_jobs, overflow, flushed, active, flush);
+  int nf = collect_fragments(S, pt, q, front, lane, njobs, eq, eq_jobs, overflow, flushed, active, flush);
   int npend = warp_decide(S, q, lane, njobs);
   deferred = false;
   if (npend > 0) {
@@ -518,7 +543,7 @@ static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const
       if (mine) {
         int f0 = fbase + incl - nfr;
         for (int i = 0; i < nf; i++) {
-          FragRef fr = q->front[i][lane];
+          FragRef fr = front[i];
           E.frag[f0 + i] = make_int2(fr.key, fr.meta);
         }
         E.dq[qid] = make_int4(f0, dq_state(nf, st, eq->hit), (int)q->result[lane], (int)eq_jobs);
@@ -534,7 +559,7 @@ static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) flag_error(S, DVG_EFLAG_CAPACITY);
   if (deferred) return F4(0, 0, 0, 0);
-  flush(nf, q->result[lane], eq_jobs);
+  flush(nf, q->result[lane], eq_jobs);  // out of line: the walk kernel's code stays small
   return blend_finish(st, bg, eq);
 }
 
@@ -621,11 +646,10 @@ struct HitWalk {
 // The hits of the lane's fragment front appended to the walk and to keys
 // (deep set past DVG_BWD_HITS); out of line, shared by the walk's flushes
 // and the final step.
-static __device__ __noinline__ void take_front(const DevScene &S, HitWalk &hw, v2 pt, const WarpQueue *q, int lane,
-                                              int nf, unsigned res, int *keys, float4 *ck, float4 *accs,
-                                              bool &deep) {
+static __device__ __noinline__ void take_front(const DevScene &S, HitWalk &hw, v2 pt, const Front &front, int nf,
+                                              unsigned res, int *keys, float4 *ck, float4 *accs, bool &deep) {
   for (int i = 0; i < nf; i++) {
-    FragRef fr = q->front[i][lane];
+    FragRef fr = front[i];
     if (!frag_hit(fr.meta, res)) continue;
     if (hw.nh >= DVG_BWD_HITS) {
       deep = true;
@@ -656,8 +680,10 @@ DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, fl
   float4 first = bg ? *bg : F4(0, 0, 0, 0);
   HitWalk hw{first, 0};
   deep = false;
-  auto flush = [&](int nf, unsigned res, unsigned) { take_front(S, hw, pt, q, lane, nf, res, keys, ck, accs, deep); };
-  int nf = collect_fragments(S, pt, q, lane, njobs, nullptr, eq_jobs, overflow, flushed, active && cached < 0, flush);
+  Front front(q, lane);
+  auto flush = [&](int nf, unsigned res, unsigned) { take_front(S, hw, pt, front, nf, res, keys, ck, accs, deep); };
+  int nf = collect_fragments(S, pt, q, front, lane, njobs, nullptr, eq_jobs, overflow, flushed, active && cached < 0,
+                             flush);
   warp_solve(S, q, lane, njobs);
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) {
@@ -711,15 +737,16 @@ DI float4 sample_color_bwd_deep(const DevScene &S, const float4 *bg, v2 screen_p
   float4 ck[DVG_MAX_FRAGMENTS / 16], accs[16];
   float4 first = bg ? *bg : F4(0, 0, 0, 0);
   HitWalk hw{first, 0};
+  Front front(q, lane);
   auto flush = [&](int nf, unsigned res, unsigned) {
     for (int i = 0; i < nf; i++) {
-      FragRef fr = q->front[i][lane];
+      FragRef fr = front[i];
       if (!frag_hit(fr.meta, res)) continue;
       dk->key[hw.nh][lane] = fr.key;
       hw.add(S, fr.key, pt, ck, accs);
     }
   };
-  int nf = collect_fragments(S, pt, q, lane, njobs, nullptr, eq_jobs, overflow, flushed, active, flush);
+  int nf = collect_fragments(S, pt, q, front, lane, njobs, nullptr, eq_jobs, overflow, flushed, active, flush);
   warp_solve(S, q, lane, njobs);
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) {
@@ -849,20 +876,48 @@ DI int prefilter_group(const DevScene &S, int g, v2 pt, PFrag *out) {
   return n;
 }
 
-// sample_color_prefiltered, forward only (diffvg.cpp:835-960)
-// With cache set, the sample's fragments (blend order) are stored for the
-// backward pass (sample idx of n): all of them, or, when they do not fit,
-// those of the leading groups that fit whole, with DVG_PF_PARTIAL set in the
-// count; the backward pass then resumes the walk after the last stored group.
+// Sample idx's entry of the prefiltered fragment cache: its first
+// DVG_PF_SLOTS fragments in slots ([slot][n]), the rest in chunks of
+// DVG_PF_CHUNK fragments (chunks[c][j]) linked from first[idx] through
+// next[c]; cnt[idx] holds the count, with DVG_PF_PARTIAL when only the
+// leading groups' fragments are stored (no chunk was left, or the sample
+// has more fragments than the reference allows).
 #define DVG_PF_PARTIAL 0x80
-DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, PFrag *cache = nullptr,
-                                       unsigned short *cache_cnt = nullptr, int n = 0, int idx = 0) {
+#define DVG_PF_CHUNKS ((DVG_MAX_PREFILTER_FRAGMENTS - DVG_PF_SLOTS) / DVG_PF_CHUNK)
+struct PfCache {
+  PFrag *slots;
+  PFrag *chunks;  // [cap][DVG_PF_CHUNK]
+  int *next;      // [cap]
+  int *first;     // [n]
+  int *count;     // chunks handed out in this pass
+  unsigned short *cnt;
+  int cap, n, idx;
+  DI PFrag *at(int i, const int *cid) const {
+    return i < DVG_PF_SLOTS ? &slots[(size_t)i * n + idx]
+                            : &chunks[(size_t)cid[(i - DVG_PF_SLOTS) / DVG_PF_CHUNK] * DVG_PF_CHUNK +
+                                      (i - DVG_PF_SLOTS) % DVG_PF_CHUNK];
+  }
+  // the chunk ids of a cached entry of nc fragments
+  DI void chunk_ids(int nc, int *cid) const {
+    for (int r = 0; DVG_PF_SLOTS + r * DVG_PF_CHUNK < nc; r++)
+      cid[r] = r == 0 ? __ldg(&first[idx]) : __ldg(&next[cid[r - 1]]);
+  }
+};
+
+// sample_color_prefiltered, forward only (diffvg.cpp:835-960)
+// With a cache, the sample's fragments (blend order) are stored for the
+// backward pass: all of them, or those of the leading groups that fit whole
+// with DVG_PF_PARTIAL set in the count, when no chunk is left for the rest
+// (the backward pass then resumes the walk after the last stored group).
+DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 screen_pt,
+                                       const PfCache *pc = nullptr) {
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   int b, e;
   bool list = cand_range(S, pt, b, e);
   float4 acc = bg ? *bg : F4(0, 0, 0, 0);
-  int nf = 0, nc = 0;
-  bool caching = cache != nullptr;
+  int nf = 0, nc = 0, nchunks = 0, asked = 0;
+  int cid[DVG_PF_CHUNKS];
+  bool caching = pc != nullptr;
   int G = S.num_groups;
   for (int k = b; k < e; k++) {
     int g = list ? __ldg(&S.tile_list[k]) : k;
@@ -870,17 +925,35 @@ DI float4 sample_color_prefiltered_fwd(const DevScene &S, const float4 *bg, v2 s
     PFrag fr[2];
     int m = prefilter_group(S, g, pt, fr);
     if (caching && m > 0) {
-      if (nc + m <= DVG_PF_SLOTS) {
-        for (int j = 0; j < m; j++) cache[(size_t)(nc + j) * n + idx] = fr[j];
+      if (nc + m > DVG_MAX_PREFILTER_FRAGMENTS) caching = false;
+      // chunks for fragments nc .. nc + m - 1
+      while (caching && DVG_PF_SLOTS + nchunks * DVG_PF_CHUNK < nc + m) {
+        int c = pc->chunks ? atomicAdd(pc->count, 1) : pc->cap;
+        asked++;
+        if (c >= pc->cap) {
+          caching = false;
+        } else {
+          if (nchunks == 0) pc->first[pc->idx] = c;
+          else pc->next[cid[nchunks - 1]] = c;
+          cid[nchunks++] = c;
+        }
+      }
+      if (caching) {
+        for (int j = 0; j < m; j++) *pc->at(nc + j, cid) = fr[j];
         nc += m;
-      } else {
-        caching = false;
       }
     }
     for (int j = 0; j < m; j++) blend(acc, fr[j].c);
     nf += m;
   }
-  if (cache_cnt) cache_cnt[idx] = (unsigned short)(caching ? nc : (nc | DVG_PF_PARTIAL));
+  if (pc) {
+    // a sample that found no chunk left adds what it would have taken, so
+    // that the pass's count is what it needed
+    int need = nf > DVG_PF_SLOTS ? (min(nf, DVG_MAX_PREFILTER_FRAGMENTS) - DVG_PF_SLOTS + DVG_PF_CHUNK - 1) /
+                                       DVG_PF_CHUNK : 0;
+    if (!caching && pc->chunks && need > asked) atomicAdd(pc->count, need - asked);
+    pc->cnt[pc->idx] = (unsigned short)(caching ? nc : (nc | DVG_PF_PARTIAL));
+  }
   if (nf > DVG_MAX_PREFILTER_FRAGMENTS) flag_error(S, DVG_EFLAG_CAPACITY);
   if (nf <= 0) return bg ? *bg : F4(0, 0, 0, 0);
   return finish_color(acc);
@@ -932,22 +1005,27 @@ DI void pf_step_adjoint(const DevScene &S, const PFrag &f, float4 p, float4 &dc,
 
 // Adjoint of sample_color_prefiltered (diffvg.cpp:960-1113) for a sample
 // whose fragments are all in the forward pass's cache (cached = their
-// count, at most DVG_PF_SLOTS): the reverse walk reads them in place.  Any
-// other sample (no valid cache entry, or only its leading groups cached)
-// sets deep and is left to sample_color_prefiltered_bwd_deep.
+// count): the reverse walk reads them in place, rebuilding each earlier run
+// of 16 blend states from its checkpoint (the same operations in the same
+// order).  Any other sample (no valid cache entry, or only its leading
+// groups cached) sets deep and is left to
+// sample_color_prefiltered_bwd_deep.
 DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color,
-                                       float4 *d_bg, int *assign, float *d_tr, float *dp, const PFrag *cache, int n,
-                                       int idx, int cached, bool &deep) {
-  deep = cached < 0 || (cached & DVG_PF_PARTIAL) != 0;
+                                       float4 *d_bg, int *assign, float *d_tr, float *dp, const PfCache &pc,
+                                       int cached, bool &deep) {
+  deep = cached < 0 || (cached & DVG_PF_PARTIAL) != 0 || cached > DVG_MAX_PREFILTER_FRAGMENTS;
   if (deep) return F4(0, 0, 0, 0);
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
-  int nc = min(cached, DVG_PF_SLOTS);
-  float4 accs[DVG_PF_SLOTS];
+  int nc = cached;
+  int cid[DVG_PF_CHUNKS];
+  pc.chunk_ids(nc, cid);
+  float4 ck[DVG_MAX_PREFILTER_FRAGMENTS / 16], accs[16];
   float4 first = bg ? *bg : F4(0, 0, 0, 0);
   float4 acc = first;
-  for (int j = 0; j < nc; j++) {
-    blend(acc, cache[(size_t)j * n + idx].c);
-    accs[j] = acc;
+  for (int i = 0; i < nc; i++) {
+    if ((i & 15) == 0) ck[i >> 4] = acc;
+    blend(acc, pc.at(i, cid)->c);
+    accs[i & 15] = acc;
   }
   if (nc <= 0) {
     if (bg) {
@@ -958,8 +1036,19 @@ DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 s
   }
   float4 fin;
   float4 dc = blend_out_adjoint(acc, d_color, fin);
-  for (int i = nc - 1; i >= 0; i--)
-    pf_step_adjoint(S, cache[(size_t)i * n + idx], i > 0 ? accs[i - 1] : first, dc, pt, dp, d_tr);
+  int last = (nc - 1) >> 4;
+  #pragma unroll 1
+  for (int r = last; r >= 0; r--) {
+    int lo = r << 4, m = min(nc - lo, 16);
+    if (r != last) {
+      float4 a = ck[r];
+      for (int j = 0; j < m; j++) {
+        blend(a, pc.at(lo + j, cid)->c);
+        accs[j] = a;
+      }
+    }
+    for (int j = m - 1; j >= 0; j--) pf_step_adjoint(S, *pc.at(lo + j, cid), j > 0 ? accs[j - 1] : ck[r], dc, pt, dp, d_tr);
+  }
   if (d_bg) { d_bg->x += dc.x; d_bg->y += dc.y; d_bg->z += dc.z; d_bg->w += dc.w; }
   return fin;
 }
@@ -975,23 +1064,25 @@ DI float4 sample_color_prefiltered_bwd(const DevScene &S, const float4 *bg, v2 s
 #define DVG_PF_RUN 4
 #define DVG_PF_RUNS (DVG_MAX_PREFILTER_FRAGMENTS / DVG_PF_RUN)
 DI float4 sample_color_prefiltered_bwd_deep(const DevScene &S, const float4 *bg, v2 screen_pt, float4 d_color,
-                                            float4 *d_bg, int *assign, float *d_tr, float *dp, const PFrag *cache,
-                                            int n, int idx, int cached) {
+                                            float4 *d_bg, int *assign, float *d_tr, float *dp, const PfCache &pc,
+                                            int cached) {
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   int b, e;
   bool list = cand_range(S, pt, b, e);
   const int G = S.num_groups;
   int nc = 0, g_done = -1;
+  int cid[DVG_PF_CHUNKS];
   if (cached >= 0) {
-    nc = min(cached & ~DVG_PF_PARTIAL, DVG_PF_SLOTS);
-    if (cached & DVG_PF_PARTIAL) g_done = nc > 0 ? cache[(size_t)(nc - 1) * n + idx].group_stroke >> 1 : -1;
+    nc = min(cached & ~DVG_PF_PARTIAL, DVG_MAX_PREFILTER_FRAGMENTS);
+    pc.chunk_ids(nc, cid);
+    if (cached & DVG_PF_PARTIAL) g_done = nc > 0 ? pc.at(nc - 1, cid)->group_stroke >> 1 : -1;
     else e = b;  // every fragment is cached: no group is walked
   }
   const int nunits = nc + (e - b);
   // the fragments of unit u (cached entry u, or candidate b + u - nc)
   auto unit = [&](int u, PFrag *out) -> int {
     if (u < nc) {
-      out[0] = cache[(size_t)u * n + idx];
+      out[0] = *pc.at(u, cid);
       return 1;
     }
     int k = b + (u - nc);

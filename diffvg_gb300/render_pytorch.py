@@ -22,6 +22,7 @@ from enum import IntEnum
 import itertools
 import threading
 import warnings
+import weakref
 
 import torch
 
@@ -211,10 +212,16 @@ class RenderFunction(torch.autograd.Function):
         Autograd sees only those tensors, so a step over thousands of shapes
         does not pay per-argument bookkeeping for the rest of the list."""
         packed = pack_scene_cached(args)
+        dims = (width, height, num_samples_x, num_samples_y, seed)
+        base = _fused_base(packed)
+        if base is not None:
+            # a scene of fuse_parameters views: render from, and differentiate
+            # with respect to, the one tensor they alias
+            return _RenderCore.apply(_RenderCall(dims, packed, None, base), background_image, base)
         T = torch.Tensor
         grad_slots = [k for k, (sl, t) in enumerate(zip(packed.slots, packed.tensors))
                       if sl.differentiable and isinstance(t, T) and t.requires_grad]
-        call = _RenderCall((width, height, num_samples_x, num_samples_y, seed), packed, grad_slots)
+        call = _RenderCall(dims, packed, grad_slots)
         return _RenderCore.apply(call, background_image, *[packed.tensors[k] for k in grad_slots])
 
     @staticmethod
@@ -273,11 +280,104 @@ class RenderFunction(torch.autograd.Function):
 class _RenderCall:
     """What one RenderFunction.apply call renders: image size, sample
     counts, seed, the packed scene and the slots whose tensors autograd
-    tracks."""
-    __slots__ = ('dims', 'packed', 'grad_slots')
+    tracks, or the fused parameter tensor (fuse_parameters) it renders from
+    and differentiates with respect to."""
+    __slots__ = ('dims', 'packed', 'grad_slots', 'fused')
 
-    def __init__(self, dims, packed, grad_slots):
-        self.dims, self.packed, self.grad_slots = dims, packed, grad_slots
+    def __init__(self, dims, packed, grad_slots, fused=None):
+        self.dims, self.packed, self.grad_slots, self.fused = dims, packed, grad_slots, fused
+
+
+# fuse_parameters tensors by storage address
+_fused = weakref.WeakValueDictionary()
+
+
+def fuse_parameters(canvas_width, canvas_height, shapes, shape_groups, filter=None):
+    """One parameter tensor for a whole scene (no reference counterpart).
+
+    Gathers every parameter tensor that serialize_scene passes for these
+    objects (radii, centres, points, thicknesses, stroke widths, corners,
+    paints and their stops, group transforms, the filter radius) into one
+    fp32 leaf tensor on the render device, in the renderer's parameter
+    layout, and rebinds each object's attribute to a view of it (a detached
+    alias: the objects read the current values, autograd does not track
+    them).  RenderFunction.apply on a scene serialized from these objects
+    then renders straight from that tensor and hands autograd that one
+    tensor: its .grad receives the whole gradient in one piece, where
+    separate leaf tensors cost autograd one node each.  Optimise it as one
+    parameter (``torch.optim.Adam([arena])``); the objects see the updates
+    through their views.  A tensor that several attributes share (such as
+    ShapeGroup's default transform) becomes one view per attribute, i.e.
+    separate parameters.  Returns (arena, filter): pass the filter to
+    serialize_scene (a new box filter of radius 0.5 when none is given, so
+    that its radius is in the tensor too).  A scene whose arguments are not
+    exactly these views (an attribute replaced later) renders through the
+    per-tensor path."""
+    if filter is None:
+        filter = PixelFilter(type=FilterType.box, radius=torch.tensor(0.5))
+    shape_names = ('radius', 'center', 'points', 'stroke_width', 'p_min', 'p_max')
+    paint_names = ('begin', 'end', 'center', 'radius', 'offsets', 'stop_colors')
+    owners = [(shp, shape_names) for shp in shapes]
+    for grp in shape_groups:
+        owners.append((grp, ('fill_color', 'stroke_color', 'shape_to_canvas')))
+        for paint in (grp.fill_color, grp.stroke_color):
+            if paint is not None and not isinstance(paint, torch.Tensor):
+                owners.append((paint, paint_names))
+    owners.append((filter, ('radius',)))
+    seen = set()
+    for obj, names in owners:  # one tensor object per attribute
+        for nm in names:
+            t = getattr(obj, nm, None)
+            if isinstance(t, torch.Tensor):
+                if id(t) in seen:
+                    setattr(obj, nm, t.detach().clone())
+                else:
+                    seen.add(id(t))
+    args = RenderFunction.serialize_scene(canvas_width, canvas_height, shapes, shape_groups, filter=filter)
+    packed = pack_scene(args)
+    device = _render_device()
+    with torch.no_grad():
+        arena = packed.param_arena(device).detach().clone().contiguous()
+    arena.requires_grad_(True)
+    data = arena.detach()
+    views = {}
+    for sl, t in zip(packed.slots, packed.tensors):
+        if isinstance(t, torch.Tensor) and id(t) not in views:
+            views[id(t)] = data[sl.offset:sl.offset + sl.numel].view(sl.shape)
+
+    for obj, names in owners:
+        for nm in names:
+            t = getattr(obj, nm, None)
+            if isinstance(t, torch.Tensor) and id(t) in views:
+                setattr(obj, nm, views[id(t)])
+    _fused[data.untyped_storage().data_ptr()] = arena
+    return arena, filter
+
+
+def _fused_base(packed):
+    """The fuse_parameters tensor that every parameter slot of packed is a
+    view of, at the slot's offset, or None.  Decided once per packed scene
+    (the packing cache returns the same object for the same arguments)."""
+    hit = getattr(packed, '_fused_base', False)
+    if hit is not False:
+        base = hit() if hit is not None else None
+        return base
+    base = None
+    ts = packed.tensors
+    if ts and isinstance(ts[0], torch.Tensor) and ts[0].is_cuda:
+        cand = _fused.get(ts[0].untyped_storage().data_ptr())
+        if cand is not None and cand.numel() == packed.num_params:
+            ptr, off0 = cand.untyped_storage().data_ptr(), cand.storage_offset()
+            ok = True
+            for sl, t in zip(packed.slots, ts):
+                if not (isinstance(t, torch.Tensor) and t.dtype == torch.float32 and t.is_contiguous() and
+                        t.untyped_storage().data_ptr() == ptr and t.storage_offset() == off0 + sl.offset):
+                    ok = False
+                    break
+            if ok:
+                base = cand
+    packed._fused_base = weakref.ref(base) if base is not None else None
+    return base
 
 
 def _render_forward(ctx, call, background_image):
@@ -287,7 +387,8 @@ def _render_forward(ctx, call, background_image):
     packed = call.packed
     device = _render_device()
     scene = _native_scene(packed, device)
-    arena = packed.param_arena(device).contiguous()
+    fused = call.fused if call.fused is not None and call.fused.device == device else None
+    arena = fused.detach() if fused is not None else packed.param_arena(device).contiguous()
     ev = _eval_positions(packed, device)
     if packed.output_type == OutputType.color:
         assert ev is None, 'eval_positions apply to the sdf output only'
@@ -316,6 +417,8 @@ def _render_forward(ctx, call, background_image):
     ctx.dims = call.dims
     ctx.device = device
     ctx.grad_slots = call.grad_slots
+    ctx.fused = call.fused
+    ctx.fused_version = call.fused._version if call.fused is not None else None
     return out
 
 
@@ -325,6 +428,9 @@ def _render_backward(ctx, grad_img):
     ctx.grad_slots order, each on its input's device)."""
     packed, scene, device = ctx.packed, ctx.scene, ctx.device
     width, height, nsx, nsy, seed = ctx.dims
+    fused = getattr(ctx, 'fused', None)
+    if fused is not None and fused._version != ctx.fused_version:
+        raise RuntimeError('the fused parameter tensor was modified in place between the render and its backward')
     grad = grad_img.to(device=device, dtype=torch.float32).contiguous()
     d_arena = torch.zeros(max(packed.num_params, 1), device=device)
     bg = ctx.background_image
@@ -346,15 +452,23 @@ def _render_backward(ctx, grad_img):
     launch(reuse | _native.DVG_FLAG_NO_SYNC)
     scene.last_token = ctx.token
     slots, tensors = packed.slots, packed.tensors
-    ks = ctx.grad_slots
-    dst_of = [tensors[k].device for k in ks]
-    bufs = {device: d_arena}
-    for dst in set(dst_of):
-        if dst != device:
-            bufs[dst] = torch.empty(d_arena.shape, dtype=torch.float32, device=dst)
-    sizes = [sl.numel for sl in slots]
-    parts = {dst: torch.split(bufs[dst][:sum(sizes)], sizes) for dst in set(dst_of)}
-    grads = []
+    if fused is not None:
+        # one gradient: the fused tensor's, the arena itself
+        bufs = {device: d_arena}
+        if fused.device != device:
+            bufs[fused.device] = torch.empty(d_arena.shape, dtype=torch.float32, device=fused.device)
+        grads = [bufs[fused.device][:fused.numel()]]
+        ks = dst_of = []
+    else:
+        ks = ctx.grad_slots
+        dst_of = [tensors[k].device for k in ks]
+        bufs = {device: d_arena}
+        for dst in set(dst_of):
+            if dst != device:
+                bufs[dst] = torch.empty(d_arena.shape, dtype=torch.float32, device=dst)
+        grads = []
+        sizes = [sl.numel for sl in slots]
+        parts = {dst: torch.split(bufs[dst][:sum(sizes)], sizes) for dst in set(dst_of)}
     for k, dst in zip(ks, dst_of):
         slot, t = slots[k], tensors[k]
         g = parts[dst][k]

@@ -91,15 +91,16 @@ def estimate_device_bytes(packed, width, height, spp):
     params = 4 * P * 6                              # params, grads, m, v, lr scale, spare
     images = 16 * npx * 3 + 4 * npx                 # image, adjoint, target; weight image
     # forward sample colours; fragment cache per sample: 16 hit keys, or with
-    # prefiltering 16 fragments of 64 B, and a count; without prefiltering
-    # also each sample's first chunk for keys past 16, and the chunks (68 B
-    # each): one per two samples, or as many as twice the mean box depth
-    # asks for (up to 15 per sample); the backward's deep-pass list
+    # prefiltering 16 fragments of 64 B, and a count; each sample's first
+    # chunk for the entries past 16, and the chunks: of 16 keys (68 B) one per
+    # two samples, of 16 fragments (1028 B) one per sixteen, or as many as
+    # twice the mean box depth asks for (up to what the reference's maximum
+    # fragment count needs); the backward's deep-pass list
+    ask = (2.0 * mean_depth(packed) - 16.0) / 16.0
     if packed.use_prefiltering:
-        cache = 16 * 64
+        cache = 16 * 64 + 4 + int(1028 * min(3.0, max(1.0 / 16.0, ask)) + 0.5)
     else:
-        chunks = min(15.0, max(0.5, (2.0 * mean_depth(packed) - 16.0) / 16.0))
-        cache = 16 * 4 + 4 + int(68 * chunks + 0.5)
+        cache = 16 * 4 + 4 + int(68 * min(15.0, max(0.5, ask)) + 0.5)
     samples = 16 * n + (cache + 2 + 4) * n
     edges = 68 * n                                  # boundary-sample records and ordering
     if ng >= 8:  # deferred fp64 walks: jobs, per-query state and colours, fragments, deferred samples

@@ -76,3 +76,44 @@ def test_direct_forward_backward_like_the_reference():
     for a, b in zip(groups, groups2):
         torch.testing.assert_close(out[idx[id(b.stroke_color)]], a.stroke_color.grad, rtol=1e-4, atol=1e-5)
         assert out[idx[id(b.shape_ids)]] is None
+
+
+def test_fused_parameters_give_the_per_tensor_gradients():
+    """fuse_parameters: the scene renders from one leaf tensor whose .grad
+    holds, at each attribute's place, the gradient the per-tensor path
+    delivers to that attribute; an Adam step on it moves the objects."""
+    import diffvg_gb300 as dvg
+    from diffvg_gb300.render_pytorch import _fused_base
+    from diffvg_gb300.packing import pack_scene_cached
+    shapes, groups = _grads({'points', 'width', 'color'})
+    w, h, shapes2, groups2 = _scene(dvg)
+    arena, filt = dvg.fuse_parameters(w, h, shapes2, groups2)
+    assert arena.is_leaf and arena.requires_grad and arena.is_cuda
+    args = dvg.RenderFunction.serialize_scene(w, h, shapes2, groups2, filter=filt)
+    assert _fused_base(pack_scene_cached(args)) is arena
+    img = dvg.RenderFunction.apply(w, h, 2, 2, 3, None, *args)
+    loss = (img * torch.linspace(0, 1, img.numel(), device=img.device).reshape(img.shape)).sum()
+    loss.backward()
+    data = arena.detach()
+    for a, b in zip(shapes, shapes2):
+        off = (b.points.storage_offset() - data.storage_offset())
+        g = arena.grad[off:off + b.points.numel()].view(b.points.shape)
+        torch.testing.assert_close(g, a.points.grad.to(g.device), rtol=1e-4, atol=1e-5)
+        off = (b.stroke_width.storage_offset() - data.storage_offset())
+        torch.testing.assert_close(arena.grad[off].reshape(a.stroke_width.grad.shape),
+                                   a.stroke_width.grad.to(arena.device), rtol=1e-4, atol=1e-5)
+    for a, b in zip(groups, groups2):
+        off = (b.stroke_color.storage_offset() - data.storage_offset())
+        torch.testing.assert_close(arena.grad[off:off + 4], a.stroke_color.grad.to(arena.device), rtol=1e-4,
+                                   atol=1e-5)
+    before = shapes2[0].points.clone()
+    opt = torch.optim.Adam([arena], lr=0.5)
+    opt.step()
+    assert not torch.equal(before, shapes2[0].points)
+    # a replaced attribute leaves the fused path: the per-tensor path renders the same image
+    shapes2[0].points = shapes2[0].points.clone()
+    args = dvg.RenderFunction.serialize_scene(w, h, shapes2, groups2, filter=filt)
+    assert _fused_base(pack_scene_cached(args)) is None
+    img2 = dvg.RenderFunction.apply(w, h, 2, 2, 3, None, *args)
+    args3 = dvg.RenderFunction.serialize_scene(w, h, shapes2, groups2, filter=filt)
+    torch.testing.assert_close(img2, dvg.RenderFunction.apply(w, h, 2, 2, 3, None, *args3))

@@ -75,15 +75,16 @@ def test_estimate_grows_with_image_and_scene():
 
 def test_estimate_counts_the_prefiltered_fragment_cache():
     """A prefiltered request caches 16 whole fragments of 64 B per sample for
-    its backward pass, a sampled one 16 fragment keys of 4 B, the chunks for
-    keys past 16 (68 B per two samples) and each sample's first chunk."""
+    its backward pass and chunks for the fragments past 16 (1028 B per
+    sixteen samples), a sampled one 16 fragment keys of 4 B and chunks for the
+    keys past 16 (68 B per two samples); both keep each sample's first chunk."""
     from diffvg_gb300.packing import pack_scene
     w, h, shapes, groups = workloads.fill_scene(dvg, seed=3, num_paths=8, canvas=128)
     plain = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups))
     pref = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=True))
     n = w * h
     diff = serve.estimate_device_bytes(pref, w, h, 1) - serve.estimate_device_bytes(plain, w, h, 1)
-    assert diff == (16 * 64 - (16 * 4 + 34 + 4)) * n
+    assert diff == (16 * 64 + 64 - (16 * 4 + 34)) * n
 
 
 def test_budget_serialises_requests_and_all_complete(server):
