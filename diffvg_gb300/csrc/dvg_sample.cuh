@@ -83,14 +83,9 @@ struct SegJob { int shape, seg; float x, y, r; };
 struct FragRef { int key, meta; };
 #define DVG_META_HIT (1 << 31)
 
-#ifndef DVG_FRONT_SMEM
-#define DVG_FRONT_SMEM 1
-#endif
 struct WarpQueue {
   SegJob job[32][DVG_LANE_JOBS];
-#if DVG_FRONT_SMEM
   FragRef front[DVG_FRONT][32];            // lane l's candidate fragments in front[0..nf)[l]
-#endif
   unsigned result[32];
   int offs[33];
   unsigned char pend[32 * DVG_LANE_JOBS];  // jobs the fp32 decision left open
@@ -99,22 +94,26 @@ struct WarpQueue {
 static_assert(32 * DVG_LANE_JOBS <= 256, "job numbers are stored in bytes");
 
 // A lane's fragment front: its column of the warp queue's front in shared
-// memory, or (DVG_FRONT_SMEM 0) a small array of its own.
-#if DVG_FRONT_SMEM
-struct Front {
+// memory (the interior adjoint, which keeps at most 16 hits itself), or
+// an array of DVG_LOCAL_FRONT entries of its own (the forward and boundary
+// passes: deep samples then rarely make the warp decide its jobs early).
+struct SharedFront {
+  static constexpr int kCap = DVG_FRONT;
   WarpQueue *q;
   int lane;
-  DI Front(WarpQueue *q_, int lane_) : q(q_), lane(lane_) {}
+  DI SharedFront(WarpQueue *q_, int lane_) : q(q_), lane(lane_) {}
   DI FragRef &operator[](int i) const { return q->front[i][lane]; }
 };
-#else
-struct Front {
-  FragRef f[DVG_FRONT];
-  DI Front(WarpQueue *, int) {}
+#ifndef DVG_LOCAL_FRONT
+#define DVG_LOCAL_FRONT 64
+#endif
+struct LocalFront {
+  static constexpr int kCap = DVG_LOCAL_FRONT;
+  FragRef f[DVG_LOCAL_FRONT];
+  DI LocalFront(WarpQueue *, int) {}
   DI FragRef &operator[](int i) { return f[i]; }
   DI const FragRef &operator[](int i) const { return f[i]; }
 };
-#endif
 
 // owner lane and slot of the warp's j-th queued job
 DI const SegJob &warp_job(const WarpQueue *q, int j, int &owner, int &idx) {
@@ -192,6 +191,13 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
   warp_fp64(S, q, lane, warp_decide(S, q, lane, njobs));
 }
 
+DI bool frag_hit(int meta, unsigned res) {
+  if (meta & DVG_META_HIT) return true;
+  int lo = meta & 255, hi = (meta >> 8) & 255;
+  unsigned mask = (hi - lo >= 32) ? 0xffffffffu : ((1u << (hi - lo)) - 1u);
+  return ((res >> lo) & mask) != 0u;
+}
+
 // Pass 1 of a sample: candidate fragments in group order, undecided stroke
 // segments queued.
 //
@@ -208,13 +214,15 @@ DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
 // reference's early returns do.
 //
 // The lane's candidate fragments go to its column of the warp's fragment
-// front.  Before a group that could overfill a lane's front, the warp
-// decides the queued jobs, every active lane hands its front in order to
-// flush(nf, results, eq_jobs) and starts an empty one, and flushed is set
-// (the same in every lane).  Returns the
+// front.  Before a group that could overfill a lane's front, every lane
+// hands the decided fragments at the start of its front to
+// flush(count, 0, 0) and keeps the rest; if a lane's front is still too
+// full, the warp decides its queued jobs, every active lane hands its whole
+// front to flush(nf, results, eq_jobs) and starts an empty one, and flushed
+// is set (the same in every lane).  Returns the
 // number of fragments left in the lane's front; overflow is set when the
 // sample has more than DVG_MAX_FRAGMENTS candidates (diffvg.cpp:542).
-template <class Flush>
+template <class Front, class Flush>
 DI int collect_fragments(const DevScene &S, v2 pt, WarpQueue *q, Front &front, int lane, int &njobs, EdgeQ *eq,
                          unsigned &eq_jobs, bool &overflow, bool &flushed, bool active, Flush &flush) {
   const unsigned full = 0xffffffffu;
@@ -239,13 +247,22 @@ DI int collect_fragments(const DevScene &S, v2 pt, WarpQueue *q, Front &front, i
     int myg = k < e ? (list ? __ldg(&S.tile_list[k]) : k) : 0x7fffffff;
     int g = __reduce_min_sync(full, myg);
     if (g == 0x7fffffff) break;
-    if (__any_sync(full, nf > DVG_FRONT - 2)) {
-      warp_solve(S, q, lane, njobs);
-      if (active) flush(nf, q->result[lane], eq_jobs);
-      nf = 0;
-      njobs = 0;
-      eq_jobs = 0u;
-      flushed = true;
+    if (__any_sync(full, nf > Front::kCap - 2)) {
+      // first hand over each lane's decided prefix (fills decide during the
+      // walk); only a front still full after that waits for the warp's jobs
+      int u = 0;
+      while (u < nf && (front[u].meta & DVG_META_HIT)) u++;
+      if (active && u > 0) flush(u, 0u, 0u);
+      for (int i = u; i < nf; i++) front[i - u] = front[i];
+      nf -= u;
+      if (__any_sync(full, nf > Front::kCap - 2)) {
+        warp_solve(S, q, lane, njobs);
+        if (active) flush(nf, q->result[lane], eq_jobs);
+        nf = 0;
+        njobs = 0;
+        eq_jobs = 0u;
+        flushed = true;
+      }
     }
     bool act = myg == g;
     unsigned tmask = act ? (list ? __ldg(&S.tile_mask[k]) : full) : 0u;
@@ -329,12 +346,6 @@ DI int collect_fragments(const DevScene &S, v2 pt, WarpQueue *q, Front &front, i
   return nf;
 }
 
-DI bool frag_hit(int meta, unsigned res) {
-  if (meta & DVG_META_HIT) return true;
-  int lo = meta & 255, hi = (meta >> 8) & 255;
-  unsigned mask = (hi - lo >= 32) ? 0xffffffffu : ((1u << (hi - lo)) - 1u);
-  return ((res >> lo) & mask) != 0u;
-}
 
 // paint of fragment key (2 * group + is_stroke) at pt
 DI float4 frag_color(const DevScene &S, int key, v2 pt) {
@@ -439,6 +450,7 @@ DI float4 blend_finish(const BlendRun &st, const float4 *bg, EdgeQ *eq, const Hi
 // The lane's fragment front blended into st: one out-of-line copy shared by
 // the walk's flushes and the final blend, so that the paint and blend code
 // is not repeated inside every walk loop.
+template <class Front>
 static __device__ __noinline__ void blend_front(const DevScene &S, BlendRun &st, v2 pt, EdgeQ *eq, const Front &front,
                                                int nf, unsigned res, unsigned eq_jobs, const HitCache *hc) {
   blend_run(S, st, pt, eq, [&](int i) { return front[i]; }, nf, res, eq_jobs, hc);
@@ -472,7 +484,7 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   if (eq) eq->hit = 0;
   BlendRun st = blend_start(bg);
-  Front front(q, lane);
+  LocalFront front(q, lane);
   auto flush = [&](int nf, unsigned res, unsigned eqj) { blend_front(S, st, pt, eq, front, nf, res, eqj, hc); };
   int nf = collect_fragments(S, pt, q, front, lane, njobs, eq, eq_jobs, overflow, flushed, active, flush);
   warp_solve(S, q, lane, njobs);
@@ -503,7 +515,7 @@ static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const
   v2 pt = V2(screen_pt.x * S.W, screen_pt.y * S.H);
   eq->hit = 0;
   BlendRun st = blend_start(bg);
-  Front front(q, lane);
+  LocalFront front(q, lane);
   auto flush = [&](int nf, unsigned res, unsigned eqj) {
     blend_front(S, st, pt, eq, front, nf, res, eqj, nullptr);
   };
@@ -646,7 +658,7 @@ struct HitWalk {
 // The hits of the lane's fragment front appended to the walk and to keys
 // (deep set past DVG_BWD_HITS); out of line, shared by the walk's flushes
 // and the final step.
-static __device__ __noinline__ void take_front(const DevScene &S, HitWalk &hw, v2 pt, const Front &front, int nf,
+static __device__ __noinline__ void take_front(const DevScene &S, HitWalk &hw, v2 pt, const SharedFront &front, int nf,
                                               unsigned res, int *keys, float4 *ck, float4 *accs, bool &deep) {
   for (int i = 0; i < nf; i++) {
     FragRef fr = front[i];
@@ -680,7 +692,7 @@ DI float4 sample_color_bwd(const DevScene &S, const float4 *bg, v2 screen_pt, fl
   float4 first = bg ? *bg : F4(0, 0, 0, 0);
   HitWalk hw{first, 0};
   deep = false;
-  Front front(q, lane);
+  SharedFront front(q, lane);
   auto flush = [&](int nf, unsigned res, unsigned) { take_front(S, hw, pt, front, nf, res, keys, ck, accs, deep); };
   int nf = collect_fragments(S, pt, q, front, lane, njobs, nullptr, eq_jobs, overflow, flushed, active && cached < 0,
                              flush);
@@ -737,7 +749,7 @@ DI float4 sample_color_bwd_deep(const DevScene &S, const float4 *bg, v2 screen_p
   float4 ck[DVG_MAX_FRAGMENTS / 16], accs[16];
   float4 first = bg ? *bg : F4(0, 0, 0, 0);
   HitWalk hw{first, 0};
-  Front front(q, lane);
+  SharedFront front(q, lane);
   auto flush = [&](int nf, unsigned res, unsigned) {
     for (int i = 0; i < nf; i++) {
       FragRef fr = front[i];

@@ -94,3 +94,22 @@ def test_gaussian_filter_scene():
     g = (dvg.FilterType.gaussian, 1.25)
     _run(lambda m: workloads.stroke_scene(m, seed=7, num_paths=128, canvas=128), 2, 4, filt=g)
     _run(lambda m: workloads.fill_scene(m, seed=8, num_paths=24, canvas=128), 1, 5, prefilter=True, filt=g)
+
+
+def test_deep_mixed_scene():
+    """Samples under 40+ overlapping strokes and fills (96x96, 1800 paths):
+    the fragment front flushes during the walk, the boundary pass settles
+    fp32-decided jobs mid-walk and defers the rest, the fragment cache takes
+    chunks past 16 keys, and the backward without a cache sends the deepest
+    samples to the deep pass."""
+    from diffvg_gb300 import workloads
+    _run(lambda dvg: workloads.mixed_scene(dvg, 77, 96, 1800), 2, 5)
+
+
+def test_deep_fill_scene_prefiltered():
+    """Prefiltered samples under many fills (96x96, 300 fills of radius
+    4-20, mean box depth 25): cache chunks past 16 fragments and the deep
+    pass's regenerated runs."""
+    from diffvg_gb300 import workloads
+    _run(lambda dvg: workloads.fill_scene(dvg, seed=9, num_paths=300, canvas=96, radius_range=(4.0, 20.0)), 1, 9,
+         prefilter=True)
