@@ -820,6 +820,9 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
   cudaError_t e = sc->weight.ensure(npx * sizeof(float));
   if (e == cudaSuccess && image) e = sc->samples.ensure(n * sizeof(float4));
   if (e == cudaSuccess && cache) e = sc->hits.ensure(hit_bytes(sc, n, pf));
+  // the forward defers its open fp64 walks as the boundary pass does, in the same arena
+  bool defer = image && !pf && edge_defers(sc, n);
+  if (e == cudaSuccess && defer) e = sc->edge.ensure(edge_bytes(sc, n));
   if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
   if (sc->d.num_groups == 0 && image) {
     // empty scene: the background (or transparent black), unfiltered
@@ -839,8 +842,10 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
         h = hit_arena(sc, n, pf);
         set_hit_cache(R, h, pf);
       }
+      EdgeRecords D{};
+      if (defer) D = edge_records(sc, n);
       timed(sc, K_WEIGHT, s, [&] { dvg::launch_weight(S, R, s); });
-      timed(sc, K_SAMPLE_FWD, s, [&] { dvg::launch_sample_fwd(S, R, samples, s); });
+      timed(sc, K_SAMPLE_FWD, s, [&] { dvg::launch_sample_fwd(S, R, samples, s, defer ? &D : nullptr); });
       timed(sc, K_RESOLVE, s, [&] { dvg::launch_resolve(R, samples, image, s); });
       e = cudaGetLastError();
       if (e == cudaSuccess && cache && sc->d.num_params > 0)
@@ -965,6 +970,25 @@ struct DvgBatch {
   BatchScene *d_fwd = nullptr, *d_bwd = nullptr;
   int *d_ints = nullptr, *d_counters = nullptr;
   size_t nints = 0;
+  // the per-scene launches around the persistent ones run on these streams,
+  // forked from and joined back into the caller's stream (graph-capturable)
+  static constexpr int kLanes = 8;
+  cudaStream_t lanes[kLanes] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kLanes] = {};
+  cudaError_t fork(cudaStream_t s) {
+    cudaError_t e = cudaEventRecord(fork_ev, s);
+    for (int j = 0; j < kLanes && e == cudaSuccess; j++) e = cudaStreamWaitEvent(lanes[j], fork_ev, 0);
+    return e;
+  }
+  cudaError_t join(cudaStream_t s) {
+    cudaError_t e = cudaSuccess;
+    for (int j = 0; j < kLanes && e == cudaSuccess; j++) {
+      e = cudaEventRecord(join_ev[j], lanes[j]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join_ev[j], 0);
+    }
+    return e;
+  }
+  cudaStream_t lane(int k) const { return lanes[k % kLanes]; }
 };
 
 namespace {
@@ -1051,6 +1075,15 @@ int dvg_batch_create(DvgScene *const *scenes, int num_scenes, DvgBatch **out) {
     dvg_batch_destroy(b);
     return cuda_fail(e, "allocating a batch");
   }
+  for (int j = 0; j < DvgBatch::kLanes && e == cudaSuccess; j++) {
+    e = cudaStreamCreateWithFlags(&b->lanes[j], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join_ev[j], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    dvg_batch_destroy(b);
+    return cuda_fail(e, "creating a batch's streams");
+  }
   char *p = reinterpret_cast<char *>(b->dev.ptr);
   b->d_fwd = carve<BatchScene>(p, n);
   b->d_bwd = carve<BatchScene>(p, n);
@@ -1066,6 +1099,11 @@ int dvg_batch_destroy(DvgBatch *b) {
   DeviceGuard guard(b->device);
   if (b->h_bs) cudaFreeHost(b->h_bs);
   if (b->h_ints) cudaFreeHost(b->h_ints);
+  for (int j = 0; j < DvgBatch::kLanes; j++) {
+    if (b->lanes[j]) cudaStreamDestroy(b->lanes[j]);
+    if (b->join_ev[j]) cudaEventDestroy(b->join_ev[j]);
+  }
+  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
   b->dev.release();
   delete b;
   return DVG_OK;
@@ -1088,15 +1126,18 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
   BatchScene *hb = b->h_bs;
   std::vector<int> live;
   std::vector<DvgRenderArgs> live_args;
+  for (int i = 0; i < n; i++)
+    if (!images[i] || (reinterpret_cast<uintptr_t>(images[i]) & 15u))
+      return fail(DVG_ERR_INVALID, "image %d must be set and 16-byte aligned", i);
+  if ((e = b->fork(s)) != cudaSuccess) return cuda_fail(e, "batched forward");
   for (int i = 0; i < n; i++) {
     DvgScene *sc = b->scenes[i];
     const DvgRenderArgs *a = &args[i];
-    if (!images[i] || (reinterpret_cast<uintptr_t>(images[i]) & 15u))
-      return fail(DVG_ERR_INVALID, "image %d must be set and 16-byte aligned", i);
+    cudaStream_t ls = b->lane(i);
     size_t npx = (size_t)a->width * a->height, ns = npx * a->num_samples_x * a->num_samples_y;
     sc->hit_live = false;
     if (sc->d.num_groups == 0) {  // empty scene: transparent black
-      e = cudaMemsetAsync(images[i], 0, npx * 4 * sizeof(float), s);
+      e = cudaMemsetAsync(images[i], 0, npx * 4 * sizeof(float), ls);
       if (e != cudaSuccess) return cuda_fail(e, "batched forward");
       continue;
     }
@@ -1108,18 +1149,19 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
     bs.S = make_dev(sc, a->params);
     DvgRenderArgs ai = *a;
     ai.flags |= DVG_FLAG_NO_SYNC;  // failures stay latched in the scene (dvg_scene_sync)
-    if ((st = prepare(sc, bs.S, &ai, s)) != DVG_OK) return st;
+    if ((st = prepare(sc, bs.S, &ai, ls)) != DVG_OK) return st;
     bs.R = make_render(sc, a);
     HitArena h = hit_arena(sc, ns, false);
     set_hit_cache(bs.R, h, false);
-    e = cudaMemsetAsync(h.chunk_count, 0, sizeof(int), s);
+    e = cudaMemsetAsync(h.chunk_count, 0, sizeof(int), ls);
     if (e != cudaSuccess) return cuda_fail(e, "batched forward");
     bs.E = EdgeRecords{};
     bs.samples = reinterpret_cast<float4 *>(sc->samples.ptr);
-    dvg::launch_weight(bs.S, bs.R, s);
+    dvg::launch_weight(bs.S, bs.R, ls);
     live.push_back(i);
     live_args.push_back(*a);
   }
+  if ((e = b->join(s)) != cudaSuccess) return cuda_fail(e, "batched forward");
   int nl = (int)live.size();
   if (nl == 0) return DVG_OK;
   int *order = b->h_ints, *item_start = b->h_ints + nl;
@@ -1128,15 +1170,17 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_ints, b->h_ints, (2 * nl + 1) * sizeof(int), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "staging a batch");
   dvg::launch_batch_sample_fwd(b->d_fwd, nl, b->d_ints, b->d_ints + nl, spt, ctas, b->d_counters, s);
+  if ((e = b->fork(s)) != cudaSuccess) return cuda_fail(e, "batched forward");
   for (int k = 0; k < nl; k++) {
     int i = live[k];
     DvgScene *sc = b->scenes[i];
     const DvgRenderArgs *a = &args[i];
+    cudaStream_t ls = b->lane(k);
     size_t ns = (size_t)a->width * a->height * a->num_samples_x * a->num_samples_y;
-    dvg::launch_resolve(hb[k].R, hb[k].samples, images[i], s);
+    dvg::launch_resolve(hb[k].R, hb[k].samples, images[i], ls);
     HitArena h = hit_arena(sc, ns, false);
     if (sc->d.num_params > 0)
-      e = cudaMemcpyAsync(h.params, a->params, (size_t)sc->d.num_params * sizeof(float), cudaMemcpyDeviceToDevice, s);
+      e = cudaMemcpyAsync(h.params, a->params, (size_t)sc->d.num_params * sizeof(float), cudaMemcpyDeviceToDevice, ls);
     if (e != cudaSuccess) return cuda_fail(e, "batched forward");
     sc->hit_live = true;
     sc->hit_pf = false;
@@ -1146,6 +1190,7 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
     sc->hit_nsy = a->num_samples_y;
     sc->hit_seed = a->seed;
   }
+  if ((e = b->join(s)) != cudaSuccess) return cuda_fail(e, "batched forward");
   e = cudaGetLastError();
   return e == cudaSuccess ? DVG_OK : cuda_fail(e, "batched forward launch");
 }
@@ -1167,11 +1212,15 @@ int dvg_batch_backward(DvgBatch *b, const DvgRenderArgs *args, const float *cons
   BatchScene *hb = b->h_bs + n;
   std::vector<int> live;
   std::vector<DvgRenderArgs> live_args;
+  for (int i = 0; i < n; i++)
+    if (!d_images[i] || !d_params[i] || (reinterpret_cast<uintptr_t>(d_images[i]) & 15u))
+      return fail(DVG_ERR_INVALID, "d_image %d / d_params %d must be set, d_image 16-byte aligned", i, i);
+  // per scene, on the batch's streams: preparation, weights, the boundary samples drawn and ordered
+  if ((e = b->fork(s)) != cudaSuccess) return cuda_fail(e, "batched backward");
   for (int i = 0; i < n; i++) {
     DvgScene *sc = b->scenes[i];
     const DvgRenderArgs *a = &args[i];
-    if (!d_images[i] || !d_params[i] || (reinterpret_cast<uintptr_t>(d_images[i]) & 15u))
-      return fail(DVG_ERR_INVALID, "d_image %d / d_params %d must be set, d_image 16-byte aligned", i, i);
+    cudaStream_t ls = b->lane(i);
     if (sc->d.num_groups == 0) continue;  // empty scene: nothing to differentiate
     size_t npx = (size_t)a->width * a->height, ns = npx * a->num_samples_x * a->num_samples_y;
     e = sc->weight.ensure(npx * sizeof(float));
@@ -1182,41 +1231,42 @@ int dvg_batch_backward(DvgBatch *b, const DvgRenderArgs *args, const float *cons
     bs.S = make_dev(sc, a->params);
     DvgRenderArgs ai = *a;
     ai.flags |= DVG_FLAG_NO_SYNC;
-    if ((st = prepare(sc, bs.S, &ai, s)) != DVG_OK) return st;
+    if ((st = prepare(sc, bs.S, &ai, ls)) != DVG_OK) return st;
     bs.R = make_render(sc, a);
     bs.R.d_params = d_params[i];
     bs.R.d_image = d_images[i];
     bs.R.deep_count = reinterpret_cast<int *>(sc->deep.ptr);
     bs.R.deep_list = bs.R.deep_count + 1;
-    e = cudaMemsetAsync(bs.R.deep_count, 0, sizeof(int), s);
+    e = cudaMemsetAsync(bs.R.deep_count, 0, sizeof(int), ls);
     if (e != cudaSuccess) return cuda_fail(e, "batched backward");
     if (hit_matches(sc, a)) {
       HitArena h = hit_arena(sc, ns, false);
-      e = cudaMemsetAsync(h.stale, 0, sizeof(unsigned), s);
+      e = cudaMemsetAsync(h.stale, 0, sizeof(unsigned), ls);
       if (e != cudaSuccess) return cuda_fail(e, "batched backward");
-      if (sc->d.num_params > 0) dvg::launch_hit_check(a->params, h.params, sc->d.num_params, h.stale, s);
+      if (sc->d.num_params > 0) dvg::launch_hit_check(a->params, h.params, sc->d.num_params, h.stale, ls);
       set_hit_cache(bs.R, h, false);
       bs.R.hit_chunk_count = nullptr;
       bs.R.hit_stale = h.stale;
     }
     bs.E = edge_records(sc, ns);
     bs.samples = nullptr;
-    dvg::launch_weight(bs.S, bs.R, s);
+    dvg::launch_weight(bs.S, bs.R, ls);
+    dvg::launch_edge_setup(bs.S, bs.R, bs.E, ls);
     live.push_back(i);
     live_args.push_back(*a);
   }
+  if ((e = b->join(s)) != cudaSuccess) return cuda_fail(e, "batched backward");
   int nl = (int)live.size();
   if (nl == 0) return DVG_OK;
   // staged ints: scene order, item starts (nl + 1), the paired-lane scenes' order
   int *ints = b->h_ints + b->nints, *d_ints = b->d_ints + b->nints;
   int *order = ints, *item_start = ints + nl, *edge_order = ints + 2 * nl + 1;
   batch_items(live_args.data(), nl, spt, order, item_start);
-  // the boundary samples: drawn and ordered per scene, evaluated together
-  // (scenes of fewer than 8 groups evaluate theirs per scene)
+  // the boundary samples are evaluated together (scenes of fewer than 8
+  // groups evaluate theirs per scene)
   int n_edge = 0;
   for (int r = 0; r < nl; r++) {
     int k = order[r];
-    dvg::launch_edge_setup(hb[k].S, hb[k].R, hb[k].E, s);
     if (b->scenes[live[k]]->d.num_groups >= 8 && hb[k].E.job_a) edge_order[n_edge++] = k;
   }
   e = cudaMemcpyAsync(b->d_bwd, hb, nl * sizeof(BatchScene), cudaMemcpyHostToDevice, s);
@@ -1225,8 +1275,11 @@ int dvg_batch_backward(DvgBatch *b, const DvgRenderArgs *args, const float *cons
   if (e != cudaSuccess) return cuda_fail(e, "staging a batch");
   dvg::launch_batch_sample_bwd(b->d_bwd, nl, d_ints, d_ints + nl, spt, ctas, b->d_counters + 1, s);
   if (n_edge > 0) dvg::launch_batch_edge(b->d_bwd, n_edge, d_ints + 2 * nl + 1, spt, ctas, b->d_counters + 2, s);
+  if ((e = b->fork(s)) != cudaSuccess) return cuda_fail(e, "batched backward");
   for (int k = 0; k < nl; k++)
-    if (!(b->scenes[live[k]]->d.num_groups >= 8 && hb[k].E.job_a)) dvg::launch_edge_eval(hb[k].S, hb[k].R, hb[k].E, s);
+    if (!(b->scenes[live[k]]->d.num_groups >= 8 && hb[k].E.job_a))
+      dvg::launch_edge_eval(hb[k].S, hb[k].R, hb[k].E, b->lane(k));
+  if ((e = b->join(s)) != cudaSuccess) return cuda_fail(e, "batched backward");
   e = cudaGetLastError();
   return e == cudaSuccess ? DVG_OK : cuda_fail(e, "batched backward launch");
 }

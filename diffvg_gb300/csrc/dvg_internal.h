@@ -28,7 +28,8 @@ cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4
 // One launcher per render kernel; the C ABI sequences them (and can record
 // CUDA events between them for per-kernel timing).
 void launch_weight(const DevScene &S, const DevRender &R, cudaStream_t st);
-void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, cudaStream_t st);
+void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, cudaStream_t st,
+                       const EdgeRecords *deferral = nullptr);
 void launch_hit_check(const float *params, const float *fwd_params, int n, unsigned *stale, cudaStream_t st);
 void launch_resolve(const DevRender &R, const float4 *samples, float *image, cudaStream_t st);
 // dbg_val / dbg_flag: per-sample background adjoint scratch (only written

@@ -100,7 +100,8 @@ __device__ __forceinline__ void tile_sample(int spp, int cta_y, int tid, int &dx
 // cta_y of image tile `tile` (a warp's lanes call it together).
 template <bool PREFILTER>
 __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRender &R, int tile, int cta_y, int tid,
-                                               float4 *samples, WarpQueue *q, int lane) {
+                                               float4 *samples, WarpQueue *q, int lane,
+                                               const EdgeRecords *D = nullptr) {
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
   int tx = tile % tiles_x, ty = tile / tiles_x;
   int dx, dy, sub;
@@ -124,15 +125,49 @@ __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRende
     bool cache = active && R.hit_keys && !bins_overflowed(S);
     if (active && R.hit_cnt && !cache) R.hit_cnt[idx] = DVG_HIT_NONE;
     HitCache hc = hit_cache(R, idx);
-    c = sample_color_fwd(S, bg, npt, nullptr, active, q, lane, cache ? &hc : nullptr);
+    bool parked = false;
+    c = sample_color_fwd(S, bg, npt, nullptr, active, q, lane, cache ? &hc : nullptr, D, idx, &parked);
+    if (parked) {  // k_fwd_finish writes its colour
+      D->ds[atomicAdd(&D->counts[3], 1)] = idx;
+      return;
+    }
   }
   if (active) samples[idx] = c;
 }
 
 template <bool PREFILTER>
 __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
-    k_sample_fwd(const __grid_constant__ DevScene S, const __grid_constant__ DevRender R, float4 *samples) {
-  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, samples, warp_queue(), threadIdx.x & 31);
+    k_sample_fwd(const __grid_constant__ DevScene S, const __grid_constant__ DevRender R, float4 *samples,
+                 const __grid_constant__ EdgeRecords D) {
+  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, samples, warp_queue(), threadIdx.x & 31,
+                            D.job_a ? &D : nullptr);
+}
+
+// The samples the forward pass deferred (D.ds): blend each one's parked
+// fragments with its fp32 and fp64 results over the blend state it parked,
+// continue its fragment-cache entry, write its colour.
+__global__ void __launch_bounds__(256) k_fwd_finish(const __grid_constant__ DevScene S,
+                                                    const __grid_constant__ DevRender R,
+                                                    const __grid_constant__ EdgeRecords D, float4 *samples) {
+  int n = *(volatile const int *)&D.counts[3];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    int idx = D.ds[k];
+    int4 rec = D.dq[idx];
+    int x, y;
+    v2 spt = sample_pos(R, idx, false, x, y);
+    v2 pt = V2(spt.x / R.w * S.W, spt.y / R.h * S.H);
+    const float4 *bg = R.background ? reinterpret_cast<const float4 *>(R.background) + (y * R.w + x) : nullptr;
+    BlendRun st{D.dq_col[idx], (rec.y >> 8) & 0x3fffff, -1, rec.w};
+    bool overflow = (rec.y >> 30) & 1;
+    HitCache hc = hit_cache(R, idx);
+    const HitCache *hcp = R.hit_keys && !bins_overflowed(S) ? &hc : nullptr;
+    const FragRef *frags = reinterpret_cast<const FragRef *>(D.frag + rec.x);
+    blend_run(S, st, pt, nullptr, [&](int i) { return frags[i]; }, rec.y & 0xff, (unsigned)rec.z | D.dq_res[idx], 0u,
+              hcp);
+    float4 c = blend_finish(st, bg, nullptr, hcp);
+    if (hcp && overflow) hc.cnt[idx] = DVG_HIT_NONE;
+    samples[idx] = c;
+  }
 }
 
 // filtered pixel colour from the sample colours around it
@@ -787,17 +822,29 @@ static int sm_count() {
   return sms[dev];
 }
 
+static unsigned persistent_grid(int ctas_per_sm) {
+  return (unsigned)(sm_count() * (ctas_per_sm > 0 ? ctas_per_sm : 1));
+}
+
 void launch_weight(const DevScene &S, const DevRender &R, cudaStream_t st) {
   k_weight<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(R, S);
 }
-void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, cudaStream_t st) {
+void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, cudaStream_t st,
+                       const EdgeRecords *D) {
   dim3 grid(tiles_of(R), R.spp);
   if (R.hit_chunk_count) cudaMemsetAsync(R.hit_chunk_count, 0, sizeof(int), st);
+  EdgeRecords none{};
   if (R.prefilter) {
-    k_sample_fwd<true><<<grid, 256, 0, st>>>(S, R, samples);
+    k_sample_fwd<true><<<grid, 256, 0, st>>>(S, R, samples, none);
   } else {
+    bool defer = D && D->job_a;
+    if (defer) cudaMemsetAsync(D->counts, 0, 4 * sizeof(int), st);
     allow_queues(k_sample_fwd<false>, QK_FWD);
-    k_sample_fwd<false><<<grid, 256, kQueueBytes, st>>>(S, R, samples);
+    k_sample_fwd<false><<<grid, 256, kQueueBytes, st>>>(S, R, samples, defer ? *D : none);
+    if (defer) {
+      k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, *D);
+      k_fwd_finish<<<persistent_grid(8), 256, 0, st>>>(S, R, *D, samples);
+    }
   }
 }
 void launch_hit_check(const float *params, const float *fwd_params, int n, unsigned *stale, cudaStream_t st) {
@@ -822,9 +869,6 @@ void launch_sample_bwd(const DevScene &S, const DevRender &R, float4 *dbg_val, i
 void launch_bg_combine(const DevScene &S, const DevRender &R, const float4 *dbg_val, const int *dbg_flag,
                        cudaStream_t st) {
   k_bg_combine<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(S, R, dbg_val, dbg_flag);
-}
-static unsigned persistent_grid(int ctas_per_sm) {
-  return (unsigned)(sm_count() * (ctas_per_sm > 0 ? ctas_per_sm : 1));
 }
 
 void launch_edge_setup(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {

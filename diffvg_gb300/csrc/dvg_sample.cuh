@@ -90,6 +90,7 @@ struct WarpQueue {
   int offs[33];
   unsigned char pend[32 * DVG_LANE_JOBS];  // jobs the fp32 decision left open
   unsigned pend_lanes;                     // lanes that own one of them
+  int qid[32];                             // the lanes' query numbers (deferral)
 };
 static_assert(32 * DVG_LANE_JOBS <= 256, "job numbers are stored in bytes");
 
@@ -472,12 +473,74 @@ DI float4 blend_deferred(const DevScene &S, const float4 *bg, v2 pt, EdgeQ *eq, 
   return blend_finish(st, bg, eq);
 }
 
+// Hands the fp64 walks the warp's fp32 decision left open (npend of them,
+// listed by warp_decide) to D's job list, and each owning lane's candidate
+// fragments and state to D (dq[qid] = {first fragment, word_y, fp32 results,
+// word_w}; dq_col[qid] = acc), when the lists have room; returns whether
+// they had (the same in every lane) and sets deferred in the lanes that
+// parked.  Without room nothing is stored.
+template <class Front>
+DI bool park_open_jobs(const EdgeRecords &D, WarpQueue *q, int lane, const Front &front, int nf, bool active,
+                       int npend, int qid, int word_y, int word_w, float4 acc, bool &deferred) {
+  const unsigned full = 0xffffffffu;
+  bool mine = active && ((q->pend_lanes >> lane) & 1u);
+  q->qid[lane] = qid;
+  // room for the deferring lanes' fragments, then for the warp's jobs
+  int nfr = mine ? nf : 0, incl = nfr;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int v = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += v;
+  }
+  int fbase = 0, jbase = 0;
+  if (lane == 31) fbase = atomicAdd(&D.counts[2], incl);
+  fbase = __shfl_sync(full, fbase, 31);
+  bool room = (long long)fbase + __shfl_sync(full, incl, 31) <= D.frag_cap;
+  if (room) {
+    if (lane == 0) jbase = atomicAdd(&D.counts[0], npend);
+    jbase = __shfl_sync(full, jbase, 0);
+    if ((long long)jbase + npend > D.job_cap) {
+      room = false;
+      for (int k = jbase + lane; k < D.job_cap && k < jbase + npend; k += 32) D.job_a[k].x = -1;
+    }
+  }
+  __syncwarp();
+  if (!room) return false;
+  #pragma unroll 1
+  for (int k = lane; k < npend; k += 32) {
+    int owner, idx;
+    SegJob jb = warp_job(q, q->pend[k], owner, idx);
+    D.job_a[jbase + k] = make_int4(q->qid[owner], idx, jb.shape, jb.seg);
+    D.job_b[jbase + k] = F4(jb.x, jb.y, jb.r, 0.f);
+  }
+  if (mine) {
+    int f0 = fbase + incl - nfr;
+    for (int i = 0; i < nf; i++) {
+      FragRef fr = front[i];
+      D.frag[f0 + i] = make_int2(fr.key, fr.meta);
+    }
+    D.dq[qid] = make_int4(f0, word_y, (int)q->result[lane], word_w);
+    D.dq_res[qid] = 0u;
+    D.dq_col[qid] = acc;
+    deferred = true;
+  }
+  __syncwarp();
+  return true;
+}
+
 // Forward colour of one sample (sample_color, diffvg.cpp:525-655); see
 // blend_run for the EdgeQuery rule and the fragment cache.
 // Out of line: the boundary pass calls it twice per sample.
+// With D (a forward colour pass of 8+ groups), the fp64 walks its fp32
+// decision leaves open go to D's job list, as in the boundary pass: the
+// lanes that own them park their fragments and blend state under their
+// sample number qid, report deferred = true and get their colour from
+// k_fwd_finish.
 static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq,
                                                       bool active, WarpQueue *q, int lane,
-                                                      const HitCache *hc = nullptr) {
+                                                      const HitCache *hc = nullptr,
+                                                      const EdgeRecords *D = nullptr, int qid = 0,
+                                                      bool *deferred = nullptr) {
   int njobs = 0;
   unsigned eq_jobs = 0;
   bool overflow = false, flushed = false;
@@ -487,9 +550,17 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
   LocalFront front(q, lane);
   auto flush = [&](int nf, unsigned res, unsigned eqj) { blend_front(S, st, pt, eq, front, nf, res, eqj, hc); };
   int nf = collect_fragments(S, pt, q, front, lane, njobs, eq, eq_jobs, overflow, flushed, active, flush);
-  warp_solve(S, q, lane, njobs);
+  int npend = warp_decide(S, q, lane, njobs);
+  bool parked = false;
+  if (npend > 0) {
+    bool room = D && park_open_jobs(*D, q, lane, front, nf, active, npend, qid,
+                                    nf | (st.nhit << 8) | ((overflow ? 1 : 0) << 30), st.chunk, st.acc, parked);
+    if (!room) warp_fp64(S, q, lane, npend);
+  }
+  if (deferred) *deferred = parked;
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) flag_error(S, DVG_EFLAG_CAPACITY);
+  if (parked) return F4(0, 0, 0, 0);
   // the final blend in line (the flushes call blend_front)
   blend_run(S, st, pt, eq, [&](int i) { return front[i]; }, nf, q->result[lane], eq_jobs, hc);
   float4 c = blend_finish(st, bg, eq, hc);
@@ -508,7 +579,6 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
 static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const EdgeRecords &E, const float4 *bg,
                                                        v2 screen_pt, EdgeQ *eq, bool active, WarpQueue *q, int lane,
                                                        int qid, bool &deferred) {
-  const unsigned full = 0xffffffffu;
   int njobs = 0;
   unsigned eq_jobs = 0;
   bool overflow = false, flushed = false;
@@ -522,52 +592,9 @@ static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const
   int nf = collect_fragments(S, pt, q, front, lane, njobs, eq, eq_jobs, overflow, flushed, active, flush);
   int npend = warp_decide(S, q, lane, njobs);
   deferred = false;
-  if (npend > 0) {
-    bool mine = active && ((q->pend_lanes >> lane) & 1u);
-    // room for the deferring lanes' fragments, then for the warp's jobs
-    int nfr = mine ? nf : 0, incl = nfr;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int v = __shfl_up_sync(full, incl, o);
-      if (lane >= o) incl += v;
-    }
-    int fbase = 0, jbase = 0;
-    if (lane == 31) fbase = atomicAdd(&E.counts[2], incl);
-    fbase = __shfl_sync(full, fbase, 31);
-    bool room = (long long)fbase + __shfl_sync(full, incl, 31) <= E.frag_cap;
-    if (room) {
-      if (lane == 0) jbase = atomicAdd(&E.counts[0], npend);
-      jbase = __shfl_sync(full, jbase, 0);
-      if ((long long)jbase + npend > E.job_cap) {
-        room = false;
-        for (int k = jbase + lane; k < E.job_cap && k < jbase + npend; k += 32) E.job_a[k].x = -1;
-      }
-    }
-    if (room) {
-      int qbase = qid - lane;  // the warp's queries are consecutive
-      #pragma unroll 1
-      for (int k = lane; k < npend; k += 32) {
-        int owner, idx;
-        SegJob jb = warp_job(q, q->pend[k], owner, idx);
-        E.job_a[jbase + k] = make_int4(qbase + owner, idx, jb.shape, jb.seg);
-        E.job_b[jbase + k] = F4(jb.x, jb.y, jb.r, 0.f);
-      }
-      if (mine) {
-        int f0 = fbase + incl - nfr;
-        for (int i = 0; i < nf; i++) {
-          FragRef fr = front[i];
-          E.frag[f0 + i] = make_int2(fr.key, fr.meta);
-        }
-        E.dq[qid] = make_int4(f0, dq_state(nf, st, eq->hit), (int)q->result[lane], (int)eq_jobs);
-        E.dq_res[qid] = 0u;
-        E.dq_col[qid] = st.acc;
-        deferred = true;
-      }
-      __syncwarp();
-    } else {
-      warp_fp64(S, q, lane, npend);
-    }
-  }
+  if (npend > 0 && !park_open_jobs(E, q, lane, front, nf, active, npend, qid, dq_state(nf, st, eq->hit),
+                                   (int)eq_jobs, st.acc, deferred))
+    warp_fp64(S, q, lane, npend);
   if (!active) return F4(0, 0, 0, 0);
   if (overflow) flag_error(S, DVG_EFLAG_CAPACITY);
   if (deferred) return F4(0, 0, 0, 0);
