@@ -775,6 +775,33 @@ def run_served(dev, rates=(2.0, 8.0, 32.0), num_requests=8, step_range=(100, 500
                                  'requests': st['requests'], 'ticks': st['ticks']}
         all_scenes += scenes
         all_reqs += reqs
+    # the highest rate again with no fragment cache: the same requests, each
+    # holding less device memory, with a backward that recomputes its
+    # fragment lists
+    rate = rates[-1]
+    gen = torch.Generator().manual_seed(7 + len(rates) - 1)
+    gaps = torch.empty(num_requests).exponential_(rate, generator=gen).tolist()
+    kw = [dict(seed=sp['seed']) for (_, _, _, _, _, sp) in scenes]
+    on = [serve.Request(dvg.RenderFunction.serialize_scene(w, h, shapes, groups), target, sp['steps'], **k)
+          for (w, h, shapes, groups, target, sp), k in zip(scenes, kw)]
+    off = [serve.Request(dvg.RenderFunction.serialize_scene(w, h, shapes, groups), target, sp['steps'],
+                         fragment_cache=False, **k) for (w, h, shapes, groups, target, sp), k in zip(scenes, kw)]
+    srv = serve.Server(device=dev, memory_budget=150 * 10 ** 9)
+    t = time.perf_counter()
+    for r, g in zip(off, gaps):
+        t += g
+        r.arrival = t
+        srv.submit(r)
+    srv.run()
+    st = srv.stats()
+    cache_off = {'rate_per_s': rate, 'p50_step_ms': round(st['p50_step_ms'], 3),
+                 'p99_step_ms': round(st['p99_step_ms'], 3), 'steps_per_s': round(st['steps_per_s'], 2),
+                 'steps': st['steps'],
+                 'mean_request_bytes': int(sum(r.device_bytes() for r in off) / len(off)),
+                 'mean_request_bytes_with_cache': int(sum(r.device_bytes() for r in on) / len(on)),
+                 'max_rel_loss_diff_vs_cache': float('%.3g' % max(
+                     abs(a.losses[-1] - b.losses[-1]) / max(abs(b.losses[-1]), 1e-12)
+                     for a, b in zip(off, reqs)))}
     # plain per-call path, one request at a time: a warm-up step (packing,
     # scene handle), then plain_steps timed steps; the loss of step
     # plain_steps + 1 is compared with the served request's
@@ -821,6 +848,7 @@ def run_served(dev, rates=(2.0, 8.0, 32.0), num_requests=8, step_range=(100, 500
             'plain_steps_per_s': round(plain_sps, 2),
             'speedup_vs_plain': {r: round(v['steps_per_s'] / plain_sps, 2) for r, v in per_rate.items()},
             'best_speedup_vs_plain': round(best / plain_sps, 2),
+            'fragment_cache_off': cache_off,
             'equal_error_check': {'step': plain_steps + 1, 'requests': len(rel),
                                   'max_rel_loss_diff': float('%.3g' % max(rel))}}
 

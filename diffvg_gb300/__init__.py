@@ -14,7 +14,8 @@ from .shape import Circle, Ellipse, Path, Polygon, Rect, ShapeGroup, from_svg_pa
 from .color import LinearGradient, RadialGradient
 from .pixel_filter import PixelFilter
 from .diffvg import ShapeType, ColorType, FilterType
-from .render_pytorch import RenderFunction, OutputType, set_print_timing, clear_scene_cache, fuse_parameters
+from .render_pytorch import (RenderFunction, OutputType, set_print_timing, clear_scene_cache, fuse_parameters,
+                             set_fragment_cache, get_fragment_cache)
 from .parse_svg import svg_to_scene
 from .save_svg import save_svg
 from .image import imwrite

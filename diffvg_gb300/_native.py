@@ -24,6 +24,7 @@ DVG_ERR_SCENE = -5
 
 DVG_FLAG_NO_SYNC = 1
 DVG_FLAG_REUSE_PREP = 2
+DVG_FLAG_NO_FRAG_CACHE = 4
 
 EXPORTS = ('dvg_scene_create', 'dvg_scene_destroy', 'dvg_scene_update_params', 'dvg_render_forward',
            'dvg_render_backward',

@@ -59,7 +59,7 @@ class BatchedScenes:
 
     def __init__(self, scene_args, num_samples=(2, 2), seeds=None, sizes=None, targets=None, lr=1e-2,
                  betas=(0.9, 0.999), eps=1e-8, trainable=DEFAULT_TRAINABLE, streams=8, check_every=16,
-                 device=None, mode='streams', tuning=(2, 1)):
+                 device=None, mode='streams', tuning=(2, 1), fragment_cache=True):
         self.device = device or torch.device('cuda', torch.cuda.current_device())
         self.nsx, self.nsy = num_samples
         self.packed = [pack_scene(a) for a in scene_args]
@@ -68,6 +68,9 @@ class BatchedScenes:
         self.sizes = list(sizes) if sizes is not None else [(p.canvas_width, p.canvas_height) for p in self.packed]
         self.lr, self.betas, self.eps = float(lr), betas, float(eps)
         self.check_every = check_every
+        # False: no per-sample fragment cache between a scene's forward and
+        # backward (the backward recomputes the fragment lists)
+        self.fragment_cache = bool(fragment_cache)
         with torch.cuda.device(self.device):
             self.scenes = [_native.NativeScene(p) for p in self.packed]
         self.offsets = []
@@ -123,6 +126,8 @@ class BatchedScenes:
         return self.params[self.offsets[i]:self.offsets[i] + self.packed[i].num_params]
 
     def _args(self, i, flags, params=None):
+        if not self.fragment_cache:
+            flags |= _native.DVG_FLAG_NO_FRAG_CACHE
         w, h = self.sizes[i]
         p = self.scene_params(i) if params is None else params
         return _native.RenderArgs(w, h, self.nsx, self.nsy, int(self.seeds[i]) & (2 ** 64 - 1),

@@ -815,8 +815,9 @@ int dvg_render_forward(DvgScene *sc, const DvgRenderArgs *a, float *image, float
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   size_t npx = (size_t)a->width * a->height, n = npx * a->num_samples_x * a->num_samples_y;
   sc->hit_live = false;
-  bool cache = image != nullptr;
+  bool cache = image != nullptr && !(a->flags & DVG_FLAG_NO_FRAG_CACHE);
   bool pf = a->use_prefiltering != 0;
+  if (image && !cache) sc->hits.release();
   cudaError_t e = sc->weight.ensure(npx * sizeof(float));
   if (e == cudaSuccess && image) e = sc->samples.ensure(n * sizeof(float4));
   if (e == cudaSuccess && cache) e = sc->hits.ensure(hit_bytes(sc, n, pf));
@@ -1142,8 +1143,10 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
       continue;
     }
     e = sc->weight.ensure(npx * sizeof(float));
+    bool cache = !(a->flags & DVG_FLAG_NO_FRAG_CACHE);
+    if (!cache) sc->hits.release();
     if (e == cudaSuccess) e = sc->samples.ensure(ns * sizeof(float4));
-    if (e == cudaSuccess) e = sc->hits.ensure(hit_bytes(sc, ns, false));
+    if (e == cudaSuccess && cache) e = sc->hits.ensure(hit_bytes(sc, ns, false));
     if (e != cudaSuccess) return cuda_fail(e, "allocating image arenas");
     BatchScene &bs = hb[live.size()];
     bs.S = make_dev(sc, a->params);
@@ -1151,10 +1154,12 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
     ai.flags |= DVG_FLAG_NO_SYNC;  // failures stay latched in the scene (dvg_scene_sync)
     if ((st = prepare(sc, bs.S, &ai, ls)) != DVG_OK) return st;
     bs.R = make_render(sc, a);
-    HitArena h = hit_arena(sc, ns, false);
-    set_hit_cache(bs.R, h, false);
-    e = cudaMemsetAsync(h.chunk_count, 0, sizeof(int), ls);
-    if (e != cudaSuccess) return cuda_fail(e, "batched forward");
+    if (cache) {
+      HitArena h = hit_arena(sc, ns, false);
+      set_hit_cache(bs.R, h, false);
+      e = cudaMemsetAsync(h.chunk_count, 0, sizeof(int), ls);
+      if (e != cudaSuccess) return cuda_fail(e, "batched forward");
+    }
     bs.E = EdgeRecords{};
     bs.samples = reinterpret_cast<float4 *>(sc->samples.ptr);
     dvg::launch_weight(bs.S, bs.R, ls);
@@ -1178,6 +1183,7 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
     cudaStream_t ls = b->lane(k);
     size_t ns = (size_t)a->width * a->height * a->num_samples_x * a->num_samples_y;
     dvg::launch_resolve(hb[k].R, hb[k].samples, images[i], ls);
+    if (a->flags & DVG_FLAG_NO_FRAG_CACHE) continue;
     HitArena h = hit_arena(sc, ns, false);
     if (sc->d.num_params > 0)
       e = cudaMemcpyAsync(h.params, a->params, (size_t)sc->d.num_params * sizeof(float), cudaMemcpyDeviceToDevice, ls);

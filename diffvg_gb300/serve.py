@@ -82,8 +82,9 @@ def mean_depth(packed):
     return area / (W * H)
 
 
-def estimate_device_bytes(packed, width, height, spp):
-    """Device bytes a request holds while resident."""
+def estimate_device_bytes(packed, width, height, spp, fragment_cache=True):
+    """Device bytes a request holds while resident (without the per-sample
+    fragment cache when `fragment_cache` is False)."""
     npx, n = width * height, width * height * spp
     P = max(packed.num_params, 1)
     nseg, ns, ng = packed.segment_ctrl.size, packed.num_shapes, packed.num_groups
@@ -101,7 +102,8 @@ def estimate_device_bytes(packed, width, height, spp):
         cache = 16 * 64 + 4 + int(1028 * min(3.0, max(1.0 / 16.0, ask)) + 0.5)
     else:
         cache = 16 * 4 + 4 + int(68 * min(15.0, max(0.5, ask)) + 0.5)
-    samples = 16 * n + (cache + 2 + 4) * n
+    cache = cache + 2 if fragment_cache else 0
+    samples = 16 * n + (cache + 4) * n
     edges = 68 * n                                  # boundary-sample records and ordering
     if ng >= 8:  # deferred fp64 walks: jobs, per-query state and colours, fragments, deferred samples
         edges += 32 * n + 2 * (16 + 4 + 16) * n + 4 * 8 * n + 4 * n
@@ -117,7 +119,7 @@ class Request:
     _ids = 0
 
     def __init__(self, scene_args, target, steps, num_samples=(2, 2), seed=0, lr=1e-2, betas=(0.9, 0.999),
-                 eps=1e-8, trainable=DEFAULT_TRAINABLE, size=None, arrival=None):
+                 eps=1e-8, trainable=DEFAULT_TRAINABLE, size=None, arrival=None, fragment_cache=True):
         Request._ids += 1
         self.id = Request._ids
         self.scene_args = scene_args
@@ -127,6 +129,10 @@ class Request:
         self.seed = seed
         self.lr, self.betas, self.eps = lr, betas, eps
         self.trainable = trainable
+        # False: the forward keeps no per-sample fragment cache and the
+        # backward recomputes each sample's fragment list (less memory per
+        # request, a slower backward)
+        self.fragment_cache = bool(fragment_cache)
         self.packed = pack_scene(scene_args)
         self.size = size or (self.packed.canvas_width, self.packed.canvas_height)
         self.arrival = arrival
@@ -148,7 +154,7 @@ class Request:
 
     def device_bytes(self):
         return estimate_device_bytes(self.packed, self.size[0], self.size[1],
-                                     self.num_samples[0] * self.num_samples[1])
+                                     self.num_samples[0] * self.num_samples[1], self.fragment_cache)
 
 
 class Slot:
@@ -181,6 +187,8 @@ class Slot:
         self._capture()
 
     def _args(self, flags):
+        if not self.req.fragment_cache:
+            flags |= _native.DVG_FLAG_NO_FRAG_CACHE
         w, h = self.req.size
         nsx, nsy = self.req.num_samples
         return _native.RenderArgs(w, h, nsx, nsy, int(self.req.seed) & (2 ** 64 - 1),

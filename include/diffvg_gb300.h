@@ -137,9 +137,16 @@ typedef struct DvgRenderArgs {
  * DVG_FLAG_REUSE_PREP: the parameter values are those of the previous call
  *   on this scene, so the derived scene data (boxes, CDFs, tile lists) is
  *   reused instead of recomputed (the autograd backward right after its
- *   forward). */
+ *   forward).
+ * DVG_FLAG_NO_FRAG_CACHE: the forward keeps no per-sample fragment cache
+ *   (about 110 B per sample, 1.1 KB per sample with prefiltering, plus
+ *   chunks for samples deeper than 16 fragments) and frees the one the scene
+ *   holds; the following backward recomputes each sample's fragment list, as
+ *   the reference does (diffvg.cpp:605-705).  Same results, less memory, a
+ *   slower backward. */
 #define DVG_FLAG_NO_SYNC 1
 #define DVG_FLAG_REUSE_PREP 2
+#define DVG_FLAG_NO_FRAG_CACHE 4
 
 typedef struct DvgScene DvgScene;
 

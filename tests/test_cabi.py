@@ -36,6 +36,19 @@ def test_library_exports_every_declared_symbol():
     assert set(_native.EXPORTS) <= set(declared_functions())
 
 
+def test_binding_constants_match_the_header():
+    """Every DVG_FLAG_* / DVG_OK / DVG_ERR_* value of the header has the same
+    value in the ctypes binding."""
+    src = open(os.path.join(ROOT, 'include', 'diffvg_gb300.h')).read()
+    defs = dict(re.findall(r'#define\s+(DVG_(?:FLAG|ERR)_[A-Z_0-9]+|DVG_OK)\s+\(?(-?\d+)\)?', src))
+    assert 'DVG_FLAG_NO_FRAG_CACHE' in defs
+    for name, val in defs.items():
+        if hasattr(_native, name):
+            assert getattr(_native, name) == int(val), name
+    for name in ('DVG_FLAG_NO_SYNC', 'DVG_FLAG_REUSE_PREP', 'DVG_FLAG_NO_FRAG_CACHE'):
+        assert getattr(_native, name) == int(defs[name])
+
+
 def test_version_and_error_strings_without_gpu():
     lib = _native.load()
     assert b'sm_103a' in lib.dvg_version()

@@ -87,6 +87,23 @@ def test_estimate_counts_the_prefiltered_fragment_cache():
     assert diff == (16 * 64 + 64 - (16 * 4 + 34)) * n
 
 
+def test_estimate_without_the_fragment_cache():
+    """A request that keeps no fragment cache saves, per sample, the 16 keys,
+    the first-chunk index, the count and the chunks; the prefiltered one the 16
+    fragments, the index, the count and its chunks."""
+    from diffvg_gb300.packing import pack_scene
+    w, h, shapes, groups = workloads.fill_scene(dvg, seed=3, num_paths=8, canvas=128)
+    for pf, per in ((False, 16 * 4 + 4 + 34 + 2), (True, 16 * 64 + 4 + 64 + 2)):
+        p = pack_scene(dvg.RenderFunction.serialize_scene(w, h, shapes, groups, use_prefiltering=pf))
+        on = serve.estimate_device_bytes(p, w, h, 1)
+        off = serve.estimate_device_bytes(p, w, h, 1, fragment_cache=False)
+        assert on - off == per * w * h
+    args = dvg.RenderFunction.serialize_scene(w, h, shapes, groups)
+    r_on = serve.Request(args, torch.zeros(h, w, 4), 1)
+    r_off = serve.Request(args, torch.zeros(h, w, 4), 1, fragment_cache=False)
+    assert r_off.device_bytes() < r_on.device_bytes()
+
+
 def test_budget_serialises_requests_and_all_complete(server):
     reqs = [_req(i, 64, 8, 3) for i in range(4)]
     s = server(budget=int(reqs[0].device_bytes() * 1.5))
