@@ -799,9 +799,12 @@ def run_served(dev, rates=(2.0, 8.0, 32.0), num_requests=8, step_range=(100, 500
                  'steps': st['steps'],
                  'mean_request_bytes': int(sum(r.device_bytes() for r in off) / len(off)),
                  'mean_request_bytes_with_cache': int(sum(r.device_bytes() for r in on) / len(on)),
+                 # the same request with and without the cache, at step plain_steps + 1 (the
+                 # trajectories then part by the order of the atomic sums, as any two runs do)
                  'max_rel_loss_diff_vs_cache': float('%.3g' % max(
-                     abs(a.losses[-1] - b.losses[-1]) / max(abs(b.losses[-1]), 1e-12)
-                     for a, b in zip(off, reqs)))}
+                     abs(a.losses[plain_steps] - b.losses[plain_steps]) / max(abs(b.losses[plain_steps]), 1e-12)
+                     for a, b in zip(off, reqs))),
+                 'loss_diff_step': plain_steps + 1}
     # plain per-call path, one request at a time: a warm-up step (packing,
     # scene handle), then plain_steps timed steps; the loss of step
     # plain_steps + 1 is compared with the served request's

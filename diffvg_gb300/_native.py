@@ -1,4 +1,8 @@
-"""ctypes binding of libdiffvg_gb300.so (include/diffvg_gb300.h).
+"""Bindings of libdiffvg_gb300.so (include/diffvg_gb300.h): the PyTorch
+operators of libdvg_torch.so (torch.ops.diffvg_gb300, csrc/dvg_torch.cpp),
+which take tensors and the current CUDA stream, and a ctypes binding of the
+same C ABI for the pointer-level calls (batches, serving slots, the C-ABI
+measurements and tests).
 
 The library is the only implementation of the render path: there is no CPU
 fallback, and loading fails loudly when the library is missing or when no
@@ -146,6 +150,31 @@ def load(build_if_missing=True):
         return lib
 
 
+_ops = None
+
+
+def ops():
+    """torch.ops.diffvg_gb300: the PyTorch operators over the C ABI, loaded
+    after (and linked against) libdiffvg_gb300.so."""
+    global _ops
+    if _ops is None:
+        load()
+        import torch
+        with _lock:
+            if _ops is None:
+                if not os.path.exists(_build.TORCH_LIB_PATH):
+                    raise RuntimeError('libdvg_torch.so is not built (run diffvg_gb300.build.build())')
+                torch.ops.load_library(_build.TORCH_LIB_PATH)
+                _ops = torch.ops.diffvg_gb300
+    return _ops
+
+
+def _i64(seed):
+    """A uint64 seed as the int64 with the same bits."""
+    seed = int(seed) & (2 ** 64 - 1)
+    return seed - 2 ** 64 if seed >= 2 ** 63 else seed
+
+
 def check(status):
     if status == DVG_OK:
         return
@@ -163,27 +192,42 @@ class NativeScene:
     """Owns a DvgScene handle: the resident topology of a packed scene."""
 
     def __init__(self, packed):
+        import torch
         lib = load()
         self._lib = lib
-        si = np.ascontiguousarray(packed.shape_info.reshape(-1), dtype=np.int32)
-        sc = np.ascontiguousarray(packed.segment_ctrl, dtype=np.int32)
-        gi = np.ascontiguousarray(packed.group_info.reshape(-1), dtype=np.int32)
-        gs = np.ascontiguousarray(packed.group_shapes, dtype=np.int32)
-        keep = [np.zeros(1, np.int32) if x.size == 0 else x for x in (si, sc, gi, gs)]
-        desc = SceneDesc(packed.canvas_width, packed.canvas_height, packed.num_shapes, packed.num_groups,
-                         max(packed.num_params, 1), int(sc.size), int(gs.size), int(packed.filter_type),
-                         int(packed.filter_radius_off),
-                         keep[0].ctypes.data_as(_IP), keep[1].ctypes.data_as(_IP),
-                         keep[2].ctypes.data_as(_IP), keep[3].ctypes.data_as(_IP))
-        h = ctypes.c_void_p()
-        check(lib.dvg_scene_create(ctypes.byref(desc), ctypes.byref(h)))
-        self.handle = h
+        self._ops = ops()
+        arrays = [np.ascontiguousarray(x, dtype=np.int32).reshape(-1)
+                  for x in (packed.shape_info, packed.segment_ctrl, packed.group_info, packed.group_shapes)]
+        sizes = [int(x.size) for x in arrays]
+        t = [torch.from_numpy(np.zeros(1, np.int32) if x.size == 0 else x) for x in arrays]
+        if sizes[1] == 0:  # the descriptor's segment and group-shape counts are the arrays' real sizes
+            t[1] = t[1][:0]
+        if sizes[3] == 0:
+            t[3] = t[3][:0]
+        st, h = self._ops.scene_create(t[0], t[1], t[2], t[3],
+                                       [packed.canvas_width, packed.canvas_height, packed.num_shapes,
+                                        packed.num_groups, max(packed.num_params, 1), int(packed.filter_type),
+                                        int(packed.filter_radius_off)])
+        check(st)
+        self.handle = ctypes.c_void_p(h)
         self.num_params = max(packed.num_params, 1)
 
     def close(self):
         if getattr(self, 'handle', None):
             self._lib.dvg_scene_destroy(self.handle)
             self.handle = None
+
+    # tensor-level calls through the PyTorch operators (current CUDA stream);
+    # dims = [width, height, num_samples_x, num_samples_y, use_prefiltering]
+    def render_forward(self, dims, seed, flags=0, params=None, background=None, eval_positions=None, image=None,
+                       sdf=None):
+        check(self._ops.render_forward(self.handle.value, params, background, eval_positions, image, sdf, dims,
+                                       _i64(seed), int(flags)))
+
+    def render_backward(self, dims, seed, d_params, flags=0, params=None, background=None, eval_positions=None,
+                        d_image=None, d_sdf=None, d_background=None, d_translation=None):
+        check(self._ops.render_backward(self.handle.value, params, background, eval_positions, d_image, d_sdf,
+                                        d_params, d_background, d_translation, dims, _i64(seed), int(flags)))
 
     def __del__(self):
         try:

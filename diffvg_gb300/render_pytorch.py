@@ -134,12 +134,9 @@ def _background(background_image, height, width, device, strict=True):
     return bg
 
 
-def _render_args(packed, width, height, nsx, nsy, seed, arena, bg, eval_positions, flags=0):
-    n_eval = 0 if eval_positions is None else int(eval_positions.shape[0])
-    return _native.RenderArgs(int(width), int(height), int(nsx), int(nsy), int(seed) & (2 ** 64 - 1),
-                              1 if packed.use_prefiltering else 0, n_eval, arena.data_ptr(),
-                              None if bg is None else bg.data_ptr(),
-                              None if n_eval == 0 else eval_positions.data_ptr(), int(flags))
+def _dims(packed, width, height, nsx, nsy):
+    """The dims argument of the torch.ops.diffvg_gb300 render operators."""
+    return [int(width), int(height), int(nsx), int(nsy), 1 if packed.use_prefiltering else 0]
 
 
 def _eval_positions(packed, device):
@@ -281,15 +278,12 @@ class RenderFunction(torch.autograd.Function):
         bg = _background(background_image, height, width, device, strict=False)
         d_translation = torch.zeros(height, width, 2, device=device)
         d_arena = torch.zeros(max(packed.num_params, 1), device=device)
-        rargs = _render_args(packed, width, height, num_samples_x, num_samples_y, seed, arena, bg, ev)
-        stream = torch.cuda.current_stream(device).cuda_stream
+        dims = _dims(packed, width, height, num_samples_x, num_samples_y)
+        color = packed.output_type == OutputType.color
         with torch.cuda.device(device):
-            if packed.output_type == OutputType.color:
-                scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
-                               d_translation_ptr=d_translation.data_ptr(), stream=stream)
-            else:
-                scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
-                               d_translation_ptr=d_translation.data_ptr(), stream=stream)
+            scene.render_backward(dims, seed, d_arena, params=arena, background=bg, eval_positions=ev,
+                                  d_image=grad if color else None, d_sdf=None if color else grad,
+                                  d_translation=d_translation)
         scene.last_token = None
         return d_translation
 
@@ -417,13 +411,11 @@ def _render_forward(ctx, call, background_image):
         raise ValueError('scene parameters contain a non-finite value')
     token = next(_token)
     flags = 0 if _fragment_cache else _native.DVG_FLAG_NO_FRAG_CACHE
-    rargs = _render_args(packed, width, height, num_samples_x, num_samples_y, seed, arena, bg, ev, flags)
-    stream = torch.cuda.current_stream(device).cuda_stream
+    dims = _dims(packed, width, height, num_samples_x, num_samples_y)
+    color = packed.output_type == OutputType.color
     with torch.cuda.device(device):
-        if packed.output_type == OutputType.color:
-            scene.forward(rargs, image_ptr=out.data_ptr(), stream=stream)
-        else:
-            scene.forward(rargs, sdf_ptr=out.data_ptr(), stream=stream)
+        scene.render_forward(dims, seed, flags, params=arena, background=bg, eval_positions=ev,
+                             image=out if color else None, sdf=None if color else out)
     scene.last_token = token
     ctx.packed = packed
     ctx.scene = scene
@@ -456,14 +448,14 @@ def _render_backward(ctx, grad_img):
     reuse = _native.DVG_FLAG_REUSE_PREP if scene.last_token == ctx.token else 0
     stream = torch.cuda.current_stream(device).cuda_stream
 
+    dims = _dims(packed, width, height, nsx, nsy)
+    color = packed.output_type == OutputType.color
+
     def launch(flags):
-        rargs = _render_args(packed, width, height, nsx, nsy, seed, ctx.arena, bg, ctx.eval_positions, flags)
         with torch.cuda.device(device):
-            if packed.output_type == OutputType.color:
-                scene.backward(rargs, d_image_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(),
-                               d_background_ptr=None if d_bg is None else d_bg.data_ptr(), stream=stream)
-            else:
-                scene.backward(rargs, d_sdf_ptr=grad.data_ptr(), d_params_ptr=d_arena.data_ptr(), stream=stream)
+            scene.render_backward(dims, seed, d_arena, flags, params=ctx.arena, background=bg,
+                                  eval_positions=ctx.eval_positions, d_image=grad if color else None,
+                                  d_sdf=None if color else grad, d_background=d_bg if color else None)
 
     # the kernels run while the host lays out the gradient views; the
     # status is checked once the gradient has been read back

@@ -1,0 +1,64 @@
+"""The PyTorch operators over the C ABI (torch.ops.diffvg_gb300,
+diffvg_gb300/csrc/dvg_torch.cpp): registration, host-side argument checks
+and status codes, all without a GPU."""
+import pytest
+import torch
+
+from diffvg_gb300 import _native
+
+OPS = {
+    'scene_create': 'scene_create(Tensor shape_info, Tensor segment_ctrl, Tensor group_info, Tensor group_shapes, '
+                    'int[] dims) -> (int, int)',
+    'scene_destroy': 'scene_destroy(int scene) -> int',
+    'render_forward': 'render_forward(int scene, Tensor? params, Tensor? background, Tensor? eval_positions, '
+                      'Tensor(a!)? image, Tensor(b!)? sdf, int[] dims, int seed, int flags) -> int',
+    'render_backward': 'render_backward(int scene, Tensor? params, Tensor? background, Tensor? eval_positions, '
+                       'Tensor? d_image, Tensor? d_sdf, Tensor(a!) d_params, Tensor(b!)? d_background, '
+                       'Tensor(c!)? d_translation, int[] dims, int seed, int flags) -> int',
+    'scene_update_params': 'scene_update_params(int scene, Tensor params) -> int',
+    'scene_sync': 'scene_sync(int scene, int device) -> int',
+}
+
+
+def test_operators_are_registered_with_their_schemas():
+    ops = _native.ops()
+    for name, schema in OPS.items():
+        assert str(getattr(ops, name).default._schema) == 'diffvg_gb300::' + schema
+
+
+def test_scene_create_reports_a_malformed_description_without_touching_the_device():
+    ops = _native.ops()
+    z = torch.zeros(1, dtype=torch.int32)
+    st, handle = ops.scene_create(z, z[:0], z, z[:0], [0, 16, 0, 0, 1, 0, 0])  # canvas width 0
+    assert st == _native.DVG_ERR_INVALID and handle == 0
+    assert b'canvas' in _native.load().dvg_last_error()
+
+
+def test_scene_create_takes_int32_cpu_topology_only():
+    ops = _native.ops()
+    z = torch.zeros(1, dtype=torch.int64)
+    with pytest.raises(RuntimeError, match='int32 CPU'):
+        ops.scene_create(z, z, z, z, [16, 16, 0, 0, 1, 0, 0])
+
+
+def test_render_operators_check_tensors_before_the_call():
+    """Wrong device, dtype or size fails in the operator, before the C ABI
+    sees any pointer (the scene handle 0 is never used)."""
+    ops = _native.ops()
+    dims = [8, 8, 1, 1, 0]
+    cpu = torch.zeros(8, 8, 4)
+    with pytest.raises(RuntimeError, match='CUDA'):
+        ops.render_forward(0, None, None, None, cpu, None, dims, 0, 0)
+    with pytest.raises(RuntimeError, match='exactly one of image / sdf'):
+        ops.render_forward(0, None, None, None, None, None, dims, 0, 0)
+    with pytest.raises(RuntimeError, match='dims'):
+        ops.render_forward(0, None, None, None, cpu, None, [8, 8], 0, 0)
+    with pytest.raises(RuntimeError, match='exactly one of d_image / d_sdf'):
+        ops.render_backward(0, None, None, None, None, None, torch.zeros(4), None, None, dims, 0, 0)
+
+
+def test_seeds_keep_their_64_bits():
+    assert _native._i64(0) == 0
+    assert _native._i64(2 ** 63) == -2 ** 63
+    assert _native._i64(2 ** 64 - 1) == -1
+    assert _native._i64(-1) == -1
