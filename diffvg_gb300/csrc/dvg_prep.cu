@@ -6,9 +6,10 @@
 // that depends on the parameter values is derived by these kernels from the
 // parameter arena, so an optimisation step never leaves the GPU:
 //   k_group_xform   canvas_to_shape = inverse(shape_to_canvas)   (shape.h:123)
-//   k_shape_prep    shape / segment boxes and stroke radii, the per-path
+//   k_shape_prep    boxes and boundary lengths of circles, ellipses, rects
+//   k_path_prep     path and segment boxes and stroke radii, the per-path
 //                   segment visiting order, boundary lengths and per-path
-//                   segment CDFs (scene.cpp:113-333, 495-625)
+//                   segment CDFs (scene.cpp:113-333, 495-625), a warp a path
 //   k_group_prep    group boxes, max stroke radius, tile range (scene.cpp:627-684)
 //   k_sampling_cdf  the (group, shape) boundary-length CDF (scene.cpp:207-246)
 //   k_bin_count / k_bin_scan / k_bin_fill
@@ -88,10 +89,120 @@ __device__ void path_leaf_order(const float4 *boxes, int n, int *out, int *scrat
   }
 }
 
+// path_leaf_order with the 32 lanes of a warp (all call it; the same
+// result).  The stable sort by key runs as bottom-up merge passes in which
+// every element finds its place by a binary search in the other run (left
+// elements count the right run's smaller keys, right elements the left
+// run's smaller or equal keys: the stable merge).  The pairing tree depends
+// on n only: its levels are replayed in every lane, each level's nodes are
+// filled by the lanes with their parent links and leaf counts, and a leaf's
+// place in the depth-first visit (child1 before child0) is the sum of the
+// leaf counts of the child1 siblings of the ancestors it reaches through
+// child0.  Keys with a NaN make the order depend on the merge sequence
+// itself: lane 0 then runs path_leaf_order.  scratch holds 10*n + 8 ints.
+__device__ void path_leaf_order_warp(const float4 *boxes, int n, int *out, int *scratch, int lane) {
+  const unsigned full = 0xffffffffu;
+  int *idx = scratch;
+  float *key = reinterpret_cast<float *>(scratch + n);
+  int *tmp = scratch + 2 * n;
+  bool nan = false;
+  for (int i = lane; i < n; i += 32) {
+    float k = 0.5f * (boxes[i].y + boxes[i].w);
+    key[i] = k;
+    idx[i] = i;
+    nan |= !(k == k);
+  }
+  if (__any_sync(full, nan)) {
+    __syncwarp();
+    if (lane == 0) path_leaf_order(boxes, n, out, scratch);
+    __syncwarp();
+    return;
+  }
+  __syncwarp();
+  if (n == 1) {
+    if (lane == 0) out[0] = 0;
+    __syncwarp();
+    return;
+  }
+  int *src = idx, *dst = tmp;
+  for (int w = 1; w < n; w *= 2) {
+    for (int i = lane; i < n; i += 32) {
+      int lo = i / (2 * w) * (2 * w), mid = min(lo + w, n), hi = min(lo + 2 * w, n);
+      int v = src[i];
+      float kv = key[v];
+      int pos;
+      if (i < mid) {  // right-run elements with a smaller key come first
+        int a = mid, b = hi;
+        while (a < b) {
+          int m = (a + b) >> 1;
+          if (key[src[m]] < kv) a = m + 1; else b = m;
+        }
+        pos = i + (a - mid);
+      } else {  // left-run elements with a smaller or equal key come first
+        int a = lo, b = mid;
+        while (a < b) {
+          int m = (a + b) >> 1;
+          if (key[src[m]] <= kv) a = m + 1; else b = m;
+        }
+        pos = lo + (i - mid) + (a - lo);
+      }
+      dst[pos] = v;
+    }
+    __syncwarp();
+    int *t = src; src = dst; dst = t;
+  }
+  // src: the segments in sorted order (sorted position -> segment)
+  int size = 2 * n - 1, root = size - 1;
+  int *c0 = scratch + 3 * n, *c1 = scratch + 5 * n, *par = scratch + 7 * n;
+  // leaf counts of the tree's nodes, over the buffers the sort no longer needs: [n, 3n) when the
+  // sorted order is in idx = [0, n), else [0, 2n) (it is then in tmp = [2n, 3n))
+  int *cnt = src == idx ? scratch + n : scratch;
+  const int *sorted = src;
+  for (int i = lane; i < n; i += 32) cnt[i] = 1;
+  if (lane == 0) par[root] = -1;
+  __syncwarp();
+  int prev_beg = 0, prev_end = n;
+  int leftover = prev_end % 2 == 0 ? -1 : prev_end - 1;
+  for (int guard = 0; guard < 2 * n + 2 && (prev_end - prev_beg >= 1 || leftover != -1); guard++) {
+    int length = (prev_end - prev_beg) / 2;
+    if ((prev_end - prev_beg) % 2 == 1 && leftover != -1 && leftover != prev_end - 1) length += 1;
+    for (int i = lane; i < length; i += 32) {
+      int a = prev_beg + 2 * i, b = prev_beg + 2 * i + 1;
+      if (b >= prev_end) b = leftover;
+      int v = prev_end + i;
+      c0[v] = a;
+      c1[v] = b;
+      par[a] = v;
+      par[b] = v;
+      cnt[v] = cnt[a] + cnt[b];
+    }
+    __syncwarp();
+    if (length > 0 && prev_beg + 2 * (length - 1) + 1 >= prev_end) leftover = -1;
+    if (length == 1 && leftover == -1) break;
+    prev_beg = prev_end;
+    prev_end = prev_beg + length;
+    if (length % 2 == 1 && leftover == -1) leftover = prev_end - 1;
+  }
+  for (int leaf = lane; leaf < n; leaf += 32) {
+    int pos = 0, v = leaf;
+    for (int guard = 0; v != root && guard < size; guard++) {
+      int u = par[v];
+      if (u < 0) break;
+      if (c0[u] == v) pos += cnt[c1[u]];
+      v = u;
+    }
+    out[pos] = sorted[leaf];
+  }
+  __syncwarp();
+}
+
+// Boxes, radii, lengths, CDFs of the non-path shapes (one thread per shape);
+// paths are k_path_prep's.
 __global__ void k_shape_prep(DevScene S) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S.num_shapes) return;
   int kind = SI(S, s, DVG_SHAPE_KIND);
+  if (kind == DVG_PATH) return;
   int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
   const float *p = S.P + po;
   float L = 0.f;
@@ -108,73 +219,107 @@ __global__ void k_shape_prep(DevScene S) {
   } else if (kind == DVG_RECT) {
     S.s_box[s] = F4(p[0], p[1], p[2], p[3]);
     L += 2 * (p[2] - p[0] + p[3] - p[1]);
-  } else {
-    int np = SI(S, s, DVG_SHAPE_NUM_POINTS), nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);
-    int so = SI(S, s, DVG_SHAPE_SEG_OFF), th = SI(S, s, DVG_SHAPE_THICKNESS_OFF);
-    float4 b = box_empty();
-    if (np > 0) { v2 q = path_pt(S, po, 0); b = F4(q.x, q.y, q.x, q.y); }
-    for (int i = 1; i < np; i++) b = box_add(b, path_pt(S, po, i));
-    S.s_box[s] = b;
-    float r = stroke_width(S, s);
-    for (int i = 0; i < nseg; i++) {
-      int nc = S.segment_ctrl[so + i], pid = S.seg_point[so + i];
-      float4 sb = box_empty();
-      float rr = r;
-      for (int k = 0; k <= nc + 1; k++) {
-        int id = (k == nc + 1) ? (pid + k) % np : pid + k;
-        sb = box_add(sb, path_pt(S, po, id));
-        if (th >= 0) {
-          float rk = S.P[th + id];
-          rr = (k == 0) ? rk : rmax(rr, rk);
-        }
-      }
-      S.seg_box[so + i] = sb;
-      S.seg_r[so + i] = rr;
-    }
-    if (nseg > 0) path_leaf_order(S.seg_box + so, nseg, S.seg_order + so, S.scratch + 10 * so + 8 * s);
-    float len = 0.f;
-    for (int i = 0; i < nseg; i++) {
-      int nc = S.segment_ctrl[so + i], i0 = S.seg_point[so + i];
-      if (nc == 0) {
-        len += dist2(path_pt(S, po, (i0 + 1) % np), path_pt(S, po, i0));
-      } else if (nc == 1) {
-        v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, (i0 + 2) % np);
-        v2 v1 = eval_quad(p0, p1, p2, 0.5f);
-        len += dist2(v1, p0) + dist2(v1, p2);
-      } else {
-        v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, i0 + 2),
-           p3 = path_pt(S, po, (i0 + 3) % np);
-        v2 v1 = eval_cubic(p0, p1, p2, p3, 1.f / 3.f), v2_ = eval_cubic(p0, p1, p2, p3, 2.f / 3.f);
-        len += dist2(v1, p0) + dist2(v1, v2_) + dist2(v2_, p3);
-      }
-    }
-    L += len;
-    float inv = 1.f / L;
-    float cdf = 0.f;
-    for (int i = 0; i < nseg; i++) {
-      int nc = S.segment_ctrl[so + i], i0 = S.seg_point[so + i];
-      float dd;
-      if (nc == 0) {
-        dd = dist2(path_pt(S, po, i0), path_pt(S, po, (i0 + 1) % np)) * inv;
-      } else if (nc == 1) {
-        v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, (i0 + 2) % np);
-        v2 v1 = eval_quad(p0, p1, p2, 0.5f);
-        dd = (dist2(p0, v1) + dist2(v1, p2)) * inv;
-      } else {
-        v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, i0 + 2),
-           p3 = path_pt(S, po, (i0 + 3) % np);
-        v2 v1 = eval_cubic(p0, p1, p2, p3, 1.f / 3.f), v2_ = eval_cubic(p0, p1, p2, p3, 2.f / 3.f);
-        dd = (dist2(v1, p0) + dist2(v1, v2_) + dist2(v2_, p3)) * inv;
-      }
-      S.seg_pmf[so + i] = dd;
-      cdf = (i == 0) ? dd : dd + cdf;
-      S.seg_cdf[so + i] = cdf;
-    }
   }
   S.s_length[s] = L;
 }
 
-// y-band segment lists of the long paths (one thread per path): the path's
+// Path shapes (one warp per path): the shape box, each segment's box and
+// stroke radius, the segments' visiting order, the boundary length and the
+// per-segment length CDF (scene.cpp:113-333, 495-625).  Lanes work on
+// segments; the sums whose rounding depends on their order (the length and
+// the CDF) run in segment order in lane 0, so every value is the one a
+// sequential pass forms.
+__global__ void k_path_prep(DevScene S) {
+  const unsigned full = 0xffffffffu;
+  int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (s >= S.num_shapes || SI(S, s, DVG_SHAPE_KIND) != DVG_PATH) return;
+  int po = SI(S, s, DVG_SHAPE_PARAM_OFF);
+  int np = SI(S, s, DVG_SHAPE_NUM_POINTS), nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);
+  int so = SI(S, s, DVG_SHAPE_SEG_OFF), th = SI(S, s, DVG_SHAPE_THICKNESS_OFF);
+  // shape box: point 0, grown by the others (box_add skips a NaN point once the box is a number, so
+  // the NaN-skipping extremes of points 1.. give the sequential result)
+  float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  for (int i = 1 + lane; i < np; i += 32) {
+    v2 q = path_pt(S, po, i);
+    mnx = fminf(mnx, q.x);
+    mny = fminf(mny, q.y);
+    mxx = fmaxf(mxx, q.x);
+    mxy = fmaxf(mxy, q.y);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = fminf(mnx, __shfl_xor_sync(full, mnx, o));
+    mny = fminf(mny, __shfl_xor_sync(full, mny, o));
+    mxx = fmaxf(mxx, __shfl_xor_sync(full, mxx, o));
+    mxy = fmaxf(mxy, __shfl_xor_sync(full, mxy, o));
+  }
+  if (lane == 0) {
+    float4 b = box_empty();
+    if (np > 0) {
+      v2 q = path_pt(S, po, 0);
+      b = F4(rmin(mnx, q.x), rmin(mny, q.y), rmax(mxx, q.x), rmax(mxy, q.y));
+    }
+    S.s_box[s] = b;
+  }
+  float r = stroke_width(S, s);
+  for (int i = lane; i < nseg; i += 32) {
+    int nc = S.segment_ctrl[so + i], pid = S.seg_point[so + i];
+    float4 sb = box_empty();
+    float rr = r;
+    for (int k = 0; k <= nc + 1; k++) {
+      int id = (k == nc + 1) ? (pid + k) % np : pid + k;
+      sb = box_add(sb, path_pt(S, po, id));
+      if (th >= 0) {
+        float rk = S.P[th + id];
+        rr = (k == 0) ? rk : rmax(rr, rk);
+      }
+    }
+    S.seg_box[so + i] = sb;
+    S.seg_r[so + i] = rr;
+  }
+  __syncwarp();
+  if (nseg > 0) path_leaf_order_warp(S.seg_box + so, nseg, S.seg_order + so, S.scratch + 10 * so + 8 * s, lane);
+  // per-segment lengths (the 3- / 4-point polylines), then their sum in segment order
+  for (int i = lane; i < nseg; i += 32) {
+    int nc = S.segment_ctrl[so + i], i0 = S.seg_point[so + i];
+    float t;
+    if (nc == 0) {
+      t = dist2(path_pt(S, po, (i0 + 1) % np), path_pt(S, po, i0));
+    } else if (nc == 1) {
+      v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, (i0 + 2) % np);
+      v2 v1 = eval_quad(p0, p1, p2, 0.5f);
+      t = dist2(v1, p0) + dist2(v1, p2);
+    } else {
+      v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i0 + 1), p2 = path_pt(S, po, i0 + 2),
+         p3 = path_pt(S, po, (i0 + 3) % np);
+      v2 v1 = eval_cubic(p0, p1, p2, p3, 1.f / 3.f), v2_ = eval_cubic(p0, p1, p2, p3, 2.f / 3.f);
+      t = dist2(v1, p0) + dist2(v1, v2_) + dist2(v2_, p3);
+    }
+    S.seg_pmf[so + i] = t;  // the length for now; the pmf below
+  }
+  __syncwarp();
+  float L = 0.f;
+  if (lane == 0) {
+    float len = 0.f;
+    for (int i = 0; i < nseg; i++) len += S.seg_pmf[so + i];
+    L += len;
+  }
+  L = __shfl_sync(full, L, 0);
+  float inv = 1.f / L;
+  for (int i = lane; i < nseg; i += 32) S.seg_pmf[so + i] = S.seg_pmf[so + i] * inv;
+  __syncwarp();
+  if (lane == 0) {
+    float cdf = 0.f;
+    for (int i = 0; i < nseg; i++) {
+      float dd = S.seg_pmf[so + i];
+      cdf = (i == 0) ? dd : dd + cdf;
+      S.seg_cdf[so + i] = cdf;
+    }
+    S.s_length[s] = L;
+  }
+}
+
+// y-band segment lists of the long paths (one warp per path): the path's
 // box is cut into bands of equal height (as many as fit at least
 // DVG_BAND_MIN_HEIGHT, at most shape_band.x), and every segment is
 // listed, by its visiting rank in ascending order, in each band from
@@ -183,13 +328,17 @@ __global__ void k_shape_prep(DevScene S) {
 // and compute_distance.h:36-300); the band lists give a point's candidates as
 // one contiguous list.  A path whose lists would pass their capacity, or
 // whose box has no finite positive height, gets none this call (band_n 0):
-// its queries scan every segment, with the same results.
+// its queries scan every segment, with the same results.  Lanes find each
+// rank's band range, count the bands' entries, and then each lane fills its
+// own bands in rank order.
 __global__ void k_band_fill(DevScene S) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned full = 0xffffffffu;
+  int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
   if (s >= S.num_shapes) return;
   int4 sb = S.shape_band[s];
   if (sb.x <= 0) return;
-  S.band_n[s] = 0;
+  if (lane == 0) S.band_n[s] = 0;
   float4 box = S.s_box[s];
   float h = box.w - box.y;
   if (!(h > 0.f) || !(h < INFINITY)) return;
@@ -198,34 +347,45 @@ __global__ void k_band_fill(DevScene S) {
   float inv = (float)nb / h;
   if (!(inv < INFINITY)) return;
   float2 geo = make_float2(box.y, inv);
-  S.band_geo[s] = geo;
+  if (lane == 0) S.band_geo[s] = geo;
   int so = SI(S, s, DVG_SHAPE_SEG_OFF), nseg = SI(S, s, DVG_SHAPE_NUM_SEGMENTS);
   int *st = S.band_start + sb.y;
   int *out = S.band_seg + sb.z;
-  for (int b = 0; b <= nb; b++) st[b] = 0;
+  int2 *range = reinterpret_cast<int2 *>(S.scratch + 10 * so + 8 * s);  // [nseg] band range of rank k
+  for (int b = lane; b <= nb; b += 32) st[b] = 0;
+  __syncwarp();
   long long total = 0;
-  for (int k = 0; k < nseg; k++) {
+  for (int k = lane; k < nseg; k += 32) {
     float4 q = S.seg_box[so + S.seg_order[so + k]];
-    if (!(q.y == q.y) || !(q.w == q.w)) continue;  // a NaN box passes no box test
-    int b0 = band_of(geo, nb, q.y), b1 = band_of(geo, nb, q.w);
-    for (int b = b0; b <= b1; b++) st[b]++;
-    total += b1 - b0 + 1;
+    int b0 = 1, b1 = 0;  // a NaN box passes no box test: no band
+    if (q.y == q.y && q.w == q.w) {
+      b0 = band_of(geo, nb, q.y);
+      b1 = band_of(geo, nb, q.w);
+      for (int b = b0; b <= b1; b++) atomicAdd(&st[b], 1);
+      total += b1 - b0 + 1;
+    }
+    range[k] = make_int2(b0, b1);
   }
+  for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(full, total, o);
+  __syncwarp();
   if (total > sb.w) return;
-  for (int b = 0, run = 0; b < nb; b++) {  // counts -> starts
-    int c = st[b];
-    st[b] = run;
-    run += c;
+  if (lane == 0) {  // counts -> starts; st[nb] = the entry count
+    for (int b = 0, run = 0; b <= nb; b++) {
+      int c = b < nb ? st[b] : 0;
+      st[b] = run;
+      run += c;
+    }
   }
-  for (int k = 0; k < nseg; k++) {  // st[b] is band b's write cursor; entries are visiting ranks
-    float4 q = S.seg_box[so + S.seg_order[so + k]];
-    if (!(q.y == q.y) || !(q.w == q.w)) continue;
-    int b0 = band_of(geo, nb, q.y), b1 = band_of(geo, nb, q.w);
-    for (int b = b0; b <= b1; b++) out[st[b]++] = k;
+  __syncwarp();
+  for (int b = lane; b < nb; b += 32) {  // each lane fills its bands, ranks ascending
+    int w = st[b];
+    for (int k = 0; k < nseg; k++) {
+      int2 r = range[k];
+      if (r.x <= b && b <= r.y) out[w++] = k;
+    }
   }
-  for (int b = nb; b > 0; b--) st[b] = st[b - 1];  // cursors (= band ends) -> starts
-  st[0] = 0;
-  S.band_n[s] = nb;
+  __syncwarp();
+  if (lane == 0) S.band_n[s] = nb;
 }
 
 __device__ __forceinline__ int clamp_tile(double f, int hi, bool lower) {
@@ -582,8 +742,9 @@ cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4
   int T = S.tiles_x * S.tiles_y;
   if (G > 0) k_group_xform<<<(G + 127) / 128, 128, 0, st>>>(S);
   if (NS > 0) k_shape_prep<<<(NS + 63) / 64, 64, 0, st>>>(S);
+  if (NS > 0) k_path_prep<<<(NS + 3) / 4, 128, 0, st>>>(S);
   if (NS > 0 && S.seg_tpts) k_seg_tree<<<(NS + 3) / 4, 128, 0, st>>>(S);
-  if (NS > 0 && S.shape_band) k_band_fill<<<(NS + 63) / 64, 64, 0, st>>>(S);
+  if (NS > 0 && S.shape_band) k_band_fill<<<(NS + 3) / 4, 128, 0, st>>>(S);
   if (G > 0) k_group_prep<<<(G + 127) / 128, 128, 0, st>>>(S, g_tile_range);
   if (G > 0) {
     k_rec_scan<<<1, 1024, 0, st>>>(S);
