@@ -21,6 +21,42 @@
 #ifndef DVG_SAMPLE_MIN_BLOCKS
 #define DVG_SAMPLE_MIN_BLOCKS 2
 #endif
+// Threads per block (256 k: k groups of 256 samples) of the sample passes and
+// of the paired-lane boundary pass; blocks of 512 run one per SM, of 256 two
+// (128 registers per thread either way).  One block of 16 warps keeps an SM's
+// warps on neighbouring samples, which walk the same candidates and code:
+// measured on the stroke-heavy 512x512 workload, forward 4.24 -> 3.76 ms and
+// boundary walk 12.87 -> 11.43 ms against two blocks of 256 (blocks of 128 or
+// 192 threads were slower still); the prefiltered adjoint (two tiles a block)
+// 2.72 -> 2.49 ms on the fill-heavy 1024x1024 workload; the prefiltered
+// forward and the sampled interior adjoint measured no better with 512.
+#ifndef DVG_FWD_THREADS
+#define DVG_FWD_THREADS 512
+#endif
+static_assert(DVG_FWD_THREADS % 256 == 0 && DVG_FWD_THREADS <= 512, "the forward pass runs 256-sample groups");
+#ifndef DVG_BWD_THREADS
+#define DVG_BWD_THREADS 256
+#endif
+#ifndef DVG_PF_FWD_THREADS
+#define DVG_PF_FWD_THREADS 256
+#endif
+#ifndef DVG_PF_BWD_THREADS
+#define DVG_PF_BWD_THREADS 512
+#endif
+static_assert(DVG_BWD_THREADS % 256 == 0 && DVG_BWD_THREADS <= 512 && DVG_PF_FWD_THREADS % 256 == 0 &&
+                  DVG_PF_FWD_THREADS <= 512 && DVG_PF_BWD_THREADS % 256 == 0 && DVG_PF_BWD_THREADS <= 512,
+              "the sample passes run 256-sample groups");
+// resident blocks per SM for a 128-register budget
+#define DVG_BLOCKS_FOR(threads) (512 / (threads))
+#ifndef DVG_EDGE_THREADS
+#define DVG_EDGE_THREADS 512
+#endif
+#ifndef DVG_EDGE_MIN_BLOCKS
+#define DVG_EDGE_MIN_BLOCKS 1
+#endif
+static_assert(DVG_EDGE_THREADS % 32 == 0 && DVG_EDGE_THREADS <= 512, "the boundary pass runs whole warps, 16 at most");
+// the single-lane boundary pass (few groups) keeps two blocks of 256: its walks are short
+#define DVG_EDGE1_THREADS 256
 
 namespace dvg {
 
@@ -96,6 +132,23 @@ __device__ __forceinline__ void tile_sample(int spp, int cta_y, int tid, int &dx
   dy = morton_y(k);
 }
 
+// The 256-sample groups of a block of the sample passes (blockDim.x / 256 of
+// them): groups of one tile when the tile has that many (blockIdx.y picks
+// which), else the groups of neighbouring tiles (blockIdx.x picks which).
+// false for a warp whose group lies past the image (it leaves whole).
+__device__ __forceinline__ bool block_group(const DevRender &R, int &tile, int &cy) {
+  int k = blockDim.x >> 8, sub = threadIdx.x >> 8;
+  if (R.spp >= k) {
+    tile = blockIdx.x;
+    cy = blockIdx.y * k + sub;
+    return cy < R.spp;
+  }
+  int tiles = ((R.w + DVG_TILE - 1) / DVG_TILE) * ((R.h + DVG_TILE - 1) / DVG_TILE);
+  tile = blockIdx.x * k + sub;
+  cy = blockIdx.y;
+  return tile < tiles;
+}
+
 // One sample of the forward sample pass: thread tid of the 256-thread group
 // cta_y of image tile `tile` (a warp's lanes call it together).
 template <bool PREFILTER>
@@ -135,11 +188,18 @@ __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRende
   if (active) samples[idx] = c;
 }
 
+// A block of 256 k threads runs groups k blockIdx.y .. k blockIdx.y + k - 1
+// of its tile's 256-sample groups (whole warps leave when their group is past
+// the tile's spp groups); launch_sample_fwd uses blocks of 256 when a tile
+// has fewer samples than a block.
 template <bool PREFILTER>
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+__global__ void __launch_bounds__(PREFILTER ? DVG_PF_FWD_THREADS : DVG_FWD_THREADS,
+                                  DVG_BLOCKS_FOR(PREFILTER ? DVG_PF_FWD_THREADS : DVG_FWD_THREADS))
     k_sample_fwd(const __grid_constant__ DevScene S, const __grid_constant__ DevRender R, float4 *samples,
                  const __grid_constant__ EdgeRecords D) {
-  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, samples, warp_queue(), threadIdx.x & 31,
+  int cy = blockIdx.y * (blockDim.x >> 8) + (threadIdx.x >> 8);
+  if (cy >= R.spp) return;
+  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, cy, threadIdx.x & 255, samples, warp_queue(), threadIdx.x & 31,
                             D.job_a ? &D : nullptr);
 }
 
@@ -278,11 +338,13 @@ __device__ __forceinline__ void sample_bwd_one(const DevScene &S, const DevRende
 }
 
 template <bool PREFILTER>
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+__global__ void __launch_bounds__(PREFILTER ? DVG_PF_BWD_THREADS : DVG_BWD_THREADS,
+                                  DVG_BLOCKS_FOR(PREFILTER ? DVG_PF_BWD_THREADS : DVG_BWD_THREADS))
     k_sample_bwd(const __grid_constant__ DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
   DevRender R = load_filter(R0, nullptr);
-  sample_bwd_one<PREFILTER>(S, R, blockIdx.x, blockIdx.y, threadIdx.x, dbg_val, dbg_flag, warp_queue(),
-                            threadIdx.x & 31);
+  int tile, cy;
+  if (!block_group(R, tile, cy)) return;
+  sample_bwd_one<PREFILTER>(S, R, tile, cy, threadIdx.x & 255, dbg_val, dbg_flag, warp_queue(), threadIdx.x & 31);
 }
 
 // The deep pass: the interior adjoint of the samples that sample_bwd_one
@@ -545,7 +607,8 @@ __device__ __forceinline__ void edge_eval_one(const DevScene &S, const DevRender
 }
 
 template <bool PAIRS>
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+__global__ void __launch_bounds__(PAIRS ? DVG_EDGE_THREADS : DVG_EDGE1_THREADS,
+                                  PAIRS ? DVG_EDGE_MIN_BLOCKS : DVG_SAMPLE_MIN_BLOCKS)
     k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, const __grid_constant__ EdgeRecords E) {
   DevRender R = load_filter(R0, nullptr);
   edge_eval_one<PAIRS>(S, R, E, (long long)blockIdx.x * blockDim.x + threadIdx.x, warp_queue(), threadIdx.x & 31);
@@ -791,18 +854,23 @@ static inline int tiles_of(const DevRender &R) {
   return ((R.w + DVG_TILE - 1) / DVG_TILE) * ((R.h + DVG_TILE - 1) / DVG_TILE);
 }
 static inline unsigned blocks_of(long long n) { return (unsigned)((n + 255) / 256); }
+// grid of a sample pass run with blocks of `threads` (block_group)
+static inline dim3 group_grid(const DevRender &R, int threads) {
+  int k = threads / 256, tiles = tiles_of(R);
+  return R.spp >= k ? dim3(tiles, (R.spp + k - 1) / k) : dim3((tiles + k - 1) / k, R.spp);
+}
 
 // Opts kernel `id` (one of QueueKernel) into kQueueBytes of dynamic shared
 // memory, once per device (devices 0-63; the others every call).
 enum QueueKernel { QK_FWD, QK_BWD, QK_EDGE_PAIRS, QK_EDGE, QK_FWD_BATCH, QK_BWD_BATCH, QK_EDGE_BATCH, QK_COUNT };
 template <class K>
-static void allow_queues(K *kernel, int id) {
+static void allow_queues(K *kernel, int id, int bytes = kQueueBytes) {
   static std::atomic<unsigned long long> done[QK_COUNT];
   int dev = 0;
   cudaGetDevice(&dev);
   unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
   if (bit && (done[id].load() & bit)) return;
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kQueueBytes);
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   done[id].fetch_or(bit);
 }
 
@@ -831,16 +899,19 @@ void launch_weight(const DevScene &S, const DevRender &R, cudaStream_t st) {
 }
 void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, cudaStream_t st,
                        const EdgeRecords *D) {
-  dim3 grid(tiles_of(R), R.spp);
   if (R.hit_chunk_count) cudaMemsetAsync(R.hit_chunk_count, 0, sizeof(int), st);
   EdgeRecords none{};
   if (R.prefilter) {
-    k_sample_fwd<true><<<grid, 256, 0, st>>>(S, R, samples, none);
+    int threads = 256 * R.spp >= DVG_PF_FWD_THREADS ? DVG_PF_FWD_THREADS : 256;
+    dim3 grid(tiles_of(R), (256 * R.spp + threads - 1) / threads);
+    k_sample_fwd<true><<<grid, threads, 0, st>>>(S, R, samples, none);
   } else {
     bool defer = D && D->job_a;
     if (defer) cudaMemsetAsync(D->counts, 0, 4 * sizeof(int), st);
-    allow_queues(k_sample_fwd<false>, QK_FWD);
-    k_sample_fwd<false><<<grid, 256, kQueueBytes, st>>>(S, R, samples, defer ? *D : none);
+    int threads = 256 * R.spp >= DVG_FWD_THREADS ? DVG_FWD_THREADS : 256;
+    dim3 grid(tiles_of(R), (256 * R.spp + threads - 1) / threads);
+    allow_queues(k_sample_fwd<false>, QK_FWD, DVG_FWD_THREADS / 32 * (int)sizeof(WarpQueue));
+    k_sample_fwd<false><<<grid, threads, threads / 32 * sizeof(WarpQueue), st>>>(S, R, samples, defer ? *D : none);
     if (defer) {
       k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, *D);
       k_fwd_finish<<<persistent_grid(8), 256, 0, st>>>(S, R, *D, samples);
@@ -855,14 +926,14 @@ void launch_resolve(const DevRender &R, const float4 *samples, float *image, cud
   k_resolve<<<blocks_of((long long)R.w * R.h), 256, 0, st>>>(R, samples, image);
 }
 void launch_sample_bwd(const DevScene &S, const DevRender &R, float4 *dbg_val, int *dbg_flag, cudaStream_t st) {
-  dim3 grid(tiles_of(R), R.spp);
   cudaMemsetAsync(R.deep_count, 0, sizeof(int), st);
   if (R.prefilter) {
-    k_sample_bwd<true><<<grid, 256, 0, st>>>(S, R, dbg_val, dbg_flag);
+    k_sample_bwd<true><<<group_grid(R, DVG_PF_BWD_THREADS), DVG_PF_BWD_THREADS, 0, st>>>(S, R, dbg_val, dbg_flag);
     k_sample_bwd_deep_pf<<<sm_count() * 2, 256, 0, st>>>(S, R, dbg_val, dbg_flag);
   } else {
-    allow_queues(k_sample_bwd<false>, QK_BWD);
-    k_sample_bwd<false><<<grid, 256, kQueueBytes, st>>>(S, R, dbg_val, dbg_flag);
+    allow_queues(k_sample_bwd<false>, QK_BWD, DVG_BWD_THREADS / 32 * (int)sizeof(WarpQueue));
+    k_sample_bwd<false><<<group_grid(R, DVG_BWD_THREADS), DVG_BWD_THREADS, DVG_BWD_THREADS / 32 * sizeof(WarpQueue),
+                          st>>>(S, R, dbg_val, dbg_flag);
     k_sample_bwd_deep<<<sm_count() * 4, 32, 0, st>>>(S, R, dbg_val, dbg_flag);
   }
 }
@@ -882,15 +953,17 @@ void launch_edge_setup(const DevScene &S, const DevRender &R, const EdgeRecords 
 void launch_edge_eval(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
   long long n = (long long)R.w * R.h * R.spp;
   if (S.num_groups >= 8) {  // two lanes per sample
-    allow_queues(k_edge_eval<true>, QK_EDGE_PAIRS);
-    k_edge_eval<true><<<blocks_of(2 * n), 256, kQueueBytes, st>>>(S, R, E);
+    allow_queues(k_edge_eval<true>, QK_EDGE_PAIRS, DVG_EDGE_THREADS / 32 * (int)sizeof(WarpQueue));
+    k_edge_eval<true><<<(unsigned)((2 * n + DVG_EDGE_THREADS - 1) / DVG_EDGE_THREADS), DVG_EDGE_THREADS,
+                        DVG_EDGE_THREADS / 32 * sizeof(WarpQueue), st>>>(S, R, E);
     if (E.job_a) {
       k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, E);
       k_edge_finish<<<persistent_grid(8), 256, 0, st>>>(S, R, E);
     }
   } else {
-    allow_queues(k_edge_eval<false>, QK_EDGE);
-    k_edge_eval<false><<<blocks_of(n), 256, kQueueBytes, st>>>(S, R, E);
+    allow_queues(k_edge_eval<false>, QK_EDGE, DVG_EDGE1_THREADS / 32 * (int)sizeof(WarpQueue));
+    k_edge_eval<false><<<(unsigned)((n + DVG_EDGE1_THREADS - 1) / DVG_EDGE1_THREADS), DVG_EDGE1_THREADS,
+                         DVG_EDGE1_THREADS / 32 * sizeof(WarpQueue), st>>>(S, R, E);
   }
 }
 void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
