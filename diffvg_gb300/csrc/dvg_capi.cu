@@ -482,6 +482,7 @@ bool hit_matches(const DvgScene *sc, const DvgRenderArgs *a) {
 // that finds no room solves its jobs in place.
 bool edge_defers(const DvgScene *sc, size_t n) { return sc->d.num_groups >= 8 && n < (1u << 30); }
 size_t edge_job_cap(size_t n) { return n; }
+size_t edge_task_cap(size_t n) { return 2 * n; }
 size_t edge_frag_cap(size_t n) { return 4 * n; }
 
 size_t edge_bytes(DvgScene *sc, size_t n) {
@@ -489,9 +490,10 @@ size_t edge_bytes(DvgScene *sc, size_t n) {
   std::vector<size_t> b = {n * sizeof(float4), n * sizeof(float4), n * sizeof(int4), n * sizeof(float2),
                            n * sizeof(int), n * sizeof(int), n * sizeof(int), T * sizeof(int), (T + 1) * sizeof(int)};
   if (edge_defers(sc, n)) {
-    size_t jc = edge_job_cap(n), fc = edge_frag_cap(n);
+    size_t jc = edge_job_cap(n), fc = edge_frag_cap(n), tc = edge_task_cap(n);
     for (size_t x : {jc * sizeof(int4), jc * sizeof(float4), 2 * n * sizeof(int4), 2 * n * sizeof(unsigned),
-                     2 * n * sizeof(float4), fc * sizeof(int2), n * sizeof(int), 4 * sizeof(int)})
+                     2 * n * sizeof(float4), fc * sizeof(int2), n * sizeof(int), 5 * jc * sizeof(double),
+                     tc * sizeof(int4), 8 * sizeof(int)})
       b.push_back(x);
   }
   return carve_size(b);
@@ -511,7 +513,7 @@ EdgeRecords edge_records(DvgScene *sc, size_t n) {
   E.tile_count = carve<int>(p, T);
   E.tile_start = carve<int>(p, T + 1);
   if (edge_defers(sc, n)) {
-    size_t jc = edge_job_cap(n), fc = edge_frag_cap(n);
+    size_t jc = edge_job_cap(n), fc = edge_frag_cap(n), tc = edge_task_cap(n);
     E.job_a = carve<int4>(p, jc);
     E.job_b = carve<float4>(p, jc);
     E.dq = carve<int4>(p, 2 * n);
@@ -519,9 +521,12 @@ EdgeRecords edge_records(DvgScene *sc, size_t n) {
     E.dq_col = carve<float4>(p, 2 * n);
     E.frag = carve<int2>(p, fc);
     E.ds = carve<int>(p, n);
-    E.counts = carve<int>(p, 4);
+    E.job_q = carve<double>(p, 5 * jc);
+    E.task = carve<int4>(p, tc);
+    E.counts = carve<int>(p, 8);
     E.job_cap = (int)std::min(jc, (size_t)0x7fffffff);
     E.frag_cap = (int)std::min(fc, (size_t)0x7fffffff);
+    E.task_cap = (int)std::min(tc, (size_t)0x7fffffff);
   }
   return E;
 }

@@ -154,8 +154,11 @@ struct EdgeRecords {
                              //   query, the blend of the fragments its walk flushed
   int2 *frag = nullptr;      // [frag_cap] candidate fragments (key, meta) of deferred queries
   int *ds = nullptr;         // [n] sorted positions of the deferred samples
-  int *counts = nullptr;     // [4] jobs, -, fragments, deferred samples reserved this call
-  int job_cap = 0, frag_cap = 0;
+  // the root brackets of the cubic jobs (k_edge_jobs), walked one per lane by k_edge_roots
+  double *job_q = nullptr;   // [5 job_cap] the job's normalised distance quintic, coefficients B..F
+  int4 *task = nullptr;      // [task_cap] {job (-1: none), lower end, upper end (float bits), -}
+  int *counts = nullptr;     // [8] jobs, -, fragments, deferred samples, brackets, bracket cursor, -, -
+  int job_cap = 0, frag_cap = 0, task_cap = 0;
 };
 // Boundary samples are ordered by canvas tile and, inside a tile, by
 // 2^DVG_EDGE_CELL_SHIFT-pixel square cell in Morton order.
@@ -1250,6 +1253,66 @@ static __device__ __noinline__ int cubic_stroke_decide(bool valid, bool uniform,
   return res;
 }
 
+// A cubic segment's control points and the stroke radius at each (per-point
+// thickness, or the shape's stroke width), as within_distance.h:143-149 reads them.
+struct CubicSeg {
+  v2 p[4];
+  float r[4];
+};
+DI CubicSeg cubic_seg(const DevScene &S, int po, int np, int th, int i0, float r) {
+  int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
+  CubicSeg c;
+  c.p[0] = path_pt(S, po, i0);
+  c.p[1] = path_pt(S, po, i1);
+  c.p[2] = path_pt(S, po, i2);
+  c.p[3] = path_pt(S, po, i3);
+  c.r[0] = c.r[1] = c.r[2] = c.r[3] = r;
+  if (th >= 0) {
+    c.r[0] = pget(S, th + i0);
+    c.r[1] = pget(S, th + i1);
+    c.r[2] = pget(S, th + i2);
+    c.r[3] = pget(S, th + i3);
+  }
+  return c;
+}
+// The stroke test at a root t of the distance quintic (within_distance.h:262-270).
+DI bool cubic_root_hits(const CubicSeg &c, v2 pt, float t) {
+  float tt = 1 - t;
+  float rr = (tt * tt * tt) * c.r[0] + (3 * tt * tt * t) * c.r[1] + (3 * tt * t * t) * c.r[2] + (t * t * t) * c.r[3];
+  return distsq2(eval_cubic(c.p[0], c.p[1], c.p[2], c.p[3], t), pt) < rr * rr;
+}
+// The brackets of a cubic segment's root walk (within_distance.h:181-261):
+// the isolator intervals in order, each one's ends evaluated, the lower end
+// kept through intervals without a sign change, the ends of a sign-change
+// bracket ordered so that Q rises from lb to ub; the walk stops after the
+// bracket that reaches t = 1.  The reference runs quintic_root in each
+// bracket in turn and returns at the first root within the stroke, so the
+// segment hits exactly when one of these brackets' roots is within it.
+// Returns the bracket count (at most 5).
+DI int quintic_brackets(const Quintic &q, float lo[5], float hi[5]) {
+  float iv[4];
+  int ni = quintic_intervals(q, iv);
+  float lower = 0.f;
+  float ct = NAN;
+  double cv = 0.0;
+  int nb = 0;
+  #pragma unroll 1
+  for (int j = 0; j < ni + 1; j++) {
+    if (j < ni && iv[j] < 0.f) continue;
+    float upper = j < ni ? rmin(iv[j], 1.f) : 1.f;
+    float lb = lower, ub = upper;
+    double lbe = quintic_eval_cached(q, lb, ct, cv), ube = quintic_eval_cached(q, ub, ct, cv);
+    if (lbe * ube > 0) continue;
+    if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
+    lo[nb] = lb;
+    hi[nb] = ub;
+    nb++;
+    if (upper >= 1.f) break;
+    lower = upper;
+  }
+  return nb;
+}
+
 // Root-solve part of the stroke test of one quadratic (nc = 1) or cubic
 // (nc = 2) segment, for a point whose end-point checks failed: the
 // quadratic's cubic and the cubic's distance quintic, solved as the
@@ -1278,11 +1341,8 @@ static __device__ __noinline__ int segment_root_test(const DevScene &S, int po, 
     }
     return 0;
   }
-  int i1 = i0 + 1, i2 = i0 + 2, i3 = (i0 + 3) % np;
-  v2 p0 = path_pt(S, po, i0), p1 = path_pt(S, po, i1), p2 = path_pt(S, po, i2), p3 = path_pt(S, po, i3);
-  float r0 = r, r1 = r, r2 = r, r3 = r;
-  if (th >= 0) { r0 = pget(S, th + i0); r1 = pget(S, th + i1); r2 = pget(S, th + i2); r3 = pget(S, th + i3); }
-  Quintic q = cubic_quintic(p0, p1, p2, p3, pt);
+  CubicSeg c = cubic_seg(S, po, np, th, i0, r);
+  Quintic q = cubic_quintic(c.p[0], c.p[1], c.p[2], c.p[3], pt);
   float iv[4];
   int ni = quintic_intervals(q, iv);
   float lower = 0.f;
@@ -1296,10 +1356,7 @@ static __device__ __noinline__ int segment_root_test(const DevScene &S, int po, 
     double lbe = quintic_eval_cached(q, lb, ct, cv), ube = quintic_eval_cached(q, ub, ct, cv);
     if (lbe * ube > 0) continue;
     if (lbe > ube) { float tmp = lb; lb = ub; ub = tmp; }
-    float t = quintic_root(q, lb, ub);
-    float tt = 1 - t;
-    float rr = (tt * tt * tt) * r0 + (3 * tt * tt * t) * r1 + (3 * tt * t * t) * r2 + (t * t * t) * r3;
-    if (distsq2(eval_cubic(p0, p1, p2, p3, t), pt) < rr * rr) return 1;
+    if (cubic_root_hits(c, pt, quintic_root(q, lb, ub))) return 1;
     if (upper >= 1.f) break;
     lower = upper;
   }

@@ -616,17 +616,131 @@ __global__ void __launch_bounds__(PAIRS ? DVG_EDGE_THREADS : DVG_EDGE1_THREADS,
 
 // The deferred fp64 root walks of the paired boundary pass, one per thread
 // (full warps): each sets its result bit in its query's dq_res.
+// The deferred fp64 root walks, first part (one job per thread): a
+// quadratic segment's test whole; for a cubic segment the normalised
+// distance quintic (kept in job_q) and its root brackets (quintic_brackets),
+// which go to the task list for k_edge_roots.  The brackets of a warp are
+// reserved together; when the list has no room the lanes walk their
+// brackets here, as segment_root_test does.
 __global__ void __launch_bounds__(256) k_edge_jobs(const __grid_constant__ DevScene S, const __grid_constant__ EdgeRecords E) {
+  const unsigned full = 0xffffffffu;
+  int lane = threadIdx.x & 31;
   int n = min(*(volatile const int *)&E.counts[0], E.job_cap);
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    int4 ja = E.job_a[k];
-    if (ja.x < 0) continue;
-    float4 jb = E.job_b[k];
-    int s = ja.z;
-    int hit = segment_root_test(S, SI(S, s, DVG_SHAPE_PARAM_OFF), SI(S, s, DVG_SHAPE_NUM_POINTS),
-                                SI(S, s, DVG_SHAPE_THICKNESS_OFF), __ldg(&S.segment_ctrl[ja.w]),
-                                __ldg(&S.seg_point[ja.w]), V2(jb.x, jb.y), jb.z);
+  // warp-uniform trip count: the lanes of a warp take jobs k0 .. k0 + 31
+  for (int k0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); k0 < n; k0 += gridDim.x * blockDim.x) {
+    int k = k0 + lane;
+    int4 ja = k < n ? E.job_a[k] : make_int4(-1, 0, 0, 0);
+    float lo[5], hi[5];
+    int nb = 0, hit = 0;
+    Quintic q{};
+    CubicSeg c{};
+    v2 pt = V2(0.f, 0.f);
+    if (ja.x >= 0) {
+      float4 jb = E.job_b[k];
+      int s = ja.z;
+      int po = SI(S, s, DVG_SHAPE_PARAM_OFF), np = SI(S, s, DVG_SHAPE_NUM_POINTS);
+      int th = SI(S, s, DVG_SHAPE_THICKNESS_OFF), nc = __ldg(&S.segment_ctrl[ja.w]), i0 = __ldg(&S.seg_point[ja.w]);
+      pt = V2(jb.x, jb.y);
+      if (nc != 2 || !E.task) {
+        hit = segment_root_test(S, po, np, th, nc, i0, pt, jb.z);
+      } else {
+        c = cubic_seg(S, po, np, th, i0, jb.z);
+        q = cubic_quintic(c.p[0], c.p[1], c.p[2], c.p[3], pt);
+        nb = quintic_brackets(q, lo, hi);
+        double *qk = E.job_q + 5 * (size_t)k;
+        qk[0] = q.B;
+        qk[1] = q.C;
+        qk[2] = q.D;
+        qk[3] = q.E;
+        qk[4] = q.F;
+      }
+    }
+    int incl = nb;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int v = __shfl_up_sync(full, incl, o);
+      if (lane >= o) incl += v;
+    }
+    int total = __shfl_sync(full, incl, 31), base = 0;
+    if (lane == 0 && total > 0) base = atomicAdd(&E.counts[4], total);
+    base = __shfl_sync(full, base, 0);
+    if ((long long)base + total <= E.task_cap) {
+      for (int i = 0; i < nb; i++)
+        E.task[base + incl - nb + i] = make_int4(k, __float_as_int(lo[i]), __float_as_int(hi[i]), 0);
+    } else {
+      for (int i = incl - nb; i < incl; i++)  // the reserved slots that fit: none of them is walked
+        if (base + i < E.task_cap) E.task[base + i] = make_int4(-1, 0, 0, 0);
+      for (int i = 0; i < nb && !hit; i++) hit = cubic_root_hits(c, pt, quintic_root(q, lo[i], hi[i])) ? 1 : 0;
+    }
     if (hit) atomicOr(&E.dq_res[ja.x], 1u << ja.y);
+  }
+}
+
+// The deferred fp64 root walks, second part: the safeguarded Newton /
+// bisection walk of every root bracket (quintic_root, within_distance.h:
+// 251-269), one bracket per lane and one iteration per step; a lane whose
+// walk stops runs the stroke test at the root, sets the job's bit when it
+// hits, and takes the next bracket of the list, so the lanes of a warp stay
+// busy whatever the iteration counts of their brackets.
+__global__ void __launch_bounds__(256) k_edge_roots(const __grid_constant__ DevScene S, const __grid_constant__ EdgeRecords E) {
+  const unsigned full = 0xffffffffu;
+  int lane = threadIdx.x & 31;
+  int ntask = min(*(volatile const int *)&E.counts[4], E.task_cap);
+  int cur = -1, job = -1, it = 0;  // cur: the lane's bracket (-1: none yet, >= ntask: no more)
+  float lb = 0.f, ub = 0.f, t = 0.f;
+  Quintic q{};
+  #pragma unroll 1
+  while (true) {
+    unsigned idle = __ballot_sync(full, cur < 0);
+    if (idle) {
+      int first = 0;
+      if (lane == 0) first = atomicAdd(&E.counts[5], __popc(idle));
+      first = __shfl_sync(full, first, 0);
+      if (cur < 0) {
+        cur = first + __popc(idle & ((1u << lane) - 1u));
+        if (cur < ntask) {
+          int4 tk = E.task[cur];
+          if (tk.x < 0) {
+            cur = -1;
+          } else {
+            job = tk.x;
+            const double *qk = E.job_q + 5 * (size_t)job;
+            q.A = 1.0;
+            q.B = qk[0];
+            q.C = qk[1];
+            q.D = qk[2];
+            q.E = qk[3];
+            q.F = qk[4];
+            lb = __int_as_float(tk.y);
+            ub = __int_as_float(tk.z);
+            t = 0.5f * (lb + ub);
+            it = 0;
+          }
+        }
+      }
+    }
+    if (__all_sync(full, cur >= ntask)) break;
+    if (cur < 0 || cur >= ntask) continue;
+    // one iteration of quintic_root
+    if (!(t >= lb && t <= ub)) t = 0.5f * (lb + ub);
+    double value = quintic_eval(q, t);
+    if (!(fabs(value) < 1e-5f || it == 19)) {
+      if (value > 0.f) ub = t; else lb = t;
+      if (!(lb > ub)) {
+        double derivative = quintic_deriv(q, t);
+        t = (float)(t - ddiv(value, derivative));
+      }
+      it++;
+      continue;
+    }
+    // the walk stopped at t: the stroke test there
+    int4 ja = E.job_a[job];
+    float4 jb = E.job_b[job];
+    int s = ja.z;
+    CubicSeg c = cubic_seg(S, SI(S, s, DVG_SHAPE_PARAM_OFF), SI(S, s, DVG_SHAPE_NUM_POINTS),
+                           SI(S, s, DVG_SHAPE_THICKNESS_OFF), __ldg(&S.seg_point[ja.w]), jb.z);
+    if (cubic_root_hits(c, V2(jb.x, jb.y), t)) atomicOr(&E.dq_res[ja.x], 1u << ja.y);
+    cur = -1;
   }
 }
 
@@ -907,13 +1021,14 @@ void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, c
     k_sample_fwd<true><<<grid, threads, 0, st>>>(S, R, samples, none);
   } else {
     bool defer = D && D->job_a;
-    if (defer) cudaMemsetAsync(D->counts, 0, 4 * sizeof(int), st);
+    if (defer) cudaMemsetAsync(D->counts, 0, 8 * sizeof(int), st);
     int threads = 256 * R.spp >= DVG_FWD_THREADS ? DVG_FWD_THREADS : 256;
     dim3 grid(tiles_of(R), (256 * R.spp + threads - 1) / threads);
     allow_queues(k_sample_fwd<false>, QK_FWD, DVG_FWD_THREADS / 32 * (int)sizeof(WarpQueue));
     k_sample_fwd<false><<<grid, threads, threads / 32 * sizeof(WarpQueue), st>>>(S, R, samples, defer ? *D : none);
     if (defer) {
       k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, *D);
+      k_edge_roots<<<persistent_grid(6), 256, 0, st>>>(S, *D);
       k_fwd_finish<<<persistent_grid(8), 256, 0, st>>>(S, R, *D, samples);
     }
   }
@@ -948,7 +1063,7 @@ void launch_edge_setup(const DevScene &S, const DevRender &R, const EdgeRecords 
   k_edge_sample<<<blocks_of(n), 256, 0, st>>>(S, R, E);
   k_edge_scan<<<1, 1024, 0, st>>>(S, E);
   k_edge_order<<<blocks_of(n), 256, 0, st>>>(E, (int)n);
-  if (S.num_groups >= 8 && E.job_a) cudaMemsetAsync(E.counts, 0, 4 * sizeof(int), st);
+  if (S.num_groups >= 8 && E.job_a) cudaMemsetAsync(E.counts, 0, 8 * sizeof(int), st);
 }
 void launch_edge_eval(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
   long long n = (long long)R.w * R.h * R.spp;
@@ -958,6 +1073,7 @@ void launch_edge_eval(const DevScene &S, const DevRender &R, const EdgeRecords &
                         DVG_EDGE_THREADS / 32 * sizeof(WarpQueue), st>>>(S, R, E);
     if (E.job_a) {
       k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, E);
+      k_edge_roots<<<persistent_grid(6), 256, 0, st>>>(S, E);
       k_edge_finish<<<persistent_grid(8), 256, 0, st>>>(S, R, E);
     }
   } else {

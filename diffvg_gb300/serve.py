@@ -105,8 +105,9 @@ def estimate_device_bytes(packed, width, height, spp, fragment_cache=True):
     cache = cache + 2 if fragment_cache else 0
     samples = 16 * n + (cache + 4) * n
     edges = 68 * n                                  # boundary-sample records and ordering
-    if ng >= 8:  # deferred fp64 walks: jobs, per-query state and colours, fragments, deferred samples
-        edges += 32 * n + 2 * (16 + 4 + 16) * n + 4 * 8 * n + 4 * n
+    if ng >= 8:  # deferred fp64 walks: jobs, per-query state and colours, fragments, deferred samples,
+        # the jobs' quintics and root brackets
+        edges += 32 * n + 2 * (16 + 4 + 16) * n + 4 * 8 * n + 4 * n + 40 * n + 2 * 16 * n
     scene = 4 * (8 * ns + 12 * ng + 2 * nseg + 2 * ng) + 64 * ng + 40 * ns + 48 * nseg + 4 * (10 * nseg + 8 * ns)
     scene += (8 * 33 + 4 * 64) * nseg                # tabulated subdivision trees of the segments
     tile_lists = 4 * max(65536, 32 * tiles) * 5 // 4 + 8 * tiles
