@@ -65,7 +65,12 @@ namespace dvg {
 // statically.
 extern __shared__ __align__(16) unsigned char dvg_smem[];
 constexpr int kQueueBytes = 8 * (int)sizeof(WarpQueue);
-__device__ __forceinline__ WarpQueue *warp_queue() { return reinterpret_cast<WarpQueue *>(dvg_smem) + (threadIdx.x >> 5); }
+// per-warp stride of the queues of the kernels that keep fragment fronts per
+// lane (the forward and boundary walks): their queues stop before the front
+constexpr int kQueueLocalBytes = DVG_QUEUE_LOCAL_BYTES;
+__device__ __forceinline__ WarpQueue *warp_queue(int stride = (int)sizeof(WarpQueue)) {
+  return reinterpret_cast<WarpQueue *>(dvg_smem + (threadIdx.x >> 5) * stride);
+}
 
 // Kernels that accumulate into caller-visible outputs do nothing when the
 // tile lists overflowed their capacity; the host then grows the lists and
@@ -199,8 +204,8 @@ __global__ void __launch_bounds__(PREFILTER ? DVG_PF_FWD_THREADS : DVG_FWD_THREA
                  const __grid_constant__ EdgeRecords D) {
   int cy = blockIdx.y * (blockDim.x >> 8) + (threadIdx.x >> 8);
   if (cy >= R.spp) return;
-  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, cy, threadIdx.x & 255, samples, warp_queue(), threadIdx.x & 31,
-                            D.job_a ? &D : nullptr);
+  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, cy, threadIdx.x & 255, samples, warp_queue(kQueueLocalBytes),
+                            threadIdx.x & 31, D.job_a ? &D : nullptr);
 }
 
 // The samples the forward pass deferred (D.ds): blend each one's parked
@@ -611,7 +616,8 @@ __global__ void __launch_bounds__(PAIRS ? DVG_EDGE_THREADS : DVG_EDGE1_THREADS,
                                   PAIRS ? DVG_EDGE_MIN_BLOCKS : DVG_SAMPLE_MIN_BLOCKS)
     k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, const __grid_constant__ EdgeRecords E) {
   DevRender R = load_filter(R0, nullptr);
-  edge_eval_one<PAIRS>(S, R, E, (long long)blockIdx.x * blockDim.x + threadIdx.x, warp_queue(), threadIdx.x & 31);
+  edge_eval_one<PAIRS>(S, R, E, (long long)blockIdx.x * blockDim.x + threadIdx.x, warp_queue(kQueueLocalBytes),
+                      threadIdx.x & 31);
 }
 
 // The deferred fp64 root walks of the paired boundary pass, one per thread
@@ -1024,8 +1030,8 @@ void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, c
     if (defer) cudaMemsetAsync(D->counts, 0, 8 * sizeof(int), st);
     int threads = 256 * R.spp >= DVG_FWD_THREADS ? DVG_FWD_THREADS : 256;
     dim3 grid(tiles_of(R), (256 * R.spp + threads - 1) / threads);
-    allow_queues(k_sample_fwd<false>, QK_FWD, DVG_FWD_THREADS / 32 * (int)sizeof(WarpQueue));
-    k_sample_fwd<false><<<grid, threads, threads / 32 * sizeof(WarpQueue), st>>>(S, R, samples, defer ? *D : none);
+    allow_queues(k_sample_fwd<false>, QK_FWD, DVG_FWD_THREADS / 32 * kQueueLocalBytes);
+    k_sample_fwd<false><<<grid, threads, threads / 32 * kQueueLocalBytes, st>>>(S, R, samples, defer ? *D : none);
     if (defer) {
       k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, *D);
       k_edge_roots<<<persistent_grid(6), 256, 0, st>>>(S, *D);
@@ -1068,18 +1074,18 @@ void launch_edge_setup(const DevScene &S, const DevRender &R, const EdgeRecords 
 void launch_edge_eval(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
   long long n = (long long)R.w * R.h * R.spp;
   if (S.num_groups >= 8) {  // two lanes per sample
-    allow_queues(k_edge_eval<true>, QK_EDGE_PAIRS, DVG_EDGE_THREADS / 32 * (int)sizeof(WarpQueue));
+    allow_queues(k_edge_eval<true>, QK_EDGE_PAIRS, DVG_EDGE_THREADS / 32 * kQueueLocalBytes);
     k_edge_eval<true><<<(unsigned)((2 * n + DVG_EDGE_THREADS - 1) / DVG_EDGE_THREADS), DVG_EDGE_THREADS,
-                        DVG_EDGE_THREADS / 32 * sizeof(WarpQueue), st>>>(S, R, E);
+                        DVG_EDGE_THREADS / 32 * kQueueLocalBytes, st>>>(S, R, E);
     if (E.job_a) {
       k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, E);
       k_edge_roots<<<persistent_grid(6), 256, 0, st>>>(S, E);
       k_edge_finish<<<persistent_grid(8), 256, 0, st>>>(S, R, E);
     }
   } else {
-    allow_queues(k_edge_eval<false>, QK_EDGE, DVG_EDGE1_THREADS / 32 * (int)sizeof(WarpQueue));
+    allow_queues(k_edge_eval<false>, QK_EDGE, DVG_EDGE1_THREADS / 32 * kQueueLocalBytes);
     k_edge_eval<false><<<(unsigned)((n + DVG_EDGE1_THREADS - 1) / DVG_EDGE1_THREADS), DVG_EDGE1_THREADS,
-                         DVG_EDGE1_THREADS / 32 * sizeof(WarpQueue), st>>>(S, R, E);
+                         DVG_EDGE1_THREADS / 32 * kQueueLocalBytes, st>>>(S, R, E);
   }
 }
 void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {

@@ -85,13 +85,18 @@ struct FragRef { int key, meta; };
 
 struct WarpQueue {
   SegJob job[32][DVG_LANE_JOBS];
-  FragRef front[DVG_FRONT][32];            // lane l's candidate fragments in front[0..nf)[l]
   unsigned result[32];
   int offs[33];
   unsigned char pend[32 * DVG_LANE_JOBS];  // jobs the fp32 decision left open
   unsigned pend_lanes;                     // lanes that own one of them
   int qid[32];                             // the lanes' query numbers (deferral)
+  // lane l's candidate fragments in front[0..nf)[l] (SharedFront).  Last, so
+  // that kernels whose lanes keep their fronts themselves (LocalFront) give
+  // each warp only the part before it (kQueueLocalBytes).
+  FragRef front[DVG_FRONT][32];
 };
+// bytes of a warp queue without its shared fragment front, rounded to 16
+#define DVG_QUEUE_LOCAL_BYTES ((int)((offsetof(WarpQueue, front) + 15) / 16 * 16))
 static_assert(32 * DVG_LANE_JOBS <= 256, "job numbers are stored in bytes");
 
 // A lane's fragment front: its column of the warp queue's front in shared
