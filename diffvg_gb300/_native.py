@@ -32,7 +32,7 @@ DVG_FLAG_NO_FRAG_CACHE = 4
 
 EXPORTS = ('dvg_scene_create', 'dvg_scene_destroy', 'dvg_scene_update_params', 'dvg_render_forward',
            'dvg_render_backward',
-           'dvg_scene_sync', 'dvg_scene_profile', 'dvg_scene_profile_read', 'dvg_mse_grad', 'dvg_adam_step',
+           'dvg_scene_sync', 'dvg_scene_info', 'dvg_scene_profile', 'dvg_scene_profile_read', 'dvg_mse_grad', 'dvg_adam_step',
            'dvg_batch_create', 'dvg_batch_destroy', 'dvg_batch_forward', 'dvg_batch_backward',
            'dvg_last_error', 'dvg_version')
 
@@ -117,6 +117,8 @@ def load(build_if_missing=True):
         lib.dvg_render_backward.restype = ctypes.c_int
         lib.dvg_scene_sync.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         lib.dvg_scene_sync.restype = ctypes.c_int
+        lib.dvg_scene_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+        lib.dvg_scene_info.restype = ctypes.c_int
         lib.dvg_scene_update_params.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
         lib.dvg_scene_update_params.restype = ctypes.c_int
         lib.dvg_scene_profile.argtypes = [ctypes.c_void_p, ctypes.c_int]

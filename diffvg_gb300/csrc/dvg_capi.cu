@@ -795,6 +795,14 @@ int dvg_scene_profile_read(DvgScene *sc, DvgKernelTime *out, int max_entries, in
   return DVG_OK;
 }
 
+int dvg_scene_info(const DvgScene *sc, int32_t *num_params, int32_t *device) {
+  dvg::clear_error();
+  if (!sc) return fail(DVG_ERR_INVALID, "scene is NULL");
+  if (num_params) *num_params = sc->d.num_params;
+  if (device) *device = sc->device;
+  return DVG_OK;
+}
+
 int dvg_scene_sync(DvgScene *sc, void *stream) {
   dvg::clear_error();
   if (!sc) return fail(DVG_ERR_INVALID, "scene is NULL");

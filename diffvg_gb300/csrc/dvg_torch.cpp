@@ -21,6 +21,17 @@ namespace {
 
 DvgScene *scene_of(int64_t handle) { return reinterpret_cast<DvgScene *>(static_cast<intptr_t>(handle)); }
 
+// the scene's parameter count and device (dvg_scene_info)
+void scene_sizes(int64_t handle, int64_t &num_params, int64_t &device) {
+  int32_t np = 0, dev = 0;
+  TORCH_CHECK(dvg_scene_info(scene_of(handle), &np, &dev) == DVG_OK, "invalid scene handle");
+  num_params = np;
+  device = dev;
+}
+void check_device(const std::optional<at::Tensor> &t, int64_t device, const char *what) {
+  TORCH_CHECK(!t.has_value() || t->get_device() == device, what, " is not on the scene's device cuda:", device);
+}
+
 // a float32, contiguous CUDA tensor with at least n elements, or (optional) none
 float *floats(const at::Tensor &t, int64_t n, const char *what) {
   TORCH_CHECK(t.is_cuda(), what, " must be a CUDA tensor");
@@ -96,7 +107,12 @@ int64_t render_forward(int64_t scene, const std::optional<at::Tensor> &params,
                        const std::optional<at::Tensor> &background, const std::optional<at::Tensor> &eval_positions,
                        const std::optional<at::Tensor> &image, const std::optional<at::Tensor> &sdf,
                        c10::IntArrayRef dims, int64_t seed, int64_t flags) {
+  TORCH_CHECK(dims.size() == 5, "dims = [width, height, num_samples_x, num_samples_y, use_prefiltering]");
   TORCH_CHECK(image.has_value() != sdf.has_value(), "exactly one of image / sdf");
+  int64_t np, dev;
+  scene_sizes(scene, np, dev);
+  floats(params, np, "params");
+  for (const auto *t : {&params, &background, &eval_positions, &image, &sdf}) check_device(*t, dev, "a tensor");
   DvgRenderArgs a = render_args(dims, seed, flags, params, background, eval_positions);
   const at::Tensor &out = image.has_value() ? *image : *sdf;
   int64_t n = image.has_value() ? 4 * dims[0] * dims[1]
@@ -112,12 +128,19 @@ int64_t render_backward(int64_t scene, const std::optional<at::Tensor> &params,
                         const at::Tensor &d_params, const std::optional<at::Tensor> &d_background,
                         const std::optional<at::Tensor> &d_translation, c10::IntArrayRef dims, int64_t seed,
                         int64_t flags) {
+  TORCH_CHECK(dims.size() == 5, "dims = [width, height, num_samples_x, num_samples_y, use_prefiltering]");
   TORCH_CHECK(d_image.has_value() != d_sdf.has_value(), "exactly one of d_image / d_sdf");
+  int64_t np, dev;
+  scene_sizes(scene, np, dev);
+  floats(params, np, "params");
+  for (const auto *t : {&params, &background, &eval_positions, &d_image, &d_sdf, &d_background, &d_translation})
+    check_device(*t, dev, "a tensor");
+  check_device(d_params, dev, "d_params");
   DvgRenderArgs a = render_args(dims, seed, flags, params, background, eval_positions);
   int64_t npx = dims[0] * dims[1];
   const float *di = floats(d_image, 4 * npx, "d_image");
   const float *ds = floats(d_sdf, a.num_eval_positions > 0 ? a.num_eval_positions : npx, "d_sdf");
-  float *dp = floats(d_params, -1, "d_params");
+  float *dp = floats(d_params, np, "d_params");
   float *db = floats(d_background, 4 * npx, "d_background");
   float *dt = floats(d_translation, 2 * npx, "d_translation");
   return dvg_render_backward(scene_of(scene), &a, di, ds, dp, db, dt, stream_for(d_params));
@@ -125,9 +148,12 @@ int64_t render_backward(int64_t scene, const std::optional<at::Tensor> &params,
 
 int64_t scene_update_params(int64_t scene, const at::Tensor &params) {
   TORCH_CHECK(params.scalar_type() == at::kFloat && params.is_contiguous(), "params must be contiguous float32");
+  int64_t np, dev;
+  scene_sizes(scene, np, dev);
+  TORCH_CHECK(params.numel() >= np, "params has ", params.numel(), " elements, needs ", np);
+  TORCH_CHECK(!params.is_cuda() || params.get_device() == dev, "params is not on the scene's device");
   void *stream = params.is_cuda() ? stream_for(params) : nullptr;
-  return dvg_scene_update_params(scene_of(scene), params.data_ptr<float>(), static_cast<int32_t>(params.numel()),
-                                 stream);
+  return dvg_scene_update_params(scene_of(scene), params.data_ptr<float>(), static_cast<int32_t>(np), stream);
 }
 
 int64_t scene_sync(int64_t scene, int64_t device) {

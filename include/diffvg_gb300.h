@@ -196,6 +196,12 @@ int dvg_render_backward(DvgScene *scene, const DvgRenderArgs *args,
  * reference is synchronous). */
 int dvg_scene_sync(DvgScene *scene, void *stream);
 
+/* Sizes a caller allocates for a scene: the floats of its parameter arena
+ * (and of the gradient arena dvg_render_backward writes) and its device.
+ * Either pointer may be NULL.  No reference counterpart (the reference's
+ * Scene owns its gradient buffers). */
+int dvg_scene_info(const DvgScene *scene, int32_t *num_params, int32_t *device);
+
 /* Per-kernel GPU time of the calls on a scene, measured with CUDA events
  * recorded on the call's stream around each kernel (no reference
  * counterpart; the reference only has a wall-clock print_timing flag,

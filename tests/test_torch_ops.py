@@ -41,20 +41,34 @@ def test_scene_create_takes_int32_cpu_topology_only():
         ops.scene_create(z, z, z, z, [16, 16, 0, 0, 1, 0, 0])
 
 
-def test_render_operators_check_tensors_before_the_call():
-    """Wrong device, dtype or size fails in the operator, before the C ABI
-    sees any pointer (the scene handle 0 is never used)."""
+def test_render_operators_check_arguments_before_the_call():
+    """Malformed arguments fail in the operator before any render entry point
+    runs: the dims list, the output choice, and the scene handle (a NULL
+    handle is reported by dvg_scene_info; tensors are then checked against
+    the scene's parameter count and device)."""
     ops = _native.ops()
     dims = [8, 8, 1, 1, 0]
     cpu = torch.zeros(8, 8, 4)
-    with pytest.raises(RuntimeError, match='CUDA'):
-        ops.render_forward(0, None, None, None, cpu, None, dims, 0, 0)
-    with pytest.raises(RuntimeError, match='exactly one of image / sdf'):
-        ops.render_forward(0, None, None, None, None, None, dims, 0, 0)
     with pytest.raises(RuntimeError, match='dims'):
         ops.render_forward(0, None, None, None, cpu, None, [8, 8], 0, 0)
+    with pytest.raises(RuntimeError, match='exactly one of image / sdf'):
+        ops.render_forward(0, None, None, None, None, None, dims, 0, 0)
+    with pytest.raises(RuntimeError, match='invalid scene handle'):
+        ops.render_forward(0, None, None, None, cpu, None, dims, 0, 0)
     with pytest.raises(RuntimeError, match='exactly one of d_image / d_sdf'):
         ops.render_backward(0, None, None, None, None, None, torch.zeros(4), None, None, dims, 0, 0)
+    with pytest.raises(RuntimeError, match='invalid scene handle'):
+        ops.render_backward(0, None, None, None, cpu, None, torch.zeros(4), None, None, dims, 0, 0)
+    with pytest.raises(RuntimeError, match='invalid scene handle'):
+        ops.scene_update_params(0, torch.zeros(4))
+
+
+def test_scene_info_reports_a_null_scene():
+    import ctypes
+    lib = _native.load()
+    n = ctypes.c_int32(-7)
+    assert lib.dvg_scene_info(None, ctypes.byref(n), None) == _native.DVG_ERR_INVALID
+    assert n.value == -7
 
 
 def test_seeds_keep_their_64_bits():
