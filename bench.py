@@ -53,7 +53,20 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(canvas=512, num_paths=2048, spp=(2, 2), seed=1, target_seed=2, filter='box', radius=0.5)
 METRIC = 'fwd+bwd Msamples/s'
 UNIT = 'Msamples/s'
-PREP_KERNELS = 7  # kernels launched by one scene preparation
+
+
+def launches_per_span(packed):
+    """Kernel launches inside each span the scene's profile table times
+    (csrc/dvg_capi.cu timed(), csrc/dvg_render.cu and dvg_prep.cu launchers):
+    preparation 11 kernels (12 with long-path band lists); the sampled
+    forward, and the boundary pass of a scene of 8+ groups, add the deferred
+    root walks (jobs, roots, finish)."""
+    import numpy as np
+    info = np.asarray(packed.shape_info).reshape(-1, 8)
+    banded = bool(((info[:, 0] == 2) & (info[:, 3] >= 64)).any()) if info.size else False
+    defer = packed.num_groups >= 8
+    return {'prepare': 11 + (1 if banded else 0), 'weight': 1, 'sample_fwd': 4 if defer else 1, 'resolve': 1,
+            'sample_bwd': 2, 'edge': 7 if defer else 4, 'sdf': 1, 'bg_combine': 1}
 HEADLINE = 'stroke_512_2x2'  # the headline workload's name among the counted configurations
 
 
@@ -331,9 +344,10 @@ def run_ours(args):
     scene.profile(False)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     value, total_ms = aggregate_throughput(float(sum(step_ms)), n_samples, args.steps, ws, dev)
+    per_span = launches_per_span(packed)
     gpu_launches = 0
     for name, (cnt, _) in kernels.items():
-        gpu_launches += cnt * (PREP_KERNELS if name == 'prepare' else 1)
+        gpu_launches += cnt * per_span.get(name, 1)
 
     # ---------------- roofline of the dominant kernel ----------------
     peak, peak_kind = _peaks()
