@@ -65,11 +65,12 @@ namespace dvg {
 // statically.
 extern __shared__ __align__(16) unsigned char dvg_smem[];
 constexpr int kQueueBytes = 8 * (int)sizeof(WarpQueue);
-// per-warp stride of the queues of the kernels that keep fragment fronts per
-// lane (the forward and boundary walks): their queues stop before the front
-constexpr int kQueueLocalBytes = DVG_QUEUE_LOCAL_BYTES;
-__device__ __forceinline__ WarpQueue *warp_queue(int stride = (int)sizeof(WarpQueue)) {
-  return reinterpret_cast<WarpQueue *>(dvg_smem + (threadIdx.x >> 5) * stride);
+__device__ __forceinline__ WarpQueue *warp_queue() { return reinterpret_cast<WarpQueue *>(dvg_smem) + (threadIdx.x >> 5); }
+// the queue of a kernel whose lanes keep their fragment fronts themselves
+// (the forward and boundary walks): it stops before the shared front
+template <class Q>
+__device__ __forceinline__ Q *warp_queue_local() {
+  return reinterpret_cast<Q *>(dvg_smem + (threadIdx.x >> 5) * queue_local_bytes<Q>());
 }
 
 // Kernels that accumulate into caller-visible outputs do nothing when the
@@ -156,9 +157,9 @@ __device__ __forceinline__ bool block_group(const DevRender &R, int &tile, int &
 
 // One sample of the forward sample pass: thread tid of the 256-thread group
 // cta_y of image tile `tile` (a warp's lanes call it together).
-template <bool PREFILTER>
+template <bool PREFILTER, class Q>
 __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRender &R, int tile, int cta_y, int tid,
-                                               float4 *samples, WarpQueue *q, int lane,
+                                               float4 *samples, Q *q, int lane,
                                                const EdgeRecords *D = nullptr) {
   int tiles_x = (R.w + DVG_TILE - 1) / DVG_TILE;
   int tx = tile % tiles_x, ty = tile / tiles_x;
@@ -197,14 +198,14 @@ __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRende
 // of its tile's 256-sample groups (whole warps leave when their group is past
 // the tile's spp groups); launch_sample_fwd uses blocks of 256 when a tile
 // has fewer samples than a block.
-template <bool PREFILTER>
+template <bool PREFILTER, class Q>
 __global__ void __launch_bounds__(PREFILTER ? DVG_PF_FWD_THREADS : DVG_FWD_THREADS,
                                   DVG_BLOCKS_FOR(PREFILTER ? DVG_PF_FWD_THREADS : DVG_FWD_THREADS))
     k_sample_fwd(const __grid_constant__ DevScene S, const __grid_constant__ DevRender R, float4 *samples,
                  const __grid_constant__ EdgeRecords D) {
   int cy = blockIdx.y * (blockDim.x >> 8) + (threadIdx.x >> 8);
   if (cy >= R.spp) return;
-  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, cy, threadIdx.x & 255, samples, warp_queue(kQueueLocalBytes),
+  sample_fwd_one<PREFILTER>(S, R, blockIdx.x, cy, threadIdx.x & 255, samples, warp_queue_local<Q>(),
                             threadIdx.x & 31, D.job_a ? &D : nullptr);
 }
 
@@ -557,9 +558,9 @@ DI void edge_accumulate(const DevScene &S, const DevRender &R, int g, int s, v2 
 // costs.
 // One lane (gi: index of the lane over the pass) of the boundary pass; R
 // carries the filter loaded by load_filter; a warp's lanes call it together.
-template <bool PAIRS>
+template <bool PAIRS, class Q>
 __device__ __forceinline__ void edge_eval_one(const DevScene &S, const DevRender &R, const EdgeRecords &E, long long gi,
-                                              WarpQueue *q, int lane) {
+                                              Q *q, int lane) {
   const unsigned full = 0xffffffffu;
   int i = (int)(PAIRS ? gi >> 1 : gi);
   bool outside = PAIRS && (gi & 1);
@@ -611,13 +612,13 @@ __device__ __forceinline__ void edge_eval_one(const DevScene &S, const DevRender
   edge_accumulate(S, R, g, s, bpt, normal, lpt, pdf, t, bd, cin, hin, cout, hout);
 }
 
-template <bool PAIRS>
+template <bool PAIRS, class Q>
 __global__ void __launch_bounds__(PAIRS ? DVG_EDGE_THREADS : DVG_EDGE1_THREADS,
                                   PAIRS ? DVG_EDGE_MIN_BLOCKS : DVG_SAMPLE_MIN_BLOCKS)
     k_edge_eval(const __grid_constant__ DevScene S, DevRender R0, const __grid_constant__ EdgeRecords E) {
   DevRender R = load_filter(R0, nullptr);
-  edge_eval_one<PAIRS>(S, R, E, (long long)blockIdx.x * blockDim.x + threadIdx.x, warp_queue(kQueueLocalBytes),
-                      threadIdx.x & 31);
+  edge_eval_one<PAIRS>(S, R, E, (long long)blockIdx.x * blockDim.x + threadIdx.x, warp_queue_local<Q>(),
+                       threadIdx.x & 31);
 }
 
 // The deferred fp64 root walks of the paired boundary pass, one per thread
@@ -982,7 +983,10 @@ static inline dim3 group_grid(const DevRender &R, int threads) {
 
 // Opts kernel `id` (one of QueueKernel) into kQueueBytes of dynamic shared
 // memory, once per device (devices 0-63; the others every call).
-enum QueueKernel { QK_FWD, QK_BWD, QK_EDGE_PAIRS, QK_EDGE, QK_FWD_BATCH, QK_BWD_BATCH, QK_EDGE_BATCH, QK_COUNT };
+enum QueueKernel {
+  QK_FWD, QK_FWD_WIDE, QK_BWD, QK_EDGE_PAIRS, QK_EDGE_PAIRS_WIDE, QK_EDGE, QK_FWD_BATCH, QK_BWD_BATCH, QK_EDGE_BATCH,
+  QK_COUNT
+};
 template <class K>
 static void allow_queues(K *kernel, int id, int bytes = kQueueBytes) {
   static std::atomic<unsigned long long> done[QK_COUNT];
@@ -1024,14 +1028,21 @@ void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, c
   if (R.prefilter) {
     int threads = 256 * R.spp >= DVG_PF_FWD_THREADS ? DVG_PF_FWD_THREADS : 256;
     dim3 grid(tiles_of(R), (256 * R.spp + threads - 1) / threads);
-    k_sample_fwd<true><<<grid, threads, 0, st>>>(S, R, samples, none);
+    k_sample_fwd<true, WarpQueue><<<grid, threads, 0, st>>>(S, R, samples, none);
   } else {
     bool defer = D && D->job_a;
     if (defer) cudaMemsetAsync(D->counts, 0, 8 * sizeof(int), st);
     int threads = 256 * R.spp >= DVG_FWD_THREADS ? DVG_FWD_THREADS : 256;
     dim3 grid(tiles_of(R), (256 * R.spp + threads - 1) / threads);
-    allow_queues(k_sample_fwd<false>, QK_FWD, DVG_FWD_THREADS / 32 * kQueueLocalBytes);
-    k_sample_fwd<false><<<grid, threads, threads / 32 * kQueueLocalBytes, st>>>(S, R, samples, defer ? *D : none);
+    if (S.wide_queues) {
+      constexpr int qb = queue_local_bytes<WarpQueueWide>();
+      allow_queues(k_sample_fwd<false, WarpQueueWide>, QK_FWD_WIDE, DVG_FWD_THREADS / 32 * qb);
+      k_sample_fwd<false, WarpQueueWide><<<grid, threads, threads / 32 * qb, st>>>(S, R, samples, defer ? *D : none);
+    } else {
+      constexpr int qb = queue_local_bytes<WarpQueue>();
+      allow_queues(k_sample_fwd<false, WarpQueue>, QK_FWD, DVG_FWD_THREADS / 32 * qb);
+      k_sample_fwd<false, WarpQueue><<<grid, threads, threads / 32 * qb, st>>>(S, R, samples, defer ? *D : none);
+    }
     if (defer) {
       k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, *D);
       k_edge_roots<<<persistent_grid(6), 256, 0, st>>>(S, *D);
@@ -1074,18 +1085,26 @@ void launch_edge_setup(const DevScene &S, const DevRender &R, const EdgeRecords 
 void launch_edge_eval(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {
   long long n = (long long)R.w * R.h * R.spp;
   if (S.num_groups >= 8) {  // two lanes per sample
-    allow_queues(k_edge_eval<true>, QK_EDGE_PAIRS, DVG_EDGE_THREADS / 32 * kQueueLocalBytes);
-    k_edge_eval<true><<<(unsigned)((2 * n + DVG_EDGE_THREADS - 1) / DVG_EDGE_THREADS), DVG_EDGE_THREADS,
-                        DVG_EDGE_THREADS / 32 * kQueueLocalBytes, st>>>(S, R, E);
+    unsigned blocks = (unsigned)((2 * n + DVG_EDGE_THREADS - 1) / DVG_EDGE_THREADS);
+    if (S.wide_queues) {
+      constexpr int qb = queue_local_bytes<WarpQueueWide>();
+      allow_queues(k_edge_eval<true, WarpQueueWide>, QK_EDGE_PAIRS_WIDE, DVG_EDGE_THREADS / 32 * qb);
+      k_edge_eval<true, WarpQueueWide><<<blocks, DVG_EDGE_THREADS, DVG_EDGE_THREADS / 32 * qb, st>>>(S, R, E);
+    } else {
+      constexpr int qb = queue_local_bytes<WarpQueue>();
+      allow_queues(k_edge_eval<true, WarpQueue>, QK_EDGE_PAIRS, DVG_EDGE_THREADS / 32 * qb);
+      k_edge_eval<true, WarpQueue><<<blocks, DVG_EDGE_THREADS, DVG_EDGE_THREADS / 32 * qb, st>>>(S, R, E);
+    }
     if (E.job_a) {
       k_edge_jobs<<<persistent_grid(8), 256, 0, st>>>(S, E);
       k_edge_roots<<<persistent_grid(6), 256, 0, st>>>(S, E);
       k_edge_finish<<<persistent_grid(8), 256, 0, st>>>(S, R, E);
     }
   } else {
-    allow_queues(k_edge_eval<false>, QK_EDGE, DVG_EDGE1_THREADS / 32 * kQueueLocalBytes);
-    k_edge_eval<false><<<(unsigned)((n + DVG_EDGE1_THREADS - 1) / DVG_EDGE1_THREADS), DVG_EDGE1_THREADS,
-                         DVG_EDGE1_THREADS / 32 * kQueueLocalBytes, st>>>(S, R, E);
+    constexpr int qb = queue_local_bytes<WarpQueue>();
+    allow_queues(k_edge_eval<false, WarpQueue>, QK_EDGE, DVG_EDGE1_THREADS / 32 * qb);
+    k_edge_eval<false, WarpQueue><<<(unsigned)((n + DVG_EDGE1_THREADS - 1) / DVG_EDGE1_THREADS), DVG_EDGE1_THREADS,
+                                    DVG_EDGE1_THREADS / 32 * qb, st>>>(S, R, E);
   }
 }
 void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cudaStream_t st) {

@@ -14,6 +14,9 @@
 
 #include "dvg_adjoint.cuh"
 
+#include <cstddef>
+#include <type_traits>
+
 // Sample position of sample idx (diffvg.cpp:1164-1180).
 DI v2 sample_pos(const DevRender &R, int idx, bool prefilter, int &x, int &y) {
   Pcg rng = pcg_init(idx, R.seed);
@@ -68,7 +71,16 @@ DI float4 finish_color(float4 acc) {
 // whose sample happens to sit near a curve.  Each lane finally blends its
 // fragments in group order with the solved results.  Every lane of the warp
 // must call the batched functions (inactive lanes pass active = false).
+#ifndef DVG_LANE_JOBS
 #define DVG_LANE_JOBS 8
+#endif
+// jobs per lane of the wide queues: the forward and boundary walks of
+// stroke-heavy scenes, whose samples queue more segment tests than 8 often
+// enough that the overflow (decided one lane at a time) costs more than the
+// shared memory the larger queue takes from L1
+#ifndef DVG_LANE_JOBS_WIDE
+#define DVG_LANE_JOBS_WIDE 12
+#endif
 // Candidate fragments a lane holds before the warp decides and blends them
 // (its column of the warp's fragment front, in shared memory).  A group adds
 // at most two (its stroke and its fill).
@@ -83,21 +95,31 @@ struct SegJob { int shape, seg; float x, y, r; };
 struct FragRef { int key, meta; };
 #define DVG_META_HIT (1 << 31)
 
-struct WarpQueue {
-  SegJob job[32][DVG_LANE_JOBS];
+template <int CAP>
+struct WarpQueueT {
+  static constexpr int kJobs = CAP;
+  // a job's number in the warp's queue
+  typedef typename std::conditional<(32 * CAP <= 256), unsigned char, unsigned short>::type JobNum;
+  SegJob job[32][CAP];
   unsigned result[32];
   int offs[33];
-  unsigned char pend[32 * DVG_LANE_JOBS];  // jobs the fp32 decision left open
+  JobNum pend[32 * CAP];                   // jobs the fp32 decision left open
   unsigned pend_lanes;                     // lanes that own one of them
   int qid[32];                             // the lanes' query numbers (deferral)
   // lane l's candidate fragments in front[0..nf)[l] (SharedFront).  Last, so
   // that kernels whose lanes keep their fronts themselves (LocalFront) give
-  // each warp only the part before it (kQueueLocalBytes).
+  // each warp only the part before it (queue_local_bytes).
   FragRef front[DVG_FRONT][32];
 };
+typedef WarpQueueT<DVG_LANE_JOBS> WarpQueue;
+typedef WarpQueueT<DVG_LANE_JOBS_WIDE> WarpQueueWide;
+static_assert(DVG_LANE_JOBS <= 31 && DVG_LANE_JOBS_WIDE <= 31,
+              "a lane's jobs are bits of a 32-bit mask and of an 8-bit range");
 // bytes of a warp queue without its shared fragment front, rounded to 16
-#define DVG_QUEUE_LOCAL_BYTES ((int)((offsetof(WarpQueue, front) + 15) / 16 * 16))
-static_assert(32 * DVG_LANE_JOBS <= 256, "job numbers are stored in bytes");
+template <class Q>
+__host__ __device__ constexpr int queue_local_bytes() {
+  return (int)((offsetof(Q, front) + 15) / 16 * 16);
+}
 
 // A lane's fragment front: its column of the warp queue's front in shared
 // memory (the interior adjoint, which keeps at most 16 hits itself), or
@@ -116,13 +138,14 @@ struct SharedFront {
 struct LocalFront {
   static constexpr int kCap = DVG_LOCAL_FRONT;
   FragRef f[DVG_LOCAL_FRONT];
-  DI LocalFront(WarpQueue *, int) {}
+  DI LocalFront(const void *, int) {}
   DI FragRef &operator[](int i) { return f[i]; }
   DI const FragRef &operator[](int i) const { return f[i]; }
 };
 
 // owner lane and slot of the warp's j-th queued job
-DI const SegJob &warp_job(const WarpQueue *q, int j, int &owner, int &idx) {
+template <class Q>
+DI const SegJob &warp_job(const Q *q, int j, int &owner, int &idx) {
   int lo = 0, hi = 31;  // last lane with offs <= j
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
@@ -136,7 +159,8 @@ DI const SegJob &warp_job(const WarpQueue *q, int j, int &owner, int &idx) {
 // Decide every queued job of the warp, spread over its lanes, with the fp32
 // decision; the jobs it leaves open are listed in q->pend (their owners in
 // q->pend_lanes).  Returns how many (the same in every lane).
-DI int warp_decide(const DevScene &S, WarpQueue *q, int lane, int njobs) {
+template <class Q>
+DI int warp_decide(const DevScene &S, Q *q, int lane, int njobs) {
   const unsigned full = 0xffffffffu;
   int incl = njobs;
 #pragma unroll
@@ -166,7 +190,7 @@ DI int warp_decide(const DevScene &S, WarpQueue *q, int lane, int njobs) {
     bool pending = valid && f == 2;
     unsigned bal = __ballot_sync(full, pending);
     if (pending) {
-      q->pend[npend + __popc(bal & ((1u << lane) - 1u))] = (unsigned char)j;
+      q->pend[npend + __popc(bal & ((1u << lane) - 1u))] = (typename Q::JobNum)j;
       atomicOr(&q->pend_lanes, 1u << owner);
     }
     npend += __popc(bal);
@@ -177,7 +201,8 @@ DI int warp_decide(const DevScene &S, WarpQueue *q, int lane, int njobs) {
 
 // The fp64 solves of the warp's open jobs, compacted so that as many lanes
 // as there are jobs run them together.
-DI void warp_fp64(const DevScene &S, WarpQueue *q, int lane, int npend) {
+template <class Q>
+DI void warp_fp64(const DevScene &S, Q *q, int lane, int npend) {
   #pragma unroll 1
   for (int k = lane; k < npend; k += 32) {
     int owner, idx;
@@ -193,7 +218,8 @@ DI void warp_fp64(const DevScene &S, WarpQueue *q, int lane, int npend) {
 
 // Decide every queued job of the warp: the fp32 decision first, then the
 // fp64 solve of the jobs it left open.
-DI void warp_solve(const DevScene &S, WarpQueue *q, int lane, int njobs) {
+template <class Q>
+DI void warp_solve(const DevScene &S, Q *q, int lane, int njobs) {
   warp_fp64(S, q, lane, warp_decide(S, q, lane, njobs));
 }
 
@@ -228,8 +254,8 @@ DI bool frag_hit(int meta, unsigned res) {
 // is set (the same in every lane).  Returns the
 // number of fragments left in the lane's front; overflow is set when the
 // sample has more than DVG_MAX_FRAGMENTS candidates (diffvg.cpp:542).
-template <class Front, class Flush>
-DI int collect_fragments(const DevScene &S, v2 pt, WarpQueue *q, Front &front, int lane, int &njobs, EdgeQ *eq,
+template <class Q, class Front, class Flush>
+DI int collect_fragments(const DevScene &S, v2 pt, Q *q, Front &front, int lane, int &njobs, EdgeQ *eq,
                          unsigned &eq_jobs, bool &overflow, bool &flushed, bool active, Flush &flush) {
   const unsigned full = 0xffffffffu;
   int k = 0, e = 0;
@@ -315,7 +341,7 @@ DI int collect_fragments(const DevScene &S, v2 pt, WarpQueue *q, Front &front, i
         } else if (test) {
           f = within_segment_pre(S, c.x, c.y, c.z, 0, a.z, a.w, a.x, lp, r);  // the lanes' tests run together
           if (f == 2) {
-            if (njobs < DVG_LANE_JOBS) {
+            if (njobs < Q::kJobs) {
               q->job[lane][njobs] = SegJob{s, a.x, lp.x, lp.y, r};
               if (mark) eq_jobs |= 1u << njobs;
               njobs++;
@@ -484,8 +510,8 @@ DI float4 blend_deferred(const DevScene &S, const float4 *bg, v2 pt, EdgeQ *eq, 
 // word_w}; dq_col[qid] = acc), when the lists have room; returns whether
 // they had (the same in every lane) and sets deferred in the lanes that
 // parked.  Without room nothing is stored.
-template <class Front>
-DI bool park_open_jobs(const EdgeRecords &D, WarpQueue *q, int lane, const Front &front, int nf, bool active,
+template <class Q, class Front>
+DI bool park_open_jobs(const EdgeRecords &D, Q *q, int lane, const Front &front, int nf, bool active,
                        int npend, int qid, int word_y, int word_w, float4 acc, bool &deferred) {
   const unsigned full = 0xffffffffu;
   bool mine = active && ((q->pend_lanes >> lane) & 1u);
@@ -541,8 +567,9 @@ DI bool park_open_jobs(const EdgeRecords &D, WarpQueue *q, int lane, const Front
 // lanes that own them park their fragments and blend state under their
 // sample number qid, report deferred = true and get their colour from
 // k_fwd_finish.
+template <class Q>
 static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const float4 *bg, v2 screen_pt, EdgeQ *eq,
-                                                      bool active, WarpQueue *q, int lane,
+                                                      bool active, Q *q, int lane,
                                                       const HitCache *hc = nullptr,
                                                       const EdgeRecords *D = nullptr, int qid = 0,
                                                       bool *deferred = nullptr) {
@@ -581,8 +608,9 @@ static __device__ __noinline__ float4 sample_color_fwd(const DevScene &S, const 
 // their walk already flushed in E.dq_col[qid], and report deferred = true
 // (their colour comes from k_edge_finish).  Without room the warp solves its
 // jobs in place, as sample_color_fwd does.
+template <class Q>
 static __device__ __noinline__ float4 sample_color_edge(const DevScene &S, const EdgeRecords &E, const float4 *bg,
-                                                       v2 screen_pt, EdgeQ *eq, bool active, WarpQueue *q, int lane,
+                                                       v2 screen_pt, EdgeQ *eq, bool active, Q *q, int lane,
                                                        int qid, bool &deferred) {
   int njobs = 0;
   unsigned eq_jobs = 0;
