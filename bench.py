@@ -58,14 +58,20 @@ UNIT = 'Msamples/s'
 def launches_per_span(packed):
     """Kernel launches inside each span the scene's profile table times
     (csrc/dvg_capi.cu timed(), csrc/dvg_render.cu and dvg_prep.cu launchers):
-    preparation 11 kernels (12 with long-path band lists); the sampled
+    preparation 7 to 12 kernels (path, segment, band-list and stroke-record
+    kernels only where the scene has them); the sampled
     forward, and the boundary pass of a scene of 8+ groups, add the deferred
     root walks (jobs, roots, finish)."""
     import numpy as np
     info = np.asarray(packed.shape_info).reshape(-1, 8)
+    groups = np.asarray(packed.group_info).reshape(-1, 12)
+    paths = bool((info[:, 0] == 2).any()) if info.size else False
     banded = bool(((info[:, 0] == 2) & (info[:, 3] >= 64)).any()) if info.size else False
+    stroked = bool((groups[:, 5] != -1).any()) if groups.size else False
+    prep = 7 + (1 if paths else 0) + (1 if np.asarray(packed.segment_ctrl).size else 0) + (1 if banded else 0) \
+        + (2 if stroked else 0)
     defer = packed.num_groups >= 8
-    return {'prepare': 11 + (1 if banded else 0), 'weight': 1, 'sample_fwd': 4 if defer else 1, 'resolve': 1,
+    return {'prepare': prep, 'weight': 1, 'sample_fwd': 4 if defer else 1, 'resolve': 1,
             'sample_bwd': 2, 'edge': 7 if defer else 4, 'sdf': 1, 'bg_combine': 1}
 HEADLINE = 'stroke_512_2x2'  # the headline workload's name among the counted configurations
 

@@ -78,6 +78,7 @@ struct DvgScene {
   int *seg_order = nullptr, *tile_start = nullptr, *tile_count = nullptr, *scratch = nullptr;
   int4 *g_tile_range = nullptr;
   int num_records = 0;  // stroke records (k_rec_fill)
+  int num_paths = 0;    // path shapes
   int2 *g_rec = nullptr;
   float4 *rec_box = nullptr;
   int4 *rec_a = nullptr, *rec_b = nullptr;
@@ -292,6 +293,8 @@ DevScene make_dev(DvgScene *sc, const float *params) {
   S.seg_tpts = sc->seg_tpts;
   S.seg_th = sc->seg_th;
   S.wide_queues = sc->wide_queues ? 1 : 0;
+  S.num_paths = sc->num_paths;
+  S.num_records = sc->num_records;
   S.shape_band = sc->shape_band;
   S.band_geo = sc->band_geo;
   S.band_n = sc->band_n;
@@ -612,6 +615,8 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   int NT = sc->num_total;
   sc->num_records = dvg::count_stroke_records(desc);
   int NR = sc->num_records;
+  for (int i = 0; i < S; i++)
+    sc->num_paths += desc->shape_info[(size_t)i * DVG_SHAPE_INFO_STRIDE + DVG_SHAPE_KIND] == DVG_PATH ? 1 : 0;
   // band lists of the paths with DVG_BAND_MIN_SEGMENTS or more segments: up
   // to one band per four segments (4 to 128), room for each segment to meet
   // four bands on average

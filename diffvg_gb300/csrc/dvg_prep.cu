@@ -742,11 +742,11 @@ cudaError_t launch_prepare(const DevScene &S, int tile_cap, int *bin_total, int4
   int T = S.tiles_x * S.tiles_y;
   if (G > 0) k_group_xform<<<(G + 127) / 128, 128, 0, st>>>(S);
   if (NS > 0) k_shape_prep<<<(NS + 63) / 64, 64, 0, st>>>(S);
-  if (NS > 0) k_path_prep<<<(NS + 3) / 4, 128, 0, st>>>(S);
-  if (NS > 0 && S.seg_tpts) k_seg_tree<<<(NS + 3) / 4, 128, 0, st>>>(S);
+  if (NS > 0 && S.num_paths > 0) k_path_prep<<<(NS + 3) / 4, 128, 0, st>>>(S);
+  if (NS > 0 && S.num_segments > 0 && S.seg_tpts) k_seg_tree<<<(NS + 3) / 4, 128, 0, st>>>(S);
   if (NS > 0 && S.shape_band) k_band_fill<<<(NS + 3) / 4, 128, 0, st>>>(S);
   if (G > 0) k_group_prep<<<(G + 127) / 128, 128, 0, st>>>(S, g_tile_range);
-  if (G > 0) {
+  if (G > 0 && S.num_records > 0) {  // without stroke records g_rec keeps the zeros it was created with
     k_rec_scan<<<1, 1024, 0, st>>>(S);
     k_rec_fill<<<(G + 127) / 128, 128, 0, st>>>(S);
   }
