@@ -990,6 +990,7 @@ int dvg_render_backward(DvgScene *sc, const DvgRenderArgs *a, const float *d_ima
 struct DvgBatch {
   int device = 0;
   std::vector<DvgScene *> scenes;
+  bool wide = false;            // every scene stroke-heavy: the batched walks take the wide queues
   DevBuf dev;                   // BatchScene[2n], int orders and item starts, counters
   BatchScene *h_bs = nullptr;   // pinned staging of the BatchScene arrays (forward, backward)
   int *h_ints = nullptr;        // pinned staging of the orders and item starts
@@ -1091,6 +1092,8 @@ int dvg_batch_create(DvgScene *const *scenes, int num_scenes, DvgBatch **out) {
   DvgBatch *b = new DvgBatch();
   b->device = scenes[0]->device;
   b->scenes.assign(scenes, scenes + num_scenes);
+  b->wide = true;
+  for (int i = 0; i < num_scenes; i++) b->wide = b->wide && scenes[i]->wide_queues;
   DeviceGuard guard(b->device);
   int n = num_scenes;
   b->nints = batch_ints(n);
@@ -1199,7 +1202,7 @@ int dvg_batch_forward(DvgBatch *b, const DvgRenderArgs *args, float *const *imag
   e = cudaMemcpyAsync(b->d_fwd, hb, nl * sizeof(BatchScene), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_ints, b->h_ints, (2 * nl + 1) * sizeof(int), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "staging a batch");
-  dvg::launch_batch_sample_fwd(b->d_fwd, nl, b->d_ints, b->d_ints + nl, spt, ctas, b->d_counters, s);
+  dvg::launch_batch_sample_fwd(b->d_fwd, nl, b->d_ints, b->d_ints + nl, spt, ctas, b->d_counters, b->wide, s);
   if ((e = b->fork(s)) != cudaSuccess) return cuda_fail(e, "batched forward");
   for (int k = 0; k < nl; k++) {
     int i = live[k];
@@ -1305,7 +1308,8 @@ int dvg_batch_backward(DvgBatch *b, const DvgRenderArgs *args, const float *cons
     e = cudaMemcpyAsync(d_ints, ints, (2 * nl + 1 + n_edge) * sizeof(int), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "staging a batch");
   dvg::launch_batch_sample_bwd(b->d_bwd, nl, d_ints, d_ints + nl, spt, ctas, b->d_counters + 1, s);
-  if (n_edge > 0) dvg::launch_batch_edge(b->d_bwd, n_edge, d_ints + 2 * nl + 1, spt, ctas, b->d_counters + 2, s);
+  if (n_edge > 0)
+    dvg::launch_batch_edge(b->d_bwd, n_edge, d_ints + 2 * nl + 1, spt, ctas, b->d_counters + 2, b->wide, s);
   if ((e = b->fork(s)) != cudaSuccess) return cuda_fail(e, "batched backward");
   for (int k = 0; k < nl; k++)
     if (!(b->scenes[live[k]]->d.num_groups >= 8 && hb[k].E.job_a))

@@ -45,13 +45,14 @@ void launch_edge_eval(const DevScene &S, const DevRender &R, const EdgeRecords &
 // Persistent batched passes over nb scenes B[order[r]] (device arrays);
 // item_start[r] is the first work item of the r-th scene (nb + 1 entries),
 // spt the 32-sample chunks per item, counter a device int (zeroed here).
-// The boundary pass takes the scenes with paired lanes (8+ groups) only.
+// The boundary pass takes the scenes with paired lanes (8+ groups) only;
+// wide: every scene's walks take the wide queues (DevScene::wide_queues).
 void launch_batch_sample_fwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
-                             int ctas_per_sm, int *counter, cudaStream_t st);
+                             int ctas_per_sm, int *counter, bool wide, cudaStream_t st);
 void launch_batch_sample_bwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
                              int ctas_per_sm, int *counter, cudaStream_t st);
 void launch_batch_edge(const BatchScene *B, int nb, const int *order, int spt, int ctas_per_sm, int *counter,
-                       cudaStream_t st);
+                       bool wide, cudaStream_t st);
 // Signed distance output (forward: sdf, backward: d_sdf).
 void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
                 const float *d_sdf, cudaStream_t st);

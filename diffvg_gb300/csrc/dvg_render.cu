@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(PAIRS ? DVG_EDGE_THREADS : DVG_EDGE1_THREADS,
 // which go to the task list for k_edge_roots.  The brackets of a warp are
 // reserved together; when the list has no room the lanes walk their
 // brackets here, as segment_root_test does.
-__global__ void __launch_bounds__(256) k_edge_jobs(const __grid_constant__ DevScene S, const __grid_constant__ EdgeRecords E) {
+__device__ __forceinline__ void edge_jobs_all(const DevScene &S, const EdgeRecords &E) {
   const unsigned full = 0xffffffffu;
   int lane = threadIdx.x & 31;
   int n = min(*(volatile const int *)&E.counts[0], E.job_cap);
@@ -683,13 +683,17 @@ __global__ void __launch_bounds__(256) k_edge_jobs(const __grid_constant__ DevSc
   }
 }
 
+__global__ void __launch_bounds__(256) k_edge_jobs(const __grid_constant__ DevScene S, const __grid_constant__ EdgeRecords E) {
+  edge_jobs_all(S, E);
+}
+
 // The deferred fp64 root walks, second part: the safeguarded Newton /
 // bisection walk of every root bracket (quintic_root, within_distance.h:
 // 251-269), one bracket per lane and one iteration per step; a lane whose
 // walk stops runs the stroke test at the root, sets the job's bit when it
 // hits, and takes the next bracket of the list, so the lanes of a warp stay
 // busy whatever the iteration counts of their brackets.
-__global__ void __launch_bounds__(256) k_edge_roots(const __grid_constant__ DevScene S, const __grid_constant__ EdgeRecords E) {
+__device__ __forceinline__ void edge_roots_all(const DevScene &S, const EdgeRecords &E) {
   const unsigned full = 0xffffffffu;
   int lane = threadIdx.x & 31;
   int ntask = min(*(volatile const int *)&E.counts[4], E.task_cap);
@@ -749,6 +753,9 @@ __global__ void __launch_bounds__(256) k_edge_roots(const __grid_constant__ DevS
     if (cubic_root_hits(c, V2(jb.x, jb.y), t)) atomicOr(&E.dq_res[ja.x], 1u << ja.y);
     cur = -1;
   }
+}
+__global__ void __launch_bounds__(256) k_edge_roots(const __grid_constant__ DevScene S, const __grid_constant__ EdgeRecords E) {
+  edge_roots_all(S, E);
 }
 
 // Deferred boundary sample k of E.ds: blend each deferred query's fragments
@@ -868,10 +875,11 @@ __device__ __forceinline__ int batch_next(int *counter, int lane) {
 
 // forward sample pass: a scene has tiles * spp * 8 chunks (the 8 warps of a
 // tile's 256-sample group)
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+template <class Q>
+__global__ void __launch_bounds__(512, 1)
     k_sample_fwd_batch(const BatchScene *B, int nb, const int *order, const int *item_start, int spt, int *counter) {
   int lane = threadIdx.x & 31;
-  WarpQueue *q = warp_queue();
+  Q *q = warp_queue_local<Q>();
   int total = __ldg(&item_start[nb]);
   #pragma unroll 1
   for (int item = batch_next(counter, lane); item < total; item = batch_next(counter, lane)) {
@@ -922,11 +930,12 @@ __global__ void __launch_bounds__(32) k_sample_bwd_deep_batch(const BatchScene *
 // paired-lane boundary pass: a scene has ceil(2 * boundary samples / 32)
 // chunks; the sample counts are known on the device only, so every block
 // forms the item list itself
-__global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
+template <class Q>
+__global__ void __launch_bounds__(512, 1)
     k_edge_eval_batch(const BatchScene *B, int nb, const int *order, int spt, int *counter) {
   __shared__ int start[DVG_BATCH_MAX + 1];
   int lane = threadIdx.x & 31;
-  WarpQueue *q = warp_queue();
+  Q *q = warp_queue_local<Q>();
   if (threadIdx.x == 0) {
     int run = 0;
     for (int r = 0; r < nb; r++) {
@@ -951,23 +960,19 @@ __global__ void __launch_bounds__(256, DVG_SAMPLE_MIN_BLOCKS)
   }
 }
 
-// deferred fp64 walks and deferred samples of every scene of the batch
+// the deferred segment tests of every scene of the batch: their quintics
+// and root brackets (as k_edge_jobs), scene after scene
 __global__ void __launch_bounds__(256) k_edge_jobs_batch(const BatchScene *B, int nb, const int *order) {
   for (int r = 0; r < nb; r++) {
     const BatchScene &b = B[__ldg(&order[r])];
-    if (!b.E.job_a) continue;
-    int n = min(*(volatile const int *)&b.E.counts[0], b.E.job_cap);
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-      int4 ja = b.E.job_a[k];
-      if (ja.x < 0) continue;
-      float4 jb = b.E.job_b[k];
-      const DevScene &S = b.S;
-      int s = ja.z;
-      int hit = segment_root_test(S, SI(S, s, DVG_SHAPE_PARAM_OFF), SI(S, s, DVG_SHAPE_NUM_POINTS),
-                                  SI(S, s, DVG_SHAPE_THICKNESS_OFF), __ldg(&S.segment_ctrl[ja.w]),
-                                  __ldg(&S.seg_point[ja.w]), V2(jb.x, jb.y), jb.z);
-      if (hit) atomicOr(&b.E.dq_res[ja.x], 1u << ja.y);
-    }
+    if (b.E.job_a) edge_jobs_all(b.S, b.E);
+  }
+}
+// their root brackets' walks (as k_edge_roots), scene after scene
+__global__ void __launch_bounds__(256) k_edge_roots_batch(const BatchScene *B, int nb, const int *order) {
+  for (int r = 0; r < nb; r++) {
+    const BatchScene &b = B[__ldg(&order[r])];
+    if (b.E.job_a) edge_roots_all(b.S, b.E);
   }
 }
 
@@ -984,8 +989,8 @@ static inline dim3 group_grid(const DevRender &R, int threads) {
 // Opts kernel `id` (one of QueueKernel) into kQueueBytes of dynamic shared
 // memory, once per device (devices 0-63; the others every call).
 enum QueueKernel {
-  QK_FWD, QK_FWD_WIDE, QK_BWD, QK_EDGE_PAIRS, QK_EDGE_PAIRS_WIDE, QK_EDGE, QK_FWD_BATCH, QK_BWD_BATCH, QK_EDGE_BATCH,
-  QK_COUNT
+  QK_FWD, QK_FWD_WIDE, QK_BWD, QK_EDGE_PAIRS, QK_EDGE_PAIRS_WIDE, QK_EDGE, QK_FWD_BATCH, QK_FWD_BATCH_WIDE,
+  QK_BWD_BATCH, QK_EDGE_BATCH, QK_EDGE_BATCH_WIDE, QK_COUNT
 };
 template <class K>
 static void allow_queues(K *kernel, int id, int bytes = kQueueBytes) {
@@ -1112,11 +1117,24 @@ void launch_edge(const DevScene &S, const DevRender &R, const EdgeRecords &E, cu
   launch_edge_eval(S, R, E, st);
 }
 
+// The batched walks run ctas_per_sm blocks of 512 / ctas_per_sm threads per
+// SM (128 registers a thread either way), with the wide queues when every
+// scene of the batch is stroke-heavy.
 void launch_batch_sample_fwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
-                             int ctas_per_sm, int *counter, cudaStream_t st) {
+                             int ctas_per_sm, int *counter, bool wide, cudaStream_t st) {
   cudaMemsetAsync(counter, 0, sizeof(int), st);
-  allow_queues(k_sample_fwd_batch, QK_FWD_BATCH);
-  k_sample_fwd_batch<<<persistent_grid(ctas_per_sm), 256, kQueueBytes, st>>>(B, nb, order, item_start, spt, counter);
+  int threads = ctas_per_sm >= 2 ? 256 : 512;
+  if (wide) {
+    constexpr int qb = queue_local_bytes<WarpQueueWide>();
+    allow_queues(k_sample_fwd_batch<WarpQueueWide>, QK_FWD_BATCH_WIDE, 512 / 32 * qb);
+    k_sample_fwd_batch<WarpQueueWide><<<persistent_grid(ctas_per_sm), threads, threads / 32 * qb, st>>>(
+        B, nb, order, item_start, spt, counter);
+  } else {
+    constexpr int qb = queue_local_bytes<WarpQueue>();
+    allow_queues(k_sample_fwd_batch<WarpQueue>, QK_FWD_BATCH, 512 / 32 * qb);
+    k_sample_fwd_batch<WarpQueue><<<persistent_grid(ctas_per_sm), threads, threads / 32 * qb, st>>>(
+        B, nb, order, item_start, spt, counter);
+  }
 }
 void launch_batch_sample_bwd(const BatchScene *B, int nb, const int *order, const int *item_start, int spt,
                              int ctas_per_sm, int *counter, cudaStream_t st) {
@@ -1126,11 +1144,22 @@ void launch_batch_sample_bwd(const BatchScene *B, int nb, const int *order, cons
   k_sample_bwd_deep_batch<<<persistent_grid(4), 32, 0, st>>>(B, nb, order);
 }
 void launch_batch_edge(const BatchScene *B, int nb, const int *order, int spt, int ctas_per_sm, int *counter,
-                       cudaStream_t st) {
+                       bool wide, cudaStream_t st) {
   cudaMemsetAsync(counter, 0, sizeof(int), st);
-  allow_queues(k_edge_eval_batch, QK_EDGE_BATCH);
-  k_edge_eval_batch<<<persistent_grid(ctas_per_sm), 256, kQueueBytes, st>>>(B, nb, order, spt, counter);
+  int threads = ctas_per_sm >= 2 ? 256 : 512;
+  if (wide) {
+    constexpr int qb = queue_local_bytes<WarpQueueWide>();
+    allow_queues(k_edge_eval_batch<WarpQueueWide>, QK_EDGE_BATCH_WIDE, 512 / 32 * qb);
+    k_edge_eval_batch<WarpQueueWide><<<persistent_grid(ctas_per_sm), threads, threads / 32 * qb, st>>>(
+        B, nb, order, spt, counter);
+  } else {
+    constexpr int qb = queue_local_bytes<WarpQueue>();
+    allow_queues(k_edge_eval_batch<WarpQueue>, QK_EDGE_BATCH, 512 / 32 * qb);
+    k_edge_eval_batch<WarpQueue><<<persistent_grid(ctas_per_sm), threads, threads / 32 * qb, st>>>(
+        B, nb, order, spt, counter);
+  }
   k_edge_jobs_batch<<<persistent_grid(8), 256, 0, st>>>(B, nb, order);
+  k_edge_roots_batch<<<persistent_grid(6), 256, 0, st>>>(B, nb, order);
   k_edge_finish_batch<<<persistent_grid(8), 256, 0, st>>>(B, nb, order);
 }
 void launch_sdf(const DevScene &S, const DevRender &R, const float *eval_positions, int num_eval, float *sdf,
