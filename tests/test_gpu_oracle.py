@@ -113,3 +113,14 @@ def test_deep_fill_scene_prefiltered():
     from diffvg_gb300 import workloads
     _run(lambda dvg: workloads.fill_scene(dvg, seed=9, num_paths=300, canvas=96, radius_range=(4.0, 20.0)), 1, 9,
          prefilter=True)
+
+
+def test_dense_stroke_scene():
+    """Samples inside or near about 65 wide strokes each (64x64, 300 paths of
+    6 cubic segments, half-widths 2-5): a stroke-only scene takes the wide
+    segment-test queues, and lanes still queue more tests than they hold, so
+    the walks decide the overflow one lane at a time besides the
+    warp-batched decisions and the deferred root walks."""
+    from diffvg_gb300 import workloads
+    _run(lambda dvg: workloads.stroke_scene(dvg, seed=21, num_paths=300, canvas=64, step=12.0, num_segments=6,
+                                            width_range=(2.0, 5.0)), 2, 6)
