@@ -79,14 +79,18 @@ def test_native_adam_matches_reference_update():
     assert torch.allclose(p.cpu().double(), ref, rtol=1e-5, atol=1e-6)
 
 
-def _batch_mixed(n=6, seed0=200):
+def _batch_mixed(n=6, seed0=200, fills=False):
     """Scenes of uneven size, one of them with fewer than 8 groups (its
-    boundary pass runs per scene inside the batched call)."""
+    boundary pass runs per scene inside the batched call); with fills, one
+    fill-heavy scene too (the batched walks then take the narrow queues)."""
     import diffvg_gb300 as dvg
     from diffvg_gb300 import workloads
     from diffvg_gb300.batch import BatchedScenes
     scenes = workloads.batched_scenes(dvg, seeds=range(seed0, seed0 + n - 1), canvases=(64, 96, 160), path_range=(8, 96))
     scenes.append(workloads.stroke_scene(dvg, seed=seed0 + 99, num_paths=5, canvas=80))
+    if fills:
+        scenes.append(workloads.fill_scene(dvg, seed=seed0 + 98, num_paths=24, canvas=96))
+        n += 1
     args = [dvg.RenderFunction.serialize_scene(w, h, s, g) for (w, h, s, g) in scenes]
     seeds = list(range(seed0, seed0 + n))
     b = BatchedScenes(args, seeds=seeds, lr=1e-2, streams=3)
@@ -98,14 +102,14 @@ def _batch_mixed(n=6, seed0=200):
     return b
 
 
-@pytest.mark.parametrize('tuning', [(1, 1), (2, 2), (2, 5)])
-def test_persistent_batch_matches_per_scene_launches(tuning):
+@pytest.mark.parametrize('tuning,fills', [((1, 1), False), ((2, 2), False), ((2, 5), False), ((1, 1), True)])
+def test_persistent_batch_matches_per_scene_launches(tuning, fills):
     """One persistent launch per pass over all scenes (dvg_batch_forward /
     dvg_batch_backward) gives every scene the images of its own launches and
     its gradients within 1e-3 relative L2 (atomic order), also after graph
     replays of full steps."""
     import torch
-    b1, b2 = _batch_mixed(), _batch_mixed()
+    b1, b2 = _batch_mixed(fills=fills), _batch_mixed(fills=fills)
     b2.set_mode('persistent', tuning)
     b1.step_eager()
     b2.step_eager()
