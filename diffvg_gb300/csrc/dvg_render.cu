@@ -48,6 +48,18 @@ static_assert(DVG_BWD_THREADS % 256 == 0 && DVG_BWD_THREADS <= 512 && DVG_PF_FWD
               "the sample passes run 256-sample groups");
 // resident blocks per SM for a 128-register budget
 #define DVG_BLOCKS_FOR(threads) (512 / (threads))
+// Resident blocks per SM of the prefiltered forward (its register budget).
+// Its per-sample closest-point code is large and instruction fetch bounds it
+// (ncu: instruction-cache hit 61 %, no_instruction the largest stall), so it
+// runs at full occupancy, 8 blocks of 256 with 32 registers (the spills go
+// to L1): fill-heavy prefiltered 1024x1024 forward 7.28 -> 5.35 ms (4 blocks,
+// 64 registers: 6.55 ms).  The prefiltered adjoint measured no gain from it.
+#ifndef DVG_PF_FWD_BLOCKS
+#define DVG_PF_FWD_BLOCKS 8
+#endif
+#ifndef DVG_PF_BWD_BLOCKS
+#define DVG_PF_BWD_BLOCKS DVG_BLOCKS_FOR(DVG_PF_BWD_THREADS)
+#endif
 #ifndef DVG_EDGE_THREADS
 #define DVG_EDGE_THREADS 512
 #endif
@@ -200,7 +212,7 @@ __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRende
 // has fewer samples than a block.
 template <bool PREFILTER, class Q>
 __global__ void __launch_bounds__(PREFILTER ? DVG_PF_FWD_THREADS : DVG_FWD_THREADS,
-                                  DVG_BLOCKS_FOR(PREFILTER ? DVG_PF_FWD_THREADS : DVG_FWD_THREADS))
+                                  PREFILTER ? DVG_PF_FWD_BLOCKS : DVG_BLOCKS_FOR(DVG_FWD_THREADS))
     k_sample_fwd(const __grid_constant__ DevScene S, const __grid_constant__ DevRender R, float4 *samples,
                  const __grid_constant__ EdgeRecords D) {
   int cy = blockIdx.y * (blockDim.x >> 8) + (threadIdx.x >> 8);
@@ -345,7 +357,7 @@ __device__ __forceinline__ void sample_bwd_one(const DevScene &S, const DevRende
 
 template <bool PREFILTER>
 __global__ void __launch_bounds__(PREFILTER ? DVG_PF_BWD_THREADS : DVG_BWD_THREADS,
-                                  DVG_BLOCKS_FOR(PREFILTER ? DVG_PF_BWD_THREADS : DVG_BWD_THREADS))
+                                  PREFILTER ? DVG_PF_BWD_BLOCKS : DVG_BLOCKS_FOR(DVG_BWD_THREADS))
     k_sample_bwd(const __grid_constant__ DevScene S, DevRender R0, float4 *dbg_val, int *dbg_flag) {
   DevRender R = load_filter(R0, nullptr);
   int tile, cy;
