@@ -100,6 +100,7 @@ struct DvgScene {
   DevBuf own_params;
   bool has_params = false;
   bool wide_queues = false;  // three quarters or more of the groups stroked (DevScene::wide_queues)
+  bool fill_heavy = false;   // 64 or more groups, a quarter or less stroked (DevScene::fill_heavy)
   // fragment cache of the last image forward (no prefiltering): per-sample
   // hit keys and counts, a copy of its parameters and the stale flag the
   // backward sets when its parameters differ
@@ -293,6 +294,7 @@ DevScene make_dev(DvgScene *sc, const float *params) {
   S.seg_tpts = sc->seg_tpts;
   S.seg_th = sc->seg_th;
   S.wide_queues = sc->wide_queues ? 1 : 0;
+  S.fill_heavy = sc->fill_heavy ? 1 : 0;
   S.num_paths = sc->num_paths;
   S.num_records = sc->num_records;
   S.shape_band = sc->shape_band;
@@ -597,11 +599,14 @@ int dvg_scene_create(const DvgSceneDesc *desc, DvgScene **out_scene) {
   sc->tiles_x = (desc->canvas_width + DVG_TILE - 1) / DVG_TILE;
   sc->tiles_y = (desc->canvas_height + DVG_TILE - 1) / DVG_TILE;
   int T = sc->tiles_x * sc->tiles_y;
-  // stroke-heavy scenes give the walks the wider segment-test queue
+  // stroke-heavy scenes give the walks the wider segment-test queue; scenes of
+  // many fills run the sampled forward at two blocks per SM (a single fill's
+  // forward is short and measured slower with it: 27.5 -> 34 us)
   int stroked = 0;
   for (int g = 0; g < G; g++)
     stroked += desc->group_info[(size_t)g * DVG_GROUP_INFO_STRIDE + DVG_GROUP_STROKE_KIND] != DVG_PAINT_NONE ? 1 : 0;
   sc->wide_queues = G > 0 && 4 * (long long)stroked >= 3 * (long long)G;
+  sc->fill_heavy = G >= 64 && 4 * (long long)stroked <= (long long)G;
   // (group, shape) pairs of the boundary CDF, in group order (scene.cpp:207-246)
   std::vector<int> smp_shape, smp_group;
   for (int g = 0; g < G; g++) {

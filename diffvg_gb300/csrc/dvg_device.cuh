@@ -67,6 +67,7 @@ struct DevScene {
   float2 *seg_tpts = nullptr;  // [NSEG * DVG_TREE_PTS] tabulated subdivision trees (curved segments), or null
   float *seg_th = nullptr;     // [NSEG * DVG_TREE_NODES]
   int wide_queues = 0;         // stroke-heavy scene: the walks queue DVG_LANE_JOBS_WIDE tests per lane
+  int fill_heavy = 0;          // fill-heavy scene: the sampled forward runs DVG_FWD_FILL_BLOCKS blocks per SM
   int num_paths = 1, num_records = 1;  // path shapes and stroke records (preparation skips the kernels of none)
   unsigned *err;            // status word (DVG_EFLAG_*)
   // y-band segment lists of long paths (null: no path has them).  A path of

@@ -49,13 +49,24 @@ static_assert(DVG_BWD_THREADS % 256 == 0 && DVG_BWD_THREADS <= 512 && DVG_PF_FWD
 // resident blocks per SM for a 128-register budget
 #define DVG_BLOCKS_FOR(threads) (512 / (threads))
 // Resident blocks per SM of the prefiltered forward (its register budget).
-// Its per-sample closest-point code is large and instruction fetch bounds it
-// (ncu: instruction-cache hit 61 %, no_instruction the largest stall), so it
-// runs at full occupancy, 8 blocks of 256 with 32 registers (the spills go
-// to L1): fill-heavy prefiltered 1024x1024 forward 7.28 -> 5.35 ms (4 blocks,
-// 64 registers: 6.55 ms).  The prefiltered adjoint measured no gain from it.
+// Its per-sample closest-point code is large and fp64-heavy; 16 warps an SM
+// left instruction-fetch misses and fp64 latency uncovered, so it runs at
+// full occupancy, 8 blocks of 256 with 32 registers, and pays in spills:
+// fill-heavy prefiltered 1024x1024 forward 7.28 -> 5.35 ms (4 blocks, 64
+// registers: 6.55 ms).  The prefiltered adjoint measured no gain from it.
 #ifndef DVG_PF_FWD_BLOCKS
 #define DVG_PF_FWD_BLOCKS 8
+#endif
+#ifndef DVG_FWD_BLOCKS
+#define DVG_FWD_BLOCKS DVG_BLOCKS_FOR(DVG_FWD_THREADS)
+#endif
+// The sampled forward of fill-heavy scenes (64 or more groups, a quarter or
+// less stroked) runs two blocks of 512 per SM with 64 registers: its walks are
+// short winding-number loops that gain from the extra warps (fill-heavy
+// 1024x1024 forward 6.97 -> 6.11 ms), where the stroke walks lose (3.48 ->
+// 4.25 ms on the stroke-heavy 512x512 workload).
+#ifndef DVG_FWD_FILL_BLOCKS
+#define DVG_FWD_FILL_BLOCKS (2 * DVG_FWD_BLOCKS)
 #endif
 #ifndef DVG_PF_BWD_BLOCKS
 #define DVG_PF_BWD_BLOCKS DVG_BLOCKS_FOR(DVG_PF_BWD_THREADS)
@@ -210,9 +221,9 @@ __device__ __forceinline__ void sample_fwd_one(const DevScene &S, const DevRende
 // of its tile's 256-sample groups (whole warps leave when their group is past
 // the tile's spp groups); launch_sample_fwd uses blocks of 256 when a tile
 // has fewer samples than a block.
-template <bool PREFILTER, class Q>
+template <bool PREFILTER, class Q, int BLOCKS = DVG_FWD_BLOCKS>
 __global__ void __launch_bounds__(PREFILTER ? DVG_PF_FWD_THREADS : DVG_FWD_THREADS,
-                                  PREFILTER ? DVG_PF_FWD_BLOCKS : DVG_BLOCKS_FOR(DVG_FWD_THREADS))
+                                  PREFILTER ? DVG_PF_FWD_BLOCKS : BLOCKS)
     k_sample_fwd(const __grid_constant__ DevScene S, const __grid_constant__ DevRender R, float4 *samples,
                  const __grid_constant__ EdgeRecords D) {
   int cy = blockIdx.y * (blockDim.x >> 8) + (threadIdx.x >> 8);
@@ -1001,7 +1012,7 @@ static inline dim3 group_grid(const DevRender &R, int threads) {
 // Opts kernel `id` (one of QueueKernel) into kQueueBytes of dynamic shared
 // memory, once per device (devices 0-63; the others every call).
 enum QueueKernel {
-  QK_FWD, QK_FWD_WIDE, QK_BWD, QK_EDGE_PAIRS, QK_EDGE_PAIRS_WIDE, QK_EDGE, QK_FWD_BATCH, QK_FWD_BATCH_WIDE,
+  QK_FWD, QK_FWD_WIDE, QK_FWD_FILL, QK_BWD, QK_EDGE_PAIRS, QK_EDGE_PAIRS_WIDE, QK_EDGE, QK_FWD_BATCH, QK_FWD_BATCH_WIDE,
   QK_BWD_BATCH, QK_EDGE_BATCH, QK_EDGE_BATCH_WIDE, QK_COUNT
 };
 template <class K>
@@ -1055,6 +1066,11 @@ void launch_sample_fwd(const DevScene &S, const DevRender &R, float4 *samples, c
       constexpr int qb = queue_local_bytes<WarpQueueWide>();
       allow_queues(k_sample_fwd<false, WarpQueueWide>, QK_FWD_WIDE, DVG_FWD_THREADS / 32 * qb);
       k_sample_fwd<false, WarpQueueWide><<<grid, threads, threads / 32 * qb, st>>>(S, R, samples, defer ? *D : none);
+    } else if (S.fill_heavy) {
+      constexpr int qb = queue_local_bytes<WarpQueue>();
+      auto *k = k_sample_fwd<false, WarpQueue, DVG_FWD_FILL_BLOCKS>;
+      allow_queues(k, QK_FWD_FILL, DVG_FWD_THREADS / 32 * qb);
+      k<<<grid, threads, threads / 32 * qb, st>>>(S, R, samples, defer ? *D : none);
     } else {
       constexpr int qb = queue_local_bytes<WarpQueue>();
       allow_queues(k_sample_fwd<false, WarpQueue>, QK_FWD, DVG_FWD_THREADS / 32 * qb);

@@ -115,6 +115,14 @@ def test_deep_fill_scene_prefiltered():
          prefilter=True)
 
 
+def test_deep_fill_scene_sampled():
+    """Sampled colours under many fills (96x96, 300 fills of radius 4-20,
+    2x2 spp): a fill-heavy scene of 64 or more groups, whose forward runs
+    two blocks per SM with 64 registers."""
+    from diffvg_gb300 import workloads
+    _run(lambda dvg: workloads.fill_scene(dvg, seed=9, num_paths=300, canvas=96, radius_range=(4.0, 20.0)), 2, 10)
+
+
 def test_dense_stroke_scene():
     """Samples inside or near about 65 wide strokes each (64x64, 300 paths of
     6 cubic segments, half-widths 2-5): a stroke-only scene takes the wide
