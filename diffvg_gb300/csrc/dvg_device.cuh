@@ -470,7 +470,9 @@ DI bool cand_range(const DevScene &S, v2 pt, int &begin, int &end) {
 // rounding margin; otherwise DVG_WINDING_UNDECIDED is returned and the caller
 // runs the reference's fp64 cubic solve.  With every decision clear of the
 // margin the reference's closed-form roots are simple roots at the same
-// crossings, so both count the same.
+// crossings, so both count the same.  When the control points all lie right
+// of pt by more than the crossing margin, so does every crossing (the curve
+// stays in their convex hull), and the pieces are counted without bisection.
 #define DVG_WINDING_UNDECIDED (-1000)
 DI float cubic_y(float a, float b, float c, float d, float t) { return ((a * t + b) * t + c) * t + d; }
 DI int winding_cubic_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
@@ -503,6 +505,8 @@ DI int winding_cubic_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
   }
   ts[nt++] = 1.f;
   float span = fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(cx), 1.f));
+  float xmargin = 4.f * m + 1e-6f * span;
+  bool right = fminf(fminf(p0.x, p1.x), fminf(p2.x, p3.x)) - pt.x > xmargin;
   int w = 0;
   float ya = cubic_y(ay, by, cy, dy, ts[0]);
   if (fabsf(ya) <= m) return DVG_WINDING_UNDECIDED;
@@ -510,7 +514,9 @@ DI int winding_cubic_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
   for (int k = 1; k < nt; k++) {
     float yb = cubic_y(ay, by, cy, dy, ts[k]);
     if (fabsf(yb) <= m) return DVG_WINDING_UNDECIDED;
-    if ((ya < 0.f) != (yb < 0.f)) {
+    if ((ya < 0.f) != (yb < 0.f) && right) {
+      w += yb > ya ? 1 : -1;
+    } else if ((ya < 0.f) != (yb < 0.f)) {
       float lo = ts[k - 1], hi = ts[k];
       bool up = yb > ya;
       #pragma unroll 1
@@ -520,7 +526,7 @@ DI int winding_cubic_fast(v2 p0, v2 p1, v2 p2, v2 p3, v2 pt) {
         if ((ym > 0.f) == up) hi = mid; else lo = mid;
       }
       float xs = cubic_y(ax, bx, cx, dx, 0.5f * (lo + hi));
-      if (fabsf(xs) <= 4.f * m + 1e-6f * span) return DVG_WINDING_UNDECIDED;
+      if (fabsf(xs) <= xmargin) return DVG_WINDING_UNDECIDED;
       if (xs > 0.f) w += up ? 1 : -1;
     }
     ya = yb;
