@@ -14,6 +14,7 @@
 #include <cstring>
 #include <optional>
 #include <tuple>
+#include <vector>
 
 #include "diffvg_gb300.h"
 
@@ -156,6 +157,31 @@ int64_t scene_update_params(int64_t scene, const at::Tensor &params) {
   return dvg_scene_update_params(scene_of(scene), params.data_ptr<float>(), static_cast<int32_t>(np), stream);
 }
 
+// Views of a gradient arena, one per parameter slot: numels[i] floats at
+// offsets[i], shaped by the next ndims[i] entries of dims.  The backward of
+// RenderFunction hands them to autograd as the gradients of the scene's
+// tensors (one C++ loop in place of a Python view per tensor).
+std::vector<at::Tensor> arena_views(const at::Tensor &arena, c10::IntArrayRef offsets, c10::IntArrayRef numels,
+                                    c10::IntArrayRef ndims, c10::IntArrayRef dims) {
+  size_t n = offsets.size();
+  TORCH_CHECK(numels.size() == n && ndims.size() == n, "offsets, numels and ndims differ in length");
+  TORCH_CHECK(arena.dim() == 1 && arena.is_contiguous(), "arena must be a contiguous 1-D tensor");
+  int64_t total = arena.numel();
+  std::vector<at::Tensor> out;
+  out.reserve(n);
+  size_t d = 0;
+  for (size_t i = 0; i < n; i++) {
+    TORCH_CHECK(offsets[i] >= 0 && numels[i] >= 0 && offsets[i] + numels[i] <= total, "slot ", i,
+                " lies outside the arena");
+    TORCH_CHECK(ndims[i] >= 0 && d + static_cast<size_t>(ndims[i]) <= dims.size(), "dims holds too few entries");
+    at::Tensor v = arena.narrow(0, offsets[i], numels[i]);
+    if (ndims[i] != 1) v = v.view(dims.slice(d, static_cast<size_t>(ndims[i])));
+    d += static_cast<size_t>(ndims[i]);
+    out.push_back(std::move(v));
+  }
+  return out;
+}
+
 int64_t scene_sync(int64_t scene, int64_t device) {
   return dvg_scene_sync(scene_of(scene), c10::cuda::getCurrentCUDAStream(static_cast<c10::DeviceIndex>(device)).stream());
 }
@@ -176,4 +202,6 @@ TORCH_LIBRARY(diffvg_gb300, m) {
         &render_backward);
   m.def("scene_update_params(int scene, Tensor params) -> int", &scene_update_params);
   m.def("scene_sync(int scene, int device) -> int", &scene_sync);
+  m.def("arena_views(Tensor(a -> *) arena, int[] offsets, int[] numels, int[] ndims, int[] dims) -> Tensor(a)[]",
+        &arena_views);
 }

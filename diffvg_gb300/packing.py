@@ -67,6 +67,20 @@ class PackedScene:
     _copied: object = None
     _staged: object = None
     _staged_views: object = None
+    _grad_views: object = None
+
+    def grad_view_spec(self, ks):
+        """(offsets, numels, ndims, dims) of the slots ks, the arguments of the
+        arena_views operator; kept for the last slot list asked for."""
+        key = tuple(ks)
+        c = self._grad_views
+        if c is not None and c[0] == key:
+            return c[1]
+        sl = [self.slots[k] for k in ks]
+        spec = ([s.offset for s in sl], [s.numel for s in sl], [len(s.shape) for s in sl],
+                [int(d) for s in sl for d in s.shape])
+        self._grad_views = (key, spec)
+        return spec
 
     def _slot_views(self, buf):
         return [buf[sl.offset:sl.offset + sl.numel].view(sl.shape) for sl in self.slots]

@@ -20,6 +20,7 @@ Differences from the reference that a caller can observe:
 from collections import OrderedDict
 from enum import IntEnum
 import itertools
+import operator
 import threading
 import warnings
 import weakref
@@ -432,6 +433,10 @@ def _render_forward(ctx, call, background_image):
     return out
 
 
+_device_of = operator.attrgetter('device')
+_dtype_of = operator.attrgetter('dtype')
+
+
 def _render_backward(ctx, grad_img):
     """The backward render of a _render_forward (render_pytorch.py:668-868):
     (background gradient or None, gradients of the call's slots in
@@ -461,32 +466,30 @@ def _render_backward(ctx, grad_img):
     # status is checked once the gradient has been read back
     launch(reuse | _native.DVG_FLAG_NO_SYNC)
     scene.last_token = ctx.token
-    slots, tensors = packed.slots, packed.tensors
+    tensors = packed.tensors
     if fused is not None:
         # one gradient: the fused tensor's, the arena itself
         bufs = {device: d_arena}
         if fused.device != device:
             bufs[fused.device] = torch.empty(d_arena.shape, dtype=torch.float32, device=fused.device)
         grads = [bufs[fused.device][:fused.numel()]]
-        ks = dst_of = []
     else:
-        ks = ctx.grad_slots
-        dst_of = [tensors[k].device for k in ks]
+        # one view of the gradient arena per slot, on its tensor's device and
+        # in its dtype (arena_views builds the views in one call)
+        ts = [tensors[k] for k in ctx.grad_slots]
+        dsts = set(map(_device_of, ts))
         bufs = {device: d_arena}
-        for dst in set(dst_of):
+        for dst in dsts:
             if dst != device:
                 bufs[dst] = torch.empty(d_arena.shape, dtype=torch.float32, device=dst)
-        grads = []
-        sizes = [sl.numel for sl in slots]
-        parts = {dst: torch.split(bufs[dst][:sum(sizes)], sizes) for dst in set(dst_of)}
-    for k, dst in zip(ks, dst_of):
-        slot, t = slots[k], tensors[k]
-        g = parts[dst][k]
-        if len(slot.shape) != 1:
-            g = g.view(slot.shape)
-        if t.dtype != g.dtype:
-            g = g.to(t.dtype)
-        grads.append(g)
+        spec = packed.grad_view_spec(ctx.grad_slots)
+        views = {dst: _native.ops().arena_views(bufs[dst], *spec) for dst in dsts}
+        if len(views) <= 1:
+            grads = list(views.popitem()[1]) if views else []
+        else:
+            grads = [views[t.device][i] for i, t in enumerate(ts)]
+        if ts and set(map(_dtype_of, ts)) != {torch.float32}:
+            grads = [g if t.dtype == g.dtype else g.to(t.dtype) for g, t in zip(grads, ts)]
     for dst, b in bufs.items():
         if dst != device:
             b.copy_(d_arena)  # waits for the kernels

@@ -17,6 +17,8 @@ OPS = {
                        'Tensor(c!)? d_translation, int[] dims, int seed, int flags) -> int',
     'scene_update_params': 'scene_update_params(int scene, Tensor params) -> int',
     'scene_sync': 'scene_sync(int scene, int device) -> int',
+    'arena_views': 'arena_views(Tensor(a -> *) arena, int[] offsets, int[] numels, int[] ndims, int[] dims) '
+                   '-> Tensor(a)[]',
 }
 
 
@@ -76,3 +78,22 @@ def test_seeds_keep_their_64_bits():
     assert _native._i64(2 ** 63) == -2 ** 63
     assert _native._i64(2 ** 64 - 1) == -1
     assert _native._i64(-1) == -1
+
+
+def test_arena_views_alias_the_arena_in_slot_shapes():
+    """The gradient views RenderFunction's backward returns: each slot's
+    floats of the one arena, in the slot's shape, sharing its storage."""
+    ops = _native.ops()
+    arena = torch.arange(20, dtype=torch.float32)
+    views = ops.arena_views(arena, [0, 4, 10, 19], [4, 6, 9, 1], [1, 2, 2, 0], [4, 3, 2, 3, 3])
+    assert [tuple(v.shape) for v in views] == [(4,), (3, 2), (3, 3), ()]
+    assert [v.data_ptr() - arena.data_ptr() for v in views] == [0, 16, 40, 76]
+    assert views[1].tolist() == [[4.0, 5.0], [6.0, 7.0], [8.0, 9.0]]
+    arena[19] = -1.0
+    assert float(views[3]) == -1.0
+    with pytest.raises(RuntimeError, match='outside the arena'):
+        ops.arena_views(arena, [15], [6], [1], [6])
+    with pytest.raises(RuntimeError, match='too few entries'):
+        ops.arena_views(arena, [0], [6], [2], [6])
+    with pytest.raises(RuntimeError, match='differ in length'):
+        ops.arena_views(arena, [0, 1], [1], [1], [1])
